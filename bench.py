@@ -1,0 +1,320 @@
+"""Benchmark of the GB300 ray-tracing core.
+
+Headline workload: the procedural terrain (1025x1025 diamond-square
+heightfield, 2,097,152 triangles) at 1920x1080, one primary ray per pixel
+plus one directional-sun shadow ray per hit, coloured Phong, RGB8 output.
+A step is one frame through the fused render kernel.  Metric: Mrays/s
+(primary + shadow rays per second, whole job).
+
+  value  device-resident throughput: scene and hierarchy in HBM, output to
+         a device buffer, CUDA events on the launching stream around each
+         frame; the L2 is flushed (a 512 MB write) between frames.
+  e2e    the same frame through the C ABI with a pinned HOST output buffer:
+         camera/light/material structs in, RGB8 out (device-to-host copy
+         inside the timed region), wall clock per call.
+
+`--impl reference` times the reference's CPU path on the host cores: the
+reference itself when it was compiled here (oracle/_ref), else the oracle's
+C restatement, on a bounded band of rows per step with all host threads.
+
+Multi-GPU (torchrun, N > 1): every rank renders its own replica of the
+frame (no data-path collective; "replicas only"); value = all ranks' rays /
+max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s (primary+shadow, 1 GB300)"
+WORKLOAD = "terrain-2M-1080p"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=1024, help="terrain cells per side (power of two)")
+    return ap.parse_args()
+
+
+def make_workload(size):
+    from raptor_gb300 import scenes
+    return scenes.terrain_scene(size_pow2=size)
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, max clock, power, throttle reasons)
+    during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+                pw.append(float(p[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "power_w_max": float(max(pw)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(scene, frame, seconds, threads=None):
+    """The reference's CPU path on this host: oracle/_ref (the reference
+    compiled from source) when present, else the oracle's C restatement.
+    Renders a band of rows sized to about `seconds` of work with all host
+    threads; returns Mrays/s and a description of the sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    if not os.path.exists(O.ORACLE_SO):
+        O.build()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    osc = O.OracleScene(scene)
+    build_s = time.perf_counter() - t0
+    H = frame["camera"]["yres"]
+    # probe a thin band, then size the sample to the budget
+    mid = H // 2
+    probe = O.OracleScene.render(osc, frame, rows=(mid, min(H, mid + 8)), threads=threads)
+    t1 = time.perf_counter()
+    probe = osc.render(frame, rows=(mid, min(H, mid + 8)), threads=threads)
+    dt = max(time.perf_counter() - t1, 1e-6)
+    rows = int(max(8, min(H, 8 * seconds / dt)))
+    r0 = max(0, mid - rows // 2)
+    r1 = min(H, r0 + rows)
+    t2 = time.perf_counter()
+    out = osc.render(frame, rows=(r0, r1), threads=threads)
+    dt = time.perf_counter() - t2
+    kind = "port"
+    return {"value": out["rays"] / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": kind,
+            "sample": f"rows {r0}..{r1} of {H} ({out['rays']} rays) of the same frame, oracle C restatement of "
+                      f"bvh traversal + ray_trace_engine::ray_trace + coloured_mapper_shader; hierarchy build "
+                      f"{build_s:.2f} s single-threaded excluded",
+            "build_seconds": build_s}
+
+
+# --------------------------------------------------------------- distributed
+
+def dist_init(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return 0, 1
+    import torch.distributed as dist
+    dist.init_process_group("nccl")
+    return dist.get_rank(), dist.get_world_size()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# -------------------------------------------------------------------- main
+
+def run_reference(args):
+    rank, world = dist_init(args.gpus)
+    if rank != 0:
+        return
+    scene, frame = make_workload(args.size)
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(scene, frame, seconds=max(1.0, args.cpu_seconds / 4.0))
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded diamond-square terrain)",
+            "config": {"workload": WORKLOAD, "triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080],
+                       "rays": "primary + 1 directional shadow ray per hit"},
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    from raptor_gb300 import core
+    rank, world = dist_init(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
+    peak_src = "measured" if peaks else "fallback"
+
+    scene, frame = make_workload(args.size)
+    cam = frame["camera"]
+    W, H = cam["xres"], cam["yres"]
+    ctx = core.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    sc = core.Scene(ctx, scene)
+    build_ms = sc.build()
+    build_ms = min(build_ms, sc.build())   # second build: warm
+    info = sc.info()
+
+    rgb_dev = torch.empty((H, W, 3), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # fetch counts for the roofline (instrumented kernel, outside the timed region)
+    ctx.set_option(core.RT_OPT_COUNT_FETCHES, 1)
+    cnt = sc.render(frame, rgb=rgb_dev)["stats"]
+    ctx.set_option(core.RT_OPT_COUNT_FETCHES, 0)
+    nodes_per_frame, tris_per_frame = cnt.nodes_fetched, cnt.tris_tested
+
+    for _ in range(args.warmup):
+        sc.render(frame, rgb=rgb_dev)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    rays = 0
+    kernel_ms = []
+    barrier(world)
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        st = sc.render(frame, rgb=rgb_dev)["stats"]
+        ev[i][1].record(stream)
+        rays += st.primary_rays + st.secondary_rays
+        kernel_ms.append(st.device_ms)
+    torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1e3
+    total_s = max_over_ranks(total_s, world)
+    value = rays * world / total_s / 1e6
+
+    # e2e: public API with a pinned host output buffer, wall clock per call
+    rgb_host = torch.empty((H, W, 3), dtype=torch.uint8).pin_memory()
+    e2e_rays = 0
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        st = sc.render(frame, rgb=rgb_host)["stats"]
+        e2e_rays += st.primary_rays + st.secondary_rays
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    clk = clocks.stop()
+    e2e = e2e_rays * world / e2e_s / 1e6
+    h2d = C_sizes()
+    mean_kernel_ms = float(np.mean(kernel_ms))
+    frame_rays = rays / args.steps
+    # algorithmic bytes per frame: nodes fetched x 80 B + triangles tested x
+    # 48 B + shading records (per hit: 32 B shade + 12 B indices + 36 B
+    # attributes) + RGB8 output
+    hits = st.primary_hits
+    alg_bytes = nodes_per_frame * 80 + tris_per_frame * 48 + hits * (32 + 12 + 36) + W * H * 3
+    achieved = alg_bytes / (mean_kernel_ms / 1e3) / 1e9
+
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded diamond-square terrain, slope colours)",
+            "config": {"workload": WORKLOAD, "triangles": int(scene["tris"].shape[0]), "resolution": [W, H],
+                       "rays": "primary + 1 directional shadow ray per hit", "rays_per_frame": frame_rays,
+                       "l2": "flushed between frames (512 MB write)", "parallelism": f"replicas x{world}",
+                       "bvh": info, "bvh_build_ms": build_ms},
+            "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 3},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None,
+                         "kernel": "k_render<false>", "peak_source": peak_src,
+                         "bytes_per_frame": alg_bytes, "nodes_per_ray": nodes_per_frame / frame_rays,
+                         "tris_per_ray": tris_per_frame / frame_rays, "kernel_ms": mean_kernel_ms},
+            "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(scene, frame, args.cpu_seconds).items()
+                                if k != "build_seconds"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sc.close()
+    ctx.close()
+
+
+def C_sizes():
+    """Bytes of the per-frame inputs handed to the device: camera, one light
+    and the material, passed by value as kernel parameters."""
+    from raptor_gb300 import core
+    import ctypes
+    return ctypes.sizeof(core.RtCamera) + ctypes.sizeof(core.RtLight) + ctypes.sizeof(core.RtMaterial)
+
+
+if __name__ == "__main__":
+    main()

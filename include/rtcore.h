@@ -1,0 +1,209 @@
+/*
+ * rtcore.h -- C ABI of the GB300 ray-tracing core (sm_103a).
+ *
+ * Drop-in replacement for the hot path of RAPTor's raytracer/ subsystem:
+ * acceleration-structure build, closest-hit / any-hit traversal with
+ * Moller-Trumbore triangle tests, and the Phong primary+shadow shading pass.
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the RAPTor project root).
+ *
+ * Conventions
+ *  - Every function returns rt_status: RT_OK (0) or a negative error code;
+ *    nothing aborts.  rt_last_error_string() describes the last error of the
+ *    calling thread.
+ *  - Pointers to bulk data may be host memory (pageable or pinned) or device
+ *    memory of the context's GPU; the core detects which.  Host buffers are
+ *    borrowed for the duration of the call; results are complete when the
+ *    call returns (host outputs) or when the context's stream reaches the end
+ *    of the call's work (device outputs).
+ *  - A context owns all device memory it allocates and one CUDA stream
+ *    (replaceable with rt_ctx_set_stream).  Calls on one context must not
+ *    run concurrently from several threads; distinct contexts are independent.
+ *  - Triangle ids are the caller's order (the reference's
+ *    primitive_store::indirection ids).  Barycentrics follow the reference:
+ *    u weighs vertex c, v weighs vertex b (triangle.h:190-235).
+ *  - Arithmetic on the hit path is IEEE binary32 in the reference's
+ *    operation order, so hit ids and distances equal the reference's
+ *    bit for bit wherever the closest hit is unique.
+ */
+#ifndef RTCORE_H
+#define RTCORE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t rt_status;
+#define RT_OK 0
+#define RT_ERR_INVALID_ARG (-1)
+#define RT_ERR_CUDA (-2)
+#define RT_ERR_OUT_OF_MEMORY (-3)
+#define RT_ERR_NOT_BUILT (-4)
+#define RT_ERR_STACK_OVERFLOW (-5)   /* traversal stack cap hit; results incomplete */
+#define RT_ERR_LIMIT (-6)            /* a bounded device loop hit its iteration cap */
+#define RT_ERR_NO_DEVICE (-7)
+#define RT_ERR_INTERNAL (-8)
+
+typedef struct rt_context rt_context;
+typedef struct rt_scene rt_scene;
+
+/* Ray: origin, direction (need not be unit), and the far limit used by
+ * any-hit queries (ignored by closest-hit).  32 bytes. */
+typedef struct rt_ray {
+    float ox, oy, oz, tmax;
+    float dx, dy, dz, pad;
+} rt_ray;
+
+/* Closest hit: tri = -1 and t = FLT_MAX on a miss (the reference's
+ * hit_description with MAX_DIST, common/common.h:230-239). */
+typedef struct rt_hit {
+    int32_t tri;
+    float t, u, v;
+} rt_hit;
+
+/* Pinhole camera, exactly the reference camera's constructor arguments
+ * (raytracer/camera.h:55-62): position, x/y/z axes, background colour
+ * (0..255), half-width w, half-height h, image-plane distance t, resolution.
+ * Pixel (x, y) looks along x_axis*(x*2w/xres - w) + y_axis*(y*2h/yres - h)
+ * + z_axis*t; row y = 0 is the bottom row (camera.h:127-140). */
+typedef struct rt_camera {
+    float pos[3];
+    float x_axis[3], y_axis[3], z_axis[3];
+    float background[3];
+    float w, h, t;
+    int32_t xres, yres;
+} rt_camera;
+
+/* Light (raytracer/light.h:17-34).  kind RT_LIGHT_POINT: point light at pos
+ * (spherical light with soft shadows off); RT_LIGHT_DIRECTIONAL: light along
+ * dir.  rgb in 0..255, d the distance drop-off. */
+#define RT_LIGHT_POINT 0
+#define RT_LIGHT_DIRECTIONAL 1
+typedef struct rt_light {
+    int32_t kind;
+    float rgb[3];
+    float pos[3];
+    float dir[3];
+    float d;
+} rt_light;
+
+/* Coloured Phong material (materials/coloured_mapper_shader.h): ka, kd, ks in
+ * 0..255, ns the specular exponent.  With per-vertex attributes uploaded, kd
+ * is modulated by the barycentric attribute (a per-vertex colour in 0..1). */
+typedef struct rt_material {
+    float ka[3], kd[3], ks[3];
+    float ns;
+} rt_material;
+
+/* Triangle flag bits (triangle.h:40, bvh_node.h:176): shadow and AO rays
+ * ignore light and transparent triangles. */
+#define RT_TRI_LIGHT 1u
+#define RT_TRI_TRANSPARENT 2u
+
+/* Frame statistics filled by the render calls (nullable). */
+typedef struct rt_render_stats {
+    int64_t primary_rays;
+    int64_t secondary_rays;    /* shadow + AO rays traced */
+    int64_t primary_hits;
+    float device_ms;           /* device time of the render kernel(s) */
+    int32_t status;            /* device status word (0 = clean) */
+    int64_t nodes_fetched;     /* wide nodes loaded (RT_OPT_COUNT_FETCHES only) */
+    int64_t tris_tested;       /* triangles tested (RT_OPT_COUNT_FETCHES only) */
+} rt_render_stats;
+
+/* ------------------------------------------------------------ context */
+
+/* Create a context on CUDA device `device` (replaces nothing: the reference
+ * has no device state).  The context creates its own non-blocking stream. */
+rt_status rt_ctx_create(int32_t device, rt_context **out);
+rt_status rt_ctx_destroy(rt_context *ctx);
+/* Run all further work of this context on `stream` (a cudaStream_t); NULL
+ * restores the context's own stream. */
+rt_status rt_ctx_set_stream(rt_context *ctx, void *stream);
+/* Wait for all work queued on the context's stream. */
+rt_status rt_ctx_synchronize(rt_context *ctx);
+/* Context options.  RT_OPT_COUNT_FETCHES (0/1): render calls use an
+ * instrumented kernel that counts node loads and triangle tests into
+ * rt_render_stats (for roofline accounting; slower, off by default). */
+#define RT_OPT_COUNT_FETCHES 1
+rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value);
+/* Message of the last error on the calling thread ("" if none). */
+const char *rt_last_error_string(void);
+/* Library version as major*10000 + minor*100 + patch. */
+int32_t rt_version(void);
+
+/* -------------------------------------------------------------- scene */
+
+/* Create an empty scene in a context. */
+rt_status rt_scene_create(rt_context *ctx, rt_scene **out);
+rt_status rt_scene_destroy(rt_scene *scene);
+
+/* Upload an indexed triangle mesh.  Replaces building a primitive_store with
+ * primitive_store::emplace_back(material, a, b, c, light, v_n, v_t)
+ * (raytracer/primitive_store.h:29-34, triangle.h:124-176): verts_xyz holds 3
+ * floats per vertex, tri_idx 3 vertex indices per triangle (a, b, c; the
+ * face normal is (b-a) x (c-a)), vert_attr (nullable) 3 floats per vertex
+ * (the per-vertex texture attribute, a colour in 0..1), tri_flags (nullable)
+ * RT_TRI_* bits per triangle.  Invalidates any built hierarchy. */
+rt_status rt_scene_upload(rt_scene *scene, const float *verts_xyz, int32_t nverts, const int32_t *tri_idx,
+                          int32_t ntris, const float *vert_attr, const uint32_t *tri_flags);
+
+/* Update vertex positions (same topology) and rebuild the hierarchy; the
+ * per-frame rebuild the physics engine's render loop needs
+ * (physics_engine/simulation_environment.cc:56-58). */
+rt_status rt_scene_update_vertices(rt_scene *scene, const float *verts_xyz, int32_t nverts);
+
+/* Build the acceleration structure: GPU Morton LBVH collapsed to 8-wide
+ * nodes with 8-bit conservatively quantised child boxes.  Replaces
+ * bvh::bvh(primitive_store&) -> bvh_builder::build
+ * (spatial_sub_division/bvh.h:27-32, bvh_builder.cc:18-178).  build_ms
+ * (nullable) receives the device build time. */
+rt_status rt_bvh_build(rt_scene *scene, float *build_ms);
+
+/* Hierarchy statistics: wide nodes, packed triangle slots, tree depth. */
+rt_status rt_bvh_info(const rt_scene *scene, int32_t *nodes, int32_t *tri_slots, int32_t *depth);
+
+/* ---------------------------------------------------------- traversal */
+
+/* Closest hit for n rays.  Replaces ssd::find_nearest_object(const ray*,
+ * hit_description*) (spatial_sub_division/ssd.h:26-44) as implemented by
+ * bvh::find_nearest_object (bvh.cc:649-709).  Accepts t > 1e-3 (EPSILON);
+ * among equal t the lowest triangle id wins. */
+rt_status rt_trace_closest(rt_scene *scene, const rt_ray *rays, int32_t n, rt_hit *hits);
+
+/* Any hit with 1e-3 < t < ray.tmax for n rays, skipping light and
+ * transparent triangles.  Replaces ssd::found_nearer_object(const ray*,
+ * float t) (ssd.h, bvh.cc:711-759, bvh_node.h:170-190).  occluded[i] is 1
+ * when ray i is blocked. */
+rt_status rt_trace_any(rt_scene *scene, const rt_ray *rays, int32_t n, uint8_t *occluded);
+
+/* ------------------------------------------------------------- render */
+
+/* Render one frame: primary ray per pixel, closest hit, one shadow ray per
+ * light from the offset hit point, coloured Phong, clamp-and-truncate to
+ * RGB8, all in one fused kernel.  Replaces ray_tracer(const ssd*, const
+ * light_list&, const primitive_store&, camera&) (raytracer.h:105,
+ * raytracer.cc:563-598) followed by camera::clip_image_to_rgb
+ * (camera.h:289-319).  rgb_out: xres*yres*3 bytes, row 0 at the bottom.
+ * hit_ids (nullable): primary-hit triangle id per pixel (-1 = background).
+ * Up to RT_MAX_LIGHTS lights. */
+#define RT_MAX_LIGHTS 8
+rt_status rt_render(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                    const rt_material *material, uint8_t *rgb_out, int32_t *hit_ids, rt_render_stats *stats);
+
+/* Ambient-occlusion render (no reference counterpart; the reference has no
+ * AO): primary closest hit, then `samples` cosine-weighted hemisphere rays
+ * per hit (Philox4x32-10 keyed by pixel and sample, seed) from the offset hit
+ * point, any-hit within `ao_dist`.  Pixel = ka + kd * unoccluded fraction.
+ * ao_count (nullable): unoccluded rays per pixel.  samples <= 64. */
+rt_status rt_render_ao(rt_scene *scene, const rt_camera *camera, const rt_material *material, int32_t samples,
+                       float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
+                       rt_render_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

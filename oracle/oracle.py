@@ -1,0 +1,299 @@
+"""ctypes front end of the oracle libraries -- TEST INFRASTRUCTURE ONLY.
+
+Loads oracle/_build/librtoracle.so (the C restatement of the reference's
+hot path) and, where it was built, oracle/_ref/libraptor_ref.so (the
+reference's own sources behind a harness).  Only tests, the smoke check and
+the CPU-baseline leg of the benchmark import this module; the product never
+does.  `build()` compiles both.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "librtoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libraptor_ref.so")
+REF_SRC = "/root/reference/RAPTor"
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("x_axis", C.c_float * 3), ("y_axis", C.c_float * 3),
+                ("z_axis", C.c_float * 3), ("background", C.c_float * 3), ("w", C.c_float),
+                ("h", C.c_float), ("t", C.c_float), ("xres", C.c_int32), ("yres", C.c_int32)]
+
+
+class Light(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
+                ("d", C.c_float)]
+
+
+class Material(C.Structure):
+    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float)]
+
+
+def make_camera(d):
+    c = Camera()
+    for k in ("pos", "x_axis", "y_axis", "z_axis", "background"):
+        getattr(c, k)[:] = [float(x) for x in d[k]]
+    c.w, c.h, c.t, c.xres, c.yres = d["w"], d["h"], d["t"], d["xres"], d["yres"]
+    return c
+
+
+def make_lights(ls):
+    arr = (Light * max(1, len(ls)))()
+    for i, d in enumerate(ls):
+        arr[i].kind = d["kind"]
+        arr[i].rgb[:] = list(d["rgb"])
+        arr[i].pos[:] = list(d["pos"])
+        arr[i].dir[:] = list(d["dir"])
+        arr[i].d = d["d"]
+    return arr
+
+
+def make_material(d):
+    m = Material()
+    m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
+    m.ns = d["ns"]
+    return m
+
+
+def build(verbose: bool = False) -> None:
+    """Compile the C restatement; compile the reference harness too when the
+    reference tree is present and the host is x86-64."""
+    os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
+    cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-o", ORACLE_SO,
+           os.path.join(HERE, "rtoracle.c"), "-lm", "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=not verbose)
+    if os.path.isdir(REF_SRC) and platform.machine() in ("x86_64", "AMD64"):
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "refbuild"), f"REF={REF_SRC}", "-j8"], check=True,
+                       capture_output=not verbose)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t)) if a is not None else None
+
+
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int32)
+_U32 = C.POINTER(C.c_uint32)
+_U8 = C.POINTER(C.c_uint8)
+
+
+def _declare(lib, prefix):
+    lib[prefix + "scene_build"].restype = C.c_double
+    lib[prefix + "scene_build"].argtypes = [C.c_void_p]
+    lib[prefix + "scene_destroy"].argtypes = [C.c_void_p]
+    lib[prefix + "trace_closest"].argtypes = [C.c_void_p, _F, _F, C.c_int32, _I, _F, _F, _F]
+    lib[prefix + "trace_any"].argtypes = [C.c_void_p, _F, _F, _F, C.c_int32, _U8]
+    lib[prefix + "camera_rays"].argtypes = [C.POINTER(Camera), C.c_int32, C.c_int32, C.c_int32, C.c_int32, _F, _F]
+    lib[prefix + "morton_code"].restype = C.c_int32
+    lib[prefix + "morton_code"].argtypes = [C.c_float] * 6
+
+
+class _Lib:
+    def __init__(self, path):
+        self.h = C.CDLL(path)
+
+    def __getitem__(self, k):
+        return getattr(self.h, k)
+
+
+class _SceneBase:
+    prefix = ""
+
+    def closest(self, ogn, dir):
+        ogn = np.ascontiguousarray(ogn, dtype=np.float32).reshape(-1, 3)
+        dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
+        n = ogn.shape[0]
+        ids = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        rc = self.lib[self.prefix + "trace_closest"](self.h, _p(ogn, C.c_float), _p(dir, C.c_float), n,
+                                                     _p(ids, C.c_int32), _p(t, C.c_float), _p(u, C.c_float),
+                                                     _p(v, C.c_float))
+        if rc != 0:
+            raise RuntimeError("trace_closest failed")
+        return ids, t, u, v
+
+    def any(self, ogn, dir, tmax):
+        ogn = np.ascontiguousarray(ogn, dtype=np.float32).reshape(-1, 3)
+        dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
+        tmax = np.ascontiguousarray(np.broadcast_to(np.asarray(tmax, np.float32), (ogn.shape[0],)))
+        occ = np.empty(ogn.shape[0], np.uint8)
+        rc = self.lib[self.prefix + "trace_any"](self.h, _p(ogn, C.c_float), _p(dir, C.c_float), _p(tmax, C.c_float),
+                                                 ogn.shape[0], _p(occ, C.c_uint8))
+        if rc != 0:
+            raise RuntimeError("trace_any failed")
+        return occ
+
+    def close(self):
+        if self.h:
+            self.lib[self.prefix + "scene_destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_oracle = None
+_ref = None
+
+
+def oracle_lib():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        lib = _Lib(ORACLE_SO)
+        _declare(lib, "ro_")
+        lib["ro_scene_create"].restype = C.c_void_p
+        lib["ro_scene_create"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32]
+        lib["ro_scene_node_count"].restype = C.c_int32
+        lib["ro_scene_node_count"].argtypes = [C.c_void_p]
+        lib["ro_render"].restype = C.c_int64
+        lib["ro_render"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32, C.POINTER(Material),
+                                     C.c_int32, C.c_int32, C.c_int32, _U8, _I, _U8, _F]
+        lib["ro_render_ao"].restype = C.c_int64
+        lib["ro_render_ao"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Material), C.c_int32, C.c_float,
+                                        C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _U8, _I, _I]
+        lib["ro_ao_rays"].argtypes = [_F, _F, C.c_uint32, C.c_int32, C.c_uint32, _F, _F]
+        lib["ro_philox4x32"].argtypes = [_U32, C.c_uint32, C.c_uint32, _U32]
+        _oracle = lib
+    return _oracle
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        lib = _Lib(REF_SO)
+        _declare(lib, "rref_")
+        lib["rref_scene_create"].restype = C.c_void_p
+        lib["rref_scene_create"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32, C.POINTER(Material)]
+        lib["rref_render"].restype = C.c_double
+        lib["rref_render"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32, _U8]
+        _ref = lib
+    return _ref
+
+
+def _scene_arrays(scene):
+    v = np.ascontiguousarray(scene["verts"], np.float32)
+    t = np.ascontiguousarray(scene["tris"], np.int32)
+    a = scene.get("vattr")
+    a = None if a is None else np.ascontiguousarray(a, np.float32)
+    f = scene.get("flags")
+    f = None if f is None else np.ascontiguousarray(f, np.uint32)
+    return v, t, a, f
+
+
+class OracleScene(_SceneBase):
+    """The C restatement, built on construction."""
+    prefix = "ro_"
+
+    def __init__(self, scene):
+        self.lib = oracle_lib()
+        v, t, a, f = _scene_arrays(scene)
+        self._keep = (v, t, a, f)
+        self.h = self.lib["ro_scene_create"](_p(v, C.c_float), v.shape[0], _p(t, C.c_int32), t.shape[0],
+                                             _p(a, C.c_float), _p(f, C.c_uint32))
+        if not self.h:
+            raise ValueError("invalid scene")
+        self.build_seconds = self.lib["ro_scene_build"](self.h)
+        if self.build_seconds < 0:
+            raise MemoryError("oracle build failed")
+
+    def node_count(self):
+        return self.lib["ro_scene_node_count"](self.h)
+
+    def render(self, frame, rows=None, threads=1, want_ids=False, want_float=False, want_occl=False):
+        cam = make_camera(frame["camera"])
+        W, H = cam.xres, cam.yres
+        r0, r1 = (0, H) if rows is None else rows
+        rgb = np.zeros((H, W, 3), np.uint8)
+        ids = np.full((H, W), -2, np.int32) if want_ids else None
+        occl = np.zeros((H, W), np.uint8) if want_occl else None
+        fimg = np.zeros((H, W, 3), np.float32) if want_float else None
+        mat = make_material(frame["material"])
+        ao = frame.get("ao")
+        if ao:
+            cnt = np.zeros((H, W), np.int32)
+            n = self.lib["ro_render_ao"](self.h, C.byref(cam), C.byref(mat), ao["samples"], ao["dist"], ao["seed"],
+                                         r0, r1, threads, _p(rgb, C.c_uint8), _p(ids, C.c_int32), _p(cnt, C.c_int32))
+            out = {"rgb": rgb, "ids": ids, "ao_count": cnt, "rays": n}
+        else:
+            ls = make_lights(frame["lights"])
+            n = self.lib["ro_render"](self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), r0, r1, threads,
+                                      _p(rgb, C.c_uint8), _p(ids, C.c_int32), _p(occl, C.c_uint8),
+                                      _p(fimg, C.c_float))
+            out = {"rgb": rgb, "ids": ids, "occl": occl, "fimg": fimg, "rays": n}
+        if n < 0:
+            raise RuntimeError("oracle render failed")
+        return out
+
+
+class RefScene(_SceneBase):
+    """The reference's own bvh + ray_tracer behind the harness (x86 only)."""
+    prefix = "rref_"
+
+    def __init__(self, scene, material):
+        self.lib = ref_lib()
+        v, t, a, f = _scene_arrays(scene)
+        self._keep = (v, t, a, f)
+        self.mat = make_material(material)
+        self.h = self.lib["rref_scene_create"](_p(v, C.c_float), v.shape[0], _p(t, C.c_int32), t.shape[0],
+                                               _p(a, C.c_float), _p(f, C.c_uint32), C.byref(self.mat))
+        self.build_seconds = self.lib["rref_scene_build"](self.h)
+
+    def render(self, frame):
+        cam = make_camera(frame["camera"])
+        rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
+        ls = make_lights(frame["lights"])
+        secs = self.lib["rref_render"](self.h, C.byref(cam), ls, len(frame["lights"]), _p(rgb, C.c_uint8))
+        return {"rgb": rgb, "seconds": secs}
+
+
+def camera_rays(cam_dict, x0=0, y0=0, w=None, h=None, lib=None):
+    lib = lib or oracle_lib()
+    cam = make_camera(cam_dict)
+    w = cam.xres if w is None else w
+    h = cam.yres if h is None else h
+    ogn = np.empty((w * h, 3), np.float32)
+    dirs = np.empty((w * h, 3), np.float32)
+    pre = "rref_" if lib is _ref else "ro_"
+    lib[pre + "camera_rays"](C.byref(cam), x0, y0, w, h, _p(ogn, C.c_float), _p(dirs, C.c_float))
+    return ogn, dirs
+
+
+def morton(x, y, z, xm, ym, zm, lib=None):
+    lib = lib or oracle_lib()
+    pre = "rref_" if lib is _ref else "ro_"
+    return lib[pre + "morton_code"](x, y, z, xm, ym, zm) & 0xFFFFFFFF
+
+
+def ao_rays(hit_point, geo_normal, pixel, nsamples, seed):
+    lib = oracle_lib()
+    hp = np.ascontiguousarray(hit_point, np.float32)
+    gn = np.ascontiguousarray(geo_normal, np.float32)
+    ogn = np.empty((nsamples, 3), np.float32)
+    dirs = np.empty((nsamples, 3), np.float32)
+    lib["ro_ao_rays"](_p(hp, C.c_float), _p(gn, C.c_float), pixel, nsamples, seed, _p(ogn, C.c_float),
+                      _p(dirs, C.c_float))
+    return ogn, dirs
+
+
+def philox(ctr, key0, key1):
+    lib = oracle_lib()
+    c = np.ascontiguousarray(ctr, np.uint32)
+    o = np.empty(4, np.uint32)
+    lib["ro_philox4x32"](_p(c, C.c_uint32), key0, key1, _p(o, C.c_uint32))
+    return o

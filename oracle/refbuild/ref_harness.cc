@@ -1,0 +1,187 @@
+// ref_harness.cc -- drives the UNMODIFIED RAPTor sources (compiled from the
+// reference tree by oracle/refbuild/Makefile) through their own public API,
+// so tests can pin the C restatement in oracle/rtoracle.c against the
+// reference itself and generate golden fixtures.
+//
+// TEST INFRASTRUCTURE ONLY.  Builds only on x86-64 hosts: the reference's
+// common/simd.h includes <immintrin.h> unconditionally.
+//
+// Entry points mirror oracle/rtoracle.h one for one (prefix rref_).
+#include <cstdint>
+#include <cstring>
+#include <chrono>
+#include <iostream>
+#include <memory>
+#include <streambuf>
+#include <vector>
+
+#include "bvh.h"
+#include "camera.h"
+#include "coloured_mapper_shader.h"
+#include "light.h"
+#include "primitive_store.h"
+#include "raytracer.h"
+#include "texture_mapper.h"
+
+#include "../rtoracle.h"
+
+using namespace raptor_raytracer;
+
+namespace {
+
+// Texture mapper that returns the interpolated per-vertex attribute scaled
+// to 0..255, which is how a per-vertex colour reaches
+// coloured_mapper_shader::shade (coloured_mapper_shader.cc:61-66).
+class vertex_colour_mapper : public texture_mapper {
+  protected:
+    float sample_texture(const ray &, ext_colour_t *const c, const point_t<> &, const point_t<> &vt) const override
+    {
+        *c = ext_colour_t(vt.x * 255.0f, vt.y * 255.0f, vt.z * 255.0f);
+        return 1.0f;
+    }
+    float sample_texture_monochrome(const ray &, point_t<> *const p, const point_t<> &, const point_t<> &vt,
+                                    const int, const int) const override
+    {
+        p->z = vt.x * 255.0f;
+        return 1.0f;
+    }
+};
+
+struct null_buf : std::streambuf {
+    int overflow(int c) override { return c; }
+    std::streamsize xsputn(const char *, std::streamsize n) override { return n; }
+};
+
+struct ref_scene {
+    std::unique_ptr<material> opaque;
+    std::unique_ptr<material> transparent;
+    primitive_store store;
+    std::unique_ptr<bvh> accel;
+};
+
+point_t<> p3(const float *p) { return point_t<>(p[0], p[1], p[2]); }
+
+}  // namespace
+
+extern "C" {
+
+void *rref_scene_create(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris, const float *vattr,
+                        const uint32_t *flags, const ro_material *m)
+{
+    (void)nverts;
+    auto *s = new ref_scene();
+    const texture_mapper *kd_map = vattr ? new vertex_colour_mapper() : nullptr;
+    s->opaque.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
+                                               ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
+                                               ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.0f, 1.0f, 0.0f,
+                                               0.0f, 0.0f, nullptr, kd_map));
+    s->transparent.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
+                                                    ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
+                                                    ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.5f, 1.0f));
+    s->store.reserve(ntris);
+    for (int32_t i = 0; i < ntris; ++i) {
+        const int32_t ia = tris[3 * i], ib = tris[3 * i + 1], ic = tris[3 * i + 2];
+        const uint32_t f = flags ? flags[i] : 0u;
+        material *mat = (f & RO_TRI_TRANSPARENT) ? s->transparent.get() : s->opaque.get();
+        if (vattr) {
+            point_t<> vt[3] = {p3(vattr + 3 * ia), p3(vattr + 3 * ib), p3(vattr + 3 * ic)};
+            s->store.emplace_back(mat, p3(verts + 3 * ia), p3(verts + 3 * ib), p3(verts + 3 * ic),
+                                  (f & RO_TRI_LIGHT) != 0, static_cast<const point_t<> *>(nullptr),
+                                  static_cast<const point_t<> *>(vt));
+        } else {
+            s->store.emplace_back(mat, p3(verts + 3 * ia), p3(verts + 3 * ib), p3(verts + 3 * ic),
+                                  (f & RO_TRI_LIGHT) != 0);
+        }
+    }
+    return s;
+}
+
+double rref_scene_build(void *h)
+{
+    auto *s = static_cast<ref_scene *>(h);
+    const auto t0 = std::chrono::steady_clock::now();
+    s->accel.reset(new bvh(s->store));
+    const auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+void rref_scene_destroy(void *h) { delete static_cast<ref_scene *>(h); }
+
+int32_t rref_trace_closest(void *h, const float *ogn, const float *dir, int32_t n, int32_t *id, float *t, float *u,
+                           float *v)
+{
+    auto *s = static_cast<ref_scene *>(h);
+    for (int32_t i = 0; i < n; ++i) {
+        const ray r(p3(ogn + 3 * i), dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+        hit_description hd;
+        id[i] = s->accel->find_nearest_object(&r, &hd);
+        t[i] = hd.d;
+        if (u) u[i] = hd.u;
+        if (v) v[i] = hd.v;
+    }
+    return 0;
+}
+
+int32_t rref_trace_any(void *h, const float *ogn, const float *dir, const float *tmax, int32_t n, uint8_t *occ)
+{
+    auto *s = static_cast<ref_scene *>(h);
+    for (int32_t i = 0; i < n; ++i) {
+        const ray r(p3(ogn + 3 * i), dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+        occ[i] = s->accel->found_nearer_object(&r, tmax[i]) ? 1 : 0;
+    }
+    return 0;
+}
+
+static camera *make_camera(const ro_camera *c)
+{
+    return new camera(p3(c->pos), p3(c->x_axis), p3(c->y_axis), p3(c->z_axis),
+                      ext_colour_t(c->background[0], c->background[1], c->background[2]), c->w, c->h, c->t,
+                      (unsigned)c->xres, (unsigned)c->yres, 1u, 1u, 0.0f, 0.0f);
+}
+
+void rref_camera_rays(const ro_camera *c, int32_t x0, int32_t y0, int32_t w, int32_t hgt, float *ogn, float *dir)
+{
+    std::unique_ptr<camera> cam(make_camera(c));
+    std::vector<ray> rays;
+    size_t k = 0;
+    for (int32_t y = y0; y < y0 + hgt; ++y)
+        for (int32_t x = x0; x < x0 + w; ++x, ++k) {
+            cam->pixel_to_co_ordinate(&rays, x, y, 1, 1, 16);
+            const point_t<> o = rays[0].get_ogn(), d = rays[0].get_dir();
+            ogn[3 * k] = o.x; ogn[3 * k + 1] = o.y; ogn[3 * k + 2] = o.z;
+            dir[3 * k] = d.x; dir[3 * k + 1] = d.y; dir[3 * k + 2] = d.z;
+        }
+}
+
+// Full-frame render through ray_tracer() (raytracer.cc:563) and
+// clip_image_to_rgb (camera.h:289).  The per-pixel progress line the
+// reference prints (raytracer.cc:529) goes to a null stream.  Returns the
+// render wall time in seconds.
+double rref_render(void *h, const ro_camera *c, const ro_light *ls, int32_t nl, uint8_t *rgb)
+{
+    auto *s = static_cast<ref_scene *>(h);
+    std::unique_ptr<camera> cam(make_camera(c));
+    light_list lights;
+    for (int32_t i = 0; i < nl; ++i) {
+        const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
+        if (ls[i].kind == 1)
+            lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
+        else
+            lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
+    }
+    null_buf nb;
+    std::streambuf *old = std::cout.rdbuf(&nb);
+    const auto t0 = std::chrono::steady_clock::now();
+    ray_tracer(s->accel.get(), lights, s->store, *cam);
+    const auto t1 = std::chrono::steady_clock::now();
+    std::cout.rdbuf(old);
+    cam->clip_image_to_rgb(rgb);
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+int32_t rref_morton_code(float x, float y, float z, float xm, float ym, float zm)
+{
+    return morton_code(x, y, z, xm, ym, zm);
+}
+
+}  // extern "C"

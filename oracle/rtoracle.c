@@ -1,0 +1,796 @@
+/*
+ * rtoracle.c -- CPU restatement of RAPTor's ray-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA core, never part of the
+ * product.  Compile with -ffp-contract=off (no FMA contraction) so the
+ * results are the reference's IEEE binary32 results on any host.
+ *
+ * Reference paths below are relative to the RAPTor project root.
+ */
+#define _POSIX_C_SOURCE 200809L
+#include "rtoracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* Constants (common/common.cc:14-17). */
+#define RO_EPSILON 1.0e-3f
+#define RO_FP_DELTA 32.0f
+#define RO_FP_DELTA_SMALL 1.0e-4f
+#define RO_MAX_DIST FLT_MAX
+/* Traversal stack height (common/common.h:63-64). */
+#define RO_MAX_STACK 100
+#define RO_LEAF_SIZE 4
+
+typedef struct { float x, y, z; } v3;
+
+static inline v3 mk(float x, float y, float z) { v3 r = {x, y, z}; return r; }
+static inline v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vmul(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline v3 vdivs(v3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+static inline v3 vneg(v3 a) { return mk(-a.x, -a.y, -a.z); }
+/* dot_product / cross_product (common/point_t.h:498-525), left to right. */
+static inline float vdot(v3 a, v3 b) { return ((a.x * b.x) + (a.y * b.y)) + (a.z * b.z); }
+static inline v3 vcross(v3 a, v3 b)
+{
+    return mk((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
+}
+/* std::min / std::max semantics: min(a,b) = (b < a) ? b : a. */
+static inline float smin(float a, float b) { return (b < a) ? b : a; }
+static inline float smax(float a, float b) { return (a < b) ? b : a; }
+static inline v3 vmin(v3 a, v3 b) { return mk(smin(a.x, b.x), smin(a.y, b.y), smin(a.z, b.z)); }
+static inline v3 vmax(v3 a, v3 b) { return mk(smax(a.x, b.x), smax(a.y, b.y), smax(a.z, b.z)); }
+/* magnitude (point_t.h:357) and normalise with EXACT_NORMALISE (point_t.h:571-585). */
+static inline float vmag(v3 a) { return sqrtf(((a.x * a.x) + (a.y * a.y)) + (a.z * a.z)); }
+static inline v3 vnorm(v3 a)
+{
+    const float d = sqrtf(((a.x * a.x) + (a.y * a.y)) + (a.z * a.z));
+    return mk(a.x / d, a.y / d, a.z / d);
+}
+static inline v3 ld3(const float *p) { return mk(p[0], p[1], p[2]); }
+
+static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
+/* float -> int32 truncation with the x86 cvttss2si result for NaN and
+ * out-of-range inputs (the integer-indefinite value), so hosts agree. */
+static inline int32_t cvtt(float f)
+{
+    if (!(f > -2147483904.0f && f < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)f;
+}
+
+/* ---------------------------------------------------------------- Morton */
+
+/* split_by_three + morton_code (common/simd.h:798-825). */
+static inline uint32_t split3(uint32_t a)
+{
+    a |= (a << 16); a &= 0x030000FFu;
+    a |= (a << 8);  a &= 0x0300F00Fu;
+    a |= (a << 4);  a &= 0x030C30C3u;
+    a |= (a << 2);  a &= 0x09249249u;
+    return a;
+}
+
+int32_t ro_morton_code(float x, float y, float z, float x_mul, float y_mul, float z_mul)
+{
+    const uint32_t xi = split3((uint32_t)cvtt(x * x_mul));
+    const uint32_t yi = split3((uint32_t)cvtt(y * y_mul));
+    const uint32_t zi = split3((uint32_t)cvtt(z * z_mul));
+    return (int32_t)(xi | (yi << 1) | (zi << 2));
+}
+
+/* ----------------------------------------------------------------- Scene */
+
+typedef struct ro_node {
+    v3 lo, hi;          /* bvh_node::_low / _high (bvh_node.h:294-311) */
+    int32_t a, b;       /* leaf: [a, b) into indirect; inner: left, right */
+    int32_t leaf;
+} ro_node;
+
+struct ro_scene {
+    int32_t ntris;
+    v3 *va, *vb, *vc;   /* triangle vertices (triangle.h:108-110) */
+    v3 *n;              /* face normal (triangle.h:170-175) */
+    v3 *ta, *tb, *tc;   /* per-vertex attribute (triangle vnt[3..5]) or NULL */
+    uint32_t *flags;
+    ro_node *nodes;
+    int32_t nnodes, root;
+    int32_t *indirect;  /* primitive_store::_indirect */
+};
+
+ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris,
+                          const float *vattr, const uint32_t *flags)
+{
+    if (ntris < 0 || nverts < 0) return NULL;
+    ro_scene *s = (ro_scene *)calloc(1, sizeof(ro_scene));
+    if (!s) return NULL;
+    s->ntris = ntris;
+    const size_t nt = (size_t)(ntris > 0 ? ntris : 1);
+    s->va = (v3 *)malloc(nt * sizeof(v3));
+    s->vb = (v3 *)malloc(nt * sizeof(v3));
+    s->vc = (v3 *)malloc(nt * sizeof(v3));
+    s->n = (v3 *)malloc(nt * sizeof(v3));
+    s->flags = (uint32_t *)calloc(nt, sizeof(uint32_t));
+    if (vattr) {
+        s->ta = (v3 *)malloc(nt * sizeof(v3));
+        s->tb = (v3 *)malloc(nt * sizeof(v3));
+        s->tc = (v3 *)malloc(nt * sizeof(v3));
+    }
+    for (int32_t i = 0; i < ntris; ++i) {
+        const int32_t ia = tris[3 * i], ib = tris[3 * i + 1], ic = tris[3 * i + 2];
+        if (ia < 0 || ib < 0 || ic < 0 || ia >= nverts || ib >= nverts || ic >= nverts) {
+            ro_scene_destroy(s);
+            return NULL;
+        }
+        s->va[i] = ld3(verts + 3 * (size_t)ia);
+        s->vb[i] = ld3(verts + 3 * (size_t)ib);
+        s->vc[i] = ld3(verts + 3 * (size_t)ic);
+        /* triangle::triangle normal (triangle.h:171-175): (b-a) x (c-a), normalised */
+        s->n[i] = vnorm(vcross(vsub(s->vb[i], s->va[i]), vsub(s->vc[i], s->va[i])));
+        if (vattr) {
+            s->ta[i] = ld3(vattr + 3 * (size_t)ia);
+            s->tb[i] = ld3(vattr + 3 * (size_t)ib);
+            s->tc[i] = ld3(vattr + 3 * (size_t)ic);
+        }
+        if (flags) s->flags[i] = flags[i];
+    }
+    return s;
+}
+
+void ro_scene_destroy(ro_scene *s)
+{
+    if (!s) return;
+    free(s->va); free(s->vb); free(s->vc); free(s->n);
+    free(s->ta); free(s->tb); free(s->tc); free(s->flags);
+    free(s->nodes); free(s->indirect);
+    free(s);
+}
+
+int32_t ro_scene_node_count(const ro_scene *s) { return s ? s->nnodes : 0; }
+
+/* -------------------------------------------------------------- Builder */
+
+typedef struct {
+    ro_scene *s;
+    const uint32_t *codes;  /* Morton code per sorted position */
+    v3 *plo, *phi;          /* primitive bounds, original order */
+    int32_t next;
+} build_ctx;
+
+static inline int clz32(uint32_t x) { return x ? __builtin_clz(x) : 32; }
+
+/* Top-down split of the Morton-sorted range [b, e) at the highest differing
+ * bit (stand-in for the reference's AAC clustering, see the file header). */
+static int32_t build_range(build_ctx *c, int32_t b, int32_t e)
+{
+    const int32_t me = c->next++;
+    ro_node *nd = &c->s->nodes[me];
+    v3 lo = mk(RO_MAX_DIST, RO_MAX_DIST, RO_MAX_DIST), hi = mk(-RO_MAX_DIST, -RO_MAX_DIST, -RO_MAX_DIST);
+    for (int32_t i = b; i < e; ++i) {
+        const int32_t p = c->s->indirect[i];
+        lo = vmin(lo, c->plo[p]);
+        hi = vmax(hi, c->phi[p]);
+    }
+    nd->lo = lo; nd->hi = hi;
+    if (e - b <= RO_LEAF_SIZE) {
+        nd->a = b; nd->b = e; nd->leaf = 1;
+        return me;
+    }
+    int32_t split;
+    const uint32_t cf = c->codes[b], cl = c->codes[e - 1];
+    if (cf == cl) {
+        split = (b + e) >> 1;
+    } else {
+        const int common = clz32(cf ^ cl);
+        split = b;
+        int32_t step = e - 1 - b;
+        do {   /* binary search for the last code sharing more than `common` bits */
+            step = (step + 1) >> 1;
+            const int32_t ns = split + step;
+            if (ns < e - 1 && clz32(cf ^ c->codes[ns]) > common) split = ns;
+        } while (step > 1);
+        split += 1;
+    }
+    const int32_t l = build_range(c, b, split);
+    const int32_t r = build_range(c, split, e);
+    nd = &c->s->nodes[me];
+    nd->a = l; nd->b = r; nd->leaf = 0;
+    return me;
+}
+
+double ro_scene_build(ro_scene *s)
+{
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (!s) return -1.0;
+    const int32_t n = s->ntris;
+    free(s->nodes); free(s->indirect);
+    s->nodes = (ro_node *)calloc((size_t)(n > 0 ? 2 * n : 1), sizeof(ro_node));
+    s->indirect = (int32_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+    if (!s->nodes || !s->indirect) return -1.0;
+    if (n == 0) {
+        s->nnodes = 1; s->root = 0;
+        s->nodes[0].lo = mk(RO_MAX_DIST, RO_MAX_DIST, RO_MAX_DIST);
+        s->nodes[0].hi = mk(-RO_MAX_DIST, -RO_MAX_DIST, -RO_MAX_DIST);
+        s->nodes[0].leaf = 1;
+        return 0.0;
+    }
+    const size_t nn = (size_t)(uint32_t)n;
+    v3 *plo = (v3 *)malloc(nn * sizeof(v3));
+    v3 *phi = (v3 *)malloc(nn * sizeof(v3));
+    uint32_t *code = (uint32_t *)malloc(nn * sizeof(uint32_t));
+    uint32_t *code2 = (uint32_t *)malloc(nn * sizeof(uint32_t));
+    int32_t *idx2 = (int32_t *)malloc(nn * sizeof(int32_t));
+    if (!plo || !phi || !code || !code2 || !idx2) {
+        free(plo); free(phi); free(code); free(code2); free(idx2);
+        return -1.0;
+    }
+    /* Primitive and scene bounds (bvh_builder.cc:30-42, triangle.h:56-57). */
+    v3 sb = mk(RO_MAX_DIST, RO_MAX_DIST, RO_MAX_DIST), st = mk(-RO_MAX_DIST, -RO_MAX_DIST, -RO_MAX_DIST);
+    for (int32_t i = 0; i < n; ++i) {
+        plo[i] = vmin(s->va[i], vmin(s->vb[i], s->vc[i]));
+        phi[i] = vmax(s->va[i], vmax(s->vb[i], s->vc[i]));
+        sb = vmin(sb, plo[i]);
+        st = vmax(st, phi[i]);
+    }
+    /* Morton codes of box centres (bvh_builder.cc:45-106). */
+    const v3 sw = vsub(st, sb);
+    const v3 width = vmul(sw, 1.00001f / 1024.0f);
+    const v3 winv = mk(1.0f / width.x, 1.0f / width.y, 1.0f / width.z);
+    for (int32_t i = 0; i < n; ++i) {
+        const v3 t = vsub(vmul(vadd(phi[i], plo[i]), 0.5f), sb);
+        code[i] = (uint32_t)ro_morton_code(t.x, t.y, t.z, winv.x, winv.y, winv.z);
+        s->indirect[i] = i;
+    }
+    /* Three stable 10-bit counting passes, low digit first (bvh_builder.cc:108-158);
+     * the 32-bit code is masked per digit so garbage high bits stay in range. */
+    for (int pass = 0; pass < 3; ++pass) {
+        uint32_t hist[1025];
+        memset(hist, 0, sizeof(hist));
+        const int sh = 10 * pass;
+        for (int32_t i = 0; i < n; ++i) hist[((code[i] >> sh) & 0x3ffu) + 1]++;
+        for (int k = 0; k < 1024; ++k) hist[k + 1] += hist[k];
+        for (int32_t i = 0; i < n; ++i) {
+            const uint32_t d = (code[i] >> sh) & 0x3ffu;
+            const uint32_t pos = hist[d]++;
+            code2[pos] = code[i];
+            idx2[pos] = s->indirect[i];
+        }
+        memcpy(code, code2, nn * sizeof(uint32_t));
+        memcpy(s->indirect, idx2, nn * sizeof(int32_t));
+    }
+    build_ctx c = {s, code, plo, phi, 0};
+    s->root = build_range(&c, 0, n);
+    s->nnodes = c.next;
+    free(plo); free(phi); free(code); free(code2); free(idx2);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+/* ------------------------------------------------------------ Traversal */
+
+typedef struct { v3 o, d; } ro_ray;
+typedef struct { float u, v, d; } ro_hit;
+
+/* triangle::is_intersecting (triangle.h:190-235): Moller-Trumbore with
+ * e1 = c - a, e2 = b - a; u weighs c, v weighs b.  Leaves h untouched when
+ * t <= EPSILON, sets d = MAX_DIST on any other rejection. */
+static inline void isect(const ro_scene *s, int32_t i, const ro_ray *r, ro_hit *h)
+{
+    const v3 a = s->va[i];
+    const v3 e1 = vsub(s->vc[i], a);
+    const v3 e2 = vsub(s->vb[i], a);
+    const v3 P = vcross(r->d, e2);
+    const float det = vdot(e1, P);
+    if (det > -0.000001f && det < 0.000001f) { h->d = RO_MAX_DIST; return; }
+    const float inv_det = 1.0f / det;
+    const v3 T = vsub(r->o, a);
+    const float u = vdot(T, P) * inv_det;
+    if (u < 0.0f) { h->d = RO_MAX_DIST; return; }
+    const v3 Q = vcross(T, e1);
+    const float v = vdot(r->d, Q) * inv_det;
+    if ((v < 0.0f) || ((u + v) > 1.0f)) { h->d = RO_MAX_DIST; return; }
+    const float t = vdot(e2, Q) * inv_det;
+    if (t > RO_EPSILON) { h->d = t; h->u = u; h->v = v; }
+}
+
+/* bvh_node::intersection_distance (bvh_node.h:61-98). */
+static inline float slab(const ro_node *nd, const ro_ray *r, v3 ird)
+{
+    v3 ld = mk((nd->lo.x - r->o.x) * ird.x, (nd->lo.y - r->o.y) * ird.y, (nd->lo.z - r->o.z) * ird.z);
+    v3 hd = mk((nd->hi.x - r->o.x) * ird.x, (nd->hi.y - r->o.y) * ird.y, (nd->hi.z - r->o.z) * ird.z);
+    float tmp;
+    if (ld.x > hd.x) { tmp = ld.x; ld.x = hd.x; hd.x = tmp; }
+    if (ld.y > hd.y) { tmp = ld.y; ld.y = hd.y; hd.y = tmp; }
+    if (ld.z > hd.z) { tmp = ld.z; ld.z = hd.z; hd.z = tmp; }
+    const float exit_t = smin(smin(hd.x, hd.y), hd.z);
+    const float enter_t = smax(smax(ld.x, ld.y), ld.z);
+    if (smax(0.0f, enter_t) > exit_t) return RO_MAX_DIST;
+    return enter_t;
+}
+
+typedef struct { float t_min; int32_t idx; } stack_el;
+
+/* bvh::find_leaf_node (bvh.cc:586-647).  Returns 1 with *cur at a leaf, or 0
+ * when both children lie beyond t_max + 100 EPSILON. */
+static inline int find_leaf(const ro_scene *s, const ro_ray *r, v3 ird, float t_max, int32_t *cur,
+                            stack_el *stack, int *sp, int *overflow)
+{
+    int32_t idx = *cur;
+    for (;;) {
+        const ro_node *nd = &s->nodes[idx];
+        if (nd->leaf) { *cur = idx; return 1; }
+        int32_t near_idx = nd->a, far_idx = nd->b;
+        float near_d = slab(&s->nodes[near_idx], r, ird);
+        float far_d = slab(&s->nodes[far_idx], r, ird);
+        if (near_d > far_d) {
+            int32_t ti = near_idx; near_idx = far_idx; far_idx = ti;
+            float tf = near_d; near_d = far_d; far_d = tf;
+        }
+        if (near_d >= (t_max + (100.0f * RO_EPSILON))) return 0;
+        if (far_d >= (t_max + (100.0f * RO_EPSILON))) {
+            idx = near_idx;
+        } else {
+            if (*sp + 1 >= RO_MAX_STACK) { *overflow = 1; return 0; }
+            ++*sp;
+            stack[*sp].idx = far_idx;
+            stack[*sp].t_min = far_d;
+            idx = near_idx;
+        }
+    }
+}
+
+/* bvh::find_nearest_object (bvh.cc:649-709) with test_leaf_node_nearest
+ * (bvh_node.h:152-168).  Returns the original triangle id or -1. */
+static int32_t closest(const ro_scene *s, const ro_ray *r, ro_hit *out)
+{
+    ro_hit best = {0.0f, 0.0f, RO_MAX_DIST};
+    const v3 ird = mk(1.0f / r->d.x, 1.0f / r->d.y, 1.0f / r->d.z);
+    if (s->ntris == 0 || slab(&s->nodes[s->root], r, ird) == RO_MAX_DIST) { *out = best; return -1; }
+    stack_el stack[RO_MAX_STACK];
+    int sp = 0, overflow = 0;
+    stack[0].idx = s->root; stack[0].t_min = RO_MAX_DIST;
+    int32_t cur = s->root;
+    int32_t hit_obj = -1;
+    for (;;) {
+        if (find_leaf(s, r, ird, best.d, &cur, stack, &sp, &overflow)) {
+            const ro_node *nd = &s->nodes[cur];
+            for (int32_t i = nd->a; i < nd->b; ++i) {
+                ro_hit h = {0.0f, 0.0f, best.d};
+                isect(s, s->indirect[i], r, &h);
+                if (h.d < best.d) { best = h; hit_obj = s->indirect[i]; }
+            }
+        }
+        if (overflow) break;
+        float tmin;
+        do {
+            if (sp == 0) { *out = best; return hit_obj; }
+            cur = stack[sp].idx;
+            tmin = stack[sp].t_min;
+            --sp;
+        } while (tmin > (best.d + (100.0f * RO_EPSILON)));
+    }
+    *out = best;
+    return hit_obj;
+}
+
+/* bvh::found_nearer_object (bvh.cc:711-759) with test_leaf_node_nearer
+ * (bvh_node.h:170-190): skips light and transparent triangles. */
+static int nearer(const ro_scene *s, const ro_ray *r, float t)
+{
+    if (s->ntris == 0) return 0;
+    const v3 ird = mk(1.0f / r->d.x, 1.0f / r->d.y, 1.0f / r->d.z);
+    stack_el stack[RO_MAX_STACK];
+    int sp = 0, overflow = 0;
+    stack[0].idx = s->root; stack[0].t_min = RO_MAX_DIST;
+    int32_t cur = s->root;
+    for (;;) {
+        if (find_leaf(s, r, ird, t, &cur, stack, &sp, &overflow)) {
+            const ro_node *nd = &s->nodes[cur];
+            for (int32_t i = nd->a; i < nd->b; ++i) {
+                const int32_t p = s->indirect[i];
+                if (s->flags[p] & (RO_TRI_LIGHT | RO_TRI_TRANSPARENT)) continue;
+                ro_hit h = {0.0f, 0.0f, t};
+                isect(s, p, r, &h);
+                if (h.d < t) return 1;
+            }
+        }
+        if (overflow || sp == 0) return 0;
+        cur = stack[sp].idx;
+        --sp;
+    }
+}
+
+int32_t ro_trace_closest(const ro_scene *s, const float *ogn, const float *dir, int32_t n,
+                         int32_t *id, float *t, float *u, float *v)
+{
+    if (!s || !s->nodes) return -1;
+    for (int32_t i = 0; i < n; ++i) {
+        ro_ray r = {ld3(ogn + 3 * (size_t)i), ld3(dir + 3 * (size_t)i)};
+        ro_hit h;
+        id[i] = closest(s, &r, &h);
+        t[i] = h.d;
+        if (u) u[i] = h.u;
+        if (v) v[i] = h.v;
+    }
+    return 0;
+}
+
+int32_t ro_trace_any(const ro_scene *s, const float *ogn, const float *dir, const float *tmax,
+                     int32_t n, uint8_t *occluded)
+{
+    if (!s || !s->nodes) return -1;
+    for (int32_t i = 0; i < n; ++i) {
+        ro_ray r = {ld3(ogn + 3 * (size_t)i), ld3(dir + 3 * (size_t)i)};
+        occluded[i] = (uint8_t)nearer(s, &r, tmax[i]);
+    }
+    return 0;
+}
+
+/* --------------------------------------------------------------- Camera */
+
+typedef struct {
+    v3 c, X, Y, Z;
+    float x_m, y_m, x_inc, y_inc, t;
+} cam_state;
+
+/* base_camera axes go through quaternion_t::rotate with the identity
+ * orientation (sdl_wrappers/base_camera.h, common/quaternion_t.h:166-169);
+ * restated literally so signed zeros come out as in the reference. */
+static v3 identity_rotate(v3 p)
+{
+    const float qw = 1.0f, qx = 0.0f, qy = 0.0f, qz = 0.0f;
+    const v3 c1 = mk((qy * p.z) - (qz * p.y), (qz * p.x) - (qx * p.z), (qx * p.y) - (qy * p.x));
+    const v3 c2 = mk((qy * c1.z) - (qz * c1.y), (qz * c1.x) - (qx * c1.z), (qx * c1.y) - (qy * c1.x));
+    const v3 a = mk(2.0f * c2.x, 2.0f * c2.y, 2.0f * c2.z);
+    const float w2 = 2.0f * qw;
+    const v3 b = mk(w2 * c1.x, w2 * c1.y, w2 * c1.z);
+    return vadd(vadd(p, a), b);
+}
+
+static cam_state cam_setup(const ro_camera *cam)
+{
+    cam_state cs;
+    cs.c = ld3(cam->pos);
+    cs.X = identity_rotate(ld3(cam->x_axis));
+    cs.Y = identity_rotate(ld3(cam->y_axis));
+    cs.Z = identity_rotate(ld3(cam->z_axis));
+    /* camera.h:60: x_m(-w), x_inc((w * 2) / x_res) */
+    cs.x_m = -cam->w;
+    cs.y_m = -cam->h;
+    cs.x_inc = (cam->w * 2.0f) / (float)cam->xres;
+    cs.y_inc = (cam->h * 2.0f) / (float)cam->yres;
+    cs.t = cam->t;
+    return cs;
+}
+
+/* camera::pixel_to_co_ordinate (camera.h:127-140): no half-pixel offset. */
+static inline ro_ray cam_ray(const cam_state *cs, int32_t x, int32_t y)
+{
+    const float x_t = ((float)x * cs->x_inc) + cs->x_m;
+    const float y_t = ((float)y * cs->y_inc) + cs->y_m;
+    const v3 screen = vadd(vadd(vmul(cs->X, x_t), vmul(cs->Y, y_t)), vmul(cs->Z, cs->t));
+    ro_ray r = {cs->c, vnorm(screen)};
+    return r;
+}
+
+void ro_camera_rays(const ro_camera *cam, int32_t x0, int32_t y0, int32_t w, int32_t h,
+                    float *ogn, float *dir)
+{
+    const cam_state cs = cam_setup(cam);
+    size_t k = 0;
+    for (int32_t y = y0; y < y0 + h; ++y)
+        for (int32_t x = x0; x < x0 + w; ++x, ++k) {
+            const ro_ray r = cam_ray(&cs, x, y);
+            ogn[3 * k] = r.o.x; ogn[3 * k + 1] = r.o.y; ogn[3 * k + 2] = r.o.z;
+            dir[3 * k] = r.d.x; dir[3 * k + 1] = r.d.y; dir[3 * k + 2] = r.d.z;
+        }
+}
+
+/* -------------------------------------------------------------- Shading */
+
+/* ray::offset_start_point(+1) (ray.h:111-157): nudge each coordinate by
+ * int(+-32 * n) units in the last place along the geometric normal, or by
+ * 1e-4 * n (from zero) when the coordinate is tiny. */
+static inline float offset_coord(float p, float n)
+{
+    uint32_t x = f2u(p);
+    if ((x & 0x7fffffffu) < f2u(RO_FP_DELTA_SMALL)) return 0.0f + (RO_FP_DELTA_SMALL * n);
+    const float off = ((x >> 31) & 1u) ? -RO_FP_DELTA : RO_FP_DELTA;
+    x += (uint32_t)cvtt((off * n) * 1.0f);
+    return u2f(x);
+}
+
+static inline v3 offset_start(v3 dst, v3 geo)
+{
+    return mk(offset_coord(dst.x, geo.x), offset_coord(dst.y, geo.y), offset_coord(dst.z, geo.z));
+}
+
+/* Light direction sign for directional lights (light.h:172-219): the light
+ * sits at +/-1e15 along n by the sign of n's major component. */
+static float dir_light_dist(v3 n)
+{
+    if (fabsf(n.x) > fabsf(n.y)) {
+        if (fabsf(n.x) > fabsf(n.z)) return (n.x < 0.0f) ? -1.0e15f : 1.0e15f;
+        return (n.z < 0.0f) ? -1.0e15f : 1.0e15f;
+    }
+    if (fabsf(n.y) > fabsf(n.z)) return (n.y < 0.0f) ? -1.0e15f : 1.0e15f;
+    return (n.z < 0.0f) ? -1.0e15f : 1.0e15f;
+}
+
+/* Shadow ray: ray::find_rays (ray.cc:91-104) -> light::find_rays
+ * (light.h:62-100) -> ray::set_up(o, dst) (ray.h:44-54). */
+static inline void shadow_ray(const ro_light *L, v3 start, ro_ray *r, float *len)
+{
+    v3 target;
+    if (L->kind == 1) {
+        const v3 n = ld3(L->dir);
+        target = vadd(start, vmul(n, dir_light_dist(n)));
+    } else {
+        target = ld3(L->pos);
+    }
+    const v3 d = vsub(target, start);
+    *len = vmag(d);
+    r->o = start;
+    r->d = vdivs(d, *len);
+}
+
+typedef struct {
+    const ro_scene *s;
+    const ro_camera *cam;
+    const ro_light *lights;
+    int32_t nlights;
+    const ro_material *mat;
+    int32_t row0, row1;
+    uint8_t *rgb;
+    int32_t *hit_id;
+    uint8_t *occl;
+    float *fimg;
+    int64_t rays;
+    /* AO mode */
+    int32_t ao_n;
+    float ao_dist;
+    uint32_t ao_seed;
+    int32_t *ao_count;
+    int32_t next_row;
+    pthread_mutex_t *lock;
+} render_job;
+
+/* Hit-point refinement + face-forwarding (raytracer.cc:30-31 and
+ * triangle::normal_at_point, triangle.h:464-498), then the interpolated
+ * attribute (triangle.h:74-79). */
+static inline void hit_setup(const ro_scene *s, const ro_ray *r, int32_t id, const ro_hit *h,
+                             v3 *dst, v3 *shader_n, v3 *geo, v3 *vt)
+{
+    v3 p = vadd(r->o, vmul(r->d, h->d));              /* calculate_destination */
+    const v3 n = s->n[id];
+    const float denom = vdot(n, r->d);
+    const float num = vdot(n, vsub(s->vc[id], p));
+    p = vadd(p, vmul(r->d, num / denom));              /* change_length */
+    if (denom > 0.0f) { *shader_n = vneg(n); *geo = vneg(n); }
+    else { *shader_n = n; *geo = n; }
+    *dst = p;
+    if (s->ta) {
+        const float w = 1.0f - (h->u + h->v);
+        *vt = vadd(vadd(vmul(s->tc[id], h->u), vmul(s->tb[id], h->v)), vmul(s->ta[id], w));
+    } else {
+        *vt = mk(RO_MAX_DIST, RO_MAX_DIST, RO_MAX_DIST);
+    }
+}
+
+/* Diffuse colour at the hit: coloured_mapper_shader.cc:61-66 with a texture
+ * mapper that returns the attribute * 255. */
+static inline v3 cur_kd(const ro_scene *s, const ro_material *m, v3 vt)
+{
+    v3 kd = ld3(m->kd);
+    if (s->ta) {
+        const v3 tex = mk(vt.x * 255.0f, vt.y * 255.0f, vt.z * 255.0f);
+        const float k = 1.0f / 255.0f;
+        kd = mk(tex.x * (m->kd[0] * k), tex.y * (m->kd[1] * k), tex.z * (m->kd[2] * k));
+    }
+    return kd;
+}
+
+/* camera::clip_image_to_rgb (camera.h:312-314): clamp then truncate. */
+static inline uint8_t clip8(float v) { return (uint8_t)smin(255.0f, smax(0.0f, v / 1.0f)); }
+
+static void render_pixel(render_job *J, const cam_state *cs, int32_t x, int32_t y)
+{
+    const ro_scene *s = J->s;
+    const ro_material *m = J->mat;
+    const size_t pix = (size_t)x + (size_t)y * (size_t)J->cam->xres;
+    const ro_ray r = cam_ray(cs, x, y);
+    ro_hit h;
+    const int32_t id = closest(s, &r, &h);
+    J->rays += 1;
+    v3 c;
+    if (h.d < RO_MAX_DIST) {
+        v3 dst, sn, geo, vt;
+        hit_setup(s, &r, id, &h, &dst, &sn, &geo, &vt);
+        const v3 start = offset_start(dst, geo);
+        const v3 kd = cur_kd(s, m, vt);
+        const v3 ks = ld3(m->ks);
+        c = mk(0.0f, 0.0f, 0.0f);
+        if (J->ao_n > 0) {
+            /* AO mode: pixel = ka + kd * unoccluded fraction */
+            float dirs[3 * 64], ogns[3 * 64];
+            const float hp[3] = {dst.x, dst.y, dst.z}, gn[3] = {geo.x, geo.y, geo.z};
+            ro_ao_rays(hp, gn, (uint32_t)pix, J->ao_n, J->ao_seed, ogns, dirs);
+            int32_t made_it = 0;
+            for (int32_t k = 0; k < J->ao_n; ++k) {
+                ro_ray ar = {ld3(ogns + 3 * k), ld3(dirs + 3 * k)};
+                if (!nearer(s, &ar, J->ao_dist)) ++made_it;
+            }
+            J->rays += J->ao_n;
+            const float frac = (float)made_it / (float)J->ao_n;
+            c = vadd(vmul(kd, frac), ld3(m->ka));
+            if (J->ao_count) J->ao_count[pix] = made_it;
+        } else {
+            for (int32_t l = 0; l < J->nlights; ++l) {
+                const ro_light *L = &J->lights[l];
+                ro_ray sr;
+                float len;
+                shadow_ray(L, start, &sr, &len);
+                const int occ = nearer(s, &sr, len);
+                J->rays += 1;
+                if (J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
+                const float magn = occ ? 0.0f : 1.0f;   /* made_it / nr_pending_shadows */
+                /* coloured_mapper_shader::shade (coloured_mapper_shader.cc:76-109) */
+                const float shade = vdot(sr.d, sn);
+                if (shade < 0.0f) continue;
+                const v3 ref = vsub(sr.d, vmul(sn, 2.0f * shade));
+                const float rdr = vdot(r.d, ref);
+                v3 sc = mk(shade * kd.x, shade * kd.y, shade * kd.z);
+                if (rdr > 0.0f) {
+                    const float p = (float)pow((double)rdr, (double)m->ns);
+                    sc = mk(sc.x + p * ks.x, sc.y + p * ks.y, sc.z + p * ks.z);
+                }
+                /* light::get_light_intensity (light.h:44-59) */
+                const float dist = len * L->d;
+                const float d_scale = (dist * dist) + 1.0f;
+                const v3 I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale,
+                                (L->rgb[2] / 255.0f) / d_scale);
+                c = mk(c.x + I.x * (sc.x * magn), c.y + I.y * (sc.y * magn), c.z + I.z * (sc.z * magn));
+            }
+            c = vadd(c, ld3(m->ka));
+        }
+    } else {
+        c = ld3(J->cam->background);     /* camera::shade (camera.h:236-239) */
+        if (J->occl) J->occl[pix] = 0;
+        if (J->ao_count) J->ao_count[pix] = 0;
+    }
+    if (J->hit_id) J->hit_id[pix] = id;
+    if (J->fimg) { J->fimg[3 * pix] = c.x; J->fimg[3 * pix + 1] = c.y; J->fimg[3 * pix + 2] = c.z; }
+    J->rgb[3 * pix] = clip8(c.x);
+    J->rgb[3 * pix + 1] = clip8(c.y);
+    J->rgb[3 * pix + 2] = clip8(c.z);
+}
+
+static void *render_worker(void *arg)
+{
+    render_job *J0 = (render_job *)arg;
+    render_job J = *J0;   /* private counters */
+    J.rays = 0;
+    const cam_state cs = cam_setup(J.cam);
+    for (;;) {
+        pthread_mutex_lock(J0->lock);
+        const int32_t y = J0->next_row++;
+        pthread_mutex_unlock(J0->lock);
+        if (y >= J.row1) break;
+        for (int32_t x = 0; x < J.cam->xres; ++x) render_pixel(&J, &cs, x, y);
+    }
+    pthread_mutex_lock(J0->lock);
+    J0->rays += J.rays;
+    pthread_mutex_unlock(J0->lock);
+    return NULL;
+}
+
+static int64_t run_render(render_job *J, int32_t nthreads)
+{
+    pthread_mutex_t lock;
+    pthread_mutex_init(&lock, NULL);
+    J->lock = &lock;
+    J->next_row = J->row0;
+    J->rays = 0;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int i = 1; i < nthreads; ++i)
+        if (pthread_create(&th[started], NULL, render_worker, J) == 0) ++started;
+    render_worker(J);
+    for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+    pthread_mutex_destroy(&lock);
+    return J->rays;
+}
+
+int64_t ro_render(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                  const ro_material *mat, int32_t row0, int32_t row1, int32_t nthreads,
+                  uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg)
+{
+    if (!s || !s->nodes || !cam || !mat || !rgb || row0 < 0 || row1 > cam->yres || row0 > row1) return -1;
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mat;
+    J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id; J.occl = occl; J.fimg = fimg;
+    return run_render(&J, nthreads);
+}
+
+int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material *mat,
+                     int32_t nsamples, float ao_dist, uint32_t seed, int32_t row0, int32_t row1,
+                     int32_t nthreads, uint8_t *rgb, int32_t *hit_id, int32_t *ao_count)
+{
+    if (!s || !s->nodes || !cam || !mat || !rgb || nsamples < 1 || nsamples > 64 || row0 < 0 ||
+        row1 > cam->yres || row0 > row1)
+        return -1;
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.cam = cam; J.mat = mat; J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id;
+    J.ao_n = nsamples; J.ao_dist = ao_dist; J.ao_seed = seed; J.ao_count = ao_count;
+    return run_render(&J, nthreads);
+}
+
+/* ------------------------------------------------------- AO ray sampler */
+
+/* Philox4x32-10 from Salmon, Moraes, Dror and Shaw, "Parallel random numbers:
+ * as easy as 1, 2, 3" (SC'11): ten rounds of two 32x32->64 multiplies with a
+ * Weyl-sequence key schedule. */
+void ro_philox4x32(const uint32_t ctr[4], uint32_t key0, uint32_t key1, uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key0, k1 = key1;
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        const uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* Cosine-weighted hemisphere directions about the geometric normal:
+ * rejection-sampled unit disk (24-bit uniforms, at most 8 tries, else the
+ * normal), lifted to the hemisphere (Malley's method), rotated by the
+ * orthonormal basis of Duff et al., "Building an Orthonormal Basis,
+ * Revisited" (JCGT 2017).  Only IEEE add/mul/div/sqrt, so every host and
+ * the GPU produce the same bits.  Origin = offset_start_point(+1). */
+void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pixel, int32_t nsamples,
+                uint32_t seed, float *ogn, float *dir)
+{
+    const v3 g = ld3(geo_normal);
+    const v3 start = offset_start(ld3(hit_point), g);
+    const float sign = (g.z < 0.0f || (g.z == 0.0f && (f2u(g.z) >> 31))) ? -1.0f : 1.0f;
+    const float a = -1.0f / (sign + g.z);
+    const float b = (g.x * g.y) * a;
+    const v3 T = mk(1.0f + ((sign * (g.x * g.x)) * a), sign * b, -(sign * g.x));
+    const v3 B = mk(b, sign + ((g.y * g.y) * a), -g.y);
+    for (int32_t s = 0; s < nsamples; ++s) {
+        float x = 0.0f, y = 0.0f;
+        int found = 0;
+        for (uint32_t call = 0; call < 4 && !found; ++call) {
+            const uint32_t ctr[4] = {pixel, (uint32_t)s, call, 0x414f5259u};
+            uint32_t rnd[4];
+            ro_philox4x32(ctr, seed, 0x52415054u, rnd);
+            for (int pair = 0; pair < 2 && !found; ++pair) {
+                const float px = ((float)(rnd[2 * pair] >> 8) * 1.1920928955078125e-7f) - 1.0f;
+                const float py = ((float)(rnd[2 * pair + 1] >> 8) * 1.1920928955078125e-7f) - 1.0f;
+                if (((px * px) + (py * py)) < 1.0f) { x = px; y = py; found = 1; }
+            }
+        }
+        const float z = sqrtf(smax(0.0f, 1.0f - ((x * x) + (y * y))));
+        const v3 d = vadd(vadd(vmul(T, x), vmul(B, y)), vmul(g, z));
+        const v3 dn = vnorm(d);
+        ogn[3 * s] = start.x; ogn[3 * s + 1] = start.y; ogn[3 * s + 2] = start.z;
+        dir[3 * s] = dn.x; dir[3 * s + 1] = dn.y; dir[3 * s + 2] = dn.z;
+    }
+}

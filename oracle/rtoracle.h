@@ -1,0 +1,127 @@
+/*
+ * rtoracle.h -- CPU restatement of RAPTor's ray-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker the CUDA core is
+ * compared against: tests, the smoke check and the CPU-baseline leg of the
+ * benchmark may load it; the product library never does.
+ *
+ * Every function restates the reference's scalar CPU path (file:line given
+ * beside each declaration, paths relative to the RAPTor project root).  All
+ * arithmetic is IEEE binary32 in the reference's operation order; the library
+ * is compiled with -ffp-contract=off so x86 and Arm give identical bits.
+ *
+ * The one deliberate difference from the reference: the hierarchy above the
+ * Morton-sorted primitives is a top-down split on the highest differing Morton
+ * bit instead of the reference's approximate agglomerative clustering
+ * (raytracer/spatial_sub_division/bvh_builder.cc:292-642).  The traversal
+ * (bvh.cc:586-759) returns the closest accepted intersection whatever the tree
+ * shape, so hits differ only where two triangles give bit-identical distances
+ * (the reference keeps the first one found).  The tests pin this restatement
+ * hit-for-hit against the reference itself where it can be compiled.
+ */
+#ifndef RTORACLE_H
+#define RTORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Camera as the reference's camera constructor takes it
+ * (raytracer/camera.h:55-62): position, x/y/z axes, background colour,
+ * half-width w, half-height h, image-plane distance t, resolution. */
+typedef struct ro_camera {
+    float pos[3];
+    float x_axis[3], y_axis[3], z_axis[3];
+    float background[3];
+    float w, h, t;
+    int32_t xres, yres;
+} ro_camera;
+
+/* Light (raytracer/light.h:17-34).  kind 0 = point light at pos (the
+ * spherical-light constructor with soft shadows off), kind 1 = directional
+ * light along dir.  rgb is in 0..255 units, d is the distance drop-off. */
+typedef struct ro_light {
+    int32_t kind;
+    float rgb[3];
+    float pos[3];
+    float dir[3];
+    float d;
+} ro_light;
+
+/* Coloured-mapper Phong material (materials/coloured_mapper_shader.h): ka,
+ * kd, ks in 0..255 units, ns the specular exponent.  When the scene carries
+ * per-vertex attributes, kd is modulated by the interpolated attribute
+ * (attribute * 255 sampled, then scaled by kd / 255). */
+typedef struct ro_material {
+    float ka[3], kd[3], ks[3];
+    float ns;
+} ro_material;
+
+typedef struct ro_scene ro_scene;
+
+/* Triangle-flag bits: bit 0 marks a light (ignored by shadow rays,
+ * triangle.h:40), bit 1 a transparent material (bvh_node.h:176). */
+#define RO_TRI_LIGHT       1u
+#define RO_TRI_TRANSPARENT 2u
+
+/* Morton code of a point (common/simd.h:798-825), truncating float->int. */
+int32_t ro_morton_code(float x, float y, float z, float x_mul, float y_mul, float z_mul);
+
+/* Scene from an indexed mesh; vattr (3 floats per vertex) and flags may be
+ * NULL.  Triangle i keeps id i, as primitive_store::indirection does. */
+ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris,
+                          const float *vattr, const uint32_t *flags);
+void ro_scene_destroy(ro_scene *s);
+
+/* Build the 2-wide BVH (Morton + stable LSD radix as bvh_builder.cc:18-158).
+ * Returns build seconds, or a negative value on failure. */
+double ro_scene_build(ro_scene *s);
+int32_t ro_scene_node_count(const ro_scene *s);
+
+/* Closest hit for n rays (bvh.cc:649-709 + triangle.h:190-235).  ogn and dir
+ * hold 3 floats per ray; id is -1 on a miss, t is FLT_MAX on a miss. */
+int32_t ro_trace_closest(const ro_scene *s, const float *ogn, const float *dir, int32_t n,
+                         int32_t *id, float *t, float *u, float *v);
+
+/* Any hit strictly inside (EPSILON, tmax) for n rays (bvh.cc:711-759,
+ * bvh_node.h:170-190). */
+int32_t ro_trace_any(const ro_scene *s, const float *ogn, const float *dir, const float *tmax,
+                     int32_t n, uint8_t *occluded);
+
+/* Primary rays of a pixel window (camera.h:127-140): origin = camera position,
+ * direction normalised with sqrt + divide (EXACT_NORMALISE). */
+void ro_camera_rays(const ro_camera *cam, int32_t x0, int32_t y0, int32_t w, int32_t h,
+                    float *ogn, float *dir);
+
+/* Render rows [row0, row1) of the frame with nthreads threads
+ * (raytracer.cc:20-87 per pixel, then camera.h:289-319 to RGB8).
+ * rgb holds 3 bytes per pixel of the full frame, row y=0 at the bottom as in
+ * the reference; hit_id (nullable) receives the primary hit id per pixel,
+ * occl (nullable) the shadow-ray result per pixel and light (1 = occluded),
+ * fimg (nullable) the unclipped float colour.  Returns rays traced. */
+int64_t ro_render(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                  const ro_material *mat, int32_t row0, int32_t row1, int32_t nthreads,
+                  uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg);
+
+/* Ambient-occlusion render (no reference counterpart: the ray generator is
+ * this project's, restated identically in the CUDA core).  Per primary hit,
+ * nsamples cosine-weighted rays from the offset hit point, any-hit within
+ * ao_dist.  Pixel = ka + kd_colour * unoccluded_fraction.  ao_count (nullable)
+ * receives the unoccluded-ray count per pixel. */
+int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material *mat,
+                     int32_t nsamples, float ao_dist, uint32_t seed, int32_t row0, int32_t row1,
+                     int32_t nthreads, uint8_t *rgb, int32_t *hit_id, int32_t *ao_count);
+
+/* The AO ray set for one hit (exposed so tests can trace single rays). */
+void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pixel, int32_t nsamples,
+                uint32_t seed, float *ogn, float *dir);
+
+/* Philox4x32-10 (Salmon et al., SC'11) keyed by (key0, key1) on counter ctr. */
+void ro_philox4x32(const uint32_t ctr[4], uint32_t key0, uint32_t key1, uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

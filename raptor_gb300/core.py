@@ -1,0 +1,270 @@
+"""Python binding of the core's C ABI (include/rtcore.h) through ctypes.
+
+This is plumbing for tests, the smoke check and the benchmark; the product
+is the shared library.  Loading fails loudly when the library has not been
+built -- there is no CPU fallback.
+
+Bulk arguments may be numpy arrays (host memory) or torch CUDA tensors
+(device memory); the library detects which.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+
+RT_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "not built",
+          -5: "stack overflow", -6: "iteration limit", -7: "no device", -8: "internal error"}
+
+RT_TRI_LIGHT = 1
+RT_TRI_TRANSPARENT = 2
+RT_LIGHT_POINT = 0
+RT_LIGHT_DIRECTIONAL = 1
+RT_MAX_LIGHTS = 8
+RT_OPT_COUNT_FETCHES = 1
+
+
+class RtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"rtcore error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class RtRay(C.Structure):
+    _fields_ = [("ox", C.c_float), ("oy", C.c_float), ("oz", C.c_float), ("tmax", C.c_float),
+                ("dx", C.c_float), ("dy", C.c_float), ("dz", C.c_float), ("pad", C.c_float)]
+
+
+class RtHit(C.Structure):
+    _fields_ = [("tri", C.c_int32), ("t", C.c_float), ("u", C.c_float), ("v", C.c_float)]
+
+
+class RtCamera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("x_axis", C.c_float * 3), ("y_axis", C.c_float * 3),
+                ("z_axis", C.c_float * 3), ("background", C.c_float * 3), ("w", C.c_float), ("h", C.c_float),
+                ("t", C.c_float), ("xres", C.c_int32), ("yres", C.c_int32)]
+
+
+class RtLight(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
+                ("d", C.c_float)]
+
+
+class RtMaterial(C.Structure):
+    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float)]
+
+
+class RtRenderStats(C.Structure):
+    _fields_ = [("primary_rays", C.c_int64), ("secondary_rays", C.c_int64), ("primary_hits", C.c_int64),
+                ("device_ms", C.c_float), ("status", C.c_int32), ("nodes_fetched", C.c_int64),
+                ("tris_tested", C.c_int64)]
+
+
+# numpy views of the C structs
+RAY_DTYPE = np.dtype([("o", np.float32, 3), ("tmax", np.float32), ("d", np.float32, 3), ("pad", np.float32)])
+HIT_DTYPE = np.dtype([("tri", np.int32), ("t", np.float32), ("u", np.float32), ("v", np.float32)])
+
+_lib = None
+
+# (name, restype, argtypes) of every exported entry point, as in rtcore.h
+_P = C.c_void_p
+SIGNATURES = [
+    ("rt_ctx_create", C.c_int32, [C.c_int32, C.POINTER(C.c_void_p)]),
+    ("rt_ctx_destroy", C.c_int32, [_P]),
+    ("rt_ctx_set_stream", C.c_int32, [_P, _P]),
+    ("rt_ctx_synchronize", C.c_int32, [_P]),
+    ("rt_ctx_set_option", C.c_int32, [_P, C.c_int32, C.c_int64]),
+    ("rt_last_error_string", C.c_char_p, []),
+    ("rt_version", C.c_int32, []),
+    ("rt_scene_create", C.c_int32, [_P, C.POINTER(C.c_void_p)]),
+    ("rt_scene_destroy", C.c_int32, [_P]),
+    ("rt_scene_upload", C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, _P, _P]),
+    ("rt_scene_update_vertices", C.c_int32, [_P, _P, C.c_int32]),
+    ("rt_bvh_build", C.c_int32, [_P, C.POINTER(C.c_float)]),
+    ("rt_bvh_info", C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("rt_trace_closest", C.c_int32, [_P, _P, C.c_int32, _P]),
+    ("rt_trace_any", C.c_int32, [_P, _P, C.c_int32, _P]),
+    ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
+                              C.POINTER(RtRenderStats)]),
+    ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
+                                 _P, _P, _P, C.POINTER(RtRenderStats)]),
+]
+
+
+def lib():
+    """Load librtcore.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"{LIB} is missing: run raptor_gb300.build.build() (there is no CPU fallback)")
+        h = C.CDLL(LIB)
+        for name, res, args in SIGNATURES:
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = h
+    return _lib
+
+
+def _check(rc):
+    if rc != RT_OK:
+        raise RtError(rc, lib().rt_last_error_string().decode())
+
+
+def ptr(a):
+    """Address of a numpy array or torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(a.ctypes.data)
+    raise TypeError(f"unsupported buffer type {type(a)}")
+
+
+def make_camera(d) -> RtCamera:
+    c = RtCamera()
+    for k in ("pos", "x_axis", "y_axis", "z_axis", "background"):
+        getattr(c, k)[:] = [float(x) for x in d[k]]
+    c.w, c.h, c.t, c.xres, c.yres = d["w"], d["h"], d["t"], d["xres"], d["yres"]
+    return c
+
+
+def make_lights(ls):
+    arr = (RtLight * max(1, len(ls)))()
+    for i, d in enumerate(ls):
+        arr[i].kind = d["kind"]
+        arr[i].rgb[:] = list(d["rgb"])
+        arr[i].pos[:] = list(d["pos"])
+        arr[i].dir[:] = list(d["dir"])
+        arr[i].d = d["d"]
+    return arr
+
+
+def make_material(d) -> RtMaterial:
+    m = RtMaterial()
+    m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
+    m.ns = d["ns"]
+    return m
+
+
+def rays_array(ogn, dirs, tmax=None):
+    n = ogn.shape[0]
+    r = np.zeros(n, RAY_DTYPE)
+    r["o"] = ogn
+    r["d"] = dirs
+    r["tmax"] = np.float32(3.4028234663852886e38) if tmax is None else tmax
+    return r
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().rt_ctx_create(device, C.byref(h)))
+        self.h = h
+
+    def set_stream(self, stream_handle):
+        _check(lib().rt_ctx_set_stream(self.h, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def synchronize(self):
+        _check(lib().rt_ctx_synchronize(self.h))
+
+    def set_option(self, option: int, value: int):
+        _check(lib().rt_ctx_set_option(self.h, option, value))
+
+    def close(self):
+        if self.h:
+            lib().rt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    def __init__(self, ctx: Context, scene=None, build: bool = True):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(lib().rt_scene_create(ctx.h, C.byref(h)))
+        self.h = h
+        self.build_ms = None
+        if scene is not None:
+            self.upload(scene["verts"], scene["tris"], scene.get("vattr"), scene.get("flags"))
+            if build:
+                self.build()
+
+    def upload(self, verts, tris, vattr=None, flags=None):
+        nv = int(verts.shape[0])
+        nt = int(tris.shape[0])
+        self._keep = (verts, tris, vattr, flags)
+        _check(lib().rt_scene_upload(self.h, ptr(verts), nv, ptr(tris), nt, ptr(vattr), ptr(flags)))
+        self.nverts, self.ntris = nv, nt
+
+    def update_vertices(self, verts):
+        _check(lib().rt_scene_update_vertices(self.h, ptr(verts), int(verts.shape[0])))
+
+    def build(self) -> float:
+        ms = C.c_float()
+        _check(lib().rt_bvh_build(self.h, C.byref(ms)))
+        self.build_ms = ms.value
+        return ms.value
+
+    def info(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().rt_bvh_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"nodes": a.value, "tri_slots": b.value, "depth": c.value}
+
+    def closest(self, rays):
+        n = int(rays.shape[0])
+        out = np.empty(n, HIT_DTYPE)
+        _check(lib().rt_trace_closest(self.h, ptr(rays), n, ptr(out)))
+        return out
+
+    def closest_into(self, rays, out):
+        _check(lib().rt_trace_closest(self.h, ptr(rays), int(rays.shape[0]), ptr(out)))
+
+    def any(self, rays):
+        n = int(rays.shape[0])
+        out = np.empty(n, np.uint8)
+        _check(lib().rt_trace_any(self.h, ptr(rays), n, ptr(out)))
+        return out
+
+    def render(self, frame, rgb=None, ids=None, want_ids=False):
+        cam = make_camera(frame["camera"])
+        W, H = cam.xres, cam.yres
+        if rgb is None:
+            rgb = np.empty((H, W, 3), np.uint8)
+        if ids is None and want_ids:
+            ids = np.empty((H, W), np.int32)
+        st = RtRenderStats()
+        mat = make_material(frame["material"])
+        ao = frame.get("ao")
+        if ao:
+            cnt = np.empty((H, W), np.int32) if want_ids else None
+            _check(lib().rt_render_ao(self.h, C.byref(cam), C.byref(mat), ao["samples"], ao["dist"], ao["seed"],
+                                      ptr(rgb), ptr(ids), ptr(cnt), C.byref(st)))
+            return {"rgb": rgb, "ids": ids, "ao_count": cnt, "stats": st}
+        ls = make_lights(frame["lights"])
+        _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
+                               C.byref(st)))
+        return {"rgb": rgb, "ids": ids, "stats": st}
+
+    def close(self):
+        if self.h:
+            lib().rt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,590 @@
+// rt_api.cu -- the C ABI (include/rtcore.h): contexts, scenes, staging of
+// host buffers, and launch of the build / trace / render kernels.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "rt_build.cuh"
+#include "rt_kernels.cuh"
+#include "rt_api_internal.cuh"
+
+using namespace rtc;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+rt_status fail(rt_status code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+rt_status cuda_fail(cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? RT_ERR_OUT_OF_MEMORY : RT_ERR_CUDA, m);
+}
+
+#define RT_CUDA(call, what)                          \
+    do {                                             \
+        cudaError_t _e = (call);                     \
+        if (_e != cudaSuccess) return cuda_fail(_e, what); \
+    } while (0)
+
+// Make the context's device current for the duration of a call.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+namespace rtc {
+
+bool is_device_ptr(const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+cudaError_t DevBuf::reserve(size_t bytes)
+{
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    const size_t want = bytes + bytes / 4 + 256;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+}
+
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+CameraView make_camera_view(const rt_camera &c)
+{
+    // base_camera axes pass through the identity quaternion rotation
+    // (sdl_wrappers/base_camera.h, common/quaternion_t.h:166-169); restated
+    // literally so the signs of zero components match the reference.
+    const auto rot = [](const float *p) {
+        const float qw = 1.0f, qx = 0.0f, qy = 0.0f, qz = 0.0f;
+        const float c1x = (qy * p[2]) - (qz * p[1]), c1y = (qz * p[0]) - (qx * p[2]), c1z = (qx * p[1]) - (qy * p[0]);
+        const float c2x = (qy * c1z) - (qz * c1y), c2y = (qz * c1x) - (qx * c1z), c2z = (qx * c1y) - (qy * c1x);
+        const float w2 = 2.0f * qw;
+        return make_float3((p[0] + (2.0f * c2x)) + (w2 * c1x), (p[1] + (2.0f * c2y)) + (w2 * c1y),
+                           (p[2] + (2.0f * c2z)) + (w2 * c1z));
+    };
+    CameraView v;
+    v.c = make_float3(c.pos[0], c.pos[1], c.pos[2]);
+    v.X = rot(c.x_axis);
+    v.Y = rot(c.y_axis);
+    v.Z = rot(c.z_axis);
+    v.x_m = -c.w;
+    v.y_m = -c.h;
+    v.x_inc = (c.w * 2.0f) / (float)c.xres;   // camera.h:60
+    v.y_inc = (c.h * 2.0f) / (float)c.yres;
+    v.t = c.t;
+    v.xres = c.xres;
+    v.yres = c.yres;
+    v.background = make_float3(c.background[0], c.background[1], c.background[2]);
+    return v;
+}
+
+LightView make_light_view(const rt_light &l)
+{
+    LightView v;
+    v.kind = l.kind;
+    v.rgb255 = make_float3(l.rgb[0] / 255.0f, l.rgb[1] / 255.0f, l.rgb[2] / 255.0f);   // light.h:17-34
+    v.pos = make_float3(l.pos[0], l.pos[1], l.pos[2]);
+    v.dir = make_float3(l.dir[0], l.dir[1], l.dir[2]);
+    v.d = l.d;
+    // light::find_major_direction (light.h:172-219)
+    const float nx = l.dir[0], ny = l.dir[1], nz = l.dir[2];
+    bool neg;
+    if (std::fabs(nx) > std::fabs(ny)) neg = (std::fabs(nx) > std::fabs(nz)) ? (nx < 0.0f) : (nz < 0.0f);
+    else neg = (std::fabs(ny) > std::fabs(nz)) ? (ny < 0.0f) : (nz < 0.0f);
+    v.dist_sign = neg ? -1.0e15f : 1.0e15f;
+    return v;
+}
+
+MaterialView make_material_view(const rt_material &m)
+{
+    MaterialView v;
+    v.ka = make_float3(m.ka[0], m.ka[1], m.ka[2]);
+    v.kd = make_float3(m.kd[0], m.kd[1], m.kd[2]);
+    v.ks = make_float3(m.ks[0], m.ks[1], m.ks[2]);
+    v.ns = m.ns;
+    return v;
+}
+
+SceneView scene_view(const rt_scene *s)
+{
+    SceneView v;
+    v.nodes = s->d_nodes;
+    v.tris = s->d_tris;
+    v.shade = s->d_shade;
+    v.idx = s->d_idx;
+    v.vattr = s->d_vattr;
+    v.flags = s->d_flags;
+    v.ntris = s->ntris;
+    v.nnodes = s->built ? s->nnodes : 0;
+    return v;
+}
+
+rt_status set_error(rt_status code, const char *msg) { return fail(code, msg); }
+rt_status set_cuda_error(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+
+// Copy n bytes of a caller buffer (host or device) into a device buffer.
+rt_status stage_in(rt_context *ctx, DevBuf &buf, const void *src, size_t bytes, const void **dev)
+{
+    if (is_device_ptr(src)) {
+        *dev = src;
+        return RT_OK;
+    }
+    RT_CUDA(buf.reserve(bytes), "staging allocation");
+    RT_CUDA(cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "host-to-device copy");
+    *dev = buf.ptr;
+    return RT_OK;
+}
+
+rt_status read_counters(rt_context *ctx, Counters *out)
+{
+    RT_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream),
+            "counter readback");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    *out = *ctx->h_counters;
+    return RT_OK;
+}
+
+rt_status status_to_error(uint32_t st)
+{
+    if (st & kStatusStackOverflow) return fail(RT_ERR_STACK_OVERFLOW, "traversal stack overflow");
+    if (st & kStatusStepLimit) return fail(RT_ERR_LIMIT, "traversal step limit reached");
+    if (st & kStatusBadIndex) return fail(RT_ERR_INTERNAL, "traversal met an index outside the scene");
+    return RT_OK;
+}
+
+}  // namespace rtc
+
+// =================================================================== C ABI
+
+extern "C" {
+
+const char *rt_last_error_string(void) { return g_last_error.c_str(); }
+
+int32_t rt_version(void) { return 100; }
+
+rt_status rt_ctx_create(int32_t device, rt_context **out)
+{
+    if (!out) return fail(RT_ERR_INVALID_ARG, "rt_ctx_create: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(RT_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= ndev) return fail(RT_ERR_INVALID_ARG, "rt_ctx_create: device index out of range");
+    DeviceGuard g(device);
+    if (!g.ok) return fail(RT_ERR_CUDA, "cudaSetDevice failed");
+    rt_context *c = new (std::nothrow) rt_context();
+    if (!c) return fail(RT_ERR_OUT_OF_MEMORY, "context allocation");
+    c->device = device;
+    cudaDeviceProp prop;
+    RT_CUDA(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    c->sm_count = prop.multiProcessorCount;
+    RT_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "stream create");
+    c->stream = c->own_stream;
+    RT_CUDA(cudaMalloc(&c->d_counters, sizeof(Counters)), "counter allocation");
+    RT_CUDA(cudaMallocHost(&c->h_counters, sizeof(Counters)), "pinned counter allocation");
+    RT_CUDA(cudaMallocHost(&c->h_scratch, 64 * sizeof(int32_t)), "pinned scratch allocation");
+    RT_CUDA(cudaEventCreate(&c->ev0), "event create");
+    RT_CUDA(cudaEventCreate(&c->ev1), "event create");
+    *out = c;
+    return RT_OK;
+}
+
+rt_status rt_ctx_destroy(rt_context *ctx)
+{
+    if (!ctx) return RT_OK;
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->stage_a.release();
+    ctx->stage_b.release();
+    ctx->stage_c.release();
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->h_scratch) cudaFreeHost(ctx->h_scratch);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_stream(rt_context *ctx, void *stream)
+{
+    if (!ctx) return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_stream: NULL context");
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
+{
+    if (!ctx) return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: NULL context");
+    if (option == RT_OPT_COUNT_FETCHES) {
+        ctx->count_fetches = value != 0;
+        return RT_OK;
+    }
+    return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown option");
+}
+
+rt_status rt_ctx_synchronize(rt_context *ctx)
+{
+    if (!ctx) return fail(RT_ERR_INVALID_ARG, "rt_ctx_synchronize: NULL context");
+    DeviceGuard g(ctx->device);
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    return RT_OK;
+}
+
+rt_status rt_scene_create(rt_context *ctx, rt_scene **out)
+{
+    if (!ctx || !out) return fail(RT_ERR_INVALID_ARG, "rt_scene_create: NULL argument");
+    rt_scene *s = new (std::nothrow) rt_scene();
+    if (!s) return fail(RT_ERR_OUT_OF_MEMORY, "scene allocation");
+    s->ctx = ctx;
+    *out = s;
+    return RT_OK;
+}
+
+static void scene_free_geometry(rt_scene *s)
+{
+    cudaFree(s->d_verts); s->d_verts = nullptr;
+    cudaFree(s->d_idx); s->d_idx = nullptr;
+    cudaFree(s->d_vattr); s->d_vattr = nullptr;
+    cudaFree(s->d_flags); s->d_flags = nullptr;
+    cudaFree(s->d_shade); s->d_shade = nullptr;
+    cudaFree(s->d_nodes); s->d_nodes = nullptr;
+    cudaFree(s->d_tris); s->d_tris = nullptr;
+    s->temp.release();
+    s->built = false;
+    s->nnodes = s->tri_slots = s->depth = 0;
+}
+
+rt_status rt_scene_destroy(rt_scene *s)
+{
+    if (!s) return RT_OK;
+    DeviceGuard g(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    scene_free_geometry(s);
+    delete s;
+    return RT_OK;
+}
+
+rt_status rt_scene_upload(rt_scene *s, const float *verts, int32_t nverts, const int32_t *tri_idx, int32_t ntris,
+                          const float *vattr, const uint32_t *flags)
+{
+    if (!s) return fail(RT_ERR_INVALID_ARG, "rt_scene_upload: NULL scene");
+    if (nverts < 0 || ntris < 0) return fail(RT_ERR_INVALID_ARG, "rt_scene_upload: negative count");
+    if ((nverts > 0 && !verts) || (ntris > 0 && !tri_idx)) return fail(RT_ERR_INVALID_ARG, "rt_scene_upload: NULL data");
+    if (ntris > (1 << 28)) return fail(RT_ERR_INVALID_ARG, "rt_scene_upload: more than 2^28 triangles");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    // validate indices on the host when the index buffer is host memory
+    const bool idx_dev = is_device_ptr(tri_idx);
+    if (!idx_dev) {
+        for (int64_t i = 0; i < 3ll * ntris; ++i)
+            if (tri_idx[i] < 0 || tri_idx[i] >= nverts)
+                return fail(RT_ERR_INVALID_ARG, "rt_scene_upload: vertex index out of range");
+    }
+    scene_free_geometry(s);
+    s->nverts = nverts;
+    s->ntris = ntris;
+    const size_t nv = (size_t)(nverts > 0 ? nverts : 1), nt = (size_t)(ntris > 0 ? ntris : 1);
+    RT_CUDA(cudaMalloc(&s->d_verts, nv * 3 * sizeof(float)), "vertex allocation");
+    RT_CUDA(cudaMalloc(&s->d_idx, nt * sizeof(int3)), "index allocation");
+    RT_CUDA(cudaMalloc(&s->d_flags, nt * sizeof(uint32_t)), "flag allocation");
+    RT_CUDA(cudaMalloc(&s->d_shade, nt * sizeof(ShadeTri)), "shade allocation");
+    if (nverts > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_verts, verts, (size_t)nverts * 3 * sizeof(float), cudaMemcpyDefault, ctx->stream),
+                "vertex copy");
+    if (ntris > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_idx, tri_idx, (size_t)ntris * sizeof(int3), cudaMemcpyDefault, ctx->stream),
+                "index copy");
+    if (vattr) {
+        RT_CUDA(cudaMalloc(&s->d_vattr, nv * 3 * sizeof(float)), "attribute allocation");
+        if (nverts > 0)
+            RT_CUDA(cudaMemcpyAsync(s->d_vattr, vattr, (size_t)nverts * 3 * sizeof(float), cudaMemcpyDefault,
+                                    ctx->stream), "attribute copy");
+    }
+    if (flags && ntris > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_flags, flags, (size_t)ntris * sizeof(uint32_t), cudaMemcpyDefault, ctx->stream),
+                "flag copy");
+    else
+        RT_CUDA(cudaMemsetAsync(s->d_flags, 0, nt * sizeof(uint32_t), ctx->stream), "flag clear");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "upload synchronize");
+    return RT_OK;
+}
+
+rt_status rt_scene_update_vertices(rt_scene *s, const float *verts, int32_t nverts)
+{
+    if (!s || !verts) return fail(RT_ERR_INVALID_ARG, "rt_scene_update_vertices: NULL argument");
+    if (nverts != s->nverts) return fail(RT_ERR_INVALID_ARG, "rt_scene_update_vertices: vertex count changed");
+    DeviceGuard g(s->ctx->device);
+    if (nverts > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_verts, verts, (size_t)nverts * 3 * sizeof(float), cudaMemcpyDefault,
+                                s->ctx->stream), "vertex copy");
+    s->built = false;
+    return rt_bvh_build(s, nullptr);
+}
+
+rt_status rt_bvh_build(rt_scene *s, float *build_ms)
+{
+    if (!s) return fail(RT_ERR_INVALID_ARG, "rt_bvh_build: NULL scene");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    s->built = false;
+    if (build_ms) *build_ms = 0.f;
+    if (s->ntris == 0) {
+        s->built = true;
+        s->nnodes = s->tri_slots = s->depth = 0;
+        return RT_OK;
+    }
+    const size_t nt = (size_t)s->ntris;
+    if (!s->d_nodes) RT_CUDA(cudaMalloc(&s->d_nodes, (nt + 1) * sizeof(WideNode)), "node allocation");
+    if (!s->d_tris) RT_CUDA(cudaMalloc(&s->d_tris, nt * sizeof(PackedTri)), "triangle allocation");
+    const size_t tb = build_temp_bytes(s->ntris);
+    RT_CUDA(s->temp.reserve(tb), "build scratch allocation");
+    BuildInputs in;
+    in.ntris = s->ntris;
+    in.verts = s->d_verts;
+    in.idx = s->d_idx;
+    in.flags = s->d_flags;
+    in.shade = s->d_shade;
+    in.nodes = s->d_nodes;
+    in.tris = s->d_tris;
+    in.max_nodes = s->ntris + 1;
+    in.sm_count = ctx->sm_count;
+    in.host_scratch = ctx->h_scratch;
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    const BuildResult R = build_wide_bvh(in, s->temp.ptr, s->temp.cap, ctx->stream);
+    if (R.status != 0) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "bvh build");
+        if (R.status == RT_ERR_STACK_OVERFLOW) return fail(RT_ERR_STACK_OVERFLOW, "bvh build: tree deeper than the traversal stack");
+        return fail(R.status, "bvh build failed");
+    }
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    RT_CUDA(cudaEventSynchronize(ctx->ev1), "event synchronize");
+    RT_CUDA(cudaGetLastError(), "bvh build kernels");
+    if (build_ms) cudaEventElapsedTime(build_ms, ctx->ev0, ctx->ev1);
+    if (R.tri_slots != s->ntris) return fail(RT_ERR_INTERNAL, "bvh build: triangle count mismatch");
+    s->nnodes = R.nodes;
+    s->tri_slots = R.tri_slots;
+    s->depth = R.depth;
+    s->built = true;
+    return RT_OK;
+}
+
+rt_status rt_bvh_info(const rt_scene *s, int32_t *nodes, int32_t *tri_slots, int32_t *depth)
+{
+    if (!s) return fail(RT_ERR_INVALID_ARG, "rt_bvh_info: NULL scene");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_info: hierarchy not built");
+    if (nodes) *nodes = s->nnodes;
+    if (tri_slots) *tri_slots = s->tri_slots;
+    if (depth) *depth = s->depth;
+    return RT_OK;
+}
+
+}  // extern "C"
+
+template <bool ANY>
+static rt_status trace_common(rt_scene *s, const rt_ray *rays, int32_t n, void *out, const char *name)
+{
+    if (!s || (n > 0 && (!rays || !out))) return fail(RT_ERR_INVALID_ARG, std::string(name) + ": NULL argument");
+    if (n < 0) return fail(RT_ERR_INVALID_ARG, std::string(name) + ": negative ray count");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, std::string(name) + ": hierarchy not built");
+    if (n == 0) return RT_OK;
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const void *d_rays = nullptr;
+    rt_status st = stage_in(ctx, ctx->stage_a, rays, (size_t)n * sizeof(rt_ray), &d_rays);
+    if (st != RT_OK) return st;
+    const size_t out_bytes = ANY ? (size_t)n : (size_t)n * sizeof(rt_hit);
+    const bool out_dev = is_device_ptr(out);
+    void *d_out = out;
+    if (!out_dev) {
+        RT_CUDA(ctx->stage_b.reserve(out_bytes), "staging allocation");
+        d_out = ctx->stage_b.ptr;
+    }
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    const SceneView sv = scene_view(s);
+    if (ANY)
+        launch_trace_any(sv, (const rt_ray *)d_rays, n, (uint8_t *)d_out, ctx->d_counters, ctx->sm_count, ctx->stream);
+    else
+        launch_trace_closest(sv, (const rt_ray *)d_rays, n, (rt_hit *)d_out, ctx->d_counters, ctx->sm_count,
+                             ctx->stream);
+    RT_CUDA(cudaGetLastError(), "trace launch");
+    if (!out_dev)
+        RT_CUDA(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream), "device-to-host copy");
+    Counters c;
+    st = read_counters(ctx, &c);
+    if (st != RT_OK) return st;
+    return status_to_error(c.status);
+}
+
+extern "C" {
+
+rt_status rt_trace_closest(rt_scene *s, const rt_ray *rays, int32_t n, rt_hit *hits)
+{
+    return trace_common<false>(s, rays, n, hits, "rt_trace_closest");
+}
+
+rt_status rt_trace_any(rt_scene *s, const rt_ray *rays, int32_t n, uint8_t *occluded)
+{
+    return trace_common<true>(s, rays, n, occluded, "rt_trace_any");
+}
+
+static rt_status check_camera(const rt_camera *cam)
+{
+    if (!cam) return fail(RT_ERR_INVALID_ARG, "NULL camera");
+    if (cam->xres <= 0 || cam->yres <= 0 || (int64_t)cam->xres * cam->yres > (int64_t)1 << 28)
+        return fail(RT_ERR_INVALID_ARG, "camera resolution out of range");
+    return RT_OK;
+}
+
+// Output staging shared by the two render calls.
+struct RenderOut {
+    uint8_t *rgb = nullptr;
+    int32_t *ids = nullptr;
+    int32_t *aux = nullptr;
+    bool rgb_host = false, ids_host = false, aux_host = false;
+};
+
+static rt_status prepare_outputs(rt_context *ctx, size_t npix, uint8_t *rgb, int32_t *ids, int32_t *aux, RenderOut &o)
+{
+    o.rgb_host = !is_device_ptr(rgb);
+    o.ids_host = ids && !is_device_ptr(ids);
+    o.aux_host = aux && !is_device_ptr(aux);
+    if (o.rgb_host) {
+        RT_CUDA(ctx->stage_a.reserve(npix * 3), "staging allocation");
+        o.rgb = (uint8_t *)ctx->stage_a.ptr;
+    } else {
+        o.rgb = rgb;
+    }
+    if (o.ids_host) {
+        RT_CUDA(ctx->stage_b.reserve(npix * 4), "staging allocation");
+        o.ids = (int32_t *)ctx->stage_b.ptr;
+    } else {
+        o.ids = ids;
+    }
+    if (o.aux_host) {
+        RT_CUDA(ctx->stage_c.reserve(npix * 4), "staging allocation");
+        o.aux = (int32_t *)ctx->stage_c.ptr;
+    } else {
+        o.aux = aux;
+    }
+    return RT_OK;
+}
+
+static rt_status finish_outputs(rt_context *ctx, size_t npix, uint8_t *rgb, int32_t *ids, int32_t *aux,
+                                const RenderOut &o, rt_render_stats *stats)
+{
+    if (o.rgb_host) RT_CUDA(cudaMemcpyAsync(rgb, o.rgb, npix * 3, cudaMemcpyDeviceToHost, ctx->stream), "rgb copy");
+    if (o.ids_host) RT_CUDA(cudaMemcpyAsync(ids, o.ids, npix * 4, cudaMemcpyDeviceToHost, ctx->stream), "id copy");
+    if (o.aux_host) RT_CUDA(cudaMemcpyAsync(aux, o.aux, npix * 4, cudaMemcpyDeviceToHost, ctx->stream), "aux copy");
+    Counters c;
+    rt_status st = read_counters(ctx, &c);
+    if (st != RT_OK) return st;
+    if (stats) {
+        stats->primary_rays = (int64_t)c.primary;
+        stats->secondary_rays = (int64_t)c.secondary;
+        stats->primary_hits = (int64_t)c.hits;
+        stats->status = (int32_t)c.status;
+        stats->nodes_fetched = (int64_t)c.nodes;
+        stats->tris_tested = (int64_t)c.tris;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->device_ms = ms;
+    }
+    return status_to_error(c.status);
+}
+
+rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                    const rt_material *material, uint8_t *rgb_out, int32_t *hit_ids, rt_render_stats *stats)
+{
+    if (!s || !material || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
+        return fail(RT_ERR_INVALID_ARG, "rt_render: light count out of range");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render: hierarchy not built");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o);
+    if (st != RT_OK) return st;
+    LightSet ls;
+    ls.n = nlights;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
+                  ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
+}
+
+rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *material, int32_t samples,
+                       float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
+                       rt_render_stats *stats)
+{
+    if (!s || !material || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (samples < 1 || samples > 64) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: samples must be 1..64");
+    if (!(ao_dist > 0.0f)) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: ao_dist must be positive");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_ao: hierarchy not built");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, hit_ids, ao_count, o);
+    if (st != RT_OK) return st;
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render_ao(scene_view(s), make_camera_view(*camera), make_material_view(*material), samples, ao_dist, seed,
+                     o.rgb, o.ids, o.aux, ctx->d_counters, ctx->sm_count, ctx->stream,
+                     ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, hit_ids, ao_count, o, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+// rt_api_internal.cuh -- host-side objects behind the C ABI handles.
+#pragma once
+
+#include <cmath>
+#include <string>
+
+#include "rt_internal.cuh"
+#include "rt_kernels.cuh"
+
+namespace rtc {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t bytes);
+    void release();
+};
+
+bool is_device_ptr(const void *p);
+CameraView make_camera_view(const rt_camera &c);
+LightView make_light_view(const rt_light &l);
+MaterialView make_material_view(const rt_material &m);
+rt_status set_error(rt_status code, const char *msg);
+rt_status set_cuda_error(cudaError_t e, const char *what);
+rt_status status_to_error(uint32_t st);
+
+}  // namespace rtc
+
+struct rt_context {
+    int device = 0;
+    int sm_count = 1;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    rtc::Counters *d_counters = nullptr;
+    rtc::Counters *h_counters = nullptr;   // pinned
+    int32_t *h_scratch = nullptr;          // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    rtc::DevBuf stage_a, stage_b, stage_c;
+    bool count_fetches = false;
+};
+
+struct rt_scene {
+    rt_context *ctx = nullptr;
+    int32_t nverts = 0, ntris = 0;
+    float *d_verts = nullptr;
+    int3 *d_idx = nullptr;
+    float *d_vattr = nullptr;
+    uint32_t *d_flags = nullptr;
+    rtc::ShadeTri *d_shade = nullptr;
+    rtc::WideNode *d_nodes = nullptr;
+    rtc::PackedTri *d_tris = nullptr;
+    int32_t nnodes = 0, tri_slots = 0, depth = 0;
+    bool built = false;
+    rtc::DevBuf temp;
+};
+
+namespace rtc {
+SceneView scene_view(const rt_scene *s);
+}

@@ -1,0 +1,502 @@
+// rt_build.cu -- GPU acceleration-structure build for the GB300 ray-tracing
+// core: Morton codes -> radix sort -> binary LBVH (Karras, HPG 2012) ->
+// bottom-up refit -> surface-area-guided collapse into 8-wide nodes with
+// 8-bit quantised child boxes (layout after Ylitie, Karras & Laine, HPG
+// 2017), conservatively rounded outwards so that no hit is ever lost.
+//
+// Replaces bvh_builder::build (raytracer/spatial_sub_division/
+// bvh_builder.cc:18-178).  The reference builds a 2-wide tree with Morton
+// codes + approximate agglomerative clustering on the CPU; hits do not
+// depend on the tree, so a different tree gives the same closest hits.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "rt_build.cuh"
+
+namespace rtc {
+
+namespace {
+
+__device__ __forceinline__ int ord_of(float f)
+{
+    const int i = __float_as_int(f);
+    return (i >= 0) ? i : (i ^ 0x7fffffff);
+}
+__device__ __forceinline__ float of_ord(int i) { return __int_as_float((i >= 0) ? i : (i ^ 0x7fffffff)); }
+
+// Per triangle (caller's order): shading record (face normal exactly as
+// triangle.h:171-175, vertex c), bounding box, centroid bounds.
+__global__ void k_prep(const float *__restrict__ verts, const int3 *__restrict__ idx, int32_t n,
+                       ShadeTri *__restrict__ shade, float4 *__restrict__ blo, float4 *__restrict__ bhi,
+                       int *__restrict__ cbounds)
+{
+    __shared__ int s_min[3][32], s_max[3][32];
+    float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int3 t = idx[i];
+        const float3 a = make_float3(verts[3 * t.x], verts[3 * t.x + 1], verts[3 * t.x + 2]);
+        const float3 b = make_float3(verts[3 * t.y], verts[3 * t.y + 1], verts[3 * t.y + 2]);
+        const float3 c = make_float3(verts[3 * t.z], verts[3 * t.z + 1], verts[3 * t.z + 2]);
+        const float3 nn = xnorm(xcross(xsub3(b, a), xsub3(c, a)));
+        ShadeTri st;
+        st.n_cx = make_float4(nn.x, nn.y, nn.z, c.x);
+        st.c_yz = make_float2(c.y, c.z);
+        st.pad = make_float2(0.f, 0.f);
+        shade[i] = st;
+        const float3 lo = make_float3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+        const float3 hi = make_float3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+        blo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+        bhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+        const float cc[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { cmin[k] = fminf(cmin[k], cc[k]); cmax[k] = fmaxf(cmax[k], cc[k]); }
+    }
+    // warp then block reduction of the centroid bounds
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            cmin[k] = fminf(cmin[k], __shfl_xor_sync(0xffffffffu, cmin[k], o));
+            cmax[k] = fmaxf(cmax[k], __shfl_xor_sync(0xffffffffu, cmax[k], o));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { s_min[k][warp] = ord_of(cmin[k]); s_max[k][warp] = ord_of(cmax[k]); }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        int mn = s_min[k][0], mx = s_max[k][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { mn = min(mn, s_min[k][w]); mx = max(mx, s_max[k][w]); }
+        atomicMin(&cbounds[k], mn);
+        atomicMax(&cbounds[3 + k], mx);
+    }
+}
+
+__device__ __forceinline__ uint64_t expand21(uint32_t v)
+{
+    uint64_t x = v & 0x1fffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+// 63-bit Morton code (21 bits per axis) of each box centre over the
+// centroid bounds; the sort breaks equal codes by triangle index.
+__global__ void k_morton(const float4 *__restrict__ blo, const float4 *__restrict__ bhi, int32_t n,
+                         const int *__restrict__ cbounds, uint64_t *__restrict__ keys, int32_t *__restrict__ vals)
+{
+    float lo[3], sc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = of_ord(cbounds[k]);
+        const float ext = of_ord(cbounds[3 + k]) - lo[k];
+        sc[k] = (ext > 0.f) ? 2097151.0f / ext : 0.f;
+    }
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = blo[i], b = bhi[i];
+        const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+        uint32_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float f = fminf(fmaxf((c[k] - lo[k]) * sc[k], 0.f), 2097151.0f);
+            q[k] = (uint32_t)f;
+        }
+        keys[i] = expand21(q[0]) | (expand21(q[1]) << 1) | (expand21(q[2]) << 2);
+        vals[i] = i;
+    }
+}
+
+// Common-prefix length of sorted keys i and j, index-extended for equal keys.
+__device__ __forceinline__ int delta(const uint64_t *__restrict__ keys, int32_t n, int32_t i, int32_t j)
+{
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = keys[i], b = keys[j];
+    if (a != b) return __clzll((long long)(a ^ b));
+    return 64 + __clz((int)((uint32_t)i ^ (uint32_t)j));
+}
+
+// Binary radix tree over the sorted keys (Karras 2012, section 4).
+// Child refs: >= 0 internal node, < 0 leaf ~k (sorted position k).
+__global__ void k_karras(const uint64_t *__restrict__ keys, int32_t n, int32_t *__restrict__ left,
+                         int32_t *__restrict__ right, int32_t *__restrict__ first, int32_t *__restrict__ last,
+                         int32_t *__restrict__ parent, int32_t *__restrict__ leaf_parent)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int32_t lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int32_t l = 0;
+    for (int32_t t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int32_t j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int32_t s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int32_t gamma = i + s * d + min(d, 0);
+    const int32_t lo = min(i, j), hi = max(i, j);
+    const int32_t lref = (lo == gamma) ? ~gamma : gamma;
+    const int32_t rref = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    left[i] = lref;
+    right[i] = rref;
+    first[i] = lo;
+    last[i] = hi;
+    if (lref < 0) leaf_parent[~lref] = i; else parent[lref] = i;
+    if (rref < 0) leaf_parent[~rref] = i; else parent[rref] = i;
+    if (i == 0) parent[0] = -1;
+}
+
+// Leaf boxes in sorted order.
+__global__ void k_leaf_boxes(const int32_t *__restrict__ vals, int32_t n, const float4 *__restrict__ blo,
+                             const float4 *__restrict__ bhi, float4 *__restrict__ llo, float4 *__restrict__ lhi)
+{
+    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int32_t t = vals[k];
+    llo[k] = blo[t];
+    lhi[k] = bhi[t];
+}
+
+// Bottom-up box refit: the second child to arrive at a node unions both.
+__global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
+                        const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
+                        const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
+                        int32_t *flags)
+{
+    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int32_t p = leaf_parent[k];
+    int guard = 0;
+    while (p >= 0 && guard++ < 256) {
+        __threadfence();
+        if (atomicAdd(&flags[p], 1) == 0) return;   // first arrival: sibling not ready
+        __threadfence();
+        const int32_t l = left[p], r = right[p];
+        const float4 a0 = (l < 0) ? llo[~l] : __ldcg(&ilo[l]);
+        const float4 a1 = (l < 0) ? lhi[~l] : __ldcg(&ihi[l]);
+        const float4 b0 = (r < 0) ? llo[~r] : __ldcg(&ilo[r]);
+        const float4 b1 = (r < 0) ? lhi[~r] : __ldcg(&ihi[r]);
+        __stcg(&ilo[p], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.f));
+        __stcg(&ihi[p], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f));
+        p = parent[p];
+    }
+}
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi)
+{
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dx * dz + dy * dz;
+}
+
+// Exponent e (biased as a float exponent) of the power-of-two grid unit for
+// an extent, with room for 252 units plus one unit of padding per side.
+__device__ __forceinline__ int grid_exponent(float extent)
+{
+    const float x = __fdiv_ru(fmaxf(extent, 0.f), 252.0f);
+    if (!(x > 0.f)) return 1;                       // 2^-126
+    const uint32_t bits = __float_as_uint(x);
+    int e = (int)((bits >> 23) & 0xffu);            // biased exponent of x
+    if (e == 0) return 1;                           // subnormal -> smallest normal unit
+    if (bits & 0x7fffffu) e += 1;                   // round up to a power of two
+    return min(max(e, 1), 253);
+}
+
+struct BuildArgs {
+    int32_t n;
+    const int32_t *left, *right, *first, *last;
+    const float4 *ilo, *ihi, *llo, *lhi;
+    const int32_t *vals;          // sorted position -> caller's triangle id
+    const float *verts;
+    const int3 *idx;
+    const uint32_t *flags;
+    WideNode *nodes;
+    PackedTri *tris;
+    int32_t *counters;            // [0] nodes allocated, [1] triangle slots allocated, [2] next-level tasks, [3] error
+    const int2 *tasks_in;         // (binary ref, wide node index)
+    int2 *tasks_out;
+    int32_t max_nodes;
+};
+
+__device__ __forceinline__ void ref_box(const BuildArgs &A, int32_t ref, float4 &lo, float4 &hi)
+{
+    if (ref < 0) { lo = A.llo[~ref]; hi = A.lhi[~ref]; }
+    else { lo = A.ilo[ref]; hi = A.ihi[ref]; }
+}
+__device__ __forceinline__ int32_t ref_count(const BuildArgs &A, int32_t ref)
+{
+    return (ref < 0) ? 1 : (A.last[ref] - A.first[ref] + 1);
+}
+__device__ __forceinline__ int32_t ref_first(const BuildArgs &A, int32_t ref) { return (ref < 0) ? ~ref : A.first[ref]; }
+
+// One thread per wide node of the current level: gather up to 8 children
+// by repeatedly opening the largest-area internal child (those too big for
+// a leaf first), assign slots by octant, quantise, emit leaves and tasks.
+__global__ void k_collapse(BuildArgs A, int32_t ntasks)
+{
+    const int32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ti >= ntasks) return;
+    const int2 task = A.tasks_in[ti];
+    const int32_t wide = task.y;
+
+    int32_t ch[8];
+    float4 clo[8], chi[8];
+    float area[8];
+    int32_t cnt[8];
+    int m = 0;
+    if (task.x < 0) {
+        ch[0] = task.x; m = 1;
+    } else {
+        ch[0] = A.left[task.x]; ch[1] = A.right[task.x]; m = 2;
+    }
+    for (int k = 0; k < m; ++k) {
+        ref_box(A, ch[k], clo[k], chi[k]);
+        area[k] = half_area(clo[k], chi[k]);
+        cnt[k] = ref_count(A, ch[k]);
+    }
+    while (m < 8) {
+        int best = -1;
+        float best_a = -1.f;
+        for (int pass = 0; pass < 2 && best < 0; ++pass) {
+            for (int k = 0; k < m; ++k) {
+                if (ch[k] < 0) continue;
+                if (pass == 0 && cnt[k] <= kMaxLeafTris) continue;
+                if (area[k] > best_a) { best_a = area[k]; best = k; }
+            }
+        }
+        if (best < 0) break;
+        const int32_t node = ch[best];
+        ch[best] = A.left[node];
+        ch[m] = A.right[node];
+        ref_box(A, ch[best], clo[best], chi[best]);
+        ref_box(A, ch[m], clo[m], chi[m]);
+        area[best] = half_area(clo[best], chi[best]);
+        area[m] = half_area(clo[m], chi[m]);
+        cnt[best] = ref_count(A, ch[best]);
+        cnt[m] = ref_count(A, ch[m]);
+        ++m;
+    }
+
+    // node box and centroid
+    float4 nlo = clo[0], nhi = chi[0];
+    for (int k = 1; k < m; ++k) {
+        nlo = make_float4(fminf(nlo.x, clo[k].x), fminf(nlo.y, clo[k].y), fminf(nlo.z, clo[k].z), 0.f);
+        nhi = make_float4(fmaxf(nhi.x, chi[k].x), fmaxf(nhi.y, chi[k].y), fmaxf(nhi.z, chi[k].z), 0.f);
+    }
+    const float pcx = 0.5f * (nlo.x + nhi.x), pcy = 0.5f * (nlo.y + nhi.y), pcz = 0.5f * (nlo.z + nhi.z);
+
+    // slot assignment: slot s holds the child met first by rays of octant s
+    // (direction signs = bits of s); greedy on dot(centroid offset, signs).
+    int slot_of[8];
+    int child_in[8];
+    for (int s = 0; s < 8; ++s) child_in[s] = -1;
+    for (int k = 0; k < m; ++k) slot_of[k] = -1;
+    for (int it = 0; it < m; ++it) {
+        float bc = FLT_MAX;
+        int bk = 0, bs = 0;
+        for (int k = 0; k < m; ++k) {
+            if (slot_of[k] >= 0) continue;
+            const float ox = 0.5f * (clo[k].x + chi[k].x) - pcx;
+            const float oy = 0.5f * (clo[k].y + chi[k].y) - pcy;
+            const float oz = 0.5f * (clo[k].z + chi[k].z) - pcz;
+            for (int s = 0; s < 8; ++s) {
+                if (child_in[s] >= 0) continue;
+                const float c = ((s & 1) ? -ox : ox) + ((s & 2) ? -oy : oy) + ((s & 4) ? -oz : oz);
+                if (c < bc) { bc = c; bk = k; bs = s; }
+            }
+        }
+        slot_of[bk] = bs;
+        child_in[bs] = bk;
+    }
+
+    // allocate children nodes and triangle slots
+    int n_int = 0, n_tri = 0;
+    for (int k = 0; k < m; ++k) {
+        if (cnt[k] > kMaxLeafTris) ++n_int; else n_tri += cnt[k];
+    }
+    const int32_t child_base = n_int ? atomicAdd(&A.counters[0], n_int) : 0;
+    const int32_t tri_base = n_tri ? atomicAdd(&A.counters[1], n_tri) : 0;
+    if (child_base + n_int > A.max_nodes || tri_base + n_tri > A.n) { atomicExch(&A.counters[3], 1); return; }
+
+    // quantisation frame
+    const int ex = grid_exponent(nhi.x - nlo.x), ey = grid_exponent(nhi.y - nlo.y), ez = grid_exponent(nhi.z - nlo.z);
+    const float ux = __int_as_float(ex << 23), uy = __int_as_float(ey << 23), uz = __int_as_float(ez << 23);
+    const float px = __fsub_rd(nlo.x, ux), py = __fsub_rd(nlo.y, uy), pz = __fsub_rd(nlo.z, uz);
+    const float ix = __int_as_float((254 - ex) << 23);   // exact 1/unit
+    const float iy = __int_as_float((254 - ey) << 23);
+    const float iz = __int_as_float((254 - ez) << 23);
+
+    WideNode W;
+    W.px = px; W.py = py; W.pz = pz;
+    W.ex = (uint8_t)ex; W.ey = (uint8_t)ey; W.ez = (uint8_t)ez;
+    W.imask = 0;
+    W.child_base = (uint32_t)child_base;
+    W.tri_base = (uint32_t)tri_base;
+    int int_k = 0, tri_off = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int k = child_in[s];
+        if (k < 0) {
+            W.meta[s] = 0;
+            W.qlo_x[s] = W.qlo_y[s] = W.qlo_z[s] = 255;
+            W.qhi_x[s] = W.qhi_y[s] = W.qhi_z[s] = 0;
+            continue;
+        }
+        const auto qlo = [](float c, float p, float inv) {
+            const float q = floorf(__fmul_rd(__fsub_rd(c, p), inv)) - 1.0f;
+            return (uint8_t)fminf(fmaxf(q, 0.f), 255.f);
+        };
+        const auto qhi = [](float c, float p, float inv) {
+            const float q = ceilf(__fmul_ru(__fsub_ru(c, p), inv)) + 1.0f;
+            return (uint8_t)fminf(fmaxf(q, 0.f), 255.f);
+        };
+        W.qlo_x[s] = qlo(clo[k].x, px, ix); W.qlo_y[s] = qlo(clo[k].y, py, iy); W.qlo_z[s] = qlo(clo[k].z, pz, iz);
+        W.qhi_x[s] = qhi(chi[k].x, px, ix); W.qhi_y[s] = qhi(chi[k].y, py, iy); W.qhi_z[s] = qhi(chi[k].z, pz, iz);
+        if (cnt[k] > kMaxLeafTris) {
+            W.imask |= (uint8_t)(1u << s);
+            W.meta[s] = (uint8_t)(0x20 | (24 + s));
+            const int slot = atomicAdd(&A.counters[2], 1);
+            A.tasks_out[slot] = make_int2(ch[k], child_base + int_k);
+            ++int_k;
+        } else {
+            const int c = cnt[k];
+            W.meta[s] = (uint8_t)((((1u << c) - 1u) << 5) | (uint32_t)tri_off);
+            const int32_t f0 = ref_first(A, ch[k]);
+            for (int j = 0; j < c; ++j) {
+                const int32_t id = A.vals[f0 + j];
+                const int3 t = A.idx[id];
+                const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
+                const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
+                const float3 cc = make_float3(A.verts[3 * t.z], A.verts[3 * t.z + 1], A.verts[3 * t.z + 2]);
+                const float3 e1 = xsub3(cc, a);   // triangle.h:193
+                const float3 e2 = xsub3(b, a);    // triangle.h:194
+                PackedTri P;
+                P.w0 = make_float4(a.x, a.y, a.z, e1.x);
+                P.w1 = make_float4(e1.y, e1.z, e2.x, e2.y);
+                P.w2 = make_float4(e2.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
+                A.tris[tri_base + tri_off + j] = P;
+            }
+            tri_off += c;
+        }
+    }
+    A.nodes[wide] = W;
+}
+
+}  // namespace
+
+size_t build_temp_bytes(int32_t n)
+{
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (const uint64_t *)nullptr, (uint64_t *)nullptr,
+                                    (const int32_t *)nullptr, (int32_t *)nullptr, n > 0 ? n : 1, 0, 64);
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    size_t b = 0;
+    b += 2 * nn * sizeof(float4);          // blo, bhi
+    b += 2 * nn * sizeof(uint64_t);        // keys in/out
+    b += 2 * nn * sizeof(int32_t);         // vals in/out
+    b += 6 * nn * sizeof(int32_t);         // left right first last parent leaf_parent
+    b += 4 * nn * sizeof(float4);          // llo lhi ilo ihi
+    b += nn * sizeof(int32_t);             // refit flags
+    b += 2 * nn * sizeof(int2);            // task queues
+    b += 64 * sizeof(int32_t);             // counters, bounds
+    b += cub_bytes + 16 * 256;
+    return b;
+}
+
+static inline char *carve(char *&p, size_t bytes)
+{
+    char *r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+}
+
+BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes, cudaStream_t st)
+{
+    BuildResult R;
+    const int32_t n = in.ntris;
+    if (n <= 0) { R.status = 0; return R; }
+    const size_t nn = (size_t)n;
+    char *p = (char *)temp;
+    float4 *blo = (float4 *)carve(p, nn * sizeof(float4));
+    float4 *bhi = (float4 *)carve(p, nn * sizeof(float4));
+    uint64_t *keys = (uint64_t *)carve(p, nn * sizeof(uint64_t));
+    uint64_t *keys2 = (uint64_t *)carve(p, nn * sizeof(uint64_t));
+    int32_t *vals = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *vals2 = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *left = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *right = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *first = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *last = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *parent = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *leaf_parent = (int32_t *)carve(p, nn * sizeof(int32_t));
+    float4 *llo = (float4 *)carve(p, nn * sizeof(float4));
+    float4 *lhi = (float4 *)carve(p, nn * sizeof(float4));
+    float4 *ilo = (float4 *)carve(p, nn * sizeof(float4));
+    float4 *ihi = (float4 *)carve(p, nn * sizeof(float4));
+    int32_t *rflags = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int2 *tq0 = (int2 *)carve(p, nn * sizeof(int2));
+    int2 *tq1 = (int2 *)carve(p, nn * sizeof(int2));
+    int32_t *counters = (int32_t *)carve(p, 64 * sizeof(int32_t));
+    int *cbounds = counters + 16;
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
+    void *cub_temp = carve(p, cub_bytes);
+    if ((size_t)(p - (char *)temp) > temp_bytes) { R.status = -3; return R; }
+
+    const int init_bounds[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000, (int)0x80000000};
+    cudaMemsetAsync(counters, 0, 16 * sizeof(int32_t), st);
+    cudaMemcpyAsync(cbounds, init_bounds, sizeof(init_bounds), cudaMemcpyHostToDevice, st);
+    const int threads = 256;
+    const int grid_pts = min((n + threads - 1) / threads, in.sm_count * 8);
+    k_prep<<<grid_pts, threads, 0, st>>>(in.verts, in.idx, n, in.shade, blo, bhi, cbounds);
+    k_morton<<<grid_pts, threads, 0, st>>>(blo, bhi, n, cbounds, keys, vals);
+    cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
+    const int g = (n + threads - 1) / threads;
+    if (n > 1) {
+        k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, parent, leaf_parent);
+    }
+    k_leaf_boxes<<<g, threads, 0, st>>>(vals2, n, blo, bhi, llo, lhi);
+    if (n > 1) {
+        cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
+        k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
+    }
+
+    BuildArgs A;
+    A.n = n; A.left = left; A.right = right; A.first = first; A.last = last;
+    A.ilo = ilo; A.ihi = ihi; A.llo = llo; A.lhi = lhi; A.vals = vals2;
+    A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
+    A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
+    A.max_nodes = in.max_nodes;
+    // root task: binary root (internal 0, or leaf 0 when n == 1) -> wide node 0
+    const int2 root = make_int2(n > 1 ? 0 : ~0, 0);
+    cudaMemcpyAsync(tq0, &root, sizeof(int2), cudaMemcpyHostToDevice, st);
+    const int32_t one = 1;
+    cudaMemcpyAsync(&counters[0], &one, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    int32_t ntasks = 1, depth = 0;
+    int32_t *h_cnt = in.host_scratch;   // pinned, >= 4 ints
+    while (ntasks > 0) {
+        if (depth >= kMaxDepth) { R.status = -5; return R; }
+        A.tasks_in = (depth & 1) ? tq1 : tq0;
+        A.tasks_out = (depth & 1) ? tq0 : tq1;
+        cudaMemsetAsync(&counters[2], 0, sizeof(int32_t), st);
+        k_collapse<<<(ntasks + 63) / 64, 64, 0, st>>>(A, ntasks);
+        cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+        if (h_cnt[3]) { R.status = -8; return R; }
+        ntasks = h_cnt[2];
+        ++depth;
+    }
+    R.status = 0;
+    R.nodes = h_cnt[0];
+    R.tri_slots = h_cnt[1];
+    R.depth = depth;
+    return R;
+}
+
+}  // namespace rtc

@@ -1,0 +1,34 @@
+// rt_build.cuh -- interface of the GPU acceleration-structure builder.
+#pragma once
+
+#include "rt_internal.cuh"
+
+namespace rtc {
+
+struct BuildInputs {
+    int32_t ntris;
+    const float *verts;       // device, 3 floats per vertex
+    const int3 *idx;          // device, caller's order
+    const uint32_t *flags;    // device or nullptr
+    ShadeTri *shade;          // device out, ntris
+    WideNode *nodes;          // device out, max_nodes
+    PackedTri *tris;          // device out, ntris
+    int32_t max_nodes;
+    int32_t sm_count;
+    int32_t *host_scratch;    // pinned host, >= 4 ints
+};
+
+struct BuildResult {
+    int32_t status = -8;      // 0 ok, else an rt_status code
+    int32_t nodes = 0;
+    int32_t tri_slots = 0;
+    int32_t depth = 0;
+};
+
+// Device scratch needed by build_wide_bvh for n triangles.
+size_t build_temp_bytes(int32_t n);
+
+// Build on stream st; synchronises st once per tree level.
+BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes, cudaStream_t st);
+
+}  // namespace rtc

@@ -1,0 +1,37 @@
+// rt_kernels.cuh -- launch interface of the traversal and render kernels.
+#pragma once
+
+#include "rt_internal.cuh"
+
+namespace rtc {
+
+constexpr int kTraceThreads = 128;   // 4 warps per block
+constexpr int kBlocksPerSM = 8;      // persistent grid = SMs x 8 blocks
+
+// Per-launch device counters (zeroed before each launch).
+struct Counters {
+    int work;                        // next work item (persistent-warp queue)
+    uint32_t status;                 // OR of kStatus* bits
+    unsigned long long primary;      // primary rays traced
+    unsigned long long hits;         // primary hits
+    unsigned long long secondary;    // shadow / AO rays traced
+    unsigned long long nodes;        // wide nodes fetched (counting kernels only)
+    unsigned long long tris;         // triangles tested (counting kernels only)
+};
+
+struct LightSet {
+    int32_t n;
+    LightView l[RT_MAX_LIGHTS];
+};
+
+void launch_trace_closest(const SceneView &sc, const rt_ray *rays, int32_t n, rt_hit *hits, Counters *ctr, int sm_count,
+                          cudaStream_t st);
+void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_t *occ, Counters *ctr, int sm_count,
+                      cudaStream_t st);
+void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
+                   uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+void launch_render_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat, int32_t samples,
+                      float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
+                      int sm_count, cudaStream_t st, bool count = false);
+
+}  // namespace rtc

@@ -1,0 +1,387 @@
+// rt_traverse.cuh -- per-ray traversal of the 8-wide quantised BVH, the
+// reference-exact Moller-Trumbore test, and the shading helpers shared by
+// every kernel of the core.
+//
+// Traversal keeps node groups (child base + hit bits) on a per-ray stack:
+// internal-child hits live in bits 24..31 at position (slot ^ octant) so the
+// lowest set bit is the child nearest the ray's origin side, the node's
+// internal-child mask rides in bits 0..7, and leaf triangles of a node are
+// tested as soon as the node is intersected (after Ylitie et al., HPG 2017).
+#pragma once
+
+#include "rt_internal.cuh"
+
+namespace rtc {
+
+struct RayState {
+    float3 o, d;
+};
+
+// Reference-exact triangle test (triangle::is_intersecting,
+// raytracer/triangle.h:190-235): e1 = c - a, e2 = b - a, reject
+// |det| < 1e-6, u weighs c, v weighs b.  Returns t, or +inf when rejected.
+__device__ __forceinline__ float mt_intersect(const float4 w0, const float4 w1, const float4 w2, const float3 o,
+                                              const float3 d, float &u_out, float &v_out)
+{
+    const float3 a = make_float3(w0.x, w0.y, w0.z);
+    const float3 e1 = make_float3(w0.w, w1.x, w1.y);
+    const float3 e2 = make_float3(w1.z, w1.w, w2.x);
+    const float3 P = xcross(d, e2);
+    const float det = xdot(e1, P);
+    const float inv_det = __frcp_rn(det);      // == 1.0f / det, correctly rounded
+    const float3 T = xsub3(o, a);
+    const float u = xmul(xdot(T, P), inv_det);
+    const float3 Q = xcross(T, e1);
+    const float v = xmul(xdot(d, Q), inv_det);
+    const float t = xmul(xdot(e2, Q), inv_det);
+    const bool reject = (det > -kDetEps && det < kDetEps) || (u < 0.0f) || (v < 0.0f) || (xadd(u, v) > 1.0f);
+    u_out = u;
+    v_out = v;
+    return reject ? __int_as_float(0x7f800000) : t;
+}
+
+// Child-box test of one wide node: returns internal-hit bits (24..31,
+// permuted by octant) | imask (0..7) in .y with child_base in .x, and the
+// triangle-hit bits (0..23) with tri_base in tgroup.
+struct NodeHits {
+    uint2 ngroup;
+    uint2 tgroup;
+};
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int s)
+{
+    return ((s < 4) ? (lo >> (8 * s)) : (hi >> (8 * (s - 4)))) & 0xffu;
+}
+
+__device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx, const float3 o,
+                                                   const float3 inv, uint32_t oct, float tmax)
+{
+    const float4 *np = reinterpret_cast<const float4 *>(nodes + idx);
+    const float4 n0 = __ldg(np + 0);
+    const float4 n1 = __ldg(np + 1);
+    const float4 n2 = __ldg(np + 2);
+    const float4 n3 = __ldg(np + 3);
+    const float4 n4 = __ldg(np + 4);
+    const uint32_t e_imask = __float_as_uint(n0.w);
+    const uint32_t ex = e_imask & 0xffu, ey = (e_imask >> 8) & 0xffu, ez = (e_imask >> 16) & 0xffu;
+    const uint32_t imask = e_imask >> 24;
+    const float sx = __uint_as_float(ex << 23) * inv.x;
+    const float sy = __uint_as_float(ey << 23) * inv.y;
+    const float sz = __uint_as_float(ez << 23) * inv.z;
+    const float ox = (n0.x - o.x) * inv.x;
+    const float oy = (n0.y - o.y) * inv.y;
+    const float oz = (n0.z - o.z) * inv.z;
+    const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+    // lo/hi byte planes; swap per axis so "near" is the entry plane
+    uint32_t nxl = __float_as_uint(n2.x), nxh = __float_as_uint(n2.y);   // qlo_x
+    uint32_t nyl = __float_as_uint(n2.z), nyh = __float_as_uint(n2.w);   // qlo_y
+    uint32_t nzl = __float_as_uint(n3.x), nzh = __float_as_uint(n3.y);   // qlo_z
+    uint32_t fxl = __float_as_uint(n3.z), fxh = __float_as_uint(n3.w);   // qhi_x
+    uint32_t fyl = __float_as_uint(n4.x), fyh = __float_as_uint(n4.y);   // qhi_y
+    uint32_t fzl = __float_as_uint(n4.z), fzh = __float_as_uint(n4.w);   // qhi_z
+    if (inv.x < 0.f) { uint32_t t = nxl; nxl = fxl; fxl = t; t = nxh; nxh = fxh; fxh = t; }
+    if (inv.y < 0.f) { uint32_t t = nyl; nyl = fyl; fyl = t; t = nyh; nyh = fyh; fyh = t; }
+    if (inv.z < 0.f) { uint32_t t = nzl; nzl = fzl; fzl = t; t = nzh; nzh = fzh; fzh = t; }
+    uint32_t hits_int = 0, hits_tri = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t meta = byte_of(meta_lo, meta_hi, s);
+        const float tnx = fmaf((float)byte_of(nxl, nxh, s), sx, ox);
+        const float tny = fmaf((float)byte_of(nyl, nyh, s), sy, oy);
+        const float tnz = fmaf((float)byte_of(nzl, nzh, s), sz, oz);
+        const float tfx = fmaf((float)byte_of(fxl, fxh, s), sx, ox);
+        const float tfy = fmaf((float)byte_of(fyl, fyh, s), sy, oy);
+        const float tfz = fmaf((float)byte_of(fzl, fzh, s), sz, oz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        if (tn <= tf && meta != 0u) {
+            if ((imask >> s) & 1u) hits_int |= 1u << (24 + (s ^ oct));
+            else hits_tri |= (meta >> 5) << (meta & 31u);
+        }
+    }
+    NodeHits h;
+    h.ngroup = make_uint2(__float_as_uint(n1.x), hits_int | imask);
+    h.tgroup = make_uint2(__float_as_uint(n1.y), hits_tri);
+    return h;
+}
+
+__device__ __forceinline__ float3 safe_inv(float3 d)
+{
+    const float tiny = 1e-20f;
+    const float x = (fabsf(d.x) > tiny) ? d.x : copysignf(tiny, d.x);
+    const float y = (fabsf(d.y) > tiny) ? d.y : copysignf(tiny, d.y);
+    const float z = (fabsf(d.z) > tiny) ? d.z : copysignf(tiny, d.z);
+    return make_float3(__frcp_rn(x), __frcp_rn(y), __frcp_rn(z));
+}
+
+__device__ __forceinline__ uint32_t octant_of(float3 d)
+{
+    return (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+}
+
+struct HitRecord {
+    int32_t id;
+    float t, u, v;
+};
+
+// Closest hit (ANY = false) or any hit inside (EPSILON, tmax) skipping light
+// and transparent triangles (ANY = true).  Returns the device status bits.
+struct FetchCount {
+    uint32_t nodes = 0;
+    uint32_t tris = 0;
+};
+
+template <bool ANY, bool COUNT = false>
+__device__ __forceinline__ uint32_t traverse(const SceneView &sc, const float3 o, const float3 d, float tmax,
+                                             HitRecord &hit, bool &occluded, FetchCount *fc = nullptr)
+{
+    hit.id = -1;
+    hit.t = FLT_MAX;
+    hit.u = 0.f;
+    hit.v = 0.f;
+    occluded = false;
+    if (sc.nnodes <= 0) return 0u;
+    const float3 inv = safe_inv(d);
+    const uint32_t oct = octant_of(d);
+    uint2 stack[kStackSize];
+    int sp = 0;
+    // start: a group holding only the root (node 0 as slot 0 of a virtual parent)
+    uint2 ngroup = make_uint2(0u, (1u << (24 + oct)) | 1u);
+    float box_tmax = ANY ? tmax : FLT_MAX;
+    uint32_t status = 0u;
+    for (int step = 0; step < kMaxTraversalSteps; ++step) {
+        uint2 tgroup = make_uint2(0u, 0u);
+        if (ngroup.y & 0xff000000u) {
+            const uint32_t bit = __ffs(ngroup.y >> 24) - 1u;
+            ngroup.y &= ~(1u << (24 + bit));
+            const uint32_t slot = bit ^ oct;
+            const uint32_t idx = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xffu);
+            if (idx >= (uint32_t)sc.nnodes) { status |= kStatusBadIndex; break; }
+            if (ngroup.y & 0xff000000u) {
+                if (sp >= kStackSize) { status |= kStatusStackOverflow; break; }
+                stack[sp++] = ngroup;
+            }
+            const NodeHits nh = intersect_node(sc.nodes, idx, o, inv, oct, box_tmax);
+            if (COUNT) ++fc->nodes;
+            ngroup = nh.ngroup;
+            tgroup = nh.tgroup;
+        }
+        while (tgroup.y != 0u) {
+            const uint32_t k = __ffs(tgroup.y) - 1u;
+            tgroup.y &= tgroup.y - 1u;
+            const uint32_t ti = tgroup.x + k;
+            if (ti >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
+            const PackedTri *tp = sc.tris + ti;
+            if (COUNT) ++fc->tris;
+            const float4 w0 = __ldg(&tp->w0);
+            const float4 w1 = __ldg(&tp->w1);
+            const float4 w2 = __ldg(&tp->w2);
+            float u, v;
+            const float t = mt_intersect(w0, w1, w2, o, d, u, v);
+            if ((uint32_t)__float_as_int(w2.y) >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
+            if (ANY) {
+                if ((__float_as_uint(w2.z) & (RT_TRI_LIGHT | RT_TRI_TRANSPARENT)) == 0u && t > kEpsilon && t < tmax) {
+                    occluded = true;
+                    hit.id = __float_as_int(w2.y);
+                    hit.t = t;
+                    return status;
+                }
+            } else {
+                const int32_t id = __float_as_int(w2.y);
+                if (t > kEpsilon && (t < hit.t || (t == hit.t && id < hit.id))) {
+                    hit.id = id;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    box_tmax = t;
+                }
+            }
+        }
+        if (!(ngroup.y & 0xff000000u)) {
+            if (sp == 0) return status;
+            ngroup = stack[--sp];
+        }
+        if (step + 1 == kMaxTraversalSteps) status |= kStatusStepLimit;
+    }
+    return status;
+}
+
+// ------------------------------------------------------------ shading
+
+// ray::offset_start_point(+1) (raytracer/ray.h:111-157).
+__device__ __forceinline__ float offset_coord(float p, float n)
+{
+    uint32_t x = __float_as_uint(p);
+    if ((x & 0x7fffffffu) < 0x38d1b717u)   // bit pattern of 1.0e-4f
+        return xadd(0.0f, xmul(1.0e-4f, n));
+    const float off = ((x >> 31) & 1u) ? -32.0f : 32.0f;
+    const float f = xmul(xmul(off, n), 1.0f);
+    int32_t iv;
+    if (!(f > -2147483904.0f && f < 2147483648.0f)) iv = INT32_MIN;
+    else iv = __float2int_rz(f);
+    x += (uint32_t)iv;
+    return __uint_as_float(x);
+}
+
+__device__ __forceinline__ float3 offset_start(float3 p, float3 n)
+{
+    return make_float3(offset_coord(p.x, n.x), offset_coord(p.y, n.y), offset_coord(p.z, n.z));
+}
+
+// Camera ray of pixel (x, y) (camera.h:127-140, EXACT_NORMALISE).
+__device__ __forceinline__ RayState camera_ray(const CameraView &cam, int x, int y)
+{
+    const float x_t = xadd(xmul((float)x, cam.x_inc), cam.x_m);
+    const float y_t = xadd(xmul((float)y, cam.y_inc), cam.y_m);
+    const float3 screen = xadd3(xadd3(xmul3(cam.X, x_t), xmul3(cam.Y, y_t)), xmul3(cam.Z, cam.t));
+    RayState r;
+    r.o = cam.c;
+    r.d = xnorm(screen);
+    return r;
+}
+
+struct SurfacePoint {
+    float3 dst;       // refined hit point
+    float3 sn;        // face-forwarded shading normal
+    float3 geo;       // face-forwarded geometric normal
+    float3 vt;        // interpolated per-vertex attribute
+    bool has_attr;
+};
+
+// Hit refinement and face-forwarding (raytracer.cc:30-31,
+// triangle::normal_at_point triangle.h:464-498) and the barycentric
+// attribute (triangle.h:74-79).
+__device__ __forceinline__ SurfacePoint surface_at(const SceneView &sc, const RayState &r, const HitRecord &h)
+{
+    SurfacePoint sp;
+    const ShadeTri st = sc.shade[h.id];
+    const float3 n = make_float3(st.n_cx.x, st.n_cx.y, st.n_cx.z);
+    const float3 c = make_float3(st.n_cx.w, st.c_yz.x, st.c_yz.y);
+    float3 p = xadd3(r.o, xmul3(r.d, h.t));
+    const float denom = xdot(n, r.d);
+    const float num = xdot(n, xsub3(c, p));
+    p = xadd3(p, xmul3(r.d, xdiv(num, denom)));
+    if (denom > 0.0f) {
+        sp.sn = make_float3(-n.x, -n.y, -n.z);
+        sp.geo = sp.sn;
+    } else {
+        sp.sn = n;
+        sp.geo = n;
+    }
+    sp.dst = p;
+    sp.has_attr = sc.vattr != nullptr;
+    if (sp.has_attr) {
+        const int3 t = sc.idx[h.id];
+        const float3 A = make_float3(sc.vattr[3 * t.x], sc.vattr[3 * t.x + 1], sc.vattr[3 * t.x + 2]);
+        const float3 B = make_float3(sc.vattr[3 * t.y], sc.vattr[3 * t.y + 1], sc.vattr[3 * t.y + 2]);
+        const float3 C = make_float3(sc.vattr[3 * t.z], sc.vattr[3 * t.z + 1], sc.vattr[3 * t.z + 2]);
+        const float w = xsub(1.0f, xadd(h.u, h.v));
+        sp.vt = xadd3(xadd3(xmul3(C, h.u), xmul3(B, h.v)), xmul3(A, w));
+    } else {
+        sp.vt = make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
+    }
+    return sp;
+}
+
+// Diffuse colour (coloured_mapper_shader.cc:61-66 with attribute*255 samples).
+__device__ __forceinline__ float3 material_kd(const MaterialView &m, const SurfacePoint &sp)
+{
+    if (!sp.has_attr) return m.kd;
+    const float k = 1.0f / 255.0f;
+    return make_float3(xmul(xmul(sp.vt.x, 255.0f), xmul(m.kd.x, k)), xmul(xmul(sp.vt.y, 255.0f), xmul(m.kd.y, k)),
+                       xmul(xmul(sp.vt.z, 255.0f), xmul(m.kd.z, k)));
+}
+
+// Shadow ray towards a light (ray::find_rays ray.cc:91-104,
+// light::find_rays light.h:62-100, ray::set_up ray.h:44-54).
+__device__ __forceinline__ void shadow_ray(const LightView &L, float3 start, float3 &dir, float &len)
+{
+    const float3 target = (L.kind == RT_LIGHT_DIRECTIONAL) ? xadd3(start, xmul3(L.dir, L.dist_sign)) : L.pos;
+    const float3 dv = xsub3(target, start);
+    len = xmag(dv);
+    dir = xdiv3(dv, len);
+}
+
+// One light's Phong term (coloured_mapper_shader.cc:76-109,
+// light::get_light_intensity light.h:44-59) added into c.
+__device__ __forceinline__ void phong_add(const LightView &L, const MaterialView &m, const float3 kd, const float3 sn,
+                                          const float3 view_dir, const float3 ldir, float len, float magn, float3 &c)
+{
+    const float shade = xdot(ldir, sn);
+    if (shade < 0.0f) return;
+    const float3 ref = xsub3(ldir, xmul3(sn, xmul(2.0f, shade)));
+    const float rdr = xdot(view_dir, ref);
+    float3 sc = make_float3(xmul(shade, kd.x), xmul(shade, kd.y), xmul(shade, kd.z));
+    if (rdr > 0.0f) {
+        const float p = (float)pow((double)rdr, (double)m.ns);
+        sc = make_float3(xadd(sc.x, xmul(p, m.ks.x)), xadd(sc.y, xmul(p, m.ks.y)), xadd(sc.z, xmul(p, m.ks.z)));
+    }
+    const float dist = xmul(len, L.d);
+    const float d_scale = xadd(xmul(dist, dist), 1.0f);
+    const float3 I = make_float3(xdiv(L.rgb255.x, d_scale), xdiv(L.rgb255.y, d_scale), xdiv(L.rgb255.z, d_scale));
+    c = make_float3(xadd(c.x, xmul(I.x, xmul(sc.x, magn))), xadd(c.y, xmul(I.y, xmul(sc.y, magn))),
+                    xadd(c.z, xmul(I.z, xmul(sc.z, magn))));
+}
+
+// camera::clip_image_to_rgb (camera.h:312-314): clamp, then truncate.
+__device__ __forceinline__ uint8_t clip8(float v)
+{
+    return (uint8_t)__float2uint_rz(smin(255.0f, smax(0.0f, xdiv(v, 1.0f))));
+}
+
+// ---------------------------------------------------------- AO sampler
+
+// Philox4x32-10 (Salmon et al., SC'11).
+__device__ __forceinline__ uint4 philox4x32(uint4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+struct AOBasis {
+    float3 T, B, g;
+};
+
+// Orthonormal basis of Duff et al. (JCGT 2017), IEEE-exact.
+__device__ __forceinline__ AOBasis ao_basis(float3 g)
+{
+    const float sign = (g.z < 0.0f || (g.z == 0.0f && (__float_as_uint(g.z) >> 31))) ? -1.0f : 1.0f;
+    const float a = xdiv(-1.0f, xadd(sign, g.z));
+    const float b = xmul(xmul(g.x, g.y), a);
+    AOBasis ob;
+    ob.T = make_float3(xadd(1.0f, xmul(xmul(sign, xmul(g.x, g.x)), a)), xmul(sign, b), -xmul(sign, g.x));
+    ob.B = make_float3(b, xadd(sign, xmul(xmul(g.y, g.y), a)), -g.y);
+    ob.g = g;
+    return ob;
+}
+
+// Direction of AO sample s for a pixel (cosine-weighted by rejection from
+// the unit disk, at most 8 tries, lifted to the hemisphere).
+__device__ __forceinline__ float3 ao_direction(const AOBasis &ob, uint32_t pixel, uint32_t s, uint32_t seed)
+{
+    float x = 0.0f, y = 0.0f;
+    bool found = false;
+    for (uint32_t call = 0; call < 4 && !found; ++call) {
+        const uint4 r = philox4x32(make_uint4(pixel, s, call, 0x414f5259u), seed, 0x52415054u);
+        const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+        for (int pair = 0; pair < 2; ++pair) {
+            if (found) break;
+            const float px = xsub(xmul((float)(rr[2 * pair] >> 8), 1.1920928955078125e-7f), 1.0f);
+            const float py = xsub(xmul((float)(rr[2 * pair + 1] >> 8), 1.1920928955078125e-7f), 1.0f);
+            if (xadd(xmul(px, px), xmul(py, py)) < 1.0f) { x = px; y = py; found = true; }
+        }
+    }
+    const float z = __fsqrt_rn(smax(0.0f, xsub(1.0f, xadd(xmul(x, x), xmul(y, y)))));
+    const float3 d = xadd3(xadd3(xmul3(ob.T, x), xmul3(ob.B, y)), xmul3(ob.g, z));
+    return xnorm(d);
+}
+
+}  // namespace rtc

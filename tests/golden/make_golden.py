@@ -1,0 +1,162 @@
+"""Regenerate the golden fixtures in this folder from the reference itself.
+
+Run where the reference tree is present (x86-64 host):
+
+    python tests/golden/make_golden.py [--ref /root/reference/RAPTor]
+
+It writes
+  bih_kats.json     traversal known-answer tests parsed from the reference's
+                    raytracer/unit_tests/bih_tests.cc (6-triangle fixtures,
+                    expected hit ids, distances and occlusion answers)
+  morton_kats.json  Morton-code known answers parsed from
+                    raytracer/unit_tests/vint_tests.cc
+  ref_small.npz     inputs and outputs of the reference's own bvh,
+                    ray_tracer() and clip_image_to_rgb() (compiled by
+                    oracle/refbuild/Makefile) on small seeded scenes
+The tests compare the C restatement (oracle/rtoracle.c) and the CUDA core
+against these files; nothing at test time reads the reference tree.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+NUM = r"(-?[0-9.]+)f?"
+
+
+def parse_bih_tests(path):
+    src = open(path).read()
+    tris = {"x": [], "y": [], "z": []}
+    pt = r"point_t\(\s*" + NUM + r"\s*,\s*" + NUM + r"\s*,\s*" + NUM + r"\s*\)"
+    for m in re.finditer(r"([xyz])_tris\.emplace_back\(mat\.get\(\),\s*" + pt + r",\s*" + pt + r",\s*" + pt, src):
+        v = [float(m.group(i)) for i in range(2, 11)]
+        tris[m.group(1)].append([v[0:3], v[3:6], v[6:9]])
+    cases = []
+    for m in re.finditer(r"BOOST_AUTO_TEST_CASE\(\s*(\w+)\s*\)\s*\{(.*?)\n\}", src, re.S):
+        name, body = m.group(1), m.group(2)
+        fx = re.search(r"bih uut\(([xyz])_tris", body)
+        rr = re.search(r"ray r\(" + pt + r",\s*" + NUM + r",\s*" + NUM + r",\s*" + NUM + r"\)", body)
+        if not fx or not rr:
+            continue
+        case = {"name": name, "fixture": fx.group(1),
+                "origin": [float(rr.group(i)) for i in (1, 2, 3)],
+                "dir": [float(rr.group(i)) for i in (4, 5, 6)]}
+        fn = re.search(r"find_nearest_object\(&r, &h\)\s*==\s*(-?\d+)", body)
+        if fn:
+            case["nearest"] = int(fn.group(1))
+        dc = re.search(r"BOOST_CHECK_CLOSE\(h\.d,\s*" + NUM, body)
+        if dc:
+            case["distance"] = float(dc.group(1))
+        fo = re.search(r"BOOST_CHECK\((!?)uut\.found_nearer_object\(&r,\s*" + NUM + r"\)\)", body)
+        if fo:
+            case["nearer_t"] = float(fo.group(2))
+            case["nearer"] = fo.group(1) != "!"
+        cases.append(case)
+    return {"source": "raytracer/unit_tests/bih_tests.cc", "tolerance_percent": 0.00001, "tris": tris,
+            "cases": cases}
+
+
+def parse_morton_tests(path):
+    src = open(path).read()
+    out = []
+    vec = r"vfp_t\s+(\w+)\(([^;]*)\);"
+    for m in re.finditer(r"BOOST_AUTO_TEST_CASE\(\s*(\w*morton_code_test)\s*\)\s*\{(.*?)\n\}", src, re.S):
+        name, body = m.group(1), m.group(2)
+        vals = {}
+        for v in re.finditer(vec, body):
+            parts = [p.strip() for p in v.group(2).split(",")]
+            nums = []
+            for p in parts:   # float literals, or "1.0f / 4.5f" evaluated in binary32 as C++ does
+                terms = [np.float32(q.strip().rstrip("f")) for q in p.split("/")]
+                val = terms[0] if len(terms) == 1 else np.float32(terms[0] / terms[1])
+                nums.append(float(val))
+            if len(nums) == 1:
+                nums = nums * 4
+            vals[v.group(1)] = nums
+        exp = [int(e.group(2), 16) for e in re.finditer(r"mc\[(\d)\]\s*==\s*(0x[0-9a-fA-F]+)", body)]
+        for i in range(4):
+            out.append({"name": f"{name}[{i}]", "x": vals["x"][i], "y": vals["y"][i], "z": vals["z"][i],
+                        "x_mul": vals["x_mul"][i], "y_mul": vals["y_mul"][i], "z_mul": vals["z_mul"][i],
+                        "expected": exp[i]})
+    return {"source": "raytracer/unit_tests/vint_tests.cc", "cases": out}
+
+
+def small_scenes():
+    from raptor_gb300 import scenes
+    out = {}
+    s, f = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    out["ico"] = (s, f)
+    h = scenes.diamond_square(32, 0.55, 1)
+    v, t, hs = scenes.heightfield_mesh(h, 64.0, 12.0)
+    col = scenes.slope_colours(hs, 2.0, 12.0)
+    s2 = scenes._pack(v, t, col)
+    f2 = {"camera": scenes.look_at_camera((0.0, 30.0, 0.0), (32.0, 6.0, 32.0), 60.0, 64, 48, (110.0, 160.0, 230.0)),
+          "lights": [scenes.directional_light((-0.4, -0.8, -0.3))], "material": dict(scenes.DEFAULT_MATERIAL)}
+    out["terrain"] = (s2, f2)
+    return out
+
+
+def soup(seed=7, n=300):
+    """Random triangle soup with some light/transparent triangles."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-5, 5, (n, 3))
+    v = (c[:, None, :] + rng.uniform(-1, 1, (n, 3, 3))).reshape(-1, 3)
+    t = np.arange(3 * n, dtype=np.int32).reshape(-1, 3)
+    flags = np.zeros(n, np.uint32)
+    flags[rng.uniform(size=n) < 0.1] = 1
+    flags[rng.uniform(size=n) < 0.1] |= 2
+    o = rng.uniform(-8, 8, (4000, 3))
+    d = rng.normal(size=(4000, 3))
+    d = d / np.sqrt((d ** 2).sum(1))[:, None]
+    tmax = rng.uniform(0.5, 12.0, 4000)
+    return ({"verts": v.astype(np.float32), "tris": t, "vattr": None, "flags": flags},
+            o.astype(np.float32), d.astype(np.float32), tmax.astype(np.float32))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference/RAPTor")
+    a = ap.parse_args()
+    kats = parse_bih_tests(os.path.join(a.ref, "raytracer/unit_tests/bih_tests.cc"))
+    json.dump(kats, open(os.path.join(HERE, "bih_kats.json"), "w"), indent=1)
+    mort = parse_morton_tests(os.path.join(a.ref, "raytracer/unit_tests/vint_tests.cc"))
+    json.dump(mort, open(os.path.join(HERE, "morton_kats.json"), "w"), indent=1)
+    print(f"bih KATs: {len(kats['cases'])}, morton KATs: {len(mort['cases'])}")
+
+    import oracle as O
+    O.build()
+    if not O.ref_available():
+        raise SystemExit("reference harness not built (needs the reference tree on an x86-64 host)")
+    arrays = {}
+    for key, (s, f) in small_scenes().items():
+        rs = O.RefScene(s, f["material"])
+        og, dr = O.camera_rays(f["camera"], lib=O.ref_lib())
+        ids, t, u, v = rs.closest(og, dr)
+        rgb = rs.render(f)["rgb"]
+        arrays.update({f"{key}_verts": s["verts"], f"{key}_tris": s["tris"], f"{key}_vattr": s["vattr"],
+                       f"{key}_ray_o": og, f"{key}_ray_d": dr, f"{key}_id": ids, f"{key}_t": t, f"{key}_u": u,
+                       f"{key}_v": v, f"{key}_rgb": rgb})
+        arrays[f"{key}_frame"] = np.frombuffer(json.dumps(f).encode(), dtype=np.uint8)
+    s, o, d, tmax = soup()
+    rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))
+    ids, t, u, v = rs.closest(o, d)
+    occ = rs.any(o, d, tmax)
+    arrays.update({"soup_verts": s["verts"], "soup_tris": s["tris"], "soup_flags": s["flags"], "soup_ray_o": o,
+                   "soup_ray_d": d, "soup_tmax": tmax, "soup_id": ids, "soup_t": t, "soup_u": u, "soup_v": v,
+                   "soup_occ": occ})
+    np.savez_compressed(os.path.join(HERE, "ref_small.npz"), **arrays)
+    print("wrote ref_small.npz:", {k: v.shape for k, v in arrays.items()})
+
+
+if __name__ == "__main__":
+    main()

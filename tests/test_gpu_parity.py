@@ -1,0 +1,239 @@
+"""Parity of the CUDA core (through the C ABI) with the reference and the
+oracle: the reference's own known-answer tests, reference outputs on small
+scenes, and the oracle on the benchmark workloads at sizes it finishes in
+seconds.  Criteria in tests/parity.py."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from parity import PIX_FRAC, compare_hits, edge_distance, pixel_agreement
+
+pytestmark = pytest.mark.gpu
+
+FLT_MAX = np.float32(3.4028234663852886e38)
+
+
+def kats():
+    return json.load(open(os.path.join(GOLDEN, "bih_kats.json")))
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(os.path.join(GOLDEN, "ref_small.npz"))
+
+
+def gpu_closest(rt, scene, o, d):
+    hits = scene.closest(rt.rays_array(o, d))
+    return hits["tri"], hits["t"], hits["u"], hits["v"]
+
+
+@pytest.mark.parametrize("case", kats()["cases"], ids=lambda c: c["name"])
+def test_bih_kats_gpu(rtlib, ctx, case):
+    """raytracer/unit_tests/bih_tests.cc, run through rt_trace_closest /
+    rt_trace_any in place of ssd::find_nearest_object / found_nearer_object."""
+    k = kats()
+    tris = np.array(k["tris"][case["fixture"]], np.float32).reshape(-1, 3)
+    sc = rtlib.Scene(ctx, {"verts": tris, "tris": np.arange(tris.shape[0], dtype=np.int32).reshape(-1, 3)})
+    o = np.array([case["origin"]], np.float32)
+    d = np.array([case["dir"]], np.float32)
+    ids, t, _, _ = gpu_closest(rtlib, sc, o, d)
+    if "nearest" in case:
+        assert ids[0] == case["nearest"]
+    if "distance" in case:
+        assert abs(t[0] - case["distance"]) <= abs(case["distance"]) * k["tolerance_percent"] / 100.0
+    if "nearer" in case:
+        occ = sc.any(rtlib.rays_array(o, d, np.float32(case["nearer_t"])))
+        assert bool(occ[0]) == case["nearer"]
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+def test_reference_outputs_gpu(rtlib, ctx, golden, key):
+    """Hits and pixels of the reference's own bvh + ray_tracer() on small
+    seeded scenes (tests/golden/ref_small.npz)."""
+    g = golden
+    frame = json.loads(bytes(g[f"{key}_frame"]).decode())
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"]}
+    sc = rtlib.Scene(ctx, scene)
+    o, d = g[f"{key}_ray_o"], g[f"{key}_ray_d"]
+    ids, t, u, v = gpu_closest(rtlib, sc, o, d)
+    ref_ids, ref_t = g[f"{key}_id"], g[f"{key}_t"]
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], o, d, ids, t, ref_ids, ref_t)
+    assert not mismatch.any(), np.nonzero(mismatch)
+    same = (ids == ref_ids) & (ids >= 0)
+    # same arithmetic as triangle::is_intersecting: distances and barycentrics bit-identical
+    assert np.array_equal(t[same].view(np.uint32), ref_t[same].view(np.uint32))
+    assert np.array_equal(u[same].view(np.uint32), g[f"{key}_u"][same].view(np.uint32))
+    out = sc.render(frame, want_ids=True)
+    assert np.array_equal(out["ids"].reshape(-1), ids)
+    keep = ~excluded.reshape(out["rgb"].shape[:2])
+    within1, exact, _ = pixel_agreement(out["rgb"][keep], g[f"{key}_rgb"][keep])
+    assert within1 >= PIX_FRAC
+    assert exact >= 0.99
+
+
+def test_soup_gpu(rtlib, ctx, golden):
+    g = golden
+    scene = {"verts": g["soup_verts"], "tris": g["soup_tris"], "flags": g["soup_flags"]}
+    sc = rtlib.Scene(ctx, scene)
+    o, d = g["soup_ray_o"], g["soup_ray_d"]
+    ids, t, u, v = gpu_closest(rtlib, sc, o, d)
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], o, d, ids, t, g["soup_id"], g["soup_t"])
+    assert not mismatch.any()
+    occ = sc.any(rtlib.rays_array(o, d, g["soup_tmax"]))
+    # occlusion exact except rays with a near-edge hit
+    near = edge_distance(scene["verts"], scene["tris"], g["soup_id"], o, d) < 1e-5
+    assert np.array_equal(occ[~near], g["soup_occ"][~near])
+
+
+@pytest.fixture(scope="module")
+def c1(oracle):
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene()
+    return scene, frame, oracle.OracleScene(scene)
+
+
+def test_c1_closest_vs_oracle(rtlib, ctx, oracle, c1):
+    """Icosphere 20,480 + 2 triangles, 512x512 primary rays."""
+    scene, frame, osc = c1
+    assert scene["tris"].shape[0] == 20482
+    o, d = oracle.camera_rays(frame["camera"])
+    sc = rtlib.Scene(ctx, scene)
+    ids, t, u, v = gpu_closest(rtlib, sc, o, d)
+    rid, rt_, ru, rv = osc.closest(o, d)
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], o, d, ids, t, rid, rt_)
+    assert not mismatch.any(), np.nonzero(mismatch)[0][:10]
+    assert excluded.mean() < 1e-3
+    same = (ids == rid) & (ids >= 0)
+    assert np.array_equal(t[same].view(np.uint32), rt_[same].view(np.uint32))
+    assert 0.3 < (ids >= 0).mean() < 0.9
+
+
+def test_c1_render_vs_oracle(rtlib, ctx, oracle, c1):
+    scene, frame, osc = c1
+    sc = rtlib.Scene(ctx, scene)
+    out = sc.render(frame, want_ids=True)
+    ref = osc.render(frame, want_ids=True)
+    st = out["stats"]
+    assert st.primary_rays == 512 * 512
+    assert st.secondary_rays == st.primary_hits == int((ref["ids"] >= 0).sum())
+    within1, exact, maxd = pixel_agreement(out["rgb"], ref["rgb"])
+    assert within1 >= PIX_FRAC, (within1, exact, maxd)
+    assert exact >= 0.999
+    # id maps agree except ties / near-edge rays
+    o, d = oracle.camera_rays(frame["camera"])
+    gi, ri = out["ids"].reshape(-1), ref["ids"].reshape(-1)
+    near = (edge_distance(scene["verts"], scene["tris"], gi, o, d) < 1e-5) | \
+           (edge_distance(scene["verts"], scene["tris"], ri, o, d) < 1e-5)
+    assert np.array_equal(gi[~near], ri[~near])
+
+
+def test_render_deterministic(rtlib, ctx, c1):
+    scene, frame, _ = c1
+    sc = rtlib.Scene(ctx, scene)
+    a = sc.render(frame)["rgb"].copy()
+    sc.build()
+    b = sc.render(frame)["rgb"]
+    assert np.array_equal(a, b)
+
+
+# ------------------------------------------------------------- edge cases
+
+def test_empty_scene(rtlib, ctx):
+    sc = rtlib.Scene(ctx, {"verts": np.zeros((0, 3), np.float32), "tris": np.zeros((0, 3), np.int32)})
+    o = np.zeros((5, 3), np.float32)
+    d = np.tile(np.array([[0, 0, 1]], np.float32), (5, 1))
+    h = sc.closest(rtlib.rays_array(o, d))
+    assert (h["tri"] == -1).all() and (h["t"] == FLT_MAX).all()
+    assert not sc.any(rtlib.rays_array(o, d, np.float32(10))).any()
+
+
+def test_single_triangle_and_epsilon(rtlib, ctx):
+    v = np.array([[0, 0, 1], [1, 0, 1], [0, 1, 1]], np.float32)
+    sc = rtlib.Scene(ctx, {"verts": v, "tris": np.array([[0, 1, 2]], np.int32)})
+    o = np.array([[0.2, 0.2, 0.0], [0.2, 0.2, 0.9995], [0.2, 0.2, 2.0], [2, 2, 0]], np.float32)
+    d = np.array([[0, 0, 1]] * 4, np.float32)
+    h = sc.closest(rtlib.rays_array(o, d))
+    assert h["tri"][0] == 0 and abs(h["t"][0] - 1.0) < 1e-6
+    assert h["tri"][1] == -1          # t = 5e-4 <= EPSILON: not accepted (triangle.h:229)
+    assert h["tri"][2] == -1 and h["tri"][3] == -1
+
+
+def test_ties_lowest_id(rtlib, ctx):
+    """Duplicate triangles: the lowest id wins among equal distances."""
+    base = np.array([[0, 0, 1], [1, 0, 1], [0, 1, 1]], np.float32)
+    v = np.tile(base, (50, 1))
+    t = np.arange(150, dtype=np.int32).reshape(-1, 3)
+    sc = rtlib.Scene(ctx, {"verts": v, "tris": t[::-1].copy()})
+    o = np.random.default_rng(0).uniform(0.05, 0.4, (64, 3)).astype(np.float32)
+    o[:, 2] = 0
+    d = np.tile(np.array([[0, 0, 1]], np.float32), (64, 1))
+    h = sc.closest(rtlib.rays_array(o, d))
+    assert (h["tri"] == 0).all()
+
+
+def test_degenerate_triangles_never_hit(rtlib, ctx):
+    v = np.array([[0, 0, 1], [1, 0, 1], [2, 0, 1], [0, 0, 2], [0, 0, 2], [0, 0, 2]], np.float32)
+    sc = rtlib.Scene(ctx, {"verts": v, "tris": np.array([[0, 1, 2], [3, 4, 5]], np.int32)})
+    rng = np.random.default_rng(1)
+    o = rng.uniform(-1, 3, (256, 3)).astype(np.float32)
+    d = rng.normal(size=(256, 3)).astype(np.float32)
+    h = sc.closest(rtlib.rays_array(o, d))
+    assert (h["tri"] == -1).all()
+
+
+def test_light_and_transparent_skipped_by_any_hit(rtlib, ctx):
+    v = np.array([[-1, -1, 1], [1, -1, 1], [0, 1, 1]] * 3, np.float32)
+    v[3:6, 2] = 2
+    v[6:9, 2] = 3
+    t = np.arange(9, dtype=np.int32).reshape(3, 3)
+    flags = np.array([1, 2, 0], np.uint32)
+    sc = rtlib.Scene(ctx, {"verts": v, "tris": t, "flags": flags})
+    o = np.zeros((3, 3), np.float32)
+    d = np.tile(np.array([[0, 0, 1]], np.float32), (3, 1))
+    occ = sc.any(rtlib.rays_array(o, d, np.array([2.5, 3.5, 0.5], np.float32)))
+    assert list(occ) == [0, 1, 0]
+    h = sc.closest(rtlib.rays_array(o, d))   # closest hit ignores the flags
+    assert (h["tri"] == 0).all()
+
+
+def test_axis_aligned_rays_and_zero_components(rtlib, ctx, oracle):
+    """Rays with exactly-zero direction components through a plane of
+    triangles lying in an axis plane (zero-thickness boxes)."""
+    from raptor_gb300 import scenes
+    h = scenes.diamond_square(16, 0.0, 5) * 0.0
+    v, t, _ = scenes.heightfield_mesh(h, 16.0, 0.0)
+    scene = {"verts": v.astype(np.float32), "tris": t}
+    sc = rtlib.Scene(ctx, scene)
+    xs, zs = np.meshgrid(np.linspace(0.05, 15.95, 40), np.linspace(0.05, 15.95, 40))
+    o = np.stack([xs.ravel(), np.full(xs.size, 5.0), zs.ravel()], 1).astype(np.float32)
+    d = np.tile(np.array([[0, -1, 0]], np.float32), (o.shape[0], 1))
+    ids, tt, _, _ = gpu_closest(rtlib, sc, o, d)
+    osc = oracle.OracleScene(scene)
+    rid, rtt, _, _ = osc.closest(o, d)
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], o, d, ids, tt, rid, rtt)
+    assert not mismatch.any()
+    assert (ids >= 0).all() and np.allclose(tt, 5.0)
+
+
+def test_host_and_device_buffers_agree(rtlib, ctx, c1):
+    torch = pytest.importorskip("torch")
+    scene, frame, _ = c1
+    sc = rtlib.Scene(ctx, scene)
+    W, H = frame["camera"]["xres"], frame["camera"]["yres"]
+    dev = torch.empty((H, W, 3), dtype=torch.uint8, device="cuda")
+    sc.render(frame, rgb=dev)
+    host = sc.render(frame)["rgb"]
+    assert np.array_equal(dev.cpu().numpy(), host)
+
+
+def test_errors_are_codes_not_crashes(rtlib, ctx):
+    sc = rtlib.Scene(ctx)
+    with pytest.raises(rtlib.RtError) as e:
+        sc.closest(rtlib.rays_array(np.zeros((1, 3), np.float32), np.ones((1, 3), np.float32)))
+    assert e.value.code == -4          # not built
+    with pytest.raises(rtlib.RtError) as e:
+        sc.upload(np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.int32))
+    assert e.value.code == -1          # index out of range

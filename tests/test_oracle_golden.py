@@ -1,0 +1,135 @@
+"""Pins the C restatement (oracle/rtoracle.c) to the reference: its own
+known-answer tests (parsed from raytracer/unit_tests/bih_tests.cc and
+vint_tests.cc) and outputs of the reference compiled from source
+(tests/golden/ref_small.npz, written by tests/golden/make_golden.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from parity import PIX_FRAC, compare_hits, pixel_agreement
+
+FLT_MAX = np.float32(3.4028234663852886e38)
+
+
+def load_kats():
+    return json.load(open(os.path.join(GOLDEN, "bih_kats.json")))
+
+
+def fixture_scene(kats, axis):
+    tris = np.array(kats["tris"][axis], np.float32).reshape(-1, 3)
+    idx = np.arange(tris.shape[0], dtype=np.int32).reshape(-1, 3)
+    return {"verts": tris, "tris": idx, "vattr": None, "flags": None}
+
+
+def test_morton_kats(oracle):
+    kats = json.load(open(os.path.join(GOLDEN, "morton_kats.json")))
+    assert len(kats["cases"]) == 12
+    for c in kats["cases"]:
+        got = oracle.morton(c["x"], c["y"], c["z"], c["x_mul"], c["y_mul"], c["z_mul"])
+        assert got == c["expected"], (c["name"], hex(got), hex(c["expected"]))
+
+
+@pytest.mark.parametrize("case", load_kats()["cases"], ids=lambda c: c["name"])
+def test_bih_kats(oracle, case):
+    kats = load_kats()
+    sc = oracle.OracleScene(fixture_scene(kats, case["fixture"]))
+    o = np.array([case["origin"]], np.float32)
+    d = np.array([case["dir"]], np.float32)
+    ids, t, _, _ = sc.closest(o, d)
+    if "nearest" in case:
+        assert ids[0] == case["nearest"]
+    if "distance" in case:
+        # BOOST_CHECK_CLOSE tolerance is a percentage
+        assert abs(t[0] - case["distance"]) <= abs(case["distance"]) * kats["tolerance_percent"] / 100.0
+    if "nearer" in case:
+        occ = sc.any(o, d, case["nearer_t"])
+        assert bool(occ[0]) == case["nearer"]
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(os.path.join(GOLDEN, "ref_small.npz"))
+
+
+def frame_of(g, key):
+    return json.loads(bytes(g[f"{key}_frame"]).decode())
+
+
+def tie_mask(ids_a, ids_b, t_a, t_b):
+    """Rays whose ids differ but whose distances are bit-identical: exact
+    ties, where the reference keeps whichever triangle it met first."""
+    return (ids_a != ids_b) & (t_a.view(np.uint32) == t_b.view(np.uint32))
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+def test_oracle_matches_reference_outputs(oracle, golden, key):
+    g = golden
+    frame = frame_of(g, key)
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"], "flags": None}
+    og, dr = oracle.camera_rays(frame["camera"])
+    # primary rays: bit-identical to the reference camera
+    assert np.array_equal(og.view(np.uint32), g[f"{key}_ray_o"].view(np.uint32))
+    assert np.array_equal(dr.view(np.uint32), g[f"{key}_ray_d"].view(np.uint32))
+    sc = oracle.OracleScene(scene)
+    ids, t, u, v = sc.closest(og, dr)
+    ref_ids, ref_t = g[f"{key}_id"], g[f"{key}_t"]
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], og, dr, ids, t, ref_ids, ref_t)
+    assert not mismatch.any(), np.nonzero(mismatch)
+    assert excluded.mean() < 0.01
+    # where the ids agree the distances are bit-identical (same arithmetic)
+    same = ids == ref_ids
+    assert np.array_equal(t[same].view(np.uint32), ref_t[same].view(np.uint32))
+    out = sc.render(frame, want_ids=True)
+    # pixels of compared (non-excluded) rays: within 1 LSB on >= 99.9%;
+    # where the ids agree the oracle's shading is the reference's, bit for bit
+    keep = ~excluded.reshape(out["rgb"].shape[:2])
+    within1, exact, _ = pixel_agreement(out["rgb"][keep], g[f"{key}_rgb"][keep])
+    assert within1 >= PIX_FRAC
+    diff = np.abs(out["rgb"].astype(int) - g[f"{key}_rgb"].astype(int)).max(axis=-1)
+    assert (diff[same.reshape(diff.shape)] == 0).all()
+
+
+def test_oracle_soup_closest_and_any(oracle, golden):
+    g = golden
+    scene = {"verts": g["soup_verts"], "tris": g["soup_tris"], "vattr": None, "flags": g["soup_flags"]}
+    sc = oracle.OracleScene(scene)
+    ids, t, u, v = sc.closest(g["soup_ray_o"], g["soup_ray_d"])
+    mismatch, _ = compare_hits(scene["verts"], scene["tris"], g["soup_ray_o"], g["soup_ray_d"], ids, t,
+                               g["soup_id"], g["soup_t"])
+    assert not mismatch.any()
+    hit = (ids >= 0) & (ids == g["soup_id"])
+    assert np.array_equal(t[hit].view(np.uint32), g["soup_t"][hit].view(np.uint32))
+    assert np.array_equal(u[hit].view(np.uint32), g["soup_u"][hit].view(np.uint32))
+    occ = sc.any(g["soup_ray_o"], g["soup_ray_d"], g["soup_tmax"])
+    assert np.array_equal(occ, g["soup_occ"])
+    assert 0.05 < occ.mean() < 0.95
+
+
+def test_philox_known_answers(oracle):
+    # Known-answer vectors of Philox4x32-10 published with Random123
+    # (Salmon et al., SC'11): zero, all-ones, and pi-digit counters/keys.
+    assert [hex(x) for x in oracle.philox([0, 0, 0, 0], 0, 0)] == \
+        ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(x) for x in oracle.philox([0xffffffff] * 4, 0xffffffff, 0xffffffff)] == \
+        ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(x) for x in oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], 0xa4093822,
+                                          0x299f31d0)] == ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_ao_rays_hemisphere(oracle):
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        n = rng.normal(size=3)
+        n = (n / np.linalg.norm(n)).astype(np.float32)
+        p = rng.uniform(-10, 10, 3).astype(np.float32)
+        o, d = oracle.ao_rays(p, n, int(rng.integers(0, 1 << 20)), 16, 5)
+        assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-6)
+        assert (d @ n >= -1e-6).all()
+        assert np.array_equal(o[0], o[-1])
+    # cosine weighting: E[cos] = 2/3 for a cosine-weighted hemisphere
+    n = np.array([0, 0, 1], np.float32)
+    cos = np.concatenate([oracle.ao_rays(np.zeros(3, np.float32), n, i, 64, 9)[1][:, 2] for i in range(200)])
+    assert abs(cos.mean() - 2.0 / 3.0) < 0.01
