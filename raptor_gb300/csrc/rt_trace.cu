@@ -139,6 +139,10 @@ __global__ void __launch_bounds__(kTraceThreads) k_render(SceneView sc, CameraVi
         warp_count(&ctr->hits, hit);
         warp_add(&ctr->secondary, shadow_rays);
     }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
     if (status) atomicOr(&ctr->status, status);
 }
 
