@@ -203,6 +203,61 @@ rt_status rt_render_ao(rt_scene *scene, const rt_camera *camera, const rt_materi
                        float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
                        rt_render_stats *stats);
 
+/* ------------------------------------------------------------ batches */
+
+/* A batch renders many scenes (own hierarchy, resolution and ray mix each)
+ * in ONE persistent launch fed by a device work queue of 32-pixel tiles,
+ * replayed from a captured CUDA graph.  No reference counterpart: the
+ * reference renders one scene per ray_tracer() call (raytracer.cc:563). */
+typedef struct rt_batch rt_batch;
+
+#define RT_JOB_SHADOW 0        /* primary + one shadow ray per light, Phong */
+#define RT_JOB_AO 1            /* primary + ao_samples AO rays, AO shading */
+#define RT_MAX_JOB_LIGHTS 2
+typedef struct rt_job {
+    int32_t scene;             /* index from rt_batch_add_scene */
+    int32_t mode;              /* RT_JOB_SHADOW or RT_JOB_AO */
+    rt_camera camera;
+    int32_t nlights;           /* RT_JOB_SHADOW: 0..RT_MAX_JOB_LIGHTS */
+    rt_light lights[RT_MAX_JOB_LIGHTS];
+    rt_material material;
+    int32_t ao_samples;        /* RT_JOB_AO: 1..64 */
+    float ao_dist;
+    uint32_t ao_seed;
+    uint8_t *rgb_out;          /* DEVICE memory, xres*yres*3 */
+    int32_t *hit_ids;          /* DEVICE memory or NULL */
+} rt_job;
+
+/* Launch shape of the batched kernel, chosen by rt_batch_autotune:
+ * threads per block (64/128/256), tiles claimed per queue access (1..16),
+ * tile width (8 -> 8x4 tiles, 16 -> 16x2), and the measured ms per frame. */
+typedef struct rt_tune_config {
+    int32_t block_threads;
+    int32_t chunk_tiles;
+    int32_t tile_w;
+    float ms;
+} rt_tune_config;
+
+rt_status rt_batch_create(rt_context *ctx, rt_batch **out);
+rt_status rt_batch_destroy(rt_batch *batch);
+/* Add a scene (same arguments as rt_scene_upload); scene_index receives its
+ * index.  Up to 1024 scenes, 2^28 triangles in total. */
+rt_status rt_batch_add_scene(rt_batch *batch, const float *verts_xyz, int32_t nverts, const int32_t *tri_idx,
+                             int32_t ntris, const float *vert_attr, const uint32_t *tri_flags, int32_t *scene_index);
+/* Build every scene's hierarchy in one batched LBVH pass. */
+rt_status rt_bvh_build_batched(rt_batch *batch, float *build_ms);
+/* Set the frames to render (re-captures the graph). */
+rt_status rt_batch_set_jobs(rt_batch *batch, const rt_job *jobs, int32_t njobs);
+/* Render all jobs: one graph launch on the context's stream.  With stats ==
+ * NULL the call returns without waiting; otherwise it waits and fills
+ * stats (device_ms = graph time). */
+rt_status rt_render_batched(rt_batch *batch, rt_render_stats *stats);
+/* Time every launch shape on the current jobs (reps graph replays each) and
+ * keep the fastest; best (nullable) receives it. */
+rt_status rt_batch_autotune(rt_batch *batch, int32_t reps, rt_tune_config *best);
+rt_status rt_batch_set_config(rt_batch *batch, const rt_tune_config *config);
+rt_status rt_batch_get_config(const rt_batch *batch, rt_tune_config *config);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,21 @@ class RtRenderStats(C.Structure):
                 ("tris_tested", C.c_int64)]
 
 
+RT_JOB_SHADOW = 0
+RT_JOB_AO = 1
+RT_MAX_JOB_LIGHTS = 2
+
+
+class RtJob(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("mode", C.c_int32), ("camera", RtCamera), ("nlights", C.c_int32),
+                ("lights", RtLight * RT_MAX_JOB_LIGHTS), ("material", RtMaterial), ("ao_samples", C.c_int32),
+                ("ao_dist", C.c_float), ("ao_seed", C.c_uint32), ("rgb_out", C.c_void_p), ("hit_ids", C.c_void_p)]
+
+
+class RtTuneConfig(C.Structure):
+    _fields_ = [("block_threads", C.c_int32), ("chunk_tiles", C.c_int32), ("tile_w", C.c_int32), ("ms", C.c_float)]
+
+
 # numpy views of the C structs
 RAY_DTYPE = np.dtype([("o", np.float32, 3), ("tmax", np.float32), ("d", np.float32, 3), ("pad", np.float32)])
 HIT_DTYPE = np.dtype([("tri", np.int32), ("t", np.float32), ("u", np.float32), ("v", np.float32)])
@@ -92,6 +107,15 @@ SIGNATURES = [
                               C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
                                  _P, _P, _P, C.POINTER(RtRenderStats)]),
+    ("rt_batch_create", C.c_int32, [_P, C.POINTER(C.c_void_p)]),
+    ("rt_batch_destroy", C.c_int32, [_P]),
+    ("rt_batch_add_scene", C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
+    ("rt_bvh_build_batched", C.c_int32, [_P, C.POINTER(C.c_float)]),
+    ("rt_batch_set_jobs", C.c_int32, [_P, C.POINTER(RtJob), C.c_int32]),
+    ("rt_render_batched", C.c_int32, [_P, C.POINTER(RtRenderStats)]),
+    ("rt_batch_autotune", C.c_int32, [_P, C.c_int32, C.POINTER(RtTuneConfig)]),
+    ("rt_batch_set_config", C.c_int32, [_P, C.POINTER(RtTuneConfig)]),
+    ("rt_batch_get_config", C.c_int32, [_P, C.POINTER(RtTuneConfig)]),
 ]
 
 
@@ -261,6 +285,88 @@ class Scene:
     def close(self):
         if self.h:
             lib().rt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_job(scene_index, frame, rgb_dev, ids_dev=None) -> RtJob:
+    """Job for one frame dict (scenes.* format) rendering into device buffers."""
+    j = RtJob()
+    j.scene = scene_index
+    j.camera = make_camera(frame["camera"])
+    j.material = make_material(frame["material"])
+    ao = frame.get("ao")
+    if ao:
+        j.mode = RT_JOB_AO
+        j.ao_samples, j.ao_dist, j.ao_seed = ao["samples"], ao["dist"], ao["seed"]
+        j.nlights = 0
+    else:
+        j.mode = RT_JOB_SHADOW
+        ls = frame["lights"]
+        if len(ls) > RT_MAX_JOB_LIGHTS:
+            raise ValueError("too many lights for a batch job")
+        j.nlights = len(ls)
+        arr = make_lights(ls)
+        for i in range(len(ls)):
+            j.lights[i] = arr[i]
+    j.rgb_out = ptr(rgb_dev).value
+    j.hit_ids = ptr(ids_dev).value if ids_dev is not None else None
+    return j
+
+
+class Batch:
+    """Many scenes in one persistent, graph-captured launch."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(lib().rt_batch_create(ctx.h, C.byref(h)))
+        self.h = h
+        self._keep = []
+        self.build_ms = None
+
+    def add_scene(self, scene) -> int:
+        idx = C.c_int32()
+        v, t = scene["verts"], scene["tris"]
+        a, f = scene.get("vattr"), scene.get("flags")
+        self._keep.append((v, t, a, f))
+        _check(lib().rt_batch_add_scene(self.h, ptr(v), int(v.shape[0]), ptr(t), int(t.shape[0]), ptr(a), ptr(f),
+                                        C.byref(idx)))
+        return idx.value
+
+    def build(self) -> float:
+        ms = C.c_float()
+        _check(lib().rt_bvh_build_batched(self.h, C.byref(ms)))
+        self.build_ms = ms.value
+        return ms.value
+
+    def set_jobs(self, jobs):
+        arr = (RtJob * max(1, len(jobs)))(*jobs)
+        self._jobs = arr
+        _check(lib().rt_batch_set_jobs(self.h, arr, len(jobs)))
+
+    def render(self, stats=True):
+        st = RtRenderStats()
+        _check(lib().rt_render_batched(self.h, C.byref(st) if stats else None))
+        return st
+
+    def autotune(self, reps=3):
+        cfg = RtTuneConfig()
+        _check(lib().rt_batch_autotune(self.h, reps, C.byref(cfg)))
+        return {"block_threads": cfg.block_threads, "chunk_tiles": cfg.chunk_tiles, "tile_w": cfg.tile_w, "ms": cfg.ms}
+
+    def set_config(self, block_threads=128, chunk_tiles=1, tile_w=8):
+        cfg = RtTuneConfig(block_threads, chunk_tiles, tile_w, 0.0)
+        _check(lib().rt_batch_set_config(self.h, C.byref(cfg)))
+
+    def close(self):
+        if self.h:
+            lib().rt_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -152,6 +152,8 @@ SceneView scene_view(const rt_scene *s)
     v.flags = s->d_flags;
     v.ntris = s->ntris;
     v.nnodes = s->built ? s->nnodes : 0;
+    v.root = 0;
+    v.tri_base = 0;
     return v;
 }
 

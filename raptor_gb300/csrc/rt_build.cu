@@ -10,6 +10,8 @@
 // depend on the tree, so a different tree gives the same closest hits.
 #include <cub/device/device_radix_sort.cuh>
 
+#include <vector>
+
 #include "rt_build.cuh"
 
 namespace rtc {
@@ -25,9 +27,11 @@ __device__ __forceinline__ float of_ord(int i) { return __int_as_float((i >= 0) 
 
 // Per triangle (caller's order): shading record (face normal exactly as
 // triangle.h:171-175, vertex c), bounding box, centroid bounds.
+// With several segments (scenes of a batch) the centroid bounds are kept per
+// segment: cbounds[6 * s + k] (k < 3 minimum, k >= 3 maximum).
 __global__ void k_prep(const float *__restrict__ verts, const int3 *__restrict__ idx, int32_t n,
-                       ShadeTri *__restrict__ shade, float4 *__restrict__ blo, float4 *__restrict__ bhi,
-                       int *__restrict__ cbounds)
+                       const int32_t *__restrict__ seg, int32_t nseg, ShadeTri *__restrict__ shade,
+                       float4 *__restrict__ blo, float4 *__restrict__ bhi, int *__restrict__ cbounds)
 {
     __shared__ int s_min[3][32], s_max[3][32];
     float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
@@ -47,9 +51,16 @@ __global__ void k_prep(const float *__restrict__ verts, const int3 *__restrict__
         blo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
         bhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
         const float cc[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+        if (nseg > 1) {
+            int *cb = cbounds + 6 * seg[i];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) { cmin[k] = fminf(cmin[k], cc[k]); cmax[k] = fmaxf(cmax[k], cc[k]); }
+            for (int k = 0; k < 3; ++k) { atomicMin(&cb[k], ord_of(cc[k])); atomicMax(&cb[3 + k], ord_of(cc[k])); }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { cmin[k] = fminf(cmin[k], cc[k]); cmax[k] = fmaxf(cmax[k], cc[k]); }
+        }
     }
+    if (nseg > 1) return;
     // warp then block reduction of the centroid bounds
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -84,28 +95,29 @@ __device__ __forceinline__ uint64_t expand21(uint32_t v)
     return x;
 }
 
-// 63-bit Morton code (21 bits per axis) of each box centre over the
-// centroid bounds; the sort breaks equal codes by triangle index.
+// Morton code of each box centre over its segment's centroid bounds, with
+// the segment id above it: key = seg << (3 * mbits) | morton (mbits bits per
+// axis; 21 for a single scene).  The sort breaks equal keys by index.
 __global__ void k_morton(const float4 *__restrict__ blo, const float4 *__restrict__ bhi, int32_t n,
-                         const int *__restrict__ cbounds, uint64_t *__restrict__ keys, int32_t *__restrict__ vals)
+                         const int32_t *__restrict__ seg, int32_t nseg, int mbits, const int *__restrict__ cbounds,
+                         uint64_t *__restrict__ keys, int32_t *__restrict__ vals)
 {
-    float lo[3], sc[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        lo[k] = of_ord(cbounds[k]);
-        const float ext = of_ord(cbounds[3 + k]) - lo[k];
-        sc[k] = (ext > 0.f) ? 2097151.0f / ext : 0.f;
-    }
+    const float qmax = (float)((1u << mbits) - 1u);
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int32_t s = (nseg > 1) ? seg[i] : 0;
+        const int *cb = cbounds + 6 * s;
         const float4 a = blo[i], b = bhi[i];
         const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
         uint32_t q[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const float f = fminf(fmaxf((c[k] - lo[k]) * sc[k], 0.f), 2097151.0f);
-            q[k] = (uint32_t)f;
+            const float lo = of_ord(cb[k]);
+            const float ext = of_ord(cb[3 + k]) - lo;
+            const float sc = (ext > 0.f) ? qmax / ext : 0.f;
+            q[k] = (uint32_t)fminf(fmaxf((c[k] - lo) * sc, 0.f), qmax);
         }
-        keys[i] = expand21(q[0]) | (expand21(q[1]) << 1) | (expand21(q[2]) << 2);
+        const uint64_t m = expand21(q[0]) | (expand21(q[1]) << 1) | (expand21(q[2]) << 2);
+        keys[i] = ((uint64_t)s << (3 * mbits)) | m;
         vals[i] = i;
     }
 }
@@ -188,6 +200,38 @@ __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32
         __stcg(&ihi[p], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f));
         p = parent[p];
     }
+}
+
+// Root of each segment: the binary node whose range is exactly the
+// segment's sorted range (the lowest common ancestor of its first and last
+// leaves; keys of one segment share the segment-id prefix).  Emits one
+// collapse task per non-empty segment and an empty wide node per empty one.
+__global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg_first,
+                        const int32_t *__restrict__ first, const int32_t *__restrict__ last,
+                        const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
+                        int2 *__restrict__ tasks, int32_t *counters, WideNode *__restrict__ nodes)
+{
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    const int32_t f = seg_first[s], l = seg_first[s + 1] - 1;
+    if (l < f) {
+        WideNode W;
+        memset(&W, 0, sizeof(W));
+        for (int k = 0; k < 8; ++k) { W.qlo_x[k] = W.qlo_y[k] = W.qlo_z[k] = 255; }
+        nodes[s] = W;
+        return;
+    }
+    int32_t root = ~f;
+    if (l > f) {
+        int32_t p = leaf_parent[f];
+        int guard = 0;
+        while (p >= 0 && !(first[p] <= f && last[p] >= l) && guard++ < 128) p = parent[p];
+        if (p < 0 || first[p] != f || last[p] != l) { atomicExch(&counters[3], 1); return; }
+        root = p;
+    }
+    const int slot = atomicAdd(&counters[2], 1);
+    tasks[slot] = make_int2(root, s);
+    (void)n;
 }
 
 __device__ __forceinline__ float half_area(float4 lo, float4 hi)
@@ -404,7 +448,8 @@ size_t build_temp_bytes(int32_t n)
     b += 4 * nn * sizeof(float4);          // llo lhi ilo ihi
     b += nn * sizeof(int32_t);             // refit flags
     b += 2 * nn * sizeof(int2);            // task queues
-    b += 64 * sizeof(int32_t);             // counters, bounds
+    b += 16 * sizeof(int32_t) + 2 * nn * sizeof(int2);   // counters, root tasks
+    b += (6 + 1) * (size_t)kMaxSegments * sizeof(int) + 1024;
     b += cub_bytes + 16 * 256;
     return b;
 }
@@ -420,8 +465,10 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
 {
     BuildResult R;
     const int32_t n = in.ntris;
-    if (n <= 0) { R.status = 0; return R; }
-    const size_t nn = (size_t)n;
+    const int32_t nseg = in.nseg > 0 ? in.nseg : 1;
+    if (nseg > kMaxSegments) { R.status = -1; return R; }
+    if (n <= 0 && nseg == 1) { R.status = 0; return R; }
+    const size_t nn = (size_t)(n > 0 ? n : 1);
     char *p = (char *)temp;
     float4 *blo = (float4 *)carve(p, nn * sizeof(float4));
     float4 *bhi = (float4 *)carve(p, nn * sizeof(float4));
@@ -440,32 +487,55 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     float4 *ilo = (float4 *)carve(p, nn * sizeof(float4));
     float4 *ihi = (float4 *)carve(p, nn * sizeof(float4));
     int32_t *rflags = (int32_t *)carve(p, nn * sizeof(int32_t));
-    int2 *tq0 = (int2 *)carve(p, nn * sizeof(int2));
-    int2 *tq1 = (int2 *)carve(p, nn * sizeof(int2));
-    int32_t *counters = (int32_t *)carve(p, 64 * sizeof(int32_t));
-    int *cbounds = counters + 16;
+    int2 *tq0 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
+    int2 *tq1 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
+    int32_t *counters = (int32_t *)carve(p, 16 * sizeof(int32_t));
+    int *cbounds = (int *)carve(p, 6 * (size_t)nseg * sizeof(int));
+    int32_t *seg_first = (int32_t *)carve(p, ((size_t)nseg + 1) * sizeof(int32_t));
     size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys2, vals, vals2, (int)nn, 0, 64, st);
     void *cub_temp = carve(p, cub_bytes);
     if ((size_t)(p - (char *)temp) > temp_bytes) { R.status = -3; return R; }
 
-    const int init_bounds[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000, (int)0x80000000};
+    // segment offsets (sorted positions of each segment = its triangle range)
+    int32_t *h_cnt = in.host_scratch;   // pinned, >= 4 ints
+    std::vector<int> init_bounds(6 * (size_t)nseg);
+    for (int s = 0; s < nseg; ++s)
+        for (int k = 0; k < 3; ++k) { init_bounds[6 * s + k] = 0x7fffffff; init_bounds[6 * s + 3 + k] = (int)0x80000000; }
     cudaMemsetAsync(counters, 0, 16 * sizeof(int32_t), st);
-    cudaMemcpyAsync(cbounds, init_bounds, sizeof(init_bounds), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(cbounds, init_bounds.data(), init_bounds.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (nseg > 1) {
+        cudaMemcpyAsync(seg_first, in.seg_first, ((size_t)nseg + 1) * sizeof(int32_t), cudaMemcpyDefault, st);
+    } else {
+        const int32_t sf[2] = {0, n};
+        cudaMemcpyAsync(seg_first, sf, sizeof(sf), cudaMemcpyHostToDevice, st);
+    }
+    int sb = 0;
+    while ((1 << sb) < nseg) ++sb;
+    const int mbits = (63 - sb) / 3;
     const int threads = 256;
-    const int grid_pts = min((n + threads - 1) / threads, in.sm_count * 8);
-    k_prep<<<grid_pts, threads, 0, st>>>(in.verts, in.idx, n, in.shade, blo, bhi, cbounds);
-    k_morton<<<grid_pts, threads, 0, st>>>(blo, bhi, n, cbounds, keys, vals);
-    cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
-    const int g = (n + threads - 1) / threads;
-    if (n > 1) {
-        k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, parent, leaf_parent);
+    if (n > 0) {
+        const int grid_pts = min((n + threads - 1) / threads, in.sm_count * 8);
+        k_prep<<<grid_pts, threads, 0, st>>>(in.verts, in.idx, n, in.seg_of_tri, nseg, in.shade, blo, bhi, cbounds);
+        k_morton<<<grid_pts, threads, 0, st>>>(blo, bhi, n, in.seg_of_tri, nseg, mbits, cbounds, keys, vals);
+        cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
+        const int g = (n + threads - 1) / threads;
+        if (n > 1) k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, parent, leaf_parent);
+        k_leaf_boxes<<<g, threads, 0, st>>>(vals2, n, blo, bhi, llo, lhi);
+        if (n > 1) {
+            cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
+            k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
+        }
     }
-    k_leaf_boxes<<<g, threads, 0, st>>>(vals2, n, blo, bhi, llo, lhi);
-    if (n > 1) {
-        cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
-        k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
-    }
+    // segment roots -> level-0 tasks; wide nodes 0..nseg-1 are the roots
+    k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0, counters,
+                                                in.nodes);
+    const int32_t nroot_nodes = nseg;
+    cudaMemcpyAsync(&counters[0], &nroot_nodes, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+    if (h_cnt[3]) { R.status = -8; return R; }
+    int32_t ntasks = h_cnt[2], depth = 0;
 
     BuildArgs A;
     A.n = n; A.left = left; A.right = right; A.first = first; A.last = last;
@@ -473,13 +543,6 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
     A.max_nodes = in.max_nodes;
-    // root task: binary root (internal 0, or leaf 0 when n == 1) -> wide node 0
-    const int2 root = make_int2(n > 1 ? 0 : ~0, 0);
-    cudaMemcpyAsync(tq0, &root, sizeof(int2), cudaMemcpyHostToDevice, st);
-    const int32_t one = 1;
-    cudaMemcpyAsync(&counters[0], &one, sizeof(int32_t), cudaMemcpyHostToDevice, st);
-    int32_t ntasks = 1, depth = 0;
-    int32_t *h_cnt = in.host_scratch;   // pinned, >= 4 ints
     while (ntasks > 0) {
         if (depth >= kMaxDepth) { R.status = -5; return R; }
         A.tasks_in = (depth & 1) ? tq1 : tq0;

@@ -16,6 +16,13 @@ struct BuildInputs {
     int32_t max_nodes;
     int32_t sm_count;
     int32_t *host_scratch;    // pinned host, >= 4 ints
+    // several scenes in one build (a batch): segment of each triangle and
+    // the triangle offset of each segment (nseg + 1 entries, host or device).
+    // nseg <= 1: a single scene, both may be nullptr.  Segment s's root is
+    // wide node s.
+    int32_t nseg = 1;
+    const int32_t *seg_of_tri = nullptr;
+    const int32_t *seg_first = nullptr;
 };
 
 struct BuildResult {

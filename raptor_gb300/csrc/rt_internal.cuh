@@ -13,6 +13,7 @@ namespace rtc {
 // ---------------------------------------------------------------- limits
 constexpr int kStackSize = 48;          // traversal stack entries (>= max tree depth)
 constexpr int kMaxDepth = 40;           // build fails above this wide-tree depth
+constexpr int kMaxSegments = 1024;   // scenes per batched build
 constexpr int kMaxLeafTris = 3;         // triangles per leaf slot (unary count in 3 bits)
 constexpr float kEpsilon = 1.0e-3f;     // common/common.cc:14
 constexpr float kDetEps = 0.000001f;    // triangle.h:201
@@ -64,6 +65,8 @@ struct SceneView {
     const uint32_t *flags;    // per triangle (caller's order)
     int32_t ntris;
     int32_t nnodes;
+    int32_t root;             // root wide node of this scene
+    int32_t tri_base;         // subtracted from packed ids to give the caller's ids
 };
 
 struct CameraView {

@@ -3,32 +3,11 @@
 // Every kernel runs a fixed grid (a multiple of the SM count) whose warps
 // claim 32 work items at a time from a device counter, so uneven ray costs
 // balance across SMs without a scheduler on the host.
-#include "rt_kernels.cuh"
-#include "rt_traverse.cuh"
+#include "rt_shade.cuh"
 
 namespace rtc {
 
 namespace {
-
-__device__ __forceinline__ int warp_claim(int *counter, int chunk)
-{
-    int base = 0;
-    if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, chunk);
-    return __shfl_sync(0xffffffffu, base, 0);
-}
-
-__device__ __forceinline__ void warp_count(unsigned long long *ctr, bool pred)
-{
-    const uint32_t b = __ballot_sync(0xffffffffu, pred);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(ctr, (unsigned long long)__popc(b));
-}
-
-__device__ __forceinline__ void warp_add(unsigned long long *ctr, uint32_t v)
-{
-    uint32_t s = v;
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
-}
 
 __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(SceneView sc, const rt_ray *__restrict__ rays,
                                                                  int32_t n, rt_hit *__restrict__ hits,
@@ -73,14 +52,6 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_any(SceneView sc, const
 
 }  // namespace
 
-// Pixel of work item `item` in 8x4 tiles (one warp = one tile).
-__device__ __forceinline__ void tile_pixel(int item, int tiles_x, int &x, int &y)
-{
-    const int tile = item >> 5, lane = item & 31;
-    x = (tile % tiles_x) * 8 + (lane & 7);
-    y = (tile / tiles_x) * 4 + (lane >> 3);
-}
-
 namespace {
 
 template <bool COUNT>
@@ -88,56 +59,28 @@ __global__ void __launch_bounds__(kTraceThreads) k_render(SceneView sc, CameraVi
                                                           MaterialView mat, uint8_t *__restrict__ rgb,
                                                           int32_t *__restrict__ ids, Counters *ctr)
 {
-    const int tiles_x = (cam.xres + 7) >> 3, tiles_y = (cam.yres + 3) >> 2;
-    const int items = tiles_x * tiles_y * 32;
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
     uint32_t status = 0;
     FetchCount fc;
     for (;;) {
         const int base = warp_claim(&ctr->work, 32);
         if (base >= items) break;
         int x, y;
-        tile_pixel(base + (threadIdx.x & 31), tiles_x, x, y);
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
         const bool live = (x < cam.xres) && (y < cam.yres);
-        HitRecord h;
-        h.id = -1;
-        h.t = FLT_MAX;
-        RayState r;
-        bool occ;
+        PixelOut po;
+        po.hit = false;
+        po.secondary = 0;
         if (live) {
-            r = camera_ray(cam, x, y);
-            status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, &fc);
-        }
-        const bool hit = live && h.t < FLT_MAX;
-        uint32_t shadow_rays = 0;
-        float3 c = cam.background;
-        if (hit) {
-            const SurfacePoint sp = surface_at(sc, r, h);
-            const float3 start = offset_start(sp.dst, sp.geo);
-            const float3 kd = material_kd(mat, sp);
-            c = make_float3(0.f, 0.f, 0.f);
-            for (int l = 0; l < lights.n; ++l) {
-                const LightView &L = lights.l[l];
-                float3 ldir;
-                float len;
-                shadow_ray(L, start, ldir, len);
-                HitRecord sh;
-                bool blocked;
-                status |= traverse<true, COUNT>(sc, start, ldir, len, sh, blocked, &fc);
-                ++shadow_rays;
-                phong_add(L, mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
-            }
-            c = xadd3(c, mat.ka);
-        }
-        if (live) {
+            po = shade_pixel_lights<COUNT>(sc, cam, lights.l, lights.n, mat, x, y, status, &fc);
             const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
-            rgb[3 * pix] = clip8(c.x);
-            rgb[3 * pix + 1] = clip8(c.y);
-            rgb[3 * pix + 2] = clip8(c.z);
-            if (ids) ids[pix] = hit ? h.id : -1;
+            store_rgb(rgb, pix, po.c);
+            if (ids) ids[pix] = po.id;
         }
         warp_count(&ctr->primary, live);
-        warp_count(&ctr->hits, hit);
-        warp_add(&ctr->secondary, shadow_rays);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
     }
     if (COUNT) {
         atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
@@ -152,54 +95,29 @@ __global__ void __launch_bounds__(kTraceThreads) k_render_ao(SceneView sc, Camer
                                                              uint8_t *__restrict__ rgb, int32_t *__restrict__ ids,
                                                              int32_t *__restrict__ ao_count, Counters *ctr)
 {
-    const int tiles_x = (cam.xres + 7) >> 3, tiles_y = (cam.yres + 3) >> 2;
-    const int items = tiles_x * tiles_y * 32;
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
     uint32_t status = 0;
     FetchCount fc;
     for (;;) {
         const int base = warp_claim(&ctr->work, 32);
         if (base >= items) break;
         int x, y;
-        tile_pixel(base + (threadIdx.x & 31), tiles_x, x, y);
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
         const bool live = (x < cam.xres) && (y < cam.yres);
-        HitRecord h;
-        h.id = -1;
-        h.t = FLT_MAX;
-        RayState r;
-        bool occ;
+        PixelOut po;
+        po.hit = false;
+        po.secondary = 0;
         if (live) {
-            r = camera_ray(cam, x, y);
-            status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, &fc);
-        }
-        const bool hit = live && h.t < FLT_MAX;
-        const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
-        float3 c = cam.background;
-        int made_it = 0;
-        if (hit) {
-            const SurfacePoint sp = surface_at(sc, r, h);
-            const float3 start = offset_start(sp.dst, sp.geo);
-            const AOBasis ob = ao_basis(sp.geo);
-            for (int s = 0; s < samples; ++s) {
-                const float3 d = ao_direction(ob, (uint32_t)pix, (uint32_t)s, seed);
-                HitRecord ah;
-                bool blocked;
-                status |= traverse<true, COUNT>(sc, start, d, ao_dist, ah, blocked, &fc);
-                if (!blocked) ++made_it;
-            }
-            const float3 kd = material_kd(mat, sp);
-            const float frac = xdiv((float)made_it, (float)samples);
-            c = xadd3(xmul3(kd, frac), mat.ka);
-        }
-        if (live) {
-            rgb[3 * pix] = clip8(c.x);
-            rgb[3 * pix + 1] = clip8(c.y);
-            rgb[3 * pix + 2] = clip8(c.z);
-            if (ids) ids[pix] = hit ? h.id : -1;
-            if (ao_count) ao_count[pix] = made_it;
+            po = shade_pixel_ao<COUNT>(sc, cam, mat, samples, ao_dist, seed, x, y, status, &fc);
+            const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+            store_rgb(rgb, pix, po.c);
+            if (ids) ids[pix] = po.id;
+            if (ao_count) ao_count[pix] = po.ao_made;
         }
         warp_count(&ctr->primary, live);
-        warp_count(&ctr->hits, hit);
-        warp_add(&ctr->secondary, hit ? (uint32_t)samples : 0u);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
     }
     if (COUNT) {
         atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);

@@ -145,8 +145,8 @@ __device__ __forceinline__ uint32_t traverse(const SceneView &sc, const float3 o
     const uint32_t oct = octant_of(d);
     uint2 stack[kStackSize];
     int sp = 0;
-    // start: a group holding only the root (node 0 as slot 0 of a virtual parent)
-    uint2 ngroup = make_uint2(0u, (1u << (24 + oct)) | 1u);
+    // start: a group holding only the root (as slot 0 of a virtual parent)
+    uint2 ngroup = make_uint2((uint32_t)sc.root, (1u << (24 + oct)) | 1u);
     float box_tmax = ANY ? tmax : FLT_MAX;
     uint32_t status = 0u;
     for (int step = 0; step < kMaxTraversalSteps; ++step) {
