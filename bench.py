@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true", help="headline workload only")
     ap.add_argument("--size", type=int, default=1024, help="terrain cells per side (power of two)")
     return ap.parse_args()
 
@@ -299,6 +300,15 @@ def main():
                          "bytes_per_frame": alg_bytes, "nodes_per_ray": nodes_per_frame / frame_rays,
                          "tris_per_ray": tris_per_frame / frame_rays, "kernel_ms": mean_kernel_ms},
             "clocks": clk}
+    if not args.no_workloads:
+        sc.close()
+        wl = {}
+        wl["icosphere-20k-512"] = workload_icosphere(ctx, stream, flush, max(5, args.steps))
+        wl["instances-4M-720p-ao16"] = workload_instances_ao(ctx, stream, flush, max(3, args.steps // 4))
+        del flush
+        torch.cuda.empty_cache()
+        wl["batched-64-scenes"] = workload_batched(ctx, stream, max(3, args.steps // 4))
+        line["workloads"] = wl
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(scene, frame, args.cpu_seconds).items()
                                 if k != "build_seconds"}
@@ -306,6 +316,96 @@ def main():
         print(json.dumps(line), flush=True)
     sc.close()
     ctx.close()
+
+
+def time_frames(fn, steps, stream, flush=None):
+    """Sum of CUDA-event times of `steps` calls of fn() on `stream`, the L2
+    flushed before each when `flush` is given.  Returns (seconds, last)."""
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    last = None
+    for i in range(steps):
+        if flush is not None:
+            flush.fill_(float(i))
+        evs[i][0].record(stream)
+        last = fn()
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / 1e3, last
+
+
+def workload_icosphere(ctx, stream, flush, steps):
+    """Icosphere 20,480 + 2 ground triangles, 512x512, primary + point-light shadow."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.icosphere_scene()
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((512, 512, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        sc.render(frame, rgb=rgb)
+    secs, st = time_frames(lambda: sc.render(frame, rgb=rgb)["stats"], steps, stream, flush)
+    rays = (st.primary_rays + st.secondary_rays) * steps
+    sc.close()
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512], "Mrays_s": rays / secs / 1e6,
+            "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_instances_ao(ctx, stream, flush, steps):
+    """2,000 instances x 2,000 triangles (4 M), 1280x720, 16 AO rays per hit
+    within distance 5 (any-hit)."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.instances_scene()
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((720, 1280, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        sc.render(frame, rgb=rgb)
+    secs, st = time_frames(lambda: sc.render(frame, rgb=rgb)["stats"], steps, stream, flush)
+    rays = (st.primary_rays + st.secondary_rays) * steps
+    out = {"triangles": int(scene["tris"].shape[0]), "resolution": [1280, 720], "Mrays_s": rays / secs / 1e6,
+           "ms_per_frame": secs / steps * 1e3, "primary_rays": st.primary_rays, "ao_rays": st.secondary_rays,
+           "bvh_build_ms": sc.build_ms}
+    sc.close()
+    return out
+
+
+def workload_batched(ctx, stream, steps):
+    """64 scenes (icosphere or heightfield, 1k-500k triangles log-uniform,
+    resolutions 128^2 .. 1920x1080, primary+shadow or primary+4 AO): the
+    plain form (one rt_render / rt_render_ao call per scene-frame) against
+    the batched form (one graph-captured persistent launch, autotuned)."""
+    import torch
+    from raptor_gb300 import core, scenes
+    items = scenes.batched_scenes()
+    b = core.Batch(ctx)
+    idx = [b.add_scene(sc) for sc, _ in items]
+    build_ms = b.build()
+    bufs = [torch.empty((fr["camera"]["yres"], fr["camera"]["xres"], 3), dtype=torch.uint8, device="cuda")
+            for _, fr in items]
+    b.set_jobs([core.make_job(i, fr, buf) for i, (_, fr), buf in zip(idx, items, bufs)])
+    tune = b.autotune(reps=2)
+    for _ in range(2):
+        b.render(stats=False)
+    secs_b, st = time_frames(lambda: b.render(stats=True), steps, stream)
+    rays = st.primary_rays + st.secondary_rays
+    # plain: one scene per call, each built on its own
+    plain = [core.Scene(ctx, sc) for sc, _ in items]
+
+    def plain_frame():
+        for s, (_, fr), buf in zip(plain, items, bufs):
+            s.render(fr, rgb=buf)
+    for _ in range(2):
+        plain_frame()
+    secs_p, _ = time_frames(plain_frame, steps, stream)
+    for s in plain:
+        s.close()
+    b.close()
+    return {"scenes": len(items), "triangles": int(sum(sc["tris"].shape[0] for sc, _ in items)),
+            "pixels": int(sum(fr["camera"]["xres"] * fr["camera"]["yres"] for _, fr in items)),
+            "rays_per_frame": rays, "batched_Mrays_s": rays * steps / secs_b / 1e6,
+            "plain_Mrays_s": rays * steps / secs_p / 1e6, "batched_ms": secs_b / steps * 1e3,
+            "plain_ms": secs_p / steps * 1e3, "speedup": secs_p / secs_b, "autotune": tune,
+            "batched_build_ms": build_ms}
 
 
 def C_sizes():

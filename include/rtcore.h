@@ -203,6 +203,30 @@ rt_status rt_render_ao(rt_scene *scene, const rt_camera *camera, const rt_materi
                        float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
                        rt_render_stats *stats);
 
+/* ---------------------------------------------------- differentiation */
+
+/* Replace the per-vertex attributes (colours) without touching geometry. */
+rt_status rt_scene_update_attributes(rt_scene *scene, const float *vert_attr, int32_t nverts);
+
+/* rt_render's frame as unclipped float colours (the camera's ext_colour_t
+ * image before camera::clip_image_to_rgb, camera.h:281-319): rgb_f32
+ * xres*yres*3 floats, hit_ids (nullable) the primary hit per pixel,
+ * occluded (nullable) per pixel a bit per light set when its shadow ray was
+ * blocked.  All outputs DEVICE memory. */
+rt_status rt_render_float(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                          const rt_material *material, float *rgb_f32, int32_t *hit_ids, uint8_t *occluded,
+                          rt_render_stats *stats);
+
+/* Adjoint of rt_render_float (no reference counterpart): given dL/dpixel
+ * (xres*yres*3 floats), writes dL/dvertex-position and dL/dvertex-attribute
+ * (nverts*3 floats each, zeroed first).  Interior gradients: the hit
+ * triangle and shadow-ray visibility of every pixel are held fixed.  The
+ * kernel re-traces each pixel instead of storing hit records (memory
+ * O(pixels + vertices)).  All buffers DEVICE memory. */
+rt_status rt_render_adjoint(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                            const rt_material *material, const float *dL_dpix, float *dL_dpos, float *dL_dattr,
+                            rt_render_stats *stats);
+
 /* ------------------------------------------------------------ batches */
 
 /* A batch renders many scenes (own hierarchy, resolution and ray mix each)

@@ -107,6 +107,11 @@ SIGNATURES = [
                               C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
                                  _P, _P, _P, C.POINTER(RtRenderStats)]),
+    ("rt_scene_update_attributes", C.c_int32, [_P, _P, C.c_int32]),
+    ("rt_render_float", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
+                                    _P, _P, _P, C.POINTER(RtRenderStats)]),
+    ("rt_render_adjoint", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
+                                      _P, _P, _P, C.POINTER(RtRenderStats)]),
     ("rt_batch_create", C.c_int32, [_P, C.POINTER(C.c_void_p)]),
     ("rt_batch_destroy", C.c_int32, [_P]),
     ("rt_batch_add_scene", C.c_int32, [_P, _P, C.c_int32, _P, C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
@@ -281,6 +286,28 @@ class Scene:
         _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
                                C.byref(st)))
         return {"rgb": rgb, "ids": ids, "stats": st}
+
+    def update_attributes(self, vattr):
+        _check(lib().rt_scene_update_attributes(self.h, ptr(vattr), int(vattr.shape[0])))
+
+    def render_float(self, frame, fimg, ids=None, occl=None):
+        """Unclipped float frame into device buffers (torch tensors)."""
+        cam = make_camera(frame["camera"])
+        ls = make_lights(frame["lights"])
+        st = RtRenderStats()
+        _check(lib().rt_render_float(self.h, C.byref(cam), ls, len(frame["lights"]),
+                                     C.byref(make_material(frame["material"])), ptr(fimg), ptr(ids), ptr(occl),
+                                     C.byref(st)))
+        return st
+
+    def render_adjoint(self, frame, dldpix, gpos, gcol):
+        cam = make_camera(frame["camera"])
+        ls = make_lights(frame["lights"])
+        st = RtRenderStats()
+        _check(lib().rt_render_adjoint(self.h, C.byref(cam), ls, len(frame["lights"]),
+                                       C.byref(make_material(frame["material"])), ptr(dldpix), ptr(gpos), ptr(gcol),
+                                       C.byref(st)))
+        return st
 
     def close(self):
         if self.h:
