@@ -167,14 +167,21 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def max_over_ranks(x, world, device="cuda"):
+    """Max of a per-rank scalar over all ranks (NCCL on GPUs, gloo on CPU)."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(rays_per_rank, max_seconds, world):
+    """Whole-job Mrays/s: every rank traced rays_per_rank rays (its own
+    replica); the job takes as long as the slowest rank."""
+    return rays_per_rank * world / max_seconds / 1e6
 
 
 # -------------------------------------------------------------------- main
@@ -260,7 +267,7 @@ def main():
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(step_ms) / 1e3
     total_s = max_over_ranks(total_s, world)
-    value = rays * world / total_s / 1e6
+    value = aggregate_rate(rays, total_s, world)
 
     # e2e: public API with a pinned host output buffer, wall clock per call
     rgb_host = torch.empty((H, W, 3), dtype=torch.uint8).pin_memory()
@@ -273,7 +280,7 @@ def main():
         e2e_rays += st.primary_rays + st.secondary_rays
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     clk = clocks.stop()
-    e2e = e2e_rays * world / e2e_s / 1e6
+    e2e = aggregate_rate(e2e_rays, e2e_s, world)
     h2d = C_sizes()
     mean_kernel_ms = float(np.mean(kernel_ms))
     frame_rays = rays / args.steps

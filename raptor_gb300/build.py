@@ -19,6 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "librtcore.so")
+CLIENT = os.path.join(OUT_DIR, "rt_client_example")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,6 +56,13 @@ def build(verbose: bool = False, extra=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # C++ client of the C ABI (run by the GPU tests)
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(HERE, "..", "include"),
+           os.path.join(HERE, "host", "rt_client_example.cpp"), "-o", CLIENT, "-L", OUT_DIR, "-lrtcore",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"client build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print("built", LIB)
     return LIB

@@ -237,3 +237,13 @@ def test_errors_are_codes_not_crashes(rtlib, ctx):
     with pytest.raises(rtlib.RtError) as e:
         sc.upload(np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.int32))
     assert e.value.code == -1          # index out of range
+
+
+def test_cpp_client_of_the_c_abi(rtlib):
+    """A C++ program linking librtcore.so answers the reference's x-axis
+    traversal known-answer tests."""
+    import subprocess
+    from raptor_gb300 import build
+    r = subprocess.run([build.CLIENT], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count(" ok") == 7
