@@ -311,10 +311,12 @@ def main():
         sc.close()
         wl = {}
         wl["icosphere-20k-512"] = workload_icosphere(ctx, stream, flush, max(5, args.steps))
+        wl["terrain-1M-1080p"] = workload_terrain_1m(ctx, stream, flush, max(5, args.steps // 2))
         wl["instances-4M-720p-ao16"] = workload_instances_ao(ctx, stream, flush, max(3, args.steps // 4))
         del flush
         torch.cuda.empty_cache()
         wl["batched-64-scenes"] = workload_batched(ctx, stream, max(3, args.steps // 4))
+        wl["adjoint-50k-256"] = workload_adjoint(ctx, stream, max(5, args.steps // 2))
         line["workloads"] = wl
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(scene, frame, args.cpu_seconds).items()
@@ -355,6 +357,49 @@ def workload_icosphere(ctx, stream, flush, steps):
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512], "Mrays_s": rays / secs / 1e6,
             "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_terrain_1m(ctx, stream, flush, steps):
+    """The 1,048,352-triangle terrain (725^2 vertices), 1920x1080: primary
+    rays alone (no light) and primary + sun shadow rays."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.terrain_scene(crop=725)
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((1080, 1920, 3), dtype=torch.uint8, device="cuda")
+    prim = dict(frame, lights=[])
+    out = {"triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080]}
+    for key, fr in (("primary_only", prim), ("primary_shadow", frame)):
+        for _ in range(3):
+            sc.render(fr, rgb=rgb)
+        secs, st = time_frames(lambda: sc.render(fr, rgb=rgb)["stats"], steps, stream, flush)
+        out[key] = {"Grays_s": (st.primary_rays + st.secondary_rays) * steps / secs / 1e9,
+                    "ms_per_frame": secs / steps * 1e3, "primary_rays": st.primary_rays,
+                    "secondary_rays": st.secondary_rays}
+    sc.close()
+    return out
+
+
+def workload_adjoint(ctx, stream, steps):
+    """Differentiable render: 50,000-triangle displaced sphere at 256x256,
+    primary + shadow; float forward vs hand-written adjoint, ms per frame."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, target_scene, frame = scenes.adjoint_scene()
+    sc = core.Scene(ctx, scene)
+    H, W = frame["camera"]["yres"], frame["camera"]["xres"]
+    img = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    dl = torch.randn((H, W, 3), dtype=torch.float32, device="cuda")
+    gp = torch.empty((scene["verts"].shape[0], 3), dtype=torch.float32, device="cuda")
+    gc = torch.empty_like(gp)
+    for _ in range(3):
+        sc.render_float(frame, img)
+        sc.render_adjoint(frame, dl, gp, gc)
+    fwd, _ = time_frames(lambda: sc.render_float(frame, img), steps, stream)
+    adj, _ = time_frames(lambda: sc.render_adjoint(frame, dl, gp, gc), steps, stream)
+    sc.close()
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [W, H], "forward_ms": fwd / steps * 1e3,
+            "adjoint_ms": adj / steps * 1e3, "adjoint_over_forward": adj / fwd}
 
 
 def workload_instances_ao(ctx, stream, flush, steps):

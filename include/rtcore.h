@@ -129,6 +129,12 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
  * instrumented kernel that counts node loads and triangle tests into
  * rt_render_stats (for roofline accounting; slower, off by default). */
 #define RT_OPT_COUNT_FETCHES 1
+/* RT_OPT_RENDER_KERNEL: RT_KERNEL_WAVE (default) -- lanes replace finished
+ * rays at once (primary -> secondary rays -> next pixel); RT_KERNEL_PIXEL --
+ * one pixel per lane until the whole warp's tile is done.  Same results. */
+#define RT_OPT_RENDER_KERNEL 2
+#define RT_KERNEL_WAVE 0
+#define RT_KERNEL_PIXEL 1
 rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value);
 /* Message of the last error on the calling thread ("" if none). */
 const char *rt_last_error_string(void);

@@ -26,6 +26,9 @@ RT_LIGHT_POINT = 0
 RT_LIGHT_DIRECTIONAL = 1
 RT_MAX_LIGHTS = 8
 RT_OPT_COUNT_FETCHES = 1
+RT_OPT_RENDER_KERNEL = 2
+RT_KERNEL_WAVE = 0
+RT_KERNEL_PIXEL = 1
 
 
 class RtError(RuntimeError):

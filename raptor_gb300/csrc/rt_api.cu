@@ -261,6 +261,12 @@ rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
         ctx->count_fetches = value != 0;
         return RT_OK;
     }
+    if (option == RT_OPT_RENDER_KERNEL) {
+        if (value != RT_KERNEL_WAVE && value != RT_KERNEL_PIXEL)
+            return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown render kernel");
+        ctx->render_kernel = (int)value;
+        return RT_OK;
+    }
     return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown option");
 }
 
@@ -556,8 +562,12 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    launch_render(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
-                  ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    if (ctx->render_kernel == RT_KERNEL_WAVE)
+        launch_render_wave(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
+                           ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    else
+        launch_render(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
+                      ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
@@ -581,9 +591,13 @@ rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *
     if (st != RT_OK) return st;
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    launch_render_ao(scene_view(s), make_camera_view(*camera), make_material_view(*material), samples, ao_dist, seed,
-                     o.rgb, o.ids, o.aux, ctx->d_counters, ctx->sm_count, ctx->stream,
-                     ctx->count_fetches);
+    if (ctx->render_kernel == RT_KERNEL_WAVE)
+        launch_render_ao_wave(scene_view(s), make_camera_view(*camera), make_material_view(*material), samples, ao_dist,
+                              seed, o.rgb, o.ids, o.aux, ctx->d_counters, ctx->sm_count, ctx->stream,
+                              ctx->count_fetches);
+    else
+        launch_render_ao(scene_view(s), make_camera_view(*camera), make_material_view(*material), samples, ao_dist,
+                         seed, o.rgb, o.ids, o.aux, ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, hit_ids, ao_count, o, stats);

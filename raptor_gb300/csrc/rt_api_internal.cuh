@@ -38,6 +38,7 @@ struct rt_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rtc::DevBuf stage_a, stage_b, stage_c;
     bool count_fetches = false;
+    int render_kernel = RT_KERNEL_WAVE;
 };
 
 struct rt_scene {

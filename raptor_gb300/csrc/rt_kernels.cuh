@@ -34,4 +34,11 @@ void launch_render_ao(const SceneView &sc, const CameraView &cam, const Material
                       float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
                       int sm_count, cudaStream_t st, bool count = false);
 
+// Lane-level ray-replacement variants (rt_wave.cu).
+void launch_render_wave(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
+                        uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+void launch_render_ao_wave(const SceneView &sc, const CameraView &cam, const MaterialView &mat, int32_t samples,
+                           float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
+                           int sm_count, cudaStream_t st, bool count = false);
+
 }  // namespace rtc

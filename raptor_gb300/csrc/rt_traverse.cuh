@@ -123,86 +123,119 @@ struct HitRecord {
     int32_t id;
     float t, u, v;
 };
-
-// Closest hit (ANY = false) or any hit inside (EPSILON, tmax) skipping light
-// and transparent triangles (ANY = true).  Returns the device status bits.
 struct FetchCount {
     uint32_t nodes = 0;
     uint32_t tris = 0;
 };
 
+// Resumable traversal state of one ray: trav_begin sets it up, each
+// trav_step intersects one node (or resumes a stacked node group) and tests
+// that node's leaf triangles.  The stack lives with the caller.
+struct Trav {
+    float3 o, d, inv;
+    uint32_t oct;
+    float tmax;        // any-hit limit
+    float box_tmax;    // boxes beyond this are culled (closest: best t so far)
+    uint2 ngroup;
+    int sp;
+    int steps;
+    HitRecord hit;
+    bool occluded;
+};
+
+__device__ __forceinline__ void trav_begin(Trav &T, const SceneView &sc, const float3 o, const float3 d, float tmax,
+                                           bool any)
+{
+    T.o = o;
+    T.d = d;
+    T.inv = safe_inv(d);
+    T.oct = octant_of(d);
+    T.tmax = tmax;
+    T.box_tmax = any ? tmax : FLT_MAX;
+    // a group holding only the root (as slot 0 of a virtual parent)
+    T.ngroup = make_uint2((uint32_t)sc.root, sc.nnodes > 0 ? ((1u << (24 + T.oct)) | 1u) : 0u);
+    T.sp = 0;
+    T.steps = 0;
+    T.hit.id = -1;
+    T.hit.t = FLT_MAX;
+    T.hit.u = 0.f;
+    T.hit.v = 0.f;
+    T.occluded = false;
+}
+
+// One traversal step; returns true when the ray is finished.  Closest hit
+// (any = false) or any hit inside (EPSILON, tmax) skipping light and
+// transparent triangles (any = true).  Status bits go to `status`.
+template <bool COUNT>
+__device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView &sc, bool any, uint32_t &status,
+                                          FetchCount *fc)
+{
+    if (++T.steps > kMaxTraversalSteps) { status |= kStatusStepLimit; return true; }
+    uint2 tgroup = make_uint2(0u, 0u);
+    if (T.ngroup.y & 0xff000000u) {
+        const uint32_t bit = __ffs(T.ngroup.y >> 24) - 1u;
+        T.ngroup.y &= ~(1u << (24 + bit));
+        const uint32_t slot = bit ^ T.oct;
+        const uint32_t idx = T.ngroup.x + __popc(T.ngroup.y & ((1u << slot) - 1u) & 0xffu);
+        if (idx >= (uint32_t)sc.nnodes) { status |= kStatusBadIndex; return true; }
+        if (T.ngroup.y & 0xff000000u) {
+            if (T.sp >= kStackSize) { status |= kStatusStackOverflow; return true; }
+            stack[T.sp++] = T.ngroup;
+        }
+        const NodeHits nh = intersect_node(sc.nodes, idx, T.o, T.inv, T.oct, T.box_tmax);
+        if (COUNT) ++fc->nodes;
+        T.ngroup = nh.ngroup;
+        tgroup = nh.tgroup;
+    }
+    while (tgroup.y != 0u) {
+        const uint32_t k = __ffs(tgroup.y) - 1u;
+        tgroup.y &= tgroup.y - 1u;
+        const uint32_t ti = tgroup.x + k;
+        if (ti >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
+        const PackedTri *tp = sc.tris + ti;
+        if (COUNT) ++fc->tris;
+        const float4 w0 = __ldg(&tp->w0);
+        const float4 w1 = __ldg(&tp->w1);
+        const float4 w2 = __ldg(&tp->w2);
+        float u, v;
+        const float t = mt_intersect(w0, w1, w2, T.o, T.d, u, v);
+        const int32_t id = __float_as_int(w2.y);
+        if ((uint32_t)id >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
+        if (any) {
+            if ((__float_as_uint(w2.z) & (RT_TRI_LIGHT | RT_TRI_TRANSPARENT)) == 0u && t > kEpsilon && t < T.tmax) {
+                T.occluded = true;
+                T.hit.id = id;
+                T.hit.t = t;
+                return true;
+            }
+        } else if (t > kEpsilon && (t < T.hit.t || (t == T.hit.t && id < T.hit.id))) {
+            T.hit.id = id;
+            T.hit.t = t;
+            T.hit.u = u;
+            T.hit.v = v;
+            T.box_tmax = t;
+        }
+    }
+    if (!(T.ngroup.y & 0xff000000u)) {
+        if (T.sp == 0) return true;
+        T.ngroup = stack[--T.sp];
+    }
+    return false;
+}
+
+// Whole traversal of one ray.  Returns the device status bits.
 template <bool ANY, bool COUNT = false>
 __device__ __forceinline__ uint32_t traverse(const SceneView &sc, const float3 o, const float3 d, float tmax,
                                              HitRecord &hit, bool &occluded, FetchCount *fc = nullptr)
 {
-    hit.id = -1;
-    hit.t = FLT_MAX;
-    hit.u = 0.f;
-    hit.v = 0.f;
-    occluded = false;
-    if (sc.nnodes <= 0) return 0u;
-    const float3 inv = safe_inv(d);
-    const uint32_t oct = octant_of(d);
     uint2 stack[kStackSize];
-    int sp = 0;
-    // start: a group holding only the root (as slot 0 of a virtual parent)
-    uint2 ngroup = make_uint2((uint32_t)sc.root, (1u << (24 + oct)) | 1u);
-    float box_tmax = ANY ? tmax : FLT_MAX;
+    Trav T;
+    trav_begin(T, sc, o, d, tmax, ANY);
     uint32_t status = 0u;
-    for (int step = 0; step < kMaxTraversalSteps; ++step) {
-        uint2 tgroup = make_uint2(0u, 0u);
-        if (ngroup.y & 0xff000000u) {
-            const uint32_t bit = __ffs(ngroup.y >> 24) - 1u;
-            ngroup.y &= ~(1u << (24 + bit));
-            const uint32_t slot = bit ^ oct;
-            const uint32_t idx = ngroup.x + __popc(ngroup.y & ((1u << slot) - 1u) & 0xffu);
-            if (idx >= (uint32_t)sc.nnodes) { status |= kStatusBadIndex; break; }
-            if (ngroup.y & 0xff000000u) {
-                if (sp >= kStackSize) { status |= kStatusStackOverflow; break; }
-                stack[sp++] = ngroup;
-            }
-            const NodeHits nh = intersect_node(sc.nodes, idx, o, inv, oct, box_tmax);
-            if (COUNT) ++fc->nodes;
-            ngroup = nh.ngroup;
-            tgroup = nh.tgroup;
-        }
-        while (tgroup.y != 0u) {
-            const uint32_t k = __ffs(tgroup.y) - 1u;
-            tgroup.y &= tgroup.y - 1u;
-            const uint32_t ti = tgroup.x + k;
-            if (ti >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
-            const PackedTri *tp = sc.tris + ti;
-            if (COUNT) ++fc->tris;
-            const float4 w0 = __ldg(&tp->w0);
-            const float4 w1 = __ldg(&tp->w1);
-            const float4 w2 = __ldg(&tp->w2);
-            float u, v;
-            const float t = mt_intersect(w0, w1, w2, o, d, u, v);
-            if ((uint32_t)__float_as_int(w2.y) >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
-            if (ANY) {
-                if ((__float_as_uint(w2.z) & (RT_TRI_LIGHT | RT_TRI_TRANSPARENT)) == 0u && t > kEpsilon && t < tmax) {
-                    occluded = true;
-                    hit.id = __float_as_int(w2.y);
-                    hit.t = t;
-                    return status;
-                }
-            } else {
-                const int32_t id = __float_as_int(w2.y);
-                if (t > kEpsilon && (t < hit.t || (t == hit.t && id < hit.id))) {
-                    hit.id = id;
-                    hit.t = t;
-                    hit.u = u;
-                    hit.v = v;
-                    box_tmax = t;
-                }
-            }
-        }
-        if (!(ngroup.y & 0xff000000u)) {
-            if (sp == 0) return status;
-            ngroup = stack[--sp];
-        }
-        if (step + 1 == kMaxTraversalSteps) status |= kStatusStepLimit;
+    while (!trav_step<COUNT>(T, stack, sc, ANY, status, fc)) {
     }
+    hit = T.hit;
+    occluded = T.occluded;
     return status;
 }
 

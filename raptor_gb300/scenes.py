@@ -227,13 +227,19 @@ def icosphere_scene(freq: int = 32, seed: int = 0, res: int = 512, ground: bool 
 
 
 def terrain_scene(size_pow2: int = 1024, roughness: float = 0.55, seed: int = 1, xres: int = 1920,
-                  yres: int = 1080, extent: float = 1024.0, height: float = 200.0):
+                  yres: int = 1080, extent: float = 1024.0, height: float = 200.0, crop: int = 0):
     """Diamond-square terrain over extent^2 with heights in [0, height]
     (2*size^2 triangles); camera 300 units above the (0, 0) corner looking at
-    the centre; directional sun; slope-based per-vertex colour."""
+    the centre; directional sun; slope-based per-vertex colour.  crop > 0
+    keeps the first crop x crop vertices (same spacing): crop = 725 gives the
+    1,048,352-triangle ("1M") variant."""
     h = diamond_square(size_pow2, roughness, seed)
+    spacing = extent / size_pow2
+    if crop:
+        h = h[:crop, :crop]
+        extent = spacing * (crop - 1)
     verts, tris, hs = heightfield_mesh(h, extent, height)
-    vattr = slope_colours(hs, extent / size_pow2, height)
+    vattr = slope_colours(hs, spacing, height)
     scene = _pack(verts, tris, vattr)
     frame = {"camera": look_at_camera((0.0, 300.0, 0.0), (extent / 2, height / 2, extent / 2), 60.0, xres, yres,
                                       background=(110.0, 160.0, 230.0)),
