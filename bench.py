@@ -227,7 +227,10 @@ def main():
     cam = frame["camera"]
     W, H = cam["xres"], cam["yres"]
     ctx = core.Context(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream, current for torch too: the L2 flush,
+    # the CUDA events and the library's kernels are ordered on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     sc = core.Scene(ctx, scene)
     build_ms = sc.build()

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -196,12 +197,18 @@ def rays_array(ogn, dirs, tmax=None):
 
 
 class Context:
+    """Owns an rt_context.  Scenes and batches made from it are closed before
+    the context itself (the C ABI requires that order)."""
+
     def __init__(self, device: int = 0):
         h = C.c_void_p()
         _check(lib().rt_ctx_create(device, C.byref(h)))
         self.h = h
+        self._children = weakref.WeakSet()
 
     def set_stream(self, stream_handle):
+        """Run on a CUDA stream given by its handle (a non-default stream:
+        handle 0 restores the context's own stream)."""
         _check(lib().rt_ctx_set_stream(self.h, C.c_void_p(stream_handle) if stream_handle else None))
 
     def synchronize(self):
@@ -212,6 +219,8 @@ class Context:
 
     def close(self):
         if self.h:
+            for child in list(self._children):
+                child.close()
             lib().rt_ctx_destroy(self.h)
             self.h = None
 
@@ -228,6 +237,7 @@ class Scene:
         h = C.c_void_p()
         _check(lib().rt_scene_create(ctx.h, C.byref(h)))
         self.h = h
+        ctx._children.add(self)
         self.build_ms = None
         if scene is not None:
             self.upload(scene["verts"], scene["tris"], scene.get("vattr"), scene.get("flags"))
@@ -313,9 +323,9 @@ class Scene:
         return st
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             lib().rt_scene_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -357,6 +367,7 @@ class Batch:
         h = C.c_void_p()
         _check(lib().rt_batch_create(ctx.h, C.byref(h)))
         self.h = h
+        ctx._children.add(self)
         self._keep = []
         self.build_ms = None
 
@@ -395,9 +406,9 @@ class Batch:
         _check(lib().rt_batch_set_config(self.h, C.byref(cfg)))
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             lib().rt_batch_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
