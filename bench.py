@@ -117,38 +117,56 @@ class ClockSampler:
 
 # ------------------------------------------------------------ CPU baseline
 
+class CpuBaseline:
+    """The reference's CPU path on this host's cores.  The reference itself
+    (oracle/_ref) builds only on x86-64 (its simd.h includes immintrin.h), so
+    on the Arm GPU host this is the oracle's C restatement (kind "port"),
+    which the tests pin to the reference's outputs.  The hierarchy is built
+    once; each step renders a band of rows sized to `seconds` of work with
+    all host threads."""
+
+    def __init__(self, scene, frame, threads=None):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        if not os.path.exists(O.ORACLE_SO):
+            O.build()
+        self.threads = threads or os.cpu_count() or 1
+        self.frame = frame
+        t0 = time.perf_counter()
+        self.scene = O.OracleScene(scene)
+        self.build_s = time.perf_counter() - t0
+        self.H = frame["camera"]["yres"]
+        self.next_row = 0
+        self.rows_per_s = None
+
+    def step(self, seconds):
+        if self.rows_per_s is None:   # probe 8 rows
+            t = time.perf_counter()
+            self.scene.render(self.frame, rows=(self.H // 2, self.H // 2 + 8), threads=self.threads)
+            self.rows_per_s = 8 / max(time.perf_counter() - t, 1e-6)
+        rows = int(max(8, min(self.H, seconds * self.rows_per_s)))
+        r0 = self.next_row % self.H
+        r1 = min(self.H, r0 + rows)
+        self.next_row = r1 % self.H
+        t = time.perf_counter()
+        out = self.scene.render(self.frame, rows=(r0, r1), threads=self.threads)
+        dt = time.perf_counter() - t
+        self.last = {"rows": (r0, r1), "rays": int(out["rays"]), "seconds": dt}
+        return out["rays"] / dt / 1e6
+
+    def describe(self):
+        r0, r1 = self.last["rows"]
+        return {"cores": self.threads, "kind": "port",
+                "sample": f"rows {r0}..{r1} of {self.H} ({self.last['rays']} rays) of the same frame per step; "
+                          f"C restatement of bvh traversal + ray_trace_engine::ray_trace + coloured_mapper_shader "
+                          f"(pinned to the reference's outputs); hierarchy build {self.build_s:.2f} s excluded"}
+
+
 def cpu_baseline(scene, frame, seconds, threads=None):
-    """The reference's CPU path on this host: oracle/_ref (the reference
-    compiled from source) when present, else the oracle's C restatement.
-    Renders a band of rows sized to about `seconds` of work with all host
-    threads; returns Mrays/s and a description of the sample."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    if not os.path.exists(O.ORACLE_SO):
-        O.build()
-    threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    osc = O.OracleScene(scene)
-    build_s = time.perf_counter() - t0
-    H = frame["camera"]["yres"]
-    # probe a thin band, then size the sample to the budget
-    mid = H // 2
-    probe = O.OracleScene.render(osc, frame, rows=(mid, min(H, mid + 8)), threads=threads)
-    t1 = time.perf_counter()
-    probe = osc.render(frame, rows=(mid, min(H, mid + 8)), threads=threads)
-    dt = max(time.perf_counter() - t1, 1e-6)
-    rows = int(max(8, min(H, 8 * seconds / dt)))
-    r0 = max(0, mid - rows // 2)
-    r1 = min(H, r0 + rows)
-    t2 = time.perf_counter()
-    out = osc.render(frame, rows=(r0, r1), threads=threads)
-    dt = time.perf_counter() - t2
-    kind = "port"
-    return {"value": out["rays"] / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": kind,
-            "sample": f"rows {r0}..{r1} of {H} ({out['rays']} rays) of the same frame, oracle C restatement of "
-                      f"bvh traversal + ray_trace_engine::ray_trace + coloured_mapper_shader; hierarchy build "
-                      f"{build_s:.2f} s single-threaded excluded",
-            "build_seconds": build_s}
+    """One bounded sample of the CPU baseline (see CpuBaseline)."""
+    cb = CpuBaseline(scene, frame, threads)
+    v = cb.step(seconds)
+    return dict(value=v, unit="Mrays/s", **cb.describe())
 
 
 # --------------------------------------------------------------- distributed
@@ -187,24 +205,29 @@ def aggregate_rate(rays_per_rank, max_seconds, world):
 # -------------------------------------------------------------------- main
 
 def run_reference(args):
+    """--impl reference: the reference's CPU path on all host cores, each
+    step a bounded band of the same frame (rank 0 only)."""
     rank, world = dist_init(args.gpus)
     if rank != 0:
         return
     scene, frame = make_workload(args.size)
-    vals = []
-    cb = None
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(scene, frame, seconds=max(1.0, args.cpu_seconds / 4.0))
-        if i >= args.warmup:
-            vals.append(cb["value"])
-    v = float(np.mean(vals))
+    cb = CpuBaseline(scene, frame)
+    per_step = max(0.5, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cb.step(per_step / 2)
+    rays = secs = 0.0
+    for _ in range(args.steps):
+        cb.step(per_step)
+        rays += cb.last["rays"]
+        secs += cb.last["seconds"]
+    v = rays / secs / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded diamond-square terrain)",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded diamond-square terrain, slope colours)",
             "config": {"workload": WORKLOAD, "triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080],
                        "rays": "primary + 1 directional shadow ray per hit"},
-            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
+            "cpu_baseline": dict(value=v, unit="Mrays/s", **cb.describe()),
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -259,12 +259,15 @@ typedef struct rt_job {
 } rt_job;
 
 /* Launch shape of the batched kernel, chosen by rt_batch_autotune:
- * threads per block (64/128/256), tiles claimed per queue access (1..16),
- * tile width (8 -> 8x4 tiles, 16 -> 16x2), and the measured ms per frame. */
+ * threads per block (64/128/256), tiles claimed per queue access (1..16,
+ * RT_KERNEL_PIXEL only), tile width (8 -> 8x4 tiles, 16 -> 16x2), kernel
+ * (RT_KERNEL_WAVE / RT_KERNEL_PIXEL, see RT_OPT_RENDER_KERNEL) and the
+ * measured ms per frame. */
 typedef struct rt_tune_config {
     int32_t block_threads;
     int32_t chunk_tiles;
     int32_t tile_w;
+    int32_t kernel;
     float ms;
 } rt_tune_config;
 

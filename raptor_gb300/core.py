@@ -80,7 +80,8 @@ class RtJob(C.Structure):
 
 
 class RtTuneConfig(C.Structure):
-    _fields_ = [("block_threads", C.c_int32), ("chunk_tiles", C.c_int32), ("tile_w", C.c_int32), ("ms", C.c_float)]
+    _fields_ = [("block_threads", C.c_int32), ("chunk_tiles", C.c_int32), ("tile_w", C.c_int32),
+                ("kernel", C.c_int32), ("ms", C.c_float)]
 
 
 # numpy views of the C structs
@@ -399,10 +400,11 @@ class Batch:
     def autotune(self, reps=3):
         cfg = RtTuneConfig()
         _check(lib().rt_batch_autotune(self.h, reps, C.byref(cfg)))
-        return {"block_threads": cfg.block_threads, "chunk_tiles": cfg.chunk_tiles, "tile_w": cfg.tile_w, "ms": cfg.ms}
+        return {"block_threads": cfg.block_threads, "chunk_tiles": cfg.chunk_tiles, "tile_w": cfg.tile_w,
+                "kernel": "wave" if cfg.kernel == RT_KERNEL_WAVE else "pixel", "ms": cfg.ms}
 
-    def set_config(self, block_threads=128, chunk_tiles=1, tile_w=8):
-        cfg = RtTuneConfig(block_threads, chunk_tiles, tile_w, 0.0)
+    def set_config(self, block_threads=128, chunk_tiles=1, tile_w=8, kernel=0):
+        cfg = RtTuneConfig(block_threads, chunk_tiles, tile_w, kernel, 0.0)
         _check(lib().rt_batch_set_config(self.h, C.byref(cfg)))
 
     def close(self):

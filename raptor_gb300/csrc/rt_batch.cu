@@ -81,12 +81,142 @@ __global__ void __launch_bounds__(256) k_render_batched(const BatchJob *__restri
     if (status) atomicOr(&ctr->status, status);
 }
 
+// Lane-replacement form: every lane carries a pixel of any job and refills
+// from the shared queue as soon as its pixel is stored (see rt_wave.cu).
 template <int TW>
-int grid_for(int threads, int sm_count)
+__global__ void __launch_bounds__(256) k_render_batched_wave(const BatchJob *__restrict__ jobs, int32_t njobs,
+                                                             int32_t total_items, Counters *ctr)
+{
+    extern __shared__ LaneShade wave_state[];
+    LaneShade &S = wave_state[threadIdx.x];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lanes_below = (1u << lane) - 1u;
+    uint2 stack[kStackSize];
+    Trav T;
+    uint32_t status = 0, n_primary = 0, n_hits = 0, n_secondary = 0;
+    int x = 0, y = 0, j = 0;
+    int phase = -1;
+    bool queue_open = true;
+    for (;;) {
+        const bool need = phase < 0 && queue_open;
+        const uint32_t needmask = __ballot_sync(0xffffffffu, need);
+        if (needmask) {
+            const int leader = __ffs(needmask) - 1;
+            int base = 0;
+            if ((int)lane == leader) base = atomicAdd(&ctr->work, __popc(needmask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(needmask) >= total_items) queue_open = false;
+            if (need) {
+                const int item = base + __popc(needmask & lanes_below);
+                if (item < total_items) {
+                    int lo = 0, hi = njobs - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (__ldg(&jobs[mid].items_begin) <= item) lo = mid; else hi = mid - 1;
+                    }
+                    j = lo;
+                    const BatchJob &J = jobs[j];
+                    tile_pixel<TW>(item - J.items_begin, J.tiles_x, x, y);
+                    if (x < J.cam.xres && y < J.cam.yres) {
+                        const RayState r = camera_ray(J.cam, x, y);
+                        trav_begin(T, J.sc, r.o, r.d, FLT_MAX, false);
+                        phase = 0;
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, phase >= 0)) {
+            if (!queue_open) break;
+            continue;
+        }
+        if (phase < 0) continue;
+        const BatchJob &J = jobs[j];
+        if (!trav_step<false>(T, stack, J.sc, phase > 0, status, nullptr)) continue;
+        const bool ao = J.mode == RT_JOB_AO;
+        const int nsec = ao ? J.ao_samples : J.nlights;
+        bool done = false;
+        if (phase == 0) {
+            ++n_primary;
+            S.c = J.cam.background;
+            S.id = -1;
+            S.made = 0;
+            if (T.hit.t < FLT_MAX) {
+                ++n_hits;
+                RayState r;
+                r.o = T.o;
+                r.d = T.d;
+                const SurfacePoint sp = surface_at(J.sc, r, T.hit);
+                S.id = T.hit.id - J.sc.tri_base;
+                S.kd = material_kd(J.mat, sp);
+                S.sn = sp.sn;
+                S.geo = sp.geo;
+                S.start = offset_start(sp.dst, sp.geo);
+                S.vd = T.d;
+                S.c = make_float3(0.f, 0.f, 0.f);
+                if (nsec > 0) {
+                    phase = 1;
+                } else {
+                    S.c = xadd3(S.c, J.mat.ka);
+                    done = true;
+                }
+            } else {
+                done = true;
+            }
+        } else {
+            ++n_secondary;
+            const int k = phase - 1;
+            if (ao) {
+                if (!T.occluded) ++S.made;
+            } else {
+                float3 ldir;
+                float len;
+                shadow_ray(J.lights[k], S.start, ldir, len);
+                float3 c = S.c;
+                phong_add(J.lights[k], J.mat, S.kd, S.sn, S.vd, ldir, len, T.occluded ? 0.0f : 1.0f, c);
+                S.c = c;
+            }
+            if (phase < nsec) {
+                ++phase;
+            } else {
+                if (ao) S.c = xadd3(xmul3(S.kd, xdiv((float)S.made, (float)nsec)), J.mat.ka);
+                else S.c = xadd3(S.c, J.mat.ka);
+                done = true;
+            }
+        }
+        if (!done) {
+            const int k = phase - 1;
+            if (ao) {
+                const AOBasis ob = ao_basis(S.geo);
+                const uint32_t pix = (uint32_t)x + (uint32_t)y * (uint32_t)J.cam.xres;
+                trav_begin(T, J.sc, S.start, ao_direction(ob, pix, (uint32_t)k, J.ao_seed), J.ao_dist, true);
+            } else {
+                float3 ldir;
+                float len;
+                shadow_ray(J.lights[k], S.start, ldir, len);
+                trav_begin(T, J.sc, S.start, ldir, len, true);
+            }
+        } else {
+            const size_t pix = (size_t)x + (size_t)y * (size_t)J.cam.xres;
+            store_rgb(J.rgb, pix, S.c);
+            if (J.ids) J.ids[pix] = S.id;
+            phase = -1;
+        }
+    }
+    warp_add(&ctr->primary, n_primary);
+    warp_add(&ctr->hits, n_hits);
+    warp_add(&ctr->secondary, n_secondary);
+    if (status) atomicOr(&ctr->status, status);
+}
+
+template <int TW>
+int grid_for(int kernel, int threads, int sm_count)
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched<TW>, threads, 0) != cudaSuccess ||
-        per_sm < 1) {
+    cudaError_t e = (kernel == RT_KERNEL_WAVE)
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched_wave<TW>, threads,
+                                                                        threads * sizeof(LaneShade))
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched<TW>, threads, 0);
+    if (e != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
@@ -120,7 +250,7 @@ struct rt_batch {
     BatchJob *d_jobs = nullptr;
     int32_t total_items = 0;
     // launch configuration and its captured graph
-    rt_tune_config cfg{128, 1, 8, 0.f};
+    rt_tune_config cfg{128, 1, 8, RT_KERNEL_WAVE, 0.f};
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
 };
@@ -164,10 +294,17 @@ void launch_batch(rt_batch *b, cudaStream_t st, int grid)
     const int threads = b->cfg.block_threads;
     const int chunk = std::max(1, b->cfg.chunk_tiles);
     const int nj = (int)b->h_jobs.size();
-    if (b->cfg.tile_w == 16)
+    const size_t smem = (size_t)threads * sizeof(LaneShade);
+    if (b->cfg.kernel == RT_KERNEL_WAVE) {
+        if (b->cfg.tile_w == 16)
+            k_render_batched_wave<16><<<grid, threads, smem, st>>>(b->d_jobs, nj, b->total_items, b->ctx->d_counters);
+        else
+            k_render_batched_wave<8><<<grid, threads, smem, st>>>(b->d_jobs, nj, b->total_items, b->ctx->d_counters);
+    } else if (b->cfg.tile_w == 16) {
         k_render_batched<16><<<grid, threads, 0, st>>>(b->d_jobs, nj, b->total_items, chunk, b->ctx->d_counters);
-    else
+    } else {
         k_render_batched<8><<<grid, threads, 0, st>>>(b->d_jobs, nj, b->total_items, chunk, b->ctx->d_counters);
+    }
 }
 
 rt_status make_graph(rt_batch *b)
@@ -176,8 +313,8 @@ rt_status make_graph(rt_batch *b)
     cudaStream_t st = b->ctx->stream;
     cudaGraph_t g = nullptr;
     // persistent grid: resident blocks per SM for this shape x SMs
-    const int grid = (b->cfg.tile_w == 16) ? grid_for<16>(b->cfg.block_threads, b->ctx->sm_count)
-                                           : grid_for<8>(b->cfg.block_threads, b->ctx->sm_count);
+    const int grid = (b->cfg.tile_w == 16) ? grid_for<16>(b->cfg.kernel, b->cfg.block_threads, b->ctx->sm_count)
+                                           : grid_for<8>(b->cfg.kernel, b->cfg.block_threads, b->ctx->sm_count);
     RT_CUDA_B(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture begin");
     launch_batch(b, st, grid);
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -442,7 +579,8 @@ rt_status rt_batch_set_config(rt_batch *b, const rt_tune_config *cfg)
 {
     if (!b || !cfg) return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_config: NULL argument");
     if ((cfg->block_threads != 64 && cfg->block_threads != 128 && cfg->block_threads != 256) ||
-        (cfg->tile_w != 8 && cfg->tile_w != 16) || cfg->chunk_tiles < 1 || cfg->chunk_tiles > 16)
+        (cfg->tile_w != 8 && cfg->tile_w != 16) || cfg->chunk_tiles < 1 || cfg->chunk_tiles > 16 ||
+        (cfg->kernel != RT_KERNEL_WAVE && cfg->kernel != RT_KERNEL_PIXEL))
         return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_config: unsupported configuration");
     Guard g(b->ctx->device);
     b->cfg = *cfg;
@@ -469,11 +607,14 @@ rt_status rt_batch_autotune(rt_batch *b, int32_t reps, rt_tune_config *best_out)
     const int threads[3] = {64, 128, 256};
     const int tiles[2] = {8, 16};
     const int chunks[3] = {1, 2, 4};
-    rt_tune_config best{128, 1, 8, 1e30f};
+    const int kernels[2] = {RT_KERNEL_WAVE, RT_KERNEL_PIXEL};
+    rt_tune_config best{128, 1, 8, RT_KERNEL_WAVE, 1e30f};
+    for (int kn : kernels)
     for (int tw : tiles)
         for (int th : threads)
             for (int ch : chunks) {
-                rt_tune_config c{th, ch, tw, 0.f};
+                if (kn == RT_KERNEL_WAVE && ch != 1) continue;   // the wave form refills per lane
+                rt_tune_config c{th, ch, tw, kn, 0.f};
                 rt_status s = rt_batch_set_config(b, &c);
                 if (s != RT_OK) return s;
                 RT_CUDA_B(cudaGraphLaunch(b->exec, ctx->stream), "graph launch");   // warm-up

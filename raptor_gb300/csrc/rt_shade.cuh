@@ -131,6 +131,14 @@ __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const Ca
     return out;
 }
 
+// Shading state a lane keeps (in shared memory) while it traces the
+// secondary rays of its pixel (lane-replacement kernels).
+struct LaneShade {
+    float3 kd, sn, start, c, vd, geo;
+    int32_t id;
+    int32_t made;
+};
+
 __device__ __forceinline__ void store_rgb(uint8_t *rgb, size_t pix, float3 c)
 {
     rgb[3 * pix] = clip8(c.x);

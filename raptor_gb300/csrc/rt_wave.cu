@@ -18,12 +18,6 @@ namespace {
 constexpr int kModeLights = 0;
 constexpr int kModeAO = 1;
 
-struct LaneShade {
-    float3 kd, sn, start, c, vd, geo;
-    int32_t id;
-    int32_t made;
-};
-
 struct AOParams {
     int32_t samples;
     float dist;

@@ -92,7 +92,7 @@ def test_autotune_keeps_results(rtlib, ctx, batch_setup):
     for (rgb, _), ref in zip(bufs, before):
         assert np.array_equal(rgb.cpu().numpy(), ref)
     # every shape gives the same frames
-    for shape in ((64, 4, 16), (256, 2, 8)):
+    for shape in ((64, 4, 16, 1), (256, 2, 8, 1), (64, 1, 16, 0), (256, 1, 8, 0)):
         b.set_config(*shape)
         b.render()
         for (rgb, _), ref in zip(bufs, before):

@@ -1,0 +1,40 @@
+"""The C restatement against the reference itself at FULL benchmark size:
+the reference's own bvh + ray_tracer() + clip_image_to_rgb (compiled from
+its sources by oracle/refbuild/Makefile) on the icosphere 512^2 and terrain
+1920x1080 frames.  Runs where the reference harness was built (x86-64 with
+the reference tree present); skipped elsewhere."""
+import os
+
+import numpy as np
+import pytest
+
+from parity import PIX_FRAC, compare_hits, pixel_agreement
+
+
+@pytest.fixture(scope="module")
+def ref(oracle):
+    if not oracle.ref_available():
+        pytest.skip("reference harness not built on this host")
+    return oracle
+
+
+@pytest.mark.parametrize("workload", ["icosphere", "terrain"])
+def test_full_frame_restatement_equals_reference(ref, workload):
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene() if workload == "icosphere" else scenes.terrain_scene()
+    rs = ref.RefScene(scene, frame["material"])
+    rr = rs.render(frame)
+    osc = ref.OracleScene(scene)
+    ro = osc.render(frame, threads=os.cpu_count() or 1, want_ids=True)
+    within1, exact, _ = pixel_agreement(ro["rgb"], rr["rgb"])
+    assert exact >= 0.9999 and within1 >= PIX_FRAC, (exact, within1)
+    # primary hits of the reference's own traversal on the reference's camera rays
+    og, dr = ref.camera_rays(frame["camera"], lib=ref.ref_lib())
+    step = 7 if workload == "terrain" else 1
+    og, dr = og[::step], dr[::step]
+    rid, rt, _, _ = rs.closest(og, dr)
+    oid, ot, _, _ = osc.closest(og, dr)
+    mismatch, excluded = compare_hits(scene["verts"], scene["tris"], og, dr, oid, ot, rid, rt)
+    assert not mismatch.any()
+    same = oid == rid
+    assert np.array_equal(ot[same].view(np.uint32), rt[same].view(np.uint32))
