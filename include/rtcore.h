@@ -129,9 +129,10 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
  * instrumented kernel that counts node loads and triangle tests into
  * rt_render_stats (for roofline accounting; slower, off by default). */
 #define RT_OPT_COUNT_FETCHES 1
-/* RT_OPT_RENDER_KERNEL: RT_KERNEL_WAVE (default) -- lanes replace finished
- * rays at once (primary -> secondary rays -> next pixel); RT_KERNEL_PIXEL --
- * one pixel per lane until the whole warp's tile is done.  Same results. */
+/* RT_OPT_RENDER_KERNEL: RT_KERNEL_PIXEL (default) -- one pixel per lane, a
+ * warp takes the next tile when all its pixels are done; RT_KERNEL_WAVE --
+ * lanes replace finished rays (primary -> secondary rays -> next pixel),
+ * shading and refills batched across lanes.  Same results. */
 #define RT_OPT_RENDER_KERNEL 2
 #define RT_KERNEL_WAVE 0
 #define RT_KERNEL_PIXEL 1

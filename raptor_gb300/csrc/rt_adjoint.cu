@@ -314,6 +314,7 @@ rt_status rt_render_float(rt_scene *s, const rt_camera *camera, const rt_light *
     Guard g(ctx->device);
     LightSet ls;
     ls.n = nlights;
+    ls.fast_pow = 0;
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     static const int grid = grid_of(k_diff<false>, ctx->sm_count);
     RT_CUDA_A(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
@@ -339,6 +340,7 @@ rt_status rt_render_adjoint(rt_scene *s, const rt_camera *camera, const rt_light
     Guard g(ctx->device);
     LightSet ls;
     ls.n = nlights;
+    ls.fast_pow = 0;
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     static const int grid = grid_of(k_diff<true>, ctx->sm_count);
     const size_t gbytes = (size_t)(s->nverts > 0 ? s->nverts : 1) * 3 * sizeof(float);

@@ -158,6 +158,17 @@ SceneView scene_view(const rt_scene *s)
 }
 
 rt_status set_error(rt_status code, const char *msg) { return fail(code, msg); }
+
+bool fast_pow_ok(const rt_light *lights, int32_t n, const rt_material &m)
+{
+    if (n > RT_MAX_LIGHTS) return false;
+    for (int c = 0; c < 3; ++c)
+        if (!(m.ks[c] >= 0.0f && m.ks[c] <= 255.0f)) return false;
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c)
+            if (!(lights[i].rgb[c] >= 0.0f && lights[i].rgb[c] <= 255.0f) || !(lights[i].d >= 0.0f)) return false;
+    return true;
+}
 rt_status set_cuda_error(cudaError_t e, const char *what) { return cuda_fail(e, what); }
 
 // Copy n bytes of a caller buffer (host or device) into a device buffer.
@@ -559,6 +570,7 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     if (st != RT_OK) return st;
     LightSet ls;
     ls.n = nlights;
+    ls.fast_pow = fast_pow_ok(lights, nlights, *material) ? 1 : 0;
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");

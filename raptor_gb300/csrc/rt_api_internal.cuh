@@ -38,7 +38,7 @@ struct rt_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rtc::DevBuf stage_a, stage_b, stage_c;
     bool count_fetches = false;
-    int render_kernel = RT_KERNEL_WAVE;
+    int render_kernel = RT_KERNEL_PIXEL;
 };
 
 struct rt_scene {

@@ -14,28 +14,14 @@
 
 #include "rt_api_internal.cuh"
 #include "rt_build.cuh"
-#include "rt_shade.cuh"
+#include "rt_wave.cuh"
 
 using namespace rtc;
 
 namespace rtc {
 
-struct BatchJob {
-    SceneView sc;
-    CameraView cam;
-    MaterialView mat;
-    LightView lights[RT_MAX_JOB_LIGHTS];
-    int32_t nlights;
-    int32_t mode;
-    int32_t ao_samples;
-    float ao_dist;
-    uint32_t ao_seed;
-    int32_t tiles_x;
-    int32_t items_begin;
-    int32_t items_end;
-    uint8_t *rgb;
-    int32_t *ids;
-};
+// A batch job is a FrameJob (rt_wave.cuh).
+using BatchJob = FrameJob;
 
 namespace {
 
@@ -68,7 +54,8 @@ __global__ void __launch_bounds__(256) k_render_batched(const BatchJob *__restri
                     po = shade_pixel_ao<false>(J.sc, J.cam, J.mat, J.ao_samples, J.ao_dist, J.ao_seed, x, y, status,
                                                nullptr);
                 else
-                    po = shade_pixel_lights<false>(J.sc, J.cam, J.lights, J.nlights, J.mat, x, y, status, nullptr);
+                    po = shade_pixel_lights<false>(J.sc, J.cam, J.lights, J.nlights, J.mat, x, y, status, nullptr,
+                                                   J.fast_pow != 0);
                 const size_t pix = (size_t)x + (size_t)y * (size_t)J.cam.xres;
                 store_rgb(J.rgb, pix, po.c);
                 if (J.ids) J.ids[pix] = po.id;
@@ -82,130 +69,13 @@ __global__ void __launch_bounds__(256) k_render_batched(const BatchJob *__restri
 }
 
 // Lane-replacement form: every lane carries a pixel of any job and refills
-// from the shared queue as soon as its pixel is stored (see rt_wave.cu).
+// from the shared queue (rt_wave.cuh).
 template <int TW>
 __global__ void __launch_bounds__(256) k_render_batched_wave(const BatchJob *__restrict__ jobs, int32_t njobs,
                                                              int32_t total_items, Counters *ctr)
 {
     extern __shared__ LaneShade wave_state[];
-    LaneShade &S = wave_state[threadIdx.x];
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t lanes_below = (1u << lane) - 1u;
-    uint2 stack[kStackSize];
-    Trav T;
-    uint32_t status = 0, n_primary = 0, n_hits = 0, n_secondary = 0;
-    int x = 0, y = 0, j = 0;
-    int phase = -1;
-    bool queue_open = true;
-    for (;;) {
-        const bool need = phase < 0 && queue_open;
-        const uint32_t needmask = __ballot_sync(0xffffffffu, need);
-        if (needmask) {
-            const int leader = __ffs(needmask) - 1;
-            int base = 0;
-            if ((int)lane == leader) base = atomicAdd(&ctr->work, __popc(needmask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (base + __popc(needmask) >= total_items) queue_open = false;
-            if (need) {
-                const int item = base + __popc(needmask & lanes_below);
-                if (item < total_items) {
-                    int lo = 0, hi = njobs - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (__ldg(&jobs[mid].items_begin) <= item) lo = mid; else hi = mid - 1;
-                    }
-                    j = lo;
-                    const BatchJob &J = jobs[j];
-                    tile_pixel<TW>(item - J.items_begin, J.tiles_x, x, y);
-                    if (x < J.cam.xres && y < J.cam.yres) {
-                        const RayState r = camera_ray(J.cam, x, y);
-                        trav_begin(T, J.sc, r.o, r.d, FLT_MAX, false);
-                        phase = 0;
-                    }
-                }
-            }
-        }
-        if (!__any_sync(0xffffffffu, phase >= 0)) {
-            if (!queue_open) break;
-            continue;
-        }
-        if (phase < 0) continue;
-        const BatchJob &J = jobs[j];
-        if (!trav_step<false>(T, stack, J.sc, phase > 0, status, nullptr)) continue;
-        const bool ao = J.mode == RT_JOB_AO;
-        const int nsec = ao ? J.ao_samples : J.nlights;
-        bool done = false;
-        if (phase == 0) {
-            ++n_primary;
-            S.c = J.cam.background;
-            S.id = -1;
-            S.made = 0;
-            if (T.hit.t < FLT_MAX) {
-                ++n_hits;
-                RayState r;
-                r.o = T.o;
-                r.d = T.d;
-                const SurfacePoint sp = surface_at(J.sc, r, T.hit);
-                S.id = T.hit.id - J.sc.tri_base;
-                S.kd = material_kd(J.mat, sp);
-                S.sn = sp.sn;
-                S.geo = sp.geo;
-                S.start = offset_start(sp.dst, sp.geo);
-                S.vd = T.d;
-                S.c = make_float3(0.f, 0.f, 0.f);
-                if (nsec > 0) {
-                    phase = 1;
-                } else {
-                    S.c = xadd3(S.c, J.mat.ka);
-                    done = true;
-                }
-            } else {
-                done = true;
-            }
-        } else {
-            ++n_secondary;
-            const int k = phase - 1;
-            if (ao) {
-                if (!T.occluded) ++S.made;
-            } else {
-                float3 ldir;
-                float len;
-                shadow_ray(J.lights[k], S.start, ldir, len);
-                float3 c = S.c;
-                phong_add(J.lights[k], J.mat, S.kd, S.sn, S.vd, ldir, len, T.occluded ? 0.0f : 1.0f, c);
-                S.c = c;
-            }
-            if (phase < nsec) {
-                ++phase;
-            } else {
-                if (ao) S.c = xadd3(xmul3(S.kd, xdiv((float)S.made, (float)nsec)), J.mat.ka);
-                else S.c = xadd3(S.c, J.mat.ka);
-                done = true;
-            }
-        }
-        if (!done) {
-            const int k = phase - 1;
-            if (ao) {
-                const AOBasis ob = ao_basis(S.geo);
-                const uint32_t pix = (uint32_t)x + (uint32_t)y * (uint32_t)J.cam.xres;
-                trav_begin(T, J.sc, S.start, ao_direction(ob, pix, (uint32_t)k, J.ao_seed), J.ao_dist, true);
-            } else {
-                float3 ldir;
-                float len;
-                shadow_ray(J.lights[k], S.start, ldir, len);
-                trav_begin(T, J.sc, S.start, ldir, len, true);
-            }
-        } else {
-            const size_t pix = (size_t)x + (size_t)y * (size_t)J.cam.xres;
-            store_rgb(J.rgb, pix, S.c);
-            if (J.ids) J.ids[pix] = S.id;
-            phase = -1;
-        }
-    }
-    warp_add(&ctr->primary, n_primary);
-    warp_add(&ctr->hits, n_hits);
-    warp_add(&ctr->secondary, n_secondary);
-    if (status) atomicOr(&ctr->status, status);
+    wave_loop<TW, false>(nullptr, jobs, njobs, total_items, wave_state[threadIdx.x], ctr);
 }
 
 template <int TW>
@@ -250,7 +120,7 @@ struct rt_batch {
     BatchJob *d_jobs = nullptr;
     int32_t total_items = 0;
     // launch configuration and its captured graph
-    rt_tune_config cfg{128, 1, 8, RT_KERNEL_WAVE, 0.f};
+    rt_tune_config cfg{128, 1, 8, RT_KERNEL_PIXEL, 0.f};
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
 };
@@ -532,6 +402,7 @@ rt_status rt_batch_set_jobs(rt_batch *b, const rt_job *jobs, int32_t njobs)
         B.mat = make_material_view(J.material);
         B.nlights = J.mode == RT_JOB_SHADOW ? J.nlights : 0;
         for (int l = 0; l < B.nlights; ++l) B.lights[l] = make_light_view(J.lights[l]);
+        B.fast_pow = fast_pow_ok(J.lights, B.nlights, J.material) ? 1 : 0;
         B.mode = J.mode;
         B.ao_samples = J.ao_samples;
         B.ao_dist = J.ao_dist;

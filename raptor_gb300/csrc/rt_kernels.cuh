@@ -21,8 +21,14 @@ struct Counters {
 
 struct LightSet {
     int32_t n;
+    int32_t fast_pow;   // single-precision specular power + exact re-shade near truncation
     LightView l[RT_MAX_LIGHTS];
 };
+
+// The fast specular path is exact in RGB8 when every light intensity and the
+// specular colour stay in the reference's 0..255 ranges (shading error bound
+// of kTruncGuard).
+bool fast_pow_ok(const rt_light *lights, int32_t n, const rt_material &m);
 
 void launch_trace_closest(const SceneView &sc, const rt_ray *rays, int32_t n, rt_hit *hits, Counters *ctr, int sm_count,
                           cudaStream_t st);

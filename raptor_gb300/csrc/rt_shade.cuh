@@ -60,7 +60,7 @@ struct PixelOut {
 template <bool COUNT>
 __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, const CameraView &cam, const LightView *lights,
                                                        int nl, const MaterialView &mat, int x, int y,
-                                                       uint32_t &status, FetchCount *fc)
+                                                       uint32_t &status, FetchCount *fc, bool fast_pow)
 {
     PixelOut out;
     out.secondary = 0;
@@ -77,6 +77,7 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
         const float3 start = offset_start(sp.dst, sp.geo);
         const float3 kd = material_kd(mat, sp);
         float3 c = make_float3(0.f, 0.f, 0.f);
+        uint32_t blocked_bits = 0;
         for (int l = 0; l < nl; ++l) {
             const LightView &L = lights[l];
             float3 ldir;
@@ -86,9 +87,13 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
             bool blocked;
             status |= traverse<true, COUNT>(sc, start, ldir, len, sh, blocked, fc);
             ++out.secondary;
-            phong_add(L, mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
+            if (blocked) blocked_bits |= 1u << l;
+            if (fast_pow) phong_add<false>(L, mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
+            else phong_add<true>(L, mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
         }
         out.c = xadd3(c, mat.ka);
+        if (fast_pow && near_truncation(out.c))
+            out.c = shade_lights_exact(lights, nl, mat, kd, sp.sn, r.d, start, blocked_bits);
     }
     return out;
 }
@@ -136,7 +141,7 @@ __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const Ca
 struct LaneShade {
     float3 kd, sn, start, c, vd, geo;
     int32_t id;
-    int32_t made;
+    int32_t made;          // AO: unoccluded rays; lights: blocked-light bits
 };
 
 __device__ __forceinline__ void store_rgb(uint8_t *rgb, size_t pix, float3 c)

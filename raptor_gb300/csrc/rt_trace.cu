@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_render(SceneView sc, CameraVi
         po.hit = false;
         po.secondary = 0;
         if (live) {
-            po = shade_pixel_lights<COUNT>(sc, cam, lights.l, lights.n, mat, x, y, status, &fc);
+            po = shade_pixel_lights<COUNT>(sc, cam, lights.l, lights.n, mat, x, y, status, &fc, lights.fast_pow != 0);
             const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
             store_rgb(rgb, pix, po.c);
             if (ids) ids[pix] = po.id;

@@ -336,7 +336,11 @@ __device__ __forceinline__ void shadow_ray(const LightView &L, float3 start, flo
 }
 
 // One light's Phong term (coloured_mapper_shader.cc:76-109,
-// light::get_light_intensity light.h:44-59) added into c.
+// light::get_light_intensity light.h:44-59) added into c.  EXACT = true
+// evaluates the specular power in double and rounds once, the reference's
+// result; EXACT = false uses single-precision powf (a few ulp), whose frames
+// are made exact by exact_if_near_boundary below.
+template <bool EXACT = true>
 __device__ __forceinline__ void phong_add(const LightView &L, const MaterialView &m, const float3 kd, const float3 sn,
                                           const float3 view_dir, const float3 ldir, float len, float magn, float3 &c)
 {
@@ -346,7 +350,7 @@ __device__ __forceinline__ void phong_add(const LightView &L, const MaterialView
     const float rdr = xdot(view_dir, ref);
     float3 sc = make_float3(xmul(shade, kd.x), xmul(shade, kd.y), xmul(shade, kd.z));
     if (rdr > 0.0f) {
-        const float p = (float)pow((double)rdr, (double)m.ns);
+        const float p = EXACT ? (float)pow((double)rdr, (double)m.ns) : powf(rdr, m.ns);
         sc = make_float3(xadd(sc.x, xmul(p, m.ks.x)), xadd(sc.y, xmul(p, m.ks.y)), xadd(sc.z, xmul(p, m.ks.z)));
     }
     const float dist = xmul(len, L.d);
@@ -360,6 +364,37 @@ __device__ __forceinline__ void phong_add(const LightView &L, const MaterialView
 __device__ __forceinline__ uint8_t clip8(float v)
 {
     return (uint8_t)__float2uint_rz(smin(255.0f, smax(0.0f, xdiv(v, 1.0f))));
+}
+
+// The single-precision specular power differs from the exact one by a few
+// ulp (<= 1e-6 relative), which moves a colour channel by far less than
+// kTruncGuard; only a channel that close to an integer can truncate
+// differently.
+constexpr float kTruncGuard = 4e-3f;
+__device__ __forceinline__ bool near_integer(float v)
+{
+    const float f = v - floorf(v);
+    return f < kTruncGuard || f > 1.0f - kTruncGuard;
+}
+__device__ __forceinline__ bool near_truncation(float3 c)
+{
+    return near_integer(c.x) || near_integer(c.y) || near_integer(c.z);
+}
+
+// Colour of a hit pixel with the exact specular power, from the stored
+// shading inputs and per-light shadow answers (bit l = light l blocked).
+__device__ __forceinline__ float3 shade_lights_exact(const LightView *lights, int nl, const MaterialView &mat,
+                                                     float3 kd, float3 sn, float3 view_dir, float3 start,
+                                                     uint32_t blocked_bits)
+{
+    float3 c = make_float3(0.f, 0.f, 0.f);
+    for (int l = 0; l < nl; ++l) {
+        float3 ldir;
+        float len;
+        shadow_ray(lights[l], start, ldir, len);
+        phong_add<true>(lights[l], mat, kd, sn, view_dir, ldir, len, ((blocked_bits >> l) & 1u) ? 0.0f : 1.0f, c);
+    }
+    return xadd3(c, mat.ka);
 }
 
 // ---------------------------------------------------------- AO sampler
