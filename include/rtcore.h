@@ -173,6 +173,16 @@ rt_status rt_bvh_build(rt_scene *scene, float *build_ms);
 /* Hierarchy statistics: wide nodes, packed triangle slots, tree depth. */
 rt_status rt_bvh_info(const rt_scene *scene, int32_t *nodes, int32_t *tri_slots, int32_t *depth);
 
+/* Child-slot usage of the built hierarchy (copies the nodes to the host). */
+typedef struct rt_bvh_stats {
+    int64_t nodes;
+    int64_t internal_slots;    /* child slots holding an internal node */
+    int64_t leaf_slots;        /* child slots holding 1..3 triangles */
+    int64_t empty_slots;
+    int64_t leaf_tris[4];      /* leaf slots by triangle count (index 1..3) */
+} rt_bvh_stats;
+rt_status rt_bvh_stats_get(const rt_scene *scene, rt_bvh_stats *out);
+
 /* ---------------------------------------------------------- traversal */
 
 /* Closest hit for n rays.  Replaces ssd::find_nearest_object(const ray*,

@@ -68,6 +68,11 @@ class RtRenderStats(C.Structure):
                 ("tris_tested", C.c_int64)]
 
 
+class RtBvhStats(C.Structure):
+    _fields_ = [("nodes", C.c_int64), ("internal_slots", C.c_int64), ("leaf_slots", C.c_int64),
+                ("empty_slots", C.c_int64), ("leaf_tris", C.c_int64 * 4)]
+
+
 RT_JOB_SHADOW = 0
 RT_JOB_AO = 1
 RT_MAX_JOB_LIGHTS = 2
@@ -106,6 +111,7 @@ SIGNATURES = [
     ("rt_scene_update_vertices", C.c_int32, [_P, _P, C.c_int32]),
     ("rt_bvh_build", C.c_int32, [_P, C.POINTER(C.c_float)]),
     ("rt_bvh_info", C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("rt_bvh_stats_get", C.c_int32, [_P, C.POINTER(RtBvhStats)]),
     ("rt_trace_closest", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_trace_any", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
@@ -265,6 +271,12 @@ class Scene:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         _check(lib().rt_bvh_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return {"nodes": a.value, "tri_slots": b.value, "depth": c.value}
+
+    def stats(self):
+        st = RtBvhStats()
+        _check(lib().rt_bvh_stats_get(self.h, C.byref(st)))
+        return {"nodes": st.nodes, "internal_slots": st.internal_slots, "leaf_slots": st.leaf_slots,
+                "empty_slots": st.empty_slots, "leaf_tris": list(st.leaf_tris)[1:]}
 
     def closest(self, rays):
         n = int(rays.shape[0])

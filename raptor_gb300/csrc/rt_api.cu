@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "rt_build.cuh"
 #include "rt_kernels.cuh"
@@ -436,6 +437,31 @@ rt_status rt_bvh_info(const rt_scene *s, int32_t *nodes, int32_t *tri_slots, int
     if (nodes) *nodes = s->nnodes;
     if (tri_slots) *tri_slots = s->tri_slots;
     if (depth) *depth = s->depth;
+    return RT_OK;
+}
+
+
+rt_status rt_bvh_stats_get(const rt_scene *s, rt_bvh_stats *out)
+{
+    if (!s || !out) return fail(RT_ERR_INVALID_ARG, "rt_bvh_stats_get: NULL argument");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_stats_get: hierarchy not built");
+    memset(out, 0, sizeof(*out));
+    out->nodes = s->nnodes;
+    if (s->nnodes == 0) return RT_OK;
+    DeviceGuard g(s->ctx->device);
+    std::vector<WideNode> h((size_t)s->nnodes);
+    RT_CUDA(cudaMemcpy(h.data(), s->d_nodes, h.size() * sizeof(WideNode), cudaMemcpyDeviceToHost), "node download");
+    for (const WideNode &n : h)
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t m = n.meta[k];
+            if (m == 0) ++out->empty_slots;
+            else if ((n.imask >> k) & 1u) ++out->internal_slots;
+            else {
+                ++out->leaf_slots;
+                const int c = __builtin_popcount(m >> 5);
+                if (c >= 1 && c <= 3) ++out->leaf_tris[c];
+            }
+        }
     return RT_OK;
 }
 

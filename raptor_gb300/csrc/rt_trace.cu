@@ -9,7 +9,7 @@ namespace rtc {
 
 namespace {
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace_closest(SceneView sc, const rt_ray *__restrict__ rays,
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_trace_closest(SceneView sc, const rt_ray *__restrict__ rays,
                                                                  int32_t n, rt_hit *__restrict__ hits,
                                                                  Counters *ctr)
 {
@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_closest(SceneView sc, c
     if (status) atomicOr(&ctr->status, status);
 }
 
-__global__ void __launch_bounds__(kTraceThreads) k_trace_any(SceneView sc, const rt_ray *__restrict__ rays, int32_t n,
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_trace_any(SceneView sc, const rt_ray *__restrict__ rays, int32_t n,
                                                              uint8_t *__restrict__ occluded, Counters *ctr)
 {
     uint32_t status = 0;
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_any(SceneView sc, const
 namespace {
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_render(SceneView sc, CameraView cam, LightSet lights,
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render(SceneView sc, CameraView cam, LightSet lights,
                                                           MaterialView mat, uint8_t *__restrict__ rgb,
                                                           int32_t *__restrict__ ids, Counters *ctr)
 {
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_render(SceneView sc, CameraVi
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_render_ao(SceneView sc, CameraView cam, MaterialView mat,
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_ao(SceneView sc, CameraView cam, MaterialView mat,
                                                              int32_t samples, float ao_dist, uint32_t seed,
                                                              uint8_t *__restrict__ rgb, int32_t *__restrict__ ids,
                                                              int32_t *__restrict__ ao_count, Counters *ctr)

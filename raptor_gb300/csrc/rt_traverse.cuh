@@ -53,6 +53,46 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int s)
     return ((s < 4) ? (lo >> (8 * s)) : (hi >> (8 * (s - 4)))) & 0xffu;
 }
 
+// Quantised byte s of a 64-bit plane as a float.  RT_NODE_PRMT: one byte
+// permute builds 2^23 + q as float bits, an exact subtraction leaves q.
+#ifndef RT_NODE_PRMT
+#define RT_NODE_PRMT 1
+#endif
+__device__ __forceinline__ float qbyte(uint32_t lo, uint32_t hi, int s)
+{
+#if RT_NODE_PRMT
+    const uint32_t w = (s < 4) ? lo : hi;
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)(s & 3))) - 8388608.0f;
+#else
+    return (float)byte_of(lo, hi, s);
+#endif
+}
+
+// max / min of three floats (one instruction with RT_NODE_MINMAX3).
+#ifndef RT_NODE_MINMAX3
+#define RT_NODE_MINMAX3 1
+#endif
+__device__ __forceinline__ float fmax3f(float a, float b, float c)
+{
+#if RT_NODE_MINMAX3
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c)
+{
+#if RT_NODE_MINMAX3
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+
 __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx, const float3 o,
                                                    const float3 inv, uint32_t oct, float tmax)
 {
@@ -86,14 +126,14 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const uint32_t meta = byte_of(meta_lo, meta_hi, s);
-        const float tnx = fmaf((float)byte_of(nxl, nxh, s), sx, ox);
-        const float tny = fmaf((float)byte_of(nyl, nyh, s), sy, oy);
-        const float tnz = fmaf((float)byte_of(nzl, nzh, s), sz, oz);
-        const float tfx = fmaf((float)byte_of(fxl, fxh, s), sx, ox);
-        const float tfy = fmaf((float)byte_of(fyl, fyh, s), sy, oy);
-        const float tfz = fmaf((float)byte_of(fzl, fzh, s), sz, oz);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        const float tnx = fmaf(qbyte(nxl, nxh, s), sx, ox);
+        const float tny = fmaf(qbyte(nyl, nyh, s), sy, oy);
+        const float tnz = fmaf(qbyte(nzl, nzh, s), sz, oz);
+        const float tfx = fmaf(qbyte(fxl, fxh, s), sx, ox);
+        const float tfy = fmaf(qbyte(fyl, fyh, s), sy, oy);
+        const float tfz = fmaf(qbyte(fzl, fzh, s), sz, oz);
+        const float tn = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
+        const float tf = fmin3f(tfx, tfy, fminf(tfz, tmax));
         if (tn <= tf && meta != 0u) {
             if ((imask >> s) & 1u) hits_int |= 1u << (24 + (s ^ oct));
             else hits_tri |= (meta >> 5) << (meta & 31u);

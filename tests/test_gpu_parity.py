@@ -298,3 +298,18 @@ def test_ao_render_vs_oracle(rtlib, ctx, oracle):
     assert np.abs(ga.astype(int) - ra).max() <= 2
     within1, exact, _ = pixel_agreement(out["rgb"], ref["rgb"])
     assert within1 >= PIX_FRAC
+
+
+def test_bvh_slot_accounting(rtlib, ctx):
+    """Every triangle sits in exactly one leaf slot of <= 3 triangles and
+    every non-root node is referenced by exactly one internal slot."""
+    from raptor_gb300 import scenes
+    scene, _ = scenes.terrain_scene(size_pow2=128, xres=64, yres=36)
+    sc = rtlib.Scene(ctx, scene)
+    st = sc.stats()
+    info = sc.info()
+    assert st["nodes"] == info["nodes"]
+    assert st["internal_slots"] == st["nodes"] - 1
+    assert sum(k * n for k, n in zip((1, 2, 3), st["leaf_tris"])) == scene["tris"].shape[0]
+    assert st["leaf_slots"] == sum(st["leaf_tris"])
+    assert st["internal_slots"] + st["leaf_slots"] + st["empty_slots"] == 8 * st["nodes"]
