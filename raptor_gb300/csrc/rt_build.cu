@@ -52,9 +52,19 @@ __global__ void k_prep(const float *__restrict__ verts, const int3 *__restrict__
         bhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
         const float cc[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
         if (nseg > 1) {
-            int *cb = cbounds + 6 * seg[i];
+            // lanes of the same segment (usually the whole warp: a segment's
+            // triangles are contiguous) reduce together; one atomic per group
+            const int si = seg[i];
+            const unsigned grp = __match_any_sync(__activemask(), si);
+            const bool leader = (int)(threadIdx.x & 31) == __ffs(grp) - 1;
+            int *cb = cbounds + 6 * si;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) { atomicMin(&cb[k], ord_of(cc[k])); atomicMax(&cb[3 + k], ord_of(cc[k])); }
+            for (int k = 0; k < 3; ++k) {
+                const int o = ord_of(cc[k]);
+                const int mn = __reduce_min_sync(grp, o);
+                const int mx = __reduce_max_sync(grp, o);
+                if (leader) { atomicMin(&cb[k], mn); atomicMax(&cb[3 + k], mx); }
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < 3; ++k) { cmin[k] = fminf(cmin[k], cc[k]); cmax[k] = fmaxf(cmax[k], cc[k]); }
@@ -209,7 +219,8 @@ __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32
 __global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg_first,
                         const int32_t *__restrict__ first, const int32_t *__restrict__ last,
                         const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
-                        int2 *__restrict__ tasks, int32_t *counters, WideNode *__restrict__ nodes)
+                        int2 *__restrict__ tasks, int32_t *level_count, int32_t *counters,
+                        WideNode *__restrict__ nodes)
 {
     const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nseg) return;
@@ -229,7 +240,7 @@ __global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg
         if (p < 0 || first[p] != f || last[p] != l) { atomicExch(&counters[3], 1); return; }
         root = p;
     }
-    const int slot = atomicAdd(&counters[2], 1);
+    const int slot = atomicAdd(&level_count[0], 1);
     tasks[slot] = make_int2(root, s);
     (void)n;
 }
@@ -263,7 +274,9 @@ struct BuildArgs {
     const uint32_t *flags;
     WideNode *nodes;
     PackedTri *tris;
-    int32_t *counters;            // [0] nodes allocated, [1] triangle slots allocated, [2] next-level tasks, [3] error
+    int32_t *counters;            // [0] nodes allocated, [1] triangle slots allocated, [2] root tasks, [3] error
+    const int32_t *cur_count;     // tasks of this level
+    int32_t *next_count;          // tasks emitted for the next level
     const int2 *tasks_in;         // (binary ref, wide node index)
     int2 *tasks_out;
     int32_t max_nodes;
@@ -283,11 +296,8 @@ __device__ __forceinline__ int32_t ref_first(const BuildArgs &A, int32_t ref) { 
 // One thread per wide node of the current level: gather up to 8 children
 // by repeatedly opening the largest-area internal child (those too big for
 // a leaf first), assign slots by octant, quantise, emit leaves and tasks.
-__global__ void k_collapse(BuildArgs A, int32_t ntasks)
+__device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 task)
 {
-    const int32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ti >= ntasks) return;
-    const int2 task = A.tasks_in[ti];
     const int32_t wide = task.y;
 
     int32_t ch[8];
@@ -405,7 +415,7 @@ __global__ void k_collapse(BuildArgs A, int32_t ntasks)
         if (cnt[k] > kMaxLeafTris) {
             W.imask |= (uint8_t)(1u << s);
             W.meta[s] = (uint8_t)(0x20 | (24 + s));
-            const int slot = atomicAdd(&A.counters[2], 1);
+            const int slot = atomicAdd(A.next_count, 1);
             A.tasks_out[slot] = make_int2(ch[k], child_base + int_k);
             ++int_k;
         } else {
@@ -430,6 +440,15 @@ __global__ void k_collapse(BuildArgs A, int32_t ntasks)
         }
     }
     A.nodes[wide] = W;
+}
+
+// One tree level: every task of the level (count read on the device, so
+// the levels run back to back without host round trips).
+__global__ void k_collapse_level(BuildArgs A)
+{
+    const int32_t ntasks = *A.cur_count;
+    for (int32_t ti = blockIdx.x * blockDim.x + threadIdx.x; ti < ntasks; ti += gridDim.x * blockDim.x)
+        collapse_task(A, A.tasks_in[ti]);
 }
 
 }  // namespace
@@ -490,6 +509,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     int2 *tq0 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
     int2 *tq1 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
     int32_t *counters = (int32_t *)carve(p, 16 * sizeof(int32_t));
+    int32_t *level_count = (int32_t *)carve(p, (kMaxDepth + 2) * sizeof(int32_t));
     int *cbounds = (int *)carve(p, 6 * (size_t)nseg * sizeof(int));
     int32_t *seg_first = (int32_t *)carve(p, ((size_t)nseg + 1) * sizeof(int32_t));
     size_t cub_bytes = 0;
@@ -527,15 +547,13 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
         }
     }
-    // segment roots -> level-0 tasks; wide nodes 0..nseg-1 are the roots
-    k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0, counters,
-                                                in.nodes);
+    // segment roots -> level-0 tasks (counted in level_count[0]); wide nodes
+    // 0..nseg-1 are the roots
+    cudaMemsetAsync(level_count, 0, (kMaxDepth + 2) * sizeof(int32_t), st);
+    k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0,
+                                                level_count, counters, in.nodes);
     const int32_t nroot_nodes = nseg;
     cudaMemcpyAsync(&counters[0], &nroot_nodes, sizeof(int32_t), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
-    if (h_cnt[3]) { R.status = -8; return R; }
-    int32_t ntasks = h_cnt[2], depth = 0;
 
     BuildArgs A;
     A.n = n; A.left = left; A.right = right; A.first = first; A.last = last;
@@ -543,18 +561,22 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
     A.max_nodes = in.max_nodes;
-    while (ntasks > 0) {
-        if (depth >= kMaxDepth) { R.status = -5; return R; }
-        A.tasks_in = (depth & 1) ? tq1 : tq0;
-        A.tasks_out = (depth & 1) ? tq0 : tq1;
-        cudaMemsetAsync(&counters[2], 0, sizeof(int32_t), st);
-        k_collapse<<<(ntasks + 63) / 64, 64, 0, st>>>(A, ntasks);
-        cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
-        if (h_cnt[3]) { R.status = -8; return R; }
-        ntasks = h_cnt[2];
-        ++depth;
+    // all levels back to back; a level past the last one finds no tasks
+    const int cgrid = max(1, min((n + nseg + 63) / 64, in.sm_count * 16));
+    for (int level = 0; level < kMaxDepth; ++level) {
+        A.tasks_in = (level & 1) ? tq1 : tq0;
+        A.tasks_out = (level & 1) ? tq0 : tq1;
+        A.cur_count = level_count + level;
+        A.next_count = level_count + level + 1;
+        k_collapse_level<<<cgrid, 64, 0, st>>>(A);
     }
+    cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(h_cnt + 4, level_count, (kMaxDepth + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+    if (h_cnt[3]) { R.status = -8; return R; }
+    if (h_cnt[4 + kMaxDepth] != 0) { R.status = -5; return R; }   // deeper than kMaxDepth levels
+    int depth = 0;
+    while (depth < kMaxDepth && h_cnt[4 + depth] > 0) ++depth;
     R.status = 0;
     R.nodes = h_cnt[0];
     R.tri_slots = h_cnt[1];

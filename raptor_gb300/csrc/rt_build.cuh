@@ -15,7 +15,7 @@ struct BuildInputs {
     PackedTri *tris;          // device out, ntris
     int32_t max_nodes;
     int32_t sm_count;
-    int32_t *host_scratch;    // pinned host, >= 4 ints
+    int32_t *host_scratch;    // pinned host, >= 5 + kMaxDepth ints
     // several scenes in one build (a batch): segment of each triangle and
     // the triangle offset of each segment (nseg + 1 entries, host or device).
     // nseg <= 1: a single scene, both may be nullptr.  Segment s's root is
