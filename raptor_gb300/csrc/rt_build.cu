@@ -428,12 +428,10 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
                 const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
                 const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
                 const float3 cc = make_float3(A.verts[3 * t.z], A.verts[3 * t.z + 1], A.verts[3 * t.z + 2]);
-                const float3 e1 = xsub3(cc, a);   // triangle.h:193
-                const float3 e2 = xsub3(b, a);    // triangle.h:194
                 PackedTri P;
-                P.w0 = make_float4(a.x, a.y, a.z, e1.x);
-                P.w1 = make_float4(e1.y, e1.z, e2.x, e2.y);
-                P.w2 = make_float4(e2.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
+                P.w0 = make_float4(a.x, a.y, a.z, b.x);
+                P.w1 = make_float4(b.y, b.z, cc.x, cc.y);
+                P.w2 = make_float4(cc.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
                 A.tris[tri_base + tri_off + j] = P;
             }
             tri_off += c;

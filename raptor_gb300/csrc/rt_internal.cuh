@@ -40,12 +40,13 @@ struct __align__(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
 
-// Packed triangle in leaf order: vertex a, e1 = c - a, e2 = b - a (the
-// reference's edge vectors, triangle.h:193-194) and the caller's id: 48 B.
+// Packed triangle in leaf order: vertices a, b, c (exactly the caller's, so
+// neighbouring triangles share bit-identical edges), the caller's id and
+// flags: 48 B.
 struct __align__(16) PackedTri {
-    float4 w0;   // a.x a.y a.z e1.x
-    float4 w1;   // e1.y e1.z e2.x e2.y
-    float4 w2;   // e2.z id(bits) flags(bits) 0
+    float4 w0;   // a.x a.y a.z b.x
+    float4 w1;   // b.y b.z c.x c.y
+    float4 w2;   // c.z id(bits) flags(bits) 0
 };
 
 // Per-triangle shading record in the caller's order: face normal n
@@ -67,6 +68,7 @@ struct SceneView {
     int32_t nnodes;
     int32_t root;             // root wide node of this scene
     int32_t tri_base;         // subtracted from packed ids to give the caller's ids
+    int32_t isect;            // RT_ISECT_REFERENCE or RT_ISECT_WATERTIGHT
 };
 
 struct CameraView {

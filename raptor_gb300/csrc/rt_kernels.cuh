@@ -7,9 +7,11 @@ namespace rtc {
 
 constexpr int kTraceThreads = 128;   // 4 warps per block
 // Minimum resident blocks per SM the render/trace kernels are compiled for
-// (caps registers per thread: 1 -> 255, 6 -> 80, 8 -> 64).
+// (caps registers per thread: 1 -> 255, 6 -> 80, 8 -> 64; 8 measured fastest:
+// more resident warps hide the latency of the node loads better than the
+// registers the cap spills).
 #ifndef RT_RENDER_MIN_BLOCKS
-#define RT_RENDER_MIN_BLOCKS 1
+#define RT_RENDER_MIN_BLOCKS 8
 #endif
 constexpr int kBlocksPerSM = 8;      // persistent grid = SMs x 8 blocks
 
