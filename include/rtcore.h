@@ -136,6 +136,14 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
 #define RT_OPT_RENDER_KERNEL 2
 #define RT_KERNEL_WAVE 0
 #define RT_KERNEL_PIXEL 1
+/* RT_OPT_INTERSECTOR: RT_ISECT_REFERENCE (default) -- the reference's
+ * Moller-Trumbore arithmetic (triangle.h:190-235), bit-identical hits;
+ * RT_ISECT_WATERTIGHT -- the watertight test of Woop, Benthin and Wald
+ * (JCGT 2013): no ray passes between two triangles that share an edge; t
+ * agrees with the reference to ~1e-6 relative, ids away from edges. */
+#define RT_OPT_INTERSECTOR 3
+#define RT_ISECT_REFERENCE 0
+#define RT_ISECT_WATERTIGHT 1
 rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value);
 /* Message of the last error on the calling thread ("" if none). */
 const char *rt_last_error_string(void);

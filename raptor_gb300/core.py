@@ -30,6 +30,9 @@ RT_OPT_COUNT_FETCHES = 1
 RT_OPT_RENDER_KERNEL = 2
 RT_KERNEL_WAVE = 0
 RT_KERNEL_PIXEL = 1
+RT_OPT_INTERSECTOR = 3
+RT_ISECT_REFERENCE = 0
+RT_ISECT_WATERTIGHT = 1
 
 
 class RtError(RuntimeError):

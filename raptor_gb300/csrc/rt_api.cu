@@ -155,6 +155,7 @@ SceneView scene_view(const rt_scene *s)
     v.nnodes = s->built ? s->nnodes : 0;
     v.root = 0;
     v.tri_base = 0;
+    v.isect = s->ctx->isect;
     return v;
 }
 
@@ -271,6 +272,12 @@ rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
     if (!ctx) return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: NULL context");
     if (option == RT_OPT_COUNT_FETCHES) {
         ctx->count_fetches = value != 0;
+        return RT_OK;
+    }
+    if (option == RT_OPT_INTERSECTOR) {
+        if (value != RT_ISECT_REFERENCE && value != RT_ISECT_WATERTIGHT)
+            return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown intersector");
+        ctx->isect = (int)value;
         return RT_OK;
     }
     if (option == RT_OPT_RENDER_KERNEL) {

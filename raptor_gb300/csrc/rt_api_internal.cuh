@@ -39,6 +39,7 @@ struct rt_context {
     rtc::DevBuf stage_a, stage_b, stage_c;
     bool count_fetches = false;
     int render_kernel = RT_KERNEL_PIXEL;
+    int isect = RT_ISECT_REFERENCE;
 };
 
 struct rt_scene {

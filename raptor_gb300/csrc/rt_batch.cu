@@ -363,7 +363,7 @@ rt_status rt_bvh_build_batched(rt_batch *b, float *build_ms)
         const int s = j.sc.root;
         j.sc.nodes = b->d_nodes; j.sc.tris = b->d_tris; j.sc.shade = b->d_shade; j.sc.idx = b->d_idx;
         j.sc.vattr = b->has_attr[s] ? b->d_vattr : nullptr; j.sc.flags = b->d_flags;
-        j.sc.ntris = ntris; j.sc.nnodes = b->nnodes; j.sc.tri_base = b->tri_off[s];
+        j.sc.ntris = ntris; j.sc.nnodes = b->nnodes; j.sc.tri_base = b->tri_off[s]; j.sc.isect = b->ctx->isect;
     }
     if (!b->h_jobs.empty()) return layout_jobs(b);
     return RT_OK;
@@ -398,6 +398,7 @@ rt_status rt_batch_set_jobs(rt_batch *b, const rt_job *jobs, int32_t njobs)
         B.sc.nnodes = b->nnodes;
         B.sc.root = s;
         B.sc.tri_base = b->tri_off[s];
+        B.sc.isect = b->ctx->isect;
         B.cam = make_camera_view(J.camera);
         B.mat = make_material_view(J.material);
         B.nlights = J.mode == RT_JOB_SHADOW ? J.nlights : 0;

@@ -24,8 +24,10 @@ __device__ __forceinline__ float mt_intersect(const float4 w0, const float4 w1, 
                                               const float3 d, float &u_out, float &v_out)
 {
     const float3 a = make_float3(w0.x, w0.y, w0.z);
-    const float3 e1 = make_float3(w0.w, w1.x, w1.y);
-    const float3 e2 = make_float3(w1.z, w1.w, w2.x);
+    const float3 b = make_float3(w0.w, w1.x, w1.y);
+    const float3 c = make_float3(w1.z, w1.w, w2.x);
+    const float3 e1 = xsub3(c, a);   // triangle.h:193
+    const float3 e2 = xsub3(b, a);   // triangle.h:194
     const float3 P = xcross(d, e2);
     const float det = xdot(e1, P);
     const float inv_det = __frcp_rn(det);      // == 1.0f / det, correctly rounded
@@ -38,6 +40,84 @@ __device__ __forceinline__ float mt_intersect(const float4 w0, const float4 w1, 
     u_out = u;
     v_out = v;
     return reject ? __int_as_float(0x7f800000) : t;
+}
+
+// Per-ray constants of the watertight test: the axis of largest |d| is z
+// (kx, ky follow, swapped when d.z < 0 to keep the winding), and the shear
+// that maps the ray to +z.
+struct Shear {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ float comp(const float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ Shear make_shear(const float3 d)
+{
+    Shear s;
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    s.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+    s.kx = (s.kz + 1) % 3;
+    s.ky = (s.kx + 1) % 3;
+    if (comp(d, s.kz) < 0.0f) { const int t = s.kx; s.kx = s.ky; s.ky = t; }
+    const float dz = comp(d, s.kz);
+    s.sx = comp(d, s.kx) / dz;
+    s.sy = comp(d, s.ky) / dz;
+    s.sz = 1.0f / dz;
+    return s;
+}
+
+// Watertight ray/triangle test of Woop, Benthin and Wald (JCGT 2013): the
+// three edge functions are evaluated in the ray's sheared frame from the
+// exact vertex positions, so two triangles sharing an edge always agree on
+// which side a ray passes (no ray leaks through a shared edge); an edge
+// function that rounds to exactly zero is re-evaluated in double.  Returns
+// t (accepting t > 0 here; the caller applies EPSILON), or +inf.  u weighs
+// c and v weighs b, as in the reference.
+__device__ __forceinline__ float wt_intersect(const float4 w0, const float4 w1, const float4 w2, const float3 o,
+                                              const Shear &sh, float &u_out, float &v_out)
+{
+    const float3 A = make_float3(w0.x - o.x, w0.y - o.y, w0.z - o.z);
+    const float3 B = make_float3(w0.w - o.x, w1.x - o.y, w1.y - o.z);
+    const float3 C = make_float3(w1.z - o.x, w1.w - o.y, w2.x - o.z);
+    const float Az = comp(A, sh.kz), Bz = comp(B, sh.kz), Cz = comp(C, sh.kz);
+    const float Ax = comp(A, sh.kx) - sh.sx * Az, Ay = comp(A, sh.ky) - sh.sy * Az;
+    const float Bx = comp(B, sh.kx) - sh.sx * Bz, By = comp(B, sh.ky) - sh.sy * Bz;
+    const float Cx = comp(C, sh.kx) - sh.sx * Cz, Cy = comp(C, sh.ky) - sh.sy * Cz;
+    // uncontracted products: an edge shared by two triangles gives exactly
+    // negated edge functions in both
+    float U = xsub(xmul(Cx, By), xmul(Cy, Bx));
+    float V = xsub(xmul(Ax, Cy), xmul(Ay, Cx));
+    float W = xsub(xmul(Bx, Ay), xmul(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    const float inf = __int_as_float(0x7f800000);
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return inf;
+    const float det = U + V + W;
+    if (det == 0.0f) return inf;
+    const float T = (U * (sh.sz * Az) + V * (sh.sz * Bz)) + W * (sh.sz * Cz);
+    const float inv = 1.0f / det;
+    const float t = T * inv;
+    if (!(t > 0.0f)) return inf;
+    u_out = W * inv;   // weight of c
+    v_out = V * inv;   // weight of b
+    return t;
+}
+
+// Out-of-line entry to the watertight test (shear set up per call), so the
+// default reference-exact path keeps its registers.
+__device__ __noinline__ float wt_intersect_ray(const float4 w0, const float4 w1, const float4 w2, const float3 o,
+                                               const float3 d, float *u_out, float *v_out)
+{
+    const Shear sh = make_shear(d);
+    float u = 0.f, v = 0.f;
+    const float t = wt_intersect(w0, w1, w2, o, sh, u, v);
+    *u_out = u;
+    *v_out = v;
+    return t;
 }
 
 // Child-box test of one wide node: returns internal-hit bits (24..31,
@@ -227,6 +307,7 @@ __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView
         T.ngroup = nh.ngroup;
         tgroup = nh.tgroup;
     }
+    const bool watertight = sc.isect == RT_ISECT_WATERTIGHT;
     while (tgroup.y != 0u) {
         const uint32_t k = __ffs(tgroup.y) - 1u;
         tgroup.y &= tgroup.y - 1u;
@@ -238,7 +319,8 @@ __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView
         const float4 w1 = __ldg(&tp->w1);
         const float4 w2 = __ldg(&tp->w2);
         float u, v;
-        const float t = mt_intersect(w0, w1, w2, T.o, T.d, u, v);
+        const float t = watertight ? wt_intersect_ray(w0, w1, w2, T.o, T.d, &u, &v)
+                                   : mt_intersect(w0, w1, w2, T.o, T.d, u, v);
         const int32_t id = __float_as_int(w2.y);
         if ((uint32_t)id >= (uint32_t)sc.ntris) { status |= kStatusBadIndex; continue; }
         if (any) {
