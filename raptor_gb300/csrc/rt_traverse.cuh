@@ -109,7 +109,7 @@ __device__ __forceinline__ float wt_intersect(const float4 w0, const float4 w1, 
 
 // Out-of-line entry to the watertight test (shear set up per call), so the
 // default reference-exact path keeps its registers.
-__device__ __noinline__ float wt_intersect_ray(const float4 w0, const float4 w1, const float4 w2, const float3 o,
+static __device__ __noinline__ float wt_intersect_ray(const float4 w0, const float4 w1, const float4 w2, const float3 o,
                                                const float3 d, float *u_out, float *v_out)
 {
     const Shear sh = make_shear(d);
