@@ -81,9 +81,11 @@ __device__ __forceinline__ float wt_intersect(const float4 w0, const float4 w1, 
     const float3 B = make_float3(w0.w - o.x, w1.x - o.y, w1.y - o.z);
     const float3 C = make_float3(w1.z - o.x, w1.w - o.y, w2.x - o.z);
     const float Az = comp(A, sh.kz), Bz = comp(B, sh.kz), Cz = comp(C, sh.kz);
-    const float Ax = comp(A, sh.kx) - sh.sx * Az, Ay = comp(A, sh.ky) - sh.sy * Az;
-    const float Bx = comp(B, sh.kx) - sh.sx * Bz, By = comp(B, sh.ky) - sh.sy * Bz;
-    const float Cx = comp(C, sh.kx) - sh.sx * Cz, Cy = comp(C, sh.ky) - sh.sy * Cz;
+    // every vertex is sheared by the same uncontracted operations, so a
+    // vertex shared by several triangles lands on the same point in all
+    const float Ax = xsub(comp(A, sh.kx), xmul(sh.sx, Az)), Ay = xsub(comp(A, sh.ky), xmul(sh.sy, Az));
+    const float Bx = xsub(comp(B, sh.kx), xmul(sh.sx, Bz)), By = xsub(comp(B, sh.ky), xmul(sh.sy, Bz));
+    const float Cx = xsub(comp(C, sh.kx), xmul(sh.sx, Cz)), Cy = xsub(comp(C, sh.ky), xmul(sh.sy, Cz));
     // uncontracted products: an edge shared by two triangles gives exactly
     // negated edge functions in both
     float U = xsub(xmul(Cx, By), xmul(Cy, Bx));

@@ -332,8 +332,11 @@ def test_watertight_intersector(rtlib, oracle):
     d = tgt.astype(np.float64) - origin
     d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
     o = np.tile(origin, (d.shape[0], 1))
-    # only targets on the visible side (the ray reaches them before the back)
-    front = (tgt.astype(np.float64) * (origin - tgt)).sum(1) > 0.05
+    # only targets well inside the visible side: at grazing angles a vertex
+    # on the silhouette may lie just outside the projected mesh, a true miss
+    vd = origin.astype(np.float64) - tgt.astype(np.float64)
+    cos_view = (tgt.astype(np.float64) * vd).sum(1) / np.linalg.norm(vd, axis=1) / np.linalg.norm(tgt, axis=1)
+    front = cos_view > 0.2
     c = rtlib.Context(0)
     sc = rtlib.Scene(c, scene)
     ref = sc.closest(rtlib.rays_array(o, d))
