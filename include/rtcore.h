@@ -205,6 +205,21 @@ rt_status rt_trace_closest(rt_scene *scene, const rt_ray *rays, int32_t n, rt_hi
  * when ray i is blocked. */
 rt_status rt_trace_any(rt_scene *scene, const rt_ray *rays, int32_t n, uint8_t *occluded);
 
+/* Closest hit, as rt_trace_closest, for callers that cannot allocate device
+ * memory (an engine whose allocator owns the whole GPU, a real-time loop
+ * that forbids allocation after start-up).  No counterpart in the
+ * reference.  Calls no cudaMalloc or cudaFree: rays and hits (host or
+ * device memory) are staged through one fixed scratch array of
+ * RT_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit.  At most RT_NOALLOC_MAX_RAYS rays per call (RT_ERR_INVALID_ARG
+ * beyond).  The first call on a device looks up the array's address; make
+ * it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, so serialise them (each call synchronises the
+ * context's stream before it returns). */
+#define RT_NOALLOC_MAX_RAYS 16384
+#define RT_NOALLOC_SCRATCH_BYTES (256 + RT_NOALLOC_MAX_RAYS * 48)
+rt_status rt_trace_closest_noalloc(rt_scene *scene, const rt_ray *rays, int32_t n, rt_hit *hits);
+
 /* ------------------------------------------------------------- render */
 
 /* Render one frame: primary ray per pixel, closest hit, one shadow ray per

@@ -117,6 +117,7 @@ SIGNATURES = [
     ("rt_bvh_stats_get", C.c_int32, [_P, C.POINTER(RtBvhStats)]),
     ("rt_trace_closest", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_trace_any", C.c_int32, [_P, _P, C.c_int32, _P]),
+    ("rt_trace_closest_noalloc", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
