@@ -232,6 +232,26 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+NCU_SUMMARY = os.path.join(ROOT, "profiles", "k_render_terrain-2M-1080p_ncu.md")
+
+
+def ncu_traffic():
+    """DRAM bytes (read + write) of one k_render launch on this workload, from
+    the committed ncu summary (a capture cannot run inside the timed bench)."""
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    total, seen = 0.0, 0
+    try:
+        for line in open(NCU_SUMMARY):
+            for name in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                if line.startswith(f"| `{name}` |"):
+                    value, unit = line.split("|")[2].split()
+                    total += float(value) * scale[unit]
+                    seen += 1
+    except (OSError, ValueError, KeyError):
+        return None
+    return total if seen == 2 else None
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -328,7 +348,9 @@ def main():
             "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 3},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None,
+                         "frac": achieved / hbm_peak,
+                         "traffic": ncu_traffic() if args.size == 1024 else None,
+                         "traffic_source": "profiles/k_render_terrain-2M-1080p_ncu.md (one launch, ncu --set full)",
                          "kernel": "k_render<false>", "peak_source": peak_src,
                          "bytes_per_frame": alg_bytes, "nodes_per_ray": nodes_per_frame / frame_rays,
                          "tris_per_ray": tris_per_frame / frame_rays, "kernel_ms": mean_kernel_ms},
