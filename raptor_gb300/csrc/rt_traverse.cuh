@@ -136,15 +136,25 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int s)
 }
 
 // Quantised byte s of a 64-bit plane as a float.  RT_NODE_PRMT: one byte
-// permute builds 2^23 + q as float bits, an exact subtraction leaves q.
+// permute places q in mantissa bits 8..15 of 1.0f, giving exactly
+// 1 + q * 2^-15; intersect_node folds the constant 1 into the node's offset
+// (kQOne below), so a plane costs one permute and one FMA.  Otherwise q
+// itself.
 #ifndef RT_NODE_PRMT
 #define RT_NODE_PRMT 1
+#endif
+#if RT_NODE_PRMT
+constexpr float kQScale = 32768.0f;   // 2^15: one quantisation step per 2^-15
+constexpr float kQOne = 1.0f;         // the byte's value at q = 0
+#else
+constexpr float kQScale = 1.0f;
+constexpr float kQOne = 0.0f;
 #endif
 __device__ __forceinline__ float qbyte(uint32_t lo, uint32_t hi, int s)
 {
 #if RT_NODE_PRMT
     const uint32_t w = (s < 4) ? lo : hi;
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)(s & 3))) - 8388608.0f;
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)(s & 3) << 4)));
 #else
     return (float)byte_of(lo, hi, s);
 #endif
@@ -175,6 +185,26 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c)
 #endif
 }
 
+// Packed single-precision FMA (fma.rn.f32x2, sm_100 family): two plane
+// distances per instruction, each half rounded exactly as fmaf.
+#ifndef RT_NODE_FMA2
+#define RT_NODE_FMA2 0
+#endif
+__device__ __forceinline__ uint64_t pack2f(float a, float b)
+{
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 fma2f(float a0, float a1, uint64_t b, uint64_t c)
+{
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pack2f(a0, a1)), "l"(b), "l"(c));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(d));
+    return r;
+}
+
 __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx, const float3 o,
                                                    const float3 inv, uint32_t oct, float tmax)
 {
@@ -187,12 +217,17 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
     const uint32_t e_imask = __float_as_uint(n0.w);
     const uint32_t ex = e_imask & 0xffu, ey = (e_imask >> 8) & 0xffu, ez = (e_imask >> 16) & 0xffu;
     const uint32_t imask = e_imask >> 24;
-    const float sx = __uint_as_float(ex << 23) * inv.x;
-    const float sy = __uint_as_float(ey << 23) * inv.y;
-    const float sz = __uint_as_float(ez << 23) * inv.z;
-    const float ox = (n0.x - o.x) * inv.x;
-    const float oy = (n0.y - o.y) * inv.y;
-    const float oz = (n0.z - o.z) * inv.z;
+    // plane t = q * step + (origin - o) * inv, evaluated as
+    // qbyte * (step * kQScale) + ((origin - o) * inv - kQOne * step * kQScale):
+    // the folded offset rounds at the magnitude of 2^15 steps, an error below
+    // 2^-9 of one step, far inside the one-step padding of every box
+    const float ux = __uint_as_float(ex << 23) * inv.x;
+    const float uy = __uint_as_float(ey << 23) * inv.y;
+    const float uz = __uint_as_float(ez << 23) * inv.z;
+    const float sx = ux * kQScale, sy = uy * kQScale, sz = uz * kQScale;
+    const float ox = fmaf(-kQOne, sx, (n0.x - o.x) * inv.x);
+    const float oy = fmaf(-kQOne, sy, (n0.y - o.y) * inv.y);
+    const float oz = fmaf(-kQOne, sz, (n0.z - o.z) * inv.z);
     const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
     // lo/hi byte planes; swap per axis so "near" is the entry plane
     uint32_t nxl = __float_as_uint(n2.x), nxh = __float_as_uint(n2.y);   // qlo_x
@@ -205,22 +240,37 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
     if (inv.y < 0.f) { uint32_t t = nyl; nyl = fyl; fyl = t; t = nyh; nyh = fyh; fyh = t; }
     if (inv.z < 0.f) { uint32_t t = nzl; nzl = fzl; fzl = t; t = nzh; nzh = fzh; fzh = t; }
     uint32_t hits_int = 0, hits_tri = 0;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
+    // slot s with its six plane distances: internal children set bit
+    // 24 + (s ^ oct), leaf slots their triangle bits
+    auto slot = [&](int s, float tnx, float tny, float tnz, float tfx, float tfy, float tfz) {
         const uint32_t meta = byte_of(meta_lo, meta_hi, s);
-        const float tnx = fmaf(qbyte(nxl, nxh, s), sx, ox);
-        const float tny = fmaf(qbyte(nyl, nyh, s), sy, oy);
-        const float tnz = fmaf(qbyte(nzl, nzh, s), sz, oz);
-        const float tfx = fmaf(qbyte(fxl, fxh, s), sx, ox);
-        const float tfy = fmaf(qbyte(fyl, fyh, s), sy, oy);
-        const float tfz = fmaf(qbyte(fzl, fzh, s), sz, oz);
         const float tn = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
         const float tf = fmin3f(tfx, tfy, fminf(tfz, tmax));
         if (tn <= tf && meta != 0u) {
             if ((imask >> s) & 1u) hits_int |= 1u << (24 + (s ^ oct));
             else hits_tri |= (meta >> 5) << (meta & 31u);
         }
+    };
+#if RT_NODE_FMA2
+    const uint64_t SX = pack2f(sx, sx), SY = pack2f(sy, sy), SZ = pack2f(sz, sz);
+    const uint64_t OX = pack2f(ox, ox), OY = pack2f(oy, oy), OZ = pack2f(oz, oz);
+#pragma unroll
+    for (int s = 0; s < 8; s += 2) {
+        const float2 tnx = fma2f(qbyte(nxl, nxh, s), qbyte(nxl, nxh, s + 1), SX, OX);
+        const float2 tny = fma2f(qbyte(nyl, nyh, s), qbyte(nyl, nyh, s + 1), SY, OY);
+        const float2 tnz = fma2f(qbyte(nzl, nzh, s), qbyte(nzl, nzh, s + 1), SZ, OZ);
+        const float2 tfx = fma2f(qbyte(fxl, fxh, s), qbyte(fxl, fxh, s + 1), SX, OX);
+        const float2 tfy = fma2f(qbyte(fyl, fyh, s), qbyte(fyl, fyh, s + 1), SY, OY);
+        const float2 tfz = fma2f(qbyte(fzl, fzh, s), qbyte(fzl, fzh, s + 1), SZ, OZ);
+        slot(s, tnx.x, tny.x, tnz.x, tfx.x, tfy.x, tfz.x);
+        slot(s + 1, tnx.y, tny.y, tnz.y, tfx.y, tfy.y, tfz.y);
     }
+#else
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+        slot(s, fmaf(qbyte(nxl, nxh, s), sx, ox), fmaf(qbyte(nyl, nyh, s), sy, oy), fmaf(qbyte(nzl, nzh, s), sz, oz),
+             fmaf(qbyte(fxl, fxh, s), sx, ox), fmaf(qbyte(fyl, fyh, s), sy, oy), fmaf(qbyte(fzl, fzh, s), sz, oz));
+#endif
     NodeHits h;
     h.ngroup = make_uint2(__float_as_uint(n1.x), hits_int | imask);
     h.tgroup = make_uint2(__float_as_uint(n1.y), hits_tri);
