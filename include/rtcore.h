@@ -144,6 +144,15 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
 #define RT_OPT_INTERSECTOR 3
 #define RT_ISECT_REFERENCE 0
 #define RT_ISECT_WATERTIGHT 1
+/* RT_OPT_BUILDER: the binary tree that rt_bvh_build / rt_bvh_build_batched
+ * collapse into 8-wide nodes.  RT_BUILDER_PLOC (default) -- bottom-up
+ * locally-ordered clustering of mutual nearest neighbours over the Morton
+ * order (Meister and Bittner 2018): lower surface area, fewer nodes per
+ * ray; RT_BUILDER_LBVH -- the Morton radix tree (Karras 2012): faster to
+ * build.  Hits do not depend on the tree. */
+#define RT_OPT_BUILDER 4
+#define RT_BUILDER_LBVH 0
+#define RT_BUILDER_PLOC 1
 rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value);
 /* Message of the last error on the calling thread ("" if none). */
 const char *rt_last_error_string(void);

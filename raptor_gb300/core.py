@@ -33,6 +33,9 @@ RT_KERNEL_PIXEL = 1
 RT_OPT_INTERSECTOR = 3
 RT_ISECT_REFERENCE = 0
 RT_ISECT_WATERTIGHT = 1
+RT_OPT_BUILDER = 4
+RT_BUILDER_LBVH = 0
+RT_BUILDER_PLOC = 1
 
 
 class RtError(RuntimeError):

@@ -280,6 +280,12 @@ rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
         ctx->isect = (int)value;
         return RT_OK;
     }
+    if (option == RT_OPT_BUILDER) {
+        if (value != RT_BUILDER_LBVH && value != RT_BUILDER_PLOC)
+            return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown builder");
+        ctx->builder = (int)value;
+        return RT_OK;
+    }
     if (option == RT_OPT_RENDER_KERNEL) {
         if (value != RT_KERNEL_WAVE && value != RT_KERNEL_PIXEL)
             return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown render kernel");
@@ -417,6 +423,7 @@ rt_status rt_bvh_build(rt_scene *s, float *build_ms)
     in.max_nodes = s->ntris + 1;
     in.sm_count = ctx->sm_count;
     in.host_scratch = ctx->h_scratch;
+    in.builder = ctx->builder == RT_BUILDER_LBVH ? kBuilderLbvh : kBuilderPloc;
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
     const BuildResult R = build_wide_bvh(in, s->temp.ptr, s->temp.cap, ctx->stream);
     if (R.status != 0) {

@@ -40,6 +40,7 @@ struct rt_context {
     bool count_fetches = false;
     int render_kernel = RT_KERNEL_PIXEL;
     int isect = RT_ISECT_REFERENCE;
+    int builder = RT_BUILDER_PLOC;
 };
 
 struct rt_scene {

@@ -1,8 +1,12 @@
 // rt_build.cu -- GPU acceleration-structure build for the GB300 ray-tracing
-// core: Morton codes -> radix sort -> binary LBVH (Karras, HPG 2012) ->
-// bottom-up refit -> surface-area-guided collapse into 8-wide nodes with
-// 8-bit quantised child boxes (layout after Ylitie, Karras & Laine, HPG
-// 2017), conservatively rounded outwards so that no hit is ever lost.
+// core: Morton codes -> radix sort -> binary tree -> surface-area-guided
+// collapse into 8-wide nodes with 8-bit quantised child boxes (layout after
+// Ylitie, Karras & Laine, HPG 2017), conservatively rounded outwards so that
+// no hit is ever lost.  The binary tree is either the Morton radix tree
+// (LBVH, Karras HPG 2012, + bottom-up refit) or, by default, bottom-up
+// locally-ordered clustering over the Morton order (PLOC, Meister & Bittner,
+// IEEE TVCG 2018), which merges mutual nearest neighbours by surface area
+// and gives trees with ~15-20 % less internal surface area.
 //
 // Replaces bvh_builder::build (raytracer/spatial_sub_division/
 // bvh_builder.cc:18-178).  The reference builds a 2-wide tree with Morton
@@ -145,7 +149,7 @@ __device__ __forceinline__ int delta(const uint64_t *__restrict__ keys, int32_t 
 // Child refs: >= 0 internal node, < 0 leaf ~k (sorted position k).
 __global__ void k_karras(const uint64_t *__restrict__ keys, int32_t n, int32_t *__restrict__ left,
                          int32_t *__restrict__ right, int32_t *__restrict__ first, int32_t *__restrict__ last,
-                         int32_t *__restrict__ parent, int32_t *__restrict__ leaf_parent)
+                         int32_t *__restrict__ count, int32_t *__restrict__ parent, int32_t *__restrict__ leaf_parent)
 {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
@@ -171,6 +175,7 @@ __global__ void k_karras(const uint64_t *__restrict__ keys, int32_t n, int32_t *
     right[i] = rref;
     first[i] = lo;
     last[i] = hi;
+    count[i] = hi - lo + 1;
     if (lref < 0) leaf_parent[~lref] = i; else parent[lref] = i;
     if (rref < 0) leaf_parent[~rref] = i; else parent[rref] = i;
     if (i == 0) parent[0] = -1;
@@ -251,6 +256,263 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi)
     return dx * dy + dx * dz + dy * dz;
 }
 
+// ------------------------------------------------------------------ PLOC
+//
+// Clusters live in Morton order as two float4 per cluster: (lo.xyz, segment)
+// and (hi.xyz, binary ref), ref >= 0 an internal node, < 0 leaf ~k (sorted
+// position k).  One iteration: every cluster finds its nearest neighbour
+// (smallest merged surface area, lowest index on ties) among the kPlocRadius
+// clusters on either side within its segment; mutual pairs merge into a new
+// internal node at the lower position; a stable compaction keeps the order.
+// An iteration that merged fewer than 1/16 of the clusters makes the next
+// one pair neighbours outright (alternating parity), which bounds the number
+// of iterations on degenerate input (many equal distances).
+//
+// state: [0,1] cluster count, [2,3] next internal node id, [4,5] forced
+// pairing (ping-pong by iteration parity), [6] clusters to end with (one per
+// non-empty segment).
+constexpr int kPlocRadius = 24;
+constexpr int kPlocGroup = 8;              // iterations between count read-backs
+constexpr int kPlocMaxIterations = 1024;
+constexpr int kPlocTile = 256;
+constexpr int kPlocBlock = 1024;
+enum : int { kStCount = 0, kStBase = 2, kStForced = 4, kStTarget = 6, kStWords = 8 };
+
+__device__ __forceinline__ float4 box_min(float4 a, float4 b)
+{
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), a.w);
+}
+__device__ __forceinline__ float4 box_max(float4 a, float4 b)
+{
+    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), a.w);
+}
+
+// Initial clusters = the sorted leaves; segment id from the key's top bits.
+__global__ void k_ploc_init(int32_t n, const uint64_t *__restrict__ keys, int seg_shift, int32_t nseg,
+                            const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *__restrict__ cl,
+                            float4 *__restrict__ ch)
+{
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int32_t seg = (nseg > 1) ? (int32_t)(keys[k] >> seg_shift) : 0;
+        const float4 a = llo[k], b = lhi[k];
+        cl[k] = make_float4(a.x, a.y, a.z, __int_as_float(seg));
+        ch[k] = make_float4(b.x, b.y, b.z, __int_as_float(~k));
+    }
+}
+
+// Segments: empty ones get an empty wide node (every ray misses), the others
+// count towards the number of clusters the iterations end with.
+__global__ void k_ploc_segments(int32_t nseg, int32_t n, const int32_t *__restrict__ seg_first, int32_t *state,
+                                WideNode *__restrict__ nodes)
+{
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) {
+        state[kStCount] = n;
+        state[kStBase] = 0;
+        state[kStForced] = 0;
+    }
+    if (s >= nseg) return;
+    if (seg_first[s + 1] > seg_first[s]) {
+        atomicAdd(&state[kStTarget], 1);
+        return;
+    }
+    WideNode W;
+    memset(&W, 0, sizeof(W));
+    for (int k = 0; k < 8; ++k) { W.qlo_x[k] = W.qlo_y[k] = W.qlo_z[k] = 255; }
+    nodes[s] = W;
+}
+
+__global__ void __launch_bounds__(kPlocTile) k_ploc_nn(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
+                                                      int32_t *__restrict__ nn, const int32_t *__restrict__ state,
+                                                      int it)
+{
+    __shared__ float4 slo[kPlocTile + 2 * kPlocRadius], shi[kPlocTile + 2 * kPlocRadius];
+    const int par = it & 1;
+    const int32_t count = state[kStCount + par];
+    const int32_t b0 = blockIdx.x * kPlocTile;
+    if (b0 >= count) return;
+    const bool done = count <= state[kStTarget];
+    const bool forced = state[kStForced + par] != 0;
+    for (int k = threadIdx.x; k < kPlocTile + 2 * kPlocRadius; k += kPlocTile) {
+        const int32_t g = b0 - kPlocRadius + k;
+        if (g >= 0 && g < count) {
+            slo[k] = cl[g];
+            shi[k] = ch[g];
+        }
+    }
+    __syncthreads();
+    const int32_t i = b0 + threadIdx.x;
+    if (i >= count) return;
+    int32_t best = -1;
+    if (!done) {
+        const int t = threadIdx.x + kPlocRadius;
+        const float4 a0 = slo[t], a1 = shi[t];
+        const int seg = __float_as_int(a0.w);
+        if (forced) {
+            const int32_t p = ((i - par) ^ 1) + par;
+            if (i - par >= 0 && p >= 0 && p < count && __float_as_int(slo[t + (p - i)].w) == seg) best = p;
+        } else {
+            float bd = __int_as_float(0x7f800000);
+#pragma unroll 4
+            for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
+                const int32_t j = i + o;
+                if (o == 0 || j < 0 || j >= count) continue;
+                const float4 b0v = slo[t + o];
+                if (__float_as_int(b0v.w) != seg) continue;
+                const float d = half_area(box_min(a0, b0v), box_max(a1, shi[t + o]));
+                if (d < bd) { bd = d; best = j; }
+            }
+        }
+    }
+    nn[i] = best;
+}
+
+// 0/1 flags of cluster i: survives (not absorbed by a lower partner) and
+// creates a node (lower half of a mutual pair).
+__device__ __forceinline__ void ploc_flags(const int32_t *__restrict__ nn, int32_t i, int32_t count, bool &keep,
+                                           bool &make)
+{
+    keep = false;
+    make = false;
+    if (i >= count) return;
+    const int32_t j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    keep = !(mutual && i > j);
+    make = mutual && i < j;
+}
+
+// Exclusive block prefix of two 0/1 flags (1024 threads); totals in *tk, *tm.
+__device__ __forceinline__ void block_prefix2(bool keep, bool make, int &pk, int &pm, int &tk, int &tm)
+{
+    __shared__ int wk[32], wm[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t bk = __ballot_sync(0xffffffffu, keep), bm = __ballot_sync(0xffffffffu, make);
+    const uint32_t below = (1u << lane) - 1u;
+    if (lane == 0) { wk[warp] = __popc(bk); wm[warp] = __popc(bm); }
+    __syncthreads();
+    if (warp == 0) {
+        int vk = wk[lane], vm = wm[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int uk = __shfl_up_sync(0xffffffffu, vk, o), um = __shfl_up_sync(0xffffffffu, vm, o);
+            if (lane >= o) { vk += uk; vm += um; }
+        }
+        wk[lane] = vk;
+        wm[lane] = vm;
+    }
+    __syncthreads();
+    pk = (warp ? wk[warp - 1] : 0) + __popc(bk & below);
+    pm = (warp ? wm[warp - 1] : 0) + __popc(bm & below);
+    tk = wk[31];
+    tm = wm[31];
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_count(const int32_t *__restrict__ nn,
+                                                          const int32_t *__restrict__ state, int it,
+                                                          int2 *__restrict__ bsum)
+{
+    const int32_t count = state[kStCount + (it & 1)];
+    if ((int32_t)blockIdx.x * kPlocBlock >= count) return;
+    const int32_t i = blockIdx.x * kPlocBlock + threadIdx.x;
+    bool keep, make;
+    ploc_flags(nn, i, count, keep, make);
+    int pk, pm, tk, tm;
+    block_prefix2(keep, make, pk, pm, tk, tm);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = make_int2(tk, tm);
+}
+
+// One block: exclusive scan of the per-block totals, next count / node base
+// / pairing mode.
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_scan(int2 *__restrict__ bsum, int32_t *state, int it)
+{
+    const int par = it & 1;
+    const int32_t count = state[kStCount + par];
+    const int32_t nb = (count + kPlocBlock - 1) / kPlocBlock;
+    const int32_t per = (nb + kPlocBlock - 1) / kPlocBlock;
+    const int32_t lo = threadIdx.x * per, hi = min(lo + per, nb);
+    int sk = 0, sm = 0;
+    for (int32_t b = lo; b < hi; ++b) { sk += bsum[b].x; sm += bsum[b].y; }
+    __shared__ int xk[kPlocBlock], xm[kPlocBlock];
+    xk[threadIdx.x] = sk;
+    xm[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = 1; o < kPlocBlock; o <<= 1) {
+        const int ak = threadIdx.x >= o ? xk[threadIdx.x - o] : 0;
+        const int am = threadIdx.x >= o ? xm[threadIdx.x - o] : 0;
+        __syncthreads();
+        xk[threadIdx.x] += ak;
+        xm[threadIdx.x] += am;
+        __syncthreads();
+    }
+    int rk = xk[threadIdx.x] - sk, rm = xm[threadIdx.x] - sm;
+    for (int32_t b = lo; b < hi; ++b) {
+        const int2 v = bsum[b];
+        bsum[b] = make_int2(rk, rm);
+        rk += v.x;
+        rm += v.y;
+    }
+    if (threadIdx.x == kPlocBlock - 1) {
+        const int total_k = xk[kPlocBlock - 1], total_m = xm[kPlocBlock - 1];
+        state[kStCount + (par ^ 1)] = total_k;
+        state[kStBase + (par ^ 1)] = state[kStBase + par] + total_m;
+        state[kStForced + (par ^ 1)] = (count > state[kStTarget] && total_m * 16 < count) ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
+                                                          float4 *__restrict__ cl2, float4 *__restrict__ ch2,
+                                                          const int32_t *__restrict__ nn,
+                                                          const int2 *__restrict__ boff,
+                                                          const int32_t *__restrict__ state, int it,
+                                                          int32_t *__restrict__ left, int32_t *__restrict__ right,
+                                                          int32_t *__restrict__ ncount, float4 *__restrict__ ilo,
+                                                          float4 *__restrict__ ihi)
+{
+    const int par = it & 1;
+    const int32_t count = state[kStCount + par];
+    if ((int32_t)blockIdx.x * kPlocBlock >= count) return;
+    const int32_t i = blockIdx.x * kPlocBlock + threadIdx.x;
+    bool keep, make;
+    ploc_flags(nn, i, count, keep, make);
+    int pk, pm, tk, tm;
+    block_prefix2(keep, make, pk, pm, tk, tm);
+    if (!keep) return;
+    const int2 bo = boff[blockIdx.x];
+    const int32_t pos = bo.x + pk;
+    float4 a0 = cl[i], a1 = ch[i];
+    if (make) {
+        const int32_t j = nn[i];
+        const float4 b0 = cl[j], b1 = ch[j];
+        const int32_t id = state[kStBase + par] + bo.y + pm;
+        const int32_t l = __float_as_int(a1.w), r = __float_as_int(b1.w);
+        left[id] = l;
+        right[id] = r;
+        ncount[id] = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
+        a0 = box_min(a0, b0);
+        a1 = box_max(a1, b1);
+        ilo[id] = make_float4(a0.x, a0.y, a0.z, 0.f);
+        ihi[id] = make_float4(a1.x, a1.y, a1.z, 0.f);
+        a1.w = __int_as_float(id);
+    }
+    cl2[pos] = a0;
+    ch2[pos] = a1;
+}
+
+// The remaining clusters (one per non-empty segment, in segment order) are
+// the roots: level-0 collapse tasks (binary ref, wide node = segment).
+__global__ void k_ploc_roots(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
+                             const int32_t *__restrict__ state, int it, int2 *__restrict__ tasks,
+                             int32_t *level_count, int32_t *counters)
+{
+    const int32_t count = state[kStCount + (it & 1)];
+    const int32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c == 0) {
+        level_count[0] = count;
+        if (count != state[kStTarget]) atomicExch(&counters[3], 1);
+    }
+    if (c >= count) return;
+    tasks[c] = make_int2(__float_as_int(ch[c].w), __float_as_int(cl[c].w));
+}
+
 // Exponent e (biased as a float exponent) of the power-of-two grid unit for
 // an extent, with room for 252 units plus one unit of padding per side.
 __device__ __forceinline__ int grid_exponent(float extent)
@@ -266,7 +528,8 @@ __device__ __forceinline__ int grid_exponent(float extent)
 
 struct BuildArgs {
     int32_t n;
-    const int32_t *left, *right, *first, *last;
+    const int32_t *left, *right;
+    const int32_t *count;         // leaves under each internal node
     const float4 *ilo, *ihi, *llo, *lhi;
     const int32_t *vals;          // sorted position -> caller's triangle id
     const float *verts;
@@ -289,9 +552,8 @@ __device__ __forceinline__ void ref_box(const BuildArgs &A, int32_t ref, float4 
 }
 __device__ __forceinline__ int32_t ref_count(const BuildArgs &A, int32_t ref)
 {
-    return (ref < 0) ? 1 : (A.last[ref] - A.first[ref] + 1);
+    return (ref < 0) ? 1 : A.count[ref];
 }
-__device__ __forceinline__ int32_t ref_first(const BuildArgs &A, int32_t ref) { return (ref < 0) ? ~ref : A.first[ref]; }
 
 // One thread per wide node of the current level: gather up to 8 children
 // by repeatedly opening the largest-area internal child (those too big for
@@ -421,9 +683,19 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
         } else {
             const int c = cnt[k];
             W.meta[s] = (uint8_t)((((1u << c) - 1u) << 5) | (uint32_t)tri_off);
-            const int32_t f0 = ref_first(A, ch[k]);
-            for (int j = 0; j < c; ++j) {
-                const int32_t id = A.vals[f0 + j];
+            // the (at most kMaxLeafTris) leaves under this child, left first
+            int32_t todo[kMaxLeafTris];
+            int sp = 0, j = 0;
+            todo[sp++] = ch[k];
+            while (sp > 0 && j < c) {
+                const int32_t r = todo[--sp];
+                if (r >= 0) {
+                    if (sp + 2 > kMaxLeafTris) { atomicExch(&A.counters[3], 1); break; }
+                    todo[sp++] = A.right[r];
+                    todo[sp++] = A.left[r];
+                    continue;
+                }
+                const int32_t id = A.vals[~r];
                 const int3 t = A.idx[id];
                 const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
                 const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
@@ -433,6 +705,7 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
                 P.w1 = make_float4(b.y, b.z, cc.x, cc.y);
                 P.w2 = make_float4(cc.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
                 A.tris[tri_base + tri_off + j] = P;
+                ++j;
             }
             tri_off += c;
         }
@@ -465,6 +738,10 @@ size_t build_temp_bytes(int32_t n)
     b += 4 * nn * sizeof(float4);          // llo lhi ilo ihi
     b += nn * sizeof(int32_t);             // refit flags
     b += 2 * nn * sizeof(int2);            // task queues
+    b += nn * sizeof(int32_t);             // leaf counts of internal nodes
+    b += 4 * nn * sizeof(float4);          // PLOC clusters (two buffers of lo, hi)
+    b += nn * sizeof(int32_t);             // PLOC nearest neighbours
+    b += (nn / kPlocBlock + 2) * sizeof(int2) + kStWords * sizeof(int32_t);
     b += 16 * sizeof(int32_t) + 2 * nn * sizeof(int2);   // counters, root tasks
     b += (6 + 1) * (size_t)kMaxSegments * sizeof(int) + 1024;
     b += cub_bytes + 16 * 256;
@@ -504,6 +781,20 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     float4 *ilo = (float4 *)carve(p, nn * sizeof(float4));
     float4 *ihi = (float4 *)carve(p, nn * sizeof(float4));
     int32_t *rflags = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *ncount = (int32_t *)carve(p, nn * sizeof(int32_t));
+    const bool ploc = in.builder == kBuilderPloc;
+    float4 *cl[2] = {nullptr, nullptr}, *chh[2] = {nullptr, nullptr};
+    int32_t *nnb = nullptr, *pstate = nullptr;
+    int2 *bsum = nullptr;
+    if (ploc) {
+        cl[0] = (float4 *)carve(p, nn * sizeof(float4));
+        chh[0] = (float4 *)carve(p, nn * sizeof(float4));
+        cl[1] = (float4 *)carve(p, nn * sizeof(float4));
+        chh[1] = (float4 *)carve(p, nn * sizeof(float4));
+        nnb = (int32_t *)carve(p, nn * sizeof(int32_t));
+        bsum = (int2 *)carve(p, (nn / kPlocBlock + 2) * sizeof(int2));
+        pstate = (int32_t *)carve(p, kStWords * sizeof(int32_t));
+    }
     int2 *tq0 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
     int2 *tq1 = (int2 *)carve(p, (nn + nseg) * sizeof(int2));
     int32_t *counters = (int32_t *)carve(p, 16 * sizeof(int32_t));
@@ -538,23 +829,54 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         k_morton<<<grid_pts, threads, 0, st>>>(blo, bhi, n, in.seg_of_tri, nseg, mbits, cbounds, keys, vals);
         cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
         const int g = (n + threads - 1) / threads;
-        if (n > 1) k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, parent, leaf_parent);
         k_leaf_boxes<<<g, threads, 0, st>>>(vals2, n, blo, bhi, llo, lhi);
-        if (n > 1) {
-            cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
-            k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
+        if (!ploc) {
+            if (n > 1) k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, ncount, parent, leaf_parent);
+            if (n > 1) {
+                cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
+                k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
+            }
         }
     }
     // segment roots -> level-0 tasks (counted in level_count[0]); wide nodes
     // 0..nseg-1 are the roots
     cudaMemsetAsync(level_count, 0, (kMaxDepth + 2) * sizeof(int32_t), st);
-    k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0,
-                                                level_count, counters, in.nodes);
+    if (ploc) {
+        cudaMemsetAsync(pstate, 0, kStWords * sizeof(int32_t), st);
+        k_ploc_segments<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, pstate, in.nodes);
+        if (n > 0)
+            k_ploc_init<<<min((n + threads - 1) / threads, in.sm_count * 8), threads, 0, st>>>(
+                n, keys2, 3 * mbits, nseg, llo, lhi, cl[0], chh[0]);
+        // iterations in groups of kPlocGroup, then one read-back of the count
+        const int tiles = (n + kPlocTile - 1) / kPlocTile;
+        const int blocks = (n + kPlocBlock - 1) / kPlocBlock;
+        int it = 0;
+        bool finished = n <= 0;
+        while (!finished) {
+            for (int k = 0; k < kPlocGroup; ++k, ++it) {
+                const int a = it & 1;
+                k_ploc_nn<<<max(tiles, 1), kPlocTile, 0, st>>>(cl[a], chh[a], nnb, pstate, it);
+                k_ploc_count<<<max(blocks, 1), kPlocBlock, 0, st>>>(nnb, pstate, it, bsum);
+                k_ploc_scan<<<1, kPlocBlock, 0, st>>>(bsum, pstate, it);
+                k_ploc_merge<<<max(blocks, 1), kPlocBlock, 0, st>>>(cl[a], chh[a], cl[a ^ 1], chh[a ^ 1], nnb, bsum,
+                                                                    pstate, it, left, right, ncount, ilo, ihi);
+            }
+            cudaMemcpyAsync(h_cnt, pstate, kStWords * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+            finished = h_cnt[kStCount + (it & 1)] <= h_cnt[kStTarget];
+            if (!finished && it >= kPlocMaxIterations) { R.status = -6; return R; }
+        }
+        k_ploc_roots<<<(nseg + 127) / 128, 128, 0, st>>>(cl[it & 1], chh[it & 1], pstate, it, tq0, level_count,
+                                                        counters);
+    } else {
+        k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0,
+                                                    level_count, counters, in.nodes);
+    }
     const int32_t nroot_nodes = nseg;
     cudaMemcpyAsync(&counters[0], &nroot_nodes, sizeof(int32_t), cudaMemcpyHostToDevice, st);
 
     BuildArgs A;
-    A.n = n; A.left = left; A.right = right; A.first = first; A.last = last;
+    A.n = n; A.left = left; A.right = right; A.count = ncount;
     A.ilo = ilo; A.ihi = ihi; A.llo = llo; A.lhi = lhi; A.vals = vals2;
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;

@@ -5,6 +5,8 @@
 
 namespace rtc {
 
+enum : int32_t { kBuilderLbvh = 0, kBuilderPloc = 1 };
+
 struct BuildInputs {
     int32_t ntris;
     const float *verts;       // device, 3 floats per vertex
@@ -16,6 +18,7 @@ struct BuildInputs {
     int32_t max_nodes;
     int32_t sm_count;
     int32_t *host_scratch;    // pinned host, >= 5 + kMaxDepth ints
+    int32_t builder = kBuilderPloc;   // binary tree: kBuilderLbvh or kBuilderPloc
     // several scenes in one build (a batch): segment of each triangle and
     // the triangle offset of each segment (nseg + 1 entries, host or device).
     // nseg <= 1: a single scene, both may be nullptr.  Segment s's root is
@@ -35,7 +38,8 @@ struct BuildResult {
 // Device scratch needed by build_wide_bvh for n triangles.
 size_t build_temp_bytes(int32_t n);
 
-// Build on stream st; synchronises st once per tree level.
+// Build on stream st; synchronises st once at the end (and, for PLOC,
+// once per kPlocGroup clustering iterations).
 BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes, cudaStream_t st);
 
 }  // namespace rtc

@@ -356,3 +356,52 @@ def test_watertight_intersector(rtlib, oracle):
     assert (b["tri"] >= 0).mean() > 0.5
     sc.close()
     c.close()
+
+
+@pytest.mark.parametrize("which", ["terrain", "instances", "sphere"])
+def test_builders_agree(rtlib, which):
+    """The clustered (PLOC) and Morton radix (LBVH) trees are different trees
+    over the same triangles: closest hits, occlusion and frames must be
+    identical, every triangle must sit in exactly one leaf slot, and the
+    clustered tree must not need more node visits."""
+    from raptor_gb300 import scenes
+    if which == "terrain":
+        scene, frame = scenes.terrain_scene(size_pow2=128, xres=160, yres=90)
+    elif which == "instances":
+        scene, frame = scenes.instances_scene(n_inst=60, xres=160, yres=90)
+    else:
+        scene, frame = scenes.icosphere_scene(freq=8, res=96)
+    rng = np.random.default_rng(9)
+    v = scene["verts"].astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    o = rng.uniform(lo - 0.2 * (hi - lo), hi + 0.2 * (hi - lo), size=(20000, 3)).astype(np.float32)
+    tgt = v[rng.integers(0, v.shape[0], 20000)]
+    d = tgt - o
+    d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+    rays = rtlib.rays_array(o, d, tmax=np.float32(0.5) * np.linalg.norm(tgt - o, axis=1).astype(np.float32))
+    out = {}
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+        c = rtlib.Context(0)
+        c.set_option(rtlib.RT_OPT_BUILDER, b)
+        c.set_option(rtlib.RT_OPT_COUNT_FETCHES, 1)
+        sc = rtlib.Scene(c, scene)
+        st = sc.stats()
+        assert sum(k * n for k, n in zip((1, 2, 3), st["leaf_tris"])) == scene["tris"].shape[0]
+        assert st["internal_slots"] == st["nodes"] - 1
+        r = sc.render(frame, want_ids=True)
+        out[b] = (sc.closest(rays), sc.any(rays), r["rgb"], r["ids"], r["stats"].nodes_fetched)
+        sc.close()
+        c.close()
+    (h0, a0, rgb0, id0, n0), (h1, a1, rgb1, id1, n1) = out[0], out[1]
+    assert np.array_equal(h0["tri"], h1["tri"])
+    assert np.array_equal(h0["t"], h1["t"])
+    assert np.array_equal(a0, a1)
+    assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
+    assert n1 <= n0 * 1.10
+
+
+def test_builder_option_rejects_unknown(rtlib):
+    c = rtlib.Context(0)
+    with pytest.raises(rtlib.RtError):
+        c.set_option(rtlib.RT_OPT_BUILDER, 7)
+    c.close()
