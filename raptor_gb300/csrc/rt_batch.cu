@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256, RT_RENDER_MIN_BLOCKS / 2) k_render_batche
 // Lane-replacement form: every lane carries a pixel of any job and refills
 // from the shared queue (rt_wave.cuh).
 template <int TW>
-__global__ void __launch_bounds__(256, RT_RENDER_MIN_BLOCKS / 2) k_render_batched_wave(const BatchJob *__restrict__ jobs, int32_t njobs,
+__global__ void __launch_bounds__(256, RT_WAVE_MIN_BLOCKS / 2) k_render_batched_wave(const BatchJob *__restrict__ jobs, int32_t njobs,
                                                              int32_t total_items, Counters *ctr)
 {
     extern __shared__ LaneShade wave_state[];

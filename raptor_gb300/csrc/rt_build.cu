@@ -192,11 +192,93 @@ __global__ void k_leaf_boxes(const int32_t *__restrict__ vals, int32_t n, const 
     lhi[k] = bhi[t];
 }
 
+__device__ __forceinline__ float half_area(float4 lo, float4 hi)
+{
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dx * dz + dy * dz;
+}
+
+// ------------------------------------------------- surface-area collapse
+//
+// Cost model of the 8-wide tree (Ylitie, Karras & Laine, HPG 2017, section
+// 3): visiting a wide node costs its surface area times kCostNode, a leaf
+// slot its area times kCostTri per triangle.  For every binary node n and
+// i = 1..8, C(n, i) is the least cost of representing n's subtree with at
+// most i slots of the parent: C(n, 1) = min(leaf, wide node = area * kCostNode
+// + D(n, 8)), C(n, i) = min(C(n, i - 1), D(n, i)), where D(n, j) = min over
+// k of C(left, k) + C(right, j - k).  The tables are built bottom-up with the
+// tree; the collapse then distributes each wide node's 8 slots by them.
+// Decision word of a node: bits 3(i-2)..3(i-2)+2 the left share k of D(n, i)
+// when C(n, i) takes it (0: C(n, i) = C(n, i - 1)), bits 21..23 the left share
+// of D(n, 8), bit 31 set when one slot holds n as a leaf.
+#ifndef RT_COLLAPSE_SAH
+#define RT_COLLAPSE_SAH 1
+#endif
+#ifndef RT_SAH_COST_TRI
+#define RT_SAH_COST_TRI 0.6f
+#endif
+constexpr float kCostNode = 1.0f;
+constexpr float kCostTri = RT_SAH_COST_TRI;
+
+// Cost table of a child ref (a leaf triangle or an internal node).
+__device__ __forceinline__ void sah_child(const float *sah, int32_t ref, float4 lo, float4 hi, float *c)
+{
+    if (ref < 0) {
+        const float v = half_area(lo, hi) * kCostTri;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) c[i] = v;
+        return;
+    }
+    const float4 *p = reinterpret_cast<const float4 *>(sah + 8 * (size_t)ref);
+    const float4 x = __ldcg(p), y = __ldcg(p + 1);
+    c[0] = x.x; c[1] = x.y; c[2] = x.z; c[3] = x.w;
+    c[4] = y.x; c[5] = y.y; c[6] = y.z; c[7] = y.w;
+}
+
+// Table and decision word of internal node id from its children's tables.
+__device__ __forceinline__ void sah_node(float *sah, uint32_t *dec, int32_t id, float area, int32_t count,
+                                         const float *cl, const float *cr)
+{
+    float dist[9];
+    uint32_t split[9];
+#pragma unroll
+    for (int j = 2; j <= 8; ++j) {
+        float best = __int_as_float(0x7f800000);
+        uint32_t bk = 1;
+#pragma unroll
+        for (int k = 1; k < j; ++k) {
+            const float v = cl[k - 1] + cr[j - k - 1];
+            if (v < best) { best = v; bk = (uint32_t)k; }
+        }
+        dist[j] = best;
+        split[j] = bk;
+    }
+    const float cint = dist[8] + area * kCostNode;
+    const float cleaf = count <= kMaxLeafTris ? area * kCostTri * (float)count : __int_as_float(0x7f800000);
+    float c[8];
+    uint32_t d = split[8] << 21;
+    c[0] = fminf(cleaf, cint);
+    if (cleaf <= cint) d |= 1u << 31;
+#pragma unroll
+    for (int i = 2; i <= 8; ++i) {
+        if (dist[i] < c[i - 2]) {
+            c[i - 1] = dist[i];
+            d |= split[i] << (3 * (i - 2));
+        } else {
+            c[i - 1] = c[i - 2];
+        }
+    }
+    float4 *p = reinterpret_cast<float4 *>(sah + 8 * (size_t)id);
+    __stcg(p, make_float4(c[0], c[1], c[2], c[3]));
+    __stcg(p + 1, make_float4(c[4], c[5], c[6], c[7]));
+    __stcg(dec + id, d);
+}
+
 // Bottom-up box refit: the second child to arrive at a node unions both.
 __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
                         const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
                         const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
-                        int32_t *flags)
+                        int32_t *flags, const int32_t *__restrict__ count, float *sah, uint32_t *dec)
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -211,8 +293,16 @@ __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32
         const float4 a1 = (l < 0) ? lhi[~l] : __ldcg(&ihi[l]);
         const float4 b0 = (r < 0) ? llo[~r] : __ldcg(&ilo[r]);
         const float4 b1 = (r < 0) ? lhi[~r] : __ldcg(&ihi[r]);
-        __stcg(&ilo[p], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.f));
-        __stcg(&ihi[p], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f));
+        const float4 plo = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.f);
+        const float4 phi = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f);
+        __stcg(&ilo[p], plo);
+        __stcg(&ihi[p], phi);
+        if (sah) {
+            float cl[8], cr[8];
+            sah_child(sah, l, a0, a1, cl);
+            sah_child(sah, r, b0, b1, cr);
+            sah_node(sah, dec, p, half_area(plo, phi), count[p], cl, cr);
+        }
         p = parent[p];
     }
 }
@@ -250,11 +340,6 @@ __global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg
     (void)n;
 }
 
-__device__ __forceinline__ float half_area(float4 lo, float4 hi)
-{
-    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-    return dx * dy + dx * dz + dy * dz;
-}
 
 // ------------------------------------------------------------------ PLOC
 //
@@ -465,7 +550,7 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restr
                                                           const int32_t *__restrict__ state, int it,
                                                           int32_t *__restrict__ left, int32_t *__restrict__ right,
                                                           int32_t *__restrict__ ncount, float4 *__restrict__ ilo,
-                                                          float4 *__restrict__ ihi)
+                                                          float4 *__restrict__ ihi, float *sah, uint32_t *dec)
 {
     const int par = it & 1;
     const int32_t count = state[kStCount + par];
@@ -486,9 +571,16 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restr
         const int32_t l = __float_as_int(a1.w), r = __float_as_int(b1.w);
         left[id] = l;
         right[id] = r;
-        ncount[id] = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
+        const int32_t cnt = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
+        ncount[id] = cnt;
+        float cl[8], cr[8];
+        if (sah) {
+            sah_child(sah, l, a0, a1, cl);
+            sah_child(sah, r, b0, b1, cr);
+        }
         a0 = box_min(a0, b0);
         a1 = box_max(a1, b1);
+        if (sah) sah_node(sah, dec, id, half_area(a0, a1), cnt, cl, cr);
         ilo[id] = make_float4(a0.x, a0.y, a0.z, 0.f);
         ihi[id] = make_float4(a1.x, a1.y, a1.z, 0.f);
         a1.w = __int_as_float(id);
@@ -530,6 +622,7 @@ struct BuildArgs {
     int32_t n;
     const int32_t *left, *right;
     const int32_t *count;         // leaves under each internal node
+    const uint32_t *dec;          // surface-area decisions (nullptr: greedy collapse)
     const float4 *ilo, *ihi, *llo, *lhi;
     const int32_t *vals;          // sorted position -> caller's triangle id
     const float *verts;
@@ -555,9 +648,43 @@ __device__ __forceinline__ int32_t ref_count(const BuildArgs &A, int32_t ref)
     return (ref < 0) ? 1 : A.count[ref];
 }
 
+// The children of wide node `node` by the surface-area decisions: its 8
+// slots split between the binary children, recursively, until a subtree
+// gets one slot (a leaf slot or a wide child node).
+__device__ __forceinline__ int sah_children(const BuildArgs &A, int32_t node, int32_t *ch, bool *leaf)
+{
+    int32_t st_ref[8];
+    int st_n[8];
+    int sp = 0, m = 0;
+    const uint32_t d = A.dec[node];
+    const int k8 = (int)((d >> 21) & 7u);
+    st_ref[sp] = A.right[node]; st_n[sp++] = 8 - k8;
+    st_ref[sp] = A.left[node]; st_n[sp++] = k8;
+    while (sp > 0 && m < 8) {
+        --sp;
+        const int32_t r = st_ref[sp];
+        int i = st_n[sp];
+        if (r < 0) { ch[m] = r; leaf[m] = true; ++m; continue; }
+        const uint32_t dr = A.dec[r];
+        while (i >= 2 && ((dr >> (3 * (i - 2))) & 7u) == 0u) --i;
+        if (i <= 1) {
+            ch[m] = r;
+            leaf[m] = (dr >> 31) != 0u;
+            ++m;
+            continue;
+        }
+        const int k = (int)((dr >> (3 * (i - 2))) & 7u);
+        if (sp + 2 > 8) { ch[m] = r; leaf[m] = false; ++m; continue; }   // cannot happen: slots sum to 8
+        st_ref[sp] = A.right[r]; st_n[sp++] = i - k;
+        st_ref[sp] = A.left[r]; st_n[sp++] = k;
+    }
+    return m;
+}
+
 // One thread per wide node of the current level: gather up to 8 children
-// by repeatedly opening the largest-area internal child (those too big for
-// a leaf first), assign slots by octant, quantise, emit leaves and tasks.
+// (by the surface-area decisions, or greedily by repeatedly opening the
+// largest-area internal child, those too big for a leaf first), assign slots
+// by octant, quantise, emit leaves and tasks.
 __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 task)
 {
     const int32_t wide = task.y;
@@ -566,9 +693,12 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
     float4 clo[8], chi[8];
     float area[8];
     int32_t cnt[8];
+    bool leaf[8];
     int m = 0;
     if (task.x < 0) {
         ch[0] = task.x; m = 1;
+    } else if (A.dec) {
+        m = sah_children(A, task.x, ch, leaf);
     } else {
         ch[0] = A.left[task.x]; ch[1] = A.right[task.x]; m = 2;
     }
@@ -577,7 +707,7 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
         area[k] = half_area(clo[k], chi[k]);
         cnt[k] = ref_count(A, ch[k]);
     }
-    while (m < 8) {
+    while (!A.dec && m < 8) {
         int best = -1;
         float best_a = -1.f;
         for (int pass = 0; pass < 2 && best < 0; ++pass) {
@@ -599,6 +729,11 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
         cnt[m] = ref_count(A, ch[m]);
         ++m;
     }
+
+    if (!A.dec || task.x < 0)
+        for (int k = 0; k < m; ++k) leaf[k] = cnt[k] <= kMaxLeafTris;
+    for (int k = 0; k < m; ++k)
+        if (leaf[k] && cnt[k] > kMaxLeafTris) { atomicExch(&A.counters[3], 1); return; }
 
     // node box and centroid
     float4 nlo = clo[0], nhi = chi[0];
@@ -635,7 +770,7 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
     // allocate children nodes and triangle slots
     int n_int = 0, n_tri = 0;
     for (int k = 0; k < m; ++k) {
-        if (cnt[k] > kMaxLeafTris) ++n_int; else n_tri += cnt[k];
+        if (!leaf[k]) ++n_int; else n_tri += cnt[k];
     }
     const int32_t child_base = n_int ? atomicAdd(&A.counters[0], n_int) : 0;
     const int32_t tri_base = n_tri ? atomicAdd(&A.counters[1], n_tri) : 0;
@@ -674,7 +809,7 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
         };
         W.qlo_x[s] = qlo(clo[k].x, px, ix); W.qlo_y[s] = qlo(clo[k].y, py, iy); W.qlo_z[s] = qlo(clo[k].z, pz, iz);
         W.qhi_x[s] = qhi(chi[k].x, px, ix); W.qhi_y[s] = qhi(chi[k].y, py, iy); W.qhi_z[s] = qhi(chi[k].z, pz, iz);
-        if (cnt[k] > kMaxLeafTris) {
+        if (!leaf[k]) {
             W.imask |= (uint8_t)(1u << s);
             W.meta[s] = (uint8_t)(0x20 | (24 + s));
             const int slot = atomicAdd(A.next_count, 1);
@@ -739,6 +874,7 @@ size_t build_temp_bytes(int32_t n)
     b += nn * sizeof(int32_t);             // refit flags
     b += 2 * nn * sizeof(int2);            // task queues
     b += nn * sizeof(int32_t);             // leaf counts of internal nodes
+    b += 9 * nn * sizeof(float);           // surface-area cost tables + decisions
     b += 4 * nn * sizeof(float4);          // PLOC clusters (two buffers of lo, hi)
     b += nn * sizeof(int32_t);             // PLOC nearest neighbours
     b += (nn / kPlocBlock + 2) * sizeof(int2) + kStWords * sizeof(int32_t);
@@ -782,6 +918,8 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     float4 *ihi = (float4 *)carve(p, nn * sizeof(float4));
     int32_t *rflags = (int32_t *)carve(p, nn * sizeof(int32_t));
     int32_t *ncount = (int32_t *)carve(p, nn * sizeof(int32_t));
+    float *sah = RT_COLLAPSE_SAH ? (float *)carve(p, 8 * nn * sizeof(float)) : nullptr;
+    uint32_t *dec = RT_COLLAPSE_SAH ? (uint32_t *)carve(p, nn * sizeof(uint32_t)) : nullptr;
     const bool ploc = in.builder == kBuilderPloc;
     float4 *cl[2] = {nullptr, nullptr}, *chh[2] = {nullptr, nullptr};
     int32_t *nnb = nullptr, *pstate = nullptr;
@@ -834,7 +972,8 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             if (n > 1) k_karras<<<g, threads, 0, st>>>(keys2, n, left, right, first, last, ncount, parent, leaf_parent);
             if (n > 1) {
                 cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
-                k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags);
+                k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags,
+                                               ncount, sah, dec);
             }
         }
     }
@@ -859,7 +998,8 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
                 k_ploc_count<<<max(blocks, 1), kPlocBlock, 0, st>>>(nnb, pstate, it, bsum);
                 k_ploc_scan<<<1, kPlocBlock, 0, st>>>(bsum, pstate, it);
                 k_ploc_merge<<<max(blocks, 1), kPlocBlock, 0, st>>>(cl[a], chh[a], cl[a ^ 1], chh[a ^ 1], nnb, bsum,
-                                                                    pstate, it, left, right, ncount, ilo, ihi);
+                                                                    pstate, it, left, right, ncount, ilo, ihi,
+                                                                    sah, dec);
             }
             cudaMemcpyAsync(h_cnt, pstate, kStWords * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
@@ -876,7 +1016,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     cudaMemcpyAsync(&counters[0], &nroot_nodes, sizeof(int32_t), cudaMemcpyHostToDevice, st);
 
     BuildArgs A;
-    A.n = n; A.left = left; A.right = right; A.count = ncount;
+    A.n = n; A.left = left; A.right = right; A.count = ncount; A.dec = dec;
     A.ilo = ilo; A.ihi = ihi; A.llo = llo; A.lhi = lhi; A.vals = vals2;
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;

@@ -10,6 +10,9 @@ constexpr int kTraceThreads = 128;   // 4 warps per block
 // (caps registers per thread: 1 -> 255, 6 -> 80, 8 -> 64; 8 measured fastest:
 // more resident warps hide the latency of the node loads better than the
 // registers the cap spills).
+#ifndef RT_WAVE_MIN_BLOCKS
+#define RT_WAVE_MIN_BLOCKS RT_RENDER_MIN_BLOCKS   // lane-replacement kernels
+#endif
 #ifndef RT_RENDER_MIN_BLOCKS
 #define RT_RENDER_MIN_BLOCKS 8
 #endif

@@ -8,7 +8,7 @@ namespace rtc {
 namespace {
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_wave(const __grid_constant__ FrameJob job, Counters *ctr)
+__global__ void __launch_bounds__(kTraceThreads, RT_WAVE_MIN_BLOCKS) k_render_wave(const __grid_constant__ FrameJob job, Counters *ctr)
 {
     __shared__ LaneShade shade_state[kTraceThreads];
     wave_loop<8, COUNT>(&job, nullptr, 1, job.items_end, shade_state[threadIdx.x], ctr);
