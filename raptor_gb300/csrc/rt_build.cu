@@ -356,12 +356,13 @@ __global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg
 // state: [0,1] cluster count, [2,3] next internal node id, [4,5] forced
 // pairing (ping-pong by iteration parity), [6] clusters to end with (one per
 // non-empty segment).
+constexpr int kCollapseGroup = 12;         // collapse levels between read-backs
 constexpr int kPlocRadius = 24;
 constexpr int kPlocGroup = 8;              // iterations between count read-backs
 constexpr int kPlocMaxIterations = 1024;
 constexpr int kPlocTile = 256;
 constexpr int kPlocBlock = 1024;
-enum : int { kStCount = 0, kStBase = 2, kStForced = 4, kStTarget = 6, kStWords = 8 };
+enum : int { kStCount = 0, kStBase = 2, kStForced = 4, kStTarget = 6, kStError = 7, kStWords = 8 };
 
 __device__ __forceinline__ float4 box_min(float4 a, float4 b)
 {
@@ -587,6 +588,165 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restr
     }
     cl2[pos] = a0;
     ch2[pos] = a1;
+}
+
+// The last iterations, once at most kPlocTailMax clusters remain: one
+// block holds every cluster in shared memory and runs the same iteration
+// (nearest neighbour, mutual pairs, stable compaction, forced pairing after
+// a slow iteration) with block barriers instead of kernel boundaries.  The
+// final clusters go back to (cl, ch) and the count to the state slot of
+// iteration `it`'s parity.
+constexpr int kPlocTailMax = 4096;
+constexpr int kPlocTailItems = kPlocTailMax / kPlocBlock;
+constexpr int kPlocTailMaxIterations = 4096;
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ cl, float4 *__restrict__ ch,
+                                                         int32_t *state, int it, int32_t *__restrict__ left,
+                                                         int32_t *__restrict__ right, int32_t *__restrict__ ncount,
+                                                         float4 *__restrict__ ilo, float4 *__restrict__ ihi,
+                                                         float *sah, uint32_t *dec)
+{
+    extern __shared__ float4 tail_smem[];
+    float4 *slo = tail_smem;                       // kPlocTailMax
+    float4 *shi = tail_smem + kPlocTailMax;        // kPlocTailMax
+    int32_t *snn = reinterpret_cast<int32_t *>(tail_smem + 2 * kPlocTailMax);   // kPlocTailMax
+    __shared__ int wsum[2][32];
+    __shared__ int s_count, s_base, s_forced, s_error;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int par = it & 1;
+    const int32_t target = state[kStTarget];
+    if (tid == 0) {
+        s_count = state[kStCount + par];
+        s_base = state[kStBase + par];
+        s_forced = state[kStForced + par];
+        s_error = 0;
+    }
+    __syncthreads();
+    const int32_t count0 = s_count;
+    for (int k = 0; k < kPlocTailItems; ++k) {
+        const int i = tid + k * kPlocBlock;
+        if (i < count0) { slo[i] = cl[i]; shi[i] = ch[i]; }
+    }
+    __syncthreads();
+    for (int step = 0; step < kPlocTailMaxIterations; ++step) {
+        const int32_t count = s_count;
+        if (count <= target) break;
+        const bool forced = s_forced != 0;
+        const int ppar = step & 1;
+        // nearest neighbours
+        for (int k = 0; k < kPlocTailItems; ++k) {
+            const int i = tid + k * kPlocBlock;
+            if (i >= count) break;
+            const float4 a0 = slo[i], a1 = shi[i];
+            const int seg = __float_as_int(a0.w);
+            int best = -1;
+            if (forced) {
+                const int p = ((i - ppar) ^ 1) + ppar;
+                if (i - ppar >= 0 && p >= 0 && p < count && __float_as_int(slo[p].w) == seg) best = p;
+            } else {
+                float bd = __int_as_float(0x7f800000);
+                const int j0 = max(0, i - kPlocRadius), j1 = min(count - 1, i + kPlocRadius);
+                for (int j = j0; j <= j1; ++j) {
+                    if (j == i) continue;
+                    const float4 b0 = slo[j];
+                    if (__float_as_int(b0.w) != seg) continue;
+                    const float d = half_area(box_min(a0, b0), box_max(a1, shi[j]));
+                    if (d < bd) { bd = d; best = j; }
+                }
+            }
+            snn[i] = best;
+        }
+        __syncthreads();
+        // flags, per-thread totals, block scan
+        bool keep[kPlocTailItems], make[kPlocTailItems];
+        int tk = 0, tm = 0;
+        for (int k = 0; k < kPlocTailItems; ++k) {
+            const int i = tid * kPlocTailItems + k;   // contiguous items per thread keep the order
+            keep[k] = make[k] = false;
+            if (i < count) {
+                const int j = snn[i];
+                const bool mutual = j >= 0 && snn[j] == i;
+                keep[k] = !(mutual && i > j);
+                make[k] = mutual && i < j;
+            }
+            tk += keep[k];
+            tm += make[k];
+        }
+        int ik = tk, im = tm;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int uk = __shfl_up_sync(0xffffffffu, ik, o), um = __shfl_up_sync(0xffffffffu, im, o);
+            if (lane >= o) { ik += uk; im += um; }
+        }
+        if (lane == 31) { wsum[0][warp] = ik; wsum[1][warp] = im; }
+        __syncthreads();
+        if (warp == 0) {
+            int vk = wsum[0][lane], vm = wsum[1][lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int uk = __shfl_up_sync(0xffffffffu, vk, o), um = __shfl_up_sync(0xffffffffu, vm, o);
+                if (lane >= o) { vk += uk; vm += um; }
+            }
+            wsum[0][lane] = vk;
+            wsum[1][lane] = vm;
+        }
+        __syncthreads();
+        int pk = (warp ? wsum[0][warp - 1] : 0) + ik - tk;
+        int pm = (warp ? wsum[1][warp - 1] : 0) + im - tm;
+        const int total_k = wsum[0][31], total_m = wsum[1][31];
+        // read every surviving cluster (and its partner) before any write
+        float4 v0[kPlocTailItems], v1[kPlocTailItems];
+        int vpos[kPlocTailItems];
+        for (int k = 0; k < kPlocTailItems; ++k) {
+            const int i = tid * kPlocTailItems + k;
+            vpos[k] = -1;
+            if (!keep[k]) continue;
+            float4 a0 = slo[i], a1 = shi[i];
+            if (make[k]) {
+                const int j = snn[i];
+                const float4 b0 = slo[j], b1 = shi[j];
+                const int32_t id = s_base + pm;
+                ++pm;
+                const int32_t l = __float_as_int(a1.w), r = __float_as_int(b1.w);
+                left[id] = l;
+                right[id] = r;
+                const int32_t cnt = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
+                ncount[id] = cnt;
+                float cla[8], cra[8];
+                if (sah) {
+                    sah_child(sah, l, a0, a1, cla);
+                    sah_child(sah, r, b0, b1, cra);
+                }
+                a0 = box_min(a0, b0);
+                a1 = box_max(a1, b1);
+                if (sah) sah_node(sah, dec, id, half_area(a0, a1), cnt, cla, cra);
+                ilo[id] = make_float4(a0.x, a0.y, a0.z, 0.f);
+                ihi[id] = make_float4(a1.x, a1.y, a1.z, 0.f);
+                a1.w = __int_as_float(id);
+            }
+            v0[k] = a0;
+            v1[k] = a1;
+            vpos[k] = pk++;
+        }
+        __syncthreads();
+        for (int k = 0; k < kPlocTailItems; ++k)
+            if (vpos[k] >= 0) { slo[vpos[k]] = v0[k]; shi[vpos[k]] = v1[k]; }
+        if (tid == 0) {
+            s_count = total_k;
+            s_base += total_m;
+            s_forced = (total_m * 16 < count) ? 1 : 0;
+            if (step == kPlocTailMaxIterations - 1 && total_k > target) s_error = 1;
+        }
+        __syncthreads();
+    }
+    const int32_t count = s_count;
+    for (int k = 0; k < kPlocTailItems; ++k) {
+        const int i = tid + k * kPlocBlock;
+        if (i < count) { cl[i] = slo[i]; ch[i] = shi[i]; }
+    }
+    if (tid == 0) {
+        state[kStCount + par] = count;
+        state[kStBase + par] = s_base;
+        if (s_error) state[kStError] = 1;
+    }
 }
 
 // The remaining clusters (one per non-empty segment, in segment order) are
@@ -991,7 +1151,11 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         const int blocks = (n + kPlocBlock - 1) / kPlocBlock;
         int it = 0;
         bool finished = n <= 0;
-        while (!finished) {
+        const size_t tail_smem = 2 * kPlocTailMax * sizeof(float4) + kPlocTailMax * sizeof(int32_t);
+        if (cudaFuncSetAttribute(k_ploc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem) !=
+            cudaSuccess) { R.status = -2; return R; }
+        bool tail = !finished && n <= kPlocTailMax;
+        while (!finished && !tail) {
             for (int k = 0; k < kPlocGroup; ++k, ++it) {
                 const int a = it & 1;
                 k_ploc_nn<<<max(tiles, 1), kPlocTile, 0, st>>>(cl[a], chh[a], nnb, pstate, it);
@@ -1004,8 +1168,12 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             cudaMemcpyAsync(h_cnt, pstate, kStWords * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
             finished = h_cnt[kStCount + (it & 1)] <= h_cnt[kStTarget];
-            if (!finished && it >= kPlocMaxIterations) { R.status = -6; return R; }
+            tail = !finished && h_cnt[kStCount + (it & 1)] <= kPlocTailMax;
+            if (!finished && !tail && it >= kPlocMaxIterations) { R.status = -6; return R; }
         }
+        if (tail)
+            k_ploc_tail<<<1, kPlocBlock, tail_smem, st>>>(cl[it & 1], chh[it & 1], pstate, it, left, right, ncount,
+                                                          ilo, ihi, sah, dec);
         k_ploc_roots<<<(nseg + 127) / 128, 128, 0, st>>>(cl[it & 1], chh[it & 1], pstate, it, tq0, level_count,
                                                         counters);
     } else {
@@ -1021,18 +1189,25 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
     A.max_nodes = in.max_nodes;
-    // all levels back to back; a level past the last one finds no tasks
+    // levels back to back in groups of kCollapseGroup (a level past the last
+    // one finds no tasks), one read-back per group: most trees end within
+    // the first group
     const int cgrid = max(1, min((n + nseg + 63) / 64, in.sm_count * 16));
-    for (int level = 0; level < kMaxDepth; ++level) {
-        A.tasks_in = (level & 1) ? tq1 : tq0;
-        A.tasks_out = (level & 1) ? tq0 : tq1;
-        A.cur_count = level_count + level;
-        A.next_count = level_count + level + 1;
-        k_collapse_level<<<cgrid, 64, 0, st>>>(A);
+    int level = 0;
+    for (;;) {
+        const int stop = min(level + kCollapseGroup, kMaxDepth);
+        for (; level < stop; ++level) {
+            A.tasks_in = (level & 1) ? tq1 : tq0;
+            A.tasks_out = (level & 1) ? tq0 : tq1;
+            A.cur_count = level_count + level;
+            A.next_count = level_count + level + 1;
+            k_collapse_level<<<cgrid, 64, 0, st>>>(A);
+        }
+        cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(h_cnt + 4, level_count, (kMaxDepth + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+        if (level >= kMaxDepth || h_cnt[4 + level] == 0 || h_cnt[3]) break;
     }
-    cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(h_cnt + 4, level_count, (kMaxDepth + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
     if (h_cnt[3]) { R.status = -8; return R; }
     if (h_cnt[4 + kMaxDepth] != 0) { R.status = -5; return R; }   // deeper than kMaxDepth levels
     int depth = 0;

@@ -405,3 +405,38 @@ def test_builder_option_rejects_unknown(rtlib):
     with pytest.raises(rtlib.RtError):
         c.set_option(rtlib.RT_OPT_BUILDER, 7)
     c.close()
+
+
+def test_builders_on_degenerate_input(rtlib):
+    """Thousands of identical triangles (every merge distance ties) and a
+    scene in two far-apart clusters: both builders must finish and agree,
+    with ties broken towards the lowest triangle id."""
+    from raptor_gb300 import scenes
+    v, t = scenes.geodesic_sphere(6)
+    tri = np.array([[0.0, 0.0, 2.0], [1.0, 0.0, 2.0], [0.0, 1.0, 2.0]], np.float32)
+    copies = 6000
+    dv = np.tile(tri, (copies, 1))
+    dt = np.arange(3 * copies, dtype=np.int32).reshape(copies, 3)
+    far = v * 0.5 + np.array([500.0, 0.0, 0.0])
+    verts = np.concatenate([dv, v, far]).astype(np.float32)
+    tris = np.concatenate([dt, t + dv.shape[0], t + dv.shape[0] + v.shape[0]]).astype(np.int32)
+    scene = {"verts": verts, "tris": tris}
+    rng = np.random.default_rng(3)
+    o = np.tile(np.array([0.2, 0.2, 6.0], np.float32), (4000, 1))
+    d = rng.normal(size=(4000, 3)) * 0.15 + np.array([0.0, 0.0, -1.0])
+    d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+    rays = rtlib.rays_array(o, d)
+    res = []
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+        c = rtlib.Context(0)
+        c.set_option(rtlib.RT_OPT_BUILDER, b)
+        sc = rtlib.Scene(c, scene)
+        st = sc.stats()
+        assert sum(k * n for k, n in zip((1, 2, 3), st["leaf_tris"])) == tris.shape[0]
+        res.append(sc.closest(rays))
+        sc.close()
+        c.close()
+    assert np.array_equal(res[0]["tri"], res[1]["tri"]) and np.array_equal(res[0]["t"], res[1]["t"])
+    hit_copy = (res[1]["tri"] >= 0) & (res[1]["tri"] < copies)
+    assert hit_copy.sum() > 100
+    assert (res[1]["tri"][hit_copy] == 0).all()     # equal t: the lowest id wins
