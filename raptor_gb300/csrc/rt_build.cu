@@ -1008,6 +1008,239 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
     A.nodes[wide] = W;
 }
 
+// The quantised box bytes of a child in the node's frame.
+__device__ __forceinline__ uint32_t quant_lo(float c, float p, float inv)
+{
+    const float q = floorf(__fmul_rd(__fsub_rd(c, p), inv)) - 1.0f;
+    return (uint32_t)fminf(fmaxf(q, 0.f), 255.f);
+}
+__device__ __forceinline__ uint32_t quant_hi(float c, float p, float inv)
+{
+    const float q = ceilf(__fmul_ru(__fsub_ru(c, p), inv)) + 1.0f;
+    return (uint32_t)fminf(fmaxf(q, 0.f), 255.f);
+}
+
+// Word h (0: slots 0-3, 1: slots 4-7) of a per-slot byte plane: every lane
+// that holds a child in that half contributes its byte; empty slots read
+// `empty`.
+__device__ __forceinline__ uint32_t plane_word(bool mine, int slot, uint32_t byte, int h, uint32_t empty)
+{
+    const bool in = mine && (slot >> 2) == h;
+    const uint32_t sh = 8u * (uint32_t)(slot & 3);
+    const uint32_t occ = __reduce_or_sync(0xffffffffu, in ? (0xffu << sh) : 0u);
+    const uint32_t val = __reduce_or_sync(0xffffffffu, in ? (byte << sh) : 0u);
+    return (empty & ~occ) | val;
+}
+
+// One wide node per warp (surface-area decisions): lane k holds child k.
+// The 8 slots are split between binary children in rounds (a lane that
+// splits keeps the left share and hands the right one to a new lane), then
+// lanes load their boxes, the node box is a warp reduction, slots go to
+// children by repeated warp arg-min of the octant cost, and the node's 20
+// words are assembled with warp OR reductions.  Same node as collapse_task
+// up to the order of equal-cost choices.
+__device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int2 task, int lane)
+{
+    const uint32_t full = 0xffffffffu;
+    int32_t ref = 0;
+    int slots = 0;
+    bool active = false, done = false, lf = false;
+    if (task.x < 0) {
+        if (lane == 0) { ref = task.x; active = done = lf = true; }
+    } else {
+        const uint32_t d = A.dec[task.x];
+        const int k8 = (int)((d >> 21) & 7u);
+        if (lane == 0) { ref = A.left[task.x]; slots = k8; active = true; }
+        if (lane == 1) { ref = A.right[task.x]; slots = 8 - k8; active = true; }
+        for (int round = 0; round < 8; ++round) {
+            bool split = false;
+            int32_t rr = 0;
+            int rs = 0;
+            if (active && !done) {
+                if (ref < 0) {
+                    done = lf = true;
+                } else {
+                    const uint32_t dr = A.dec[ref];
+                    int i = slots;
+                    while (i >= 2 && ((dr >> (3 * (i - 2))) & 7u) == 0u) --i;
+                    if (i <= 1) {
+                        done = true;
+                        lf = (dr >> 31) != 0u;
+                    } else {
+                        const int kl = (int)((dr >> (3 * (i - 2))) & 7u);
+                        split = true;
+                        rr = A.right[ref];
+                        rs = i - kl;
+                        ref = A.left[ref];
+                        slots = kl;
+                    }
+                }
+            }
+            const uint32_t sb = __ballot_sync(full, split);
+            if (!sb) break;
+            const int nact = __popc(__ballot_sync(full, active));
+            if (nact + __popc(sb) > 8) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }   // slots sum to 8
+            // receiving lane nact + r takes the right share of the r-th splitter
+            const int r = lane - nact;
+            const int src = (r >= 0 && r < __popc(sb)) ? (int)__fns(sb, 0, r + 1) : lane;
+            const int32_t got_ref = __shfl_sync(full, rr, src);
+            const int got_slots = __shfl_sync(full, rs, src);
+            if (r >= 0 && r < __popc(sb)) {
+                ref = got_ref;
+                slots = got_slots;
+                active = true;
+                done = lf = false;
+            }
+        }
+    }
+    const uint32_t amask = __ballot_sync(full, active);
+    const int m = __popc(amask);
+    if (__ballot_sync(full, active && !done)) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }
+
+    float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+    int32_t cnt = 0;
+    if (active) {
+        ref_box(A, ref, lo, hi);
+        cnt = ref_count(A, ref);
+        if (lf && cnt > kMaxLeafTris) lf = false;   // cannot happen: the tables allow <= 3
+    }
+    // node box
+    const float nlox = of_ord(__reduce_min_sync(full, ord_of(lo.x)));
+    const float nloy = of_ord(__reduce_min_sync(full, ord_of(lo.y)));
+    const float nloz = of_ord(__reduce_min_sync(full, ord_of(lo.z)));
+    const float nhix = of_ord(__reduce_max_sync(full, ord_of(hi.x)));
+    const float nhiy = of_ord(__reduce_max_sync(full, ord_of(hi.y)));
+    const float nhiz = of_ord(__reduce_max_sync(full, ord_of(hi.z)));
+    const float pcx = 0.5f * (nlox + nhix), pcy = 0.5f * (nloy + nhiy), pcz = 0.5f * (nloz + nhiz);
+
+    // slots: slot s holds the child met first by rays of octant s
+    const float ox = 0.5f * (lo.x + hi.x) - pcx, oy = 0.5f * (lo.y + hi.y) - pcy, oz = 0.5f * (lo.z + hi.z) - pcz;
+    int myslot = -1;
+    uint32_t taken = 0;
+    for (int it = 0; it < m; ++it) {
+        const bool open = active && myslot < 0;
+        float bc = FLT_MAX;
+        int bs = 0;
+        if (open) {
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                if ((taken >> s) & 1u) continue;
+                const float c = ((s & 1) ? -ox : ox) + ((s & 2) ? -oy : oy) + ((s & 4) ? -oz : oz);
+                if (c < bc) { bc = c; bs = s; }
+            }
+        }
+        const int o = open ? ord_of(bc) : 0x7fffffff;
+        const int mn = __reduce_min_sync(full, o);
+        const uint32_t cand = __ballot_sync(full, open && o == mn);
+        const int winner = __ffs(cand) - 1;
+        const int ws = __shfl_sync(full, bs, winner);
+        if (lane == winner) myslot = ws;
+        taken |= 1u << ws;
+    }
+
+    // allocation: internal children contiguous in slot order, leaf triangles
+    // in slot order
+    const bool internal = active && !lf;
+    const uint32_t imask = __reduce_or_sync(full, internal ? (1u << myslot) : 0u);
+    const int n_int = __popc(imask);
+    const uint32_t cnt_lo = __reduce_or_sync(full, (active && lf && myslot < 4) ? ((uint32_t)cnt << (8 * myslot)) : 0u);
+    const uint32_t cnt_hi = __reduce_or_sync(full, (active && lf && myslot >= 4) ? ((uint32_t)cnt << (8 * (myslot - 4))) : 0u);
+    int n_tri = 0, tri_off = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int c = (int)(((s < 4 ? cnt_lo : cnt_hi) >> (8 * (s & 3))) & 0xffu);
+        if (s < myslot) tri_off += c;
+        n_tri += c;
+    }
+    int32_t child_base = 0, tri_base = 0, next = 0;
+    if (lane == 0) {
+        if (n_int) child_base = atomicAdd(&A.counters[0], n_int);
+        if (n_tri) tri_base = atomicAdd(&A.counters[1], n_tri);
+        if (n_int) next = atomicAdd(A.next_count, n_int);
+    }
+    child_base = __shfl_sync(full, child_base, 0);
+    tri_base = __shfl_sync(full, tri_base, 0);
+    next = __shfl_sync(full, next, 0);
+    if (child_base + n_int > A.max_nodes || tri_base + n_tri > A.n) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }
+
+    // quantisation frame
+    const int ex = grid_exponent(nhix - nlox), ey = grid_exponent(nhiy - nloy), ez = grid_exponent(nhiz - nloz);
+    const float ux = __int_as_float(ex << 23), uy = __int_as_float(ey << 23), uz = __int_as_float(ez << 23);
+    const float px = __fsub_rd(nlox, ux), py = __fsub_rd(nloy, uy), pz = __fsub_rd(nloz, uz);
+    const float ix = __int_as_float((254 - ex) << 23);   // exact 1/unit
+    const float iy = __int_as_float((254 - ey) << 23);
+    const float iz = __int_as_float((254 - ez) << 23);
+    uint32_t meta = 0, qlx = 255, qly = 255, qlz = 255, qhx = 0, qhy = 0, qhz = 0;
+    if (active) {
+        qlx = quant_lo(lo.x, px, ix); qly = quant_lo(lo.y, py, iy); qlz = quant_lo(lo.z, pz, iz);
+        qhx = quant_hi(hi.x, px, ix); qhy = quant_hi(hi.y, py, iy); qhz = quant_hi(hi.z, pz, iz);
+        meta = internal ? (0x20u | (uint32_t)(24 + myslot)) : ((((1u << cnt) - 1u) << 5) | (uint32_t)tri_off);
+    }
+    uint32_t w[20];
+    w[0] = __float_as_uint(px);
+    w[1] = __float_as_uint(py);
+    w[2] = __float_as_uint(pz);
+    w[3] = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16) | (imask << 24);
+    w[4] = (uint32_t)child_base;
+    w[5] = (uint32_t)tri_base;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        w[6 + h] = plane_word(active, myslot, meta, h, 0u);
+        w[8 + h] = plane_word(active, myslot, qlx, h, 0xffffffffu);
+        w[10 + h] = plane_word(active, myslot, qly, h, 0xffffffffu);
+        w[12 + h] = plane_word(active, myslot, qlz, h, 0xffffffffu);
+        w[14 + h] = plane_word(active, myslot, qhx, h, 0u);
+        w[16 + h] = plane_word(active, myslot, qhy, h, 0u);
+        w[18 + h] = plane_word(active, myslot, qhz, h, 0u);
+    }
+    if (lane < 5) {
+        uint4 v;
+        v.x = w[0]; v.y = w[1]; v.z = w[2]; v.w = w[3];
+#pragma unroll
+        for (int q = 1; q < 5; ++q)
+            if (lane == q) { v.x = w[4 * q]; v.y = w[4 * q + 1]; v.z = w[4 * q + 2]; v.w = w[4 * q + 3]; }
+        reinterpret_cast<uint4 *>(A.nodes + task.y)[lane] = v;
+    }
+    if (internal) {
+        const int rank = __popc(imask & ((1u << myslot) - 1u));
+        A.tasks_out[next + rank] = make_int2(ref, child_base + rank);
+    } else if (active) {
+        // the (at most kMaxLeafTris) leaves under this child, left first
+        int32_t todo[kMaxLeafTris];
+        int sp = 0, j = 0;
+        todo[sp++] = ref;
+        while (sp > 0 && j < cnt) {
+            const int32_t r = todo[--sp];
+            if (r >= 0) {
+                if (sp + 2 > kMaxLeafTris) { atomicExch(&A.counters[3], 1); break; }
+                todo[sp++] = A.right[r];
+                todo[sp++] = A.left[r];
+                continue;
+            }
+            const int32_t id = A.vals[~r];
+            const int3 t = A.idx[id];
+            const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
+            const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
+            const float3 cc = make_float3(A.verts[3 * t.z], A.verts[3 * t.z + 1], A.verts[3 * t.z + 2]);
+            PackedTri P;
+            P.w0 = make_float4(a.x, a.y, a.z, b.x);
+            P.w1 = make_float4(b.y, b.z, cc.x, cc.y);
+            P.w2 = make_float4(cc.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
+            A.tris[tri_base + tri_off + j] = P;
+            ++j;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_collapse_level_warp(BuildArgs A)
+{
+    const int32_t ntasks = *A.cur_count;
+    const int lane = threadIdx.x & 31;
+    const int32_t wid = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int32_t nw = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    for (int32_t ti = wid; ti < ntasks; ti += nw) collapse_task_warp(A, A.tasks_in[ti], lane);
+}
+
 // One tree level: every task of the level (count read on the device, so
 // the levels run back to back without host round trips).
 __global__ void k_collapse_level(BuildArgs A)
@@ -1193,6 +1426,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     // one finds no tasks), one read-back per group: most trees end within
     // the first group
     const int cgrid = max(1, min((n + nseg + 63) / 64, in.sm_count * 16));
+    const int wgrid = max(1, min((n + nseg + 3) / 4, in.sm_count * 32));
     int level = 0;
     for (;;) {
         const int stop = min(level + kCollapseGroup, kMaxDepth);
@@ -1201,7 +1435,10 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             A.tasks_out = (level & 1) ? tq0 : tq1;
             A.cur_count = level_count + level;
             A.next_count = level_count + level + 1;
-            k_collapse_level<<<cgrid, 64, 0, st>>>(A);
+            if (A.dec)
+                k_collapse_level_warp<<<wgrid, 128, 0, st>>>(A);
+            else
+                k_collapse_level<<<cgrid, 64, 0, st>>>(A);
         }
         cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(h_cnt + 4, level_count, (kMaxDepth + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
