@@ -440,3 +440,36 @@ def test_builders_on_degenerate_input(rtlib):
     hit_copy = (res[1]["tri"] >= 0) & (res[1]["tri"] < copies)
     assert hit_copy.sum() > 100
     assert (res[1]["tri"][hit_copy] == 0).all()     # equal t: the lowest id wins
+
+
+def test_update_vertices_equals_fresh_upload(rtlib, ctx, oracle):
+    """The per-frame path of a simulation (same topology, moved vertices,
+    rebuild) gives exactly the hits and frame of a scene uploaded fresh at
+    the new positions, and the oracle's hits."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=10, res=96)
+    sc = rtlib.Scene(ctx, scene)
+    rng = np.random.default_rng(17)
+    rays = None
+    for step in range(3):
+        moved = dict(scene)
+        v = scene["verts"].astype(np.float64)
+        v = v + np.array([0.05 * step, -0.03 * step, 0.02 * step]) + rng.normal(0.0, 0.002, v.shape)
+        moved["verts"] = v.astype(np.float32)
+        sc.update_vertices(moved["verts"])
+        fresh = rtlib.Scene(ctx, moved)
+        if rays is None:
+            o = np.tile(np.array([0.1, 0.3, 4.0], np.float32), (3000, 1))
+            d = rng.normal(size=(3000, 3)) * 0.2 + np.array([0.0, 0.0, -1.0])
+            d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+            rays = rtlib.rays_array(o, d)
+        a, b = sc.closest(rays), fresh.closest(rays)
+        assert np.array_equal(a["tri"], b["tri"]) and np.array_equal(a["t"], b["t"])
+        ra, rb = sc.render(frame, want_ids=True), fresh.render(frame, want_ids=True)
+        assert np.array_equal(ra["rgb"], rb["rgb"]) and np.array_equal(ra["ids"], rb["ids"])
+        o3, d3 = np.ascontiguousarray(rays["o"]), np.ascontiguousarray(rays["d"])
+        rid, rt_, _, _ = oracle.OracleScene(moved).closest(o3, d3)
+        mismatch, _ = compare_hits(moved["verts"], moved["tris"], o3, d3, a["tri"], a["t"], rid, rt_)
+        assert not mismatch.any()
+        fresh.close()
+    sc.close()
