@@ -473,3 +473,69 @@ def test_update_vertices_equals_fresh_upload(rtlib, ctx, oracle):
         assert not mismatch.any()
         fresh.close()
     sc.close()
+
+
+@pytest.mark.parametrize("bright", [False, True], ids=["fast_pow", "exact_pow"])
+def test_eight_lights_vs_oracle(rtlib, ctx, oracle, bright):
+    """RT_MAX_LIGHTS (8) point and directional lights, with light colours in
+    0..255 (single-precision specular power + exact re-shade near
+    truncation) and above 255 (exact power throughout): frames agree with
+    the oracle; a ninth light is refused."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=12, res=128)
+    rng = np.random.default_rng(23)
+    lights = []
+    for k in range(8):
+        rgb = tuple(float(x) for x in rng.uniform(40.0, 400.0 if bright else 255.0, 3))
+        if k % 2:
+            lights.append(scenes.directional_light(rng.normal(size=3), rgb=rgb))
+        else:
+            lights.append(scenes.point_light(rng.uniform(-4.0, 4.0, 3) + np.array([0.0, 4.0, 0.0]), rgb=rgb,
+                                             d=float(rng.uniform(0.0, 0.2))))
+    f = dict(frame)
+    f["lights"] = lights
+    sc = rtlib.Scene(ctx, scene)
+    got = sc.render(f, want_ids=True)
+    ref = oracle.OracleScene(scene).render(f, want_ids=True)
+    within1, exact, worst = pixel_agreement(got["rgb"], ref["rgb"])
+    assert within1 >= PIX_FRAC, (within1, exact, worst)
+    assert exact >= 0.99
+    f9 = dict(f)
+    f9["lights"] = lights + [lights[0]]
+    with pytest.raises(rtlib.RtError):
+        sc.render(f9)
+    sc.close()
+
+
+def test_batch_at_the_scene_limit(rtlib, ctx):
+    """1024 scenes (the most one batched build takes; the segment id uses 10
+    key bits) render exactly as each scene alone; a 1025th is refused."""
+    torch = pytest.importorskip("torch")
+    from raptor_gb300 import scenes
+    rng = np.random.default_rng(29)
+    b = rtlib.Batch(ctx)
+    items = []
+    for k in range(1024):
+        v, t = scenes.geodesic_sphere(1 + k % 3)
+        v = v * float(rng.uniform(0.5, 1.5)) + rng.normal(0.0, 0.2, 3)
+        sc = {"verts": v.astype(np.float32), "tris": t}
+        items.append((b.add_scene(sc), sc))
+    with pytest.raises(rtlib.RtError):
+        b.add_scene(items[0][1])
+    b.build()
+    _, frame = scenes.icosphere_scene(freq=2, res=24)
+    jobs, bufs = [], []
+    for idx, _ in items[::8]:
+        W, H = frame["camera"]["xres"], frame["camera"]["yres"]
+        rgb = torch.zeros((H, W, 3), dtype=torch.uint8, device="cuda")
+        ids = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+        bufs.append((rgb, ids))
+        jobs.append(rtlib.make_job(idx, frame, rgb, ids))
+    b.set_jobs(jobs)
+    b.render()
+    for (rgb, ids), (_, sc) in zip(bufs, items[::8]):
+        s = rtlib.Scene(ctx, sc)
+        r = s.render(frame, want_ids=True)
+        assert np.array_equal(rgb.cpu().numpy(), r["rgb"]) and np.array_equal(ids.cpu().numpy(), r["ids"])
+        s.close()
+    b.close()
