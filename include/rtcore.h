@@ -180,6 +180,15 @@ rt_status rt_scene_upload(rt_scene *scene, const float *verts_xyz, int32_t nvert
  * (physics_engine/simulation_environment.cc:56-58). */
 rt_status rt_scene_update_vertices(rt_scene *scene, const float *verts_xyz, int32_t nverts);
 
+/* Update vertex positions (same topology) and refit the existing hierarchy
+ * instead of rebuilding it: shading records and boxes recomputed bottom-up,
+ * every wide node re-quantised, the tree's topology kept.  The cheap
+ * per-frame path for small motions of the same physics-engine loop
+ * (physics_engine/simulation_environment.cc:56-58); hits are exact as after
+ * a rebuild, traversal slows as the motion departs from the built layout.
+ * Requires a built scene.  refit_ms (nullable): device time. */
+rt_status rt_scene_refit_vertices(rt_scene *scene, const float *verts_xyz, int32_t nverts, float *refit_ms);
+
 /* Build the acceleration structure: GPU Morton LBVH collapsed to 8-wide
  * nodes with 8-bit conservatively quantised child boxes.  Replaces
  * bvh::bvh(primitive_store&) -> bvh_builder::build

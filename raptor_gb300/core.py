@@ -121,6 +121,7 @@ SIGNATURES = [
     ("rt_trace_closest", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_trace_any", C.c_int32, [_P, _P, C.c_int32, _P]),
     ("rt_trace_closest_noalloc", C.c_int32, [_P, _P, C.c_int32, _P]),
+    ("rt_scene_refit_vertices", C.c_int32, [_P, _P, C.c_int32, C.POINTER(C.c_float)]),
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
@@ -267,6 +268,12 @@ class Scene:
 
     def update_vertices(self, verts):
         _check(lib().rt_scene_update_vertices(self.h, ptr(verts), int(verts.shape[0])))
+
+    def refit_vertices(self, verts) -> float:
+        """Move the vertices and refit the existing tree; returns device ms."""
+        ms = C.c_float()
+        _check(lib().rt_scene_refit_vertices(self.h, ptr(verts), int(verts.shape[0]), C.byref(ms)))
+        return ms.value
 
     def build(self) -> float:
         ms = C.c_float()

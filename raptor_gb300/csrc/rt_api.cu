@@ -401,6 +401,7 @@ rt_status rt_bvh_build(rt_scene *s, float *build_ms)
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);
     s->built = false;
+    s->refit = RefitArrays();
     if (build_ms) *build_ms = 0.f;
     if (s->ntris == 0) {
         s->built = true;
@@ -440,6 +441,38 @@ rt_status rt_bvh_build(rt_scene *s, float *build_ms)
     s->nnodes = R.nodes;
     s->tri_slots = R.tri_slots;
     s->depth = R.depth;
+    s->refit = R.refit;
+    s->built = true;
+    return RT_OK;
+}
+
+rt_status rt_scene_refit_vertices(rt_scene *s, const float *verts, int32_t nverts, float *refit_ms)
+{
+    if (!s || !verts) return fail(RT_ERR_INVALID_ARG, "rt_scene_refit_vertices: NULL argument");
+    if (nverts != s->nverts) return fail(RT_ERR_INVALID_ARG, "rt_scene_refit_vertices: vertex count changed");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_scene_refit_vertices: hierarchy not built");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    if (refit_ms) *refit_ms = 0.f;
+    if (nverts > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_verts, verts, (size_t)nverts * 3 * sizeof(float), cudaMemcpyDefault, ctx->stream),
+                "vertex copy");
+    if (!s->refit.valid) {   // one triangle or none: nothing to keep, build again
+        s->built = false;
+        return rt_bvh_build(s, refit_ms);
+    }
+    s->built = false;
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    const int32_t st = refit_wide_bvh(s->refit, s->d_verts, s->d_idx, s->d_shade, s->d_nodes, s->d_tris,
+                                      ctx->h_scratch, ctx->stream);
+    if (st != 0) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "refit");
+        return fail(st, "rt_scene_refit_vertices: refit failed");
+    }
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    RT_CUDA(cudaEventSynchronize(ctx->ev1), "event synchronize");
+    if (refit_ms) cudaEventElapsedTime(refit_ms, ctx->ev0, ctx->ev1);
     s->built = true;
     return RT_OK;
 }

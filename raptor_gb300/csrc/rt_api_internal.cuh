@@ -4,6 +4,7 @@
 #include <cmath>
 #include <string>
 
+#include "rt_build.cuh"
 #include "rt_internal.cuh"
 #include "rt_kernels.cuh"
 
@@ -56,6 +57,7 @@ struct rt_scene {
     int32_t nnodes = 0, tri_slots = 0, depth = 0;
     bool built = false;
     rtc::DevBuf temp;
+    rtc::RefitArrays refit;   // the last build's tree, for rt_scene_refit_vertices
 };
 
 namespace rtc {

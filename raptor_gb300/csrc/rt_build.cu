@@ -274,17 +274,22 @@ __device__ __forceinline__ void sah_node(float *sah, uint32_t *dec, int32_t id, 
     __stcg(dec + id, d);
 }
 
+constexpr int kRefitMaxDepth = 1 << 16;   // binary levels a refit walk may climb
+constexpr int32_t kEmptySlot = INT32_MIN;
+
 // Bottom-up box refit: the second child to arrive at a node unions both.
 __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
                         const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
                         const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
-                        int32_t *flags, const int32_t *__restrict__ count, float *sah, uint32_t *dec)
+                        int32_t *flags, const int32_t *__restrict__ count, float *sah, uint32_t *dec,
+                        int32_t *err)
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int32_t p = leaf_parent[k];
     int guard = 0;
-    while (p >= 0 && guard++ < 256) {
+    while (p >= 0) {
+        if (++guard > kRefitMaxDepth) { atomicExch(err, 1); return; }
         __threadfence();
         if (atomicAdd(&flags[p], 1) == 0) return;   // first arrival: sibling not ready
         __threadfence();
@@ -551,7 +556,9 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restr
                                                           const int32_t *__restrict__ state, int it,
                                                           int32_t *__restrict__ left, int32_t *__restrict__ right,
                                                           int32_t *__restrict__ ncount, float4 *__restrict__ ilo,
-                                                          float4 *__restrict__ ihi, float *sah, uint32_t *dec)
+                                                          float4 *__restrict__ ihi, float *sah, uint32_t *dec,
+                                                          int32_t *__restrict__ parent,
+                                                          int32_t *__restrict__ leaf_parent)
 {
     const int par = it & 1;
     const int32_t count = state[kStCount + par];
@@ -572,6 +579,8 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_merge(const float4 *__restr
         const int32_t l = __float_as_int(a1.w), r = __float_as_int(b1.w);
         left[id] = l;
         right[id] = r;
+        if (l < 0) leaf_parent[~l] = id; else parent[l] = id;
+        if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
         const int32_t cnt = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
         ncount[id] = cnt;
         float cl[8], cr[8];
@@ -604,7 +613,8 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
                                                          int32_t *state, int it, int32_t *__restrict__ left,
                                                          int32_t *__restrict__ right, int32_t *__restrict__ ncount,
                                                          float4 *__restrict__ ilo, float4 *__restrict__ ihi,
-                                                         float *sah, uint32_t *dec)
+                                                         float *sah, uint32_t *dec, int32_t *__restrict__ parent,
+                                                         int32_t *__restrict__ leaf_parent)
 {
     extern __shared__ float4 tail_smem[];
     float4 *slo = tail_smem;                       // kPlocTailMax
@@ -708,6 +718,8 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
                 const int32_t l = __float_as_int(a1.w), r = __float_as_int(b1.w);
                 left[id] = l;
                 right[id] = r;
+                if (l < 0) leaf_parent[~l] = id; else parent[l] = id;
+                if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
                 const int32_t cnt = (l < 0 ? 1 : ncount[l]) + (r < 0 ? 1 : ncount[r]);
                 ncount[id] = cnt;
                 float cla[8], cra[8];
@@ -753,7 +765,8 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
 // the roots: level-0 collapse tasks (binary ref, wide node = segment).
 __global__ void k_ploc_roots(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
                              const int32_t *__restrict__ state, int it, int2 *__restrict__ tasks,
-                             int32_t *level_count, int32_t *counters)
+                             int32_t *level_count, int32_t *counters, int32_t *__restrict__ parent,
+                             int32_t *__restrict__ leaf_parent)
 {
     const int32_t count = state[kStCount + (it & 1)];
     const int32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -762,7 +775,9 @@ __global__ void k_ploc_roots(const float4 *__restrict__ cl, const float4 *__rest
         if (count != state[kStTarget]) atomicExch(&counters[3], 1);
     }
     if (c >= count) return;
-    tasks[c] = make_int2(__float_as_int(ch[c].w), __float_as_int(cl[c].w));
+    const int32_t root = __float_as_int(ch[c].w);
+    if (root < 0) leaf_parent[~root] = -1; else parent[root] = -1;
+    tasks[c] = make_int2(root, __float_as_int(cl[c].w));
 }
 
 // Exponent e (biased as a float exponent) of the power-of-two grid unit for
@@ -783,6 +798,7 @@ struct BuildArgs {
     const int32_t *left, *right;
     const int32_t *count;         // leaves under each internal node
     const uint32_t *dec;          // surface-area decisions (nullptr: greedy collapse)
+    int32_t *slot_ref;            // binary ref of every slot of every wide node (kEmptySlot: none)
     const float4 *ilo, *ihi, *llo, *lhi;
     const int32_t *vals;          // sorted position -> caller's triangle id
     const float *verts;
@@ -953,6 +969,7 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
     int int_k = 0, tri_off = 0;
     for (int s = 0; s < 8; ++s) {
         const int k = child_in[s];
+        A.slot_ref[8 * (size_t)wide + s] = k < 0 ? kEmptySlot : ch[k];
         if (k < 0) {
             W.meta[s] = 0;
             W.qlo_x[s] = W.qlo_y[s] = W.qlo_z[s] = 255;
@@ -1201,6 +1218,11 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
             if (lane == q) { v.x = w[4 * q]; v.y = w[4 * q + 1]; v.z = w[4 * q + 2]; v.w = w[4 * q + 3]; }
         reinterpret_cast<uint4 *>(A.nodes + task.y)[lane] = v;
     }
+    {
+        const uint32_t occ = __reduce_or_sync(full, active ? (1u << myslot) : 0u);
+        if (active) A.slot_ref[8 * (size_t)task.y + myslot] = ref;
+        if (lane < 8 && !((occ >> lane) & 1u)) A.slot_ref[8 * (size_t)task.y + lane] = kEmptySlot;
+    }
     if (internal) {
         const int rank = __popc(imask & ((1u << myslot) - 1u));
         A.tasks_out[next + rank] = make_int2(ref, child_base + rank);
@@ -1267,6 +1289,7 @@ size_t build_temp_bytes(int32_t n)
     b += nn * sizeof(int32_t);             // refit flags
     b += 2 * nn * sizeof(int2);            // task queues
     b += nn * sizeof(int32_t);             // leaf counts of internal nodes
+    b += 8 * (nn + kMaxSegments + 2) * sizeof(int32_t);   // slot refs of the wide nodes
     b += 9 * nn * sizeof(float);           // surface-area cost tables + decisions
     b += 4 * nn * sizeof(float4);          // PLOC clusters (two buffers of lo, hi)
     b += nn * sizeof(int32_t);             // PLOC nearest neighbours
@@ -1311,6 +1334,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     float4 *ihi = (float4 *)carve(p, nn * sizeof(float4));
     int32_t *rflags = (int32_t *)carve(p, nn * sizeof(int32_t));
     int32_t *ncount = (int32_t *)carve(p, nn * sizeof(int32_t));
+    int32_t *slot_ref = (int32_t *)carve(p, 8 * ((size_t)in.max_nodes + 1) * sizeof(int32_t));
     float *sah = RT_COLLAPSE_SAH ? (float *)carve(p, 8 * nn * sizeof(float)) : nullptr;
     uint32_t *dec = RT_COLLAPSE_SAH ? (uint32_t *)carve(p, nn * sizeof(uint32_t)) : nullptr;
     const bool ploc = in.builder == kBuilderPloc;
@@ -1366,7 +1390,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             if (n > 1) {
                 cudaMemsetAsync(rflags, 0, nn * sizeof(int32_t), st);
                 k_refit<<<g, threads, 0, st>>>(n, left, right, parent, leaf_parent, llo, lhi, ilo, ihi, rflags,
-                                               ncount, sah, dec);
+                                               ncount, sah, dec, counters + 3);
             }
         }
     }
@@ -1396,7 +1420,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
                 k_ploc_scan<<<1, kPlocBlock, 0, st>>>(bsum, pstate, it);
                 k_ploc_merge<<<max(blocks, 1), kPlocBlock, 0, st>>>(cl[a], chh[a], cl[a ^ 1], chh[a ^ 1], nnb, bsum,
                                                                     pstate, it, left, right, ncount, ilo, ihi,
-                                                                    sah, dec);
+                                                                    sah, dec, parent, leaf_parent);
             }
             cudaMemcpyAsync(h_cnt, pstate, kStWords * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
@@ -1406,9 +1430,9 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         }
         if (tail)
             k_ploc_tail<<<1, kPlocBlock, tail_smem, st>>>(cl[it & 1], chh[it & 1], pstate, it, left, right, ncount,
-                                                          ilo, ihi, sah, dec);
+                                                          ilo, ihi, sah, dec, parent, leaf_parent);
         k_ploc_roots<<<(nseg + 127) / 128, 128, 0, st>>>(cl[it & 1], chh[it & 1], pstate, it, tq0, level_count,
-                                                        counters);
+                                                        counters, parent, leaf_parent);
     } else {
         k_roots<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, first, last, parent, leaf_parent, tq0,
                                                     level_count, counters, in.nodes);
@@ -1417,7 +1441,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     cudaMemcpyAsync(&counters[0], &nroot_nodes, sizeof(int32_t), cudaMemcpyHostToDevice, st);
 
     BuildArgs A;
-    A.n = n; A.left = left; A.right = right; A.count = ncount; A.dec = dec;
+    A.n = n; A.left = left; A.right = right; A.count = ncount; A.dec = dec; A.slot_ref = slot_ref;
     A.ilo = ilo; A.ihi = ihi; A.llo = llo; A.lhi = lhi; A.vals = vals2;
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
@@ -1453,7 +1477,113 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     R.nodes = h_cnt[0];
     R.tri_slots = h_cnt[1];
     R.depth = depth;
+    RefitArrays &K = R.refit;
+    K.valid = nseg == 1 && n > 1;
+    K.vals = vals2; K.left = left; K.right = right; K.parent = parent; K.leaf_parent = leaf_parent;
+    K.blo = blo; K.bhi = bhi; K.llo = llo; K.lhi = lhi; K.ilo = ilo; K.ihi = ihi; K.flags = rflags;
+    K.slot_ref = slot_ref; K.err = counters + 3;
+    K.ntris = n; K.nnodes = R.nodes; K.tri_slots = R.tri_slots;
     return R;
+}
+
+namespace {
+
+// Refit, per triangle (caller's order): shading record and box.
+__global__ void k_refit_tris(const float *__restrict__ verts, const int3 *__restrict__ idx, int32_t n,
+                             ShadeTri *__restrict__ shade, float4 *__restrict__ blo, float4 *__restrict__ bhi)
+{
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int3 t = idx[i];
+        const float3 a = make_float3(verts[3 * t.x], verts[3 * t.x + 1], verts[3 * t.x + 2]);
+        const float3 b = make_float3(verts[3 * t.y], verts[3 * t.y + 1], verts[3 * t.y + 2]);
+        const float3 c = make_float3(verts[3 * t.z], verts[3 * t.z + 1], verts[3 * t.z + 2]);
+        const float3 nn = xnorm(xcross(xsub3(b, a), xsub3(c, a)));
+        ShadeTri st;
+        st.n_cx = make_float4(nn.x, nn.y, nn.z, c.x);
+        st.c_yz = make_float2(c.y, c.z);
+        st.pad = make_float2(0.f, 0.f);
+        shade[i] = st;
+        blo[i] = make_float4(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)), 0.f);
+        bhi[i] = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.f);
+    }
+}
+
+// Refit, per wide node: new quantisation frame from its children's refitted
+// boxes, every occupied slot re-quantised; links and triangle groups kept.
+__global__ void k_requant(WideNode *__restrict__ nodes, int32_t nnodes, const int32_t *__restrict__ slot_ref,
+                          const float4 *__restrict__ llo, const float4 *__restrict__ lhi,
+                          const float4 *__restrict__ ilo, const float4 *__restrict__ ihi)
+{
+    const int32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nnodes) return;
+    float4 lo[8], hi[8];
+    float4 nlo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), nhi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
+    uint32_t occ = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int32_t r = slot_ref[8 * (size_t)w + s];
+        if (r == kEmptySlot) continue;
+        occ |= 1u << s;
+        lo[s] = r < 0 ? llo[~r] : __ldcg(&ilo[r]);
+        hi[s] = r < 0 ? lhi[~r] : __ldcg(&ihi[r]);
+        nlo = make_float4(fminf(nlo.x, lo[s].x), fminf(nlo.y, lo[s].y), fminf(nlo.z, lo[s].z), 0.f);
+        nhi = make_float4(fmaxf(nhi.x, hi[s].x), fmaxf(nhi.y, hi[s].y), fmaxf(nhi.z, hi[s].z), 0.f);
+    }
+    if (!occ) return;
+    const int ex = grid_exponent(nhi.x - nlo.x), ey = grid_exponent(nhi.y - nlo.y), ez = grid_exponent(nhi.z - nlo.z);
+    const float ux = __int_as_float(ex << 23), uy = __int_as_float(ey << 23), uz = __int_as_float(ez << 23);
+    const float px = __fsub_rd(nlo.x, ux), py = __fsub_rd(nlo.y, uy), pz = __fsub_rd(nlo.z, uz);
+    const float ix = __int_as_float((254 - ex) << 23);
+    const float iy = __int_as_float((254 - ey) << 23);
+    const float iz = __int_as_float((254 - ez) << 23);
+    WideNode W = nodes[w];
+    W.px = px; W.py = py; W.pz = pz;
+    W.ex = (uint8_t)ex; W.ey = (uint8_t)ey; W.ez = (uint8_t)ez;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        if (!((occ >> s) & 1u)) continue;
+        W.qlo_x[s] = (uint8_t)quant_lo(lo[s].x, px, ix); W.qlo_y[s] = (uint8_t)quant_lo(lo[s].y, py, iy);
+        W.qlo_z[s] = (uint8_t)quant_lo(lo[s].z, pz, iz);
+        W.qhi_x[s] = (uint8_t)quant_hi(hi[s].x, px, ix); W.qhi_y[s] = (uint8_t)quant_hi(hi[s].y, py, iy);
+        W.qhi_z[s] = (uint8_t)quant_hi(hi[s].z, pz, iz);
+    }
+    nodes[w] = W;
+}
+
+// Refit, per packed triangle (leaf order): the new vertices, id and flags kept.
+__global__ void k_repack(PackedTri *__restrict__ tris, int32_t nslots, const float *__restrict__ verts,
+                         const int3 *__restrict__ idx)
+{
+    const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nslots) return;
+    PackedTri P = tris[j];
+    const int3 t = idx[__float_as_int(P.w2.y)];
+    P.w0 = make_float4(verts[3 * t.x], verts[3 * t.x + 1], verts[3 * t.x + 2], verts[3 * t.y]);
+    P.w1 = make_float4(verts[3 * t.y + 1], verts[3 * t.y + 2], verts[3 * t.z], verts[3 * t.z + 1]);
+    P.w2.x = verts[3 * t.z + 2];
+    tris[j] = P;
+}
+
+}  // namespace
+
+int32_t refit_wide_bvh(const RefitArrays &K, const float *verts, const int3 *idx, ShadeTri *shade, WideNode *nodes,
+                       PackedTri *tris, int32_t *host_scratch, cudaStream_t st)
+{
+    if (!K.valid) return -4;
+    const int threads = 256;
+    const int32_t n = K.ntris;
+    const int g = (n + threads - 1) / threads;
+    cudaMemsetAsync(K.err, 0, sizeof(int32_t), st);
+    k_refit_tris<<<g, threads, 0, st>>>(verts, idx, n, shade, K.blo, K.bhi);
+    k_leaf_boxes<<<g, threads, 0, st>>>(K.vals, n, K.blo, K.bhi, K.llo, K.lhi);
+    cudaMemsetAsync(K.flags, 0, (size_t)n * sizeof(int32_t), st);
+    k_refit<<<g, threads, 0, st>>>(n, K.left, K.right, K.parent, K.leaf_parent, K.llo, K.lhi, K.ilo, K.ihi, K.flags,
+                                   nullptr, nullptr, nullptr, K.err);
+    k_requant<<<(K.nnodes + 127) / 128, 128, 0, st>>>(nodes, K.nnodes, K.slot_ref, K.llo, K.lhi, K.ilo, K.ihi);
+    k_repack<<<(K.tri_slots + 255) / 256, 256, 0, st>>>(tris, K.tri_slots, verts, idx);
+    cudaMemcpyAsync(host_scratch, K.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -2;
+    return host_scratch[0] ? -8 : 0;
 }
 
 }  // namespace rtc

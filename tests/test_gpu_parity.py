@@ -539,3 +539,48 @@ def test_batch_at_the_scene_limit(rtlib, ctx):
         assert np.array_equal(rgb.cpu().numpy(), r["rgb"]) and np.array_equal(ids.cpu().numpy(), r["ids"])
         s.close()
     b.close()
+
+
+@pytest.mark.parametrize("builder", ["lbvh", "ploc"])
+def test_refit_equals_fresh_upload(rtlib, builder):
+    """rt_scene_refit_vertices keeps the tree's topology and refits boxes and
+    quantisation: after small and large motions the closest hits, any hits
+    and frames equal those of a scene built fresh at the new positions; the
+    node count does not change.  Refit needs a built scene."""
+    from raptor_gb300 import scenes
+    c = rtlib.Context(0)
+    c.set_option(rtlib.RT_OPT_BUILDER, rtlib.RT_BUILDER_LBVH if builder == "lbvh" else rtlib.RT_BUILDER_PLOC)
+    scene, frame = scenes.terrain_scene(size_pow2=128, xres=160, yres=90)
+    sc = rtlib.Scene(c, scene)
+    nodes0 = sc.info()["nodes"]
+    rng = np.random.default_rng(31)
+    v0 = scene["verts"].astype(np.float64)
+    lo, hi = v0.min(0), v0.max(0)
+    o = rng.uniform(lo, hi, size=(20000, 3))
+    o[:, 1] = hi[1] + 50.0
+    d = rng.normal(size=(20000, 3)) * 0.3 + np.array([0.0, -1.0, 0.0])
+    d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+    rays = rtlib.rays_array(o.astype(np.float32), d, tmax=np.float32(120.0))
+    for step, (shift, wobble, scale) in enumerate([(0.5, 0.05, 1.0), (3.0, 0.5, 1.0), (0.0, 2.0, 1.8)]):
+        v = v0 * np.array([1.0, scale, 1.0]) + np.array([shift, 0.0, -shift]) + rng.normal(0.0, wobble, v0.shape)
+        moved = dict(scene)
+        moved["verts"] = v.astype(np.float32)
+        ms = sc.refit_vertices(moved["verts"])
+        assert ms > 0.0
+        assert sc.info()["nodes"] == nodes0
+        fresh = rtlib.Scene(c, moved)
+        a, b = sc.closest(rays), fresh.closest(rays)
+        assert np.array_equal(a["tri"], b["tri"]) and np.array_equal(a["t"], b["t"]), step
+        assert np.array_equal(sc.any(rays), fresh.any(rays))
+        ra, rb = sc.render(frame, want_ids=True), fresh.render(frame, want_ids=True)
+        assert np.array_equal(ra["rgb"], rb["rgb"]) and np.array_equal(ra["ids"], rb["ids"])
+        fresh.close()
+    st = sc.stats()
+    assert sum(k * n for k, n in zip((1, 2, 3), st["leaf_tris"])) == scene["tris"].shape[0]
+    # an uploaded but unbuilt scene refuses a refit
+    raw = rtlib.Scene(c, scene, build=False)
+    with pytest.raises(rtlib.RtError):
+        raw.refit_vertices(scene["verts"])
+    raw.close()
+    sc.close()
+    c.close()
