@@ -85,6 +85,28 @@ class gpu_bvh : public ssd
             gpu_detail::check(rt_bvh_build(_scene, nullptr));
         }
 
+        // Per-frame update of a simulation loop that keeps the same
+        // primitives and moves their vertices (the rebuild at
+        // physics_engine/simulation_environment.cc:56-58): refits the
+        // existing hierarchy instead of building a new one.
+        void refit(const primitive_store &prims)
+        {
+            const int n = prims.size();
+            std::vector<float> verts(9 * (size_t)n);
+            for (int i = 0; i < n; ++i)
+            {
+                const triangle *t = prims.primitive(i);
+                const point_t<> v[3] = { t->get_vertex_a(), t->get_vertex_b(), t->get_vertex_c() };
+                for (int k = 0; k < 3; ++k)
+                {
+                    verts[9 * i + 3 * k + 0] = v[k].x;
+                    verts[9 * i + 3 * k + 1] = v[k].y;
+                    verts[9 * i + 3 * k + 2] = v[k].z;
+                }
+            }
+            gpu_detail::check(rt_scene_refit_vertices(_scene, verts.data(), 3 * n, nullptr));
+        }
+
         ~gpu_bvh() { rt_scene_destroy(_scene); }
         gpu_bvh(const gpu_bvh &) = delete;
         gpu_bvh &operator=(const gpu_bvh &) = delete;
