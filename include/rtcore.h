@@ -252,6 +252,16 @@ rt_status rt_trace_closest_noalloc(rt_scene *scene, const rt_ray *rays, int32_t 
 rt_status rt_render(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
                     const rt_material *material, uint8_t *rgb_out, int32_t *hit_ids, rt_render_stats *stats);
 
+/* Anti-aliased frame: aa_x * aa_y rays per output pixel on the supersampled
+ * camera grid (xres * aa_x by yres * aa_y), each shaded as by rt_render, and
+ * their colours averaged into the xres * yres RGB8 output.  Replaces the
+ * reference camera built with anti-aliasing factors x_a_res / y_a_res
+ * (raytracer/camera.h:55-62) rendered by ray_tracer and downsampled by
+ * camera::clip_image_to_rgb (camera.h:289-319: samples summed x outer, y
+ * inner, divided by their count, clamped, truncated).  aa_x, aa_y in 1..16. */
+rt_status rt_render_aa(rt_scene *scene, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const rt_light *lights,
+                       int32_t nlights, const rt_material *material, uint8_t *rgb_out, rt_render_stats *stats);
+
 /* Ambient-occlusion render (no reference counterpart; the reference has no
  * AO): primary closest hit, then `samples` cosine-weighted hemisphere rays
  * per hit (Philox4x32-10 keyed by pixel and sample, seed) from the offset hit

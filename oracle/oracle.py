@@ -182,6 +182,9 @@ def ref_lib():
         lib["rref_scene_create"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32, C.POINTER(Material)]
         lib["rref_render"].restype = C.c_double
         lib["rref_render"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32, _U8]
+        lib["rref_render_aa"].restype = C.c_double
+        lib["rref_render_aa"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32, C.POINTER(Light),
+                                          C.c_int32, _U8]
         _ref = lib
     return _ref
 
@@ -254,12 +257,48 @@ class RefScene(_SceneBase):
                                                _p(a, C.c_float), _p(f, C.c_uint32), C.byref(self.mat))
         self.build_seconds = self.lib["rref_scene_build"](self.h)
 
-    def render(self, frame):
+    def render(self, frame, aa=(1, 1)):
+        """ray_tracer + clip_image_to_rgb; aa = (x_a_res, y_a_res) rays per
+        output pixel along x and y (the camera's anti-aliasing factors)."""
         cam = make_camera(frame["camera"])
         rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
         ls = make_lights(frame["lights"])
-        secs = self.lib["rref_render"](self.h, C.byref(cam), ls, len(frame["lights"]), _p(rgb, C.c_uint8))
+        secs = self.lib["rref_render_aa"](self.h, C.byref(cam), int(aa[0]), int(aa[1]), ls, len(frame["lights"]),
+                                          _p(rgb, C.c_uint8))
         return {"rgb": rgb, "seconds": secs}
+
+
+def supersampled(frame, aa_x, aa_y):
+    """The frame with aa_x * aa_y camera rays per output pixel: the camera
+    grid the reference traces for x_a_res / y_a_res (camera.h:55-62)."""
+    f = dict(frame)
+    cam = dict(frame["camera"])
+    cam["xres"] = cam["xres"] * aa_x
+    cam["yres"] = cam["yres"] * aa_y
+    f["camera"] = cam
+    return f
+
+
+def downsample_rgb8(fimg, aa_x, aa_y):
+    """camera::clip_image_to_rgb (camera.h:289-319) on a supersampled float
+    image (row = y): per output pixel the samples are summed in binary32,
+    a_x outer and a_y inner, starting from 0, divided by their count,
+    clamped to [0, 255] and truncated."""
+    fimg = np.asarray(fimg, np.float32)
+    H, W = fimg.shape[0] // aa_y, fimg.shape[1] // aa_x
+    acc = np.zeros((H, W, 3), np.float32)
+    for a_x in range(aa_x):
+        for a_y in range(aa_y):
+            acc = acc + fimg[a_y::aa_y, a_x::aa_x, :][:H, :W]
+    v = acc / np.float32(aa_x * aa_y)
+    return np.minimum(np.float32(255.0), np.maximum(np.float32(0.0), v)).astype(np.uint8)
+
+
+def render_aa(scene_obj, frame, aa_x, aa_y):
+    """Anti-aliased frame by the restatement: the supersampled float image of
+    OracleScene.render, then downsample_rgb8."""
+    out = scene_obj.render(supersampled(frame, aa_x, aa_y), want_float=True)
+    return downsample_rgb8(out["fimg"], aa_x, aa_y)
 
 
 def camera_rays(cam_dict, x0=0, y0=0, w=None, h=None, lib=None):

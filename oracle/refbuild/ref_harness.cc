@@ -132,11 +132,11 @@ int32_t rref_trace_any(void *h, const float *ogn, const float *dir, const float 
     return 0;
 }
 
-static camera *make_camera(const ro_camera *c)
+static camera *make_camera(const ro_camera *c, unsigned aa_x = 1u, unsigned aa_y = 1u)
 {
     return new camera(p3(c->pos), p3(c->x_axis), p3(c->y_axis), p3(c->z_axis),
                       ext_colour_t(c->background[0], c->background[1], c->background[2]), c->w, c->h, c->t,
-                      (unsigned)c->xres, (unsigned)c->yres, 1u, 1u, 0.0f, 0.0f);
+                      (unsigned)c->xres, (unsigned)c->yres, aa_x, aa_y, 0.0f, 0.0f);
 }
 
 void rref_camera_rays(const ro_camera *c, int32_t x0, int32_t y0, int32_t w, int32_t hgt, float *ogn, float *dir)
@@ -157,10 +157,22 @@ void rref_camera_rays(const ro_camera *c, int32_t x0, int32_t y0, int32_t w, int
 // clip_image_to_rgb (camera.h:289).  The per-pixel progress line the
 // reference prints (raytracer.cc:529) goes to a null stream.  Returns the
 // render wall time in seconds.
+// The same with anti-aliasing: the camera traces aa_x * aa_y rays per output
+// pixel (camera.h:55-62, x_a_res / y_a_res) and clip_image_to_rgb averages
+// them (camera.h:289-319).  rgb holds xres * yres output pixels.
+double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
+                      uint8_t *rgb);
+
 double rref_render(void *h, const ro_camera *c, const ro_light *ls, int32_t nl, uint8_t *rgb)
 {
+    return rref_render_aa(h, c, 1, 1, ls, nl, rgb);
+}
+
+double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
+                      uint8_t *rgb)
+{
     auto *s = static_cast<ref_scene *>(h);
-    std::unique_ptr<camera> cam(make_camera(c));
+    std::unique_ptr<camera> cam(make_camera(c, (unsigned)aa_x, (unsigned)aa_y));
     light_list lights;
     for (int32_t i = 0; i < nl; ++i) {
         const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);

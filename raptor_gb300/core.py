@@ -124,6 +124,8 @@ SIGNATURES = [
     ("rt_scene_refit_vertices", C.c_int32, [_P, _P, C.c_int32, C.POINTER(C.c_float)]),
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
+    ("rt_render_aa", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight), C.c_int32,
+                                 C.POINTER(RtMaterial), _P, C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
                                  _P, _P, _P, C.POINTER(RtRenderStats)]),
     ("rt_scene_update_attributes", C.c_int32, [_P, _P, C.c_int32]),
@@ -326,6 +328,17 @@ class Scene:
         _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
                                C.byref(st)))
         return {"rgb": rgb, "ids": ids, "stats": st}
+
+    def render_aa(self, frame, aa_x, aa_y, rgb=None):
+        """Anti-aliased frame: aa_x * aa_y rays per output pixel, averaged."""
+        cam = make_camera(frame["camera"])
+        if rgb is None:
+            rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
+        st = RtRenderStats()
+        ls = make_lights(frame["lights"])
+        _check(lib().rt_render_aa(self.h, C.byref(cam), int(aa_x), int(aa_y), ls, len(frame["lights"]),
+                                  C.byref(make_material(frame["material"])), ptr(rgb), C.byref(st)))
+        return {"rgb": rgb, "stats": st}
 
     def update_attributes(self, vattr):
         _check(lib().rt_scene_update_attributes(self.h, ptr(vattr), int(vattr.shape[0])))

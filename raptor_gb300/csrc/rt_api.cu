@@ -658,6 +658,42 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
 }
 
+rt_status rt_render_aa(rt_scene *s, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const rt_light *lights,
+                       int32_t nlights, const rt_material *material, uint8_t *rgb_out, rt_render_stats *stats)
+{
+    if (!s || !material || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render_aa: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (aa_x < 1 || aa_x > 16 || aa_y < 1 || aa_y > 16)
+        return fail(RT_ERR_INVALID_ARG, "rt_render_aa: anti-aliasing factors must be 1..16");
+    rt_camera fine = *camera;   // the supersampled grid the rays are traced on
+    fine.xres = camera->xres * aa_x;
+    fine.yres = camera->yres * aa_y;
+    st = check_camera(&fine);
+    if (st != RT_OK) return st;
+    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
+        return fail(RT_ERR_INVALID_ARG, "rt_render_aa: light count out of range");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_aa: hierarchy not built");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
+    if (st != RT_OK) return st;
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = fast_pow_ok(lights, nlights, *material) ? 1 : 0;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render_aa(scene_view(s), make_camera_view(fine), ls, make_material_view(*material), aa_x, aa_y,
+                     camera->xres, camera->yres, o.rgb, ctx->d_counters, ctx->sm_count, ctx->stream,
+                     ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, stats);
+}
+
 rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *material, int32_t samples,
                        float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
                        rt_render_stats *stats)

@@ -126,6 +126,66 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
     if (status) atomicOr(&ctr->status, status);
 }
 
+// Anti-aliased frame (camera x_a_res / y_a_res, camera.h:55-62, averaged by
+// clip_image_to_rgb, camera.h:289-319): one output pixel per lane; its
+// aa_x * aa_y samples on the supersampled camera grid are shaded and summed
+// a_x outer, a_y inner, divided by their count, clamped and truncated.  With
+// the single-precision specular power, an average within the truncation
+// guard of an integer is recomputed from samples shaded with the exact
+// power.
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_aa(SceneView sc, CameraView cam,
+                                                             LightSet lights, MaterialView mat, int32_t aa_x,
+                                                             int32_t aa_y, int32_t out_x, int32_t out_y,
+                                                             uint8_t *__restrict__ rgb, Counters *ctr)
+{
+    int tiles_x;
+    const int items = tiles_of<8>(out_x, out_y, tiles_x) * 32;
+    const float nsamples = (float)(aa_x * aa_y);
+    uint32_t status = 0;
+    FetchCount fc;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items) break;
+        int x, y;
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
+        const bool live = (x < out_x) && (y < out_y);
+        uint32_t primary = 0, hits = 0, secondary = 0;
+        if (live) {
+            float3 sum = make_float3(0.f, 0.f, 0.f);
+            for (int ax = 0; ax < aa_x; ++ax)
+                for (int ay = 0; ay < aa_y; ++ay) {
+                    const PixelOut po = shade_pixel_lights<COUNT>(sc, cam, lights.l, lights.n, mat, x * aa_x + ax,
+                                                                  y * aa_y + ay, status, &fc, lights.fast_pow != 0);
+                    sum = xadd3(sum, po.c);
+                    ++primary;
+                    hits += po.hit ? 1u : 0u;
+                    secondary += po.secondary;
+                }
+            float3 avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+            if (lights.fast_pow && near_truncation(avg)) {
+                sum = make_float3(0.f, 0.f, 0.f);
+                for (int ax = 0; ax < aa_x; ++ax)
+                    for (int ay = 0; ay < aa_y; ++ay) {
+                        const PixelOut po = shade_pixel_lights<false>(sc, cam, lights.l, lights.n, mat, x * aa_x + ax,
+                                                                      y * aa_y + ay, status, nullptr, false);
+                        sum = xadd3(sum, po.c);
+                    }
+                avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+            }
+            store_rgb(rgb, (size_t)x + (size_t)y * (size_t)out_x, avg);
+        }
+        warp_add(&ctr->primary, primary);
+        warp_add(&ctr->hits, hits);
+        warp_add(&ctr->secondary, secondary);
+    }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
 }  // namespace
 
 // Persistent grid: SMs x resident blocks per SM (from the occupancy API).
@@ -162,6 +222,17 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
         k_render<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
     else
         k_render<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+}
+
+void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
+                      int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, Counters *ctr,
+                      int sm_count, cudaStream_t st, bool count)
+{
+    static const int grid = grid_of(k_render_aa<false>, sm_count);
+    if (count)
+        k_render_aa<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, ctr);
+    else
+        k_render_aa<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, ctr);
 }
 
 void launch_render_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat, int32_t samples,

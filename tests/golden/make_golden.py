@@ -12,7 +12,8 @@ It writes
                     raytracer/unit_tests/vint_tests.cc
   ref_small.npz     inputs and outputs of the reference's own bvh,
                     ray_tracer() and clip_image_to_rgb() (compiled by
-                    oracle/refbuild/Makefile) on small seeded scenes
+                    oracle/refbuild/Makefile) on small seeded scenes, also
+                    with the camera's anti-aliasing factors (2x2, 3x2)
 The tests compare the C restatement (oracle/rtoracle.c) and the CUDA core
 against these files; nothing at test time reads the reference tree.
 """
@@ -91,6 +92,9 @@ def parse_morton_tests(path):
     return {"source": "raytracer/unit_tests/vint_tests.cc", "cases": out}
 
 
+AA_FACTORS = ((2, 2), (3, 2))
+
+
 def small_scenes():
     from raptor_gb300 import scenes
     out = {}
@@ -146,6 +150,9 @@ def main():
         arrays.update({f"{key}_verts": s["verts"], f"{key}_tris": s["tris"], f"{key}_vattr": s["vattr"],
                        f"{key}_ray_o": og, f"{key}_ray_d": dr, f"{key}_id": ids, f"{key}_t": t, f"{key}_u": u,
                        f"{key}_v": v, f"{key}_rgb": rgb})
+        # anti-aliased frames: the camera's x_a_res / y_a_res factors
+        for ax, ay in AA_FACTORS:
+            arrays[f"{key}_aa{ax}{ay}_rgb"] = rs.render(f, aa=(ax, ay))["rgb"]
         arrays[f"{key}_frame"] = np.frombuffer(json.dumps(f).encode(), dtype=np.uint8)
     s, o, d, tmax = soup()
     rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))

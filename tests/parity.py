@@ -60,3 +60,21 @@ def compare_hits(verts, tris, o, d, ids_a, t_a, ids_b, t_b):
 def pixel_agreement(rgb_a, rgb_b):
     diff = np.abs(rgb_a.astype(np.int32) - rgb_b.astype(np.int32)).max(axis=-1)
     return float((diff <= 1).mean()), float((diff == 0).mean()), int(diff.max())
+
+
+def aa_edge_pixels(oracle, scene, frame, aa_x, aa_y):
+    """Output pixels of an anti-aliased frame with at least one sample whose
+    primary hit lies within EDGE_EPS of a triangle edge (FP64 barycentrics),
+    on the oracle's supersampled camera rays: where a sample may legitimately
+    hit a different triangle than the reference's."""
+    fine = oracle.supersampled(frame, aa_x, aa_y)
+    o, d = oracle.camera_rays(fine["camera"])
+    ids, t, _, _ = oracle.OracleScene(scene).closest(o, d)
+    near = edge_distance(scene["verts"], scene["tris"], ids, o, d) < EDGE_EPS
+    H, W = frame["camera"]["yres"], frame["camera"]["xres"]
+    near = near.reshape(H * aa_y, W * aa_x)
+    out = np.zeros((H, W), bool)
+    for a_x in range(aa_x):
+        for a_y in range(aa_y):
+            out |= near[a_y::aa_y, a_x::aa_x][:H, :W]
+    return out

@@ -584,3 +584,47 @@ def test_refit_equals_fresh_upload(rtlib, builder):
     raw.close()
     sc.close()
     c.close()
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+@pytest.mark.parametrize("aa", [(2, 2), (3, 2)], ids=["aa22", "aa32"])
+def test_anti_aliasing_vs_reference_fixture(rtlib, ctx, oracle, golden, key, aa):
+    """rt_render_aa against the reference's own anti-aliased frames (camera
+    x_a_res / y_a_res + clip_image_to_rgb): equal on every output pixel none
+    of whose samples hits near a triangle edge."""
+    from parity import aa_edge_pixels
+    g = golden
+    frame = json.loads(bytes(g[f"{key}_frame"]).decode())
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"]}
+    sc = rtlib.Scene(ctx, scene)
+    r = sc.render_aa(frame, *aa)
+    st = r["stats"]
+    W, H = frame["camera"]["xres"], frame["camera"]["yres"]
+    assert st.primary_rays == W * H * aa[0] * aa[1]
+    ref = g[f"{key}_aa{aa[0]}{aa[1]}_rgb"]
+    edge = aa_edge_pixels(oracle, scene, frame, *aa)
+    assert np.array_equal(r["rgb"][~edge], ref[~edge])
+    sc.close()
+
+
+@pytest.mark.parametrize("bright", [False, True], ids=["fast_pow", "exact_pow"])
+def test_anti_aliasing_vs_oracle(rtlib, ctx, oracle, bright):
+    """4x4 anti-aliasing with several lights, in both specular-power modes:
+    the GPU frame equals the restatement's (supersampled float image,
+    binary32 downsample) away from edge samples; bad factors are refused."""
+    from parity import aa_edge_pixels
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=12, res=96)
+    f = dict(frame)
+    f["lights"] = [scenes.point_light((3.0, 5.0, 3.0), rgb=(300.0, 280.0, 260.0) if bright else (255.0, 240.0, 230.0)),
+                   scenes.directional_light((0.3, -1.0, -0.4), rgb=(90.0, 100.0, 120.0))]
+    sc = rtlib.Scene(ctx, scene)
+    got = sc.render_aa(f, 4, 4)["rgb"]
+    want = oracle.render_aa(oracle.OracleScene(scene), f, 4, 4)
+    edge = aa_edge_pixels(oracle, scene, f, 4, 4)
+    assert edge.mean() < 0.05
+    assert np.array_equal(got[~edge], want[~edge])
+    for bad in ((0, 1), (1, 17)):
+        with pytest.raises(rtlib.RtError):
+            sc.render_aa(f, *bad)
+    sc.close()

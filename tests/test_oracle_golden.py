@@ -133,3 +133,22 @@ def test_ao_rays_hemisphere(oracle):
     n = np.array([0, 0, 1], np.float32)
     cos = np.concatenate([oracle.ao_rays(np.zeros(3, np.float32), n, i, 64, 9)[1][:, 2] for i in range(200)])
     assert abs(cos.mean() - 2.0 / 3.0) < 0.01
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+@pytest.mark.parametrize("aa", [(2, 2), (3, 2)], ids=["aa22", "aa32"])
+def test_oracle_anti_aliasing_matches_reference(oracle, golden, key, aa):
+    """camera anti-aliasing (x_a_res / y_a_res) + clip_image_to_rgb's
+    downsample: the restatement's frame equals the reference's on every
+    output pixel none of whose samples hits near a triangle edge."""
+    from parity import aa_edge_pixels
+    g = golden
+    frame = frame_of(g, key)
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"], "flags": None}
+    ref = g[f"{key}_aa{aa[0]}{aa[1]}_rgb"]
+    got = oracle.render_aa(oracle.OracleScene(scene), frame, *aa)
+    edge = aa_edge_pixels(oracle, scene, frame, *aa)
+    assert edge.mean() < 0.02
+    assert np.array_equal(got[~edge], ref[~edge])
+    within1, exact, _ = pixel_agreement(got, ref)
+    assert exact >= 0.99
