@@ -92,10 +92,16 @@ typedef struct rt_light {
 
 /* Coloured Phong material (materials/coloured_mapper_shader.h): ka, kd, ks in
  * 0..255, ns the specular exponent.  With per-vertex attributes uploaded, kd
- * is modulated by the barycentric attribute (a per-vertex colour in 0..1). */
+ * is modulated by the barycentric attribute (a per-vertex colour in 0..1).
+ * rf: mirror reflectivity (the shader's rf, 0 = none): rt_render adds rf
+ * times the colour of the mirror ray (ray::reflect, ray.cc:118-135),
+ * recursively while the ray's power (product of rf) exceeds 0.1
+ * (MIN_REFLECTIVE_POWER, common.h:31); at most 63 bounces. */
+#define RT_MAX_BOUNCES 63
 typedef struct rt_material {
     float ka[3], kd[3], ks[3];
     float ns;
+    float rf;
 } rt_material;
 
 /* Triangle flag bits (triangle.h:40, bvh_node.h:176): shadow and AO rays

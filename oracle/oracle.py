@@ -33,7 +33,8 @@ class Light(C.Structure):
 
 
 class Material(C.Structure):
-    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float)]
+    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
+                ("rf", C.c_float)]
 
 
 def make_camera(d):
@@ -59,6 +60,7 @@ def make_material(d):
     m = Material()
     m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
     m.ns = d["ns"]
+    m.rf = d.get("rf", 0.0)
     return m
 
 

@@ -73,7 +73,7 @@ void *rref_scene_create(const float *verts, int32_t nverts, const int32_t *tris,
     const texture_mapper *kd_map = vattr ? new vertex_colour_mapper() : nullptr;
     s->opaque.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
                                                ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
-                                               ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.0f, 1.0f, 0.0f,
+                                               ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.0f, 1.0f, m->rf,
                                                0.0f, 0.0f, nullptr, kd_map));
     s->transparent.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
                                                     ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),

@@ -600,71 +600,101 @@ static inline v3 cur_kd(const ro_scene *s, const ro_material *m, v3 vt)
 /* camera::clip_image_to_rgb (camera.h:312-314): clamp then truncate. */
 static inline uint8_t clip8(float v) { return (uint8_t)smin(255.0f, smax(0.0f, v / 1.0f)); }
 
-static void render_pixel(render_job *J, const cam_state *cs, int32_t x, int32_t y)
+/* MIN_REFLECTIVE_POWER (common/common.h:31), a double literal: the float
+ * ray power is compared after promotion to double. */
+#define RO_MIN_REFLECTIVE_POWER 0.1
+
+/* The colour of one ray (ray_trace_engine::ray_trace, raytracer.cc:20-87):
+ * closest hit; hit refinement; one shadow ray per light; coloured Phong
+ * (coloured_mapper_shader::shade, coloured_mapper_shader.cc:76-112); then,
+ * for a reflective material, the mirror ray of ray::reflect (ray.cc:118-135:
+ * power = magn * rf, traced while power > MIN_REFLECTIVE_POWER, direction
+ * dir - n * (2 * dir.n), from the offset start point) whose colour, averaged
+ * over its one ray, is added times rf (combind_secondary_rays,
+ * coloured_mapper_shader.cc:117-122).  A miss is the background
+ * (camera::shade, camera.h:236-239).  first: the camera ray (writes the
+ * occlusion / AO outputs).  Returns the hit triangle or -1. */
+static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int first, size_t pix, v3 *out)
 {
     const ro_scene *s = J->s;
     const ro_material *m = J->mat;
+    ro_hit h;
+    const int32_t id = closest(s, r, &h);
+    J->rays += 1;
+    if (!(h.d < RO_MAX_DIST)) {
+        *out = ld3(J->cam->background);
+        if (first && J->occl) J->occl[pix] = 0;
+        if (first && J->ao_count) J->ao_count[pix] = 0;
+        return id;
+    }
+    v3 dst, sn, geo, vt;
+    hit_setup(s, r, id, &h, &dst, &sn, &geo, &vt);
+    const v3 start = offset_start(dst, geo);
+    const v3 kd = cur_kd(s, m, vt);
+    const v3 ks = ld3(m->ks);
+    v3 c = mk(0.0f, 0.0f, 0.0f);
+    if (J->ao_n > 0) {
+        /* AO mode: pixel = ka + kd * unoccluded fraction */
+        float dirs[3 * 64], ogns[3 * 64];
+        const float hp[3] = {dst.x, dst.y, dst.z}, gn[3] = {geo.x, geo.y, geo.z};
+        ro_ao_rays(hp, gn, (uint32_t)pix, J->ao_n, J->ao_seed, ogns, dirs);
+        int32_t made_it = 0;
+        for (int32_t k = 0; k < J->ao_n; ++k) {
+            ro_ray ar = {ld3(ogns + 3 * k), ld3(dirs + 3 * k)};
+            if (!nearer(s, &ar, J->ao_dist)) ++made_it;
+        }
+        J->rays += J->ao_n;
+        const float frac = (float)made_it / (float)J->ao_n;
+        c = vadd(vmul(kd, frac), ld3(m->ka));
+        if (J->ao_count) J->ao_count[pix] = made_it;
+        *out = c;
+        return id;
+    }
+    for (int32_t l = 0; l < J->nlights; ++l) {
+        const ro_light *L = &J->lights[l];
+        ro_ray sr;
+        float len;
+        shadow_ray(L, start, &sr, &len);
+        const int occ = nearer(s, &sr, len);
+        J->rays += 1;
+        if (first && J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
+        const float lmagn = occ ? 0.0f : 1.0f;   /* made_it / nr_pending_shadows */
+        const float shade = vdot(sr.d, sn);
+        if (shade < 0.0f) continue;
+        const v3 ref = vsub(sr.d, vmul(sn, 2.0f * shade));
+        const float rdr = vdot(r->d, ref);
+        v3 sc = mk(shade * kd.x, shade * kd.y, shade * kd.z);
+        if (rdr > 0.0f) {
+            const float p = (float)pow((double)rdr, (double)m->ns);
+            sc = mk(sc.x + p * ks.x, sc.y + p * ks.y, sc.z + p * ks.z);
+        }
+        /* light::get_light_intensity (light.h:44-59) */
+        const float dist = len * L->d;
+        const float d_scale = (dist * dist) + 1.0f;
+        const v3 I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale,
+                        (L->rgb[2] / 255.0f) / d_scale);
+        c = mk(c.x + I.x * (sc.x * lmagn), c.y + I.y * (sc.y * lmagn), c.z + I.z * (sc.z * lmagn));
+    }
+    c = vadd(c, ld3(m->ka));
+    const float refl_power = magn * m->rf;
+    if ((double)refl_power > RO_MIN_REFLECTIVE_POWER) {
+        const float rdn = 2.0f * vdot(r->d, sn);
+        const ro_ray rr = {start, vsub(r->d, vmul(sn, rdn))};
+        v3 cr;
+        trace_colour(J, &rr, refl_power, 0, pix, &cr);
+        const v3 avg = vdivs(vadd(mk(0.0f, 0.0f, 0.0f), cr), 1.0f);
+        c = vadd(c, vmul(avg, m->rf));
+    }
+    *out = c;
+    return id;
+}
+
+static void render_pixel(render_job *J, const cam_state *cs, int32_t x, int32_t y)
+{
     const size_t pix = (size_t)x + (size_t)y * (size_t)J->cam->xres;
     const ro_ray r = cam_ray(cs, x, y);
-    ro_hit h;
-    const int32_t id = closest(s, &r, &h);
-    J->rays += 1;
     v3 c;
-    if (h.d < RO_MAX_DIST) {
-        v3 dst, sn, geo, vt;
-        hit_setup(s, &r, id, &h, &dst, &sn, &geo, &vt);
-        const v3 start = offset_start(dst, geo);
-        const v3 kd = cur_kd(s, m, vt);
-        const v3 ks = ld3(m->ks);
-        c = mk(0.0f, 0.0f, 0.0f);
-        if (J->ao_n > 0) {
-            /* AO mode: pixel = ka + kd * unoccluded fraction */
-            float dirs[3 * 64], ogns[3 * 64];
-            const float hp[3] = {dst.x, dst.y, dst.z}, gn[3] = {geo.x, geo.y, geo.z};
-            ro_ao_rays(hp, gn, (uint32_t)pix, J->ao_n, J->ao_seed, ogns, dirs);
-            int32_t made_it = 0;
-            for (int32_t k = 0; k < J->ao_n; ++k) {
-                ro_ray ar = {ld3(ogns + 3 * k), ld3(dirs + 3 * k)};
-                if (!nearer(s, &ar, J->ao_dist)) ++made_it;
-            }
-            J->rays += J->ao_n;
-            const float frac = (float)made_it / (float)J->ao_n;
-            c = vadd(vmul(kd, frac), ld3(m->ka));
-            if (J->ao_count) J->ao_count[pix] = made_it;
-        } else {
-            for (int32_t l = 0; l < J->nlights; ++l) {
-                const ro_light *L = &J->lights[l];
-                ro_ray sr;
-                float len;
-                shadow_ray(L, start, &sr, &len);
-                const int occ = nearer(s, &sr, len);
-                J->rays += 1;
-                if (J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
-                const float magn = occ ? 0.0f : 1.0f;   /* made_it / nr_pending_shadows */
-                /* coloured_mapper_shader::shade (coloured_mapper_shader.cc:76-109) */
-                const float shade = vdot(sr.d, sn);
-                if (shade < 0.0f) continue;
-                const v3 ref = vsub(sr.d, vmul(sn, 2.0f * shade));
-                const float rdr = vdot(r.d, ref);
-                v3 sc = mk(shade * kd.x, shade * kd.y, shade * kd.z);
-                if (rdr > 0.0f) {
-                    const float p = (float)pow((double)rdr, (double)m->ns);
-                    sc = mk(sc.x + p * ks.x, sc.y + p * ks.y, sc.z + p * ks.z);
-                }
-                /* light::get_light_intensity (light.h:44-59) */
-                const float dist = len * L->d;
-                const float d_scale = (dist * dist) + 1.0f;
-                const v3 I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale,
-                                (L->rgb[2] / 255.0f) / d_scale);
-                c = mk(c.x + I.x * (sc.x * magn), c.y + I.y * (sc.y * magn), c.z + I.z * (sc.z * magn));
-            }
-            c = vadd(c, ld3(m->ka));
-        }
-    } else {
-        c = ld3(J->cam->background);     /* camera::shade (camera.h:236-239) */
-        if (J->occl) J->occl[pix] = 0;
-        if (J->ao_count) J->ao_count[pix] = 0;
-    }
+    const int32_t id = trace_colour(J, &r, 1.0f, 1, pix, &c);
     if (J->hit_id) J->hit_id[pix] = id;
     if (J->fimg) { J->fimg[3 * pix] = c.x; J->fimg[3 * pix + 1] = c.y; J->fimg[3 * pix + 2] = c.z; }
     J->rgb[3 * pix] = clip8(c.x);

@@ -57,6 +57,7 @@ typedef struct ro_light {
 typedef struct ro_material {
     float ka[3], kd[3], ks[3];
     float ns;
+    float rf;     /* mirror reflectivity, coloured_mapper_shader's rf (0: none) */
 } ro_material;
 
 typedef struct ro_scene ro_scene;

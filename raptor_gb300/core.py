@@ -65,7 +65,8 @@ class RtLight(C.Structure):
 
 
 class RtMaterial(C.Structure):
-    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float)]
+    _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
+                ("rf", C.c_float)]
 
 
 class RtRenderStats(C.Structure):
@@ -201,6 +202,7 @@ def make_material(d) -> RtMaterial:
     m = RtMaterial()
     m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
     m.ns = d["ns"]
+    m.rf = d.get("rf", 0.0)
     return m
 
 

@@ -139,6 +139,7 @@ MaterialView make_material_view(const rt_material &m)
     v.kd = make_float3(m.kd[0], m.kd[1], m.kd[2]);
     v.ks = make_float3(m.ks[0], m.ks[1], m.ks[2]);
     v.ns = m.ns;
+    v.rf = m.rf;
     return v;
 }
 
@@ -250,6 +251,7 @@ rt_status rt_ctx_destroy(rt_context *ctx)
     ctx->stage_a.release();
     ctx->stage_b.release();
     ctx->stage_c.release();
+    ctx->redo.release();
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->h_scratch) cudaFreeHost(ctx->h_scratch);
@@ -561,6 +563,24 @@ rt_status rt_trace_any(rt_scene *s, const rt_ray *rays, int32_t n, uint8_t *occl
     return trace_common<true>(s, rays, n, occluded, "rt_trace_any");
 }
 
+// Mirror reflectivity: 0 (none), or a value whose chain of ray powers
+// (1, rf, rf*rf, ... in binary32) drops to 0.1 or below within
+// RT_MAX_BOUNCES reflections.  Entry points without reflections take 0 only.
+static rt_status check_reflectivity(float rf, const char *who, bool supported = true)
+{
+    if (rf == 0.0f) return RT_OK;
+    std::string w(who);
+    if (!supported) return fail(RT_ERR_INVALID_ARG, w + ": reflective materials (rf > 0) are rendered by rt_render");
+    if (!(rf > 0.0f) || !(rf < 1.0f)) return fail(RT_ERR_INVALID_ARG, w + ": reflectivity must be 0 or in (0, 1)");
+    float magn = 1.0f;
+    for (int k = 0; k <= RT_MAX_BOUNCES; ++k) {
+        const float power = magn * rf;
+        if (!((double)power > 0.1)) return RT_OK;
+        magn = power;
+    }
+    return fail(RT_ERR_INVALID_ARG, w + ": reflectivity needs more than RT_MAX_BOUNCES mirror bounces");
+}
+
 static rt_status check_camera(const rt_camera *cam)
 {
     if (!cam) return fail(RT_ERR_INVALID_ARG, "NULL camera");
@@ -634,6 +654,8 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     if (st != RT_OK) return st;
     if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
         return fail(RT_ERR_INVALID_ARG, "rt_render: light count out of range");
+    st = check_reflectivity(material->rf, "rt_render");
+    if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render: hierarchy not built");
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);
@@ -647,7 +669,10 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    if (ctx->render_kernel == RT_KERNEL_WAVE)
+    if (material->rf > 0.0f)
+        launch_render_reflect(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb,
+                              o.ids, ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    else if (ctx->render_kernel == RT_KERNEL_WAVE)
         launch_render_wave(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
                            ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
     else
@@ -673,6 +698,8 @@ rt_status rt_render_aa(rt_scene *s, const rt_camera *camera, int32_t aa_x, int32
     if (st != RT_OK) return st;
     if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
         return fail(RT_ERR_INVALID_ARG, "rt_render_aa: light count out of range");
+    st = check_reflectivity(material->rf, "rt_render_aa", false);
+    if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_aa: hierarchy not built");
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);
@@ -686,9 +713,10 @@ rt_status rt_render_aa(rt_scene *s, const rt_camera *camera, int32_t aa_x, int32
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    RT_CUDA(ctx->redo.reserve(npix * sizeof(int32_t)), "redo queue allocation");
     launch_render_aa(scene_view(s), make_camera_view(fine), ls, make_material_view(*material), aa_x, aa_y,
-                     camera->xres, camera->yres, o.rgb, ctx->d_counters, ctx->sm_count, ctx->stream,
-                     ctx->count_fetches);
+                     camera->xres, camera->yres, o.rgb, (int32_t *)ctx->redo.ptr, ctx->d_counters, ctx->sm_count,
+                     ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, stats);
@@ -703,6 +731,8 @@ rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *
     if (st != RT_OK) return st;
     if (samples < 1 || samples > 64) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: samples must be 1..64");
     if (!(ao_dist > 0.0f)) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: ao_dist must be positive");
+    st = check_reflectivity(material->rf, "rt_render_ao", false);
+    if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_ao: hierarchy not built");
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);

@@ -38,6 +38,7 @@ struct rt_context {
     int32_t *h_scratch = nullptr;          // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rtc::DevBuf stage_a, stage_b, stage_c;
+    rtc::DevBuf redo;                      // pixels queued for an exact second pass
     bool count_fetches = false;
     int render_kernel = RT_KERNEL_PIXEL;
     int isect = RT_ISECT_REFERENCE;

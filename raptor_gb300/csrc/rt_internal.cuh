@@ -90,6 +90,7 @@ struct LightView {
 struct MaterialView {
     float3 ka, kd, ks;
     float ns;
+    float rf;    // mirror reflectivity (0: none)
 };
 
 // -------------------------------------------------- IEEE-exact helpers

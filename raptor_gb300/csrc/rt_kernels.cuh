@@ -27,6 +27,7 @@ struct Counters {
     unsigned long long secondary;    // shadow / AO rays traced
     unsigned long long nodes;        // wide nodes fetched (counting kernels only)
     unsigned long long tris;         // triangles tested (counting kernels only)
+    int redo;                        // pixels queued for an exact second pass
 };
 
 struct LightSet {
@@ -46,9 +47,12 @@ void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_
                       cudaStream_t st);
 void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                    uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+void launch_render_reflect(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
+                           uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st,
+                           bool count = false);
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
-                      int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, Counters *ctr,
-                      int sm_count, cudaStream_t st, bool count = false);
+                      int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, int32_t *redo,
+                      Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
 void launch_render_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat, int32_t samples,
                       float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
                       int sm_count, cudaStream_t st, bool count = false);

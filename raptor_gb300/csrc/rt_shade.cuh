@@ -98,6 +98,74 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
     return out;
 }
 
+// Primary ray and its chain of mirror reflections (reflective material,
+// rf > 0): at every hit the coloured Phong of shade_pixel_lights with the
+// exact specular power, then, while the ray's power magn * rf exceeds 0.1
+// (compared in double, as the reference's MIN_REFLECTIVE_POWER literal), the
+// mirror ray dir - n * (2 dir.n) from the offset start point (ray::reflect,
+// ray.cc:118-135).  The colours combine from the deepest ray outwards,
+// c_k + c_(k+1) * rf (combind_secondary_rays, coloured_mapper_shader.cc:
+// 117-122); a ray that misses is the background.  `chain` holds up to
+// RT_MAX_BOUNCES + 1 colours.
+template <bool COUNT>
+__device__ __forceinline__ PixelOut shade_pixel_reflect(const SceneView &sc, const CameraView &cam, const LightView *lights,
+                                                        int nl, const MaterialView &mat, int x, int y, float3 *chain,
+                                                        uint32_t &status, FetchCount *fc)
+{
+    PixelOut out;
+    out.secondary = 0;
+    out.ao_made = 0;
+    out.hit = false;
+    out.id = -1;
+    RayState r = camera_ray(cam, x, y);
+    float magn = 1.0f;
+    int last = 0;
+    for (int k = 0;; ++k) {
+        HitRecord h;
+        bool occ;
+        status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
+        if (k > 0) ++out.secondary;
+        if (!(h.t < FLT_MAX)) {
+            chain[k] = cam.background;
+            last = k;
+            break;
+        }
+        if (k == 0) {
+            out.hit = true;
+            out.id = h.id - sc.tri_base;
+        }
+        const SurfacePoint sp = surface_at(sc, r, h);
+        const float3 start = offset_start(sp.dst, sp.geo);
+        const float3 kd = material_kd(mat, sp);
+        float3 c = make_float3(0.f, 0.f, 0.f);
+        for (int l = 0; l < nl; ++l) {
+            float3 ldir;
+            float len;
+            shadow_ray(lights[l], start, ldir, len);
+            HitRecord sh;
+            bool blocked;
+            status |= traverse<true, COUNT>(sc, start, ldir, len, sh, blocked, fc);
+            ++out.secondary;
+            phong_add<true>(lights[l], mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
+        }
+        chain[k] = xadd3(c, mat.ka);
+        const float power = xmul(magn, mat.rf);
+        if (!((double)power > 0.1) || k == RT_MAX_BOUNCES) {
+            if ((double)power > 0.1) status |= kStatusStepLimit;   // deeper than the host allowed
+            last = k;
+            break;
+        }
+        const float rdn = xmul(2.0f, xdot(r.d, sp.sn));
+        r.o = start;
+        r.d = xsub3(r.d, xmul3(sp.sn, rdn));
+        magn = power;
+    }
+    float3 acc = chain[last];
+    for (int k = last - 1; k >= 0; --k) acc = xadd3(chain[k], xmul3(acc, mat.rf));
+    out.c = acc;
+    return out;
+}
+
 // Primary ray, closest hit, `samples` cosine-weighted AO rays within ao_dist.
 template <bool COUNT>
 __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat,

@@ -130,14 +130,16 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
 // clip_image_to_rgb, camera.h:289-319): one output pixel per lane; its
 // aa_x * aa_y samples on the supersampled camera grid are shaded and summed
 // a_x outer, a_y inner, divided by their count, clamped and truncated.  With
-// the single-precision specular power, an average within the truncation
-// guard of an integer is recomputed from samples shaded with the exact
-// power.
+// the single-precision specular power, a pixel whose average lands within
+// the truncation guard of an integer is queued (redo) for k_render_aa_fix,
+// which recomputes it from samples shaded with the exact power in a compact
+// second pass, so that no warp waits on one lane's exact re-shade.
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_aa(SceneView sc, CameraView cam,
                                                              LightSet lights, MaterialView mat, int32_t aa_x,
                                                              int32_t aa_y, int32_t out_x, int32_t out_y,
-                                                             uint8_t *__restrict__ rgb, Counters *ctr)
+                                                             uint8_t *__restrict__ rgb, int32_t *__restrict__ redo,
+                                                             Counters *ctr)
 {
     int tiles_x;
     const int items = tiles_of<8>(out_x, out_y, tiles_x) * 32;
@@ -162,22 +164,84 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
                     hits += po.hit ? 1u : 0u;
                     secondary += po.secondary;
                 }
-            float3 avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+            const float3 avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+            const int32_t pix = x + y * out_x;
             if (lights.fast_pow && near_truncation(avg)) {
-                sum = make_float3(0.f, 0.f, 0.f);
-                for (int ax = 0; ax < aa_x; ++ax)
-                    for (int ay = 0; ay < aa_y; ++ay) {
-                        const PixelOut po = shade_pixel_lights<false>(sc, cam, lights.l, lights.n, mat, x * aa_x + ax,
-                                                                      y * aa_y + ay, status, nullptr, false);
-                        sum = xadd3(sum, po.c);
-                    }
-                avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+                const int slot = atomicAdd(&ctr->redo, 1);
+                if (slot < out_x * out_y) redo[slot] = pix;
+            } else {
+                store_rgb(rgb, (size_t)pix, avg);
             }
-            store_rgb(rgb, (size_t)x + (size_t)y * (size_t)out_x, avg);
         }
         warp_add(&ctr->primary, primary);
         warp_add(&ctr->hits, hits);
         warp_add(&ctr->secondary, secondary);
+    }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// The queued pixels of k_render_aa, one per thread, every sample shaded
+// with the exact specular power.
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_aa_fix(SceneView sc, CameraView cam,
+                                                                 LightSet lights, MaterialView mat, int32_t aa_x,
+                                                                 int32_t aa_y, int32_t out_x,
+                                                                 uint8_t *__restrict__ rgb,
+                                                                 const int32_t *__restrict__ redo, Counters *ctr)
+{
+    const int32_t n = min(ctr->redo, out_x * (cam.yres / aa_y));
+    const float nsamples = (float)(aa_x * aa_y);
+    uint32_t status = 0;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int32_t pix = redo[i];
+        const int x = pix % out_x, y = pix / out_x;
+        float3 sum = make_float3(0.f, 0.f, 0.f);
+        for (int ax = 0; ax < aa_x; ++ax)
+            for (int ay = 0; ay < aa_y; ++ay) {
+                const PixelOut po = shade_pixel_lights<false>(sc, cam, lights.l, lights.n, mat, x * aa_x + ax,
+                                                              y * aa_y + ay, status, nullptr, false);
+                sum = xadd3(sum, po.c);
+            }
+        store_rgb(rgb, (size_t)pix,
+                  make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples)));
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// Frame of a reflective material: one pixel per lane, the mirror-ray chain
+// of shade_pixel_reflect (its colours in a per-thread chain array).
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_reflect(SceneView sc, CameraView cam,
+                                                                  LightSet lights, MaterialView mat,
+                                                                  uint8_t *__restrict__ rgb,
+                                                                  int32_t *__restrict__ ids, Counters *ctr)
+{
+    float3 chain[RT_MAX_BOUNCES + 1];
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
+    uint32_t status = 0;
+    FetchCount fc;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items) break;
+        int x, y;
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
+        const bool live = (x < cam.xres) && (y < cam.yres);
+        PixelOut po;
+        po.hit = false;
+        po.secondary = 0;
+        if (live) {
+            po = shade_pixel_reflect<COUNT>(sc, cam, lights.l, lights.n, mat, x, y, chain, status, &fc);
+            const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+            store_rgb(rgb, pix, po.c);
+            if (ids) ids[pix] = po.id;
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
     }
     if (COUNT) {
         atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
@@ -224,15 +288,29 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
         k_render<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
 }
 
+void launch_render_reflect(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
+                           uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
+{
+    static const int grid = grid_of(k_render_reflect<false>, sm_count);
+    if (count)
+        k_render_reflect<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+    else
+        k_render_reflect<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+}
+
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
-                      int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, Counters *ctr,
-                      int sm_count, cudaStream_t st, bool count)
+                      int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, int32_t *redo,
+                      Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
     static const int grid = grid_of(k_render_aa<false>, sm_count);
     if (count)
-        k_render_aa<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, ctr);
+        k_render_aa<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, redo,
+                                                           ctr);
     else
-        k_render_aa<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, ctr);
+        k_render_aa<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, redo,
+                                                            ctr);
+    if (lights.fast_pow)
+        k_render_aa_fix<<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, rgb, redo, ctr);
 }
 
 void launch_render_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat, int32_t samples,

@@ -193,7 +193,8 @@ struct gpu_light_args
 // nullable.
 inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_light_args> &lights,
                            const gpu_camera_args &cam_args, camera &c, const ext_colour_t &ka, const ext_colour_t &kd,
-                           const ext_colour_t &ks, const float ns, const float *vertex_colours = nullptr)
+                           const ext_colour_t &ks, const float ns, const float *vertex_colours = nullptr,
+                           const float rf = 0.0f)
 {
     rt_camera cam;
     const point_t<> *ax[4] = { &cam_args.position, &cam_args.x_axis, &cam_args.y_axis, &cam_args.z_axis };
@@ -217,6 +218,7 @@ inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_lig
     m.kd[0] = kd.r; m.kd[1] = kd.g; m.kd[2] = kd.b;
     m.ks[0] = ks.r; m.ks[1] = ks.g; m.ks[2] = ks.b;
     m.ns = ns;
+    m.rf = rf;
     rt_scene *s = accel->scene();
     if (vertex_colours)
     {

@@ -13,7 +13,8 @@ It writes
   ref_small.npz     inputs and outputs of the reference's own bvh,
                     ray_tracer() and clip_image_to_rgb() (compiled by
                     oracle/refbuild/Makefile) on small seeded scenes, also
-                    with the camera's anti-aliasing factors (2x2, 3x2)
+                    with the camera's anti-aliasing factors (2x2, 3x2) and
+                    with a reflective material
 The tests compare the C restatement (oracle/rtoracle.c) and the CUDA core
 against these files; nothing at test time reads the reference tree.
 """
@@ -93,6 +94,7 @@ def parse_morton_tests(path):
 
 
 AA_FACTORS = ((2, 2), (3, 2))
+REFLECTIVITY = {"ico": 0.5, "terrain": 0.35}
 
 
 def small_scenes():
@@ -153,6 +155,11 @@ def main():
         # anti-aliased frames: the camera's x_a_res / y_a_res factors
         for ax, ay in AA_FACTORS:
             arrays[f"{key}_aa{ax}{ay}_rgb"] = rs.render(f, aa=(ax, ay))["rgb"]
+        # a reflective material: mirror rays while their power exceeds 0.1
+        mat = dict(f["material"], rf=REFLECTIVITY[key])
+        fr = dict(f, material=mat)
+        arrays[f"{key}_refl_rf"] = np.array([REFLECTIVITY[key]], np.float32)
+        arrays[f"{key}_refl_rgb"] = O.RefScene(s, mat).render(fr)["rgb"]
         arrays[f"{key}_frame"] = np.frombuffer(json.dumps(f).encode(), dtype=np.uint8)
     s, o, d, tmax = soup()
     rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))

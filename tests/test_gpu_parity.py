@@ -628,3 +628,46 @@ def test_anti_aliasing_vs_oracle(rtlib, ctx, oracle, bright):
         with pytest.raises(rtlib.RtError):
             sc.render_aa(f, *bad)
     sc.close()
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+def test_reflections_vs_reference_and_oracle(rtlib, ctx, oracle, golden, key):
+    """rt_render with a reflective material (mirror chains while the ray
+    power exceeds 0.1): the frame agrees with the reference's own frame and
+    with the restatement's on all but edge pixels (primary or mirror rays
+    grazing a triangle edge)."""
+    g = golden
+    frame = json.loads(bytes(g[f"{key}_frame"]).decode())
+    frame["material"] = dict(frame["material"], rf=float(g[f"{key}_refl_rf"][0]))
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"]}
+    sc = rtlib.Scene(ctx, scene)
+    r = sc.render(frame, want_ids=True)
+    want = oracle.OracleScene(scene).render(frame)["rgb"]
+    within1, exact, _ = pixel_agreement(r["rgb"], want)
+    assert exact >= 0.998, exact
+    within1, exact, _ = pixel_agreement(r["rgb"], g[f"{key}_refl_rgb"])
+    assert exact >= 0.995, exact
+    assert r["stats"].secondary_rays > r["stats"].primary_hits     # shadow + mirror rays
+    sc.close()
+
+
+def test_reflectivity_limits(rtlib, ctx):
+    """rf >= 1 never decays and rf whose chain needs more than RT_MAX_BOUNCES
+    bounces are refused; the entry points without mirror rays refuse rf > 0."""
+    torch = pytest.importorskip("torch")
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=4, res=32)
+    sc = rtlib.Scene(ctx, scene)
+    for rf in (1.0, 0.97, -0.2):
+        f = dict(frame, material=dict(frame["material"], rf=rf))
+        with pytest.raises(rtlib.RtError):
+            sc.render(f)
+    f = dict(frame, material=dict(frame["material"], rf=0.96))   # 56 bounces: allowed
+    sc.render(f)
+    f = dict(frame, material=dict(frame["material"], rf=0.5))
+    with pytest.raises(rtlib.RtError):
+        sc.render_aa(f, 2, 2)
+    fao = dict(f, ao={"samples": 4, "dist": 1.0, "seed": 1})
+    with pytest.raises(rtlib.RtError):
+        sc.render(fao)
+    sc.close()

@@ -152,3 +152,27 @@ def test_oracle_anti_aliasing_matches_reference(oracle, golden, key, aa):
     assert np.array_equal(got[~edge], ref[~edge])
     within1, exact, _ = pixel_agreement(got, ref)
     assert exact >= 0.99
+
+
+@pytest.mark.parametrize("key", ["ico", "terrain"])
+def test_oracle_reflections_match_reference(oracle, golden, key):
+    """A reflective material (the shader's rf): mirror rays traced while
+    their power exceeds 0.1, colours added times rf.  The restatement's
+    frame equals the reference's on every pixel whose primary hit is not
+    near an edge."""
+    g = golden
+    frame = frame_of(g, key)
+    rf = float(g[f"{key}_refl_rf"][0])
+    frame["material"] = dict(frame["material"], rf=rf)
+    scene = {"verts": g[f"{key}_verts"], "tris": g[f"{key}_tris"], "vattr": g[f"{key}_vattr"], "flags": None}
+    og, dr = oracle.camera_rays(frame["camera"])
+    sc = oracle.OracleScene(scene)
+    ids, t, _, _ = sc.closest(og, dr)
+    _, excluded = compare_hits(scene["verts"], scene["tris"], og, dr, ids, t, g[f"{key}_id"], g[f"{key}_t"])
+    out = sc.render(frame)["rgb"]
+    ref = g[f"{key}_refl_rgb"]
+    keep = ~excluded.reshape(out.shape[:2])
+    within1, exact, _ = pixel_agreement(out[keep], ref[keep])
+    assert exact >= 0.998, exact
+    plain = sc.render(frame_of(g, key))["rgb"]
+    assert (np.abs(out.astype(int) - plain.astype(int)).max(-1) > 0).mean() > 0.1   # reflections visible
