@@ -359,6 +359,7 @@ def main():
         sc.close()
         wl = {}
         wl["icosphere-20k-512"] = workload_icosphere(ctx, stream, flush, max(5, args.steps))
+        wl["icosphere-20k-512-mirror"] = workload_icosphere_mirror(ctx, stream, flush, max(5, args.steps))
         wl["terrain-1M-1080p"] = workload_terrain_1m(ctx, stream, flush, max(5, args.steps // 2))
         wl["terrain-2M-1080p-aa2x2"] = workload_terrain_aa(ctx, stream, flush, max(3, args.steps // 4))
         wl["instances-4M-720p-ao16"] = workload_instances_ao(ctx, stream, flush, max(3, args.steps // 4))
@@ -423,6 +424,24 @@ def workload_terrain_aa(ctx, stream, flush, steps):
     rays = (st.primary_rays + st.secondary_rays) * steps
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080], "aa": [2, 2],
+            "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_icosphere_mirror(ctx, stream, flush, steps):
+    """The icosphere frame with a reflective material (rf 0.5: the camera
+    ray and up to three mirror bounces per pixel, each with its shadow ray)."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.icosphere_scene()
+    frame = dict(frame, material=dict(frame["material"], rf=0.5))
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((512, 512, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        sc.render(frame, rgb=rgb)
+    secs, st = time_frames(lambda: sc.render(frame, rgb=rgb)["stats"], steps, stream, flush)
+    rays = (st.primary_rays + st.secondary_rays) * steps
+    sc.close()
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512], "rf": 0.5,
             "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
 
 
