@@ -671,3 +671,50 @@ def test_reflectivity_limits(rtlib, ctx):
     with pytest.raises(rtlib.RtError):
         sc.render(fao)
     sc.close()
+
+
+def test_large_scene_33m_triangles(rtlib):
+    """A 4096^2 heightfield (33,554,432 triangles, 16x the headline scene):
+    both builders finish, place every triangle in one leaf slot, and give
+    the same closest hits, occlusion and frame; a refit keeps the hits of a
+    rebuild."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.terrain_scene(size_pow2=4096, xres=320, yres=180)
+    n = scene["tris"].shape[0]
+    assert n == 33554432
+    rng = np.random.default_rng(37)
+    v = scene["verts"]
+    lo, hi = v.min(0).astype(np.float64), v.max(0).astype(np.float64)
+    o = rng.uniform(lo, hi, size=(200000, 3))
+    o[:, 1] = hi[1] + 20.0
+    d = rng.normal(size=(200000, 3)) * 0.5 + np.array([0.0, -1.0, 0.0])
+    d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+    rays = rtlib.rays_array(o.astype(np.float32), d, tmax=np.float32(150.0))
+    res = []
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+        c = rtlib.Context(0)
+        c.set_option(rtlib.RT_OPT_BUILDER, b)
+        sc = rtlib.Scene(c, scene)
+        st = sc.stats()
+        assert sum(k * m for k, m in zip((1, 2, 3), st["leaf_tris"])) == n
+        assert st["internal_slots"] == st["nodes"] - 1
+        hits, occ = sc.closest(rays), sc.any(rays)
+        r = sc.render(frame, want_ids=True)
+        assert r["stats"].status == 0
+        res.append((hits, occ, r["rgb"], r["ids"]))
+        if b == rtlib.RT_BUILDER_PLOC:
+            moved = scene["verts"].copy()
+            moved[:, 1] += np.float32(1.5)
+            sc.refit_vertices(moved)
+            after_refit = sc.closest(rays)
+            sc.update_vertices(moved)
+            after_build = sc.closest(rays)
+            assert np.array_equal(after_refit["tri"], after_build["tri"])
+            assert np.array_equal(after_refit["t"], after_build["t"])
+        sc.close()
+        c.close()
+    (h0, a0, rgb0, id0), (h1, a1, rgb1, id1) = res
+    assert np.array_equal(h0["tri"], h1["tri"]) and np.array_equal(h0["t"], h1["t"])
+    assert np.array_equal(a0, a1)
+    assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
+    assert (h1["tri"] >= 0).mean() > 0.5
