@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-workloads", action="store_true", help="headline workload only")
     ap.add_argument("--size", type=int, default=1024, help="terrain cells per side (power of two)")
+    ap.add_argument("--only", default=None, choices=sorted(WORKLOADS),
+                    help="run one extra workload alone and print its JSON (for profiling)")
     return ap.parse_args()
 
 
@@ -253,10 +255,44 @@ def ncu_traffic():
     return total if seen == 2 else None
 
 
+# The extra workloads by name: (function, uses the L2 flush, steps from --steps).
+WORKLOADS = {
+    "icosphere-20k-512": ("workload_icosphere", True, lambda k: max(5, k)),
+    "icosphere-20k-512-mirror": ("workload_icosphere_mirror", True, lambda k: max(5, k)),
+    "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
+    "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
+    "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
+    "batched-64-scenes": ("workload_batched", False, lambda k: max(3, k // 4)),
+    "adjoint-50k-256": ("workload_adjoint", False, lambda k: max(5, k // 2)),
+}
+
+
+def run_one_workload(args):
+    """--only NAME: one extra workload on its own (rank 0, one GPU)."""
+    import torch
+    from raptor_gb300 import core
+    torch.cuda.set_device(0)
+    ctx = core.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    fn_name, flushed, steps = WORKLOADS[args.only]
+    fn = globals()[fn_name]
+    if flushed:
+        flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        out = fn(ctx, stream, flush, steps(args.steps))
+    else:
+        out = fn(ctx, stream, steps(args.steps))
+    print(json.dumps({"workload": args.only, **out}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_one_workload(args)
     import torch
     from raptor_gb300 import core
     rank, world = dist_init(args.gpus)
@@ -367,15 +403,14 @@ def main():
     if not args.no_workloads:
         sc.close()
         wl = {}
-        wl["icosphere-20k-512"] = workload_icosphere(ctx, stream, flush, max(5, args.steps))
-        wl["icosphere-20k-512-mirror"] = workload_icosphere_mirror(ctx, stream, flush, max(5, args.steps))
-        wl["terrain-1M-1080p"] = workload_terrain_1m(ctx, stream, flush, max(5, args.steps // 2))
-        wl["terrain-2M-1080p-aa2x2"] = workload_terrain_aa(ctx, stream, flush, max(3, args.steps // 4))
-        wl["instances-4M-720p-ao16"] = workload_instances_ao(ctx, stream, flush, max(3, args.steps // 4))
+        for name, (fn_name, flushed, steps) in WORKLOADS.items():
+            if flushed:
+                wl[name] = globals()[fn_name](ctx, stream, flush, steps(args.steps))
         del flush
         torch.cuda.empty_cache()
-        wl["batched-64-scenes"] = workload_batched(ctx, stream, max(3, args.steps // 4))
-        wl["adjoint-50k-256"] = workload_adjoint(ctx, stream, max(5, args.steps // 2))
+        for name, (fn_name, flushed, steps) in WORKLOADS.items():
+            if not flushed:
+                wl[name] = globals()[fn_name](ctx, stream, steps(args.steps))
         line["workloads"] = wl
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(scene, frame, args.cpu_seconds).items()
