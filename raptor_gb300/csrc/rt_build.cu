@@ -413,11 +413,21 @@ __global__ void k_ploc_segments(int32_t nseg, int32_t n, const int32_t *__restri
     nodes[s] = W;
 }
 
+// Nearest neighbours of a tile of kPlocTile clusters.  The merged-box
+// surface area is symmetric, so each pair is evaluated once: every row of the
+// tile and the kPlocRadius rows before it computes its distances to the
+// kPlocRadius clusters after it (dist, rows padded to an odd stride against
+// bank conflicts), and each cluster then scans its backward distances (from
+// the rows before it) and its forward ones in increasing neighbour order,
+// keeping the first smallest, exactly as a full two-sided scan would.
+constexpr int kPlocRow = kPlocRadius + 1;
+
 __global__ void __launch_bounds__(kPlocTile) k_ploc_nn(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
                                                       int32_t *__restrict__ nn, const int32_t *__restrict__ state,
                                                       int it)
 {
     __shared__ float4 slo[kPlocTile + 2 * kPlocRadius], shi[kPlocTile + 2 * kPlocRadius];
+    __shared__ float dist[(kPlocTile + kPlocRadius) * kPlocRow];
     const int par = it & 1;
     const int32_t count = state[kStCount + par];
     const int32_t b0 = blockIdx.x * kPlocTile;
@@ -432,26 +442,49 @@ __global__ void __launch_bounds__(kPlocTile) k_ploc_nn(const float4 *__restrict_
         }
     }
     __syncthreads();
+    const float inf = __int_as_float(0x7f800000);
+    if (!done && !forced) {
+        // forward distances of rows r = 0 .. kPlocTile + kPlocRadius - 1
+        // (cluster b0 - kPlocRadius + r) to the kPlocRadius clusters after it
+        for (int r = threadIdx.x; r < kPlocTile + kPlocRadius; r += kPlocTile) {
+            const int32_t g = b0 - kPlocRadius + r;
+            float *row = dist + r * kPlocRow;
+            if (g < 0 || g >= count) {
+                for (int k = 0; k < kPlocRadius; ++k) row[k] = inf;
+                continue;
+            }
+            const float4 a0 = slo[r], a1 = shi[r];
+            const int seg = __float_as_int(a0.w);
+#pragma unroll 4
+            for (int k = 1; k <= kPlocRadius; ++k) {
+                float d = inf;
+                if (g + k < count) {
+                    const float4 b0v = slo[r + k];
+                    if (__float_as_int(b0v.w) == seg) d = half_area(box_min(a0, b0v), box_max(a1, shi[r + k]));
+                }
+                row[k - 1] = d;
+            }
+        }
+    }
+    __syncthreads();
     const int32_t i = b0 + threadIdx.x;
     if (i >= count) return;
     int32_t best = -1;
     if (!done) {
         const int t = threadIdx.x + kPlocRadius;
-        const float4 a0 = slo[t], a1 = shi[t];
-        const int seg = __float_as_int(a0.w);
         if (forced) {
+            const int seg = __float_as_int(slo[t].w);
             const int32_t p = ((i - par) ^ 1) + par;
             if (i - par >= 0 && p >= 0 && p < count && __float_as_int(slo[t + (p - i)].w) == seg) best = p;
         } else {
-            float bd = __int_as_float(0x7f800000);
-#pragma unroll 4
-            for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
-                const int32_t j = i + o;
-                if (o == 0 || j < 0 || j >= count) continue;
-                const float4 b0v = slo[t + o];
-                if (__float_as_int(b0v.w) != seg) continue;
-                const float d = half_area(box_min(a0, b0v), box_max(a1, shi[t + o]));
-                if (d < bd) { bd = d; best = j; }
+            float bd = inf;
+            for (int k = kPlocRadius; k >= 1; --k) {   // neighbours i - k, nearest last
+                const float d = dist[(t - k) * kPlocRow + (k - 1)];
+                if (d < bd) { bd = d; best = i - k; }
+            }
+            for (int k = 1; k <= kPlocRadius; ++k) {   // neighbours i + k
+                const float d = dist[t * kPlocRow + (k - 1)];
+                if (d < bd) { bd = d; best = i + k; }
             }
         }
     }
