@@ -89,6 +89,12 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render(
     if (status) atomicOr(&ctr->status, status);
 }
 
+// RT_AO_SPREAD: spread each warp's AO rays over all its lanes (default), or
+// one pixel's rays per lane.
+#ifndef RT_AO_SPREAD
+#define RT_AO_SPREAD 1
+#endif
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_ao(SceneView sc, CameraView cam, MaterialView mat,
                                                              int32_t samples, float ao_dist, uint32_t seed,
@@ -105,6 +111,80 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
         int x, y;
         tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
         const bool live = (x < cam.xres) && (y < cam.yres);
+#if RT_AO_SPREAD
+        // primary ray per lane; then the warp's hits * samples AO rays are
+        // spread over all 32 lanes (a lane whose pixel missed takes rays of
+        // its neighbours), each ray's origin and basis fetched from the lane
+        // that owns its pixel, the unoccluded counts gathered per owner in
+        // shared memory.  Same rays, same counts as shade_pixel_ao.
+        __shared__ int made_s[kTraceThreads];
+        const int lane = threadIdx.x & 31;
+        const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+        bool hit = false;
+        int32_t id = -1;
+        float3 start = make_float3(0.f, 0.f, 0.f), kd = make_float3(0.f, 0.f, 0.f);
+        AOBasis ob;
+        ob.T = ob.B = ob.g = make_float3(0.f, 0.f, 0.f);
+        if (live) {
+            const RayState r = camera_ray(cam, x, y);
+            HitRecord h;
+            bool occ;
+            status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, &fc);
+            hit = h.t < FLT_MAX;
+            if (hit) {
+                id = h.id - sc.tri_base;
+                const SurfacePoint sp = surface_at(sc, r, h);
+                start = offset_start(sp.dst, sp.geo);
+                ob = ao_basis(sp.geo);
+                kd = material_kd(mat, sp);
+            }
+        }
+        made_s[threadIdx.x] = 0;
+        __syncwarp();
+        const uint32_t hitmask = __ballot_sync(0xffffffffu, hit);
+        const int total = __popc(hitmask) * samples;
+        for (int r0 = 0; r0 < total; r0 += 32) {
+            const int r = r0 + lane;
+            const bool active = r < total;
+            const int q = active ? r / samples : 0;
+            const int k = active ? r - q * samples : 0;
+            const int owner = active ? (int)__fns(hitmask, 0, q + 1) : lane;
+            const float3 o = make_float3(__shfl_sync(0xffffffffu, start.x, owner),
+                                         __shfl_sync(0xffffffffu, start.y, owner),
+                                         __shfl_sync(0xffffffffu, start.z, owner));
+            AOBasis b;
+            b.T = make_float3(__shfl_sync(0xffffffffu, ob.T.x, owner), __shfl_sync(0xffffffffu, ob.T.y, owner),
+                              __shfl_sync(0xffffffffu, ob.T.z, owner));
+            b.B = make_float3(__shfl_sync(0xffffffffu, ob.B.x, owner), __shfl_sync(0xffffffffu, ob.B.y, owner),
+                              __shfl_sync(0xffffffffu, ob.B.z, owner));
+            b.g = make_float3(__shfl_sync(0xffffffffu, ob.g.x, owner), __shfl_sync(0xffffffffu, ob.g.y, owner),
+                              __shfl_sync(0xffffffffu, ob.g.z, owner));
+            const uint32_t opix = (uint32_t)__shfl_sync(0xffffffffu, (int)pix, owner);
+            if (active) {
+                const float3 d = ao_direction(b, opix, (uint32_t)k, seed);
+                HitRecord ah;
+                bool blocked;
+                status |= traverse<true, COUNT>(sc, o, d, ao_dist, ah, blocked, &fc);
+                if (!blocked) atomicAdd(&made_s[(threadIdx.x & ~31) + owner], 1);
+            }
+        }
+        __syncwarp();
+        if (live) {
+            float3 c = cam.background;
+            int made = 0;
+            if (hit) {
+                made = made_s[threadIdx.x];
+                const float frac = xdiv((float)made, (float)samples);
+                c = xadd3(xmul3(kd, frac), mat.ka);
+            }
+            store_rgb(rgb, pix, c);
+            if (ids) ids[pix] = id;
+            if (ao_count) ao_count[pix] = made;
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, hit);
+        warp_add(&ctr->secondary, hit ? (uint32_t)samples : 0u);
+#else
         PixelOut po;
         po.hit = false;
         po.secondary = 0;
@@ -118,6 +198,7 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
         warp_count(&ctr->primary, live);
         warp_count(&ctr->hits, po.hit);
         warp_add(&ctr->secondary, po.secondary);
+#endif
     }
     if (COUNT) {
         atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
