@@ -123,7 +123,7 @@ class ClockSampler:
 class CpuBaseline:
     """The reference's CPU path on this host's cores.  The reference itself
     (oracle/_ref) builds only on x86-64 (its simd.h includes immintrin.h), so
-    on the Arm GPU host this is the oracle's C restatement (kind "port"),
+    on an Arm host this is the oracle's C restatement (kind "port"),
     which the tests pin to the reference's outputs.  The hierarchy is built
     once; each step renders a band of rows sized to `seconds` of work with
     all host threads."""

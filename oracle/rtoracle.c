@@ -1,8 +1,8 @@
 /*
  * rtoracle.c -- CPU restatement of RAPTor's ray-tracing hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA core, never part of the
- * product.  Compile with -ffp-contract=off (no FMA contraction) so the
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA core is compared against,
+ * never part of the product.  Compile with -ffp-contract=off (no FMA contraction) so the
  * results are the reference's IEEE binary32 results on any host.
  *
  * Reference paths below are relative to the RAPTor project root.

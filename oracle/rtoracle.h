@@ -1,7 +1,7 @@
 /*
  * rtoracle.h -- CPU restatement of RAPTor's ray-tracing hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the CUDA core is
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA core is
  * compared against: tests, the smoke check and the CPU-baseline leg of the
  * benchmark may load it; the product library never does.
  *
