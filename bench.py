@@ -259,6 +259,7 @@ def ncu_traffic():
 WORKLOADS = {
     "icosphere-20k-512": ("workload_icosphere", True, lambda k: max(5, k)),
     "icosphere-20k-512-mirror": ("workload_icosphere_mirror", True, lambda k: max(5, k)),
+    "glass-41k-512": ("workload_glass", True, lambda k: max(5, k)),
     "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
     "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
     "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
@@ -486,6 +487,25 @@ def workload_icosphere_mirror(ctx, stream, flush, steps):
     rays = (st.primary_rays + st.secondary_rays) * steps
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512], "rf": 0.5,
+            "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_glass(ctx, stream, flush, steps):
+    """Per-triangle materials with refraction: a glass sphere (tran 0.6, ri
+    1.5, rf 0.2) before an opaque sphere on a reflective ground (rf 0.3),
+    20,480 triangles per sphere, 512x512, two lights; each pixel's ray tree
+    of mirror and refracted rays, every hit with its shadow rays."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.glass_scene(freq=32, res=512)
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((512, 512, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        sc.render(frame, rgb=rgb)
+    secs, st = time_frames(lambda: sc.render(frame, rgb=rgb)["stats"], steps, stream, flush)
+    rays = (st.primary_rays + st.secondary_rays) * steps
+    sc.close()
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512],
             "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
 
 

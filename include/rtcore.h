@@ -96,13 +96,29 @@ typedef struct rt_light {
  * rf: mirror reflectivity (the shader's rf, 0 = none): rt_render adds rf
  * times the colour of the mirror ray (ray::reflect, ray.cc:118-135),
  * recursively while the ray's power (product of rf) exceeds 0.1
- * (MIN_REFLECTIVE_POWER, common.h:31); at most 63 bounces. */
-#define RT_MAX_BOUNCES 63
+ * (MIN_REFLECTIVE_POWER, common.h:31).  A pixel's ray tree (mirror and
+ * refracted rays) may be at most RT_MAX_BOUNCES levels below the camera ray
+ * and hold at most RT_MAX_TREE_RAYS rays, bounded from the largest rf and
+ * tran of the materials in use (worst-case powers rf^i * tran^j above 0.1);
+ * materials needing more are refused. */
+#define RT_MAX_BOUNCES 31
+#define RT_MAX_TREE_RAYS 1024
 typedef struct rt_material {
     float ka[3], kd[3], ks[3];
     float ns;
     float rf;
+    /* tran: transparency, the weight of the refracted colour (the shader's
+     * tran, 0 = opaque); ri: refractive index (inverted for a ray entering
+     * the front face).  rt_render adds tran times the colour of the ray of
+     * ray::refract (ray.cc:198-281) while its power exceeds 0.1; none beyond
+     * the critical angle.  Triangles of a refracting material should carry
+     * RT_TRI_TRANSPARENT, as the reference's transparent materials do, so
+     * that shadow rays pass them. */
+    float tran, ri;
+    uint32_t flags;   /* RT_MAT_NO_VERTEX_COLOUR: kd ignores the vertex attribute */
 } rt_material;
+#define RT_MAT_NO_VERTEX_COLOUR 1u
+#define RT_MAX_MATERIALS 16
 
 /* Triangle flag bits (triangle.h:40, bvh_node.h:176): shadow and AO rays
  * ignore light and transparent triangles. */
@@ -257,6 +273,27 @@ rt_status rt_trace_closest_noalloc(rt_scene *scene, const rt_ray *rays, int32_t 
 #define RT_MAX_LIGHTS 8
 rt_status rt_render(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
                     const rt_material *material, uint8_t *rgb_out, int32_t *hit_ids, rt_render_stats *stats);
+
+/* Per-triangle materials: mat_of_tri[i] (ntris entries, host or device
+ * memory) indexes the table given to rt_render_materials; NULL returns every
+ * triangle to material 0.  The reference keeps a material pointer per
+ * triangle (triangle.h:99-106). */
+rt_status rt_scene_set_materials(rt_scene *scene, const int32_t *mat_of_tri, int32_t ntris);
+
+/* rt_render with a table of up to RT_MAX_MATERIALS materials indexed per
+ * triangle: every hit is shaded with its triangle's material, and mirror
+ * (rf) and refracted (tran, ri) rays are traced as a tree, reflection
+ * before refraction, each colour added times its weight
+ * (ray_trace_engine::ray_trace, raytracer.cc:20-87, and
+ * combind_secondary_rays, coloured_mapper_shader.cc:117-130).  At most
+ * RT_MAX_BOUNCES levels and RT_MAX_TREE_RAYS rays per pixel (tables needing
+ * more are refused).  Without rt_scene_set_materials every triangle takes
+ * materials[0]; rt_render is the one-material case and ignores the
+ * per-triangle indices.  Every index set on the scene must be below
+ * nmaterials. */
+rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                              const rt_material *materials, int32_t nmaterials, uint8_t *rgb_out, int32_t *hit_ids,
+                              rt_render_stats *stats);
 
 /* Anti-aliased frame: aa_x * aa_y rays per output pixel on the supersampled
  * camera grid (xres * aa_x by yres * aa_y), each shaded as by rt_render, and

@@ -34,7 +34,7 @@ class Light(C.Structure):
 
 class Material(C.Structure):
     _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
-                ("rf", C.c_float)]
+                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
 
 
 def make_camera(d):
@@ -61,7 +61,17 @@ def make_material(d):
     m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
     m.ns = d["ns"]
     m.rf = d.get("rf", 0.0)
+    m.tran = d.get("tran", 0.0)
+    m.ri = d.get("ri", 1.0)
+    m.flags = d.get("flags", 0)
     return m
+
+
+def make_materials(ds):
+    arr = (Material * len(ds))()
+    for i, d in enumerate(ds):
+        arr[i] = make_material(d)
+    return arr
 
 
 def build(verbose: bool = False) -> None:
@@ -162,6 +172,12 @@ def oracle_lib():
         lib["ro_render"].restype = C.c_int64
         lib["ro_render"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32, C.POINTER(Material),
                                      C.c_int32, C.c_int32, C.c_int32, _U8, _I, _U8, _F]
+        lib["ro_render_mt"].restype = C.c_int64
+        lib["ro_render_mt"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
+                                        C.POINTER(Material), C.c_int32, C.c_int32, C.c_int32, C.c_int32, _U8, _I,
+                                        _U8, _F]
+        lib["ro_scene_set_materials"].restype = C.c_int32
+        lib["ro_scene_set_materials"].argtypes = [C.c_void_p, _I]
         lib["ro_render_ao"].restype = C.c_int64
         lib["ro_render_ao"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Material), C.c_int32, C.c_float,
                                         C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _U8, _I, _I]
@@ -182,6 +198,9 @@ def ref_lib():
         _declare(lib, "rref_")
         lib["rref_scene_create"].restype = C.c_void_p
         lib["rref_scene_create"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32, C.POINTER(Material)]
+        lib["rref_scene_create_mt"].restype = C.c_void_p
+        lib["rref_scene_create_mt"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32, C.POINTER(Material),
+                                                C.c_int32, _I]
         lib["rref_render"].restype = C.c_double
         lib["rref_render"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32, _U8]
         lib["rref_render_aa"].restype = C.c_double
@@ -213,6 +232,11 @@ class OracleScene(_SceneBase):
                                              _p(a, C.c_float), _p(f, C.c_uint32))
         if not self.h:
             raise ValueError("invalid scene")
+        if scene.get("mat_of_tri") is not None:
+            mt = np.ascontiguousarray(scene["mat_of_tri"], np.int32)
+            self._keep = self._keep + (mt,)
+            if self.lib["ro_scene_set_materials"](self.h, _p(mt, C.c_int32)) != 0:
+                raise MemoryError("oracle materials failed")
         self.build_seconds = self.lib["ro_scene_build"](self.h)
         if self.build_seconds < 0:
             raise MemoryError("oracle build failed")
@@ -237,9 +261,15 @@ class OracleScene(_SceneBase):
             out = {"rgb": rgb, "ids": ids, "ao_count": cnt, "rays": n}
         else:
             ls = make_lights(frame["lights"])
-            n = self.lib["ro_render"](self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), r0, r1, threads,
-                                      _p(rgb, C.c_uint8), _p(ids, C.c_int32), _p(occl, C.c_uint8),
-                                      _p(fimg, C.c_float))
+            table = make_materials(frame["materials"]) if frame.get("materials") else None
+            if table is not None:
+                n = self.lib["ro_render_mt"](self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table), r0, r1,
+                                             threads, _p(rgb, C.c_uint8), _p(ids, C.c_int32), _p(occl, C.c_uint8),
+                                             _p(fimg, C.c_float))
+            else:
+                n = self.lib["ro_render"](self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), r0, r1,
+                                          threads, _p(rgb, C.c_uint8), _p(ids, C.c_int32), _p(occl, C.c_uint8),
+                                          _p(fimg, C.c_float))
             out = {"rgb": rgb, "ids": ids, "occl": occl, "fimg": fimg, "rays": n}
         if n < 0:
             raise RuntimeError("oracle render failed")
@@ -251,12 +281,23 @@ class RefScene(_SceneBase):
     prefix = "rref_"
 
     def __init__(self, scene, material):
+        """material: one material dict, or a list of them indexed by
+        scene["mat_of_tri"] (one coloured_mapper_shader per entry)."""
         self.lib = ref_lib()
         v, t, a, f = _scene_arrays(scene)
         self._keep = (v, t, a, f)
-        self.mat = make_material(material)
-        self.h = self.lib["rref_scene_create"](_p(v, C.c_float), v.shape[0], _p(t, C.c_int32), t.shape[0],
-                                               _p(a, C.c_float), _p(f, C.c_uint32), C.byref(self.mat))
+        if isinstance(material, (list, tuple)):
+            self.mat = make_materials(material)
+            mt = scene.get("mat_of_tri")
+            mt = None if mt is None else np.ascontiguousarray(mt, np.int32)
+            self._keep = self._keep + (mt,)
+            self.h = self.lib["rref_scene_create_mt"](_p(v, C.c_float), v.shape[0], _p(t, C.c_int32), t.shape[0],
+                                                      _p(a, C.c_float), _p(f, C.c_uint32), self.mat, len(self.mat),
+                                                      _p(mt, C.c_int32))
+        else:
+            self.mat = make_material(material)
+            self.h = self.lib["rref_scene_create"](_p(v, C.c_float), v.shape[0], _p(t, C.c_int32), t.shape[0],
+                                                   _p(a, C.c_float), _p(f, C.c_uint32), C.byref(self.mat))
         self.build_seconds = self.lib["rref_scene_build"](self.h)
 
     def render(self, frame, aa=(1, 1)):

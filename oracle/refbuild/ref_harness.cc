@@ -55,6 +55,7 @@ struct null_buf : std::streambuf {
 struct ref_scene {
     std::unique_ptr<material> opaque;
     std::unique_ptr<material> transparent;
+    std::vector<std::unique_ptr<material>> table;
     primitive_store store;
     std::unique_ptr<bvh> accel;
 };
@@ -83,6 +84,43 @@ void *rref_scene_create(const float *verts, int32_t nverts, const int32_t *tris,
         const int32_t ia = tris[3 * i], ib = tris[3 * i + 1], ic = tris[3 * i + 2];
         const uint32_t f = flags ? flags[i] : 0u;
         material *mat = (f & RO_TRI_TRANSPARENT) ? s->transparent.get() : s->opaque.get();
+        if (vattr) {
+            point_t<> vt[3] = {p3(vattr + 3 * ia), p3(vattr + 3 * ib), p3(vattr + 3 * ic)};
+            s->store.emplace_back(mat, p3(verts + 3 * ia), p3(verts + 3 * ib), p3(verts + 3 * ic),
+                                  (f & RO_TRI_LIGHT) != 0, static_cast<const point_t<> *>(nullptr),
+                                  static_cast<const point_t<> *>(vt));
+        } else {
+            s->store.emplace_back(mat, p3(verts + 3 * ia), p3(verts + 3 * ib), p3(verts + 3 * ic),
+                                  (f & RO_TRI_LIGHT) != 0);
+        }
+    }
+    return s;
+}
+
+// A scene whose triangles carry per-triangle materials from a table (the
+// reference's material pointer per triangle, triangle.h:99-106): one
+// coloured_mapper_shader per entry with its tran, ri and rf; kd follows the
+// vertex colour unless the entry says otherwise.
+void *rref_scene_create_mt(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris, const float *vattr,
+                           const uint32_t *flags, const ro_material *mats, int32_t nmats, const int32_t *mat_of_tri)
+{
+    (void)nverts;
+    auto *s = new ref_scene();
+    for (int32_t k = 0; k < nmats; ++k) {
+        const ro_material *m = &mats[k];
+        // each shader owns (and deletes) its texture mappers: one per entry
+        const texture_mapper *map =
+            (vattr && !(m->flags & RO_MAT_NO_VERTEX_COLOUR)) ? new vertex_colour_mapper() : nullptr;
+        s->table.emplace_back(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
+                                                         ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
+                                                         ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, m->tran,
+                                                         m->ri, m->rf, 0.0f, 0.0f, nullptr, map));
+    }
+    s->store.reserve(ntris);
+    for (int32_t i = 0; i < ntris; ++i) {
+        const int32_t ia = tris[3 * i], ib = tris[3 * i + 1], ic = tris[3 * i + 2];
+        const uint32_t f = flags ? flags[i] : 0u;
+        material *mat = s->table[mat_of_tri ? mat_of_tri[i] : 0].get();
         if (vattr) {
             point_t<> vt[3] = {p3(vattr + 3 * ia), p3(vattr + 3 * ib), p3(vattr + 3 * ic)};
             s->store.emplace_back(mat, p3(verts + 3 * ia), p3(verts + 3 * ib), p3(verts + 3 * ic),

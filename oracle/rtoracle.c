@@ -102,6 +102,7 @@ struct ro_scene {
     ro_node *nodes;
     int32_t nnodes, root;
     int32_t *indirect;  /* primitive_store::_indirect */
+    int32_t *mat;       /* material index per triangle, or NULL (all 0) */
 };
 
 ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris,
@@ -145,6 +146,7 @@ ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tri
 
 void ro_scene_destroy(ro_scene *s)
 {
+    if (s) free(s->mat);
     if (!s) return;
     free(s->va); free(s->vb); free(s->vc); free(s->n);
     free(s->ta); free(s->tb); free(s->tc); free(s->flags);
@@ -498,18 +500,27 @@ void ro_camera_rays(const ro_camera *cam, int32_t x0, int32_t y0, int32_t w, int
 /* ray::offset_start_point(+1) (ray.h:111-157): nudge each coordinate by
  * int(+-32 * n) units in the last place along the geometric normal, or by
  * 1e-4 * n (from zero) when the coordinate is tiny. */
-static inline float offset_coord(float p, float n)
+static inline float offset_coord_d(float p, float n, float d)
 {
     uint32_t x = f2u(p);
     if ((x & 0x7fffffffu) < f2u(RO_FP_DELTA_SMALL)) return 0.0f + (RO_FP_DELTA_SMALL * n);
     const float off = ((x >> 31) & 1u) ? -RO_FP_DELTA : RO_FP_DELTA;
-    x += (uint32_t)cvtt((off * n) * 1.0f);
+    x += (uint32_t)cvtt((off * n) * d);
     return u2f(x);
 }
 
 static inline v3 offset_start(v3 dst, v3 geo)
 {
-    return mk(offset_coord(dst.x, geo.x), offset_coord(dst.y, geo.y), offset_coord(dst.z, geo.z));
+    return mk(offset_coord_d(dst.x, geo.x, 1.0f), offset_coord_d(dst.y, geo.y, 1.0f),
+              offset_coord_d(dst.z, geo.z, 1.0f));
+}
+
+/* offset_start_point(-1): into the surface (the refraction start point); the
+ * tiny-coordinate case still steps along +n, as the reference does. */
+static inline v3 offset_start_in(v3 dst, v3 geo)
+{
+    return mk(offset_coord_d(dst.x, geo.x, -1.0f), offset_coord_d(dst.y, geo.y, -1.0f),
+              offset_coord_d(dst.z, geo.z, -1.0f));
 }
 
 /* Light direction sign for directional lights (light.h:172-219): the light
@@ -546,7 +557,9 @@ typedef struct {
     const ro_camera *cam;
     const ro_light *lights;
     int32_t nlights;
-    const ro_material *mat;
+    const ro_material *mat;       /* AO mode and material 0 */
+    const ro_material *mats;      /* material table (ro_render_mt) */
+    int32_t nmats;
     int32_t row0, row1;
     uint8_t *rgb;
     int32_t *hit_id;
@@ -566,7 +579,7 @@ typedef struct {
  * triangle::normal_at_point, triangle.h:464-498), then the interpolated
  * attribute (triangle.h:74-79). */
 static inline void hit_setup(const ro_scene *s, const ro_ray *r, int32_t id, const ro_hit *h,
-                             v3 *dst, v3 *shader_n, v3 *geo, v3 *vt)
+                             v3 *dst, v3 *shader_n, v3 *geo, v3 *vt, int *out_in)
 {
     v3 p = vadd(r->o, vmul(r->d, h->d));              /* calculate_destination */
     const v3 n = s->n[id];
@@ -575,6 +588,7 @@ static inline void hit_setup(const ro_scene *s, const ro_ray *r, int32_t id, con
     p = vadd(p, vmul(r->d, num / denom));              /* change_length */
     if (denom > 0.0f) { *shader_n = vneg(n); *geo = vneg(n); }
     else { *shader_n = n; *geo = n; }
+    if (out_in) *out_in = !(denom > 0.0f);    /* hit_t::out_in: the ray enters the front face */
     *dst = p;
     if (s->ta) {
         const float w = 1.0f - (h->u + h->v);
@@ -589,7 +603,7 @@ static inline void hit_setup(const ro_scene *s, const ro_ray *r, int32_t id, con
 static inline v3 cur_kd(const ro_scene *s, const ro_material *m, v3 vt)
 {
     v3 kd = ld3(m->kd);
-    if (s->ta) {
+    if (s->ta && !(m->flags & RO_MAT_NO_VERTEX_COLOUR)) {
         const v3 tex = mk(vt.x * 255.0f, vt.y * 255.0f, vt.z * 255.0f);
         const float k = 1.0f / 255.0f;
         kd = mk(tex.x * (m->kd[0] * k), tex.y * (m->kd[1] * k), tex.z * (m->kd[2] * k));
@@ -617,7 +631,6 @@ static inline uint8_t clip8(float v) { return (uint8_t)smin(255.0f, smax(0.0f, v
 static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int first, size_t pix, v3 *out)
 {
     const ro_scene *s = J->s;
-    const ro_material *m = J->mat;
     ro_hit h;
     const int32_t id = closest(s, r, &h);
     J->rays += 1;
@@ -627,8 +640,10 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
         if (first && J->ao_count) J->ao_count[pix] = 0;
         return id;
     }
+    const ro_material *m = J->ao_n > 0 ? J->mat : &J->mats[s->mat ? s->mat[id] : 0];
     v3 dst, sn, geo, vt;
-    hit_setup(s, r, id, &h, &dst, &sn, &geo, &vt);
+    int out_in;
+    hit_setup(s, r, id, &h, &dst, &sn, &geo, &vt, &out_in);
     const v3 start = offset_start(dst, geo);
     const v3 kd = cur_kd(s, m, vt);
     const v3 ks = ld3(m->ks);
@@ -676,15 +691,38 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
         c = mk(c.x + I.x * (sc.x * lmagn), c.y + I.y * (sc.y * lmagn), c.z + I.z * (sc.z * lmagn));
     }
     c = vadd(c, ld3(m->ka));
+    /* ray::reflect (ray.cc:118-135) */
     const float refl_power = magn * m->rf;
+    int has_refl = 0;
+    v3 refl_c = mk(0.0f, 0.0f, 0.0f);
     if ((double)refl_power > RO_MIN_REFLECTIVE_POWER) {
         const float rdn = 2.0f * vdot(r->d, sn);
         const ro_ray rr = {start, vsub(r->d, vmul(sn, rdn))};
-        v3 cr;
-        trace_colour(J, &rr, refl_power, 0, pix, &cr);
-        const v3 avg = vdivs(vadd(mk(0.0f, 0.0f, 0.0f), cr), 1.0f);
-        c = vadd(c, vmul(avg, m->rf));
+        trace_colour(J, &rr, refl_power, 0, pix, &refl_c);
+        has_refl = 1;
     }
+    /* ray::refract (ray.cc:198-281): ri inverted for a ray entering the
+     * front face, none beyond the critical angle, start point pushed into
+     * the surface */
+    const float refr_power = magn * m->tran;
+    int has_refr = 0;
+    v3 refr_c = mk(0.0f, 0.0f, 0.0f);
+    if ((double)refr_power > RO_MIN_REFLECTIVE_POWER) {
+        float ri = m->ri;
+        const float rdn = -vdot(r->d, sn);
+        if (out_in) ri = 1.0f / ri;
+        const float cos_t2 = 1.0f - (ri * ri) * (1.0f - rdn * rdn);
+        if (!(cos_t2 < 0.0f)) {
+            const float off = ri * rdn - sqrtf(cos_t2);
+            const ro_ray rr = {offset_start_in(dst, geo), vadd(vmul(r->d, ri), vmul(sn, off))};
+            trace_colour(J, &rr, refr_power, 0, pix, &refr_c);
+            has_refr = 1;
+        }
+    }
+    /* combind_secondary_rays (coloured_mapper_shader.cc:117-130): the one
+     * ray's average colour times rf, then times tran */
+    if (m->rf > 0.0f && has_refl) c = vadd(c, vmul(vdivs(vadd(mk(0.0f, 0.0f, 0.0f), refl_c), 1.0f), m->rf));
+    if (m->tran > 0.0f && has_refr) c = vadd(c, vmul(vdivs(vadd(mk(0.0f, 0.0f, 0.0f), refr_c), 1.0f), m->tran));
     *out = c;
     return id;
 }
@@ -747,9 +785,38 @@ int64_t ro_render(const ro_scene *s, const ro_camera *cam, const ro_light *light
     if (!s || !s->nodes || !cam || !mat || !rgb || row0 < 0 || row1 > cam->yres || row0 > row1) return -1;
     render_job J;
     memset(&J, 0, sizeof(J));
-    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mat;
+    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mat; J.mats = mat; J.nmats = 1;
     J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id; J.occl = occl; J.fimg = fimg;
     return run_render(&J, nthreads);
+}
+
+int64_t ro_render_mt(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                     const ro_material *mats, int32_t nmats, int32_t row0, int32_t row1, int32_t nthreads,
+                     uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg)
+{
+    if (!s || !s->nodes || !cam || !mats || nmats < 1 || !rgb || row0 < 0 || row1 > cam->yres || row0 > row1)
+        return -1;
+    if (s->mat)
+        for (int32_t i = 0; i < s->ntris; ++i)
+            if (s->mat[i] < 0 || s->mat[i] >= nmats) return -1;
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mats; J.mats = mats; J.nmats = nmats;
+    J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id; J.occl = occl; J.fimg = fimg;
+    return run_render(&J, nthreads);
+}
+
+int32_t ro_scene_set_materials(ro_scene *s, const int32_t *mat_of_tri)
+{
+    if (!s) return -1;
+    free(s->mat);
+    s->mat = NULL;
+    if (!mat_of_tri) return 0;
+    const size_t nt = (size_t)(s->ntris > 0 ? s->ntris : 1);
+    s->mat = (int32_t *)malloc(nt * sizeof(int32_t));
+    if (!s->mat) return -1;
+    memcpy(s->mat, mat_of_tri, (size_t)s->ntris * sizeof(int32_t));
+    return 0;
 }
 
 int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material *mat,

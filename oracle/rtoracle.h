@@ -58,7 +58,11 @@ typedef struct ro_material {
     float ka[3], kd[3], ks[3];
     float ns;
     float rf;     /* mirror reflectivity, coloured_mapper_shader's rf (0: none) */
+    float tran;   /* transparency: refracted colour weight, the shader's tran (0: none) */
+    float ri;     /* refractive index, the shader's ri */
+    uint32_t flags;   /* RO_MAT_NO_VERTEX_COLOUR: kd not modulated by the vertex attribute */
 } ro_material;
+#define RO_MAT_NO_VERTEX_COLOUR 1u
 
 typedef struct ro_scene ro_scene;
 
@@ -105,6 +109,20 @@ void ro_camera_rays(const ro_camera *cam, int32_t x0, int32_t y0, int32_t w, int
 int64_t ro_render(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
                   const ro_material *mat, int32_t row0, int32_t row1, int32_t nthreads,
                   uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg);
+
+/* Per-triangle materials: mat_of_tri[i] indexes the table given to
+ * ro_render_mt (NULL: every triangle uses material 0). */
+int32_t ro_scene_set_materials(ro_scene *s, const int32_t *mat_of_tri);
+
+/* ro_render with a material table (the reference's per-triangle material
+ * pointers, triangle.h:99-106): reflections (rf) and refractions (tran, ri)
+ * are traced recursively as ray_trace_engine::ray_trace does.  Shadow rays
+ * pass the triangles flagged RO_TRI_TRANSPARENT; the reference passes those
+ * whose material has tran > 0 (material::is_transparent, material.h:63), so
+ * the flags are to agree with the table. */
+int64_t ro_render_mt(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                     const ro_material *mats, int32_t nmats, int32_t row0, int32_t row1, int32_t nthreads,
+                     uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg);
 
 /* Ambient-occlusion render (no reference counterpart: the ray generator is
  * this project's, restated identically in the CUDA core).  Per primary hit,

@@ -66,7 +66,7 @@ class RtLight(C.Structure):
 
 class RtMaterial(C.Structure):
     _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
-                ("rf", C.c_float)]
+                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
 
 
 class RtRenderStats(C.Structure):
@@ -125,6 +125,9 @@ SIGNATURES = [
     ("rt_scene_refit_vertices", C.c_int32, [_P, _P, C.c_int32, C.POINTER(C.c_float)]),
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
+    ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
+    ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
+                                        C.POINTER(RtMaterial), C.c_int32, _P, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_aa", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight), C.c_int32,
                                  C.POINTER(RtMaterial), _P, C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
@@ -203,7 +206,17 @@ def make_material(d) -> RtMaterial:
     m.ka[:], m.kd[:], m.ks[:] = list(d["ka"]), list(d["kd"]), list(d["ks"])
     m.ns = d["ns"]
     m.rf = d.get("rf", 0.0)
+    m.tran = d.get("tran", 0.0)
+    m.ri = d.get("ri", 1.0)
+    m.flags = d.get("flags", 0)
     return m
+
+
+def make_materials(ds):
+    arr = (RtMaterial * len(ds))()
+    for i, d in enumerate(ds):
+        arr[i] = make_material(d)
+    return arr
 
 
 def rays_array(ogn, dirs, tmax=None):
@@ -260,6 +273,8 @@ class Scene:
         self.build_ms = None
         if scene is not None:
             self.upload(scene["verts"], scene["tris"], scene.get("vattr"), scene.get("flags"))
+            if scene.get("mat_of_tri") is not None:
+                self.set_materials(scene["mat_of_tri"])
             if build:
                 self.build()
 
@@ -269,6 +284,16 @@ class Scene:
         self._keep = (verts, tris, vattr, flags)
         _check(lib().rt_scene_upload(self.h, ptr(verts), nv, ptr(tris), nt, ptr(vattr), ptr(flags)))
         self.nverts, self.ntris = nv, nt
+
+    def set_materials(self, mat_of_tri):
+        """Material index per triangle (None: every triangle uses material 0)."""
+        if mat_of_tri is None:
+            _check(lib().rt_scene_set_materials(self.h, None, 0))
+            self._mat = None
+            return
+        mt = np.ascontiguousarray(mat_of_tri, np.int32)
+        _check(lib().rt_scene_set_materials(self.h, ptr(mt), int(mt.shape[0])))
+        self._mat = mt
 
     def update_vertices(self, verts):
         _check(lib().rt_scene_update_vertices(self.h, ptr(verts), int(verts.shape[0])))
@@ -319,7 +344,7 @@ class Scene:
         if ids is None and want_ids:
             ids = np.empty((H, W), np.int32)
         st = RtRenderStats()
-        mat = make_material(frame["material"])
+        mat = make_material(frame["material"] if "material" in frame else frame["materials"][0])
         ao = frame.get("ao")
         if ao:
             cnt = np.empty((H, W), np.int32) if want_ids else None
@@ -327,8 +352,13 @@ class Scene:
                                       ptr(rgb), ptr(ids), ptr(cnt), C.byref(st)))
             return {"rgb": rgb, "ids": ids, "ao_count": cnt, "stats": st}
         ls = make_lights(frame["lights"])
-        _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
-                               C.byref(st)))
+        if frame.get("materials"):
+            table = make_materials(frame["materials"])
+            _check(lib().rt_render_materials(self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table),
+                                             ptr(rgb), ptr(ids), C.byref(st)))
+        else:
+            _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
+                                   C.byref(st)))
         return {"rgb": rgb, "ids": ids, "stats": st}
 
     def render_aa(self, frame, aa_x, aa_y, rgb=None):

@@ -259,8 +259,9 @@ rt_status check_frame(rt_scene *s, const rt_camera *cam, const rt_light *lights,
     if (cam->xres <= 0 || cam->yres <= 0 || (int64_t)cam->xres * cam->yres > (int64_t)1 << 28)
         return set_error(RT_ERR_INVALID_ARG, "camera resolution out of range");
     if (nl < 0 || nl > RT_MAX_LIGHTS || (nl > 0 && !lights)) return set_error(RT_ERR_INVALID_ARG, "light count out of range");
-    if (m->rf != 0.0f)
-        return set_error(RT_ERR_INVALID_ARG, "reflective materials (rf > 0) are rendered by rt_render only");
+    if (m->rf != 0.0f || m->tran != 0.0f)
+        return set_error(RT_ERR_INVALID_ARG,
+                         "reflective or transparent materials (rf, tran > 0) are rendered by rt_render only");
     if (!s->built) return set_error(RT_ERR_NOT_BUILT, "hierarchy not built");
     return RT_OK;
 }

@@ -1,5 +1,7 @@
 // rt_api.cu -- the C ABI (include/rtcore.h): contexts, scenes, staging of
 // host buffers, and launch of the build / trace / render kernels.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -140,6 +142,9 @@ MaterialView make_material_view(const rt_material &m)
     v.ks = make_float3(m.ks[0], m.ks[1], m.ks[2]);
     v.ns = m.ns;
     v.rf = m.rf;
+    v.tran = m.tran;
+    v.ri = m.ri;
+    v.flags = m.flags;
     return v;
 }
 
@@ -157,6 +162,7 @@ SceneView scene_view(const rt_scene *s)
     v.root = 0;
     v.tri_base = 0;
     v.isect = s->ctx->isect;
+    v.mat = s->d_mat;
     return v;
 }
 
@@ -322,6 +328,7 @@ static void scene_free_geometry(rt_scene *s)
     cudaFree(s->d_vattr); s->d_vattr = nullptr;
     cudaFree(s->d_flags); s->d_flags = nullptr;
     cudaFree(s->d_shade); s->d_shade = nullptr;
+    cudaFree(s->d_mat); s->d_mat = nullptr; s->mat_max = -1;
     cudaFree(s->d_nodes); s->d_nodes = nullptr;
     cudaFree(s->d_tris); s->d_tris = nullptr;
     s->temp.release();
@@ -563,22 +570,66 @@ rt_status rt_trace_any(rt_scene *s, const rt_ray *rays, int32_t n, uint8_t *occl
     return trace_common<true>(s, rays, n, occluded, "rt_trace_any");
 }
 
-// Mirror reflectivity: 0 (none), or a value whose chain of ray powers
-// (1, rf, rf*rf, ... in binary32) drops to 0.1 or below within
-// RT_MAX_BOUNCES reflections.  Entry points without reflections take 0 only.
-static rt_status check_reflectivity(float rf, const char *who, bool supported = true)
+// Secondary-ray weights of a material: rf and tran each 0 (none) or in
+// (0, 1); a refracting material needs a finite positive ri.  Entry points
+// without secondary rays take rf = tran = 0 only.
+static rt_status check_weights(const rt_material &m, const std::string &w, bool supported)
 {
-    if (rf == 0.0f) return RT_OK;
-    std::string w(who);
-    if (!supported) return fail(RT_ERR_INVALID_ARG, w + ": reflective materials (rf > 0) are rendered by rt_render");
-    if (!(rf > 0.0f) || !(rf < 1.0f)) return fail(RT_ERR_INVALID_ARG, w + ": reflectivity must be 0 or in (0, 1)");
-    float magn = 1.0f;
-    for (int k = 0; k <= RT_MAX_BOUNCES; ++k) {
-        const float power = magn * rf;
-        if (!((double)power > 0.1)) return RT_OK;
-        magn = power;
+    if (m.rf == 0.0f && m.tran == 0.0f) return RT_OK;
+    if (!supported)
+        return fail(RT_ERR_INVALID_ARG, w + ": reflective or transparent materials (rf, tran > 0) are rendered by "
+                                            "rt_render and rt_render_materials");
+    if (!(m.rf >= 0.0f) || !(m.rf < 1.0f)) return fail(RT_ERR_INVALID_ARG, w + ": reflectivity must be 0 or in (0, 1)");
+    if (!(m.tran >= 0.0f) || !(m.tran < 1.0f))
+        return fail(RT_ERR_INVALID_ARG, w + ": transparency must be 0 or in (0, 1)");
+    if (m.tran > 0.0f && !(m.ri > 0.0f && m.ri < 3.0e38f))
+        return fail(RT_ERR_INVALID_ARG, w + ": a transparent material needs a finite positive refractive index");
+    return RT_OK;
+}
+
+// Worst-case ray tree of a set of materials: a ray of power p spawns a
+// mirror ray of power p * rf and a refracted ray of power p * tran, each
+// traced while its power exceeds 0.1.  With a = the largest rf and b = the
+// largest tran, a ray reached by i reflections and j refractions has power
+// at most a^i * b^j (times 1 + 2^-24 per binary32 product, hence the slack
+// on the threshold), and at most C(i + j, i) rays share (i, j).  The tree
+// must stay within RT_MAX_BOUNCES levels and RT_MAX_TREE_RAYS rays.
+static rt_status check_tree(const rt_material *m, int32_t n, const std::string &w)
+{
+    double a = 0.0, b = 0.0;
+    for (int32_t k = 0; k < n; ++k) {
+        a = std::max(a, (double)m[k].rf);
+        b = std::max(b, (double)m[k].tran);
     }
-    return fail(RT_ERR_INVALID_ARG, w + ": reflectivity needs more than RT_MAX_BOUNCES mirror bounces");
+    const double thr = 0.1 * (1.0 - 1.0e-5);
+    double rays = 0.0;
+    int depth = 0;
+    const int lim = 4 * RT_MAX_BOUNCES;
+    for (int i = 0; i <= lim; ++i) {
+        double binom = 1.0;   // C(i + j, i), j = 0
+        for (int j = 0; i + j <= lim; ++j) {
+            const double p = std::pow(a, i) * std::pow(b, j);
+            if (!(p > thr) && (i + j) > 0) break;
+            rays += binom;
+            depth = std::max(depth, i + j);
+            binom = binom * (double)(i + j + 1) / (double)(j + 1);
+        }
+    }
+    if (depth > RT_MAX_BOUNCES)
+        return fail(RT_ERR_INVALID_ARG, w + ": reflectivity and transparency need more than RT_MAX_BOUNCES levels of "
+                                            "secondary rays");
+    if (rays > (double)RT_MAX_TREE_RAYS)
+        return fail(RT_ERR_INVALID_ARG, w + ": reflectivity and transparency allow more than RT_MAX_TREE_RAYS rays "
+                                            "per pixel");
+    return RT_OK;
+}
+
+static rt_status check_material(const rt_material &m, const char *who, bool supported = true)
+{
+    const std::string w(who);
+    const rt_status st = check_weights(m, w, supported);
+    if (st != RT_OK || (m.rf == 0.0f && m.tran == 0.0f)) return st;
+    return check_tree(&m, 1, w);
 }
 
 static rt_status check_camera(const rt_camera *cam)
@@ -646,6 +697,113 @@ static rt_status finish_outputs(rt_context *ctx, size_t npix, uint8_t *rgb, int3
     return status_to_error(c.status);
 }
 
+rt_status rt_scene_set_materials(rt_scene *s, const int32_t *mat_of_tri, int32_t ntris)
+{
+    if (!s) return fail(RT_ERR_INVALID_ARG, "rt_scene_set_materials: NULL scene");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (!mat_of_tri) {
+        cudaFree(s->d_mat);
+        s->d_mat = nullptr;
+        s->mat_max = -1;
+        return RT_OK;
+    }
+    if (ntris != s->ntris) return fail(RT_ERR_INVALID_ARG, "rt_scene_set_materials: ntris differs from the scene's");
+    int32_t lo = 0, hi = 0;
+    const bool dev = is_device_ptr(mat_of_tri);
+    if (!dev) {
+        for (int32_t i = 0; i < ntris; ++i) {
+            lo = std::min(lo, mat_of_tri[i]);
+            hi = std::max(hi, mat_of_tri[i]);
+        }
+        if (lo < 0 || hi >= RT_MAX_MATERIALS)
+            return fail(RT_ERR_INVALID_ARG, "rt_scene_set_materials: material index outside 0..RT_MAX_MATERIALS-1");
+    }
+    int32_t *d = s->d_mat;
+    if (!d) RT_CUDA(cudaMalloc(&d, (size_t)std::max(ntris, 1) * sizeof(int32_t)), "material index allocation");
+    s->d_mat = d;
+    s->mat_max = -1;
+    if (ntris > 0)
+        RT_CUDA(cudaMemcpyAsync(d, mat_of_tri, (size_t)ntris * sizeof(int32_t), cudaMemcpyDefault, ctx->stream),
+                "material index copy");
+    if (dev) {
+        RT_CUDA(ctx->stage_c.reserve(2 * sizeof(int32_t)), "staging allocation");
+        int32_t *range = (int32_t *)ctx->stage_c.ptr;
+        launch_index_range(d, ntris, range, ctx->stream);
+        RT_CUDA(cudaGetLastError(), "index range launch");
+        RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, range, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream),
+                "index range readback");
+        RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+        lo = ctx->h_scratch[0];
+        hi = ctx->h_scratch[1];
+        if (lo < 0 || hi >= RT_MAX_MATERIALS) {
+            cudaFree(s->d_mat);
+            s->d_mat = nullptr;
+            return fail(RT_ERR_INVALID_ARG, "rt_scene_set_materials: material index outside 0..RT_MAX_MATERIALS-1");
+        }
+    }
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "material upload synchronize");
+    s->mat_max = hi;
+    return RT_OK;
+}
+
+// A frame whose materials spawn secondary rays (or differ per triangle):
+// the ray-tree kernel.
+static rt_status render_tree(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                             const rt_material *mats, int32_t nmats, bool per_triangle, uint8_t *rgb_out,
+                             int32_t *hit_ids, rt_render_stats *stats)
+{
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    RenderOut o;
+    rt_status st = prepare_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o);
+    if (st != RT_OK) return st;
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = 0;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    MaterialTable mt;
+    mt.n = nmats;
+    for (int i = 0; i < nmats; ++i) mt.m[i] = make_material_view(mats[i]);
+    SceneView sv = scene_view(s);
+    if (!per_triangle) sv.mat = nullptr;
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render_tree(sv, make_camera_view(*camera), ls, mt, o.rgb, o.ids, ctx->d_counters, ctx->sm_count,
+                       ctx->stream, ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
+}
+
+rt_status rt_render_materials(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                              const rt_material *materials, int32_t nmaterials, uint8_t *rgb_out, int32_t *hit_ids,
+                              rt_render_stats *stats)
+{
+    if (!s || !materials || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render_materials: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
+        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: light count out of range");
+    if (nmaterials < 1 || nmaterials > RT_MAX_MATERIALS)
+        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: material count must be 1..RT_MAX_MATERIALS");
+    const std::string w("rt_render_materials");
+    for (int32_t i = 0; i < nmaterials; ++i) {
+        st = check_weights(materials[i], w, true);
+        if (st != RT_OK) return st;
+    }
+    st = check_tree(materials, nmaterials, w);
+    if (st != RT_OK) return st;
+    if (s->mat_max >= nmaterials)
+        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: the scene's material indices exceed the table");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_materials: hierarchy not built");
+    const bool plain = nmaterials == 1 && materials[0].rf == 0.0f && materials[0].tran == 0.0f;
+    if (plain) return rt_render(s, camera, lights, nlights, materials, rgb_out, hit_ids, stats);
+    return render_tree(s, camera, lights, nlights, materials, nmaterials, true, rgb_out, hit_ids, stats);
+}
+
 rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
                     const rt_material *material, uint8_t *rgb_out, int32_t *hit_ids, rt_render_stats *stats)
 {
@@ -654,9 +812,11 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     if (st != RT_OK) return st;
     if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
         return fail(RT_ERR_INVALID_ARG, "rt_render: light count out of range");
-    st = check_reflectivity(material->rf, "rt_render");
+    st = check_material(*material, "rt_render");
     if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render: hierarchy not built");
+    if (material->rf > 0.0f || material->tran > 0.0f)
+        return render_tree(s, camera, lights, nlights, material, 1, false, rgb_out, hit_ids, stats);
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);
     const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
@@ -669,10 +829,7 @@ rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    if (material->rf > 0.0f)
-        launch_render_reflect(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb,
-                              o.ids, ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
-    else if (ctx->render_kernel == RT_KERNEL_WAVE)
+    if (ctx->render_kernel == RT_KERNEL_WAVE)
         launch_render_wave(scene_view(s), make_camera_view(*camera), ls, make_material_view(*material), o.rgb, o.ids,
                            ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
     else
@@ -698,7 +855,7 @@ rt_status rt_render_aa(rt_scene *s, const rt_camera *camera, int32_t aa_x, int32
     if (st != RT_OK) return st;
     if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
         return fail(RT_ERR_INVALID_ARG, "rt_render_aa: light count out of range");
-    st = check_reflectivity(material->rf, "rt_render_aa", false);
+    st = check_material(*material, "rt_render_aa", false);
     if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_aa: hierarchy not built");
     rt_context *ctx = s->ctx;
@@ -731,7 +888,7 @@ rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *
     if (st != RT_OK) return st;
     if (samples < 1 || samples > 64) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: samples must be 1..64");
     if (!(ao_dist > 0.0f)) return fail(RT_ERR_INVALID_ARG, "rt_render_ao: ao_dist must be positive");
-    st = check_reflectivity(material->rf, "rt_render_ao", false);
+    st = check_material(*material, "rt_render_ao", false);
     if (st != RT_OK) return st;
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_ao: hierarchy not built");
     rt_context *ctx = s->ctx;

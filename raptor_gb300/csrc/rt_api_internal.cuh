@@ -53,6 +53,8 @@ struct rt_scene {
     float *d_vattr = nullptr;
     uint32_t *d_flags = nullptr;
     rtc::ShadeTri *d_shade = nullptr;
+    int32_t *d_mat = nullptr;             // material index per triangle (rt_scene_set_materials)
+    int32_t mat_max = -1;                 // largest index in d_mat (-1: none set)
     rtc::WideNode *d_nodes = nullptr;
     rtc::PackedTri *d_tris = nullptr;
     int32_t nnodes = 0, tri_slots = 0, depth = 0;

@@ -383,8 +383,9 @@ rt_status rt_batch_set_jobs(rt_batch *b, const rt_job *jobs, int32_t njobs)
         if (J.camera.xres <= 0 || J.camera.yres <= 0 || (int64_t)J.camera.xres * J.camera.yres > (1 << 26))
             return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_jobs: resolution out of range");
         if (J.mode != RT_JOB_SHADOW && J.mode != RT_JOB_AO) return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_jobs: bad mode");
-        if (J.material.rf != 0.0f)
-            return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_jobs: reflective materials (rf > 0) are rendered by rt_render");
+        if (J.material.rf != 0.0f || J.material.tran != 0.0f)
+            return bfail(RT_ERR_INVALID_ARG,
+                         "rt_batch_set_jobs: reflective or transparent materials (rf, tran > 0) are rendered by rt_render");
         if (J.mode == RT_JOB_SHADOW && (J.nlights < 0 || J.nlights > RT_MAX_JOB_LIGHTS))
             return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_jobs: light count out of range");
         if (J.mode == RT_JOB_AO && (J.ao_samples < 1 || J.ao_samples > 64 || !(J.ao_dist > 0.f)))

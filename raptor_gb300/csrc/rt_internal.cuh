@@ -69,6 +69,7 @@ struct SceneView {
     int32_t root;             // root wide node of this scene
     int32_t tri_base;         // subtracted from packed ids to give the caller's ids
     int32_t isect;            // RT_ISECT_REFERENCE or RT_ISECT_WATERTIGHT
+    const int32_t *mat = nullptr;   // material index per triangle (caller's order) or nullptr
 };
 
 struct CameraView {
@@ -91,6 +92,16 @@ struct MaterialView {
     float3 ka, kd, ks;
     float ns;
     float rf;    // mirror reflectivity (0: none)
+    float tran;  // transparency: refracted colour weight (0: opaque)
+    float ri;    // refractive index
+    uint32_t flags;   // RT_MAT_NO_VERTEX_COLOUR
+};
+
+// Materials of a frame (rt_render_materials), indexed per triangle by
+// SceneView::mat.
+struct MaterialTable {
+    int32_t n;
+    MaterialView m[RT_MAX_MATERIALS];
 };
 
 // -------------------------------------------------- IEEE-exact helpers

@@ -47,9 +47,9 @@ void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_
                       cudaStream_t st);
 void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                    uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
-void launch_render_reflect(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
-                           uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st,
-                           bool count = false);
+void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
+                        uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t st);
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                       int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, int32_t *redo,
                       Counters *ctr, int sm_count, cudaStream_t st, bool count = false);

@@ -98,71 +98,151 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
     return out;
 }
 
-// Primary ray and its chain of mirror reflections (reflective material,
-// rf > 0): at every hit the coloured Phong of shade_pixel_lights with the
-// exact specular power, then, while the ray's power magn * rf exceeds 0.1
-// (compared in double, as the reference's MIN_REFLECTIVE_POWER literal), the
-// mirror ray dir - n * (2 dir.n) from the offset start point (ray::reflect,
-// ray.cc:118-135).  The colours combine from the deepest ray outwards,
-// c_k + c_(k+1) * rf (combind_secondary_rays, coloured_mapper_shader.cc:
-// 117-122); a ray that misses is the background.  `chain` holds up to
-// RT_MAX_BOUNCES + 1 colours.
+// One pending ray of a pixel's ray tree and, once it has hit, what its
+// children need: the hit point and geometric normal (start points), the
+// shading normal, the incoming direction, the material, and the colour
+// accumulated so far.
+struct TreeFrame {
+    float3 o_or_dst;   // stage 0: ray origin; later: refined hit point
+    float3 d;          // ray direction
+    float3 sn, geo;
+    float3 c;
+    float magn;
+    int32_t mat;
+    int32_t stage;     // 0 trace, 1 reflection next, 2 refraction next, 3 done
+    int32_t out_in;    // the ray entered the front face (hit_t::out_in)
+};
+
+// A pixel's ray tree (ray_trace_engine::ray_trace, raytracer.cc:20-87, as a
+// post-order walk with an explicit stack): at every hit the coloured Phong
+// of its triangle's material with the exact specular power; then the
+// mirror ray (ray::reflect, ray.cc:118-135: power magn * rf, traced while it
+// exceeds 0.1 compared in double) and the refracted ray (ray::refract,
+// ray.cc:198-281: power magn * tran, ri inverted for a ray entering the
+// front face, none beyond the critical angle, start point pushed into the
+// surface), each child's colour added to its parent's times rf, then tran
+// (combind_secondary_rays, coloured_mapper_shader.cc:117-130).  A ray that
+// misses is the background.  `frames` holds RT_MAX_BOUNCES + 1 entries.
 template <bool COUNT>
-__device__ __forceinline__ PixelOut shade_pixel_reflect(const SceneView &sc, const CameraView &cam, const LightView *lights,
-                                                        int nl, const MaterialView &mat, int x, int y, float3 *chain,
-                                                        uint32_t &status, FetchCount *fc)
+__device__ __forceinline__ PixelOut shade_pixel_tree(const SceneView &sc, const CameraView &cam, const LightView *lights,
+                                                     int nl, const MaterialTable &mt, int x, int y, TreeFrame *frames,
+                                                     uint32_t &status, FetchCount *fc)
 {
     PixelOut out;
     out.secondary = 0;
     out.ao_made = 0;
     out.hit = false;
     out.id = -1;
-    RayState r = camera_ray(cam, x, y);
-    float magn = 1.0f;
-    int last = 0;
-    for (int k = 0;; ++k) {
-        HitRecord h;
-        bool occ;
-        status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
-        if (k > 0) ++out.secondary;
-        if (!(h.t < FLT_MAX)) {
-            chain[k] = cam.background;
-            last = k;
-            break;
+    out.c = cam.background;
+    const RayState cr = camera_ray(cam, x, y);
+    int sp = 0;
+    frames[0].o_or_dst = cr.o;
+    frames[0].d = cr.d;
+    frames[0].magn = 1.0f;
+    frames[0].stage = 0;
+    sp = 1;
+    for (int guard = 0; sp > 0 && guard < 4 * RT_MAX_TREE_RAYS; ++guard) {
+        TreeFrame &F = frames[sp - 1];
+        if (F.stage == 0) {
+            HitRecord h;
+            bool occ;
+            status |= traverse<false, COUNT>(sc, F.o_or_dst, F.d, FLT_MAX, h, occ, fc);
+            if (sp > 1) ++out.secondary;
+            if (!(h.t < FLT_MAX)) {
+                // background; deliver to the parent below
+                F.c = cam.background;
+                F.stage = 3;
+            } else {
+                const int32_t id = h.id - sc.tri_base;
+                if (sp == 1) {
+                    out.hit = true;
+                    out.id = id;
+                }
+                int32_t mi = sc.mat ? __ldg(&sc.mat[id]) : 0;
+                if (mi < 0 || mi >= mt.n) { status |= kStatusBadIndex; mi = 0; }
+                const MaterialView &m = mt.m[mi];
+                RayState r;
+                r.o = F.o_or_dst;
+                r.d = F.d;
+                const SurfacePoint spt = surface_at(sc, r, h);
+                const float3 start = offset_start(spt.dst, spt.geo);
+                const float3 kd = material_kd(m, spt);
+                float3 c = make_float3(0.f, 0.f, 0.f);
+                for (int l = 0; l < nl; ++l) {
+                    float3 ldir;
+                    float len;
+                    shadow_ray(lights[l], start, ldir, len);
+                    HitRecord shh;
+                    bool blocked;
+                    status |= traverse<true, COUNT>(sc, start, ldir, len, shh, blocked, fc);
+                    ++out.secondary;
+                    phong_add<true>(lights[l], m, kd, spt.sn, F.d, ldir, len, blocked ? 0.0f : 1.0f, c);
+                }
+                F.c = xadd3(c, m.ka);
+                F.o_or_dst = spt.dst;
+                F.sn = spt.sn;
+                F.geo = spt.geo;
+                F.mat = mi;
+                F.out_in = spt.out_in ? 1 : 0;
+                F.stage = 1;
+            }
         }
-        if (k == 0) {
-            out.hit = true;
-            out.id = h.id - sc.tri_base;
+        if (F.stage == 1) {
+            F.stage = 2;
+            const MaterialView &m = mt.m[F.mat];
+            const float power = xmul(F.magn, m.rf);
+            if ((double)power > 0.1) {
+                if (sp > RT_MAX_BOUNCES) { status |= kStatusStepLimit; }
+                else {
+                    TreeFrame &C = frames[sp];
+                    const float rdn = xmul(2.0f, xdot(F.d, F.sn));
+                    C.o_or_dst = offset_start(F.o_or_dst, F.geo);
+                    C.d = xsub3(F.d, xmul3(F.sn, rdn));
+                    C.magn = power;
+                    C.stage = 0;
+                    ++sp;
+                    continue;
+                }
+            }
         }
-        const SurfacePoint sp = surface_at(sc, r, h);
-        const float3 start = offset_start(sp.dst, sp.geo);
-        const float3 kd = material_kd(mat, sp);
-        float3 c = make_float3(0.f, 0.f, 0.f);
-        for (int l = 0; l < nl; ++l) {
-            float3 ldir;
-            float len;
-            shadow_ray(lights[l], start, ldir, len);
-            HitRecord sh;
-            bool blocked;
-            status |= traverse<true, COUNT>(sc, start, ldir, len, sh, blocked, fc);
-            ++out.secondary;
-            phong_add<true>(lights[l], mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
+        if (F.stage == 2) {
+            F.stage = 3;
+            const MaterialView &m = mt.m[F.mat];
+            const float power = xmul(F.magn, m.tran);
+            if ((double)power > 0.1) {
+                float ri = m.ri;
+                const float rdn = -xdot(F.d, F.sn);
+                if (F.out_in) ri = xdiv(1.0f, ri);
+                const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
+                if (!(cos_t2 < 0.0f)) {
+                    if (sp > RT_MAX_BOUNCES) { status |= kStatusStepLimit; }
+                    else {
+                        const float off = xsub(xmul(ri, rdn), __fsqrt_rn(cos_t2));
+                        TreeFrame &C = frames[sp];
+                        C.o_or_dst = offset_start_in(F.o_or_dst, F.geo);
+                        C.d = xadd3(xmul3(F.d, ri), xmul3(F.sn, off));
+                        C.magn = power;
+                        C.stage = 0;
+                        ++sp;
+                        continue;
+                    }
+                }
+            }
         }
-        chain[k] = xadd3(c, mat.ka);
-        const float power = xmul(magn, mat.rf);
-        if (!((double)power > 0.1) || k == RT_MAX_BOUNCES) {
-            if ((double)power > 0.1) status |= kStatusStepLimit;   // deeper than the host allowed
-            last = k;
-            break;
+        // stage 3: the frame's colour is complete; deliver it to its parent
+        const float3 col = F.c;
+        --sp;
+        if (sp == 0) {
+            out.c = col;
+        } else {
+            TreeFrame &P = frames[sp - 1];
+            const MaterialView &pm = mt.m[P.mat];
+            // P.stage is 2 after its mirror child, 3 after its refracted child
+            const float w = (P.stage == 2) ? pm.rf : pm.tran;
+            P.c = xadd3(P.c, xmul3(xadd3(make_float3(0.f, 0.f, 0.f), col), w));
         }
-        const float rdn = xmul(2.0f, xdot(r.d, sp.sn));
-        r.o = start;
-        r.d = xsub3(r.d, xmul3(sp.sn, rdn));
-        magn = power;
     }
-    float3 acc = chain[last];
-    for (int k = last - 1; k >= 0; --k) acc = xadd3(chain[k], xmul3(acc, mat.rf));
-    out.c = acc;
+    if (sp > 0) status |= kStatusStepLimit;
     return out;
 }
 

@@ -292,15 +292,15 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
     if (status) atomicOr(&ctr->status, status);
 }
 
-// Frame of a reflective material: one pixel per lane, the mirror-ray chain
-// of shade_pixel_reflect (its colours in a per-thread chain array).
+// Frame with secondary rays or per-triangle materials: one pixel per lane,
+// the pixel's ray tree walked by shade_pixel_tree (its pending rays in a
+// per-thread frame stack).
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_reflect(SceneView sc, CameraView cam,
-                                                                  LightSet lights, MaterialView mat,
-                                                                  uint8_t *__restrict__ rgb,
-                                                                  int32_t *__restrict__ ids, Counters *ctr)
+__global__ void __launch_bounds__(kTraceThreads) k_render_tree(SceneView sc, CameraView cam, LightSet lights,
+                                                               MaterialTable mt, uint8_t *__restrict__ rgb,
+                                                               int32_t *__restrict__ ids, Counters *ctr)
 {
-    float3 chain[RT_MAX_BOUNCES + 1];
+    TreeFrame frames[RT_MAX_BOUNCES + 1];
     int tiles_x;
     const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
     uint32_t status = 0;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
         po.hit = false;
         po.secondary = 0;
         if (live) {
-            po = shade_pixel_reflect<COUNT>(sc, cam, lights.l, lights.n, mat, x, y, chain, status, &fc);
+            po = shade_pixel_tree<COUNT>(sc, cam, lights.l, lights.n, mt, x, y, frames, status, &fc);
             const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
             store_rgb(rgb, pix, po.c);
             if (ids) ids[pix] = po.id;
@@ -329,6 +329,25 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
         atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
     }
     if (status) atomicOr(&ctr->status, status);
+}
+
+// Smallest and largest of n indices (out[0], out[1]; n >= 0).
+__global__ void k_index_range(const int32_t *__restrict__ v, int32_t n, int32_t *out)
+{
+    int32_t lo = 0, hi = 0;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int32_t x = v[i];
+        lo = min(lo, x);
+        hi = max(hi, x);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&out[0], lo);
+        atomicMax(&out[1], hi);
+    }
 }
 
 }  // namespace
@@ -369,14 +388,22 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
         k_render<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
 }
 
-void launch_render_reflect(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
-                           uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
+void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
+                        uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_reflect<false>, sm_count);
+    static const int grid = grid_of(k_render_tree<false>, sm_count);
     if (count)
-        k_render_reflect<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+        k_render_tree<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, ids, ctr);
     else
-        k_render_reflect<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+        k_render_tree<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, ids, ctr);
+}
+
+void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t st)
+{
+    cudaMemsetAsync(out, 0, 2 * sizeof(int32_t), st);
+    const int blocks = (n + 255) / 256;
+    const int grid = blocks < 1 ? 1 : (blocks > 1216 ? 1216 : blocks);
+    k_index_range<<<grid, 256, 0, st>>>(v, n, out);
 }
 
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,

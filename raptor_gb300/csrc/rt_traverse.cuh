@@ -415,14 +415,17 @@ __device__ __forceinline__ uint32_t traverse(const SceneView &sc, const float3 o
 
 // ------------------------------------------------------------ shading
 
-// ray::offset_start_point(+1) (raytracer/ray.h:111-157).
-__device__ __forceinline__ float offset_coord(float p, float n)
+// ray::offset_start_point(d) (raytracer/ray.h:111-157) for d = +1 (out of
+// the surface, dsign 1) or -1 (into it, the refraction start point): each
+// coordinate moves by int(+-32 * n * d) units in the last place, or, when
+// the coordinate is tiny, to 1e-4 * n whatever d.
+__device__ __forceinline__ float offset_coord(float p, float n, float dsign = 1.0f)
 {
     uint32_t x = __float_as_uint(p);
     if ((x & 0x7fffffffu) < 0x38d1b717u)   // bit pattern of 1.0e-4f
         return xadd(0.0f, xmul(1.0e-4f, n));
     const float off = ((x >> 31) & 1u) ? -32.0f : 32.0f;
-    const float f = xmul(xmul(off, n), 1.0f);
+    const float f = xmul(xmul(off, n), dsign);
     int32_t iv;
     if (!(f > -2147483904.0f && f < 2147483648.0f)) iv = INT32_MIN;
     else iv = __float2int_rz(f);
@@ -433,6 +436,11 @@ __device__ __forceinline__ float offset_coord(float p, float n)
 __device__ __forceinline__ float3 offset_start(float3 p, float3 n)
 {
     return make_float3(offset_coord(p.x, n.x), offset_coord(p.y, n.y), offset_coord(p.z, n.z));
+}
+
+__device__ __forceinline__ float3 offset_start_in(float3 p, float3 n)
+{
+    return make_float3(offset_coord(p.x, n.x, -1.0f), offset_coord(p.y, n.y, -1.0f), offset_coord(p.z, n.z, -1.0f));
 }
 
 // Camera ray of pixel (x, y) (camera.h:127-140, EXACT_NORMALISE).
@@ -453,6 +461,7 @@ struct SurfacePoint {
     float3 geo;       // face-forwarded geometric normal
     float3 vt;        // interpolated per-vertex attribute
     bool has_attr;
+    bool out_in;      // the ray meets the front face (hit_t::out_in)
 };
 
 // Hit refinement and face-forwarding (raytracer.cc:30-31,
@@ -475,6 +484,7 @@ __device__ __forceinline__ SurfacePoint surface_at(const SceneView &sc, const Ra
         sp.sn = n;
         sp.geo = n;
     }
+    sp.out_in = !(denom > 0.0f);
     sp.dst = p;
     sp.has_attr = sc.vattr != nullptr;
     if (sp.has_attr) {
@@ -493,7 +503,7 @@ __device__ __forceinline__ SurfacePoint surface_at(const SceneView &sc, const Ra
 // Diffuse colour (coloured_mapper_shader.cc:61-66 with attribute*255 samples).
 __device__ __forceinline__ float3 material_kd(const MaterialView &m, const SurfacePoint &sp)
 {
-    if (!sp.has_attr) return m.kd;
+    if (!sp.has_attr || (m.flags & RT_MAT_NO_VERTEX_COLOUR)) return m.kd;
     const float k = 1.0f / 255.0f;
     return make_float3(xmul(xmul(sp.vt.x, 255.0f), xmul(m.kd.x, k)), xmul(xmul(sp.vt.y, 255.0f), xmul(m.kd.y, k)),
                        xmul(xmul(sp.vt.z, 255.0f), xmul(m.kd.z, k)));

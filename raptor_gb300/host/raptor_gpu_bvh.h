@@ -190,11 +190,12 @@ struct gpu_light_args
 // pixel through camera::set_pixel (camera.h:281), so clip_image_to_rgb and
 // the image writers work unchanged.  vertex_colours: 3 floats per vertex of
 // the store in triangle order (a, b, c of triangle 0, then triangle 1, ...),
-// nullable.
+// nullable.  rf, tran, ri: the material's reflectivity, transparency and
+// refractive index (coloured_mapper_shader's rf, tran, ri).
 inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_light_args> &lights,
                            const gpu_camera_args &cam_args, camera &c, const ext_colour_t &ka, const ext_colour_t &kd,
                            const ext_colour_t &ks, const float ns, const float *vertex_colours = nullptr,
-                           const float rf = 0.0f)
+                           const float rf = 0.0f, const float tran = 0.0f, const float ri = 1.0f)
 {
     rt_camera cam;
     const point_t<> *ax[4] = { &cam_args.position, &cam_args.x_axis, &cam_args.y_axis, &cam_args.z_axis };
@@ -219,6 +220,9 @@ inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_lig
     m.ks[0] = ks.r; m.ks[1] = ks.g; m.ks[2] = ks.b;
     m.ns = ns;
     m.rf = rf;
+    m.tran = tran;
+    m.ri = ri;
+    m.flags = 0u;
     rt_scene *s = accel->scene();
     if (vertex_colours)
     {

@@ -226,6 +226,41 @@ def icosphere_scene(freq: int = 32, seed: int = 0, res: int = 512, ground: bool 
     return scene, frame
 
 
+def glass_scene(freq: int = 8, res: int = 64, tran: float = 0.6, ri: float = 1.5, rf_glass: float = 0.2,
+                rf_ground: float = 0.3, seed: int = 0):
+    """A glass sphere (r = 1 at the origin, material 1: transparency `tran`,
+    refractive index `ri`, reflectivity `rf_glass`, a flat kd that ignores
+    the vertex colours, triangles flagged transparent so shadow rays pass)
+    in front of an opaque sphere (r = 0.6 at (0.4, -0.2, -2.5)), both on a
+    40 x 40 ground at y = -1 of reflectivity `rf_ground` (material 0).
+    Camera at (0.3, 0.8, 4) looking at (0, -0.2, 0), 50 deg vertical FOV, sky
+    background; a point light at (3, 5, 3) and a dimmer directional light.
+    The scene dict carries `mat_of_tri`, the frame its `materials` table."""
+    v1, t1 = geodesic_sphere(freq)
+    v2, t2 = geodesic_sphere(freq)
+    v2 = v2 * 0.6 + np.array([0.4, -0.2, -2.5])
+    g = np.array([[-20, -1, -20], [20, -1, -20], [20, -1, 20], [-20, -1, 20]], np.float64)
+    tg = np.array([[0, 2, 1], [0, 3, 2]])
+    verts = np.concatenate([v1, v2, g])
+    tris = np.concatenate([t1, t2 + len(v1), tg + len(v1) + len(v2)]).astype(np.int32)
+    rng = np.random.default_rng(seed)
+    vattr = rng.uniform(0.0, 1.0, (len(verts), 3))
+    flags = np.zeros(len(tris), np.uint32)
+    flags[:len(t1)] = 2
+    mat_of_tri = np.zeros(len(tris), np.int32)
+    mat_of_tri[:len(t1)] = 1
+    scene = _pack(verts, tris, vattr, flags)
+    scene["mat_of_tri"] = mat_of_tri
+    base = dict(DEFAULT_MATERIAL)
+    mats = [dict(base, rf=rf_ground),
+            dict(base, kd=(30.0, 30.0, 40.0), tran=tran, ri=ri, rf=rf_glass, flags=1)]
+    cam = look_at_camera((0.3, 0.8, 4.0), (0.0, -0.2, 0.0), 50.0, res, res, background=(110.0, 160.0, 230.0))
+    frame = {"camera": cam,
+             "lights": [point_light((3.0, 5.0, 3.0)), directional_light((-0.4, -0.8, -0.3), rgb=(80.0, 80.0, 90.0))],
+             "materials": mats, "material": mats[0]}
+    return scene, frame
+
+
 def terrain_scene(size_pow2: int = 1024, roughness: float = 0.55, seed: int = 1, xres: int = 1920,
                   yres: int = 1080, extent: float = 1024.0, height: float = 200.0, crop: int = 0):
     """Diamond-square terrain over extent^2 with heights in [0, height]

@@ -95,6 +95,10 @@ def parse_morton_tests(path):
 
 AA_FACTORS = ((2, 2), (3, 2))
 REFLECTIVITY = {"ico": 0.5, "terrain": 0.35}
+# glass-sphere frames (scenes.glass_scene keyword arguments): refraction with
+# and without reflections, an index of 1, total internal reflection (2.4)
+GLASS = ({}, {"ri": 1.0}, {"ri": 1.33, "tran": 0.9, "rf_glass": 0.0},
+         {"ri": 2.4, "tran": 0.5, "rf_glass": 0.5, "rf_ground": 0.0})
 
 
 def small_scenes():
@@ -161,6 +165,12 @@ def main():
         arrays[f"{key}_refl_rf"] = np.array([REFLECTIVITY[key]], np.float32)
         arrays[f"{key}_refl_rgb"] = O.RefScene(s, mat).render(fr)["rgb"]
         arrays[f"{key}_frame"] = np.frombuffer(json.dumps(f).encode(), dtype=np.uint8)
+    # per-triangle materials with refraction: the glass sphere
+    from raptor_gb300 import scenes
+    for k, kw in enumerate(GLASS):
+        s, f = scenes.glass_scene(**kw)
+        arrays[f"glass{k}_rgb"] = O.RefScene(s, f["materials"]).render(f)["rgb"]
+        arrays[f"glass{k}_args"] = np.frombuffer(json.dumps(kw).encode(), dtype=np.uint8)
     s, o, d, tmax = soup()
     rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))
     ids, t, u, v = rs.closest(o, d)

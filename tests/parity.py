@@ -78,3 +78,17 @@ def aa_edge_pixels(oracle, scene, frame, aa_x, aa_y):
         for a_y in range(aa_y):
             out |= near[a_y::aa_y, a_x::aa_x][:H, :W]
     return out
+
+
+def glass_cases():
+    """(k, keyword arguments of scenes.glass_scene) of the glass-sphere
+    frames stored in the golden fixture (keys glass{k}_rgb, glass{k}_args)."""
+    import json
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_small.npz"))
+    out = []
+    k = 0
+    while f"glass{k}_args" in g.files:
+        out.append((k, json.loads(g[f"glass{k}_args"].tobytes().decode())))
+        k += 1
+    return out

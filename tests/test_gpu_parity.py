@@ -2,6 +2,7 @@
 oracle: the reference's own known-answer tests, reference outputs on small
 scenes, and the oracle on the benchmark workloads at sizes it finishes in
 seconds.  Criteria in tests/parity.py."""
+import ctypes as C
 import json
 import os
 
@@ -9,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import PIX_FRAC, compare_hits, edge_distance, pixel_agreement
+from parity import PIX_FRAC, compare_hits, edge_distance, glass_cases, pixel_agreement
 
 pytestmark = pytest.mark.gpu
 
@@ -653,23 +654,93 @@ def test_reflections_vs_reference_and_oracle(rtlib, ctx, oracle, golden, key):
 
 def test_reflectivity_limits(rtlib, ctx):
     """rf >= 1 never decays and rf whose chain needs more than RT_MAX_BOUNCES
-    bounces are refused; the entry points without mirror rays refuse rf > 0."""
-    torch = pytest.importorskip("torch")
+    bounces are refused; so are trees of more than RT_MAX_TREE_RAYS rays and
+    refracting materials without a usable index; the entry points without
+    secondary rays refuse rf > 0 and tran > 0."""
     from raptor_gb300 import scenes
     scene, frame = scenes.icosphere_scene(freq=4, res=32)
     sc = rtlib.Scene(ctx, scene)
-    for rf in (1.0, 0.97, -0.2):
-        f = dict(frame, material=dict(frame["material"], rf=rf))
+    m0 = frame["material"]
+    bad = [dict(m0, rf=1.0), dict(m0, rf=0.94), dict(m0, rf=-0.2), dict(m0, tran=1.0), dict(m0, tran=-0.1),
+           dict(m0, rf=0.8, tran=0.8),              # 2047 rays per pixel
+           dict(m0, tran=0.5, ri=0.0), dict(m0, tran=0.5, ri=float("inf"))]
+    for m in bad:
         with pytest.raises(rtlib.RtError):
-            sc.render(f)
-    f = dict(frame, material=dict(frame["material"], rf=0.96))   # 56 bounces: allowed
-    sc.render(f)
-    f = dict(frame, material=dict(frame["material"], rf=0.5))
+            sc.render(dict(frame, material=m))
+    for m in (dict(m0, rf=0.93),                    # 31 bounces: allowed
+              dict(m0, rf=0.7, tran=0.7, ri=1.2),   # 127 rays
+              dict(m0, tran=0.93, ri=1.0)):
+        sc.render(dict(frame, material=m))
+    # a table is bounded by its largest rf and largest tran together
     with pytest.raises(rtlib.RtError):
-        sc.render_aa(f, 2, 2)
-    fao = dict(f, ao={"samples": 4, "dist": 1.0, "seed": 1})
+        sc.render(dict(frame, materials=[dict(m0, rf=0.8), dict(m0, tran=0.8, ri=1.5)]))
     with pytest.raises(rtlib.RtError):
-        sc.render(fao)
+        sc.render(dict(frame, materials=[m0] * 17))
+    for m in (dict(m0, rf=0.5), dict(m0, tran=0.5, ri=1.5)):
+        f = dict(frame, material=m)
+        with pytest.raises(rtlib.RtError):
+            sc.render_aa(f, 2, 2)
+        with pytest.raises(rtlib.RtError):
+            sc.render(dict(f, ao={"samples": 4, "dist": 1.0, "seed": 1}))
+    sc.close()
+
+
+@pytest.mark.parametrize("case", glass_cases(), ids=lambda c: f"glass{c[0]}")
+def test_refraction_vs_reference_and_oracle(rtlib, ctx, oracle, golden, case):
+    """rt_render_materials on a glass sphere (refraction with ri inverted on
+    entry, total internal reflection for ri 2.4, mirror rays on the glass and
+    the ground, per-triangle materials): the frame equals the restatement's
+    and the reference's own on all but a few edge pixels."""
+    from raptor_gb300 import scenes
+    k, kw = case
+    scene, frame = scenes.glass_scene(**kw)
+    sc = rtlib.Scene(ctx, scene)
+    r = sc.render(frame, want_ids=True)
+    o = oracle.OracleScene(scene).render(frame, want_ids=True)
+    within1, exact, _ = pixel_agreement(r["rgb"], o["rgb"])
+    assert exact >= 0.998, exact
+    assert (r["ids"] == o["ids"]).mean() >= 0.998
+    within1, exact, _ = pixel_agreement(r["rgb"], golden[f"glass{k}_rgb"])
+    assert exact >= 0.995, exact
+    assert r["stats"].secondary_rays > 2 * r["stats"].primary_hits    # shadow + mirror + refracted rays
+    sc.close()
+
+
+def test_materials_per_triangle(rtlib, ctx, oracle):
+    """Per-triangle material indices from host and from device memory give
+    the oracle's frame; indices outside 0..RT_MAX_MATERIALS-1 or beyond the
+    table are refused; clearing them returns every triangle to material 0."""
+    torch = pytest.importorskip("torch")
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=12, res=96)
+    nt = scene["tris"].shape[0]
+    rng = np.random.default_rng(5)
+    mat = rng.integers(0, 4, nt).astype(np.int32)
+    m0 = frame["material"]
+    table = [dict(m0, kd=(204.0, 60.0, 60.0)), dict(m0, kd=(60.0, 204.0, 60.0), rf=0.4),
+             dict(m0, kd=(60.0, 60.0, 204.0), ns=5.0, flags=1), dict(m0, ka=(5.0, 5.0, 5.0), ks=(0.0, 0.0, 0.0))]
+    f = dict(frame, materials=table)
+    want = oracle.OracleScene(dict(scene, mat_of_tri=mat)).render(f)["rgb"]
+    sc = rtlib.Scene(ctx, scene)
+    sc.set_materials(mat)
+    got = sc.render(f)["rgb"]
+    assert pixel_agreement(got, want)[1] >= 0.998
+    d_mat = torch.from_numpy(mat).cuda()
+    _check = rtlib.lib().rt_scene_set_materials
+    assert _check(sc.h, C.c_void_p(d_mat.data_ptr()), nt) == 0
+    assert np.array_equal(sc.render(f)["rgb"], got)
+    with pytest.raises(rtlib.RtError):      # index 3 set, table of 3
+        sc.render(dict(frame, materials=table[:3]))
+    for badv in (-1, 16):
+        bad = mat.copy()
+        bad[nt // 2] = badv
+        with pytest.raises(rtlib.RtError):
+            sc.set_materials(bad)
+        d_bad = torch.from_numpy(bad).cuda()
+        assert _check(sc.h, C.c_void_p(d_bad.data_ptr()), nt) != 0
+    assert _check(sc.h, None, 0) == 0
+    plain = sc.render(dict(frame, materials=table[:1]))["rgb"]
+    assert np.array_equal(plain, sc.render(dict(frame, material=table[0]))["rgb"])
     sc.close()
 
 

@@ -1,6 +1,7 @@
 """Randomised parity sweep: seeded random scenes (triangle soups with light
 and transparent flags, spheres, heightfields), random cameras, light mixes and
-materials; every frame, hit-id map and a batch of random rays is compared
+materials (tables of refracting and reflecting materials indexed per
+triangle on odd seeds); every frame, hit-id map and a batch of random rays is compared
 with the oracle under the parity rules of tests/parity.py."""
 import numpy as np
 import pytest
@@ -48,7 +49,21 @@ def random_case(seed):
     mat = {"ka": tuple(float(x) for x in rng.uniform(0, 60, 3)), "kd": tuple(float(x) for x in rng.uniform(0, 255, 3)),
            "ks": tuple(float(x) for x in rng.uniform(0, 255, 3)), "ns": float(rng.uniform(1, 60)),
            "rf": float(rng.choice([0.0, 0.0, 0.3, 0.6]))}
-    return scene, {"camera": cam, "lights": lights, "material": mat}, rng
+    frame = {"camera": cam, "lights": lights, "material": mat}
+    if seed % 2 == 1:
+        # a table of 1-4 materials, some refracting, indexed per triangle
+        table = []
+        for _ in range(int(rng.integers(1, 5))):
+            table.append(dict(mat, kd=tuple(float(x) for x in rng.uniform(0, 255, 3)),
+                              rf=float(rng.choice([0.0, 0.3, 0.6])), tran=float(rng.choice([0.0, 0.4, 0.7])),
+                              ri=float(rng.uniform(0.8, 2.2)), flags=int(rng.integers(0, 2))))
+        scene["mat_of_tri"] = rng.integers(0, len(table), scene["tris"].shape[0]).astype(np.int32)
+        frame["materials"] = table
+        # shadow rays pass the triangles of refracting materials (the
+        # reference's material::is_transparent, set when tran > 0)
+        see_through = np.array([m["tran"] > 0.0 for m in table])[scene["mat_of_tri"]]
+        scene["flags"] = (scene["flags"] & np.uint32(1)) | np.where(see_through, np.uint32(2), np.uint32(0))
+    return scene, frame, rng
 
 
 @pytest.mark.parametrize("seed", range(24))

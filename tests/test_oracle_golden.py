@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import PIX_FRAC, compare_hits, pixel_agreement
+from parity import PIX_FRAC, compare_hits, glass_cases, pixel_agreement
 
 FLT_MAX = np.float32(3.4028234663852886e38)
 
@@ -176,3 +176,22 @@ def test_oracle_reflections_match_reference(oracle, golden, key):
     assert exact >= 0.998, exact
     plain = sc.render(frame_of(g, key))["rgb"]
     assert (np.abs(out.astype(int) - plain.astype(int)).max(-1) > 0).mean() > 0.1   # reflections visible
+
+
+@pytest.mark.parametrize("case", glass_cases(), ids=lambda c: f"glass{c[0]}")
+def test_oracle_refraction_matches_reference(oracle, golden, case):
+    """Per-triangle materials with refraction (the shader's tran and ri,
+    ray::refract): a glass sphere before an opaque one on a reflective
+    ground.  The restatement's frame equals the reference's pixel for
+    pixel; the refracted rays change a visible part of the frame."""
+    from raptor_gb300 import scenes
+    k, kw = case
+    scene, frame = scenes.glass_scene(**kw)
+    sc = oracle.OracleScene(scene)
+    out = sc.render(frame)["rgb"]
+    ref = golden[f"glass{k}_rgb"]
+    within1, exact, _ = pixel_agreement(out, ref)
+    assert exact >= 0.999, exact
+    opaque = dict(frame, materials=[dict(m, tran=0.0, rf=0.0) for m in frame["materials"]])
+    plain = sc.render(opaque)["rgb"]
+    assert (np.abs(out.astype(int) - plain.astype(int)).max(-1) > 0).mean() > 0.05

@@ -38,3 +38,16 @@ def test_full_frame_restatement_equals_reference(ref, workload):
     assert not mismatch.any()
     same = oid == rid
     assert np.array_equal(ot[same].view(np.uint32), rt[same].view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", range(1, 24, 2))
+def test_random_material_tables_equal_reference(ref, seed):
+    """The randomised scenes with per-triangle material tables (reflecting
+    and refracting entries): the restatement's frame equals the reference's
+    on every pixel."""
+    from test_gpu_random_scenes import random_case
+    scene, frame, _ = random_case(seed)
+    rr = ref.RefScene(scene, frame["materials"]).render(frame)
+    ro = ref.OracleScene(scene).render(frame)
+    within1, exact, _ = pixel_agreement(ro["rgb"], rr["rgb"])
+    assert exact == 1.0, (exact, within1)
