@@ -260,6 +260,7 @@ WORKLOADS = {
     "icosphere-20k-512": ("workload_icosphere", True, lambda k: max(5, k)),
     "icosphere-20k-512-mirror": ("workload_icosphere_mirror", True, lambda k: max(5, k)),
     "glass-41k-512": ("workload_glass", True, lambda k: max(5, k)),
+    "terrain-2M-1080p-tonemap": ("workload_terrain_tonemap", True, lambda k: max(3, k // 4)),
     "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
     "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
     "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
@@ -507,6 +508,28 @@ def workload_glass(ctx, stream, flush, steps):
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512],
             "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_terrain_tonemap(ctx, stream, flush, steps):
+    """The headline terrain frame (2,097,152 triangles, 1920x1080) through the
+    framebuffer epilogue: float frame, exposure tone mapping (key 0.18) and
+    sRGB gamma, then RGB8; the plain frame beside it."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.terrain_scene()
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((1080, 1920, 3), dtype=torch.uint8, device="cuda")
+    tone = {"mode": 5, "gamma": 2.2}
+    out = {"triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080], "tone": tone}
+    for key, fn in (("plain", lambda: sc.render(frame, rgb=rgb)["stats"]),
+                    ("tone_mapped", lambda: sc.render_tone_mapped(frame, tone, rgb=rgb)["stats"])):
+        for _ in range(3):
+            fn()
+        secs, st = time_frames(fn, steps, stream, flush)
+        out[key] = {"ms_per_frame": secs / steps * 1e3,
+                    "Grays_s": (st.primary_rays + st.secondary_rays) * steps / secs / 1e9}
+    sc.close()
+    return out
 
 
 def workload_terrain_1m(ctx, stream, flush, steps):

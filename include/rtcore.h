@@ -295,6 +295,49 @@ rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt
                               const rt_material *materials, int32_t nmaterials, uint8_t *rgb_out, int32_t *hit_ids,
                               rt_render_stats *stats);
 
+/* Framebuffer epilogue: the reference's global tone mapping
+ * (camera::tone_map, raytracer/camera.cc:1124-1463, with glare and temporal
+ * adaptation off; mode values of tone_mapping_mode_t, camera.h:43-45) and
+ * gamma correction (camera::gamma_correct, camera.cc:1466-1500).  key, xw,
+ * yw, desaturate and stretch are tone_map's key, xw, yw, ds and sc (its
+ * defaults: 0.18, 1/3, 1/3, 0, 0); gamma > 0 applies gamma_correct(gamma)
+ * after tone mapping (2.2 selects the sRGB curve, as in the reference), 0
+ * none. */
+#define RT_TONE_NONE 0
+#define RT_TONE_GLOBAL_CONTRAST 1
+#define RT_TONE_GLOBAL_NON_LINEAR 4
+#define RT_TONE_GLOBAL_EXPOSURE 5
+#define RT_TONE_GLOBAL_AVG_LUMINANCE 6
+#define RT_TONE_GLOBAL_MAX_LUMINANCE 7
+#define RT_TONE_GLOBAL_FERWERDA 9
+typedef struct rt_tone_map {
+    int32_t mode;
+    float key, xw, yw;
+    int32_t desaturate, stretch;
+    float gamma;
+} rt_tone_map;
+
+/* A frame of rt_render_materials traced on the anti-aliased grid (aa_x *
+ * aa_y rays per output pixel, 1..16 each), kept as floats, tone mapped and
+ * gamma corrected as a whole (tone NULL: neither), then averaged per output
+ * pixel, clamped and truncated to RGB8 (camera::clip_image_to_rgb,
+ * camera.h:289-319).  Replaces ray_tracer + camera::tone_map +
+ * camera::gamma_correct + clip_image_to_rgb.  The luminance statistics of
+ * the tone mappers are summed in double where the reference sums binary32
+ * in pixel order, so frames may differ from the reference's by one level in
+ * a few pixels. */
+rt_status rt_render_tone_mapped(rt_scene *scene, const rt_camera *camera, int32_t aa_x, int32_t aa_y,
+                                const rt_light *lights, int32_t nlights, const rt_material *materials,
+                                int32_t nmaterials, const rt_tone_map *tone, uint8_t *rgb_out,
+                                rt_render_stats *stats);
+
+/* The binary32 sum of values[0..n) in index order, rounded after every
+ * addition exactly as a sequential loop `s += values[i]` rounds it (the way
+ * camera::tone_map accumulates its log-luminance, camera.cc:1158), computed
+ * on the GPU; rt_render_tone_mapped uses the same machinery.  values: host
+ * or device, finite. */
+rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n, float *sum_out);
+
 /* Anti-aliased frame: aa_x * aa_y rays per output pixel on the supersampled
  * camera grid (xres * aa_x by yres * aa_y), each shaded as by rt_render, and
  * their colours averaged into the xres * yres RGB8 output.  Replaces the

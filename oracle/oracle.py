@@ -37,6 +37,26 @@ class Material(C.Structure):
                 ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
 
 
+class ToneMap(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("key", C.c_float), ("xw", C.c_float), ("yw", C.c_float),
+                ("desaturate", C.c_int32), ("stretch", C.c_int32), ("gamma", C.c_float)]
+
+
+def make_tone_map(d):
+    """Tone-map dict -> ToneMap; the defaults are camera::tone_map's
+    (key 0.18, white point 1/3, 1/3, no desaturation or stretch) and no
+    gamma correction."""
+    t = ToneMap()
+    t.mode = d.get("mode", 0)
+    t.key = d.get("key", 0.18)
+    t.xw = d.get("xw", float(np.float32(1.0) / np.float32(3.0)))
+    t.yw = d.get("yw", float(np.float32(1.0) / np.float32(3.0)))
+    t.desaturate = int(bool(d.get("desaturate", False)))
+    t.stretch = int(bool(d.get("stretch", False)))
+    t.gamma = d.get("gamma", 0.0)
+    return t
+
+
 def make_camera(d):
     c = Camera()
     for k in ("pos", "x_axis", "y_axis", "z_axis", "background"):
@@ -178,6 +198,8 @@ def oracle_lib():
                                         _U8, _F]
         lib["ro_scene_set_materials"].restype = C.c_int32
         lib["ro_scene_set_materials"].argtypes = [C.c_void_p, _I]
+        lib["ro_tone_map_frame"].restype = C.c_int32
+        lib["ro_tone_map_frame"].argtypes = [_F, C.c_int32, C.c_int32, C.POINTER(ToneMap)]
         lib["ro_render_ao"].restype = C.c_int64
         lib["ro_render_ao"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Material), C.c_int32, C.c_float,
                                         C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _U8, _I, _I]
@@ -206,6 +228,9 @@ def ref_lib():
         lib["rref_render_aa"].restype = C.c_double
         lib["rref_render_aa"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32, C.POINTER(Light),
                                           C.c_int32, _U8]
+        lib["rref_render_tone_mapped"].restype = C.c_double
+        lib["rref_render_tone_mapped"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32,
+                                                   C.POINTER(Light), C.c_int32, C.POINTER(ToneMap), _U8]
         _ref = lib
     return _ref
 
@@ -300,14 +325,21 @@ class RefScene(_SceneBase):
                                                    _p(a, C.c_float), _p(f, C.c_uint32), C.byref(self.mat))
         self.build_seconds = self.lib["rref_scene_build"](self.h)
 
-    def render(self, frame, aa=(1, 1)):
+    def render(self, frame, aa=(1, 1), tone=None):
         """ray_tracer + clip_image_to_rgb; aa = (x_a_res, y_a_res) rays per
-        output pixel along x and y (the camera's anti-aliasing factors)."""
+        output pixel along x and y (the camera's anti-aliasing factors);
+        tone: a tone-map dict (camera::tone_map + gamma_correct before the
+        clip) or None."""
         cam = make_camera(frame["camera"])
         rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
         ls = make_lights(frame["lights"])
-        secs = self.lib["rref_render_aa"](self.h, C.byref(cam), int(aa[0]), int(aa[1]), ls, len(frame["lights"]),
-                                          _p(rgb, C.c_uint8))
+        if tone is None:
+            secs = self.lib["rref_render_aa"](self.h, C.byref(cam), int(aa[0]), int(aa[1]), ls,
+                                              len(frame["lights"]), _p(rgb, C.c_uint8))
+        else:
+            tm = make_tone_map(tone)
+            secs = self.lib["rref_render_tone_mapped"](self.h, C.byref(cam), int(aa[0]), int(aa[1]), ls,
+                                                       len(frame["lights"]), C.byref(tm), _p(rgb, C.c_uint8))
         return {"rgb": rgb, "seconds": secs}
 
 
@@ -342,6 +374,23 @@ def render_aa(scene_obj, frame, aa_x, aa_y):
     OracleScene.render, then downsample_rgb8."""
     out = scene_obj.render(supersampled(frame, aa_x, aa_y), want_float=True)
     return downsample_rgb8(out["fimg"], aa_x, aa_y)
+
+
+def tone_map_frame(fimg, tone):
+    """camera::tone_map + gamma_correct restated (ro_tone_map_frame) on a
+    copy of a float frame (rows = y, 0..255 colours)."""
+    img = np.array(fimg, np.float32, order="C", copy=True)
+    tm = make_tone_map(tone)
+    if oracle_lib()["ro_tone_map_frame"](_p(img, C.c_float), img.shape[1], img.shape[0], C.byref(tm)) != 0:
+        raise ValueError("unsupported tone-mapping mode")
+    return img
+
+
+def render_tone_mapped(scene_obj, frame, tone, aa=(1, 1)):
+    """Tone-mapped (anti-aliased) frame by the restatement: the supersampled
+    float image, tone_map_frame, then downsample_rgb8."""
+    out = scene_obj.render(supersampled(frame, *aa), want_float=True)
+    return downsample_rgb8(tone_map_frame(out["fimg"], tone), *aa)
 
 
 def camera_rays(cam_dict, x0=0, y0=0, w=None, h=None, lib=None):

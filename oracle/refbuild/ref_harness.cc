@@ -206,8 +206,12 @@ double rref_render(void *h, const ro_camera *c, const ro_light *ls, int32_t nl, 
     return rref_render_aa(h, c, 1, 1, ls, nl, rgb);
 }
 
-double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
-                      uint8_t *rgb)
+// The frame of rref_render_aa, tone mapped by the reference's
+// camera::tone_map (camera.cc:1124) with glare and temporal adaptation off,
+// then camera::gamma_correct (camera.cc:1466) when tm->gamma > 0, before
+// clip_image_to_rgb.  tm NULL: neither.
+double rref_render_tone_mapped(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls,
+                               int32_t nl, const ro_tone_map *tm, uint8_t *rgb)
 {
     auto *s = static_cast<ref_scene *>(h);
     std::unique_ptr<camera> cam(make_camera(c, (unsigned)aa_x, (unsigned)aa_y));
@@ -223,10 +227,21 @@ double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, c
     std::streambuf *old = std::cout.rdbuf(&nb);
     const auto t0 = std::chrono::steady_clock::now();
     ray_tracer(s->accel.get(), lights, s->store, *cam);
+    if (tm) {
+        cam->tone_map(static_cast<tone_mapping_mode_t>(tm->mode), tm->key, tm->xw, tm->yw, false, false,
+                      tm->desaturate != 0, tm->stretch != 0);
+        if (tm->gamma > 0.0f) cam->gamma_correct(tm->gamma);
+    }
     const auto t1 = std::chrono::steady_clock::now();
     std::cout.rdbuf(old);
     cam->clip_image_to_rgb(rgb);
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
+                      uint8_t *rgb)
+{
+    return rref_render_tone_mapped(h, c, aa_x, aa_y, ls, nl, nullptr, rgb);
 }
 
 int32_t rref_morton_code(float x, float y, float z, float xm, float ym, float zm)

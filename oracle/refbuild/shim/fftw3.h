@@ -1,0 +1,20 @@
+// Declaration-only stand-in for FFTW (single precision).  The reference's
+// camera.cc uses it for its glare filter, which the harness never enables;
+// io_stubs.cc defines the names so the library loads.
+#pragma once
+#include <cstddef>
+typedef float fftwf_complex[2];
+typedef struct fftwf_plan_s *fftwf_plan;
+#define FFTW_FORWARD (-1)
+#define FFTW_BACKWARD (+1)
+#define FFTW_ESTIMATE (1U << 6)
+extern "C" {
+void *fftwf_malloc(size_t n);
+void fftwf_free(void *p);
+void fftwf_execute(const fftwf_plan p);
+void fftwf_destroy_plan(fftwf_plan p);
+fftwf_plan fftwf_plan_dft_2d(int n0, int n1, fftwf_complex *in, fftwf_complex *out, int sign, unsigned flags);
+fftwf_plan fftwf_plan_dft_r2c_3d(int n0, int n1, int n2, float *in, fftwf_complex *out, unsigned flags);
+fftwf_plan fftwf_plan_many_dft_r2c(int rank, const int *n, int howmany, float *in, const int *inembed, int istride, int idist, fftwf_complex *out, const int *onembed, int ostride, int odist, unsigned flags);
+fftwf_plan fftwf_plan_many_dft_c2r(int rank, const int *n, int howmany, fftwf_complex *in, const int *inembed, int istride, int idist, float *out, const int *onembed, int ostride, int odist, unsigned flags);
+}

@@ -1,5 +1,6 @@
-// Declaration-only stand-in for libpng. The reference's inline image readers
-// reference these names; they are never called on the traced path.
+// Declaration-only stand-in for libpng. The reference's image readers and
+// writers (texture_mapper.h, camera.cc) reference these names; they are never
+// called on the traced path (io_stubs.cc defines them so the library loads).
 #pragma once
 #include <cstdio>
 #include <csetjmp>
@@ -34,3 +35,10 @@ void png_read_update_info(png_structp, png_infop);
 png_size_t png_get_rowbytes(png_structp, png_infop);
 void png_read_image(png_structp, png_bytepp);
 void png_destroy_read_struct(png_structpp, png_infopp, png_infopp);
+#define PNG_COMPRESSION_TYPE_DEFAULT 0
+#define PNG_FILTER_TYPE_DEFAULT 0
+void png_destroy_write_struct(png_structpp, png_infopp);
+void png_set_IHDR(png_structp, png_infop, png_uint_32, png_uint_32, int, int, int, int, int);
+void png_write_info(png_structp, png_infop);
+void png_write_image(png_structp, png_bytepp);
+void png_write_end(png_structp, png_infop);

@@ -891,3 +891,161 @@ void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pi
         dir[3 * s] = dn.x; dir[3 * s + 1] = dn.y; dir[3 * s + 2] = dn.z;
     }
 }
+
+/* ------------------------------------------------------ Tone mapping */
+
+/* RGB -> CIE XYZ rows and scotopic weights of camera::tone_map
+ * (camera.cc:1127-1130). */
+static const float TM_XB[3] = {0.4124f, 0.3576f, 0.1805f};
+static const float TM_YB[3] = {0.2126f, 0.7151f, 0.0721f};
+static const float TM_ZB[3] = {0.0193f, 0.1192f, 0.9505f};
+static const float TM_VB[3] = {0.01477f, 0.497f, 0.631f};
+
+int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *tm)
+{
+    const int32_t mode = tm->mode;
+    if (!(mode == 0 || mode == 1 || mode == 4 || mode == 5 || mode == 6 || mode == 7 || mode == 9)) return -1;
+    const int32_t n = w * h;
+    /* first pass: to CIE Yxy, log-average and maximum luminance */
+    float Yi = 0.0f, maxY = 0.0f, rgbAvg = 0.0f;
+    int numpix = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        float *p = img + 3 * (size_t)i;
+        const float r = p[0] / 255.0f, g = p[1] / 255.0f, b = p[2] / 255.0f;
+        if (mode == 5) rgbAvg += (r + g + b) * (1.0f / 3.0f);
+        const float X = 683.0f * (((TM_XB[0] * r) + (TM_XB[1] * g)) + (TM_XB[2] * b));
+        float Y = 683.0f * (((TM_YB[0] * r) + (TM_YB[1] * g)) + (TM_YB[2] * b));
+        const float Z = 683.0f * (((TM_ZB[0] * r) + (TM_ZB[1] * g)) + (TM_ZB[2] * b));
+        if (Y < 3.18e-7f) {
+            Y = 3.18e-7f;
+        } else {
+            numpix++;
+            maxY = smax(maxY, Y);
+            Yi += log10f(Y);
+        }
+        const float W = (Y + X) + Z;
+        float x = X / W, y = Y / W;
+        if (tm->desaturate) {
+            float s;
+            const float l = log10f(Y);
+            if (l < -2.0f) {
+                s = 0.0f;
+            } else if (l < 0.6f) {
+                const float q = (l + 2.0f) / 2.6f;
+                const float q2 = q * q;
+                s = (3.0f * q2) - ((2.0f * q) * q2);
+            } else {
+                s = 1.0f;
+            }
+            const float V = 1700.0f * (((TM_VB[0] * r) + (TM_VB[1] * g)) + (TM_VB[2] * b));
+            x = ((1.0f - s) * tm->xw) + (s * ((x + tm->xw) - (1.0f / 3.0f)));
+            y = ((1.0f - s) * tm->yw) + (s * ((y + tm->yw) - (1.0f / 3.0f)));
+            Y = ((0.4468f * (1.0f - s)) * V) + (s * Y);
+        }
+        p[0] = x;
+        p[1] = Y;
+        p[2] = y;
+    }
+    if (numpix) Yi /= (float)numpix;
+    rgbAvg /= (float)(uint32_t)n;
+    Yi = powf(10.0f, Yi);
+    /* luminance scaling by mode (camera.cc:1276-1425) */
+    const float key = tm->key;
+    if (mode == 1) {
+        const float Yw = 300.0f;
+        const float num = 1.219f + powf(Yw * 0.5f, 0.4f);
+        const float den = 1.219f + powf(Yi, 0.4f);
+        const float sf = (1.0f / Yw) * powf(num / den, 2.5f);
+        for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
+    } else if (mode == 4) {
+        const float sf = key / Yi;
+        maxY *= sf;
+        maxY = 1.0f / (maxY * maxY);
+        for (int32_t i = 0; i < n; ++i) {
+            float g = img[3 * (size_t)i + 1] * sf;
+            if (maxY != 0.0f) g *= (1.0f + (g * maxY)) / (1.0f + g);
+            img[3 * (size_t)i + 1] = g;
+        }
+    } else if (mode == 5) {
+        const float sf = key / Yi;
+        maxY *= sf;
+        for (int32_t i = 0; i < n; ++i) {
+            float g = img[3 * (size_t)i + 1] * sf;
+            if (maxY != 0.0f) g = 1.0f - expf(-g);
+            img[3 * (size_t)i + 1] = g;
+        }
+    } else if (mode == 6) {
+        /* rgbAvg is only accumulated in exposure mode (camera.cc:1142), so
+         * here it is 0 and the scale stays 1, as in the reference */
+        float sf = 1.0f;
+        if (rgbAvg != 0.0f) sf *= key * (0.5f / (rgbAvg * 683.0f));
+        for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
+    } else if (mode == 7) {
+        const float sf = key / maxY;
+        for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
+    } else if (mode == 9) {
+        const float lda = 800.0f;
+        const float log_lda = logf(lda * 0.5f);
+        const float log_la = logf(Yi);
+        float tp, ts, k;
+        if (log_la <= -2.6f) tp = -0.72f;
+        else if (log_la <= 1.9f) tp = powf((0.249f * log_la) + 0.65f, 2.7f) - 0.72f;
+        else tp = log_la - 1.255f;
+        const float mp = (log_lda - 1.255f) / tp;
+        if (log_la <= -3.94f) ts = -2.86f;
+        else if (log_la < -1.44f) ts = powf((0.405f * log_la) + 1.6f, 2.18f) - 2.86f;
+        else ts = log_la - 0.395f;
+        const float ms = (log_lda - 1.255f) / ts;
+        if (log_la < -2.0f) k = 1.0f;
+        else if (log_la < 1.0f) k = 1.0f - ((log_la + 2.0f) * (1.0f / 3.0f));
+        else k = 0.0f;
+        for (int32_t i = 0; i < n; ++i) {
+            const float g = img[3 * (size_t)i + 1];
+            const float ldp = mp * g, lds = ms * g;
+            img[3 * (size_t)i + 1] = (1.0f / lda) * (ldp + (k * lds));
+        }
+    } else {
+        const float sf = 1.0f / 683.0f;
+        for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
+    }
+    /* contrast stretch (camera.cc:1428-1450) */
+    if (tm->stretch) {
+        float maxY2 = -RO_MAX_DIST, minY2 = RO_MAX_DIST;
+        for (int32_t i = 0; i < n; ++i) {
+            maxY2 = smax(maxY2, img[3 * (size_t)i + 1]);
+            minY2 = smin(minY2, img[3 * (size_t)i + 1]);
+        }
+        if (((minY2 > 0.0f) || (maxY2 < 0.0f)) && (minY2 < maxY2)) {
+            const float offset = smin(-minY2, 0.0f);
+            const float scale = 1.0f / (smin(1.0f, maxY2) - smax(0.0f, minY2));
+            for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] = (img[3 * (size_t)i + 1] + offset) * scale;
+        }
+    }
+    /* Yxy -> RGB in 0..255 (camera.cc:2080-2098), then gamma (camera.cc:1466-1500) */
+    for (int32_t i = 0; i < n; ++i) {
+        float *p = img + 3 * (size_t)i;
+        const float x = p[0], Y = p[1], y = p[2];
+        const float X = (x * Y) / y;
+        const float Z = (((1.0f - x) - y) * Y) / y;
+        float r = ((826.353f * X) + (-391.986f * Y)) + (-127.143f * Z);
+        float g = ((-247.0695f * X) + (478.329f * Y)) + (10.5825f * Z);
+        float b = ((14.2035f * X) + (-52.02f * Y)) + (269.535f * Z);
+        if (tm->gamma > 0.0f) {
+            const float gm = tm->gamma;
+            float c[3] = {r / 255.0f, g / 255.0f, b / 255.0f};
+            for (int k = 0; k < 3; ++k) {
+                c[k] = smin(smax(c[k], 0.0f), 1.0f);
+                if (fabsf(gm - 2.2f) > 0.001f) c[k] = powf(c[k], 1.0f / gm);
+                else if (fabsf(gm - 1.0f) > 0.001f)
+                    c[k] = (c[k] <= 0.0031308f) ? (12.92f * c[k]) : ((1.055f * powf(c[k], 1.0f / 2.4f)) - 0.055f);
+            }
+            r = c[0] * 255.0f;
+            g = c[1] * 255.0f;
+            b = c[2] * 255.0f;
+        }
+        p[0] = r;
+        p[1] = g;
+        p[2] = b;
+    }
+    return 0;
+}

@@ -140,6 +140,25 @@ void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pi
 /* Philox4x32-10 (Salmon et al., SC'11) keyed by (key0, key1) on counter ctr. */
 void ro_philox4x32(const uint32_t ctr[4], uint32_t key0, uint32_t key1, uint32_t out[4]);
 
+/* Tone-mapping parameters of camera::tone_map (raytracer/camera.h:378):
+ * mode is a tone_mapping_mode_t value (camera.h:43-45) of a global mode
+ * (0 none, 1 contrast, 4 non-linear, 5 exposure, 6 average luminance,
+ * 7 maximum luminance, 9 Ferwerda); key, xw, yw as the reference's
+ * arguments; desaturate / stretch its ds / sc flags (glare and temporal
+ * adaptation off); gamma > 0 applies camera::gamma_correct(gamma) after. */
+typedef struct ro_tone_map {
+    int32_t mode;
+    float key, xw, yw;
+    int32_t desaturate, stretch;
+    float gamma;
+} ro_tone_map;
+
+/* camera::tone_map (camera.cc:1124-1463) + convert_Yxy_to_rgb
+ * (camera.cc:2080-2098) + gamma_correct (camera.cc:1466-1500) in place on a
+ * w*h frame of 0..255 colours (3 floats per pixel, index x + y*w).
+ * Returns 0, or -1 for an unsupported mode. */
+int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *tm);
+
 #ifdef __cplusplus
 }
 #endif

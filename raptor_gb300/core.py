@@ -69,6 +69,11 @@ class RtMaterial(C.Structure):
                 ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
 
 
+class RtToneMap(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("key", C.c_float), ("xw", C.c_float), ("yw", C.c_float),
+                ("desaturate", C.c_int32), ("stretch", C.c_int32), ("gamma", C.c_float)]
+
+
 class RtRenderStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("secondary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("device_ms", C.c_float), ("status", C.c_int32), ("nodes_fetched", C.c_int64),
@@ -126,8 +131,12 @@ SIGNATURES = [
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
     ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
+    ("rt_sum_sequential_f32", C.c_int32, [_P, _P, C.c_int64, C.POINTER(C.c_float)]),
     ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
                                         C.POINTER(RtMaterial), C.c_int32, _P, _P, C.POINTER(RtRenderStats)]),
+    ("rt_render_tone_mapped", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight),
+                                          C.c_int32, C.POINTER(RtMaterial), C.c_int32, C.POINTER(RtToneMap), _P,
+                                          C.POINTER(RtRenderStats)]),
     ("rt_render_aa", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight), C.c_int32,
                                  C.POINTER(RtMaterial), _P, C.POINTER(RtRenderStats)]),
     ("rt_render_ao", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtMaterial), C.c_int32, C.c_float, C.c_uint32,
@@ -212,6 +221,20 @@ def make_material(d) -> RtMaterial:
     return m
 
 
+def make_tone_map(d) -> RtToneMap:
+    """Tone-map dict -> RtToneMap with camera::tone_map's defaults (key 0.18,
+    white point 1/3, 1/3, no desaturation or stretch) and no gamma."""
+    t = RtToneMap()
+    third = float(np.float32(1.0) / np.float32(3.0))
+    t.mode = d.get("mode", 0)
+    t.key = d.get("key", 0.18)
+    t.xw, t.yw = d.get("xw", third), d.get("yw", third)
+    t.desaturate = int(bool(d.get("desaturate", False)))
+    t.stretch = int(bool(d.get("stretch", False)))
+    t.gamma = d.get("gamma", 0.0)
+    return t
+
+
 def make_materials(ds):
     arr = (RtMaterial * len(ds))()
     for i, d in enumerate(ds):
@@ -248,6 +271,15 @@ class Context:
 
     def set_option(self, option: int, value: int):
         _check(lib().rt_ctx_set_option(self.h, option, value))
+
+    def sum_sequential(self, values) -> np.float32:
+        """The binary32 sum of values in index order, rounded as a
+        sequential loop rounds it (computed on the GPU)."""
+        v = np.ascontiguousarray(values, np.float32) if isinstance(values, np.ndarray) else values
+        out = C.c_float()
+        n = int(v.shape[0]) if hasattr(v, "shape") else len(v)
+        _check(lib().rt_sum_sequential_f32(self.h, ptr(v), n, C.byref(out)))
+        return np.float32(out.value)
 
     def close(self):
         if self.h:
@@ -360,6 +392,21 @@ class Scene:
             _check(lib().rt_render(self.h, C.byref(cam), ls, len(frame["lights"]), C.byref(mat), ptr(rgb), ptr(ids),
                                    C.byref(st)))
         return {"rgb": rgb, "ids": ids, "stats": st}
+
+    def render_tone_mapped(self, frame, tone=None, aa=(1, 1), rgb=None):
+        """Frame on the aa grid, tone mapped and gamma corrected (tone dict or
+        None), averaged to RGB8; frame["materials"] or frame["material"]."""
+        cam = make_camera(frame["camera"])
+        if rgb is None:
+            rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
+        st = RtRenderStats()
+        ls = make_lights(frame["lights"])
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        tm = make_tone_map(tone) if tone is not None else None
+        _check(lib().rt_render_tone_mapped(self.h, C.byref(cam), int(aa[0]), int(aa[1]), ls, len(frame["lights"]),
+                                           table, len(table), C.byref(tm) if tm is not None else None, ptr(rgb),
+                                           C.byref(st)))
+        return {"rgb": rgb, "stats": st}
 
     def render_aa(self, frame, aa_x, aa_y, rgb=None):
         """Anti-aliased frame: aa_x * aa_y rays per output pixel, averaged."""

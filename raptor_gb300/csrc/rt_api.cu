@@ -771,11 +771,126 @@ static rt_status render_tree(rt_scene *s, const rt_camera *camera, const rt_ligh
     if (!per_triangle) sv.mat = nullptr;
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    launch_render_tree(sv, make_camera_view(*camera), ls, mt, o.rgb, o.ids, ctx->d_counters, ctx->sm_count,
+    launch_render_tree(sv, make_camera_view(*camera), ls, mt, o.rgb, nullptr, o.ids, ctx->d_counters, ctx->sm_count,
                        ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
+}
+
+// Lights and a material table for the scene's per-triangle indices.
+static rt_status check_table(const rt_scene *s, const rt_light *lights, int32_t nlights, const rt_material *materials,
+                             int32_t nmaterials, const std::string &w)
+{
+    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
+        return fail(RT_ERR_INVALID_ARG, w + ": light count out of range");
+    if (nmaterials < 1 || nmaterials > RT_MAX_MATERIALS)
+        return fail(RT_ERR_INVALID_ARG, w + ": material count must be 1..RT_MAX_MATERIALS");
+    for (int32_t i = 0; i < nmaterials; ++i) {
+        const rt_status st = check_weights(materials[i], w, true);
+        if (st != RT_OK) return st;
+    }
+    const rt_status st = check_tree(materials, nmaterials, w);
+    if (st != RT_OK) return st;
+    if (s->mat_max >= nmaterials) return fail(RT_ERR_INVALID_ARG, w + ": the scene's material indices exceed the table");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, w + ": hierarchy not built");
+    return RT_OK;
+}
+
+rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n, float *sum_out)
+{
+    if (!ctx || !sum_out || (n > 0 && !values)) return fail(RT_ERR_INVALID_ARG, "rt_sum_sequential_f32: NULL argument");
+    if (n < 0 || n > ((int64_t)1 << 32)) return fail(RT_ERR_INVALID_ARG, "rt_sum_sequential_f32: n out of range");
+    *sum_out = 0.0f;
+    if (n == 0) return RT_OK;
+    DeviceGuard g(ctx->device);
+    const void *dv = nullptr;
+    rt_status st = stage_in(ctx, ctx->stage_a, values, (size_t)n * sizeof(float), &dv);
+    if (st != RT_OK) return st;
+    RT_CUDA(ctx->tone.reserve(sizeof(ToneAcc) + 256 + tone_scratch_bytes(n)), "scratch allocation");
+    ToneAcc *acc = (ToneAcc *)ctx->tone.ptr;
+    uint32_t *mx = (uint32_t *)((char *)ctx->tone.ptr + 128);
+    launch_abs_max((const float *)dv, n, mx, ctx->sm_count, ctx->stream);
+    RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, mx, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "readback");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    uint32_t bits = (uint32_t)ctx->h_scratch[0];
+    if (bits >= 0x7f800000u) return fail(RT_ERR_INVALID_ARG, "rt_sum_sequential_f32: values must be finite");
+    if (bits == 0) return RT_OK;   // all zeros: +0
+    float max_abs;
+    std::memcpy(&max_abs, &bits, sizeof(float));
+    launch_sequential_sum((const float *)dv, n, max_abs, acc, (char *)ctx->tone.ptr + 256, ctx->sm_count, ctx->stream);
+    RT_CUDA(cudaGetLastError(), "sum launch");
+    RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, &acc->sum_f, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+            "readback");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    std::memcpy(sum_out, ctx->h_scratch, sizeof(float));
+    return RT_OK;
+}
+
+rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa_x, int32_t aa_y,
+                                const rt_light *lights, int32_t nlights, const rt_material *materials,
+                                int32_t nmaterials, const rt_tone_map *tone, uint8_t *rgb_out, rt_render_stats *stats)
+{
+    if (!s || !materials || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (aa_x < 1 || aa_x > 16 || aa_y < 1 || aa_y > 16)
+        return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: anti-aliasing factors must be 1..16");
+    rt_camera fine = *camera;
+    fine.xres = camera->xres * aa_x;
+    fine.yres = camera->yres * aa_y;
+    st = check_camera(&fine);
+    if (st != RT_OK) return st;
+    st = check_table(s, lights, nlights, materials, nmaterials, "rt_render_tone_mapped");
+    if (st != RT_OK) return st;
+    ToneView tv = {};
+    if (tone) {
+        const int m = tone->mode;
+        if (!(m == RT_TONE_NONE || m == RT_TONE_GLOBAL_CONTRAST || m == RT_TONE_GLOBAL_NON_LINEAR ||
+              m == RT_TONE_GLOBAL_EXPOSURE || m == RT_TONE_GLOBAL_AVG_LUMINANCE || m == RT_TONE_GLOBAL_MAX_LUMINANCE ||
+              m == RT_TONE_GLOBAL_FERWERDA))
+            return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: unsupported tone-mapping mode");
+        const float lim = 3.0e38f;
+        if (!(std::fabs(tone->key) < lim && std::fabs(tone->xw) < lim && std::fabs(tone->yw) < lim &&
+              tone->gamma >= 0.0f && tone->gamma < lim))
+            return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: key, white point and gamma must be finite, "
+                                            "gamma >= 0");
+        tv.enabled = 1;
+        tv.mode = m;
+        tv.key = tone->key;
+        tv.xw = tone->xw;
+        tv.yw = tone->yw;
+        tv.desaturate = tone->desaturate ? 1 : 0;
+        tv.stretch = tone->stretch ? 1 : 0;
+        tv.gamma = tone->gamma;
+    }
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    const size_t nfine = (size_t)fine.xres * (size_t)fine.yres;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
+    if (st != RT_OK) return st;
+    RT_CUDA(ctx->fimg.reserve(nfine * 3 * sizeof(float)), "float frame allocation");
+    RT_CUDA(ctx->tone.reserve(sizeof(ToneAcc) + 256 + tone_scratch_bytes((int64_t)nfine)),
+            "tone accumulator allocation");
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = 0;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    MaterialTable mt;
+    mt.n = nmaterials;
+    for (int i = 0; i < nmaterials; ++i) mt.m[i] = make_material_view(materials[i]);
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render_tree(scene_view(s), make_camera_view(fine), ls, mt, nullptr, (float *)ctx->fimg.ptr, nullptr,
+                       ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    launch_tone_map((const float *)ctx->fimg.ptr, fine.xres, fine.yres, aa_x, aa_y, tv, o.rgb, (ToneAcc *)ctx->tone.ptr,
+                    (char *)ctx->tone.ptr + 256, ctx->sm_count, ctx->stream);
+    RT_CUDA(cudaGetLastError(), "tone-map launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, stats);
 }
 
 rt_status rt_render_materials(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
@@ -785,20 +900,8 @@ rt_status rt_render_materials(rt_scene *s, const rt_camera *camera, const rt_lig
     if (!s || !materials || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_render_materials: NULL argument");
     rt_status st = check_camera(camera);
     if (st != RT_OK) return st;
-    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
-        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: light count out of range");
-    if (nmaterials < 1 || nmaterials > RT_MAX_MATERIALS)
-        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: material count must be 1..RT_MAX_MATERIALS");
-    const std::string w("rt_render_materials");
-    for (int32_t i = 0; i < nmaterials; ++i) {
-        st = check_weights(materials[i], w, true);
-        if (st != RT_OK) return st;
-    }
-    st = check_tree(materials, nmaterials, w);
+    st = check_table(s, lights, nlights, materials, nmaterials, "rt_render_materials");
     if (st != RT_OK) return st;
-    if (s->mat_max >= nmaterials)
-        return fail(RT_ERR_INVALID_ARG, "rt_render_materials: the scene's material indices exceed the table");
-    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_render_materials: hierarchy not built");
     const bool plain = nmaterials == 1 && materials[0].rf == 0.0f && materials[0].tran == 0.0f;
     if (plain) return rt_render(s, camera, lights, nlights, materials, rgb_out, hit_ids, stats);
     return render_tree(s, camera, lights, nlights, materials, nmaterials, true, rgb_out, hit_ids, stats);

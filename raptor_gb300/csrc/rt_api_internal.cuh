@@ -39,6 +39,8 @@ struct rt_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rtc::DevBuf stage_a, stage_b, stage_c;
     rtc::DevBuf redo;                      // pixels queued for an exact second pass
+    rtc::DevBuf fimg;                      // float frame of rt_render_tone_mapped
+    rtc::DevBuf tone;                      // its tone-mapping accumulators
     bool count_fetches = false;
     int render_kernel = RT_KERNEL_PIXEL;
     int isect = RT_ISECT_REFERENCE;

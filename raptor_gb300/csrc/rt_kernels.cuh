@@ -30,6 +30,29 @@ struct Counters {
     int redo;                        // pixels queued for an exact second pass
 };
 
+// Tone-mapping parameters (rt_tone_map) and the per-frame accumulators of
+// the tone-mapping kernels (rt_tonemap.cu).
+struct ToneView {
+    int32_t enabled;   // 0: the downsample and clip alone
+    int32_t mode;
+    float key, xw, yw;
+    int32_t desaturate, stretch;
+    float gamma;
+};
+struct ToneScalars {
+    float sf;    // luminance scale
+    float aux;   // non-linear: 1 / (maxY * sf)^2; exposure: maxY * sf
+    float k, mp, ms;   // Ferwerda: rod weight, cone and rod scales
+};
+struct ToneAcc {
+    float sum_f;               // binary32 sum of log10 luminance over the counted samples, in sample order
+    unsigned long long count;  // samples with luminance >= 3.18e-7
+    uint32_t max_bits;         // largest such luminance (float bits)
+    uint32_t gmin, gmax;       // mapped-luminance range (order keys), stretch only
+    int32_t redo;              // output pixels queued for the exact pass
+    ToneScalars s;
+};
+
 struct LightSet {
     int32_t n;
     int32_t fast_pow;   // single-precision specular power + exact re-shade near truncation
@@ -48,8 +71,20 @@ void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_
 void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                    uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
 void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
-                        uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+                        uint8_t *rgb, float *fimg, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st,
+                        bool count = false);
 void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t st);
+// fimg: fw x fh float frame (3 floats per sample, the supersampled grid of
+// an ow x oh output with aa_x x aa_y samples per pixel) -> rgb (ow x oh).
+// The binary32 sum of v[0..n) in index order, as a sequential loop rounds it
+// (into acc->sum_f); max_abs: the largest |v[i]| (launch_abs_max), > 0.
+void launch_abs_max(const float *v, int64_t n, uint32_t *out, int sm_count, cudaStream_t st);
+void launch_sequential_sum(const float *v, int64_t n, float max_abs, ToneAcc *acc, void *scratch, int sm_count,
+                           cudaStream_t st);
+// scratch: tone_scratch_bytes(fw * fh) of device memory.
+size_t tone_scratch_bytes(int64_t n);
+void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
+                     uint8_t *rgb, ToneAcc *acc, void *scratch, int sm_count, cudaStream_t st);
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                       int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, int32_t *redo,
                       Counters *ctr, int sm_count, cudaStream_t st, bool count = false);

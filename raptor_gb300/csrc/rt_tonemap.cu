@@ -1,0 +1,741 @@
+// rt_tonemap.cu -- framebuffer epilogue: the reference's global tone
+// mapping (camera::tone_map, raytracer/camera.cc:1124-1463, glare and
+// temporal adaptation off), the CIE Yxy -> RGB conversion
+// (camera::convert_Yxy_to_rgb, camera.cc:2080-2098), gamma correction
+// (camera::gamma_correct, camera.cc:1466-1500) and the anti-aliasing
+// downsample with clamp-and-truncate to RGB8 (camera::clip_image_to_rgb,
+// camera.h:289-319), on the float frame the ray-tree kernel writes.
+//
+// Kernels, in stream order:
+//   k_tone_terms    one pass over the samples: count and maximum of the
+//                   luminances above 3.18e-7, their log10 terms and the
+//                   per-chunk increments of the exact sequential sum
+//   k_tone_coarse   the chunk increments summed over groups of chunks
+//   k_tone_sum      one warp: the reference's binary32 sum of the terms,
+//                   reproduced exactly, then the mode's scale factors
+//   k_tone_range    (contrast stretch only) minimum and maximum of the
+//                   mapped luminance
+//   k_tone_final    per output pixel: every sample through the whole
+//                   per-pixel chain, averaged, clamped, truncated; single-
+//                   precision library calls, pixels near a truncation
+//                   boundary queued
+//   k_tone_fix      the queued pixels with the library calls evaluated in
+//                   double and rounded once (the reference's float results)
+// Every per-pixel step uses the reference's binary32 operation order.
+#include <cmath>
+
+#include "rt_kernels.cuh"
+#include "rt_traverse.cuh"
+
+namespace rtc {
+namespace {
+
+constexpr int kToneThreads = 256;
+
+// The reference's float library calls, evaluated in double and rounded
+// once (EXACT), or by the single-precision CUDA functions (a few ulp), whose
+// pixels are redone exactly when they land near a truncation boundary.
+__device__ __forceinline__ float log10_f(float v) { return (float)log10((double)v); }
+__device__ __forceinline__ float log_f(float v) { return (float)log((double)v); }
+__device__ __forceinline__ float exp_f(float v) { return (float)exp((double)v); }
+__device__ __forceinline__ float pow_f(float a, float b) { return (float)pow((double)a, (double)b); }
+template <bool EXACT> __device__ __forceinline__ float tl_log10(float v) { return EXACT ? log10_f(v) : log10f(v); }
+template <bool EXACT> __device__ __forceinline__ float tl_exp(float v) { return EXACT ? exp_f(v) : expf(v); }
+template <bool EXACT> __device__ __forceinline__ float tl_pow(float a, float b) { return EXACT ? pow_f(a, b) : powf(a, b); }
+
+// RGB (0..1) -> CIE luminance scaled by 683 (camera.cc:1149-1151).
+__device__ __forceinline__ float lum683(float r, float g, float b)
+{
+    return xmul(683.0f, xadd(xadd(xmul(0.2126f, r), xmul(0.7151f, g)), xmul(0.0721f, b)));
+}
+
+struct Yxy {
+    float x, Y, y;
+};
+
+// First loop of camera::tone_map for one sample (camera.cc:1137-1193):
+// XYZ, the luminance floor, chromaticity, optional desaturation.
+template <bool EXACT>
+__device__ __forceinline__ Yxy to_yxy(float3 c, const ToneView &t)
+{
+    const float r = xdiv(c.x, 255.0f), g = xdiv(c.y, 255.0f), b = xdiv(c.z, 255.0f);
+    const float X = xmul(683.0f, xadd(xadd(xmul(0.4124f, r), xmul(0.3576f, g)), xmul(0.1805f, b)));
+    float Y = lum683(r, g, b);
+    const float Z = xmul(683.0f, xadd(xadd(xmul(0.0193f, r), xmul(0.1192f, g)), xmul(0.9505f, b)));
+    if (Y < 3.18e-7f) Y = 3.18e-7f;
+    const float W = xadd(xadd(Y, X), Z);
+    Yxy o;
+    o.x = xdiv(X, W);
+    o.y = xdiv(Y, W);
+    o.Y = Y;
+    if (t.desaturate) {
+        float s;
+        const float l = tl_log10<EXACT>(Y);
+        if (l < -2.0f) {
+            s = 0.0f;
+        } else if (l < 0.6f) {
+            const float q = xdiv(xadd(l, 2.0f), 2.6f);
+            const float q2 = xmul(q, q);
+            s = xsub(xmul(3.0f, q2), xmul(xmul(2.0f, q), q2));
+        } else {
+            s = 1.0f;
+        }
+        const float V = xmul(1700.0f, xadd(xadd(xmul(0.01477f, r), xmul(0.497f, g)), xmul(0.631f, b)));
+        const float third = 1.0f / 3.0f;
+        const float one_s = xsub(1.0f, s);
+        o.x = xadd(xmul(one_s, t.xw), xmul(s, xsub(xadd(o.x, t.xw), third)));
+        o.y = xadd(xmul(one_s, t.yw), xmul(s, xsub(xadd(o.y, t.yw), third)));
+        o.Y = xadd(xmul(xmul(0.4468f, one_s), V), xmul(s, Y));
+    }
+    return o;
+}
+
+// The mode's luminance scaling (camera.cc:1276-1425) of one sample.
+template <bool EXACT>
+__device__ __forceinline__ float map_lum(float g, const ToneView &t, const ToneScalars &k)
+{
+    switch (t.mode) {
+    case RT_TONE_GLOBAL_NON_LINEAR:
+        g = xmul(g, k.sf);
+        if (k.aux != 0.0f) g = xmul(g, xdiv(xadd(1.0f, xmul(g, k.aux)), xadd(1.0f, g)));
+        return g;
+    case RT_TONE_GLOBAL_EXPOSURE:
+        g = xmul(g, k.sf);
+        if (k.aux != 0.0f) g = xsub(1.0f, tl_exp<EXACT>(-g));
+        return g;
+    case RT_TONE_GLOBAL_FERWERDA: {
+        const float ldp = xmul(k.mp, g), lds = xmul(k.ms, g);
+        return xmul(1.0f / 800.0f, xadd(ldp, xmul(k.k, lds)));
+    }
+    default:   // none, contrast, average and maximum luminance: one scale
+        return xmul(g, k.sf);
+    }
+}
+
+// Yxy -> RGB in 0..255 (camera.cc:2085-2096), then gamma (camera.cc:1470-1497).
+template <bool EXACT>
+__device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma)
+{
+    const float X = xdiv(xmul(x, Y), y);
+    const float Z = xdiv(xmul(xsub(xsub(1.0f, x), y), Y), y);
+    float3 c;
+    c.x = xadd(xadd(xmul(826.353f, X), xmul(-391.986f, Y)), xmul(-127.143f, Z));
+    c.y = xadd(xadd(xmul(-247.0695f, X), xmul(478.329f, Y)), xmul(10.5825f, Z));
+    c.z = xadd(xadd(xmul(14.2035f, X), xmul(-52.02f, Y)), xmul(269.535f, Z));
+    if (gamma > 0.0f) {
+        float v[3] = {xdiv(c.x, 255.0f), xdiv(c.y, 255.0f), xdiv(c.z, 255.0f)};
+        const bool plain = fabsf(xsub(gamma, 2.2f)) > 0.001f;
+        const bool srgb = !plain && fabsf(xsub(gamma, 1.0f)) > 0.001f;
+        const float inv = xdiv(1.0f, gamma);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            float a = v[i];
+            a = (a < 0.0f) ? 0.0f : a;   // std::max(a, 0), then std::min(., 1)
+            a = (1.0f < a) ? 1.0f : a;
+            if (plain) a = tl_pow<EXACT>(a, inv);
+            else if (srgb)
+                a = (a <= 0.0031308f) ? xmul(12.92f, a) : xsub(xmul(1.055f, tl_pow<EXACT>(a, 1.0f / 2.4f)), 0.055f);
+            v[i] = a;
+        }
+        c = make_float3(xmul(v[0], 255.0f), xmul(v[1], 255.0f), xmul(v[2], 255.0f));
+    }
+    return c;
+}
+
+// Order-preserving key of a float for unsigned atomics (no NaNs here).
+__device__ __forceinline__ uint32_t order_key(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// ---- the log-average luminance, summed as the reference sums it
+//
+// The reference adds log10(Y) of every counted sample to a binary32 sum in
+// sample order (camera.cc:1158).  That sum is reproduced exactly: while the
+// running sum S stays in one binade [2^e, 2^(e+1)), every addition rounds
+// to a multiple of u = 2^(e-23), so S + a_i = S + u * rne(a_i / u) as long
+// as no rne is a tie and no partial sum leaves the binade.  k_tone_terms
+// writes the terms and, per chunk of kSumChunk terms and for each of 32
+// candidate binades, the sums of the positive and of the negative rne
+// increments and a tie flag; k_tone_sum walks the chunks in order with one
+// warp, applying a chunk in one step when its increments provably keep S
+// inside S's binade and adding its terms one by one otherwise (the first
+// chunk, binade changes, ties).  Uncounted samples contribute +0, which
+// leaves S unchanged.
+constexpr int kSumChunk = 512;
+constexpr int kSumThreads = 128;
+constexpr int kSumPerThread = kSumChunk / kSumThreads;
+
+struct ChunkSum {
+    int32_t pos, neg;   // sums of the positive / negative increments in units of u, saturated at +-2^30
+    int32_t tie, pad;
+};
+
+// Increments and their sums beyond +-2^24 units can never be applied (the
+// sum would leave the binade), so they are stored saturated.
+constexpr int32_t kSat = 1 << 30;
+__device__ __forceinline__ int32_t sat32(long long v) { return v > kSat ? kSat : (v < -kSat ? -kSat : (int32_t)v); }
+
+// values non-null: the terms are given (rt_sum_sequential_f32) instead of
+// derived from the frame.
+__global__ void __launch_bounds__(kSumThreads) k_tone_terms(const float *__restrict__ fimg,
+                                                            const float *__restrict__ values, int64_t n, int32_t e_lo,
+                                                            float *__restrict__ terms, ChunkSum *__restrict__ rec,
+                                                            ToneAcc *acc)
+{
+    __shared__ long long s_pos[32], s_neg[32];
+    __shared__ int32_t s_tie[32];
+    if (threadIdx.x < 32) {
+        s_pos[threadIdx.x] = 0;
+        s_neg[threadIdx.x] = 0;
+        s_tie[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kSumChunk;
+    float a[kSumPerThread];
+    uint32_t cnt = 0, maxb = 0;
+#pragma unroll
+    for (int t = 0; t < kSumPerThread; ++t) {
+        const int64_t i = base + t * kSumThreads + threadIdx.x;
+        a[t] = 0.0f;
+        if (i < n && values) {
+            a[t] = values[i];
+        } else if (i < n) {
+            const float r = xdiv(fimg[3 * i], 255.0f), g = xdiv(fimg[3 * i + 1], 255.0f),
+                        b = xdiv(fimg[3 * i + 2], 255.0f);
+            const float Y = lum683(r, g, b);
+            if (!(Y < 3.18e-7f)) {
+                ++cnt;
+                maxb = max(maxb, __float_as_uint(Y));   // Y > 0: bit order is value order
+                a[t] = log10_f(Y);
+            }
+        }
+        terms[i] = a[t];   // the padding of the last chunk holds +0
+    }
+    const int lane = threadIdx.x & 31;
+    for (int ei = 0; ei < 32; ++ei) {
+        long long pos = 0, neg = 0;
+        int32_t tie = 0;
+#pragma unroll
+        for (int t = 0; t < kSumPerThread; ++t) {
+            const float k = ldexpf(a[t], 23 - (e_lo + ei));   // exact: a power-of-two scale
+            long long q;
+            if (fabsf(k) < 33554432.0f) {                      // |k| < 2^25
+                q = __float2int_rn(k);                         // round to nearest, ties to even
+                tie |= (xsub(k, floorf(k)) == 0.5f) ? 1 : 0;
+            } else {
+                q = (k > 0.0f) ? (1ll << 26) : -(1ll << 26);   // too large to apply: saturates the sums
+            }
+            if (q > 0) pos += q;
+            else neg += q;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            pos += __shfl_xor_sync(0xffffffffu, pos, o);
+            neg += __shfl_xor_sync(0xffffffffu, neg, o);
+            tie |= __shfl_xor_sync(0xffffffffu, tie, o);
+        }
+        if (lane == 0) {
+            atomicAdd((unsigned long long *)&s_pos[ei], (unsigned long long)pos);
+            atomicAdd((unsigned long long *)&s_neg[ei], (unsigned long long)neg);
+            atomicOr(&s_tie[ei], tie);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        maxb = max(maxb, __shfl_xor_sync(0xffffffffu, maxb, o));
+    }
+    if (lane == 0 && cnt) {
+        atomicAdd(&acc->count, (unsigned long long)cnt);
+        atomicMax(&acc->max_bits, maxb);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        ChunkSum c;
+        c.pos = sat32(s_pos[threadIdx.x]);
+        c.neg = sat32(s_neg[threadIdx.x]);
+        c.tie = s_tie[threadIdx.x];
+        c.pad = 0;
+        rec[(int64_t)blockIdx.x * 32 + threadIdx.x] = c;
+    }
+}
+
+// The scale factors of camera::tone_map's mode branch (camera.cc:1203-1425)
+// from the log-luminance sum, the counted samples and the maximum.
+__device__ void tone_scalars(const ToneView &t, ToneAcc *acc)
+{
+    float Yi = 0.0f;
+    if (acc->count) Yi = xdiv(acc->sum_f, (float)acc->count);
+    Yi = pow_f(10.0f, Yi);
+    float maxY = __uint_as_float(acc->max_bits);
+    ToneScalars k;
+    k.sf = 1.0f;
+    k.aux = 0.0f;
+    k.k = k.mp = k.ms = 0.0f;
+    switch (t.mode) {
+    case RT_TONE_GLOBAL_CONTRAST: {
+        const float Yw = 300.0f;
+        const float num = xadd(1.219f, pow_f(xmul(Yw, 0.5f), 0.4f));
+        const float den = xadd(1.219f, pow_f(Yi, 0.4f));
+        k.sf = xmul(xdiv(1.0f, Yw), pow_f(xdiv(num, den), 2.5f));
+        break;
+    }
+    case RT_TONE_GLOBAL_NON_LINEAR:
+        k.sf = xdiv(t.key, Yi);
+        maxY = xmul(maxY, k.sf);
+        k.aux = xdiv(1.0f, xmul(maxY, maxY));
+        break;
+    case RT_TONE_GLOBAL_EXPOSURE:
+        k.sf = xdiv(t.key, Yi);
+        k.aux = xmul(maxY, k.sf);
+        break;
+    case RT_TONE_GLOBAL_AVG_LUMINANCE:
+        // the reference accumulates its RGB average only in exposure mode
+        // (camera.cc:1142), so here it is zero and the scale stays 1
+        k.sf = 1.0f;
+        break;
+    case RT_TONE_GLOBAL_MAX_LUMINANCE:
+        k.sf = xdiv(t.key, maxY);
+        break;
+    case RT_TONE_GLOBAL_FERWERDA: {
+        const float log_lda = log_f(xmul(800.0f, 0.5f));
+        const float log_la = log_f(Yi);
+        float tp, ts;
+        if (log_la <= -2.6f) tp = -0.72f;
+        else if (log_la <= 1.9f) tp = xsub(pow_f(xadd(xmul(0.249f, log_la), 0.65f), 2.7f), 0.72f);
+        else tp = xsub(log_la, 1.255f);
+        k.mp = xdiv(xsub(log_lda, 1.255f), tp);
+        if (log_la <= -3.94f) ts = -2.86f;
+        else if (log_la < -1.44f) ts = xsub(pow_f(xadd(xmul(0.405f, log_la), 1.6f), 2.18f), 2.86f);
+        else ts = xsub(log_la, 0.395f);
+        k.ms = xdiv(xsub(log_lda, 1.255f), ts);
+        if (log_la < -2.0f) k.k = 1.0f;
+        else if (log_la < 1.0f) k.k = xsub(1.0f, xmul(xadd(log_la, 2.0f), 1.0f / 3.0f));
+        else k.k = 0.0f;
+        break;
+    }
+    default:
+        k.sf = 1.0f / 683.0f;
+        break;
+    }
+    acc->s = k;
+    acc->gmin = 0xffffffffu;
+    acc->gmax = 0u;
+}
+
+// Coarse records: per group of kCoarse chunks and candidate binade, the
+// sums of its chunks' records.
+constexpr int kCoarse = 8;
+
+__global__ void k_tone_coarse(const ChunkSum *__restrict__ rec, int64_t nchunks, int64_t ncoarse,
+                              ChunkSum *__restrict__ crec)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= ncoarse * 32) return;
+    const int64_t c = idx >> 5;
+    const int ei = (int)(idx & 31);
+    long long pos = 0, neg = 0;
+    int32_t tie = 0;
+    for (int f = 0; f < kCoarse; ++f) {
+        const int64_t j = c * kCoarse + f;
+        if (j >= nchunks) break;
+        const ChunkSum r = rec[j * 32 + ei];
+        pos += r.pos;
+        neg += r.neg;
+        tie |= r.tie;
+    }
+    ChunkSum sum;
+    sum.pos = sat32(pos);
+    sum.neg = sat32(neg);
+    sum.tie = tie;
+    sum.pad = 0;
+    crec[idx] = sum;
+}
+
+// S as e and M (S = M * 2^(e-23), 2^23 <= |M| < 2^24) for a normal S, and
+// back for 2^23 < |M| < 2^24: integer operations on the bits only.
+__device__ __forceinline__ bool split(float S, int &e, int32_t &M)
+{
+    const uint32_t b = __float_as_uint(S);
+    const uint32_t ex = (b >> 23) & 0xffu;
+    if (ex == 0u || ex == 0xffu) return false;   // zero, subnormal, infinite
+    e = (int)ex - 127;
+    const int32_t m = (int32_t)((b & 0x7fffffu) | 0x800000u);
+    M = (b >> 31) ? -m : m;
+    return true;
+}
+__device__ __forceinline__ float join(int e, int32_t M)
+{
+    const uint32_t sign = (M < 0) ? 0x80000000u : 0u;
+    const uint32_t m = (uint32_t)((M < 0) ? -M : M);
+    return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (m & 0x7fffffu));
+}
+
+// Whether M + P stays strictly inside the binade of M (units of u): then
+// the exact partial sum lies inside it too and rounds on the grid of u.
+__device__ __forceinline__ bool inside(int32_t M, int32_t P)
+{
+    const int32_t lo = (1 << 23) + 1, hi = (1 << 24) - 1;
+    const int32_t v = M + P;
+    return (M > 0) ? (v >= lo && v <= hi) : (v <= -lo && v >= -hi);
+}
+
+// Records first .. first + 31 (lane l: record first + l, for the binade of
+// S; count valid) tried as one run: each record keeps S in its binade when
+// M + (the increments of the records before it) + its neg and + its pos
+// both stay inside and it has no tie.  The records before the first that
+// fails are applied (exactly: every prefix sum stays on the grid of u).
+// Returns how many were applied; 32 when all were.  Uniform across the warp.
+__device__ __forceinline__ int apply_records(float &S, const ChunkSum *__restrict__ recs, int64_t first, int64_t count,
+                                             int64_t stride, int32_t e_lo)
+{
+    const int lane = threadIdx.x & 31;
+    int e;
+    int32_t M;
+    if (!split(S, e, M) || e - e_lo < 0 || e - e_lo >= 32) return 0;
+    const int64_t idx = first + lane;
+    ChunkSum r = {0, 0, 1, 0};
+    if (idx < count) r = recs[idx * stride + (e - e_lo)];
+    // this record's total, clamped: a record beyond +-2^24 never applies
+    const int32_t d = min(max(r.pos + r.neg, -(1 << 25)), 1 << 25);
+    int32_t incl = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int32_t base = incl - d;
+    const bool ok = idx < count && !r.tie && inside(M, base + r.neg) && inside(M, base + r.pos);
+    const uint32_t fail = __ballot_sync(0xffffffffu, !ok);
+    const int n = fail ? __ffs(fail) - 1 : 32;
+    if (n > 0) S = join(e, M + __shfl_sync(0xffffffffu, incl, n - 1));
+    return n;
+}
+
+// Adds slice v (32 terms, lane order) to S term by term.
+__device__ __forceinline__ float add_slice(float S, float v)
+{
+#pragma unroll
+    for (int l = 0; l < 32; ++l) S = xadd(S, __shfl_sync(0xffffffffu, v, l));
+    return S;
+}
+
+// The 512 terms of chunk j (16 slices of 32, slice q holding terms
+// q*32 .. q*32+31 in lane order) added to S in order.  For S's binade all
+// remaining slices are scanned at once (rounded increments, warp scans,
+// running bases); the slices before the first one whose prefix sums leave
+// the binade (or hold a tie) are applied in one step, that slice term by
+// term, and the rest tried again in the new binade.  Uniform across the warp.
+__device__ float sum_chunk(float S, const float *__restrict__ terms, int64_t j)
+{
+    constexpr int Q = kSumChunk / 32;
+    const int lane = threadIdx.x & 31;
+    float a[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) a[q] = terms[j * kSumChunk + q * 32 + lane];
+    int q0 = 0;
+    for (int round = 0; round <= Q && q0 < Q; ++round) {
+        int e;
+        int32_t M;
+        int bad = q0;   // the first slice that cannot be applied
+        if (split(S, e, M) && 23 - e <= 127) {
+            const float scale = __int_as_float((23 - e + 127) << 23);   // 2^(23-e)
+            int32_t P[Q];
+            uint32_t fails = 0;   // bit q: slice q fails in this lane
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const float k = xmul(a[q], scale);   // exact: a power-of-two scale
+                const bool big = !(fabsf(k) < 33554432.0f);
+                const bool tie = !big && xsub(k, floorf(k)) == 0.5f;
+                P[q] = big ? 0 : __float2int_rn(k);
+                if (big || tie) fails |= 1u << q;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const int32_t v = __shfl_up_sync(0xffffffffu, P[q], o);
+                    if (lane >= o) P[q] += v;
+                }
+            // running base over the slices from q0 on
+            int32_t base = 0;
+            int32_t base_at[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                base_at[q] = base;
+                if (q >= q0) base += min(max(__shfl_sync(0xffffffffu, P[q], 31), -(1 << 25)), 1 << 25);
+            }
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (q >= q0 && !inside(M, base_at[q] + P[q])) fails |= 1u << q;
+            fails = __reduce_or_sync(0xffffffffu, fails) & ~((1u << q0) - 1u);
+            bad = fails ? __ffs(fails) - 1 : Q;
+            if (bad > q0) {
+                int32_t upto = 0;
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    if (q == bad - 1) upto = __shfl_sync(0xffffffffu, base_at[q] + P[q], 31);
+                S = join(e, M + upto);
+            }
+        }
+        if (bad >= Q) break;
+        float v = 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (q == bad) v = a[q];
+        S = add_slice(S, v);
+        q0 = bad + 1;
+    }
+    return S;
+}
+
+// One warp walks the groups of kCoarse chunks in order, 32 group records at
+// a time (apply_records); a group that cannot be applied goes chunk by
+// chunk (its records), a chunk slice by slice (sum_chunk).  Then the scale
+// factors.
+__global__ void __launch_bounds__(32) k_tone_sum(const float *__restrict__ terms, const ChunkSum *__restrict__ rec,
+                                                 const ChunkSum *__restrict__ crec, int64_t nchunks, int64_t ncoarse,
+                                                 int32_t e_lo, ToneView t, ToneAcc *acc, bool scalars)
+{
+    float S = 0.0f;
+    int64_t c = 0;
+    for (int64_t guard = 0; c < ncoarse && guard < 4 * ncoarse + 64; ++guard) {
+        const int n = apply_records(S, crec, c, ncoarse, 32, e_lo);
+        c += n;
+        if (n == 32 || c >= ncoarse) continue;
+        // group c chunk by chunk
+        const int64_t j_end = (c + 1) * kCoarse < nchunks ? (c + 1) * kCoarse : nchunks;
+        int64_t j = c * kCoarse;
+        for (int g2 = 0; j < j_end && g2 <= kCoarse; ++g2) {
+            const int m = apply_records(S, rec, j, j_end, 32, e_lo);
+            j += m;
+            if (j >= j_end) break;
+            S = sum_chunk(S, terms, j);
+            ++j;
+        }
+        ++c;
+    }
+    if (threadIdx.x == 0) {
+        acc->sum_f = S;
+        if (scalars) tone_scalars(t, acc);
+    }
+}
+
+// Largest |value| (bit pattern of the magnitude; finite values order as
+// their bits).
+__global__ void k_abs_max(const float *__restrict__ v, int64_t n, uint32_t *out)
+{
+    uint32_t m = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, __float_as_uint(v[i]) & 0x7fffffffu);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void __launch_bounds__(kToneThreads) k_tone_range(const float *__restrict__ fimg, int64_t n, ToneView t,
+                                                             ToneAcc *acc)
+{
+    const ToneScalars k = acc->s;
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const Yxy p = to_yxy<true>(make_float3(fimg[3 * i], fimg[3 * i + 1], fimg[3 * i + 2]), t);
+        const uint32_t key = order_key(map_lum<true>(p.Y, t, k));
+        lo = min(lo, key);
+        hi = max(hi, key);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&acc->gmin, lo);
+        atomicMax(&acc->gmax, hi);
+    }
+}
+
+// One output pixel: each of its aa_x * aa_y samples through the chain, then
+// clip_image_to_rgb's sum (a_x outer, a_y inner) and division.
+template <bool EXACT>
+__device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int32_t fw, int32_t aa_x, int32_t aa_y,
+                                             int32_t ox, int32_t oy, const ToneView &t, const ToneScalars &k,
+                                             bool stretch, float offset, float scale, float samples)
+{
+    float3 a = make_float3(0.0f, 0.0f, 0.0f);
+    for (int32_t ax = 0; ax < aa_x; ++ax)
+        for (int32_t ay = 0; ay < aa_y; ++ay) {
+            const int64_t s = (int64_t)(ox * aa_x + ax) + (int64_t)(oy * aa_y + ay) * fw;
+            float3 c = make_float3(fimg[3 * s], fimg[3 * s + 1], fimg[3 * s + 2]);
+            if (t.enabled) {
+                const Yxy p = to_yxy<EXACT>(c, t);
+                float g = map_lum<EXACT>(p.Y, t, k);
+                if (stretch) g = xmul(xadd(g, offset), scale);
+                c = to_rgb<EXACT>(p.x, g, p.y, t.gamma);
+            }
+            a = xadd3(a, c);
+        }
+    return make_float3(xdiv(a.x, samples), xdiv(a.y, samples), xdiv(a.z, samples));
+}
+
+// A channel within kTruncGuard of an integer in [0, 255] may truncate
+// differently once its float library calls are exact.
+__device__ __forceinline__ bool near_integer(float v)
+{
+    return v > -kTruncGuard && v < 255.0f + kTruncGuard && fabsf(v - rintf(v)) < kTruncGuard;
+}
+
+// The stretch parameters of camera.cc:1428-1450: applied when the mapped
+// range is positive or negative and not a single value.
+struct Stretch {
+    bool on;
+    float offset, scale;
+};
+__device__ __forceinline__ Stretch stretch_of(const ToneView &t, const ToneAcc *acc)
+{
+    Stretch r = {false, 0.0f, 1.0f};
+    if (!t.enabled || !t.stretch) return r;
+    const float minY2 = key_float(acc->gmin), maxY2 = key_float(acc->gmax);
+    if (((minY2 > 0.0f) || (maxY2 < 0.0f)) && (minY2 < maxY2)) {
+        r.on = true;
+        r.offset = (0.0f < -minY2) ? 0.0f : -minY2;          // std::min(-minY2, 0)
+        const float top = (maxY2 < 1.0f) ? maxY2 : 1.0f;     // std::min(1, maxY2)
+        const float bot = (0.0f < minY2) ? minY2 : 0.0f;     // std::max(0, minY2)
+        r.scale = xdiv(1.0f, xsub(top, bot));
+    }
+    return r;
+}
+
+__device__ __forceinline__ void store_pixel(uint8_t *rgb, int64_t o, float3 v)
+{
+    rgb[3 * o] = clip8(v.x);
+    rgb[3 * o + 1] = clip8(v.y);
+    rgb[3 * o + 2] = clip8(v.z);
+}
+
+// Per output pixel: tone_pixel with the single-precision library calls; a
+// pixel with a channel near a truncation boundary is queued for k_tone_fix
+// instead (warp-aggregated append), then the clamp and truncation of
+// clip_image_to_rgb.
+__global__ void __launch_bounds__(kToneThreads) k_tone_final(const float *__restrict__ fimg, int32_t fw, int32_t aa_x,
+                                                             int32_t aa_y, int32_t ow, int32_t oh, ToneView t,
+                                                             ToneAcc *acc, int32_t *__restrict__ redo,
+                                                             uint8_t *__restrict__ rgb)
+{
+    ToneScalars k = {};
+    if (t.enabled) k = acc->s;
+    const Stretch sr = stretch_of(t, acc);
+    const int64_t npix = (int64_t)ow * oh;
+    const float samples = (float)(aa_x * aa_y);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t steps = (npix + stride - 1) / stride;   // uniform trip count: whole warps append
+    for (int64_t it = 0; it < steps; ++it) {
+        const int64_t o = start + it * stride;
+        bool queue = false;
+        if (o < npix) {
+            const int32_t oy = (int32_t)(o / ow), ox = (int32_t)(o - (int64_t)oy * ow);
+            const float3 v = tone_pixel<false>(fimg, fw, aa_x, aa_y, ox, oy, t, k, sr.on, sr.offset, sr.scale, samples);
+            queue = t.enabled && (near_integer(v.x) || near_integer(v.y) || near_integer(v.z));
+            if (!queue) store_pixel(rgb, o, v);
+        }
+        const uint32_t b = __ballot_sync(0xffffffffu, queue);
+        if (b) {
+            int base = 0;
+            const int lane = threadIdx.x & 31;
+            if (lane == 0) base = atomicAdd(&acc->redo, __popc(b));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (queue) redo[base + __popc(b & ((1u << lane) - 1u))] = (int32_t)o;
+        }
+    }
+}
+
+// The queued pixels, with the library calls evaluated exactly.
+__global__ void __launch_bounds__(kToneThreads) k_tone_fix(const float *__restrict__ fimg, int32_t fw, int32_t aa_x,
+                                                           int32_t aa_y, int32_t ow, ToneView t, const ToneAcc *acc,
+                                                           const int32_t *__restrict__ redo, uint8_t *__restrict__ rgb)
+{
+    const ToneScalars k = acc->s;
+    const Stretch sr = stretch_of(t, acc);
+    const int n = acc->redo;
+    const float samples = (float)(aa_x * aa_y);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int64_t o = redo[i];
+        const int32_t oy = (int32_t)(o / ow), ox = (int32_t)(o - (int64_t)oy * ow);
+        store_pixel(rgb, o, tone_pixel<true>(fimg, fw, aa_x, aa_y, ox, oy, t, k, sr.on, sr.offset, sr.scale, samples));
+    }
+}
+
+int blocks_for(int64_t n, int sm_count)
+{
+    const int64_t b = (n + kToneThreads - 1) / kToneThreads;
+    const int64_t cap = (int64_t)sm_count * 8;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+}  // namespace
+
+size_t tone_scratch_bytes(int64_t n)
+{
+    const int64_t nchunks = (n + kSumChunk - 1) / kSumChunk;
+    const int64_t ncoarse = (nchunks + kCoarse - 1) / kCoarse;
+    return (size_t)nchunks * kSumChunk * sizeof(float) + (size_t)(nchunks + ncoarse) * 32 * sizeof(ChunkSum) +
+           (size_t)n * sizeof(int32_t);   // redo queue (at most one entry per output pixel)
+}
+
+void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
+                     uint8_t *rgb, ToneAcc *acc, void *scratch, int sm_count, cudaStream_t st)
+{
+    const int64_t n = (int64_t)fw * fh;
+    const int32_t ow = fw / aa_x, oh = fh / aa_y;
+    // scratch: terms | chunk records | coarse records | redo queue
+    const int64_t nchunks = (n + kSumChunk - 1) / kSumChunk;
+    const int64_t ncoarse = (nchunks + kCoarse - 1) / kCoarse;
+    float *terms = (float *)scratch;
+    ChunkSum *rec = (ChunkSum *)(terms + nchunks * kSumChunk);
+    ChunkSum *crec = rec + nchunks * 32;
+    int32_t *redo = (int32_t *)(crec + ncoarse * 32);
+    cudaMemsetAsync(acc, 0, sizeof(ToneAcc), st);
+    if (t.enabled) {
+        // candidate binades: |S| <= 39 n (|log10 Y| < 39 for any float Y)
+        const int32_t e_hi = (int32_t)std::floor(std::log2(39.0 * (double)n)) + 1;
+        const int32_t e_lo = e_hi - 31;
+        k_tone_terms<<<(unsigned)nchunks, kSumThreads, 0, st>>>(fimg, nullptr, n, e_lo, terms, rec, acc);
+        k_tone_coarse<<<(unsigned)((ncoarse * 32 + 255) / 256), 256, 0, st>>>(rec, nchunks, ncoarse, crec);
+        k_tone_sum<<<1, 32, 0, st>>>(terms, rec, crec, nchunks, ncoarse, e_lo, t, acc, true);
+        if (t.stretch) k_tone_range<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(fimg, n, t, acc);
+    }
+    k_tone_final<<<blocks_for((int64_t)ow * oh, sm_count), kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, oh, t, acc,
+                                                                                  redo, rgb);
+    if (t.enabled) k_tone_fix<<<sm_count, kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, t, acc, redo, rgb);
+}
+
+void launch_abs_max(const float *v, int64_t n, uint32_t *out, int sm_count, cudaStream_t st)
+{
+    cudaMemsetAsync(out, 0, sizeof(uint32_t), st);
+    k_abs_max<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(v, n, out);
+}
+
+void launch_sequential_sum(const float *v, int64_t n, float max_abs, ToneAcc *acc, void *scratch, int sm_count,
+                           cudaStream_t st)
+{
+    (void)sm_count;
+    const int64_t nchunks = (n + kSumChunk - 1) / kSumChunk;
+    const int64_t ncoarse = (nchunks + kCoarse - 1) / kCoarse;
+    float *terms = (float *)scratch;
+    ChunkSum *rec = (ChunkSum *)(terms + nchunks * kSumChunk);
+    ChunkSum *crec = rec + nchunks * 32;
+    // candidate binades: |S| <= max_abs * n
+    int32_t e_hi = (int32_t)std::floor(std::log2((double)max_abs * (double)n)) + 1;
+    if (e_hi > 128) e_hi = 128;
+    const int32_t e_lo = e_hi - 31;
+    cudaMemsetAsync(acc, 0, sizeof(ToneAcc), st);
+    ToneView t = {};
+    k_tone_terms<<<(unsigned)nchunks, kSumThreads, 0, st>>>(nullptr, v, n, e_lo, terms, rec, acc);
+    k_tone_coarse<<<(unsigned)((ncoarse * 32 + 255) / 256), 256, 0, st>>>(rec, nchunks, ncoarse, crec);
+    k_tone_sum<<<1, 32, 0, st>>>(terms, rec, crec, nchunks, ncoarse, e_lo, t, acc, false);
+}
+
+}  // namespace rtc

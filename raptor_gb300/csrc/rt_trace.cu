@@ -294,11 +294,13 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
 
 // Frame with secondary rays or per-triangle materials: one pixel per lane,
 // the pixel's ray tree walked by shade_pixel_tree (its pending rays in a
-// per-thread frame stack).
+// per-thread frame stack).  fimg non-null: the unclipped colour (3 floats
+// per pixel) is written instead of RGB8.
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_render_tree(SceneView sc, CameraView cam, LightSet lights,
                                                                MaterialTable mt, uint8_t *__restrict__ rgb,
-                                                               int32_t *__restrict__ ids, Counters *ctr)
+                                                               float *__restrict__ fimg, int32_t *__restrict__ ids,
+                                                               Counters *ctr)
 {
     TreeFrame frames[RT_MAX_BOUNCES + 1];
     int tiles_x;
@@ -317,7 +319,13 @@ __global__ void __launch_bounds__(kTraceThreads) k_render_tree(SceneView sc, Cam
         if (live) {
             po = shade_pixel_tree<COUNT>(sc, cam, lights.l, lights.n, mt, x, y, frames, status, &fc);
             const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
-            store_rgb(rgb, pix, po.c);
+            if (fimg) {
+                fimg[3 * pix] = po.c.x;
+                fimg[3 * pix + 1] = po.c.y;
+                fimg[3 * pix + 2] = po.c.z;
+            } else {
+                store_rgb(rgb, pix, po.c);
+            }
             if (ids) ids[pix] = po.id;
         }
         warp_count(&ctr->primary, live);
@@ -389,13 +397,14 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
 }
 
 void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
-                        uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
+                        uint8_t *rgb, float *fimg, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st,
+                        bool count)
 {
     static const int grid = grid_of(k_render_tree<false>, sm_count);
     if (count)
-        k_render_tree<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, ids, ctr);
+        k_render_tree<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, fimg, ids, ctr);
     else
-        k_render_tree<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, ids, ctr);
+        k_render_tree<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, fimg, ids, ctr);
 }
 
 void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t st)

@@ -99,6 +99,13 @@ REFLECTIVITY = {"ico": 0.5, "terrain": 0.35}
 # and without reflections, an index of 1, total internal reflection (2.4)
 GLASS = ({}, {"ri": 1.0}, {"ri": 1.33, "tran": 0.9, "rf_glass": 0.0},
          {"ri": 2.4, "tran": 0.5, "rf_glass": 0.5, "rf_ground": 0.0})
+# tone-mapped frames: (camera::tone_map arguments + gamma, anti-aliasing factors)
+TONE = (({"mode": 0}, (1, 1)), ({"mode": 1}, (1, 1)), ({"mode": 4, "gamma": 2.2}, (1, 1)),
+        ({"mode": 5}, (1, 1)), ({"mode": 6}, (1, 1)), ({"mode": 7, "gamma": 1.8}, (1, 1)),
+        ({"mode": 9}, (1, 1)), ({"mode": 4, "desaturate": True, "key": 0.5}, (1, 1)),
+        ({"mode": 5, "stretch": True}, (1, 1)), ({"mode": 1, "desaturate": True, "stretch": True, "gamma": 2.2}, (2, 2)),
+        ({"mode": 9, "desaturate": True, "stretch": True, "gamma": 1.0}, (3, 2)), ({"mode": 0, "gamma": 2.2}, (1, 1)),
+        ({"mode": 7, "key": 0.3, "stretch": True}, (2, 1)))
 
 
 def small_scenes():
@@ -165,12 +172,19 @@ def main():
         arrays[f"{key}_refl_rf"] = np.array([REFLECTIVITY[key]], np.float32)
         arrays[f"{key}_refl_rgb"] = O.RefScene(s, mat).render(fr)["rgb"]
         arrays[f"{key}_frame"] = np.frombuffer(json.dumps(f).encode(), dtype=np.uint8)
+        # tone mapping and gamma (camera::tone_map, camera::gamma_correct)
+        for k, (tone, aa) in enumerate(TONE):
+            arrays[f"{key}_tone{k}_rgb"] = rs.render(f, aa=aa, tone=tone)["rgb"]
     # per-triangle materials with refraction: the glass sphere
     from raptor_gb300 import scenes
     for k, kw in enumerate(GLASS):
         s, f = scenes.glass_scene(**kw)
         arrays[f"glass{k}_rgb"] = O.RefScene(s, f["materials"]).render(f)["rgb"]
         arrays[f"glass{k}_args"] = np.frombuffer(json.dumps(kw).encode(), dtype=np.uint8)
+        if k == 0:
+            for j, (tone, aa) in enumerate(TONE):
+                arrays[f"glass0_tone{j}_rgb"] = O.RefScene(s, f["materials"]).render(f, aa=aa, tone=tone)["rgb"]
+    arrays["tone_cases"] = np.frombuffer(json.dumps([[t, list(aa)] for t, aa in TONE]).encode(), dtype=np.uint8)
     s, o, d, tmax = soup()
     rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))
     ids, t, u, v = rs.closest(o, d)

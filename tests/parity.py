@@ -92,3 +92,12 @@ def glass_cases():
         out.append((k, json.loads(g[f"glass{k}_args"].tobytes().decode())))
         k += 1
     return out
+
+
+def tone_cases():
+    """(k, tone-map dict, (aa_x, aa_y)) of the tone-mapped golden frames
+    (keys {scene}_tone{k}_rgb)."""
+    import json
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_small.npz"))
+    return [(k, t, tuple(aa)) for k, (t, aa) in enumerate(json.loads(g["tone_cases"].tobytes().decode()))]

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import PIX_FRAC, compare_hits, edge_distance, glass_cases, pixel_agreement
+from parity import PIX_FRAC, compare_hits, edge_distance, glass_cases, pixel_agreement, tone_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -789,3 +789,63 @@ def test_large_scene_33m_triangles(rtlib):
     assert np.array_equal(a0, a1)
     assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
     assert (h1["tri"] >= 0).mean() > 0.5
+
+
+@pytest.mark.parametrize("case", tone_cases(), ids=lambda c: f"tone{c[0]}")
+def test_tone_mapping_vs_reference_and_oracle(rtlib, ctx, oracle, golden, case):
+    """rt_render_tone_mapped: float frame on the anti-aliased grid, the
+    reference's global tone mapping and gamma, then the downsample.  Against
+    the reference's own frames and the restatement's: within one level
+    everywhere but a few pixels (the luminance statistics are summed in
+    double here, in binary32 pixel order there)."""
+    from raptor_gb300 import scenes
+    k, tone, aa = case
+    for key in ("terrain", "glass0", "ico"):
+        if key == "glass0":
+            scene, frame = scenes.glass_scene()
+        else:
+            frame = json.loads(bytes(golden[f"{key}_frame"]).decode())
+            scene = {"verts": golden[f"{key}_verts"], "tris": golden[f"{key}_tris"], "vattr": golden[f"{key}_vattr"]}
+        sc = rtlib.Scene(ctx, scene)
+        got = sc.render_tone_mapped(frame, tone, aa)["rgb"]
+        sc.close()
+        want = oracle.render_tone_mapped(oracle.OracleScene(scene), frame, tone, aa)
+        ref = golden[f"{key}_tone{k}_rgb"]
+        for other in (want, ref):
+            within1, exact, _ = pixel_agreement(got, other)
+            # the icosphere's frames differ at a few edge pixels (tie hits)
+            # before tone mapping, which moves its luminance statistics
+            assert within1 >= (0.995 if key == "ico" else 0.998) and exact >= 0.95, (key, within1, exact)
+
+
+def test_tone_map_off_equals_plain_frames(rtlib, ctx):
+    """Without a tone map the float-frame path gives rt_render's frame at
+    aa 1x1 and rt_render_aa's at 2x2 and 3x2, bit for bit."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=16, res=128)
+    sc = rtlib.Scene(ctx, scene)
+    assert np.array_equal(sc.render_tone_mapped(frame)["rgb"], sc.render(frame)["rgb"])
+    for ax, ay in ((2, 2), (3, 2)):
+        assert np.array_equal(sc.render_tone_mapped(frame, None, (ax, ay))["rgb"], sc.render_aa(frame, ax, ay)["rgb"])
+    with pytest.raises(rtlib.RtError):
+        sc.render_tone_mapped(frame, {"mode": 2})       # local histogram: not a global mode
+    with pytest.raises(rtlib.RtError):
+        sc.render_tone_mapped(frame, {"mode": 0, "gamma": -1.0})
+    sc.close()
+
+
+def test_tone_mapping_terrain_medium_vs_oracle(rtlib, ctx, oracle):
+    """A 131,072-triangle terrain at 480x270 with 2x2 anti-aliasing (518,400
+    samples): exposure and Ferwerda tone mapping with gamma against the
+    restatement."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.terrain_scene(size_pow2=256, xres=480, yres=270)
+    sc = rtlib.Scene(ctx, scene)
+    osc = oracle.OracleScene(scene)
+    for tone in ({"mode": 5, "gamma": 2.2}, {"mode": 9, "desaturate": True, "stretch": True, "gamma": 1.6}):
+        got = sc.render_tone_mapped(frame, tone, (2, 2))["rgb"]
+        fimg = osc.render(oracle.supersampled(frame, 2, 2), threads=os.cpu_count() or 1, want_float=True)["fimg"]
+        want = oracle.downsample_rgb8(oracle.tone_map_frame(fimg, tone), 2, 2)
+        within1, exact, _ = pixel_agreement(got, want)
+        assert within1 >= 0.998 and exact >= 0.95, (tone, within1, exact)
+    sc.close()

@@ -1,0 +1,52 @@
+"""rt_sum_sequential_f32: the GPU reproduces the binary32 sum a sequential
+loop computes (np.cumsum in float32 adds in order and rounds every step),
+bit for bit, on the inputs where a parallel or double-precision sum would
+differ: long runs of equal values (a sky), mixed signs, sums crossing many
+binades, ties, ragged lengths, zeros and a wide exponent range."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def seq(v):
+    v = np.asarray(v, np.float32)
+    return np.float32(0.0) if v.size == 0 else np.cumsum(v, dtype=np.float32)[-1]
+
+
+def cases():
+    rng = np.random.default_rng(61)
+    sky = np.full(600_000, np.log10(np.float32(151.3)), np.float32)
+    lit = rng.uniform(0.5, 2.8, 1_400_000).astype(np.float32)
+    yield "sky_then_lit", np.concatenate([sky, lit, sky[:1000]])
+    yield "log_luminance_2M", np.log10(rng.uniform(1e-3, 683.0, 2_073_600)).astype(np.float32)
+    yield "mixed_sign", rng.normal(0.2, 3.0, 300_000).astype(np.float32)
+    yield "negative", -rng.uniform(0.0, 7.0, 100_003).astype(np.float32)
+    yield "cancelling", np.tile(np.array([1.5, -1.5, 0.25, -0.25], np.float32), 50_000)
+    yield "halves", np.full(70_000, 0.5, np.float32)          # sums on exact grid points: ties
+    yield "tiny_then_big", np.concatenate([np.full(5000, 1e-30, np.float32), np.full(5000, 3.0e4, np.float32)])
+    yield "wide_range", (rng.uniform(-1, 1, 50_000) * 10.0 ** rng.integers(-20, 20, 50_000)).astype(np.float32)
+    for n in (1, 31, 511, 512, 513, 4095, 4097):
+        yield f"n{n}", rng.uniform(0.0, 2.0, n).astype(np.float32)
+    yield "zeros", np.zeros(1000, np.float32)
+
+
+@pytest.mark.parametrize("name,values", list(cases()), ids=lambda x: x if isinstance(x, str) else "")
+def test_sequential_sum_bit_exact(rtlib, ctx, name, values):
+    got = ctx.sum_sequential(values)
+    want = seq(values)
+    assert got.view(np.uint32) == want.view(np.uint32), (name, got, want, np.float64(values).sum())
+
+
+def test_sequential_sum_differs_from_exact_sum(rtlib, ctx):
+    """The runs of equal values make the sequential sum differ from the
+    exactly rounded sum: the kernel follows the sequential one."""
+    v = np.full(600_000, np.log10(np.float32(151.3)), np.float32)
+    exact = np.float32(np.sum(v.astype(np.float64)))
+    got = ctx.sum_sequential(v)
+    assert got == seq(v) and got != exact
+
+
+def test_sequential_sum_rejects_non_finite(rtlib, ctx):
+    with pytest.raises(rtlib.RtError):
+        ctx.sum_sequential(np.array([1.0, np.inf], np.float32))
