@@ -261,6 +261,7 @@ WORKLOADS = {
     "icosphere-20k-512-mirror": ("workload_icosphere_mirror", True, lambda k: max(5, k)),
     "glass-41k-512": ("workload_glass", True, lambda k: max(5, k)),
     "terrain-2M-1080p-tonemap": ("workload_terrain_tonemap", True, lambda k: max(3, k // 4)),
+    "terrain-2M-ingest-ply": ("workload_ingest", False, lambda k: 3),
     "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
     "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
     "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
@@ -508,6 +509,40 @@ def workload_glass(ctx, stream, flush, steps):
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512],
             "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def workload_ingest(ctx, stream, steps):
+    """Scene ingest of the headline terrain (2,097,152 triangles) from a
+    40 MB big-endian binary PLY held in host memory: rt_mesh_parse (host),
+    then rt_scene_upload + rt_bvh_build (device); wall-clock, best of
+    `steps`."""
+    import time
+    import numpy as np
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, _ = scenes.terrain_scene()
+    v, t = scene["verts"], scene["tris"]
+    hdr = ["ply", "format binary_big_endian 1.0", f"element vertex {len(v)}", "property float x",
+           "property float y", "property float z", f"element face {len(t)}",
+           "property list uchar int vertex_indices", "end_header"]
+    faces = np.zeros(len(t), dtype=[("n", "u1"), ("i", ">i4", (3,))])
+    faces["n"] = 3
+    faces["i"] = t
+    data = ("\n".join(hdr) + "\n").encode() + v.astype(">f4").tobytes() + faces.tobytes()
+    best_parse = best_build = float("inf")
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        m = core.parse_mesh(data, core.RT_MESH_PLY)
+        t1 = time.perf_counter()
+        sc = core.Scene(ctx, m)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        sc.close()
+        best_parse = min(best_parse, t1 - t0)
+        best_build = min(best_build, t2 - t1)
+    assert m["tris"].shape[0] == t.shape[0]
+    return {"triangles": int(t.shape[0]), "file_mb": len(data) / 1e6, "parse_ms": best_parse * 1e3,
+            "upload_build_ms": best_build * 1e3, "parse_mb_s": len(data) / 1e6 / best_parse}
 
 
 def workload_terrain_tonemap(ctx, stream, flush, steps):

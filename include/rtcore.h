@@ -295,6 +295,30 @@ rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt
                               const rt_material *materials, int32_t nmaterials, uint8_t *rgb_out, int32_t *hit_ids,
                               rt_render_stats *stats);
 
+/* ------------------------------------------------------- scene ingest */
+
+/* A triangle mesh read from a file, triangulated as the reference's parsers
+ * triangulate it and in the order they fill its primitive_store, so triangle
+ * i here is primitive i there (raytracer/parsers/off_parser.cc:15-100,
+ * ply_parser.cc:480-583, polygon_to_triangles.h:240-389).  verts: 3 floats
+ * per vertex; tris: 3 vertex indices per triangle (rt_scene_upload's
+ * arrays); tri_rgb: 3 bytes per triangle when the file colours its faces
+ * (binary PLY), else NULL; kd: the parser's default diffuse colour (OFF 170,
+ * PLY 200).  Arrays are malloc'd; rt_mesh_free releases them. */
+#define RT_MESH_AUTO 0   /* by file extension: .off, .ply */
+#define RT_MESH_OFF 1
+#define RT_MESH_PLY 2    /* format ascii 1.0 or binary_big_endian 1.0 */
+typedef struct rt_mesh {
+    int32_t nverts, ntris;
+    float *verts;
+    int32_t *tris;
+    uint8_t *tri_rgb;
+    float kd[3];
+} rt_mesh;
+rt_status rt_mesh_load(const char *path, int32_t format, rt_mesh *out);
+rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *out);
+void rt_mesh_free(rt_mesh *mesh);
+
 /* Framebuffer epilogue: the reference's global tone mapping
  * (camera::tone_map, raytracer/camera.cc:1124-1463, with glare and temporal
  * adaptation off; mode values of tone_mapping_mode_t, camera.h:43-45) and

@@ -228,6 +228,8 @@ def ref_lib():
         lib["rref_render_aa"].restype = C.c_double
         lib["rref_render_aa"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32, C.POINTER(Light),
                                           C.c_int32, _U8]
+        lib["rref_parse_mesh"].restype = C.c_int64
+        lib["rref_parse_mesh"].argtypes = [C.c_char_p, C.c_int32, _F, C.c_int64, C.POINTER(C.c_int32)]
         lib["rref_render_tone_mapped"].restype = C.c_double
         lib["rref_render_tone_mapped"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32,
                                                    C.POINTER(Light), C.c_int32, C.POINTER(ToneMap), _U8]
@@ -374,6 +376,20 @@ def render_aa(scene_obj, frame, aa_x, aa_y):
     OracleScene.render, then downsample_rgb8."""
     out = scene_obj.render(supersampled(frame, aa_x, aa_y), want_float=True)
     return downsample_rgb8(out["fimg"], aa_x, aa_y)
+
+
+def ref_parse_mesh(path, kind):
+    """The reference's own OFF (kind 1) / PLY (kind 2) parser on a file:
+    (triangles as an (n, 9) float32 array of a, b, c vertices in
+    primitive_store order, number of materials it made)."""
+    lib = ref_lib()
+    nmat = C.c_int32()
+    n = lib["rref_parse_mesh"](str(path).encode(), kind, None, 0, C.byref(nmat))
+    if n < 0:
+        raise OSError(f"cannot open {path}")
+    out = np.zeros((max(n, 1), 9), np.float32)
+    lib["rref_parse_mesh"](str(path).encode(), kind, _p(out, C.c_float), n, C.byref(nmat))
+    return out[:n], nmat.value
 
 
 def tone_map_frame(fimg, tone):

@@ -15,6 +15,9 @@
 #include <streambuf>
 #include <vector>
 
+#include <fstream>
+#include <list>
+
 #include "bvh.h"
 #include "camera.h"
 #include "coloured_mapper_shader.h"
@@ -22,6 +25,8 @@
 #include "primitive_store.h"
 #include "raytracer.h"
 #include "texture_mapper.h"
+#include "off_parser.h"
+#include "ply_parser.h"
 
 #include "../rtoracle.h"
 
@@ -247,6 +252,39 @@ double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, c
 int32_t rref_morton_code(float x, float y, float z, float xm, float ym, float zm)
 {
     return morton_code(x, y, z, xm, ym, zm);
+}
+
+// A mesh file through the reference's own parser (off_parser.cc /
+// ply_parser.cc; kind 1 OFF, 2 PLY): the vertices of each primitive in
+// primitive_store order (9 floats per triangle, at most max_tris written)
+// and the number of materials the parser made (*nmat).  Returns the
+// triangle count, or -1 if the file cannot be opened.
+int64_t rref_parse_mesh(const char *path, int32_t kind, float *tri_out, int64_t max_tris, int32_t *nmat)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return -1;
+    light_list lights;
+    primitive_store store;
+    std::list<material *> mats;
+    if (kind == 1) {
+        off_parser(f, lights, store, mats, nullptr);
+    } else {
+        camera *cam = nullptr;
+        ply_parser(f, lights, store, mats, &cam);
+    }
+    const int64_t n = (int64_t)store.size();
+    for (int64_t i = 0; i < n && i < max_tris; ++i) {
+        const triangle *t = store.primitive((int)i);
+        const point_t<> v[3] = {t->get_vertex_a(), t->get_vertex_b(), t->get_vertex_c()};
+        for (int k = 0; k < 3; ++k) {
+            tri_out[9 * i + 3 * k] = v[k].x;
+            tri_out[9 * i + 3 * k + 1] = v[k].y;
+            tri_out[9 * i + 3 * k + 2] = v[k].z;
+        }
+    }
+    *nmat = (int32_t)mats.size();
+    for (material *m : mats) delete m;
+    return n;
 }
 
 }  // extern "C"

@@ -31,11 +31,11 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _compile(src: str, extra) -> str:
-    obj = os.path.join(BUILD_DIR, os.path.basename(src).replace(".cu", ".o"))
+    obj = os.path.join(BUILD_DIR, os.path.splitext(os.path.basename(src))[0] + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I", os.path.join(HERE, "..", "include"), "-c", src, "-o", obj, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)

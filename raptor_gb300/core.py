@@ -74,6 +74,14 @@ class RtToneMap(C.Structure):
                 ("desaturate", C.c_int32), ("stretch", C.c_int32), ("gamma", C.c_float)]
 
 
+class RtMesh(C.Structure):
+    _fields_ = [("nverts", C.c_int32), ("ntris", C.c_int32), ("verts", C.POINTER(C.c_float)),
+                ("tris", C.POINTER(C.c_int32)), ("tri_rgb", C.POINTER(C.c_uint8)), ("kd", C.c_float * 3)]
+
+
+RT_MESH_AUTO, RT_MESH_OFF, RT_MESH_PLY = 0, 1, 2
+
+
 class RtRenderStats(C.Structure):
     _fields_ = [("primary_rays", C.c_int64), ("secondary_rays", C.c_int64), ("primary_hits", C.c_int64),
                 ("device_ms", C.c_float), ("status", C.c_int32), ("nodes_fetched", C.c_int64),
@@ -132,6 +140,9 @@ SIGNATURES = [
                               C.POINTER(RtRenderStats)]),
     ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
     ("rt_sum_sequential_f32", C.c_int32, [_P, _P, C.c_int64, C.POINTER(C.c_float)]),
+    ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
+    ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
+    ("rt_mesh_free", None, [C.POINTER(RtMesh)]),
     ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
                                         C.POINTER(RtMaterial), C.c_int32, _P, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_tone_mapped", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight),
@@ -240,6 +251,36 @@ def make_materials(ds):
     for i, d in enumerate(ds):
         arr[i] = make_material(d)
     return arr
+
+
+def _mesh_dict(m: RtMesh):
+    nv, nt = m.nverts, m.ntris
+    verts = np.ctypeslib.as_array(m.verts, shape=(max(nv, 1) * 3,))[: nv * 3].reshape(nv, 3).copy()
+    tris = np.ctypeslib.as_array(m.tris, shape=(max(nt, 1) * 3,))[: nt * 3].reshape(nt, 3).copy()
+    rgb = None
+    if m.tri_rgb:
+        rgb = np.ctypeslib.as_array(m.tri_rgb, shape=(max(nt, 1) * 3,))[: nt * 3].reshape(nt, 3).copy()
+    return {"verts": verts, "tris": tris, "vattr": None, "flags": None, "tri_rgb": rgb, "kd": tuple(m.kd)}
+
+
+def parse_mesh(data: bytes, fmt: int):
+    """rt_mesh_parse on a file's bytes -> scene dict (verts, tris, tri_rgb, kd)."""
+    m = RtMesh()
+    _check(lib().rt_mesh_parse(data, len(data), fmt, C.byref(m)))
+    try:
+        return _mesh_dict(m)
+    finally:
+        lib().rt_mesh_free(C.byref(m))
+
+
+def load_mesh(path, fmt: int = 0):
+    """rt_mesh_load -> scene dict (verts, tris, tri_rgb, kd)."""
+    m = RtMesh()
+    _check(lib().rt_mesh_load(str(path).encode(), fmt, C.byref(m)))
+    try:
+        return _mesh_dict(m)
+    finally:
+        lib().rt_mesh_free(C.byref(m))
 
 
 def rays_array(ogn, dirs, tmax=None):

@@ -1015,3 +1015,6 @@ rt_status rt_render_ao(rt_scene *s, const rt_camera *camera, const rt_material *
 }
 
 }  // extern "C"
+
+// The error setter of the host-only translation units (scene ingest).
+rt_status rt_set_error_message(rt_status code, const char *msg) { return rtc::set_error(code, msg); }

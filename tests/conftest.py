@@ -35,3 +35,9 @@ def ctx(rtlib):
     c = rtlib.Context(0)
     yield c
     c.close()
+
+
+@pytest.fixture(scope="session")
+def golden_npz():
+    import numpy as np
+    return np.load(os.path.join(GOLDEN, "ref_small.npz"))

@@ -140,6 +140,75 @@ def soup(seed=7, n=300):
             o.astype(np.float32), d.astype(np.float32), tmax.astype(np.float32))
 
 
+def _polygons(rng):
+    """Faces for the parser cases: convex and concave polygons, collinear
+    vertices, a star, as (vertex list, face list) in the plane z = const."""
+    verts, faces = [], []
+
+    def add(pts):
+        base = len(verts)
+        verts.extend(pts)
+        faces.append(list(range(base, base + len(pts))))
+
+    for k, n in enumerate((4, 5, 6, 7, 9)):
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        r = rng.uniform(0.5, 1.5, n)
+        add([(float(np.cos(a) * q + 3 * k), float(np.sin(a) * q), 0.25 * k) for a, q in zip(ang, r)])
+    add([(0, 0, 2), (2, 0, 2), (2, 1, 2), (1, 1, 2), (1, 2, 2), (0, 2, 2)])                # L shape
+    add([(0, 0, 3), (1, 0, 3), (2, 0, 3), (2, 1, 3), (0, 1, 3)])                           # collinear vertex
+    star = []
+    for i in range(10):
+        rr = 1.0 if i % 2 == 0 else 0.4
+        star.append((float(rr * np.cos(np.pi * i / 5) + 6), float(rr * np.sin(np.pi * i / 5)), 4.0))
+    add(star)
+    add([(0, 0, 5), (0.5, 0.2, 5), (1, 0, 5), (1, 1, 5), (0.5, 0.8, 5), (0, 1, 5)])       # two notches
+    return verts, faces
+
+
+def mesh_files():
+    """(name, kind 1 OFF / 2 PLY, file bytes) for the parser cases."""
+    import struct
+    from raptor_gb300 import scenes
+    rng = np.random.default_rng(11)
+    sv, st = scenes.geodesic_sphere(3)
+    pv, pf = _polygons(rng)
+    verts = [tuple(float(x) for x in v) for v in sv] + [(x * 0.5 + 5.0, y * 0.5, z * 0.5) for x, y, z in pv]
+    faces = [list(map(int, t)) for t in st] + [[i + len(sv) for i in f] for f in pf]
+    out = []
+    # OFF, LF and CRLF line ends, padded fields
+    for name, nl in (("off_lf", "\n"), ("off_crlf", "\r\n")):
+        lines = ["OFF", f"{len(verts)} {len(faces)} 0"]
+        lines += [f"{x!r} {y!r}  {z!r}" if i % 3 else f"  {x:.9g}\t{y:.9g} {z:.9g}" for i, (x, y, z) in enumerate(verts)]
+        lines += [" ".join([str(len(f))] + [str(i) for i in f]) for f in faces]
+        out.append((name, 1, (nl.join(lines) + nl).encode()))
+    # PLY ascii: comments, normals and colours on the vertices, degenerate triangles
+    dverts = verts + [(9.0, 9.0, 9.0), (9.0, 9.0, 9.0), (10.0, 9.0, 9.0), (11.0, 9.0, 9.0)]
+    dfaces = faces + [[len(verts), len(verts) + 1, len(verts) + 2], [len(verts), len(verts) + 2, len(verts) + 3]]
+    hdr = ["ply", "format ascii 1.0", "comment made by the parser tests", f"element vertex {len(dverts)}",
+           "property float x", "property float y", "property float z", "property float nx", "property float ny",
+           "property float nz", "property uchar red", "property uchar green", "property uchar blue",
+           f"element face {len(dfaces)}", "property list uchar int vertex_indices", "end_header"]
+    body = [f"{x!r} {y!r} {z!r} 0 0 1 {i % 256} 7 9" for i, (x, y, z) in enumerate(dverts)]
+    body += [" ".join([str(len(f))] + [str(i) for i in f]) for f in dfaces]
+    out.append(("ply_ascii", 2, ("\n".join(hdr + body) + "\n").encode()))
+    # PLY binary big endian: vertex colour + normal + an extra float, face
+    # intensity before and colour + an extra uchar after the index list
+    hdr = ["ply", "format binary_big_endian 1.0", "obj_info synthetic", f"element vertex {len(dverts)}",
+           "property float x", "property float y", "property float z", "property uchar red",
+           "property uchar green", "property uchar blue", "property float nx", "property float ny",
+           "property float nz", "property float confidence", f"element face {len(dfaces)}",
+           "property uchar intensity", "property list uchar int vertex_indices", "property uchar red",
+           "property uchar green", "property uchar blue", "property uchar flags", "end_header"]
+    data = bytearray(("\n".join(hdr) + "\n").encode())
+    for i, (x, y, z) in enumerate(dverts):
+        data += struct.pack(">fff", x, y, z) + bytes([i % 256, 3, 5]) + struct.pack(">ffff", 0, 0, 1, 0.5)
+    palette = [(200, 10, 10), (10, 200, 10), (10, 10, 200), (90, 90, 90)]
+    for k, f in enumerate(dfaces):
+        data += bytes([17]) + bytes([len(f)]) + struct.pack(f">{len(f)}i", *f) + bytes(palette[k % 4]) + bytes([1])
+    out.append(("ply_binary", 2, bytes(data)))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference/RAPTor")
@@ -185,6 +254,19 @@ def main():
             for j, (tone, aa) in enumerate(TONE):
                 arrays[f"glass0_tone{j}_rgb"] = O.RefScene(s, f["materials"]).render(f, aa=aa, tone=tone)["rgb"]
     arrays["tone_cases"] = np.frombuffer(json.dumps([[t, list(aa)] for t, aa in TONE]).encode(), dtype=np.uint8)
+    # scene ingest: the reference's own OFF and PLY parsers
+    import tempfile
+    cases = mesh_files()
+    with tempfile.TemporaryDirectory() as td:
+        for k, (name, kind, data) in enumerate(cases):
+            path = os.path.join(td, f"{name}.{'off' if kind == 1 else 'ply'}")
+            open(path, "wb").write(data)
+            tris, nmat = O.ref_parse_mesh(path, kind)
+            arrays[f"mesh{k}_bytes"] = np.frombuffer(data, np.uint8)
+            arrays[f"mesh{k}_kind"] = np.array([kind], np.int32)
+            arrays[f"mesh{k}_tris"] = tris
+            arrays[f"mesh{k}_nmat"] = np.array([nmat], np.int32)
+            print(f"mesh {name}: {tris.shape[0]} triangles, {nmat} materials")
     s, o, d, tmax = soup()
     rs = O.RefScene(s, dict(__import__("raptor_gb300.scenes", fromlist=["x"]).DEFAULT_MATERIAL))
     ids, t, u, v = rs.closest(o, d)

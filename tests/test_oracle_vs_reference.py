@@ -51,3 +51,43 @@ def test_random_material_tables_equal_reference(ref, seed):
     ro = ref.OracleScene(scene).render(frame)
     within1, exact, _ = pixel_agreement(ro["rgb"], rr["rgb"])
     assert exact == 1.0, (exact, within1)
+
+
+def random_polygon_off(seed, nfaces=1500):
+    """An OFF file of random planar polygons in random orientations: star-
+    shaped and spiky (concave) rings of 3..14 vertices, some with repeated
+    or collinear vertices."""
+    rng = np.random.default_rng(seed)
+    verts, faces = [], []
+    for _ in range(nfaces):
+        n = int(rng.integers(3, 15))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, n))
+        r = rng.uniform(0.2, 1.5, n) if rng.uniform() < 0.6 else np.ones(n)
+        pts = np.stack([np.cos(ang) * r, np.sin(ang) * r, np.zeros(n)], 1)
+        if rng.uniform() < 0.1 and n > 3:
+            pts[1] = 0.5 * (pts[0] + pts[2])          # a collinear middle vertex
+        q = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+        pts = pts @ q.T + rng.uniform(-20, 20, 3)
+        base = len(verts)
+        verts.extend(pts.astype(np.float32).tolist())
+        faces.append(list(range(base, base + n)))
+    lines = ["OFF", f"{len(verts)} {len(faces)} 0"]
+    lines += [" ".join(repr(float(np.float32(c))) for c in v) for v in verts]
+    lines += [" ".join([str(len(f))] + [str(i) for i in f]) for f in faces]
+    return ("\n".join(lines) + "\n").encode()
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_polygons_triangulated_as_reference(ref, tmp_path, seed):
+    """rt_mesh_parse triangulates random concave polygons exactly as the
+    reference's face_to_triangles (polygon_to_triangles.h), triangle by
+    triangle."""
+    from raptor_gb300 import core
+    data = random_polygon_off(seed)
+    p = tmp_path / "poly.off"
+    p.write_bytes(data)
+    want, _ = ref.ref_parse_mesh(p, 1)
+    m = core.parse_mesh(data, core.RT_MESH_OFF)
+    got = m["verts"][m["tris"]].reshape(-1, 9)
+    assert got.shape == want.shape
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
