@@ -300,20 +300,27 @@ rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt
 /* A triangle mesh read from a file, triangulated as the reference's parsers
  * triangulate it and in the order they fill its primitive_store, so triangle
  * i here is primitive i there (raytracer/parsers/off_parser.cc:15-100,
- * ply_parser.cc:480-583, polygon_to_triangles.h:240-389).  verts: 3 floats
- * per vertex; tris: 3 vertex indices per triangle (rt_scene_upload's
- * arrays); tri_rgb: 3 bytes per triangle when the file colours its faces
- * (binary PLY), else NULL; kd: the parser's default diffuse colour (OFF 170,
- * PLY 200).  Arrays are malloc'd; rt_mesh_free releases them. */
-#define RT_MESH_AUTO 0   /* by file extension: .off, .ply */
+ * ply_parser.cc:480-583, obj_parser.cc:762-857, polygon_to_triangles.h:
+ * 240-389).  verts: 3 floats per vertex; tris: 3 vertex indices per triangle
+ * (rt_scene_upload's arrays); tri_rgb: 3 bytes per triangle when the file
+ * colours its faces (binary PLY), else NULL; tri_mat: per triangle the
+ * material of an OBJ file (0: the default, i: the i-th distinct usemtl name
+ * in order of first use; nmat of them), else NULL; kd: the parser's default
+ * diffuse colour (OFF 170, PLY and OBJ 200).  OBJ material libraries
+ * (mtllib) and vertex normals / texture coordinates are read past, not
+ * returned.  Arrays are malloc'd; rt_mesh_free releases them. */
+#define RT_MESH_AUTO 0   /* by file extension: .off, .ply, .obj */
 #define RT_MESH_OFF 1
 #define RT_MESH_PLY 2    /* format ascii 1.0 or binary_big_endian 1.0 */
+#define RT_MESH_OBJ 3
 typedef struct rt_mesh {
     int32_t nverts, ntris;
     float *verts;
     int32_t *tris;
     uint8_t *tri_rgb;
     float kd[3];
+    int32_t *tri_mat;
+    int32_t nmat;
 } rt_mesh;
 rt_status rt_mesh_load(const char *path, int32_t format, rt_mesh *out);
 rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *out);

@@ -1,5 +1,5 @@
-// Definitions of the image-I/O and FFT names that the reference's camera.cc
-// and texture readers reference (declared in shim/).  TEST INFRASTRUCTURE
+// Definitions of the image-I/O and FFT names that the reference's camera.cc,
+// picture_functions.cc and texture readers reference (declared in shim/).  TEST INFRASTRUCTURE
 // ONLY: the harness never writes or reads image files nor enables the glare
 // filter, so none of these is ever called; each aborts if it were.
 #include <cstdlib>
@@ -9,6 +9,11 @@
 extern "C" {
 #include <jpeglib.h>
 #include <png.h>
+#include <tga.h>
+TGA *TGAOpen(char *, const char *) { std::abort(); }
+int TGAReadImage(TGA *, TGAData *) { std::abort(); }
+int TGAWriteImage(TGA *, TGAData *) { std::abort(); }
+void TGAClose(TGA *) { std::abort(); }
 jmp_buf &png_jmpbuf(png_structp) { std::abort(); }
 int png_sig_cmp(png_bytep, png_size_t, png_size_t) { std::abort(); }
 png_structp png_create_read_struct(const char *, void *, void *, void *) { std::abort(); }
@@ -56,3 +61,33 @@ fftwf_plan fftwf_plan_dft_r2c_3d(int n0, int n1, int n2, float *in, fftwf_comple
 fftwf_plan fftwf_plan_many_dft_r2c(int rank, const int *n, int howmany, float *in, const int *inembed, int istride, int idist, fftwf_complex *out, const int *onembed, int ostride, int odist, unsigned flags) { std::abort(); }
 fftwf_plan fftwf_plan_many_dft_c2r(int rank, const int *n, int howmany, fftwf_complex *in, const int *inembed, int istride, int idist, float *out, const int *onembed, int ostride, int odist, unsigned flags) { std::abort(); }
 }
+
+// The case-insensitive comparison of the Boost.StringAlgo stand-in
+// (shim/boost/algorithm/string.hpp), used by the reference's picture loader.
+#include <cctype>
+#include <string>
+#include "boost/algorithm/string.hpp"
+namespace boost {
+bool iequals(const std::string &a, const std::string &b)
+{
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+        if (std::tolower((unsigned char)a[i]) != std::tolower((unsigned char)b[i])) return false;
+    return true;
+}
+}  // namespace boost
+
+// boost::filesystem::extension of the Boost.Filesystem stand-in
+// (shim/boost/filesystem.hpp): the last '.' and what follows it.
+#include "boost/filesystem.hpp"
+namespace boost {
+namespace filesystem {
+std::string extension(const std::string &p)
+{
+    const size_t dot = p.find_last_of('.');
+    const size_t slash = p.find_last_of('/');
+    if (dot == std::string::npos || (slash != std::string::npos && dot < slash)) return std::string();
+    return p.substr(dot);
+}
+}  // namespace filesystem
+}  // namespace boost

@@ -25,6 +25,7 @@
 #include "primitive_store.h"
 #include "raytracer.h"
 #include "texture_mapper.h"
+#include "obj_parser.h"
 #include "off_parser.h"
 #include "ply_parser.h"
 
@@ -255,7 +256,7 @@ int32_t rref_morton_code(float x, float y, float z, float xm, float ym, float zm
 }
 
 // A mesh file through the reference's own parser (off_parser.cc /
-// ply_parser.cc; kind 1 OFF, 2 PLY): the vertices of each primitive in
+// ply_parser.cc / obj_parser.cc; kind 1 OFF, 2 PLY, 3 OBJ): the vertices of each primitive in
 // primitive_store order (9 floats per triangle, at most max_tris written)
 // and the number of materials the parser made (*nmat).  Returns the
 // triangle count, or -1 if the file cannot be opened.
@@ -268,6 +269,9 @@ int64_t rref_parse_mesh(const char *path, int32_t kind, float *tri_out, int64_t 
     std::list<material *> mats;
     if (kind == 1) {
         off_parser(f, lights, store, mats, nullptr);
+    } else if (kind == 3) {
+        camera *cam = nullptr;
+        obj_parser(f, std::string(""), lights, store, mats, &cam);
     } else {
         camera *cam = nullptr;
         ply_parser(f, lights, store, mats, &cam);

@@ -76,10 +76,11 @@ class RtToneMap(C.Structure):
 
 class RtMesh(C.Structure):
     _fields_ = [("nverts", C.c_int32), ("ntris", C.c_int32), ("verts", C.POINTER(C.c_float)),
-                ("tris", C.POINTER(C.c_int32)), ("tri_rgb", C.POINTER(C.c_uint8)), ("kd", C.c_float * 3)]
+                ("tris", C.POINTER(C.c_int32)), ("tri_rgb", C.POINTER(C.c_uint8)), ("kd", C.c_float * 3),
+                ("tri_mat", C.POINTER(C.c_int32)), ("nmat", C.c_int32)]
 
 
-RT_MESH_AUTO, RT_MESH_OFF, RT_MESH_PLY = 0, 1, 2
+RT_MESH_AUTO, RT_MESH_OFF, RT_MESH_PLY, RT_MESH_OBJ = 0, 1, 2, 3
 
 
 class RtRenderStats(C.Structure):
@@ -260,7 +261,11 @@ def _mesh_dict(m: RtMesh):
     rgb = None
     if m.tri_rgb:
         rgb = np.ctypeslib.as_array(m.tri_rgb, shape=(max(nt, 1) * 3,))[: nt * 3].reshape(nt, 3).copy()
-    return {"verts": verts, "tris": tris, "vattr": None, "flags": None, "tri_rgb": rgb, "kd": tuple(m.kd)}
+    mat = None
+    if m.tri_mat:
+        mat = np.ctypeslib.as_array(m.tri_mat, shape=(max(nt, 1),))[:nt].copy()
+    return {"verts": verts, "tris": tris, "vattr": None, "flags": None, "tri_rgb": rgb, "kd": tuple(m.kd),
+            "tri_mat": mat, "nmat": m.nmat}
 
 
 def parse_mesh(data: bytes, fmt: int):

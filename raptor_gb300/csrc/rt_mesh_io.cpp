@@ -15,6 +15,11 @@
 //                                     colour); degenerate triangles dropped;
 //                                     default diffuse 200, face colours in
 //                                     binary files
+//   raytracer/parsers/obj_parser.cc   v / vt / vn / f (v, v/t, v//n, v/t/n,
+//                                     negative indices relative to the end),
+//                                     usemtl groups, g / o / s and comments
+//                                     skipped, degenerate triangles dropped;
+//                                     material libraries are not read
 //   raytracer/parsers/polygon_to_triangles.h  the ear-clipping of faces with
 //                                     more than 3 vertices (face_to_triangles)
 //   parsers/parser_common.h           token rules: numbers read by atof/atoi
@@ -54,7 +59,9 @@ struct Mesh {
     std::vector<float> verts;
     std::vector<int32_t> tris;
     std::vector<uint8_t> rgb;   // per triangle, when the file colours its faces
-    bool coloured = false;
+    std::vector<int32_t> mat;   // per triangle, when the file names materials
+    bool coloured = false, named = false;
+    int32_t cur_mat = 0, nmat = 1;
     float kd = 0.0f;
     V3 vert(int32_t i) const { return {verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]}; }
     void add(int32_t a, int32_t b, int32_t c, const uint8_t *col)
@@ -63,6 +70,7 @@ struct Mesh {
         tris.push_back(b);
         tris.push_back(c);
         if (coloured) rgb.insert(rgb.end(), col, col + 3);
+        if (named) mat.push_back(cur_mat);
     }
 };
 
@@ -438,6 +446,121 @@ rt_status parse_ply(Cursor cur, Mesh &m)
     return RT_OK;
 }
 
+// obj_parser.cc: the next statement, past white space and '#' comments.
+const char *obj_statement(const char *at, const char *end)
+{
+    while (at < end) {
+        if (*at == '#') {
+            while (at < end && *at != '\n') ++at;
+            ++at;
+        } else if (*at == ' ' || *at == '\t' || *at == '\n' || *at == '\r') {
+            ++at;
+        } else {
+            return at;
+        }
+    }
+    return end;
+}
+
+rt_status parse_obj(Cursor cur, Mesh &m)
+{
+    m.kd = 200.0f;
+    m.named = true;
+    std::vector<std::string> names;   // usemtl names in order of first use (index + 1)
+    long nvt = 0, nvn = 0;
+    std::vector<int32_t> face;
+    const char *const last = cur.end - 1;   // the reference stops one byte before the end
+    while (cur.c < last) {
+        cur.c = obj_statement(cur.c, last);
+        if (cur.c >= last) break;
+        if (cur.starts("mtllib")) {
+            cur.next_line();   // material libraries are not read
+        } else if (cur.starts("usemtl")) {
+            // raptor_parsers::get_next_string: the word after the keyword
+            while (cur.c < cur.end && *cur.c != ' ') ++cur.c;
+            cur.skip_spaces();
+            const char *s = cur.c;
+            while (cur.c < cur.end && *cur.c != ' ' && *cur.c != '\n' && *cur.c != '\r') ++cur.c;
+            const std::string name(s, cur.c);
+            size_t k = 0;
+            while (k < names.size() && names[k] != name) ++k;
+            if (k == names.size()) names.push_back(name);
+            m.cur_mat = (int32_t)k + 1;
+            --cur.c;
+            cur.next_line();
+        } else if (cur.starts("vn")) {
+            cur.next_float();
+            cur.next_float();
+            cur.next_float();
+            cur.next_line();
+            ++nvn;
+        } else if (cur.starts("vt")) {
+            cur.next_float();
+            cur.next_float();
+            cur.next_line();
+            ++nvt;
+        } else if (*cur.c == 'f') {
+            // find_vertex: past the keyword, then spaces
+            auto find_vertex = [&]() {
+                while (cur.c < cur.end && *cur.c != ' ' && *cur.c != '\n' && *cur.c != '\r') ++cur.c;
+                cur.skip_spaces();
+            };
+            // is_triplet_delimiter: past one character, then to '/' or the field's end
+            auto delimiter = [&]() {
+                ++cur.c;
+                while (cur.c < cur.end && *cur.c != '/' && *cur.c != ' ' && *cur.c != '\n' && *cur.c != '\r') ++cur.c;
+                return cur.c < cur.end && *cur.c == '/';
+            };
+            const long nv = (long)(m.verts.size() / 3);
+            face.clear();
+            find_vertex();
+            while (cur.c < cur.end && *cur.c != '\n' && *cur.c != '\r') {
+                long vi = std::strtol(cur.c, nullptr, 10);
+                vi = (vi < 0) ? nv + vi : vi - 1;
+                if (vi < 0 || vi >= nv) return bad("rt_mesh: OBJ vertex index out of range");
+                face.push_back((int32_t)vi);
+                if (delimiter()) {
+                    if (cur.c + 1 < cur.end && cur.c[1] != '/') {
+                        ++cur.c;
+                        long ti = std::strtol(cur.c, nullptr, 10);
+                        ti = (ti < 0) ? nvt + ti : ti - 1;
+                        if (ti < 0 || ti >= nvt) return bad("rt_mesh: OBJ texture index out of range");
+                    }
+                    if (delimiter()) {
+                        ++cur.c;
+                        long ni = std::strtol(cur.c, nullptr, 10);
+                        ni = (ni < 0) ? nvn + ni : ni - 1;
+                        if (ni < 0 || ni >= nvn) return bad("rt_mesh: OBJ normal index out of range");
+                    }
+                }
+                find_vertex();
+            }
+            if (cur.c < cur.end) ++cur.c;
+            if (face.size() == 3) {
+                // obj_parser.cc drops triangles with two equal points or
+                // parallel unit edges (zero cross product)
+                const V3 a0 = m.vert(face[0]), b0 = m.vert(face[1]), c0 = m.vert(face[2]);
+                if (differ(a0, b0) && differ(a0, c0) && differ(b0, c0)) {
+                    const V3 n = cross(unit(sub(a0, b0)), unit(sub(b0, c0)));
+                    if (dot(n, n) > 0.0f) m.add(face[0], face[1], face[2], nullptr);
+                }
+            } else {
+                triangulate(m, face, nullptr);
+            }
+        } else if (*cur.c == 'v') {
+            m.verts.push_back(cur.next_float());
+            m.verts.push_back(cur.next_float());
+            m.verts.push_back(cur.next_float());
+            cur.next_line();
+        } else {
+            // g, o, s and statements the reference does not know: the line is skipped
+            cur.next_line();
+        }
+    }
+    m.nmat = (int32_t)names.size() + 1;
+    return RT_OK;
+}
+
 bool ends_with(const std::string &s, const char *suf)
 {
     const size_t n = std::strlen(suf);
@@ -462,7 +585,8 @@ rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *
 {
     if (!data || !out || len < 0) return bad("rt_mesh_parse: NULL argument");
     std::memset(out, 0, sizeof(*out));
-    if (format != RT_MESH_OFF && format != RT_MESH_PLY) return bad("rt_mesh_parse: format must be RT_MESH_OFF or PLY");
+    if (format != RT_MESH_OFF && format != RT_MESH_PLY && format != RT_MESH_OBJ)
+        return bad("rt_mesh_parse: format must be RT_MESH_OFF, PLY or OBJ");
     // a NUL-terminated copy: the token rules read up to the next separator
     std::vector<char> buf((size_t)len + 1, '\0');
     std::memcpy(buf.data(), data, (size_t)len);
@@ -470,7 +594,7 @@ rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *
     Mesh m;
     rt_status st;
     try {
-        st = (format == RT_MESH_OFF) ? parse_off(cur, m) : parse_ply(cur, m);
+        st = (format == RT_MESH_OFF) ? parse_off(cur, m) : (format == RT_MESH_PLY) ? parse_ply(cur, m) : parse_obj(cur, m);
     } catch (const std::bad_alloc &) {
         return rt_set_error_message(RT_ERR_OUT_OF_MEMORY, "rt_mesh_parse: out of host memory");
     }
@@ -480,8 +604,10 @@ rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *
     out->verts = copy_out(m.verts);
     out->tris = copy_out(m.tris);
     out->tri_rgb = m.coloured ? copy_out(m.rgb) : nullptr;
+    out->tri_mat = m.named ? copy_out(m.mat) : nullptr;
+    out->nmat = m.nmat;
     out->kd[0] = out->kd[1] = out->kd[2] = m.kd;
-    if (!out->verts || !out->tris || (m.coloured && !out->tri_rgb)) {
+    if (!out->verts || !out->tris || (m.coloured && !out->tri_rgb) || (m.named && !out->tri_mat)) {
         rt_mesh_free(out);
         return rt_set_error_message(RT_ERR_OUT_OF_MEMORY, "rt_mesh_parse: out of host memory");
     }
@@ -496,7 +622,8 @@ rt_status rt_mesh_load(const char *path, int32_t format, rt_mesh *out)
         const std::string p(path);
         if (ends_with(p, ".off")) format = RT_MESH_OFF;
         else if (ends_with(p, ".ply")) format = RT_MESH_PLY;
-        else return bad("rt_mesh_load: unknown file extension (expected .off or .ply)");
+        else if (ends_with(p, ".obj")) format = RT_MESH_OBJ;
+        else return bad("rt_mesh_load: unknown file extension (expected .off, .ply or .obj)");
     }
     FILE *f = std::fopen(path, "rb");
     if (!f) return bad("rt_mesh_load: cannot open the file");
@@ -514,9 +641,11 @@ void rt_mesh_free(rt_mesh *m)
     std::free(m->verts);
     std::free(m->tris);
     std::free(m->tri_rgb);
+    std::free(m->tri_mat);
     m->verts = nullptr;
     m->tris = nullptr;
     m->tri_rgb = nullptr;
+    m->tri_mat = nullptr;
     m->nverts = m->ntris = 0;
 }
 

@@ -206,6 +206,30 @@ def mesh_files():
     for k, f in enumerate(dfaces):
         data += bytes([17]) + bytes([len(f)]) + struct.pack(f">{len(f)}i", *f) + bytes(palette[k % 4]) + bytes([1])
     out.append(("ply_binary", 2, bytes(data)))
+    # OBJ: v / vt / vn, faces as v, v/t, v//n and v/t/n with negative
+    # (relative) indices, usemtl groups, g / o / s lines, comments, CRLF
+    for name, nl in (("obj_lf", "\n"), ("obj_crlf", "\r\n")):
+        lines = ["# synthetic OBJ for the parser tests", "o scene", "g sphere"]
+        lines += [f"v {x!r} {y!r} {z!r}" for x, y, z in dverts]
+        lines += [f"vt {float(i % 7) / 7!r} {float(i % 5) / 5!r}" for i in range(len(dverts))]
+        lines += [f"vn {x!r} {y!r} {z + 0.5!r}" for x, y, z in dverts]
+        mats = ["stone", "glass", "stone", "metal"]
+        for k, f in enumerate(dfaces):
+            if k % 37 == 0:
+                lines.append(f"usemtl {mats[(k // 37) % 4]}")
+            if k % 50 == 0:
+                lines.append(f"s {k % 2}")
+            form = k % 4
+            if form == 0:
+                toks = [str(i + 1) for i in f]
+            elif form == 1:
+                toks = [f"{i + 1}/{i + 1}" for i in f]
+            elif form == 2:
+                toks = [f"{i - len(dverts)}//{i + 1}" for i in f]
+            else:
+                toks = [f"{i + 1}/{i - len(dverts)}/{i - len(dverts)}" for i in f]
+            lines.append("f " + " ".join(toks))
+        out.append((name, 3, (nl.join(lines) + nl).encode()))
     return out
 
 
@@ -259,7 +283,7 @@ def main():
     cases = mesh_files()
     with tempfile.TemporaryDirectory() as td:
         for k, (name, kind, data) in enumerate(cases):
-            path = os.path.join(td, f"{name}.{'off' if kind == 1 else 'ply'}")
+            path = os.path.join(td, f"{name}.{('off', 'ply', 'obj')[kind - 1]}")
             open(path, "wb").write(data)
             tris, nmat = O.ref_parse_mesh(path, kind)
             arrays[f"mesh{k}_bytes"] = np.frombuffer(data, np.uint8)

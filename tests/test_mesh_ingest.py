@@ -3,7 +3,8 @@ triangles the reference's own parsers put into its primitive_store, in the
 same order and bit for bit (tests/golden: synthetic files with convex and
 concave polygons, collinear vertices, a star, degenerate triangles, CRLF
 line ends, comments, vertex normals and colours, face intensity and face
-colours, big-endian binary), so triangle ids match the reference's."""
+colours, big-endian binary, OBJ index forms v, v/t, v//n, v/t/n with
+negative indices, usemtl groups), so triangle ids match the reference's."""
 import numpy as np
 import pytest
 
@@ -35,8 +36,26 @@ def test_mesh_matches_reference_parser(rtlib, golden_npz, k):
     if m["tri_rgb"] is not None:
         # one material per distinct face colour, plus the default one
         assert len({tuple(c) for c in m["tri_rgb"]}) + 1 == nmat
+    elif m["tri_mat"] is not None:
+        # OBJ: the default material plus one per distinct usemtl name
+        assert m["nmat"] == nmat and set(np.unique(m["tri_mat"])) <= set(range(nmat))
     else:
         assert nmat == 1
+
+
+def test_obj_material_groups(rtlib, golden_npz):
+    """usemtl switches the material of the triangles that follow; names
+    repeat onto their first index."""
+    k = next(i for i in mesh_cases() if int(golden_npz[f"mesh{i}_kind"][0]) == 3)
+    text = golden_npz[f"mesh{k}_bytes"].tobytes().decode()
+    m = rtlib.parse_mesh(text.encode(), rtlib.RT_MESH_OBJ)
+    # the first usemtl precedes the first face: no triangle keeps material 0
+    assert m["tri_mat"].min() == 1 and m["nmat"] == 4
+    names = []
+    for line in text.splitlines():
+        if line.startswith("usemtl "):
+            names.append(line.split()[1])
+    assert list(dict.fromkeys(names)) == ["stone", "glass", "metal"]
 
 
 def test_mesh_load_from_file_and_errors(rtlib, golden_npz, tmp_path):

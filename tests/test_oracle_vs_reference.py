@@ -91,3 +91,34 @@ def test_random_polygons_triangulated_as_reference(ref, tmp_path, seed):
     got = m["verts"][m["tris"]].reshape(-1, 9)
     assert got.shape == want.shape
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_random_polygons_obj_as_reference(ref, tmp_path, seed):
+    """The same random polygons as an OBJ file (index forms v, v/t, v//n,
+    v/t/n, some negative): rt_mesh_parse matches obj_parser triangle by
+    triangle."""
+    from raptor_gb300 import core
+    rng = np.random.default_rng(seed)
+    off = random_polygon_off(seed, nfaces=800).decode().splitlines()
+    nv, nf, _ = map(int, off[1].split())
+    verts = off[2:2 + nv]
+    lines = ["# random polygons"] + [f"v {v}" for v in verts] + [f"vn 0 0 1", "vt 0.5 0.5"]
+    for k, f in enumerate(off[2 + nv:2 + nv + nf]):
+        idx = [int(x) for x in f.split()[1:]]
+        if k % 97 == 0:
+            lines.append(f"usemtl m{k % 3}")
+        toks = []
+        for i in idx:
+            vi = str(i + 1) if rng.uniform() < 0.7 else str(i - nv)
+            form = int(rng.integers(0, 4))
+            toks.append([vi, f"{vi}/1", f"{vi}//1", f"{vi}/-1/1"][form])
+        lines.append("f " + " ".join(toks))
+    data = ("\n".join(lines) + "\n").encode()
+    p = tmp_path / "poly.obj"
+    p.write_bytes(data)
+    want, nmat = ref.ref_parse_mesh(p, 3)
+    m = core.parse_mesh(data, core.RT_MESH_OBJ)
+    got = m["verts"][m["tris"]].reshape(-1, 9)
+    assert got.shape == want.shape and m["nmat"] == nmat
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
