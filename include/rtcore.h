@@ -326,16 +326,20 @@ rt_status rt_mesh_load(const char *path, int32_t format, rt_mesh *out);
 rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *out);
 void rt_mesh_free(rt_mesh *mesh);
 
-/* Framebuffer epilogue: the reference's global tone mapping
+/* Framebuffer epilogue: the reference's global and histogram tone mapping
  * (camera::tone_map, raytracer/camera.cc:1124-1463, with glare and temporal
  * adaptation off; mode values of tone_mapping_mode_t, camera.h:43-45) and
  * gamma correction (camera::gamma_correct, camera.cc:1466-1500).  key, xw,
  * yw, desaturate and stretch are tone_map's key, xw, yw, ds and sc (its
  * defaults: 0.18, 1/3, 1/3, 0, 0); gamma > 0 applies gamma_correct(gamma)
  * after tone mapping (2.2 selects the sRGB curve, as in the reference), 0
- * none. */
+ * none.  The histogram modes (camera::histogram_tone_map, camera.cc:
+ * 1843-2062) resample the frame to one block per degree of the camera's
+ * view and need a view of at least 2 degrees each way. */
 #define RT_TONE_NONE 0
 #define RT_TONE_GLOBAL_CONTRAST 1
+#define RT_TONE_LOCAL_HISTOGRAM 2          /* camera::histogram_tone_map(false) */
+#define RT_TONE_LOCAL_HUMAN_HISTOGRAM 3    /* histogram_tone_map(true): visibility-limited */
 #define RT_TONE_GLOBAL_NON_LINEAR 4
 #define RT_TONE_GLOBAL_EXPOSURE 5
 #define RT_TONE_GLOBAL_AVG_LUMINANCE 6
@@ -361,6 +365,14 @@ rt_status rt_render_tone_mapped(rt_scene *scene, const rt_camera *camera, int32_
                                 const rt_light *lights, int32_t nlights, const rt_material *materials,
                                 int32_t nmaterials, const rt_tone_map *tone, uint8_t *rgb_out,
                                 rt_render_stats *stats);
+
+/* The tone map of rt_render_tone_mapped applied to a given float frame
+ * (3 floats per sample in 0..255 units, the camera's xres * aa_x by
+ * yres * aa_y grid, row 0 at the bottom; host or device), e.g. one made by
+ * rt_render_float: camera::tone_map + gamma_correct + clip_image_to_rgb on
+ * a camera whose image is that frame. */
+rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const float *fimg,
+                            const rt_tone_map *tone, uint8_t *rgb_out);
 
 /* The binary32 sum of values[0..n) in index order, rounded after every
  * addition exactly as a sequential loop `s += values[i]` rounds it (the way

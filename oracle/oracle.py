@@ -39,10 +39,11 @@ class Material(C.Structure):
 
 class ToneMap(C.Structure):
     _fields_ = [("mode", C.c_int32), ("key", C.c_float), ("xw", C.c_float), ("yw", C.c_float),
-                ("desaturate", C.c_int32), ("stretch", C.c_int32), ("gamma", C.c_float)]
+                ("desaturate", C.c_int32), ("stretch", C.c_int32), ("gamma", C.c_float),
+                ("cam_w", C.c_float), ("cam_h", C.c_float), ("cam_t", C.c_float)]
 
 
-def make_tone_map(d):
+def make_tone_map(d, camera=None):
     """Tone-map dict -> ToneMap; the defaults are camera::tone_map's
     (key 0.18, white point 1/3, 1/3, no desaturation or stretch) and no
     gamma correction."""
@@ -54,6 +55,8 @@ def make_tone_map(d):
     t.desaturate = int(bool(d.get("desaturate", False)))
     t.stretch = int(bool(d.get("stretch", False)))
     t.gamma = d.get("gamma", 0.0)
+    if camera is not None:
+        t.cam_w, t.cam_h, t.cam_t = camera["w"], camera["h"], camera["t"]
     return t
 
 
@@ -230,6 +233,8 @@ def ref_lib():
                                           C.c_int32, _U8]
         lib["rref_parse_mesh"].restype = C.c_int64
         lib["rref_parse_mesh"].argtypes = [C.c_char_p, C.c_int32, _F, C.c_int64, C.POINTER(C.c_int32)]
+        lib["rref_tone_map_image"].restype = None
+        lib["rref_tone_map_image"].argtypes = [C.POINTER(Camera), C.c_int32, C.c_int32, _F, C.POINTER(ToneMap), _U8]
         lib["rref_render_tone_mapped"].restype = C.c_double
         lib["rref_render_tone_mapped"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32,
                                                    C.POINTER(Light), C.c_int32, C.POINTER(ToneMap), _U8]
@@ -378,6 +383,17 @@ def render_aa(scene_obj, frame, aa_x, aa_y):
     return downsample_rgb8(out["fimg"], aa_x, aa_y)
 
 
+def ref_tone_map_image(fimg, camera, tone, aa=(1, 1)):
+    """The reference's camera::tone_map + gamma_correct + clip_image_to_rgb
+    on a given supersampled float frame (rows = y)."""
+    cam = make_camera(camera)
+    img = np.ascontiguousarray(fimg, np.float32)
+    rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
+    ref_lib()["rref_tone_map_image"](C.byref(cam), int(aa[0]), int(aa[1]), _p(img, C.c_float),
+                                     C.byref(make_tone_map(tone, camera)), _p(rgb, C.c_uint8))
+    return rgb
+
+
 def ref_parse_mesh(path, kind):
     """The reference's own OFF (kind 1) / PLY (kind 2) parser on a file:
     (triangles as an (n, 9) float32 array of a, b, c vertices in
@@ -392,11 +408,12 @@ def ref_parse_mesh(path, kind):
     return out[:n], nmat.value
 
 
-def tone_map_frame(fimg, tone):
+def tone_map_frame(fimg, tone, camera=None):
     """camera::tone_map + gamma_correct restated (ro_tone_map_frame) on a
-    copy of a float frame (rows = y, 0..255 colours)."""
+    copy of a float frame (rows = y, 0..255 colours); camera: the frame's
+    camera dict (needed by the histogram modes)."""
     img = np.array(fimg, np.float32, order="C", copy=True)
-    tm = make_tone_map(tone)
+    tm = make_tone_map(tone, camera)
     if oracle_lib()["ro_tone_map_frame"](_p(img, C.c_float), img.shape[1], img.shape[0], C.byref(tm)) != 0:
         raise ValueError("unsupported tone-mapping mode")
     return img
@@ -406,7 +423,7 @@ def render_tone_mapped(scene_obj, frame, tone, aa=(1, 1)):
     """Tone-mapped (anti-aliased) frame by the restatement: the supersampled
     float image, tone_map_frame, then downsample_rgb8."""
     out = scene_obj.render(supersampled(frame, *aa), want_float=True)
-    return downsample_rgb8(tone_map_frame(out["fimg"], tone), *aa)
+    return downsample_rgb8(tone_map_frame(out["fimg"], tone, frame["camera"]), *aa)
 
 
 def camera_rays(cam_dict, x0=0, y0=0, w=None, h=None, lib=None):

@@ -244,6 +244,27 @@ double rref_render_tone_mapped(void *h, const ro_camera *c, int32_t aa_x, int32_
     return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// The reference's tone mapping alone: a camera of c's geometry (aa_x * aa_y
+// samples per output pixel) whose image is set to fimg (3 floats per
+// sample of the supersampled grid, row y = 0 first) through
+// camera::set_pixel, then tone_map + gamma_correct as above and
+// clip_image_to_rgb.
+void rref_tone_map_image(const ro_camera *c, int32_t aa_x, int32_t aa_y, const float *fimg, const ro_tone_map *tm,
+                         uint8_t *rgb)
+{
+    std::unique_ptr<camera> cam(make_camera(c, (unsigned)aa_x, (unsigned)aa_y));
+    const int32_t fw = c->xres * aa_x, fh = c->yres * aa_y;
+    for (int32_t y = 0; y < fh; ++y)
+        for (int32_t x = 0; x < fw; ++x) {
+            const float *p = fimg + 3 * ((size_t)y * fw + x);
+            cam->set_pixel(ext_colour_t(p[0], p[1], p[2]), x, y);
+        }
+    cam->tone_map(static_cast<tone_mapping_mode_t>(tm->mode), tm->key, tm->xw, tm->yw, false, false,
+                  tm->desaturate != 0, tm->stretch != 0);
+    if (tm->gamma > 0.0f) cam->gamma_correct(tm->gamma);
+    cam->clip_image_to_rgb(rgb);
+}
+
 double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
                       uint8_t *rgb)
 {

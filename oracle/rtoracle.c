@@ -901,10 +901,148 @@ static const float TM_YB[3] = {0.2126f, 0.7151f, 0.0721f};
 static const float TM_ZB[3] = {0.0193f, 0.1192f, 0.9505f};
 static const float TM_VB[3] = {0.01477f, 0.497f, 0.631f};
 
+/* camera::just_noticable_difference (camera.cc:1814-1840). */
+static float tm_jnd(float La)
+{
+    const float lLa = log10f(La);
+    float lLt;
+    if (lLa < -3.94f) lLt = -2.86f;
+    else if (lLa < -1.44f) lLt = powf((0.405f * lLa) + 1.6f, 2.18f) - 2.86f;
+    else if (lLa < -0.0184f) lLt = lLa - 0.395f;
+    else if (lLa < 1.9f) lLt = powf((0.249f * lLa) + 0.65f, 2.7f) - 0.72f;
+    else lLt = lLa - 1.255f;
+    return powf(10.0f, lLt);
+}
+
+#define RO_PI 3.1415926535897932384626433f
+
+/* camera::histogram_tone_map (camera.cc:1843-2062) on the luminance (the g
+ * channel, 3 floats per pixel) of a w*h frame: resample to one pixel per
+ * degree of view, a 100-bin histogram of log luminance, trimmed against
+ * a linear (or, human, the visibility-limited) ceiling until fewer than
+ * 2.5 % of the pixels are trimmed, then every pixel mapped through the
+ * cumulative histogram.  lw_avg: the log-average luminance (the contrast
+ * fallback).  Returns silently for a black image, as the reference does. */
+static void tm_histogram(float *img, int32_t w, int32_t h, const ro_tone_map *tm, int human, float lw_avg)
+{
+    const float x_m = -tm->cam_w, y_m = -tm->cam_h;
+    const float x_angle = (-2.0f * x_m) / tm->cam_t;
+    const float y_angle = (-2.0f * y_m) / tm->cam_t;
+    const int sx = (int)(x_angle * (360.0f / (2.0f * RO_PI)));
+    const int sy = (int)(y_angle * (360.0f / (2.0f * RO_PI)));
+    float *sl = (float *)calloc((size_t)(sx > 0 ? sx : 1) * (size_t)(sy > 0 ? sy : 1), sizeof(float));
+    if (!sl) return;
+    const float inc_x = (float)w / (float)sx, inc_y = (float)h / (float)sy;
+    float y0 = 0.0f, y1 = inc_y;
+    for (int j = 0; j < sy; ++j) {
+        float x0 = 0.0f, x1 = inc_x;
+        for (int i = 0; i < sx; ++i) {
+            float acc = 0.0f;
+            for (int y = (int)y0; y <= (int)y1; ++y)
+                for (int x = (int)x0; x <= (int)x1; ++x) acc += img[3 * ((size_t)y * w + x) + 1];
+            sl[j * sx + i] = acc / (((x1 - x0) + 1.0f) * ((y1 - y0) + 1.0f));
+            x0 = x1;
+            x1 = smin((float)w - 1.0f, x1 + inc_x);
+        }
+        y0 = y1;
+        y1 = smin((float)h - 1.0f, y1 + inc_y);
+    }
+    const int bins = 100;
+    int pix_gt0 = 0;
+    float lw_min = RO_MAX_DIST, lw_max = 0.0f;
+    for (int i = 0; i < sx * sy; ++i)
+        if (sl[i] > 0.0f) {
+            lw_min = smin(lw_min, sl[i]);
+            lw_max = smax(lw_max, sl[i]);
+            ++pix_gt0;
+        }
+    if (lw_min <= 0.0f) { free(sl); return; }
+    lw_min = smax(lw_min, 1.0e-4f);
+    const float bw_min = logf(lw_min);
+    float bw_max = logf(lw_max);
+    if (bw_max == bw_min) bw_max += 0.0001f * fabsf(bw_max);
+    const float ld_max = 300.0f, ld_min = 1.0f;
+    const float bd_max = logf(ld_max), bd_min = logf(ld_min);
+    const size_t n = (size_t)w * (size_t)h;
+    if ((bd_max - bd_min) > (bw_max - bw_min)) {
+        const float sf = (bd_max - bd_min) / (bw_max - bw_min);
+        for (size_t i = 0; i < n; ++i) img[3 * i + 1] = (img[3 * i + 1] * sf) + bd_min;
+        free(sl);
+        return;
+    }
+    int his[101];
+    float cdf[101];
+    memset(his, 0, sizeof(his));
+    memset(cdf, 0, sizeof(cdf));
+    for (int i = 0; i < sx * sy; ++i)
+        if (sl[i] > 0.0f) {
+            int b = (int)(((logf(sl[i]) - bw_min) / (bw_max - bw_min)) * (float)bins) + 1;
+            b = b < 0 ? 0 : (b > bins ? bins : b);
+            his[b]++;
+        }
+    float sum = 0.0f;
+    for (int i = 1; i <= bins; ++i) {
+        sum += (float)his[i];
+        cdf[i] = sum / (float)pix_gt0;
+    }
+    const float tolerance = 0.025f * (float)pix_gt0;
+    const float bin_step = (bw_max - bw_min) / (float)bins;
+    const float lw_step = (1.0f / (float)bins) * (bw_max - bw_min);
+    int trimmings;
+    for (int guard = 0; guard < 100000; ++guard) {
+        trimmings = 0;
+        if ((float)pix_gt0 < tolerance) {
+            const float num = 1.219f + powf(ld_max * 0.5f, 0.4f);
+            const float den = 1.219f + powf(lw_avg, 0.4f);
+            const float sf = (1.0f / ld_max) * powf(num / den, 2.5f);
+            for (size_t i = 0; i < n; ++i) img[3 * i + 1] *= sf;
+            free(sl);
+            return;
+        }
+        for (int i = 1; i <= bins; ++i) {
+            float ceiling = ((float)pix_gt0 * bin_step) / (bd_max - bd_min);
+            if (human) {
+                const float bde = bd_min + ((bd_max - bd_min) * cdf[i]);
+                const float ld = expf(bde);
+                const float bw = ((float)i * lw_step) + bw_min;
+                const float lw = expf(bw);
+                ceiling *= (tm_jnd(ld) * lw) / (tm_jnd(lw) * ld);
+            }
+            if ((float)his[i] > ceiling) {
+                trimmings += his[i] - (int)ceiling;
+                his[i] = (int)ceiling;
+            }
+        }
+        pix_gt0 = 0;
+        for (int i = 1; i <= bins; ++i) pix_gt0 += his[i];
+        sum = 0.0f;
+        for (int i = 1; i <= bins; ++i) {
+            sum += (float)his[i];
+            cdf[i] = sum / (float)pix_gt0;
+        }
+        if (!((float)trimmings > tolerance)) break;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        const float g = img[3 * i + 1];
+        if (g > 0.0f) {
+            const float bw = logf(g);
+            float bf = ((bw - bw_min) / (bw_max - bw_min)) * (float)bins;
+            bf = smin(smax(bf, 0.0f), (float)bins);
+            const int b0 = (int)bf;
+            const int b1 = (b0 + 1) < bins ? (b0 + 1) : bins;
+            const float s = bf - (float)b0;
+            const float pbw = ((1.0f - s) * cdf[b0]) + (s * cdf[b1]);
+            const float bde = bd_min + ((bd_max - bd_min) * pbw);
+            img[3 * i + 1] = expf(bde) / ld_max;
+        }
+    }
+    free(sl);
+}
+
 int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *tm)
 {
     const int32_t mode = tm->mode;
-    if (!(mode == 0 || mode == 1 || mode == 4 || mode == 5 || mode == 6 || mode == 7 || mode == 9)) return -1;
+    if (!(mode >= 0 && mode <= 9 && mode != 8)) return -1;
     const int32_t n = w * h;
     /* first pass: to CIE Yxy, log-average and maximum luminance */
     float Yi = 0.0f, maxY = 0.0f, rgbAvg = 0.0f;
@@ -983,6 +1121,8 @@ int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *t
     } else if (mode == 7) {
         const float sf = key / maxY;
         for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
+    } else if (mode == 2 || mode == 3) {
+        tm_histogram(img, w, h, tm, mode == 3, Yi);
     } else if (mode == 9) {
         const float lda = 800.0f;
         const float log_lda = logf(lda * 0.5f);

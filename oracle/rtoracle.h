@@ -141,16 +141,21 @@ void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pi
 void ro_philox4x32(const uint32_t ctr[4], uint32_t key0, uint32_t key1, uint32_t out[4]);
 
 /* Tone-mapping parameters of camera::tone_map (raytracer/camera.h:378):
- * mode is a tone_mapping_mode_t value (camera.h:43-45) of a global mode
- * (0 none, 1 contrast, 4 non-linear, 5 exposure, 6 average luminance,
- * 7 maximum luminance, 9 Ferwerda); key, xw, yw as the reference's
- * arguments; desaturate / stretch its ds / sc flags (glare and temporal
- * adaptation off); gamma > 0 applies camera::gamma_correct(gamma) after. */
+ * mode is a tone_mapping_mode_t value (camera.h:43-45): 0 none,
+ * 1 contrast, 2 local histogram, 3 local histogram with human contrast
+ * limits, 4 non-linear, 5 exposure, 6 average luminance, 7 maximum
+ * luminance, 9 Ferwerda; key, xw, yw as the reference's arguments;
+ * desaturate / stretch its ds / sc flags (glare and temporal adaptation
+ * off); gamma > 0 applies camera::gamma_correct(gamma) after.  cam_w,
+ * cam_h, cam_t: the camera's half-width, half-height and image-plane
+ * distance (the histogram modes resample the frame to one pixel per
+ * degree of view). */
 typedef struct ro_tone_map {
     int32_t mode;
     float key, xw, yw;
     int32_t desaturate, stretch;
     float gamma;
+    float cam_w, cam_h, cam_t;
 } ro_tone_map;
 
 /* camera::tone_map (camera.cc:1124-1463) + convert_Yxy_to_rgb

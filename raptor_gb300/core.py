@@ -141,6 +141,7 @@ SIGNATURES = [
                               C.POINTER(RtRenderStats)]),
     ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
     ("rt_sum_sequential_f32", C.c_int32, [_P, _P, C.c_int64, C.POINTER(C.c_float)]),
+    ("rt_tone_map_image", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, _P, C.POINTER(RtToneMap), _P]),
     ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_free", None, [C.POINTER(RtMesh)]),
@@ -317,6 +318,18 @@ class Context:
 
     def set_option(self, option: int, value: int):
         _check(lib().rt_ctx_set_option(self.h, option, value))
+
+    def tone_map_image(self, fimg, camera, tone, aa=(1, 1), rgb=None):
+        """rt_tone_map_image: tone map + gamma + downsample of a given float
+        frame (rows = y, the aa-supersampled grid of `camera`)."""
+        cam = make_camera(camera)
+        if rgb is None:
+            rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
+        img = np.ascontiguousarray(fimg, np.float32) if isinstance(fimg, np.ndarray) else fimg
+        tm = make_tone_map(tone) if tone is not None else None
+        _check(lib().rt_tone_map_image(self.h, C.byref(cam), int(aa[0]), int(aa[1]), ptr(img),
+                                       C.byref(tm) if tm is not None else None, ptr(rgb)))
+        return rgb
 
     def sum_sequential(self, values) -> np.float32:
         """The binary32 sum of values in index order, rounded as a

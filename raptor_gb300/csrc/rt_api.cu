@@ -797,6 +797,89 @@ static rt_status check_table(const rt_scene *s, const rt_light *lights, int32_t 
     return RT_OK;
 }
 
+// Layout of ctx->tone: the ToneAcc, a 4-byte word for reductions, then the
+// scratch of the tone-mapping kernels.
+static constexpr size_t kToneWord = (sizeof(ToneAcc) + 255) / 256 * 256;
+static constexpr size_t kToneScratch = kToneWord + 256;
+
+// The tone map of a frame: its parameters checked, and for the histogram
+// modes the per-degree resampling of camera::histogram_tone_map
+// (camera.cc:1846-1855) computed in the reference's binary32 operations.
+static rt_status tone_view(const rt_tone_map *tone, const rt_camera &cam, int32_t fw, int32_t fh, const std::string &w,
+                           ToneView &tv)
+{
+    tv = ToneView{};
+    if (!tone) return RT_OK;
+    const int m = tone->mode;
+    if (!(m == RT_TONE_NONE || m == RT_TONE_GLOBAL_CONTRAST || m == RT_TONE_LOCAL_HISTOGRAM ||
+          m == RT_TONE_LOCAL_HUMAN_HISTOGRAM || m == RT_TONE_GLOBAL_NON_LINEAR || m == RT_TONE_GLOBAL_EXPOSURE ||
+          m == RT_TONE_GLOBAL_AVG_LUMINANCE || m == RT_TONE_GLOBAL_MAX_LUMINANCE || m == RT_TONE_GLOBAL_FERWERDA))
+        return fail(RT_ERR_INVALID_ARG, w + ": unsupported tone-mapping mode");
+    const float lim = 3.0e38f;
+    if (!(std::fabs(tone->key) < lim && std::fabs(tone->xw) < lim && std::fabs(tone->yw) < lim && tone->gamma >= 0.0f &&
+          tone->gamma < lim))
+        return fail(RT_ERR_INVALID_ARG, w + ": key, white point and gamma must be finite, gamma >= 0");
+    tv.enabled = 1;
+    tv.mode = m;
+    tv.key = tone->key;
+    tv.xw = tone->xw;
+    tv.yw = tone->yw;
+    tv.desaturate = tone->desaturate ? 1 : 0;
+    tv.stretch = tone->stretch ? 1 : 0;
+    tv.gamma = tone->gamma;
+    if (m == RT_TONE_LOCAL_HISTOGRAM || m == RT_TONE_LOCAL_HUMAN_HISTOGRAM) {
+        const float pi = 3.1415926535897932384626433f;
+        const float x_m = -cam.w, y_m = -cam.h;   // camera.h:60: x_m = -w, y_m = -h
+        const float x_angle = (-2.0f * x_m) / cam.t, y_angle = (-2.0f * y_m) / cam.t;
+        const float per_rad = 360.0f / (2.0f * pi);
+        const float sx = x_angle * per_rad, sy = y_angle * per_rad;
+        if (!(sx >= 2.0f && sy >= 2.0f && sx < 65536.0f && sy < 65536.0f))
+            return fail(RT_ERR_INVALID_ARG, w + ": histogram tone mapping needs a view of 2 to 65535 degrees");
+        tv.hist_sx = (int32_t)sx;
+        tv.hist_sy = (int32_t)sy;
+        tv.hist_inc_x = (float)fw / (float)tv.hist_sx;
+        tv.hist_inc_y = (float)fh / (float)tv.hist_sy;
+    }
+    return RT_OK;
+}
+
+static int64_t tone_blocks(const ToneView &tv) { return (int64_t)tv.hist_sx * tv.hist_sy; }
+
+rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const float *fimg,
+                            const rt_tone_map *tone, uint8_t *rgb_out)
+{
+    if (!ctx || !fimg || !rgb_out) return fail(RT_ERR_INVALID_ARG, "rt_tone_map_image: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    if (aa_x < 1 || aa_x > 16 || aa_y < 1 || aa_y > 16)
+        return fail(RT_ERR_INVALID_ARG, "rt_tone_map_image: anti-aliasing factors must be 1..16");
+    rt_camera fine = *camera;
+    fine.xres = camera->xres * aa_x;
+    fine.yres = camera->yres * aa_y;
+    st = check_camera(&fine);
+    if (st != RT_OK) return st;
+    ToneView tv;
+    st = tone_view(tone, *camera, fine.xres, fine.yres, "rt_tone_map_image", tv);
+    if (st != RT_OK) return st;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    const size_t nfine = (size_t)fine.xres * (size_t)fine.yres;
+    const void *dimg = nullptr;
+    st = stage_in(ctx, ctx->stage_b, fimg, nfine * 3 * sizeof(float), &dimg);
+    if (st != RT_OK) return st;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
+    if (st != RT_OK) return st;
+    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv))), "scratch allocation");
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_tone_map((const float *)dimg, fine.xres, fine.yres, aa_x, aa_y, tv, o.rgb, (ToneAcc *)ctx->tone.ptr,
+                    (char *)ctx->tone.ptr + kToneScratch, ctx->sm_count, ctx->stream);
+    RT_CUDA(cudaGetLastError(), "tone-map launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, nullptr);
+}
+
 rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n, float *sum_out)
 {
     if (!ctx || !sum_out || (n > 0 && !values)) return fail(RT_ERR_INVALID_ARG, "rt_sum_sequential_f32: NULL argument");
@@ -807,9 +890,9 @@ rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n,
     const void *dv = nullptr;
     rt_status st = stage_in(ctx, ctx->stage_a, values, (size_t)n * sizeof(float), &dv);
     if (st != RT_OK) return st;
-    RT_CUDA(ctx->tone.reserve(sizeof(ToneAcc) + 256 + tone_scratch_bytes(n)), "scratch allocation");
+    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes(n)), "scratch allocation");
     ToneAcc *acc = (ToneAcc *)ctx->tone.ptr;
-    uint32_t *mx = (uint32_t *)((char *)ctx->tone.ptr + 128);
+    uint32_t *mx = (uint32_t *)((char *)ctx->tone.ptr + kToneWord);
     launch_abs_max((const float *)dv, n, mx, ctx->sm_count, ctx->stream);
     RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, mx, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream), "readback");
     RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
@@ -818,7 +901,8 @@ rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n,
     if (bits == 0) return RT_OK;   // all zeros: +0
     float max_abs;
     std::memcpy(&max_abs, &bits, sizeof(float));
-    launch_sequential_sum((const float *)dv, n, max_abs, acc, (char *)ctx->tone.ptr + 256, ctx->sm_count, ctx->stream);
+    launch_sequential_sum((const float *)dv, n, max_abs, acc, (char *)ctx->tone.ptr + kToneScratch, ctx->sm_count,
+                          ctx->stream);
     RT_CUDA(cudaGetLastError(), "sum launch");
     RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, &acc->sum_f, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
             "readback");
@@ -843,27 +927,9 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
     if (st != RT_OK) return st;
     st = check_table(s, lights, nlights, materials, nmaterials, "rt_render_tone_mapped");
     if (st != RT_OK) return st;
-    ToneView tv = {};
-    if (tone) {
-        const int m = tone->mode;
-        if (!(m == RT_TONE_NONE || m == RT_TONE_GLOBAL_CONTRAST || m == RT_TONE_GLOBAL_NON_LINEAR ||
-              m == RT_TONE_GLOBAL_EXPOSURE || m == RT_TONE_GLOBAL_AVG_LUMINANCE || m == RT_TONE_GLOBAL_MAX_LUMINANCE ||
-              m == RT_TONE_GLOBAL_FERWERDA))
-            return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: unsupported tone-mapping mode");
-        const float lim = 3.0e38f;
-        if (!(std::fabs(tone->key) < lim && std::fabs(tone->xw) < lim && std::fabs(tone->yw) < lim &&
-              tone->gamma >= 0.0f && tone->gamma < lim))
-            return fail(RT_ERR_INVALID_ARG, "rt_render_tone_mapped: key, white point and gamma must be finite, "
-                                            "gamma >= 0");
-        tv.enabled = 1;
-        tv.mode = m;
-        tv.key = tone->key;
-        tv.xw = tone->xw;
-        tv.yw = tone->yw;
-        tv.desaturate = tone->desaturate ? 1 : 0;
-        tv.stretch = tone->stretch ? 1 : 0;
-        tv.gamma = tone->gamma;
-    }
+    ToneView tv;
+    st = tone_view(tone, *camera, fine.xres, fine.yres, "rt_render_tone_mapped", tv);
+    if (st != RT_OK) return st;
     rt_context *ctx = s->ctx;
     DeviceGuard g(ctx->device);
     const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
@@ -872,7 +938,7 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
     st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
     if (st != RT_OK) return st;
     RT_CUDA(ctx->fimg.reserve(nfine * 3 * sizeof(float)), "float frame allocation");
-    RT_CUDA(ctx->tone.reserve(sizeof(ToneAcc) + 256 + tone_scratch_bytes((int64_t)nfine)),
+    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv))),
             "tone accumulator allocation");
     LightSet ls;
     ls.n = nlights;
@@ -887,7 +953,7 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
                        ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     launch_tone_map((const float *)ctx->fimg.ptr, fine.xres, fine.yres, aa_x, aa_y, tv, o.rgb, (ToneAcc *)ctx->tone.ptr,
-                    (char *)ctx->tone.ptr + 256, ctx->sm_count, ctx->stream);
+                    (char *)ctx->tone.ptr + kToneScratch, ctx->sm_count, ctx->stream);
     RT_CUDA(cudaGetLastError(), "tone-map launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, stats);

@@ -38,6 +38,16 @@ struct ToneView {
     float key, xw, yw;
     int32_t desaturate, stretch;
     float gamma;
+    // histogram modes: the frame resampled to hist_sx x hist_sy blocks of
+    // hist_inc_x x hist_inc_y samples (one per degree of view)
+    int32_t hist_sx, hist_sy;
+    float hist_inc_x, hist_inc_y;
+};
+// The luminance map of the histogram modes (camera::histogram_tone_map).
+struct ToneHist {
+    int32_t kind;   // 0 black image (no change), 1 linear, 2 contrast, 3 histogram
+    float sf, bd_min, bd_max, bw_min, bw_max;
+    float cdf[101];
 };
 struct ToneScalars {
     float sf;    // luminance scale
@@ -50,7 +60,9 @@ struct ToneAcc {
     uint32_t max_bits;         // largest such luminance (float bits)
     uint32_t gmin, gmax;       // mapped-luminance range (order keys), stretch only
     int32_t redo;              // output pixels queued for the exact pass
+    float Yi;                  // log-average luminance
     ToneScalars s;
+    ToneHist h;
 };
 
 struct LightSet {
@@ -81,8 +93,9 @@ void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t 
 void launch_abs_max(const float *v, int64_t n, uint32_t *out, int sm_count, cudaStream_t st);
 void launch_sequential_sum(const float *v, int64_t n, float max_abs, ToneAcc *acc, void *scratch, int sm_count,
                            cudaStream_t st);
-// scratch: tone_scratch_bytes(fw * fh) of device memory.
-size_t tone_scratch_bytes(int64_t n);
+// scratch: tone_scratch_bytes(fw * fh, blocks) of device memory (blocks:
+// hist_sx * hist_sy of a histogram mode, else 0).
+size_t tone_scratch_bytes(int64_t n, int64_t blocks = 0);
 void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
                      uint8_t *rgb, ToneAcc *acc, void *scratch, int sm_count, cudaStream_t st);
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,

@@ -13,6 +13,8 @@
 //   k_tone_coarse   the chunk increments summed over groups of chunks
 //   k_tone_sum      one warp: the reference's binary32 sum of the terms,
 //                   reproduced exactly, then the mode's scale factors
+//   k_hist_blocks   (histogram modes) the luminance averaged per degree of view
+//   k_hist_main     (histogram modes) histogram, trimming, cumulative map
 //   k_tone_range    (contrast stretch only) minimum and maximum of the
 //                   mapped luminance
 //   k_tone_final    per output pixel: every sample through the whole
@@ -91,10 +93,43 @@ __device__ __forceinline__ Yxy to_yxy(float3 c, const ToneView &t)
 }
 
 // The mode's luminance scaling (camera.cc:1276-1425) of one sample.
+template <bool EXACT> __device__ __forceinline__ float tl_log(float v) { return EXACT ? log_f(v) : logf(v); }
+
+// camera::histogram_tone_map's final loop (camera.cc:2040-2056) for one
+// luminance, and its linear and contrast fallbacks.
 template <bool EXACT>
-__device__ __forceinline__ float map_lum(float g, const ToneView &t, const ToneScalars &k)
+__device__ __forceinline__ float map_hist(float g, const ToneHist &h)
+{
+    switch (h.kind) {
+    case 1:
+        return xadd(xmul(g, h.sf), h.bd_min);
+    case 2:
+        return xmul(g, h.sf);
+    case 3: {
+        if (!(g > 0.0f)) return g;
+        const float bw = tl_log<EXACT>(g);
+        float bf = xmul(xdiv(xsub(bw, h.bw_min), xsub(h.bw_max, h.bw_min)), 100.0f);
+        bf = (bf < 0.0f) ? 0.0f : bf;            // std::max(bf, 0), then std::min(., bins)
+        bf = (100.0f < bf) ? 100.0f : bf;
+        const int b0 = (int)bf;
+        const int b1 = (b0 + 1 < 100) ? b0 + 1 : 100;
+        const float s = xsub(bf, (float)b0);
+        const float pbw = xadd(xmul(xsub(1.0f, s), h.cdf[b0]), xmul(s, h.cdf[b1]));
+        const float bde = xadd(h.bd_min, xmul(xsub(h.bd_max, h.bd_min), pbw));
+        return xdiv(tl_exp<EXACT>(bde), 300.0f);
+    }
+    default:
+        return g;
+    }
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float map_lum(float g, const ToneView &t, const ToneScalars &k, const ToneHist &hh)
 {
     switch (t.mode) {
+    case RT_TONE_LOCAL_HISTOGRAM:
+    case RT_TONE_LOCAL_HUMAN_HISTOGRAM:
+        return map_hist<EXACT>(g, hh);
     case RT_TONE_GLOBAL_NON_LINEAR:
         g = xmul(g, k.sf);
         if (k.aux != 0.0f) g = xmul(g, xdiv(xadd(1.0f, xmul(g, k.aux)), xadd(1.0f, g)));
@@ -140,6 +175,189 @@ __device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma)
         c = make_float3(xmul(v[0], 255.0f), xmul(v[1], 255.0f), xmul(v[2], 255.0f));
     }
     return c;
+}
+
+// ---- camera::histogram_tone_map (camera.cc:1843-2062)
+
+// The frame's luminance averaged over one block per degree of view
+// (camera.cc:1856-1880): block (i, j) sums the samples of rows
+// int(y0)..int(y1) and columns int(x0)..int(x1) in that order, where the
+// bounds follow the reference's running sums (x1 = min(w - 1, x1 + inc)).
+// One thread per block.
+__global__ void __launch_bounds__(kToneThreads) k_hist_blocks(const float *__restrict__ fimg, int32_t fw, int32_t fh,
+                                                              ToneView t, float *__restrict__ blocks)
+{
+    const int64_t nb = (int64_t)t.hist_sx * t.hist_sy;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(b % t.hist_sx), j = (int)(b / t.hist_sx);
+        float x0 = 0.0f, x1 = t.hist_inc_x, y0 = 0.0f, y1 = t.hist_inc_y;
+        const float xmax = xsub((float)fw, 1.0f), ymax = xsub((float)fh, 1.0f);
+        for (int q = 0; q < i; ++q) {
+            x0 = x1;
+            const float nx = xadd(x1, t.hist_inc_x);
+            x1 = (nx < xmax) ? nx : xmax;   // std::min(x_res - 1, x1 + inc)
+        }
+        for (int q = 0; q < j; ++q) {
+            y0 = y1;
+            const float ny = xadd(y1, t.hist_inc_y);
+            y1 = (ny < ymax) ? ny : ymax;
+        }
+        float acc = 0.0f;
+        for (int y = (int)y0; y <= (int)y1; ++y)
+            for (int x = (int)x0; x <= (int)x1; ++x) {
+                const int64_t s = (int64_t)y * fw + x;
+                acc = xadd(acc, to_yxy<true>(make_float3(fimg[3 * s], fimg[3 * s + 1], fimg[3 * s + 2]), t).Y);
+            }
+        blocks[b] = xdiv(acc, xmul(xadd(xsub(x1, x0), 1.0f), xadd(xsub(y1, y0), 1.0f)));
+    }
+}
+
+// camera::just_noticable_difference (camera.cc:1814-1840).
+__device__ __forceinline__ float jnd(float La)
+{
+    const float l = log10_f(La);
+    float t;
+    if (l < -3.94f) t = -2.86f;
+    else if (l < -1.44f) t = xsub(pow_f(xadd(xmul(0.405f, l), 1.6f), 2.18f), 2.86f);
+    else if (l < -0.0184f) t = xsub(l, 0.395f);
+    else if (l < 1.9f) t = xsub(pow_f(xadd(xmul(0.249f, l), 0.65f), 2.7f), 0.72f);
+    else t = xsub(l, 1.255f);
+    return pow_f(10.0f, t);
+}
+
+// The rest of histogram_tone_map up to the final per-pixel loop, in one
+// block of 128 threads: range of the positive blocks, the linear and
+// contrast fallbacks, a 100-bin histogram of log luminance, and the
+// trimming iterations (each bin's ceiling in its own thread; counts and the
+// cumulative histogram are integers below 2^24, so their binary32 running
+// sums are exact in any order).  Iterations are capped at 10,000; the
+// reference's loop ends far sooner (each pass trims a bin down to its
+// ceiling).
+__global__ void __launch_bounds__(128) k_hist_main(const float *__restrict__ blocks, ToneView t, ToneAcc *acc)
+{
+    __shared__ int his[101];
+    __shared__ float cdf[101];
+    __shared__ int s_cnt, s_trim;
+    __shared__ uint32_t s_min, s_max;
+    const int tid = threadIdx.x;
+    const int64_t nb = (int64_t)t.hist_sx * t.hist_sy;
+    if (tid == 0) {
+        s_cnt = 0;
+        s_min = 0x7f7fffffu;   // FLT_MAX
+        s_max = 0u;
+    }
+    if (tid <= 100) {
+        his[tid] = 0;
+        cdf[tid] = 0.0f;
+    }
+    __syncthreads();
+    int cnt = 0;
+    uint32_t mn = 0x7f7fffffu, mx = 0u;
+    for (int64_t b = tid; b < nb; b += blockDim.x) {
+        const float v = blocks[b];
+        if (v > 0.0f) {
+            mn = min(mn, __float_as_uint(v));   // positive: bit order is value order
+            mx = max(mx, __float_as_uint(v));
+            ++cnt;
+        }
+    }
+    atomicAdd(&s_cnt, cnt);
+    atomicMin(&s_min, mn);
+    atomicMax(&s_max, mx);
+    __syncthreads();
+    ToneHist &H = acc->h;
+    int pix_gt0 = s_cnt;
+    float lw_min = __uint_as_float(s_min), lw_max = __uint_as_float(s_max);
+    if (!(lw_min > 0.0f)) {   // never: lw_min starts at FLT_MAX and only takes positive values
+        if (tid == 0) H.kind = 0;
+        return;
+    }
+    lw_min = (lw_min < 1.0e-4f) ? 1.0e-4f : lw_min;   // std::max(lw_min, min_lum)
+    const float bw_min = log_f(lw_min);
+    float bw_max = log_f(lw_max);
+    if (bw_max == bw_min) bw_max = xadd(bw_max, xmul(0.0001f, fabsf(bw_max)));
+    const float ld_max = 300.0f;
+    const float bd_max = log_f(ld_max), bd_min = log_f(1.0f);
+    if (tid == 0) {
+        H.bd_min = bd_min;
+        H.bd_max = bd_max;
+        H.bw_min = bw_min;
+        H.bw_max = bw_max;
+    }
+    if (xsub(bd_max, bd_min) > xsub(bw_max, bw_min)) {
+        if (tid == 0) {
+            H.kind = 1;
+            H.sf = xdiv(xsub(bd_max, bd_min), xsub(bw_max, bw_min));
+        }
+        return;
+    }
+    for (int64_t b = tid; b < nb; b += blockDim.x) {
+        const float v = blocks[b];
+        if (v > 0.0f) {
+            int bin = (int)xmul(xdiv(xsub(log_f(v), bw_min), xsub(bw_max, bw_min)), 100.0f) + 1;
+            bin = bin < 0 ? 0 : (bin > 100 ? 100 : bin);
+            atomicAdd(&his[bin], 1);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float sum = 0.0f;
+        for (int i = 1; i <= 100; ++i) {
+            sum = xadd(sum, (float)his[i]);
+            cdf[i] = xdiv(sum, (float)pix_gt0);
+        }
+    }
+    __syncthreads();
+    const float tolerance = xmul(0.025f, (float)pix_gt0);
+    const float bin_step = xdiv(xsub(bw_max, bw_min), 100.0f);
+    const float lw_step = xmul(1.0f / 100.0f, xsub(bw_max, bw_min));
+    const bool human = t.mode == RT_TONE_LOCAL_HUMAN_HISTOGRAM;
+    for (int iter = 0; iter < 10000; ++iter) {
+        if ((float)pix_gt0 < tolerance) {
+            if (tid == 0) {
+                const float num = xadd(1.219f, pow_f(xmul(ld_max, 0.5f), 0.4f));
+                const float den = xadd(1.219f, pow_f(acc->Yi, 0.4f));
+                H.kind = 2;
+                H.sf = xmul(xdiv(1.0f, ld_max), pow_f(xdiv(num, den), 2.5f));
+            }
+            return;
+        }
+        if (tid == 0) s_trim = 0;
+        __syncthreads();
+        const int i = tid + 1;
+        if (i <= 100) {
+            float ceiling = xdiv(xmul((float)pix_gt0, bin_step), xsub(bd_max, bd_min));
+            if (human) {
+                const float bde = xadd(bd_min, xmul(xsub(bd_max, bd_min), cdf[i]));
+                const float ld = exp_f(bde);
+                const float bw = xadd(xmul((float)i, lw_step), bw_min);
+                const float lw = exp_f(bw);
+                ceiling = xmul(ceiling, xdiv(xmul(jnd(ld), lw), xmul(jnd(lw), ld)));
+            }
+            if ((float)his[i] > ceiling) {
+                atomicAdd(&s_trim, his[i] - (int)ceiling);
+                his[i] = (int)ceiling;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int p = 0;
+            for (int k = 1; k <= 100; ++k) p += his[k];
+            s_cnt = p;
+            float sum = 0.0f;
+            for (int k = 1; k <= 100; ++k) {
+                sum = xadd(sum, (float)his[k]);
+                cdf[k] = xdiv(sum, (float)p);
+            }
+        }
+        __syncthreads();
+        pix_gt0 = s_cnt;
+        const int trimmings = s_trim;
+        __syncthreads();
+        if (!((float)trimmings > tolerance)) break;
+    }
+    if (tid <= 100) H.cdf[tid] = cdf[tid];
+    if (tid == 0) H.kind = 3;
 }
 
 // Order-preserving key of a float for unsigned atomics (no NaNs here).
@@ -271,6 +489,7 @@ __device__ void tone_scalars(const ToneView &t, ToneAcc *acc)
     float Yi = 0.0f;
     if (acc->count) Yi = xdiv(acc->sum_f, (float)acc->count);
     Yi = pow_f(10.0f, Yi);
+    acc->Yi = Yi;
     float maxY = __uint_as_float(acc->max_bits);
     ToneScalars k;
     k.sf = 1.0f;
@@ -543,7 +762,7 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_range(const float *__rest
     uint32_t lo = 0xffffffffu, hi = 0u;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const Yxy p = to_yxy<true>(make_float3(fimg[3 * i], fimg[3 * i + 1], fimg[3 * i + 2]), t);
-        const uint32_t key = order_key(map_lum<true>(p.Y, t, k));
+        const uint32_t key = order_key(map_lum<true>(p.Y, t, k, acc->h));
         lo = min(lo, key);
         hi = max(hi, key);
     }
@@ -562,7 +781,8 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_range(const float *__rest
 template <bool EXACT>
 __device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int32_t fw, int32_t aa_x, int32_t aa_y,
                                              int32_t ox, int32_t oy, const ToneView &t, const ToneScalars &k,
-                                             bool stretch, float offset, float scale, float samples)
+                                             const ToneHist &hh, bool stretch, float offset, float scale,
+                                             float samples)
 {
     float3 a = make_float3(0.0f, 0.0f, 0.0f);
     for (int32_t ax = 0; ax < aa_x; ++ax)
@@ -571,7 +791,7 @@ __device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int
             float3 c = make_float3(fimg[3 * s], fimg[3 * s + 1], fimg[3 * s + 2]);
             if (t.enabled) {
                 const Yxy p = to_yxy<EXACT>(c, t);
-                float g = map_lum<EXACT>(p.Y, t, k);
+                float g = map_lum<EXACT>(p.Y, t, k, hh);
                 if (stretch) g = xmul(xadd(g, offset), scale);
                 c = to_rgb<EXACT>(p.x, g, p.y, t.gamma);
             }
@@ -637,7 +857,8 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_final(const float *__rest
         bool queue = false;
         if (o < npix) {
             const int32_t oy = (int32_t)(o / ow), ox = (int32_t)(o - (int64_t)oy * ow);
-            const float3 v = tone_pixel<false>(fimg, fw, aa_x, aa_y, ox, oy, t, k, sr.on, sr.offset, sr.scale, samples);
+            const float3 v =
+                tone_pixel<false>(fimg, fw, aa_x, aa_y, ox, oy, t, k, acc->h, sr.on, sr.offset, sr.scale, samples);
             queue = t.enabled && (near_integer(v.x) || near_integer(v.y) || near_integer(v.z));
             if (!queue) store_pixel(rgb, o, v);
         }
@@ -664,7 +885,8 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_fix(const float *__restri
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int64_t o = redo[i];
         const int32_t oy = (int32_t)(o / ow), ox = (int32_t)(o - (int64_t)oy * ow);
-        store_pixel(rgb, o, tone_pixel<true>(fimg, fw, aa_x, aa_y, ox, oy, t, k, sr.on, sr.offset, sr.scale, samples));
+        store_pixel(rgb, o,
+                    tone_pixel<true>(fimg, fw, aa_x, aa_y, ox, oy, t, k, acc->h, sr.on, sr.offset, sr.scale, samples));
     }
 }
 
@@ -677,12 +899,13 @@ int blocks_for(int64_t n, int sm_count)
 
 }  // namespace
 
-size_t tone_scratch_bytes(int64_t n)
+size_t tone_scratch_bytes(int64_t n, int64_t blocks)
 {
     const int64_t nchunks = (n + kSumChunk - 1) / kSumChunk;
     const int64_t ncoarse = (nchunks + kCoarse - 1) / kCoarse;
     return (size_t)nchunks * kSumChunk * sizeof(float) + (size_t)(nchunks + ncoarse) * 32 * sizeof(ChunkSum) +
-           (size_t)n * sizeof(int32_t);   // redo queue (at most one entry per output pixel)
+           (size_t)n * sizeof(int32_t) +   // redo queue (at most one entry per output pixel)
+           (size_t)blocks * sizeof(float);  // histogram modes: the per-degree luminance blocks
 }
 
 void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
@@ -697,6 +920,7 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
     ChunkSum *rec = (ChunkSum *)(terms + nchunks * kSumChunk);
     ChunkSum *crec = rec + nchunks * 32;
     int32_t *redo = (int32_t *)(crec + ncoarse * 32);
+    float *hblocks = (float *)(redo + n);
     cudaMemsetAsync(acc, 0, sizeof(ToneAcc), st);
     if (t.enabled) {
         // candidate binades: |S| <= 39 n (|log10 Y| < 39 for any float Y)
@@ -705,6 +929,11 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
         k_tone_terms<<<(unsigned)nchunks, kSumThreads, 0, st>>>(fimg, nullptr, n, e_lo, terms, rec, acc);
         k_tone_coarse<<<(unsigned)((ncoarse * 32 + 255) / 256), 256, 0, st>>>(rec, nchunks, ncoarse, crec);
         k_tone_sum<<<1, 32, 0, st>>>(terms, rec, crec, nchunks, ncoarse, e_lo, t, acc, true);
+        if (t.mode == RT_TONE_LOCAL_HISTOGRAM || t.mode == RT_TONE_LOCAL_HUMAN_HISTOGRAM) {
+            const int64_t nb = (int64_t)t.hist_sx * t.hist_sy;
+            k_hist_blocks<<<blocks_for(nb, sm_count), kToneThreads, 0, st>>>(fimg, fw, fh, t, hblocks);
+            k_hist_main<<<1, 128, 0, st>>>(hblocks, t, acc);
+        }
         if (t.stretch) k_tone_range<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(fimg, n, t, acc);
     }
     k_tone_final<<<blocks_for((int64_t)ow * oh, sm_count), kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, oh, t, acc,

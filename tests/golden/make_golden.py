@@ -140,6 +140,24 @@ def soup(seed=7, n=300):
             o.astype(np.float32), d.astype(np.float32), tmax.astype(np.float32))
 
 
+# tone maps applied by the reference to fixed float frames (the histogram
+# modes need a wide luminance range: a dark ambient term, a strong specular
+# highlight and a dim coloured light on the icosphere)
+FRAME_TONE = (({"mode": 2}, (1, 1)), ({"mode": 3}, (1, 1)),
+              ({"mode": 3, "desaturate": True, "stretch": True, "gamma": 2.2}, (2, 2)),
+              ({"mode": 2, "stretch": True, "gamma": 1.8}, (3, 2)), ({"mode": 3, "gamma": 2.2}, (2, 1)),
+              ({"mode": 5, "gamma": 2.2}, (1, 1)), ({"mode": 9, "desaturate": True}, (2, 2)))
+
+
+def hdr_frame():
+    from raptor_gb300 import scenes
+    s, f = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    f = dict(f, material=dict(f["material"], ka=(0.4, 0.4, 0.4), ks=(255.0, 255.0, 255.0), ns=30.0),
+             lights=[scenes.point_light((3.0, 5.0, 3.0)),
+                     scenes.point_light((-2.0, 0.5, 1.5), rgb=(40.0, 30.0, 255.0), d=0.3)])
+    return s, f
+
+
 def _polygons(rng):
     """Faces for the parser cases: convex and concave polygons, collinear
     vertices, a star, as (vertex list, face list) in the plane z = const."""
@@ -268,6 +286,16 @@ def main():
         # tone mapping and gamma (camera::tone_map, camera::gamma_correct)
         for k, (tone, aa) in enumerate(TONE):
             arrays[f"{key}_tone{k}_rgb"] = rs.render(f, aa=aa, tone=tone)["rgb"]
+    # the reference's tone maps on fixed float frames (the restatement's
+    # render of the HDR icosphere on each anti-aliasing grid)
+    hs, hf = hdr_frame()
+    osc = O.OracleScene(hs)
+    for k, (tone, aa) in enumerate(FRAME_TONE):
+        fimg = osc.render(O.supersampled(hf, *aa), want_float=True)["fimg"]
+        arrays[f"ftone{k}_fimg"] = fimg.astype(np.float32)
+        arrays[f"ftone{k}_rgb"] = O.ref_tone_map_image(fimg, hf["camera"], tone, aa)
+    arrays["ftone_cases"] = np.frombuffer(json.dumps([[t, list(aa)] for t, aa in FRAME_TONE]).encode(), np.uint8)
+    arrays["ftone_camera"] = np.frombuffer(json.dumps(hf["camera"]).encode(), np.uint8)
     # per-triangle materials with refraction: the glass sphere
     from raptor_gb300 import scenes
     for k, kw in enumerate(GLASS):

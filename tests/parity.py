@@ -101,3 +101,12 @@ def tone_cases():
     import os
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_small.npz"))
     return [(k, t, tuple(aa)) for k, (t, aa) in enumerate(json.loads(g["tone_cases"].tobytes().decode()))]
+
+
+def frame_tone_cases():
+    """(k, tone-map dict, (aa_x, aa_y)) of the tone maps the reference
+    applied to fixed float frames (keys ftone{k}_fimg, ftone{k}_rgb)."""
+    import json
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_small.npz"))
+    return [(k, t, tuple(aa)) for k, (t, aa) in enumerate(json.loads(g["ftone_cases"].tobytes().decode()))]

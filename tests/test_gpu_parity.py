@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import PIX_FRAC, compare_hits, edge_distance, glass_cases, pixel_agreement, tone_cases
+from parity import PIX_FRAC, compare_hits, edge_distance, frame_tone_cases, glass_cases, pixel_agreement, tone_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -828,7 +828,7 @@ def test_tone_map_off_equals_plain_frames(rtlib, ctx):
     for ax, ay in ((2, 2), (3, 2)):
         assert np.array_equal(sc.render_tone_mapped(frame, None, (ax, ay))["rgb"], sc.render_aa(frame, ax, ay)["rgb"])
     with pytest.raises(rtlib.RtError):
-        sc.render_tone_mapped(frame, {"mode": 2})       # local histogram: not a global mode
+        sc.render_tone_mapped(frame, {"mode": 8})       # the bilateral-filter mapper is not offered
     with pytest.raises(rtlib.RtError):
         sc.render_tone_mapped(frame, {"mode": 0, "gamma": -1.0})
     sc.close()
@@ -848,4 +848,55 @@ def test_tone_mapping_terrain_medium_vs_oracle(rtlib, ctx, oracle):
         want = oracle.downsample_rgb8(oracle.tone_map_frame(fimg, tone), 2, 2)
         within1, exact, _ = pixel_agreement(got, want)
         assert within1 >= 0.998 and exact >= 0.95, (tone, within1, exact)
+    sc.close()
+
+
+@pytest.mark.parametrize("case", frame_tone_cases(), ids=lambda c: f"ftone{c[0]}")
+def test_tone_map_image_vs_reference(rtlib, ctx, golden, case):
+    """rt_tone_map_image on the float frames the reference tone mapped
+    (histogram modes with and without the visibility ceiling, desaturation,
+    stretch, gamma, anti-aliasing; two global modes): the same RGB8 frame,
+    from device and from host buffers."""
+    torch = pytest.importorskip("torch")
+    k, tone, aa = case
+    cam = json.loads(golden["ftone_camera"].tobytes().decode())
+    fimg = golden[f"ftone{k}_fimg"]
+    ref = golden[f"ftone{k}_rgb"]
+    got = ctx.tone_map_image(fimg, cam, tone, aa)
+    within1, exact, _ = pixel_agreement(got, ref)
+    assert within1 == 1.0 and exact >= 0.999, (within1, exact)
+    d_img = torch.from_numpy(np.ascontiguousarray(fimg)).cuda()
+    d_rgb = torch.empty(ref.shape, dtype=torch.uint8, device="cuda")
+    ctx.tone_map_image(d_img, cam, tone, aa, rgb=d_rgb)
+    assert np.array_equal(d_rgb.cpu().numpy(), got)
+
+
+def test_histogram_tone_mapping_render(rtlib, ctx, oracle):
+    """rt_render_tone_mapped with the histogram modes on the HDR icosphere
+    (the mode the reference's interactive viewer uses) equals
+    rt_tone_map_image of the same scene's float frame (rt_render_float), and
+    the restatement's tone map of that float frame; a view narrower than
+    2 degrees is refused."""
+    torch = pytest.importorskip("torch")
+    from raptor_gb300 import scenes
+    s, f = scenes.icosphere_scene(freq=8, seed=0, res=96)
+    f = dict(f, material=dict(f["material"], ka=(0.4, 0.4, 0.4), ks=(255.0, 255.0, 255.0), ns=30.0),
+             lights=[scenes.point_light((3.0, 5.0, 3.0)), scenes.point_light((-2.0, 0.5, 1.5), rgb=(40.0, 30.0, 255.0), d=0.3)])
+    sc = rtlib.Scene(ctx, s)
+    for tone, aa in (({"mode": 3}, (2, 2)), ({"mode": 2, "gamma": 2.2}, (1, 1)),
+                     ({"mode": 3, "desaturate": True, "stretch": True}, (3, 2))):
+        got = sc.render_tone_mapped(f, tone, aa)["rgb"]
+        fine = oracle.supersampled(f, *aa)
+        H, W = fine["camera"]["yres"], fine["camera"]["xres"]
+        d_fimg = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+        sc.render_float(fine, d_fimg)
+        torch.cuda.synchronize()
+        assert np.array_equal(ctx.tone_map_image(d_fimg, f["camera"], tone, aa), got)
+        want = oracle.downsample_rgb8(oracle.tone_map_frame(d_fimg.cpu().numpy(), tone, f["camera"]), *aa)
+        within1, exact, _ = pixel_agreement(got, want)
+        assert within1 == 1.0 and exact >= 0.999, (tone, within1, exact)
+        assert got.std() > 20.0
+    narrow = dict(f, camera=dict(f["camera"], w=0.01, h=0.01))
+    with pytest.raises(rtlib.RtError):
+        sc.render_tone_mapped(narrow, {"mode": 3})
     sc.close()

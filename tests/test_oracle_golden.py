@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from parity import PIX_FRAC, compare_hits, glass_cases, pixel_agreement, tone_cases
+from parity import PIX_FRAC, compare_hits, frame_tone_cases, glass_cases, pixel_agreement, tone_cases
 
 FLT_MAX = np.float32(3.4028234663852886e38)
 
@@ -227,3 +227,18 @@ def test_tone_mapping_modes_differ(oracle, golden):
     plain = golden["terrain_rgb"]
     assert all((f != plain).any() for f in frames)
     assert len({f.tobytes() for f in frames}) == len(frames)
+
+
+@pytest.mark.parametrize("case", frame_tone_cases(), ids=lambda c: f"ftone{c[0]}")
+def test_oracle_tone_map_of_fixed_frame_matches_reference(oracle, golden, case):
+    """The histogram tone mappers (camera::histogram_tone_map: per-degree
+    resampling, 100-bin histogram, trimming with and without the human
+    visibility ceiling, cumulative map) and global ones, applied by the
+    restatement and by the reference to the same float frame: every pixel
+    equal."""
+    k, tone, aa = case
+    cam = json.loads(golden["ftone_camera"].tobytes().decode())
+    out = oracle.downsample_rgb8(oracle.tone_map_frame(golden[f"ftone{k}_fimg"], tone, cam), *aa)
+    ref = golden[f"ftone{k}_rgb"]
+    assert np.array_equal(out, ref)
+    assert ref.std() > 20.0      # a frame with contrast, not a saturated one
