@@ -296,8 +296,16 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
 // the pixel's ray tree walked by shade_pixel_tree (its pending rays in a
 // per-thread frame stack).  fimg non-null: the unclipped colour (3 floats
 // per pixel) is written instead of RGB8.
+// Resident blocks per SM the ray-tree kernel is compiled for (its frame
+// stack lives in local memory either way).  Measured on the glass-sphere
+// frame (512^2, 41k triangles): 1 / 4 / 5 / 6 / 8 blocks (142 / 128 / 96 /
+// 80 / 64 registers) give 0.83 / 0.77 / 0.73 / 0.75 / 0.85 ms.
+#ifndef RT_TREE_MIN_BLOCKS
+#define RT_TREE_MIN_BLOCKS 5
+#endif
+
 template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_render_tree(SceneView sc, CameraView cam, LightSet lights,
+__global__ void __launch_bounds__(kTraceThreads, RT_TREE_MIN_BLOCKS) k_render_tree(SceneView sc, CameraView cam, LightSet lights,
                                                                MaterialTable mt, uint8_t *__restrict__ rgb,
                                                                float *__restrict__ fimg, int32_t *__restrict__ ids,
                                                                Counters *ctr)
