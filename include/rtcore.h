@@ -374,6 +374,13 @@ rt_status rt_render_tone_mapped(rt_scene *scene, const rt_camera *camera, int32_
 rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const float *fimg,
                             const rt_tone_map *tone, uint8_t *rgb_out);
 
+/* Diagnostic of the tone mapper's log10 (float-float evaluation, rounded
+ * once): on n positive floats drawn from every binade (seeded), counts the
+ * values whose decided result differs from log10 evaluated in double and
+ * rounded (*mismatches, expected 0) and the values left to the double
+ * evaluation (*undecided). */
+rt_status rt_check_log10(rt_context *ctx, int64_t n, uint64_t seed, int64_t *mismatches, int64_t *undecided);
+
 /* The binary32 sum of values[0..n) in index order, rounded after every
  * addition exactly as a sequential loop `s += values[i]` rounds it (the way
  * camera::tone_map accumulates its log-luminance, camera.cc:1158), computed

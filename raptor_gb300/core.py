@@ -141,6 +141,7 @@ SIGNATURES = [
                               C.POINTER(RtRenderStats)]),
     ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
     ("rt_sum_sequential_f32", C.c_int32, [_P, _P, C.c_int64, C.POINTER(C.c_float)]),
+    ("rt_check_log10", C.c_int32, [_P, C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("rt_tone_map_image", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, _P, C.POINTER(RtToneMap), _P]),
     ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
@@ -330,6 +331,12 @@ class Context:
         _check(lib().rt_tone_map_image(self.h, C.byref(cam), int(aa[0]), int(aa[1]), ptr(img),
                                        C.byref(tm) if tm is not None else None, ptr(rgb)))
         return rgb
+
+    def check_log10(self, n: int, seed: int = 1):
+        """(mismatches, undecided) of the tone mapper's float-float log10."""
+        bad, und = C.c_int64(), C.c_int64()
+        _check(lib().rt_check_log10(self.h, int(n), int(seed), C.byref(bad), C.byref(und)))
+        return bad.value, und.value
 
     def sum_sequential(self, values) -> np.float32:
         """The binary32 sum of values in index order, rounded as a

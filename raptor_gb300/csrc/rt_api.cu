@@ -880,6 +880,24 @@ rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa
     return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, nullptr);
 }
 
+rt_status rt_check_log10(rt_context *ctx, int64_t n, uint64_t seed, int64_t *mismatches, int64_t *undecided)
+{
+    if (!ctx || !mismatches || !undecided || n < 0) return fail(RT_ERR_INVALID_ARG, "rt_check_log10: bad argument");
+    DeviceGuard g(ctx->device);
+    RT_CUDA(ctx->tone.reserve(kToneScratch + 256), "scratch allocation");
+    unsigned long long *d = (unsigned long long *)((char *)ctx->tone.ptr + kToneWord);
+    launch_check_log10(n, seed, d, ctx->sm_count, ctx->stream);
+    RT_CUDA(cudaGetLastError(), "check launch");
+    RT_CUDA(cudaMemcpyAsync(ctx->h_scratch, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream),
+            "readback");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+    unsigned long long h[2];
+    std::memcpy(h, ctx->h_scratch, sizeof(h));
+    *mismatches = (int64_t)h[0];
+    *undecided = (int64_t)h[1];
+    return RT_OK;
+}
+
 rt_status rt_sum_sequential_f32(rt_context *ctx, const float *values, int64_t n, float *sum_out)
 {
     if (!ctx || !sum_out || (n > 0 && !values)) return fail(RT_ERR_INVALID_ARG, "rt_sum_sequential_f32: NULL argument");

@@ -91,6 +91,7 @@ void launch_index_range(const int32_t *v, int32_t n, int32_t *out, cudaStream_t 
 // The binary32 sum of v[0..n) in index order, as a sequential loop rounds it
 // (into acc->sum_f); max_abs: the largest |v[i]| (launch_abs_max), > 0.
 void launch_abs_max(const float *v, int64_t n, uint32_t *out, int sm_count, cudaStream_t st);
+void launch_check_log10(int64_t n, uint64_t seed, unsigned long long *out, int sm_count, cudaStream_t st);
 void launch_sequential_sum(const float *v, int64_t n, float max_abs, ToneAcc *acc, void *scratch, int sm_count,
                            cudaStream_t st);
 // scratch: tone_scratch_bytes(fw * fh, blocks) of device memory (blocks:

@@ -8,8 +8,10 @@
 //
 // Kernels, in stream order:
 //   k_tone_terms    one pass over the samples: count and maximum of the
-//                   luminances above 3.18e-7, their log10 terms and the
-//                   per-chunk increments of the exact sequential sum
+//                   luminances above 3.18e-7, their log10 terms (rounded
+//                   once from the exact value: float-float, double for the
+//                   few too close to a rounding boundary) and the per-chunk
+//                   increments of the exact sequential sum
 //   k_tone_coarse   the chunk increments summed over groups of chunks
 //   k_tone_sum      one warp: the reference's binary32 sum of the terms,
 //                   reproduced exactly, then the mode's scale factors
@@ -42,6 +44,106 @@ __device__ __forceinline__ float log_f(float v) { return (float)log((double)v); 
 __device__ __forceinline__ float exp_f(float v) { return (float)exp((double)v); }
 __device__ __forceinline__ float pow_f(float a, float b) { return (float)pow((double)a, (double)b); }
 template <bool EXACT> __device__ __forceinline__ float tl_log10(float v) { return EXACT ? log10_f(v) : log10f(v); }
+
+// ---- log10 of a positive float, correctly rounded, in float-float arithmetic
+//
+// log10(y) = e * log10(2) + (2 / ln 10) * atanh((m - 1) / (m + 1)) with
+// y = m * 2^e, m in [sqrt(1/2), sqrt(2)), so |(m - 1) / (m + 1)| < 0.1716 and
+// the atanh series f + f^3/3 + f^5/5 + ... reaches 2^-40 by f^13.  The
+// quotient, f^3/3 and the two constant products are carried as float pairs
+// (exact products by fma), the smaller terms in float; the result's error
+// stays below 2^-33 of its value.  When the float-float value lies within
+// that error of a rounding boundary the rounding cannot be decided and the
+// function returns false; the caller evaluates log10 in double.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = xadd(a, b);
+    const float bb = xsub(s, a);
+    const float err = xadd(xsub(a, xsub(s, bb)), xsub(b, bb));
+    return {s, err};
+}
+__device__ __forceinline__ FF two_prod(float a, float b)
+{
+    const float p = xmul(a, b);
+    return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    FF p = two_prod(a.hi, b.hi);
+    p.lo = xadd(p.lo, xadd(xmul(a.hi, b.lo), xmul(a.lo, b.hi)));
+    return two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    FF s = two_sum(a.hi, b.hi);
+    s.lo = xadd(s.lo, xadd(a.lo, b.lo));
+    return two_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ bool log10_ff(float y, float &out)
+{
+    const uint32_t bits = __float_as_uint(y);
+    if (bits < 0x00800000u || bits >= 0x7f800000u) return false;   // zero, subnormal, negative, inf, nan
+    int e = (int)(bits >> 23) - 127;
+    uint32_t mb = (bits & 0x7fffffu) | 0x3f800000u;
+    if (mb > 0x3fb504f3u) {   // m > sqrt(2): halve it
+        mb -= 0x00800000u;
+        ++e;
+    }
+    const float m = __uint_as_float(mb);
+    const float num = xsub(m, 1.0f);               // exact (Sterbenz)
+    const FF den = two_sum(m, 1.0f);
+    // f = num / den as a float pair
+    const float q = __fdiv_rn(num, den.hi);
+    const float rem = xsub(fmaf(-q, den.hi, num), xmul(q, den.lo));
+    const FF f = two_sum(q, __fdiv_rn(rem, den.hi));
+    // f^3 / 3 as a pair, the rest of the series in float
+    const FF f2 = ff_mul(f, f);
+    const FF f3 = ff_mul(f2, f);
+    const FF third = {__uint_as_float(0x3eaaaaabu), __uint_as_float(0xb22aaaabu)};   // 1/3
+    const FF t3 = ff_mul(f3, third);
+    const float s = f2.hi;
+    const float rest = xmul(xmul(f3.hi, s),
+                            xadd(1.0f / 5.0f, xmul(s, xadd(1.0f / 7.0f, xmul(s, xadd(1.0f / 9.0f,
+                                 xmul(s, xadd(1.0f / 11.0f, xmul(s, 1.0f / 13.0f)))))))));
+    FF at = ff_add(f, t3);
+    at = ff_add(at, FF{rest, 0.0f});
+    // log10 = 2 * atanh * (1 / ln 10) + e * log10(2)
+    const FF inv_ln10 = {__uint_as_float(0x3ede5bd9u), __uint_as_float(0xb22d91afu)};
+    const FF log10_2 = {__uint_as_float(0x3e9a209bu), __uint_as_float(0xb2760860u)};
+    const FF lm = ff_mul(FF{xmul(2.0f, at.hi), xmul(2.0f, at.lo)}, inv_ln10);
+    const FF le = ff_mul(FF{(float)e, 0.0f}, log10_2);
+    const FF r = ff_add(le, lm);
+    const float rn = xadd(r.hi, r.lo);
+    if (rn == 0.0f) {   // y == 1
+        out = 0.0f;
+        return r.hi == 0.0f && r.lo == 0.0f;
+    }
+    // distance from the rounding boundaries around rn, against the error bound
+    const float d = xadd(xsub(r.hi, rn), r.lo);
+    const uint32_t rb = __float_as_uint(rn) & 0x7fffffffu;
+    const float ulp = __uint_as_float(((rb >> 23) - 23u) << 23);         // ulp of |rn| (normal rn)
+    const bool pow2 = (rb & 0x7fffffu) == 0u;                             // the ulp below |rn| is half of it
+    const float up = 0.5f * ulp, down = pow2 ? 0.25f * ulp : 0.5f * ulp;
+    const float towards_zero = (rn > 0.0f) ? -d : d;                     // d measured towards 0
+    const float margin = xmul(fabsf(rn), 1.1641532e-10f);                 // 2^-33 of the value
+    const bool ok = (rb >> 23) > 24u &&
+                    ((towards_zero >= 0.0f) ? (towards_zero < down - margin) : (-towards_zero < up - margin));
+    out = rn;
+    return ok;
+}
+
+// log10 rounded once from the exact value: float-float, double where the
+// float-float value is too close to a rounding boundary.
+__device__ __forceinline__ float log10_cr(float y)
+{
+    float r;
+    if (log10_ff(y, r)) return r;
+    return log10_f(y);
+}
 template <bool EXACT> __device__ __forceinline__ float tl_exp(float v) { return EXACT ? exp_f(v) : expf(v); }
 template <bool EXACT> __device__ __forceinline__ float tl_pow(float a, float b) { return EXACT ? pow_f(a, b) : powf(a, b); }
 
@@ -430,7 +532,7 @@ __global__ void __launch_bounds__(kSumThreads) k_tone_terms(const float *__restr
             if (!(Y < 3.18e-7f)) {
                 ++cnt;
                 maxb = max(maxb, __float_as_uint(Y));   // Y > 0: bit order is value order
-                a[t] = log10_f(Y);
+                a[t] = log10_cr(Y);
             }
         }
         terms[i] = a[t];   // the padding of the last chunk holds +0
@@ -939,6 +1041,46 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
     k_tone_final<<<blocks_for((int64_t)ow * oh, sm_count), kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, oh, t, acc,
                                                                                   redo, rgb);
     if (t.enabled) k_tone_fix<<<sm_count, kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, t, acc, redo, rgb);
+}
+
+namespace {
+// log10_ff against log10 in double on n floats spread over every binade
+// (counter-based: element i maps to a float from its hash): out[0] counts
+// disagreements of decided values, out[1] undecided values.
+__global__ void k_check_log10(int64_t n, uint64_t seed, unsigned long long *out)
+{
+    unsigned long long bad = 0, undecided = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = (uint64_t)i * 0x9E3779B97F4A7C15ull + seed;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        // positive normal floats, with a quarter of them near 1 (where log10 is small)
+        uint32_t bits = (uint32_t)(z & 0x7fffffffu);
+        if ((z >> 62) == 0u) bits = 0x3f000000u + (uint32_t)((z >> 32) & 0x00ffffffu);
+        if (bits < 0x00800000u || bits >= 0x7f800000u) continue;
+        float r;
+        if (log10_ff(__uint_as_float(bits), r)) {
+            if (__float_as_uint(r) != __float_as_uint(log10_f(__uint_as_float(bits)))) ++bad;
+        } else {
+            ++undecided;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        undecided += __shfl_xor_sync(0xffffffffu, undecided, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], bad);
+        atomicAdd(&out[1], undecided);
+    }
+}
+}  // namespace
+
+void launch_check_log10(int64_t n, uint64_t seed, unsigned long long *out, int sm_count, cudaStream_t st)
+{
+    cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
+    k_check_log10<<<sm_count * 8, 256, 0, st>>>(n, seed, out);
 }
 
 void launch_abs_max(const float *v, int64_t n, uint32_t *out, int sm_count, cudaStream_t st)

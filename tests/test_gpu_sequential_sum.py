@@ -50,3 +50,12 @@ def test_sequential_sum_differs_from_exact_sum(rtlib, ctx):
 def test_sequential_sum_rejects_non_finite(rtlib, ctx):
     with pytest.raises(rtlib.RtError):
         ctx.sum_sequential(np.array([1.0, np.inf], np.float32))
+
+
+def test_log10_float_float_rounds_as_double(rtlib, ctx):
+    """The tone mapper's log10 terms (float-float, rounded once) equal log10
+    evaluated in double and rounded on 2^25 floats from every binade; the
+    few too close to a rounding boundary to decide are left to double."""
+    bad, undecided = ctx.check_log10(1 << 25, seed=7)
+    assert bad == 0
+    assert undecided < (1 << 25) * 5e-3, undecided      # measured 0.28 %
