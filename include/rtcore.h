@@ -280,6 +280,14 @@ rt_status rt_render(rt_scene *scene, const rt_camera *camera, const rt_light *li
  * triangle (triangle.h:99-106). */
 rt_status rt_scene_set_materials(rt_scene *scene, const int32_t *mat_of_tri, int32_t ntris);
 
+/* Per-triangle corner normals for smooth shading: 9 floats per triangle
+ * (normals at vertices a, b, c; host or device memory), interpolated by
+ * the hit's barycentrics into the shading normal as the reference's
+ * triangle::normal_at_point does with vertex normals (triangle.h:473-476);
+ * a triangle whose first float is FLT_MAX keeps its face normal.  NULL
+ * removes them.  Shadow and secondary ray origins keep the face normal. */
+rt_status rt_scene_set_normals(rt_scene *scene, const float *corner_normals, int32_t ntris);
+
 /* rt_render with a table of up to RT_MAX_MATERIALS materials indexed per
  * triangle: every hit is shaded with its triangle's material, and mirror
  * (rf) and refracted (tran, ri) rays are traced as a tree, reflection
@@ -306,8 +314,9 @@ rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt
  * colours its faces (binary PLY), else NULL; tri_mat: per triangle the
  * material of an OBJ file (0: the default, i: the i-th distinct usemtl name
  * in order of first use; nmat of them), else NULL; kd: the parser's default
- * diffuse colour (OFF 170, PLY and OBJ 200).  OBJ material libraries
- * (mtllib) and vertex normals / texture coordinates are read past, not
+ * diffuse colour (OFF 170, PLY and OBJ 200).  OBJ vertex normals come
+ * back per triangle corner (normalised, as parse_vn_statement does); OBJ
+ * material libraries (mtllib) and texture coordinates are read past, not
  * returned.  Arrays are malloc'd; rt_mesh_free releases them. */
 #define RT_MESH_AUTO 0   /* by file extension: .off, .ply, .obj */
 #define RT_MESH_OFF 1
@@ -321,6 +330,8 @@ typedef struct rt_mesh {
     float kd[3];
     int32_t *tri_mat;
     int32_t nmat;
+    float *corner_normals;   /* OBJ vertex normals: 9 floats per triangle for rt_scene_set_normals
+                                (FLT_MAX first: none), or NULL */
 } rt_mesh;
 rt_status rt_mesh_load(const char *path, int32_t format, rt_mesh *out);
 rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *out);

@@ -199,6 +199,8 @@ def oracle_lib():
         lib["ro_render_mt"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
                                         C.POINTER(Material), C.c_int32, C.c_int32, C.c_int32, C.c_int32, _U8, _I,
                                         _U8, _F]
+        lib["ro_scene_set_normals"].restype = C.c_int32
+        lib["ro_scene_set_normals"].argtypes = [C.c_void_p, _F]
         lib["ro_scene_set_materials"].restype = C.c_int32
         lib["ro_scene_set_materials"].argtypes = [C.c_void_p, _I]
         lib["ro_tone_map_frame"].restype = C.c_int32
@@ -233,6 +235,9 @@ def ref_lib():
                                           C.c_int32, _U8]
         lib["rref_parse_mesh"].restype = C.c_int64
         lib["rref_parse_mesh"].argtypes = [C.c_char_p, C.c_int32, _F, C.c_int64, C.POINTER(C.c_int32)]
+        lib["rref_parse_and_render"].restype = C.c_int64
+        lib["rref_parse_and_render"].argtypes = [C.c_char_p, C.c_int32, C.POINTER(Camera), C.POINTER(Light),
+                                                 C.c_int32, _U8]
         lib["rref_tone_map_image"].restype = None
         lib["rref_tone_map_image"].argtypes = [C.POINTER(Camera), C.c_int32, C.c_int32, _F, C.POINTER(ToneMap), _U8]
         lib["rref_render_tone_mapped"].restype = C.c_double
@@ -269,6 +274,11 @@ class OracleScene(_SceneBase):
             self._keep = self._keep + (mt,)
             if self.lib["ro_scene_set_materials"](self.h, _p(mt, C.c_int32)) != 0:
                 raise MemoryError("oracle materials failed")
+        if scene.get("corner_normals") is not None:
+            cn = np.ascontiguousarray(scene["corner_normals"], np.float32)
+            self._keep = self._keep + (cn,)
+            if self.lib["ro_scene_set_normals"](self.h, _p(cn, C.c_float)) != 0:
+                raise MemoryError("oracle normals failed")
         self.build_seconds = self.lib["ro_scene_build"](self.h)
         if self.build_seconds < 0:
             raise MemoryError("oracle build failed")
@@ -391,6 +401,19 @@ def ref_tone_map_image(fimg, camera, tone, aa=(1, 1)):
     rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
     ref_lib()["rref_tone_map_image"](C.byref(cam), int(aa[0]), int(aa[1]), _p(img, C.c_float),
                                      C.byref(make_tone_map(tone, camera)), _p(rgb, C.c_uint8))
+    return rgb
+
+
+def ref_parse_and_render(path, kind, frame):
+    """The reference's own parser (its default phong materials) followed by
+    its bvh, ray_tracer and clip_image_to_rgb on frame's camera and lights."""
+    cam = make_camera(frame["camera"])
+    rgb = np.zeros((cam.yres, cam.xres, 3), np.uint8)
+    ls = make_lights(frame["lights"])
+    n = ref_lib()["rref_parse_and_render"](str(path).encode(), kind, C.byref(cam), ls, len(frame["lights"]),
+                                           _p(rgb, C.c_uint8))
+    if n < 0:
+        raise OSError(f"cannot open {path}")
     return rgb
 
 

@@ -312,4 +312,41 @@ int64_t rref_parse_mesh(const char *path, int32_t kind, float *tri_out, int64_t 
     return n;
 }
 
+// A mesh file parsed by the reference's own parser (kind 1 OFF, 2 PLY,
+// 3 OBJ) with the materials it creates (phong_shader), then rendered by
+// ray_tracer and clip_image_to_rgb.  Returns the triangle count, or -1.
+int64_t rref_parse_and_render(const char *path, int32_t kind, const ro_camera *c, const ro_light *ls, int32_t nl,
+                              uint8_t *rgb)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return -1;
+    light_list parsed_lights;
+    primitive_store store;
+    std::list<material *> mats;
+    camera *cam_unused = nullptr;
+    if (kind == 1) off_parser(f, parsed_lights, store, mats, nullptr);
+    else if (kind == 3) obj_parser(f, std::string(""), parsed_lights, store, mats, &cam_unused);
+    else ply_parser(f, parsed_lights, store, mats, &cam_unused);
+    const int64_t n = (int64_t)store.size();
+    {
+        std::unique_ptr<bvh> accel(new bvh(store));
+        std::unique_ptr<camera> cam(make_camera(c));
+        light_list lights;
+        for (int32_t i = 0; i < nl; ++i) {
+            const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
+            if (ls[i].kind == 1)
+                lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
+            else
+                lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
+        }
+        null_buf nb;
+        std::streambuf *old = std::cout.rdbuf(&nb);
+        ray_tracer(accel.get(), lights, store, *cam);
+        std::cout.rdbuf(old);
+        cam->clip_image_to_rgb(rgb);
+    }
+    for (material *m : mats) delete m;
+    return n;
+}
+
 }  // extern "C"

@@ -103,6 +103,7 @@ struct ro_scene {
     int32_t nnodes, root;
     int32_t *indirect;  /* primitive_store::_indirect */
     int32_t *mat;       /* material index per triangle, or NULL (all 0) */
+    float *cn;          /* corner normals, 9 floats per triangle, or NULL (x of a = FLT_MAX: none) */
 };
 
 ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris,
@@ -147,6 +148,7 @@ ro_scene *ro_scene_create(const float *verts, int32_t nverts, const int32_t *tri
 void ro_scene_destroy(ro_scene *s)
 {
     if (s) free(s->mat);
+    if (s) free(s->cn);
     if (!s) return;
     free(s->va); free(s->vb); free(s->vc); free(s->n);
     free(s->ta); free(s->tb); free(s->tc); free(s->flags);
@@ -586,8 +588,16 @@ static inline void hit_setup(const ro_scene *s, const ro_ray *r, int32_t id, con
     const float denom = vdot(n, r->d);
     const float num = vdot(n, vsub(s->vc[id], p));
     p = vadd(p, vmul(r->d, num / denom));              /* change_length */
-    if (denom > 0.0f) { *shader_n = vneg(n); *geo = vneg(n); }
-    else { *shader_n = n; *geo = n; }
+    /* the shading normal interpolates the triangle's vertex normals when it
+     * has them (triangle.h:473-476) */
+    v3 sn = n;
+    if (s->cn && s->cn[9 * (size_t)id] != RO_MAX_DIST) {
+        const float *c = s->cn + 9 * (size_t)id;
+        const float w = 1.0f - (h->u + h->v);
+        sn = vadd(vadd(vmul(mk(c[6], c[7], c[8]), h->u), vmul(mk(c[3], c[4], c[5]), h->v)), vmul(mk(c[0], c[1], c[2]), w));
+    }
+    if (denom > 0.0f) { *shader_n = vneg(sn); *geo = vneg(n); }
+    else { *shader_n = sn; *geo = n; }
     if (out_in) *out_in = !(denom > 0.0f);    /* hit_t::out_in: the ray enters the front face */
     *dst = p;
     if (s->ta) {
@@ -804,6 +814,19 @@ int64_t ro_render_mt(const ro_scene *s, const ro_camera *cam, const ro_light *li
     J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mats; J.mats = mats; J.nmats = nmats;
     J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id; J.occl = occl; J.fimg = fimg;
     return run_render(&J, nthreads);
+}
+
+int32_t ro_scene_set_normals(ro_scene *s, const float *corner_normals)
+{
+    if (!s) return -1;
+    free(s->cn);
+    s->cn = NULL;
+    if (!corner_normals) return 0;
+    const size_t nt = (size_t)(s->ntris > 0 ? s->ntris : 1);
+    s->cn = (float *)malloc(nt * 9 * sizeof(float));
+    if (!s->cn) return -1;
+    memcpy(s->cn, corner_normals, (size_t)s->ntris * 9 * sizeof(float));
+    return 0;
 }
 
 int32_t ro_scene_set_materials(ro_scene *s, const int32_t *mat_of_tri)

@@ -110,6 +110,12 @@ int64_t ro_render(const ro_scene *s, const ro_camera *cam, const ro_light *light
                   const ro_material *mat, int32_t row0, int32_t row1, int32_t nthreads,
                   uint8_t *rgb, int32_t *hit_id, uint8_t *occl, float *fimg);
 
+/* Per-triangle corner normals (9 floats per triangle, NULL: none; a
+ * triangle whose first float is FLT_MAX keeps its face normal): the shading
+ * normal interpolates them as triangle::normal_at_point does with vertex
+ * normals (triangle.h:464-498). */
+int32_t ro_scene_set_normals(ro_scene *s, const float *corner_normals);
+
 /* Per-triangle materials: mat_of_tri[i] indexes the table given to
  * ro_render_mt (NULL: every triangle uses material 0). */
 int32_t ro_scene_set_materials(ro_scene *s, const int32_t *mat_of_tri);

@@ -77,7 +77,7 @@ class RtToneMap(C.Structure):
 class RtMesh(C.Structure):
     _fields_ = [("nverts", C.c_int32), ("ntris", C.c_int32), ("verts", C.POINTER(C.c_float)),
                 ("tris", C.POINTER(C.c_int32)), ("tri_rgb", C.POINTER(C.c_uint8)), ("kd", C.c_float * 3),
-                ("tri_mat", C.POINTER(C.c_int32)), ("nmat", C.c_int32)]
+                ("tri_mat", C.POINTER(C.c_int32)), ("nmat", C.c_int32), ("corner_normals", C.POINTER(C.c_float))]
 
 
 RT_MESH_AUTO, RT_MESH_OFF, RT_MESH_PLY, RT_MESH_OBJ = 0, 1, 2, 3
@@ -140,6 +140,7 @@ SIGNATURES = [
     ("rt_render", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial), _P, _P,
                               C.POINTER(RtRenderStats)]),
     ("rt_scene_set_materials", C.c_int32, [_P, _P, C.c_int32]),
+    ("rt_scene_set_normals", C.c_int32, [_P, _P, C.c_int32]),
     ("rt_sum_sequential_f32", C.c_int32, [_P, _P, C.c_int64, C.POINTER(C.c_float)]),
     ("rt_check_log10", C.c_int32, [_P, C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("rt_tone_map_image", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, _P, C.POINTER(RtToneMap), _P]),
@@ -266,8 +267,11 @@ def _mesh_dict(m: RtMesh):
     mat = None
     if m.tri_mat:
         mat = np.ctypeslib.as_array(m.tri_mat, shape=(max(nt, 1),))[:nt].copy()
+    cn = None
+    if m.corner_normals:
+        cn = np.ctypeslib.as_array(m.corner_normals, shape=(max(nt, 1) * 9,))[: nt * 9].reshape(nt, 9).copy()
     return {"verts": verts, "tris": tris, "vattr": None, "flags": None, "tri_rgb": rgb, "kd": tuple(m.kd),
-            "tri_mat": mat, "nmat": m.nmat}
+            "tri_mat": mat, "nmat": m.nmat, "corner_normals": cn}
 
 
 def parse_mesh(data: bytes, fmt: int):
@@ -373,6 +377,8 @@ class Scene:
             self.upload(scene["verts"], scene["tris"], scene.get("vattr"), scene.get("flags"))
             if scene.get("mat_of_tri") is not None:
                 self.set_materials(scene["mat_of_tri"])
+            if scene.get("corner_normals") is not None:
+                self.set_normals(scene["corner_normals"])
             if build:
                 self.build()
 
@@ -382,6 +388,16 @@ class Scene:
         self._keep = (verts, tris, vattr, flags)
         _check(lib().rt_scene_upload(self.h, ptr(verts), nv, ptr(tris), nt, ptr(vattr), ptr(flags)))
         self.nverts, self.ntris = nv, nt
+
+    def set_normals(self, corner_normals):
+        """Corner normals per triangle ((n, 3, 3) or n*9 floats), None: none."""
+        if corner_normals is None:
+            _check(lib().rt_scene_set_normals(self.h, None, 0))
+            self._cn = None
+            return
+        cn = np.ascontiguousarray(corner_normals, np.float32).reshape(-1, 9)
+        _check(lib().rt_scene_set_normals(self.h, ptr(cn), int(cn.shape[0])))
+        self._cn = cn
 
     def set_materials(self, mat_of_tri):
         """Material index per triangle (None: every triangle uses material 0)."""

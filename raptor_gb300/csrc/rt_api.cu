@@ -163,6 +163,7 @@ SceneView scene_view(const rt_scene *s)
     v.tri_base = 0;
     v.isect = s->ctx->isect;
     v.mat = s->d_mat;
+    v.cnorm = s->d_cnorm;
     return v;
 }
 
@@ -329,6 +330,7 @@ static void scene_free_geometry(rt_scene *s)
     cudaFree(s->d_flags); s->d_flags = nullptr;
     cudaFree(s->d_shade); s->d_shade = nullptr;
     cudaFree(s->d_mat); s->d_mat = nullptr; s->mat_max = -1;
+    cudaFree(s->d_cnorm); s->d_cnorm = nullptr;
     cudaFree(s->d_nodes); s->d_nodes = nullptr;
     cudaFree(s->d_tris); s->d_tris = nullptr;
     s->temp.release();
@@ -695,6 +697,27 @@ static rt_status finish_outputs(rt_context *ctx, size_t npix, uint8_t *rgb, int3
         stats->device_ms = ms;
     }
     return status_to_error(c.status);
+}
+
+rt_status rt_scene_set_normals(rt_scene *s, const float *corner_normals, int32_t ntris)
+{
+    if (!s) return fail(RT_ERR_INVALID_ARG, "rt_scene_set_normals: NULL scene");
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (!corner_normals) {
+        cudaFree(s->d_cnorm);
+        s->d_cnorm = nullptr;
+        return RT_OK;
+    }
+    if (ntris != s->ntris) return fail(RT_ERR_INVALID_ARG, "rt_scene_set_normals: ntris differs from the scene's");
+    if (!s->d_cnorm)
+        RT_CUDA(cudaMalloc(&s->d_cnorm, (size_t)std::max(ntris, 1) * 9 * sizeof(float)), "normal allocation");
+    if (ntris > 0)
+        RT_CUDA(cudaMemcpyAsync(s->d_cnorm, corner_normals, (size_t)ntris * 9 * sizeof(float), cudaMemcpyDefault,
+                                ctx->stream), "normal copy");
+    RT_CUDA(cudaStreamSynchronize(ctx->stream), "normal upload synchronize");
+    return RT_OK;
 }
 
 rt_status rt_scene_set_materials(rt_scene *s, const int32_t *mat_of_tri, int32_t ntris)

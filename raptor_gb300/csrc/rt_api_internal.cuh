@@ -57,6 +57,7 @@ struct rt_scene {
     rtc::ShadeTri *d_shade = nullptr;
     int32_t *d_mat = nullptr;             // material index per triangle (rt_scene_set_materials)
     int32_t mat_max = -1;                 // largest index in d_mat (-1: none set)
+    float *d_cnorm = nullptr;             // corner normals, 9 floats per triangle (rt_scene_set_normals)
     rtc::WideNode *d_nodes = nullptr;
     rtc::PackedTri *d_tris = nullptr;
     int32_t nnodes = 0, tri_slots = 0, depth = 0;

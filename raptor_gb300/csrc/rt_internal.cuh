@@ -70,6 +70,7 @@ struct SceneView {
     int32_t tri_base;         // subtracted from packed ids to give the caller's ids
     int32_t isect;            // RT_ISECT_REFERENCE or RT_ISECT_WATERTIGHT
     const int32_t *mat = nullptr;   // material index per triangle (caller's order) or nullptr
+    const float *cnorm = nullptr;   // 9 floats per triangle: corner normals a, b, c (x of a = FLT_MAX: none)
 };
 
 struct CameraView {

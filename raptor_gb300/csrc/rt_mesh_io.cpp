@@ -60,17 +60,25 @@ struct Mesh {
     std::vector<int32_t> tris;
     std::vector<uint8_t> rgb;   // per triangle, when the file colours its faces
     std::vector<int32_t> mat;   // per triangle, when the file names materials
-    bool coloured = false, named = false;
+    std::vector<float> cn;      // 9 per triangle (corner normals), when the file has vertex normals
+    bool coloured = false, named = false, normals = false;
     int32_t cur_mat = 0, nmat = 1;
     float kd = 0.0f;
     V3 vert(int32_t i) const { return {verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]}; }
-    void add(int32_t a, int32_t b, int32_t c, const uint8_t *col)
+    void add(int32_t a, int32_t b, int32_t c, const uint8_t *col, const V3 *nrm = nullptr)
     {
         tris.push_back(a);
         tris.push_back(b);
         tris.push_back(c);
         if (coloured) rgb.insert(rgb.end(), col, col + 3);
         if (named) mat.push_back(cur_mat);
+        if (normals) {
+            for (int k = 0; k < 3; ++k) {
+                cn.push_back(nrm ? nrm[k].x : 3.402823466e38f);
+                cn.push_back(nrm ? nrm[k].y : 0.0f);
+                cn.push_back(nrm ? nrm[k].z : 0.0f);
+            }
+        }
     }
 };
 
@@ -81,7 +89,8 @@ struct Mesh {
 // the face's way and holds no face vertex strictly inside; a collinear
 // triple drops its middle vertex without a triangle; stop when two vertices
 // remain or a full lap accepts nothing.
-void triangulate(Mesh &m, const std::vector<int32_t> &face, const uint8_t *col)
+void triangulate(Mesh &m, const std::vector<int32_t> &face, const uint8_t *col,
+                 const std::vector<V3> *fnorm = nullptr)
 {
     const size_t n = face.size();
     if (n < 3) return;
@@ -118,8 +127,16 @@ void triangulate(Mesh &m, const std::vector<int32_t> &face, const uint8_t *col)
                 for (size_t i = 0; i < n && !inside; ++i)
                     inside = same_side(p[i], a, ab) && same_side(p[i], b, bc) && same_side(p[i], c, ca);
             }
-            if (dot(tn, fn) > 0.0f && !inside) m.add(face[prev], face[cur], face[next], col);
-            else accepted = false;
+            if (dot(tn, fn) > 0.0f && !inside) {
+                if (fnorm) {
+                    const V3 cn3[3] = {(*fnorm)[prev], (*fnorm)[cur], (*fnorm)[next]};
+                    m.add(face[prev], face[cur], face[next], col, cn3);
+                } else {
+                    m.add(face[prev], face[cur], face[next], col);
+                }
+            } else {
+                accepted = false;
+            }
         }
         if (accepted) {
             --left;
@@ -468,7 +485,9 @@ rt_status parse_obj(Cursor cur, Mesh &m)
     m.named = true;
     std::vector<std::string> names;   // usemtl names in order of first use (index + 1)
     long nvt = 0, nvn = 0;
+    std::vector<V3> vn;                // unit vertex normals (parse_vn_statement normalises)
     std::vector<int32_t> face;
+    std::vector<V3> face_n;
     const char *const last = cur.end - 1;   // the reference stops one byte before the end
     while (cur.c < last) {
         cur.c = obj_statement(cur.c, last);
@@ -489,10 +508,13 @@ rt_status parse_obj(Cursor cur, Mesh &m)
             --cur.c;
             cur.next_line();
         } else if (cur.starts("vn")) {
-            cur.next_float();
-            cur.next_float();
-            cur.next_float();
+            V3 n;
+            n.x = cur.next_float();
+            n.y = cur.next_float();
+            n.z = cur.next_float();
             cur.next_line();
+            vn.push_back(unit(n));
+            m.normals = true;
             ++nvn;
         } else if (cur.starts("vt")) {
             cur.next_float();
@@ -513,6 +535,7 @@ rt_status parse_obj(Cursor cur, Mesh &m)
             };
             const long nv = (long)(m.verts.size() / 3);
             face.clear();
+            face_n.clear();
             find_vertex();
             while (cur.c < cur.end && *cur.c != '\n' && *cur.c != '\r') {
                 long vi = std::strtol(cur.c, nullptr, 10);
@@ -531,6 +554,7 @@ rt_status parse_obj(Cursor cur, Mesh &m)
                         long ni = std::strtol(cur.c, nullptr, 10);
                         ni = (ni < 0) ? nvn + ni : ni - 1;
                         if (ni < 0 || ni >= nvn) return bad("rt_mesh: OBJ normal index out of range");
+                        face_n.push_back(vn[ni]);
                     }
                 }
                 find_vertex();
@@ -542,10 +566,11 @@ rt_status parse_obj(Cursor cur, Mesh &m)
                 const V3 a0 = m.vert(face[0]), b0 = m.vert(face[1]), c0 = m.vert(face[2]);
                 if (differ(a0, b0) && differ(a0, c0) && differ(b0, c0)) {
                     const V3 n = cross(unit(sub(a0, b0)), unit(sub(b0, c0)));
-                    if (dot(n, n) > 0.0f) m.add(face[0], face[1], face[2], nullptr);
+                    if (dot(n, n) > 0.0f)
+                        m.add(face[0], face[1], face[2], nullptr, face_n.size() == 3 ? face_n.data() : nullptr);
                 }
             } else {
-                triangulate(m, face, nullptr);
+                triangulate(m, face, nullptr, face_n.size() == face.size() ? &face_n : nullptr);
             }
         } else if (*cur.c == 'v') {
             m.verts.push_back(cur.next_float());
@@ -605,9 +630,11 @@ rt_status rt_mesh_parse(const char *data, int64_t len, int32_t format, rt_mesh *
     out->tris = copy_out(m.tris);
     out->tri_rgb = m.coloured ? copy_out(m.rgb) : nullptr;
     out->tri_mat = m.named ? copy_out(m.mat) : nullptr;
+    out->corner_normals = m.normals ? copy_out(m.cn) : nullptr;
     out->nmat = m.nmat;
     out->kd[0] = out->kd[1] = out->kd[2] = m.kd;
-    if (!out->verts || !out->tris || (m.coloured && !out->tri_rgb) || (m.named && !out->tri_mat)) {
+    if (!out->verts || !out->tris || (m.coloured && !out->tri_rgb) || (m.named && !out->tri_mat) ||
+        (m.normals && !out->corner_normals)) {
         rt_mesh_free(out);
         return rt_set_error_message(RT_ERR_OUT_OF_MEMORY, "rt_mesh_parse: out of host memory");
     }
@@ -642,6 +669,8 @@ void rt_mesh_free(rt_mesh *m)
     std::free(m->tris);
     std::free(m->tri_rgb);
     std::free(m->tri_mat);
+    std::free(m->corner_normals);
+    m->corner_normals = nullptr;
     m->verts = nullptr;
     m->tris = nullptr;
     m->tri_rgb = nullptr;

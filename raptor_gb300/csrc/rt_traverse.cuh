@@ -477,11 +477,24 @@ __device__ __forceinline__ SurfacePoint surface_at(const SceneView &sc, const Ra
     const float denom = xdot(n, r.d);
     const float num = xdot(n, xsub3(c, p));
     p = xadd3(p, xmul3(r.d, xdiv(num, denom)));
+    // shading normal: the triangle's corner normals interpolated by the
+    // hit's barycentrics when it has them (triangle.h:473-476), else the
+    // face normal; both face-forwarded with the face normal's test
+    float3 sn = n;
+    if (sc.cnorm) {
+        const float *cn = sc.cnorm + 9 * (size_t)h.id;
+        if (cn[0] != FLT_MAX) {
+            const float3 A = make_float3(cn[0], cn[1], cn[2]), B = make_float3(cn[3], cn[4], cn[5]),
+                         C = make_float3(cn[6], cn[7], cn[8]);
+            const float w = xsub(1.0f, xadd(h.u, h.v));
+            sn = xadd3(xadd3(xmul3(C, h.u), xmul3(B, h.v)), xmul3(A, w));
+        }
+    }
     if (denom > 0.0f) {
-        sp.sn = make_float3(-n.x, -n.y, -n.z);
-        sp.geo = sp.sn;
+        sp.sn = make_float3(-sn.x, -sn.y, -sn.z);
+        sp.geo = make_float3(-n.x, -n.y, -n.z);
     } else {
-        sp.sn = n;
+        sp.sn = sn;
         sp.geo = n;
     }
     sp.out_in = !(denom > 0.0f);

@@ -183,6 +183,21 @@ def _polygons(rng):
     return verts, faces
 
 
+def mesh_frame(tris):
+    """A camera looking at the bounding box of the parsed triangles from
+    above and in front, with one point light and one directional light."""
+    from raptor_gb300 import scenes
+    v = tris.reshape(-1, 3).astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    c = (lo + hi) / 2
+    size = float(np.max(hi - lo))
+    eye = c + np.array([0.1 * size, 0.6 * size, 1.2 * size])
+    cam = scenes.look_at_camera(tuple(eye), tuple(c), 50.0, 96, 64, background=(30.0, 40.0, 60.0))
+    lights = [scenes.point_light(tuple(c + np.array([0.3 * size, 1.0 * size, 0.8 * size]))),
+              scenes.directional_light((-0.3, -0.9, -0.2), rgb=(90.0, 90.0, 90.0))]
+    return {"camera": cam, "lights": lights}
+
+
 def mesh_files():
     """(name, kind 1 OFF / 2 PLY, file bytes) for the parser cases."""
     import struct
@@ -314,6 +329,11 @@ def main():
             path = os.path.join(td, f"{name}.{('off', 'ply', 'obj')[kind - 1]}")
             open(path, "wb").write(data)
             tris, nmat = O.ref_parse_mesh(path, kind)
+            # the reference's own render of the parsed scene (its parser's
+            # phong materials), for the ingest -> render parity test
+            frame = mesh_frame(tris)
+            arrays[f"mesh{k}_render_rgb"] = O.ref_parse_and_render(path, kind, frame)
+            arrays[f"mesh{k}_frame"] = np.frombuffer(json.dumps(frame).encode(), np.uint8)
             arrays[f"mesh{k}_bytes"] = np.frombuffer(data, np.uint8)
             arrays[f"mesh{k}_kind"] = np.array([kind], np.int32)
             arrays[f"mesh{k}_tris"] = tris

@@ -900,3 +900,25 @@ def test_histogram_tone_mapping_render(rtlib, ctx, oracle):
     with pytest.raises(rtlib.RtError):
         sc.render_tone_mapped(narrow, {"mode": 3})
     sc.close()
+
+
+def mesh_cases_gpu():
+    g = np.load(os.path.join(GOLDEN, "ref_small.npz"))
+    return [k for k in range(64) if f"mesh{k}_bytes" in g.files]
+
+
+@pytest.mark.parametrize("k", mesh_cases_gpu())
+def test_ingested_scene_renders_as_reference_on_gpu(rtlib, ctx, oracle, golden, k):
+    """Parse (rt_mesh_parse) -> upload -> render with the parser's materials,
+    face colours as a material table and OBJ vertex normals as corner
+    normals: the reference's own frame of the same file (its parser, bvh and
+    ray_tracer), and the restatement's, on all but tie pixels."""
+    from test_mesh_ingest import mesh_scene
+    scene, frame, ref = mesh_scene(rtlib, golden, k)
+    sc = rtlib.Scene(ctx, scene)
+    got = sc.render(frame)["rgb"]
+    sc.close()
+    want = oracle.OracleScene(scene).render(frame)["rgb"]
+    for other in (ref, want):
+        within1, exact, _ = pixel_agreement(got, other)
+        assert exact >= 0.995, (exact, within1)
