@@ -1,7 +1,8 @@
 """Randomised parity sweep: seeded random scenes (triangle soups with light
 and transparent flags, spheres, heightfields), random cameras, light mixes and
 materials (tables of refracting and reflecting materials indexed per
-triangle on odd seeds); every frame, hit-id map and a batch of random rays is compared
+triangle on odd seeds, corner normals for smooth shading on every fourth);
+every frame, hit-id map and a batch of random rays is compared
 with the oracle under the parity rules of tests/parity.py."""
 import numpy as np
 import pytest
@@ -63,6 +64,15 @@ def random_case(seed):
         # reference's material::is_transparent, set when tran > 0)
         see_through = np.array([m["tran"] > 0.0 for m in table])[scene["mat_of_tri"]]
         scene["flags"] = (scene["flags"] & np.uint32(1)) | np.where(see_through, np.uint32(2), np.uint32(0))
+    if seed % 4 == 2:
+        # smooth shading: unit corner normals near the face normal, some
+        # triangles without (first float FLT_MAX)
+        nt = scene["tris"].shape[0]
+        cn = rng.normal(size=(nt, 3, 3)).astype(np.float32)
+        cn /= np.linalg.norm(cn, axis=2, keepdims=True)
+        cn = cn.reshape(nt, 9)
+        cn[rng.uniform(size=nt) < 0.2, 0] = np.float32(3.4028234663852886e38)
+        scene["corner_normals"] = cn
     return scene, frame, rng
 
 
