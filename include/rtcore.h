@@ -79,15 +79,21 @@ typedef struct rt_camera {
 
 /* Light (raytracer/light.h:17-34).  kind RT_LIGHT_POINT: point light at pos
  * (spherical light with soft shadows off); RT_LIGHT_DIRECTIONAL: light along
- * dir.  rgb in 0..255, d the distance drop-off. */
+ * dir; RT_LIGHT_SPOT: point light at pos whose intensity falls off with the
+ * angle a = acos(shadow-ray direction . dir) as clamp(1 - (a - s_a) /
+ * (s_b - s_a), 0, 1) (the spot-light constructor and get_light_intensity,
+ * light.h:24-25, 44-59; s_b = 0 leaves it a point light).  rgb in 0..255, d
+ * the distance drop-off. */
 #define RT_LIGHT_POINT 0
 #define RT_LIGHT_DIRECTIONAL 1
+#define RT_LIGHT_SPOT 2
 typedef struct rt_light {
     int32_t kind;
     float rgb[3];
     float pos[3];
     float dir[3];
     float d;
+    float s_a, s_b;   /* RT_LIGHT_SPOT: inner and outer cone angles (radians) */
 } rt_light;
 
 /* Coloured Phong material (materials/coloured_mapper_shader.h): ka, kd, ks in

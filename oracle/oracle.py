@@ -29,7 +29,7 @@ class Camera(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
-                ("d", C.c_float)]
+                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float)]
 
 
 class Material(C.Structure):
@@ -76,6 +76,8 @@ def make_lights(ls):
         arr[i].pos[:] = list(d["pos"])
         arr[i].dir[:] = list(d["dir"])
         arr[i].d = d["d"]
+        arr[i].s_a = d.get("s_a", 0.0)
+        arr[i].s_b = d.get("s_b", 0.0)
     return arr
 
 

@@ -226,6 +226,8 @@ double rref_render_tone_mapped(void *h, const ro_camera *c, int32_t aa_x, int32_
         const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
         if (ls[i].kind == 1)
             lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
+        else if (ls[i].kind == 2)   // spot light (light.h:24-25)
+            lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, 0.0f);
         else
             lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
     }
@@ -336,6 +338,8 @@ int64_t rref_parse_and_render(const char *path, int32_t kind, const ro_camera *c
             const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
             if (ls[i].kind == 1)
                 lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
+            else if (ls[i].kind == 2)
+                lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, 0.0f);
             else
                 lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
         }

@@ -696,8 +696,17 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
         /* light::get_light_intensity (light.h:44-59) */
         const float dist = len * L->d;
         const float d_scale = (dist * dist) + 1.0f;
-        const v3 I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale,
-                        (L->rgb[2] / 255.0f) / d_scale);
+        v3 I;
+        if (L->kind == 2 && L->s_b != 0.0f) {
+            /* spot light: falls off with the angle off its axis */
+            const float a = acosf(vdot(sr.d, ld3(L->dir)));
+            const float p = (a - L->s_a) / (L->s_b - L->s_a);
+            const float f = smax(0.0f, smin(1.0f, 1.0f - p));
+            const float fs = f / d_scale;
+            I = mk((L->rgb[0] / 255.0f) * fs, (L->rgb[1] / 255.0f) * fs, (L->rgb[2] / 255.0f) * fs);
+        } else {
+            I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale, (L->rgb[2] / 255.0f) / d_scale);
+        }
         c = mk(c.x + I.x * (sc.x * lmagn), c.y + I.y * (sc.y * lmagn), c.z + I.z * (sc.z * lmagn));
     }
     c = vadd(c, ld3(m->ka));

@@ -48,6 +48,7 @@ typedef struct ro_light {
     float pos[3];
     float dir[3];
     float d;
+    float s_a, s_b;   /* kind 2 (spot light at pos, axis dir): cone angles, light.h:24-25 */
 } ro_light;
 
 /* Coloured-mapper Phong material (materials/coloured_mapper_shader.h): ka,

@@ -61,7 +61,7 @@ class RtCamera(C.Structure):
 
 class RtLight(C.Structure):
     _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
-                ("d", C.c_float)]
+                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float)]
 
 
 class RtMaterial(C.Structure):
@@ -222,6 +222,8 @@ def make_lights(ls):
         arr[i].pos[:] = list(d["pos"])
         arr[i].dir[:] = list(d["dir"])
         arr[i].d = d["d"]
+        arr[i].s_a = d.get("s_a", 0.0)
+        arr[i].s_b = d.get("s_b", 0.0)
     return arr
 
 

@@ -125,6 +125,8 @@ LightView make_light_view(const rt_light &l)
     v.pos = make_float3(l.pos[0], l.pos[1], l.pos[2]);
     v.dir = make_float3(l.dir[0], l.dir[1], l.dir[2]);
     v.d = l.d;
+    v.s_a = (l.kind == RT_LIGHT_SPOT) ? l.s_a : 0.0f;
+    v.s_b = (l.kind == RT_LIGHT_SPOT) ? l.s_b : 0.0f;
     // light::find_major_direction (light.h:172-219)
     const float nx = l.dir[0], ny = l.dir[1], nz = l.dir[2];
     bool neg;

@@ -552,7 +552,19 @@ __device__ __forceinline__ void phong_add(const LightView &L, const MaterialView
     }
     const float dist = xmul(len, L.d);
     const float d_scale = xadd(xmul(dist, dist), 1.0f);
-    const float3 I = make_float3(xdiv(L.rgb255.x, d_scale), xdiv(L.rgb255.y, d_scale), xdiv(L.rgb255.z, d_scale));
+    float3 I;
+    if (L.s_b != 0.0f) {
+        // spot light: intensity by the angle off its axis (light.h:49-55)
+        const float cosa = xdot(ldir, L.dir);
+        const float a = EXACT ? (float)acos((double)cosa) : acosf(cosa);
+        const float p = xdiv(xsub(a, L.s_a), xsub(L.s_b, L.s_a));
+        const float q = xsub(1.0f, p);
+        const float f = (0.0f < ((q < 1.0f) ? q : 1.0f)) ? ((q < 1.0f) ? q : 1.0f) : 0.0f;   // max(0, min(1, q))
+        const float fs = xdiv(f, d_scale);
+        I = make_float3(xmul(L.rgb255.x, fs), xmul(L.rgb255.y, fs), xmul(L.rgb255.z, fs));
+    } else {
+        I = make_float3(xdiv(L.rgb255.x, d_scale), xdiv(L.rgb255.y, d_scale), xdiv(L.rgb255.z, d_scale));
+    }
     c = make_float3(xadd(c.x, xmul(I.x, xmul(sc.x, magn))), xadd(c.y, xmul(I.y, xmul(sc.y, magn))),
                     xadd(c.z, xmul(I.z, xmul(sc.z, magn))));
 }

@@ -181,9 +181,10 @@ struct gpu_light_args
 {
     bool directional;
     ext_colour_t rgb;      /* 0..255 */
-    point_t<> centre;      /* point light */
-    point_t<> direction;   /* directional light */
+    point_t<> centre;      /* point and spot light */
+    point_t<> direction;   /* directional light; a spot light's n */
     float d;
+    float s_a = 0.0f, s_b = 0.0f;   /* spot light cone (light.h:24-25); s_b = 0: not a spot light */
 };
 
 // ray_tracer() replacement: renders the frame on the GPU and writes every
@@ -213,6 +214,9 @@ inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_lig
         ls[i].pos[0] = l.centre.x; ls[i].pos[1] = l.centre.y; ls[i].pos[2] = l.centre.z;
         ls[i].dir[0] = l.direction.x; ls[i].dir[1] = l.direction.y; ls[i].dir[2] = l.direction.z;
         ls[i].d = l.d;
+        if (!l.directional && l.s_b != 0.0f) ls[i].kind = RT_LIGHT_SPOT;
+        ls[i].s_a = l.s_a;
+        ls[i].s_b = l.s_b;
     }
     rt_material m;
     m.ka[0] = ka.r; m.ka[1] = ka.g; m.ka[2] = ka.b;

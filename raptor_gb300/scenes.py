@@ -190,6 +190,15 @@ def point_light(pos, rgb=(255.0, 255.0, 255.0), d=0.0):
     return {"kind": 0, "rgb": tuple(rgb), "pos": tuple(float(x) for x in pos), "dir": (0.0, 0.0, 0.0), "d": float(d)}
 
 
+def spot_light(pos, direction, s_a, s_b, rgb=(255.0, 255.0, 255.0), d=0.0):
+    """Spot light at pos along `direction` (unit), full intensity within
+    s_a radians of the axis, none beyond s_b."""
+    n = np.asarray(direction, np.float64)
+    n = n / np.linalg.norm(n)
+    return {"kind": 2, "rgb": tuple(rgb), "pos": tuple(float(x) for x in pos), "dir": tuple(float(x) for x in n),
+            "d": d, "s_a": float(s_a), "s_b": float(s_b)}
+
+
 def directional_light(direction, rgb=(255.0, 255.0, 255.0), d=0.0):
     n = np.asarray(direction, dtype=np.float64)
     n = n / np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])

@@ -149,6 +149,18 @@ FRAME_TONE = (({"mode": 2}, (1, 1)), ({"mode": 3}, (1, 1)),
               ({"mode": 5, "gamma": 2.2}, (1, 1)), ({"mode": 9, "desaturate": True}, (2, 2)))
 
 
+def spot_frames():
+    """The icosphere lit by spot lights (light.h:24-25, 49-55): narrow and
+    wide cones, a coloured one with distance fall-off beside a point light."""
+    from raptor_gb300 import scenes
+    s, f = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    sets = ([scenes.spot_light((0.0, 4.0, 1.0), (0.0, 1.0, 0.25), 0.2, 0.6)],
+            [scenes.spot_light((2.0, 3.0, 2.0), (0.5, 0.6, 0.5), 0.1, 0.3, rgb=(255.0, 200.0, 100.0), d=0.05),
+             scenes.point_light((-3.0, 4.0, 2.0), rgb=(60.0, 60.0, 90.0))],
+            [scenes.spot_light((0.0, 2.0, 3.0), (0.0, 0.5, 1.0), 0.0, 1.2)])
+    return s, [dict(f, lights=ls) for ls in sets]
+
+
 def hdr_frame():
     from raptor_gb300 import scenes
     s, f = scenes.icosphere_scene(freq=8, seed=0, res=64)
@@ -311,6 +323,12 @@ def main():
         arrays[f"ftone{k}_rgb"] = O.ref_tone_map_image(fimg, hf["camera"], tone, aa)
     arrays["ftone_cases"] = np.frombuffer(json.dumps([[t, list(aa)] for t, aa in FRAME_TONE]).encode(), np.uint8)
     arrays["ftone_camera"] = np.frombuffer(json.dumps(hf["camera"]).encode(), np.uint8)
+    # spot lights
+    ss, sframes = spot_frames()
+    rs = O.RefScene(ss, sframes[0]["material"])
+    for k, fr in enumerate(sframes):
+        arrays[f"spot{k}_rgb"] = rs.render(fr)["rgb"]
+        arrays[f"spot{k}_frame"] = np.frombuffer(json.dumps(fr).encode(), np.uint8)
     # per-triangle materials with refraction: the glass sphere
     from raptor_gb300 import scenes
     for k, kw in enumerate(GLASS):

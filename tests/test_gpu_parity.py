@@ -922,3 +922,20 @@ def test_ingested_scene_renders_as_reference_on_gpu(rtlib, ctx, oracle, golden, 
     for other in (ref, want):
         within1, exact, _ = pixel_agreement(got, other)
         assert exact >= 0.995, (exact, within1)
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_spot_lights_vs_reference_and_oracle(rtlib, ctx, oracle, golden, k):
+    """RT_LIGHT_SPOT through rt_render (fused kernel: single-precision acos
+    and power with the exact re-shade near truncation), rt_render_materials
+    (ray-tree kernel, exact) and the batched form: the reference's frames."""
+    from raptor_gb300 import scenes
+    frame = json.loads(golden[f"spot{k}_frame"].tobytes().decode())
+    s, _ = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    sc = rtlib.Scene(ctx, s)
+    want = oracle.OracleScene(s).render(frame)["rgb"]
+    for got in (sc.render(frame)["rgb"], sc.render(dict(frame, materials=[frame["material"]] * 2))["rgb"]):
+        for other in (want, golden[f"spot{k}_rgb"]):
+            within1, exact, _ = pixel_agreement(got, other)
+            assert exact >= 0.998, (exact, within1)
+    sc.close()

@@ -242,3 +242,16 @@ def test_oracle_tone_map_of_fixed_frame_matches_reference(oracle, golden, case):
     ref = golden[f"ftone{k}_rgb"]
     assert np.array_equal(out, ref)
     assert ref.std() > 20.0      # a frame with contrast, not a saturated one
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_oracle_spot_lights_match_reference(oracle, golden, k):
+    """Spot lights (light.h:24-25, intensity by the angle off the axis,
+    light.h:49-55) restated: the reference's own frames (but for the
+    icosphere's few tie pixels)."""
+    from raptor_gb300 import scenes
+    frame = json.loads(golden[f"spot{k}_frame"].tobytes().decode())
+    s, _ = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    out = oracle.OracleScene(s).render(frame)["rgb"]
+    within1, exact, _ = pixel_agreement(out, golden[f"spot{k}_rgb"])
+    assert exact >= 0.998, exact
