@@ -1011,9 +1011,32 @@ rt_status rt_render_materials(rt_scene *s, const rt_camera *camera, const rt_lig
     if (st != RT_OK) return st;
     st = check_table(s, lights, nlights, materials, nmaterials, "rt_render_materials");
     if (st != RT_OK) return st;
-    const bool plain = nmaterials == 1 && materials[0].rf == 0.0f && materials[0].tran == 0.0f;
-    if (plain) return rt_render(s, camera, lights, nlights, materials, rgb_out, hit_ids, stats);
-    return render_tree(s, camera, lights, nlights, materials, nmaterials, true, rgb_out, hit_ids, stats);
+    bool secondary = false;
+    for (int32_t i = 0; i < nmaterials; ++i) secondary |= materials[i].rf != 0.0f || materials[i].tran != 0.0f;
+    if (secondary) return render_tree(s, camera, lights, nlights, materials, nmaterials, true, rgb_out, hit_ids, stats);
+    if (nmaterials == 1 || !s->d_mat) return rt_render(s, camera, lights, nlights, materials, rgb_out, hit_ids, stats);
+    // per-triangle materials without secondary rays: the fused kernel with a table
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    RenderOut o;
+    st = prepare_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o);
+    if (st != RT_OK) return st;
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = 1;
+    for (int32_t i = 0; i < nmaterials; ++i) ls.fast_pow &= fast_pow_ok(lights, nlights, materials[i]) ? 1 : 0;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    MaterialTable mt;
+    mt.n = nmaterials;
+    for (int i = 0; i < nmaterials; ++i) mt.m[i] = make_material_view(materials[i]);
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    launch_render_table(scene_view(s), make_camera_view(*camera), ls, mt, o.rgb, o.ids, ctx->d_counters, ctx->sm_count,
+                        ctx->stream, ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    return finish_outputs(ctx, npix, rgb_out, hit_ids, nullptr, o, stats);
 }
 
 rt_status rt_render(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,

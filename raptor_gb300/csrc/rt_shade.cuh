@@ -56,11 +56,14 @@ struct PixelOut {
 };
 
 // Primary ray, closest hit, one shadow ray per light, coloured Phong
-// (ray_trace_engine::ray_trace, raytracer.cc:20-87).
-template <bool COUNT>
+// (ray_trace_engine::ray_trace, raytracer.cc:20-87).  TABLE: the hit
+// triangle's material from `table` (per-triangle indices in sc.mat), else
+// `mat0` for every triangle.
+template <bool COUNT, bool TABLE = false>
 __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, const CameraView &cam, const LightView *lights,
-                                                       int nl, const MaterialView &mat, int x, int y,
-                                                       uint32_t &status, FetchCount *fc, bool fast_pow)
+                                                       int nl, const MaterialView &mat0, int x, int y,
+                                                       uint32_t &status, FetchCount *fc, bool fast_pow,
+                                                       const MaterialTable *table = nullptr)
 {
     PixelOut out;
     out.secondary = 0;
@@ -73,6 +76,12 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
     out.id = out.hit ? h.id - sc.tri_base : -1;
     out.c = cam.background;
     if (out.hit) {
+        int32_t mi = 0;
+        if (TABLE && sc.mat) {
+            mi = __ldg(&sc.mat[out.id]);
+            if (mi < 0 || mi >= table->n) { status |= kStatusBadIndex; mi = 0; }
+        }
+        const MaterialView &mat = TABLE ? table->m[mi] : mat0;
         const SurfacePoint sp = surface_at(sc, r, h);
         const float3 start = offset_start(sp.dst, sp.geo);
         const float3 kd = material_kd(mat, sp);

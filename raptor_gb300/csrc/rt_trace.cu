@@ -89,6 +89,46 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render(
     if (status) atomicOr(&ctr->status, status);
 }
 
+// k_render with the hit triangle's material taken from a table
+// (rt_render_materials without mirror or refracted rays): a separate kernel
+// so that the single-material one keeps its code and parameter block.
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_table(SceneView sc, CameraView cam, LightSet lights,
+                                                          MaterialView mat, uint8_t *__restrict__ rgb,
+                                                          int32_t *__restrict__ ids, Counters *ctr,
+                                                          MaterialTable table)
+{
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
+    uint32_t status = 0;
+    FetchCount fc;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items) break;
+        int x, y;
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
+        const bool live = (x < cam.xres) && (y < cam.yres);
+        PixelOut po;
+        po.hit = false;
+        po.secondary = 0;
+        if (live) {
+            po = shade_pixel_lights<COUNT, true>(sc, cam, lights.l, lights.n, mat, x, y, status, &fc,
+                                                 lights.fast_pow != 0, &table);
+            const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+            store_rgb(rgb, pix, po.c);
+            if (ids) ids[pix] = po.id;
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
+    }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
 // RT_AO_SPREAD: spread each warp's AO rays over all its lanes (default), or
 // one pixel's rays per lane.
 #ifndef RT_AO_SPREAD
@@ -402,6 +442,16 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
         k_render<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
     else
         k_render<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+}
+
+void launch_render_table(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
+                         uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
+{
+    static const int grid = grid_of(k_render_table<false>, sm_count);
+    if (count)
+        k_render_table<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt.m[0], rgb, ids, ctr, mt);
+    else
+        k_render_table<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt.m[0], rgb, ids, ctr, mt);
 }
 
 void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,

@@ -731,6 +731,11 @@ def test_materials_per_triangle(rtlib, ctx, oracle):
     assert np.array_equal(sc.render(f)["rgb"], got)
     with pytest.raises(rtlib.RtError):      # index 3 set, table of 3
         sc.render(dict(frame, materials=table[:3]))
+    # without mirror or refracted rays the fused kernel takes the table
+    flat = [dict(m, rf=0.0) for m in table]
+    got_flat = sc.render(dict(frame, materials=flat))["rgb"]
+    want_flat = oracle.OracleScene(dict(scene, mat_of_tri=mat)).render(dict(frame, materials=flat))["rgb"]
+    assert pixel_agreement(got_flat, want_flat)[1] >= 0.998
     for badv in (-1, 16):
         bad = mat.copy()
         bad[nt // 2] = badv
