@@ -352,7 +352,8 @@ void rt_mesh_free(rt_mesh *mesh);
  * after tone mapping (2.2 selects the sRGB curve, as in the reference), 0
  * none.  The histogram modes (camera::histogram_tone_map, camera.cc:
  * 1843-2062) resample the frame to one block per degree of the camera's
- * view and need a view of at least 2 degrees each way. */
+ * view and need a view of 2 to 4096 degrees each way (measured as the
+ * reference measures it: 2w/t and 2h/t radians). */
 #define RT_TONE_NONE 0
 #define RT_TONE_GLOBAL_CONTRAST 1
 #define RT_TONE_LOCAL_HISTOGRAM 2          /* camera::histogram_tone_map(false) */

@@ -858,8 +858,9 @@ static rt_status tone_view(const rt_tone_map *tone, const rt_camera &cam, int32_
         const float x_angle = (-2.0f * x_m) / cam.t, y_angle = (-2.0f * y_m) / cam.t;
         const float per_rad = 360.0f / (2.0f * pi);
         const float sx = x_angle * per_rad, sy = y_angle * per_rad;
-        if (!(sx >= 2.0f && sy >= 2.0f && sx < 65536.0f && sy < 65536.0f))
-            return fail(RT_ERR_INVALID_ARG, w + ": histogram tone mapping needs a view of 2 to 65535 degrees");
+        if (!(sx >= 2.0f && sy >= 2.0f && sx < 4097.0f && sy < 4097.0f))
+            return fail(RT_ERR_INVALID_ARG, w + ": histogram tone mapping needs a view of 2 to 4096 degrees "
+                                                "(2w/t and 2h/t in the reference's degree measure)");
         tv.hist_sx = (int32_t)sx;
         tv.hist_sy = (int32_t)sy;
         tv.hist_inc_x = (float)fw / (float)tv.hist_sx;

@@ -26,6 +26,7 @@
 //                                     after the reference's own skipping of
 //                                     spaces, tabs and separators
 // Host code only (no device work): it feeds rt_scene_upload.
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>

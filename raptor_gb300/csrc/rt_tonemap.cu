@@ -281,29 +281,39 @@ __device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma)
 
 // ---- camera::histogram_tone_map (camera.cc:1843-2062)
 
+// The block bounds of camera.cc:1856-1880 as the reference's running sums
+// produce them (x1 = min(w - 1, x1 + inc), x0 = the previous x1): thread 0
+// the columns, thread 1 the rows, into bx (2 * hist_sx floats) and by.
+__global__ void k_hist_bounds(int32_t fw, int32_t fh, ToneView t, float *__restrict__ bx, float *__restrict__ by)
+{
+    const bool cols = threadIdx.x == 0;
+    if (threadIdx.x > 1) return;
+    const int n = cols ? t.hist_sx : t.hist_sy;
+    const float inc = cols ? t.hist_inc_x : t.hist_inc_y;
+    const float vmax = xsub((float)(cols ? fw : fh), 1.0f);
+    float *out = cols ? bx : by;
+    float v0 = 0.0f, v1 = inc;
+    for (int q = 0; q < n; ++q) {
+        out[2 * q] = v0;
+        out[2 * q + 1] = v1;
+        v0 = v1;
+        const float nv = xadd(v1, inc);
+        v1 = (nv < vmax) ? nv : vmax;   // std::min(res - 1, v1 + inc)
+    }
+}
+
 // The frame's luminance averaged over one block per degree of view
 // (camera.cc:1856-1880): block (i, j) sums the samples of rows
-// int(y0)..int(y1) and columns int(x0)..int(x1) in that order, where the
-// bounds follow the reference's running sums (x1 = min(w - 1, x1 + inc)).
-// One thread per block.
+// int(y0)..int(y1) and columns int(x0)..int(x1) in that order.  One thread
+// per block.
 __global__ void __launch_bounds__(kToneThreads) k_hist_blocks(const float *__restrict__ fimg, int32_t fw, int32_t fh,
-                                                              ToneView t, float *__restrict__ blocks)
+                                                              ToneView t, const float *__restrict__ bx,
+                                                              const float *__restrict__ by, float *__restrict__ blocks)
 {
     const int64_t nb = (int64_t)t.hist_sx * t.hist_sy;
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(b % t.hist_sx), j = (int)(b / t.hist_sx);
-        float x0 = 0.0f, x1 = t.hist_inc_x, y0 = 0.0f, y1 = t.hist_inc_y;
-        const float xmax = xsub((float)fw, 1.0f), ymax = xsub((float)fh, 1.0f);
-        for (int q = 0; q < i; ++q) {
-            x0 = x1;
-            const float nx = xadd(x1, t.hist_inc_x);
-            x1 = (nx < xmax) ? nx : xmax;   // std::min(x_res - 1, x1 + inc)
-        }
-        for (int q = 0; q < j; ++q) {
-            y0 = y1;
-            const float ny = xadd(y1, t.hist_inc_y);
-            y1 = (ny < ymax) ? ny : ymax;
-        }
+        const float x0 = bx[2 * i], x1 = bx[2 * i + 1], y0 = by[2 * j], y1 = by[2 * j + 1];
         float acc = 0.0f;
         for (int y = (int)y0; y <= (int)y1; ++y)
             for (int x = (int)x0; x <= (int)x1; ++x) {
@@ -1007,7 +1017,8 @@ size_t tone_scratch_bytes(int64_t n, int64_t blocks)
     const int64_t ncoarse = (nchunks + kCoarse - 1) / kCoarse;
     return (size_t)nchunks * kSumChunk * sizeof(float) + (size_t)(nchunks + ncoarse) * 32 * sizeof(ChunkSum) +
            (size_t)n * sizeof(int32_t) +   // redo queue (at most one entry per output pixel)
-           (size_t)blocks * sizeof(float);  // histogram modes: the per-degree luminance blocks
+           (size_t)blocks * sizeof(float) +  // histogram modes: the per-degree luminance blocks
+           (size_t)2 * 2 * 4096 * sizeof(float);   // and their bounds (at most 4096 per axis)
 }
 
 void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
@@ -1033,7 +1044,9 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
         k_tone_sum<<<1, 32, 0, st>>>(terms, rec, crec, nchunks, ncoarse, e_lo, t, acc, true);
         if (t.mode == RT_TONE_LOCAL_HISTOGRAM || t.mode == RT_TONE_LOCAL_HUMAN_HISTOGRAM) {
             const int64_t nb = (int64_t)t.hist_sx * t.hist_sy;
-            k_hist_blocks<<<blocks_for(nb, sm_count), kToneThreads, 0, st>>>(fimg, fw, fh, t, hblocks);
+            float *bx = hblocks + nb, *by = bx + 2 * 4096;
+            k_hist_bounds<<<1, 32, 0, st>>>(fw, fh, t, bx, by);
+            k_hist_blocks<<<blocks_for(nb, sm_count), kToneThreads, 0, st>>>(fimg, fw, fh, t, bx, by, hblocks);
             k_hist_main<<<1, 128, 0, st>>>(hblocks, t, acc);
         }
         if (t.stretch) k_tone_range<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(fimg, n, t, acc);
