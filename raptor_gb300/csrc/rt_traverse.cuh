@@ -554,9 +554,12 @@ __device__ __forceinline__ void phong_add(const LightView &L, const MaterialView
     const float d_scale = xadd(xmul(dist, dist), 1.0f);
     float3 I;
     if (L.s_b != 0.0f) {
-        // spot light: intensity by the angle off its axis (light.h:49-55)
+        // spot light: intensity by the angle off its axis (light.h:49-55);
+        // the angle always in double, rounded once: divided by a narrow
+        // cone width, a few ulp of acosf would not stay within the
+        // truncation guard
         const float cosa = xdot(ldir, L.dir);
-        const float a = EXACT ? (float)acos((double)cosa) : acosf(cosa);
+        const float a = (float)acos((double)cosa);
         const float p = xdiv(xsub(a, L.s_a), xsub(L.s_b, L.s_a));
         const float q = xsub(1.0f, p);
         const float f = (0.0f < ((q < 1.0f) ? q : 1.0f)) ? ((q < 1.0f) ? q : 1.0f) : 0.0f;   // max(0, min(1, q))

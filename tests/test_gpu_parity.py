@@ -931,8 +931,8 @@ def test_ingested_scene_renders_as_reference_on_gpu(rtlib, ctx, oracle, golden, 
 
 @pytest.mark.parametrize("k", [0, 1, 2])
 def test_spot_lights_vs_reference_and_oracle(rtlib, ctx, oracle, golden, k):
-    """RT_LIGHT_SPOT through rt_render (fused kernel: single-precision acos
-    and power with the exact re-shade near truncation), rt_render_materials
+    """RT_LIGHT_SPOT through rt_render (fused kernel: single-precision
+    power with the exact re-shade near truncation), rt_render_materials
     (ray-tree kernel, exact) and the batched form: the reference's frames."""
     from raptor_gb300 import scenes
     frame = json.loads(golden[f"spot{k}_frame"].tobytes().decode())
@@ -944,3 +944,21 @@ def test_spot_lights_vs_reference_and_oracle(rtlib, ctx, oracle, golden, k):
             within1, exact, _ = pixel_agreement(got, other)
             assert exact >= 0.998, (exact, within1)
     sc.close()
+
+
+def test_narrow_spot_cone_vs_oracle(rtlib, ctx, oracle, golden):
+    """Spot cones 0.003 rad wide between full and no intensity: the angle
+    off the axis, divided by that width, is taken in double on every path,
+    so the fused kernel's frame still equals the oracle's."""
+    from raptor_gb300 import scenes
+    frame = json.loads(golden["spot0_frame"].tobytes().decode())
+    frame["lights"] = [dict(l, s_b=l["s_a"] + 0.003) if l["kind"] == 2 else l for l in frame["lights"]]
+    cam = dict(frame["camera"], xres=384, yres=384)
+    frame["camera"] = cam
+    s, _ = scenes.icosphere_scene(freq=8, seed=0, res=64)
+    sc = rtlib.Scene(ctx, s)
+    want = oracle.OracleScene(s).render(frame)["rgb"]
+    got = sc.render(frame)["rgb"]
+    sc.close()
+    within1, exact, _ = pixel_agreement(got, want)
+    assert exact >= 0.998, (exact, within1)
