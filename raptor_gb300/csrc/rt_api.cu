@@ -993,8 +993,14 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
     for (int i = 0; i < nmaterials; ++i) mt.m[i] = make_material_view(materials[i]);
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
-    launch_render_tree(scene_view(s), make_camera_view(fine), ls, mt, nullptr, (float *)ctx->fimg.ptr, nullptr,
-                       ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    bool secondary = false;
+    for (int i = 0; i < nmaterials; ++i) secondary = secondary || materials[i].rf > 0.0f || materials[i].tran > 0.0f;
+    if (secondary)
+        launch_render_tree(scene_view(s), make_camera_view(fine), ls, mt, nullptr, (float *)ctx->fimg.ptr, nullptr,
+                           ctx->d_counters, ctx->sm_count, ctx->stream, ctx->count_fetches);
+    else
+        launch_render_float(scene_view(s), make_camera_view(fine), ls, mt, (float *)ctx->fimg.ptr, ctx->d_counters,
+                            ctx->sm_count, ctx->stream, ctx->count_fetches);
     RT_CUDA(cudaGetLastError(), "render launch");
     launch_tone_map((const float *)ctx->fimg.ptr, fine.xres, fine.yres, aa_x, aa_y, tv, o.rgb, (ToneAcc *)ctx->tone.ptr,
                     (char *)ctx->tone.ptr + kToneScratch, ctx->sm_count, ctx->stream);

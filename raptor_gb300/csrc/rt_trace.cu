@@ -89,6 +89,47 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render(
     if (status) atomicOr(&ctr->status, status);
 }
 
+// The unclipped colour (3 floats per pixel, exact specular power) of a
+// frame without secondary rays, for the tone-mapping epilogue: the fused
+// primary + shadow kernel, its material per triangle from `table` (entry 0
+// when the scene has no indices).
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_float(SceneView sc, CameraView cam, LightSet lights,
+                                                          MaterialTable table, float *__restrict__ fimg,
+                                                          Counters *ctr)
+{
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
+    uint32_t status = 0;
+    FetchCount fc;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items) break;
+        int x, y;
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
+        const bool live = (x < cam.xres) && (y < cam.yres);
+        PixelOut po;
+        po.hit = false;
+        po.secondary = 0;
+        if (live) {
+            po = shade_pixel_lights<COUNT, true>(sc, cam, lights.l, lights.n, table.m[0], x, y, status, &fc, false,
+                                                 &table);
+            const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+            fimg[3 * pix] = po.c.x;
+            fimg[3 * pix + 1] = po.c.y;
+            fimg[3 * pix + 2] = po.c.z;
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
+    }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
 // k_render with the hit triangle's material taken from a table
 // (rt_render_materials without mirror or refracted rays): a separate kernel
 // so that the single-material one keeps its code and parameter block.
@@ -442,6 +483,16 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
         k_render<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
     else
         k_render<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
+}
+
+void launch_render_float(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
+                         float *fimg, Counters *ctr, int sm_count, cudaStream_t st, bool count)
+{
+    static const int grid = grid_of(k_render_float<false>, sm_count);
+    if (count)
+        k_render_float<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, fimg, ctr);
+    else
+        k_render_float<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, fimg, ctr);
 }
 
 void launch_render_table(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
