@@ -547,34 +547,42 @@ __global__ void __launch_bounds__(kSumThreads) k_tone_terms(const float *__restr
         }
         terms[i] = a[t];   // the padding of the last chunk holds +0
     }
+    // Per binade ei: the warp's sums of the positive and negative rounded
+    // increments (one redux each) and its tie flags (bit ei, one redux for
+    // all 32); lane ei keeps binade ei's sums.  A lane's own sums (4 terms of
+    // |q| <= 2^26) fit in int32; each is clamped to +-2^25 before the warp
+    // sum, so that sum stays below 2^30 and is exact unless some lane was
+    // clamped, in which case it is >= 2^25 in magnitude: a record that large
+    // never applies, whatever its exact value.
     const int lane = threadIdx.x & 31;
+    int32_t my_pos = 0, my_neg = 0;
+    uint32_t ties = 0;
     for (int ei = 0; ei < 32; ++ei) {
-        long long pos = 0, neg = 0;
-        int32_t tie = 0;
+        int32_t pos = 0, neg = 0;
 #pragma unroll
         for (int t = 0; t < kSumPerThread; ++t) {
             const float k = ldexpf(a[t], 23 - (e_lo + ei));   // exact: a power-of-two scale
-            long long q;
+            int32_t q;
             if (fabsf(k) < 33554432.0f) {                      // |k| < 2^25
                 q = __float2int_rn(k);                         // round to nearest, ties to even
-                tie |= (xsub(k, floorf(k)) == 0.5f) ? 1 : 0;
+                if (xsub(k, floorf(k)) == 0.5f) ties |= 1u << ei;
             } else {
-                q = (k > 0.0f) ? (1ll << 26) : -(1ll << 26);   // too large to apply: saturates the sums
+                q = (k > 0.0f) ? (1 << 26) : -(1 << 26);       // too large to apply: saturates the sums
             }
             if (q > 0) pos += q;
             else neg += q;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            pos += __shfl_xor_sync(0xffffffffu, pos, o);
-            neg += __shfl_xor_sync(0xffffffffu, neg, o);
-            tie |= __shfl_xor_sync(0xffffffffu, tie, o);
-        }
-        if (lane == 0) {
-            atomicAdd((unsigned long long *)&s_pos[ei], (unsigned long long)pos);
-            atomicAdd((unsigned long long *)&s_neg[ei], (unsigned long long)neg);
-            atomicOr(&s_tie[ei], tie);
+        const int32_t wpos = __reduce_add_sync(0xffffffffu, min(pos, 1 << 25));
+        const int32_t wneg = __reduce_add_sync(0xffffffffu, max(neg, -(1 << 25)));
+        if (lane == ei) {
+            my_pos = wpos;
+            my_neg = wneg;
         }
     }
+    ties = __reduce_or_sync(0xffffffffu, ties);
+    atomicAdd((unsigned long long *)&s_pos[lane], (unsigned long long)(long long)my_pos);
+    atomicAdd((unsigned long long *)&s_neg[lane], (unsigned long long)(long long)my_neg);
+    if ((ties >> lane) & 1u) atomicOr(&s_tie[lane], 1);
     for (int o = 16; o > 0; o >>= 1) {
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         maxb = max(maxb, __shfl_xor_sync(0xffffffffu, maxb, o));
