@@ -18,7 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "librtoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libraptor_ref.so")
-REF_SRC = "/root/reference/RAPTor"
+# RAPTor source tree (the directory holding common/ and raytracer/); the
+# RAPTOR_REF environment variable overrides the default checkout location.
+REF_SRC = os.environ.get("RAPTOR_REF", "/root/reference/RAPTor")
 
 
 class Camera(C.Structure):
@@ -212,6 +214,10 @@ def oracle_lib():
                                         C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _U8, _I, _I]
         lib["ro_ao_rays"].argtypes = [_F, _F, C.c_uint32, C.c_int32, C.c_uint32, _F, _F]
         lib["ro_philox4x32"].argtypes = [_U32, C.c_uint32, C.c_uint32, _U32]
+        lib["ro_pixel_secondary_rays"].restype = C.c_int32
+        lib["ro_pixel_secondary_rays"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
+                                                   C.c_int32, C.c_float, C.c_uint32, C.c_int32, C.c_int32, _I, _F,
+                                                   _F, _F]
         _oracle = lib
     return _oracle
 
@@ -287,6 +293,27 @@ class OracleScene(_SceneBase):
 
     def node_count(self):
         return self.lib["ro_scene_node_count"](self.h)
+
+    def pixel_secondary_rays(self, frame, x, y):
+        """(primary hit id, ogn, dir, tmax) of the secondary rays pixel
+        (x, y) of the frame spawns: its AO rays for an AO frame, else one
+        shadow ray per light (ro_pixel_secondary_rays)."""
+        cam = make_camera(frame["camera"])
+        ao = frame.get("ao")
+        lights = frame.get("lights") or []
+        ls = make_lights(lights)
+        n_max = max(1, ao["samples"] if ao else len(lights))
+        ogn = np.zeros((n_max, 3), np.float32)
+        dirs = np.zeros((n_max, 3), np.float32)
+        tmax = np.zeros(n_max, np.float32)
+        hid = np.zeros(1, np.int32)
+        n = self.lib["ro_pixel_secondary_rays"](self.h, C.byref(cam), ls, 0 if ao else len(lights),
+                                                ao["samples"] if ao else 0, ao["dist"] if ao else 0.0,
+                                                ao["seed"] if ao else 0, int(x), int(y), _p(hid, C.c_int32),
+                                                _p(ogn, C.c_float), _p(dirs, C.c_float), _p(tmax, C.c_float))
+        if n < 0:
+            raise ValueError("bad pixel or frame")
+        return int(hid[0]), ogn[:n], dirs[:n], tmax[:n]
 
     def render(self, frame, rows=None, threads=1, want_ids=False, want_float=False, want_occl=False):
         cam = make_camera(frame["camera"])

@@ -865,6 +865,41 @@ int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material 
     return run_render(&J, nthreads);
 }
 
+int32_t ro_pixel_secondary_rays(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                                int32_t ao_n, float ao_dist, uint32_t ao_seed, int32_t x, int32_t y,
+                                int32_t *hit_id, float *ogn, float *dir, float *tmax)
+{
+    if (!s || !s->nodes || !cam || !hit_id || !ogn || !dir || !tmax || x < 0 || y < 0 || x >= cam->xres ||
+        y >= cam->yres || ao_n < 0 || ao_n > 64 || nlights < 0 || nlights > 64 || (nlights > 0 && !lights))
+        return -1;
+    const cam_state cs = cam_setup(cam);
+    const ro_ray r = cam_ray(&cs, x, y);
+    ro_hit h;
+    const int32_t id = closest(s, &r, &h);
+    *hit_id = id;
+    if (!(h.d < RO_MAX_DIST)) return 0;
+    v3 dst, sn, geo, vt;
+    int out_in;
+    hit_setup(s, &r, id, &h, &dst, &sn, &geo, &vt, &out_in);
+    if (ao_n > 0) {
+        const float hp[3] = {dst.x, dst.y, dst.z}, gn[3] = {geo.x, geo.y, geo.z};
+        const size_t pix = (size_t)x + (size_t)y * (size_t)cam->xres;
+        ro_ao_rays(hp, gn, (uint32_t)pix, ao_n, ao_seed, ogn, dir);
+        for (int32_t k = 0; k < ao_n; ++k) tmax[k] = ao_dist;
+        return ao_n;
+    }
+    const v3 start = offset_start(dst, geo);
+    for (int32_t l = 0; l < nlights; ++l) {
+        ro_ray sr;
+        float len;
+        shadow_ray(&lights[l], start, &sr, &len);
+        ogn[3 * l] = sr.o.x; ogn[3 * l + 1] = sr.o.y; ogn[3 * l + 2] = sr.o.z;
+        dir[3 * l] = sr.d.x; dir[3 * l + 1] = sr.d.y; dir[3 * l + 2] = sr.d.z;
+        tmax[l] = len;
+    }
+    return nlights;
+}
+
 /* ------------------------------------------------------- AO ray sampler */
 
 /* Philox4x32-10 from Salmon, Moraes, Dror and Shaw, "Parallel random numbers:

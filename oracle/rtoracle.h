@@ -140,6 +140,18 @@ int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material 
                      int32_t nsamples, float ao_dist, uint32_t seed, int32_t row0, int32_t row1,
                      int32_t nthreads, uint8_t *rgb, int32_t *hit_id, int32_t *ao_count);
 
+/* The secondary rays the camera ray of pixel (x, y) spawns, exactly as the
+ * renders above trace them: with ao_n > 0 the ao_n rays of ro_ao_rays
+ * (tmax = ao_dist), else one shadow ray per light (raytracer.cc:44-64,
+ * light.h:62-100; tmax = the distance to the light).  hit_id receives the
+ * primary hit (-1: miss, no rays).  ogn / dir hold 3 floats per ray and tmax
+ * one, room for max(ao_n, nlights) rays.  Returns the number of rays, or -1
+ * on bad arguments.  Lets a test re-trace exactly the rays on which two
+ * renders disagree. */
+int32_t ro_pixel_secondary_rays(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                                int32_t ao_n, float ao_dist, uint32_t ao_seed, int32_t x, int32_t y,
+                                int32_t *hit_id, float *ogn, float *dir, float *tmax);
+
 /* The AO ray set for one hit (exposed so tests can trace single rays). */
 void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pixel, int32_t nsamples,
                 uint32_t seed, float *ogn, float *dir);

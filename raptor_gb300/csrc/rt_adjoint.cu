@@ -242,15 +242,17 @@ struct Guard {
     }
 };
 
+// Resident blocks per SM of a kernel (asked once per kernel; the grid is
+// this times the calling context's SM count).
 template <typename K>
-int grid_of(K kernel, int sm_count)
+int blocks_per_sm(K kernel)
 {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 4;
     }
-    return sm_count * per_sm;
+    return per_sm;
 }
 
 rt_status check_frame(rt_scene *s, const rt_camera *cam, const rt_light *lights, int32_t nl, const rt_material *m)
@@ -322,7 +324,8 @@ rt_status rt_render_float(rt_scene *s, const rt_camera *camera, const rt_light *
     ls.n = nlights;
     ls.fast_pow = 0;
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
-    static const int grid = grid_of(k_diff<false>, ctx->sm_count);
+    static const int per_sm = blocks_per_sm(k_diff<false>);
+    const int grid = per_sm * ctx->sm_count;
     RT_CUDA_A(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA_A(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
     k_diff<false><<<grid, kTraceThreads, 0, ctx->stream>>>(scene_view(s), s->d_verts, make_camera_view(*camera), ls,
@@ -348,7 +351,8 @@ rt_status rt_render_adjoint(rt_scene *s, const rt_camera *camera, const rt_light
     ls.n = nlights;
     ls.fast_pow = 0;
     for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
-    static const int grid = grid_of(k_diff<true>, ctx->sm_count);
+    static const int per_sm = blocks_per_sm(k_diff<true>);
+    const int grid = per_sm * ctx->sm_count;
     const size_t gbytes = (size_t)(s->nverts > 0 ? s->nverts : 1) * 3 * sizeof(float);
     RT_CUDA_A(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA_A(cudaEventRecord(ctx->ev0, ctx->stream), "event record");

@@ -248,6 +248,7 @@ rt_status rt_ctx_create(int32_t device, rt_context **out)
     RT_CUDA(cudaMallocHost(&c->h_scratch, 64 * sizeof(int32_t)), "pinned scratch allocation");
     RT_CUDA(cudaEventCreate(&c->ev0), "event create");
     RT_CUDA(cudaEventCreate(&c->ev1), "event create");
+    noalloc_context_opened(device);
     *out = c;
     return RT_OK;
 }
@@ -267,6 +268,7 @@ rt_status rt_ctx_destroy(rt_context *ctx)
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    noalloc_context_closed(ctx->device);
     delete ctx;
     return RT_OK;
 }

@@ -26,6 +26,12 @@ rt_status set_error(rt_status code, const char *msg);
 rt_status set_cuda_error(cudaError_t e, const char *what);
 rt_status status_to_error(uint32_t st);
 
+// Live contexts per device, kept for the allocation-free entry point: its
+// cached scratch address on a device is forgotten when the last context on
+// that device is destroyed (a device reset in between may move the module).
+void noalloc_context_opened(int device);
+void noalloc_context_closed(int device);
+
 }  // namespace rtc
 
 struct rt_context {

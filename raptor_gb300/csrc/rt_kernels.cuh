@@ -82,10 +82,10 @@ void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_
                       cudaStream_t st);
 void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                    uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
-// k_render with per-triangle materials from a table (no secondary rays).
 // Float frame (3 floats per pixel, exact) of a frame without secondary rays.
 void launch_render_float(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
                          float *fimg, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
+// k_render with per-triangle materials from a table (no secondary rays).
 void launch_render_table(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
                          uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count = false);
 void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,

@@ -15,7 +15,10 @@
 // name is only a host-side stand-in for the symbol; the device address is
 // looked up once per device with cudaGetSymbolAddress (on the first call that
 // runs on that device, which should therefore come before any stream
-// capture) and passed to the copies and the kernel as a plain pointer.
+// capture) and passed to the copies and the kernel as a plain pointer.  The
+// cached address is dropped when the last context on the device is
+// destroyed, so a device reset between contexts (which may load the module
+// at a new address) is followed by a fresh lookup.
 //
 // Every call shares the array and leaves its contents behind; the counters
 // the kernel needs at zero are cleared by each call.  Calls that overlap on
@@ -43,6 +46,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 unsigned char *g_scratch_ptr[kMaxDevices] = {};
+int g_live_contexts[kMaxDevices] = {};
 
 // Device address of the scratch array on `device` (which must be current).
 rt_status scratch_on(int device, unsigned char **out)
@@ -66,6 +70,21 @@ rt_status cuda_check(cudaError_t e, const char *what)
 }
 
 }  // namespace
+
+void noalloc_context_opened(int device)
+{
+    if (device < 0 || device >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    ++g_live_contexts[device];
+}
+
+void noalloc_context_closed(int device)
+{
+    if (device < 0 || device >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_live_contexts[device] > 0 && --g_live_contexts[device] == 0) g_scratch_ptr[device] = nullptr;
+}
+
 }  // namespace rtc
 
 using namespace rtc;

@@ -449,36 +449,41 @@ __global__ void k_index_range(const int32_t *__restrict__ v, int32_t n, int32_t 
 
 }  // namespace
 
-// Persistent grid: SMs x resident blocks per SM (from the occupancy API).
+// Persistent grid: the context's SMs x resident blocks per SM.  The
+// occupancy is a property of the kernel alone, so each launcher asks the
+// occupancy API once and scales it by the SM count of the calling context.
 template <typename K>
-static int grid_of(K kernel, int sm_count)
+static int blocks_per_sm(K kernel)
 {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 4;
     }
-    return sm_count * per_sm;
+    return per_sm;
 }
 
 void launch_trace_closest(const SceneView &sc, const rt_ray *rays, int32_t n, rt_hit *hits, Counters *ctr, int sm_count,
                           cudaStream_t st)
 {
-    static const int grid = grid_of(k_trace_closest, sm_count);
+    static const int per_sm = blocks_per_sm(k_trace_closest);
+    const int grid = per_sm * sm_count;
     k_trace_closest<<<grid, kTraceThreads, 0, st>>>(sc, rays, n, hits, ctr);
 }
 
 void launch_trace_any(const SceneView &sc, const rt_ray *rays, int32_t n, uint8_t *occ, Counters *ctr, int sm_count,
                       cudaStream_t st)
 {
-    static const int grid = grid_of(k_trace_any, sm_count);
+    static const int per_sm = blocks_per_sm(k_trace_any);
+    const int grid = per_sm * sm_count;
     k_trace_any<<<grid, kTraceThreads, 0, st>>>(sc, rays, n, occ, ctr);
 }
 
 void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                    uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, rgb, ids, ctr);
     else
@@ -488,7 +493,8 @@ void launch_render(const SceneView &sc, const CameraView &cam, const LightSet &l
 void launch_render_float(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
                          float *fimg, Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_float<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_float<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render_float<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, fimg, ctr);
     else
@@ -498,7 +504,8 @@ void launch_render_float(const SceneView &sc, const CameraView &cam, const Light
 void launch_render_table(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialTable &mt,
                          uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_table<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_table<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render_table<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt.m[0], rgb, ids, ctr, mt);
     else
@@ -509,7 +516,8 @@ void launch_render_tree(const SceneView &sc, const CameraView &cam, const LightS
                         uint8_t *rgb, float *fimg, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st,
                         bool count)
 {
-    static const int grid = grid_of(k_render_tree<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_tree<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render_tree<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mt, rgb, fimg, ids, ctr);
     else
@@ -528,7 +536,8 @@ void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet
                       int32_t aa_x, int32_t aa_y, int32_t out_x, int32_t out_y, uint8_t *rgb, int32_t *redo,
                       Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_aa<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_aa<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render_aa<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, redo,
                                                            ctr);
@@ -543,7 +552,8 @@ void launch_render_ao(const SceneView &sc, const CameraView &cam, const Material
                       float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
                       int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_ao<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_ao<false>);
+    const int grid = per_sm * sm_count;
     if (count)
         k_render_ao<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, mat, samples, ao_dist, seed, rgb, ids, ao_count, ctr);
     else

@@ -14,15 +14,17 @@ __global__ void __launch_bounds__(kTraceThreads, RT_WAVE_MIN_BLOCKS) k_render_wa
     wave_loop<8, COUNT>(&job, nullptr, 1, job.items_end, shade_state[threadIdx.x], ctr);
 }
 
+// Resident blocks per SM of a kernel (asked once per kernel; the grid is
+// this times the calling context's SM count).
 template <typename K>
-int grid_of(K kernel, int sm_count)
+int blocks_per_sm(K kernel)
 {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 4;
     }
-    return sm_count * per_sm;
+    return per_sm;
 }
 
 FrameJob single_job(const SceneView &sc, const CameraView &cam, const MaterialView &mat, uint8_t *rgb, int32_t *ids)
@@ -46,7 +48,8 @@ FrameJob single_job(const SceneView &sc, const CameraView &cam, const MaterialVi
 void launch_render_wave(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,
                         uint8_t *rgb, int32_t *ids, Counters *ctr, int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_wave<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_wave<false>);
+    const int grid = per_sm * sm_count;
     FrameJob J = single_job(sc, cam, mat, rgb, ids);
     J.mode = RT_JOB_SHADOW;
     J.nlights = lights.n;
@@ -62,7 +65,8 @@ void launch_render_ao_wave(const SceneView &sc, const CameraView &cam, const Mat
                            float ao_dist, uint32_t seed, uint8_t *rgb, int32_t *ids, int32_t *ao_count, Counters *ctr,
                            int sm_count, cudaStream_t st, bool count)
 {
-    static const int grid = grid_of(k_render_wave<false>, sm_count);
+    static const int per_sm = blocks_per_sm(k_render_wave<false>);
+    const int grid = per_sm * sm_count;
     FrameJob J = single_job(sc, cam, mat, rgb, ids);
     J.mode = RT_JOB_AO;
     J.ao_samples = samples;

@@ -280,7 +280,7 @@ def mesh_files():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/RAPTor")
+    ap.add_argument("--ref", default=os.environ.get("RAPTOR_REF", "/root/reference/RAPTor"))
     a = ap.parse_args()
     kats = parse_bih_tests(os.path.join(a.ref, "raytracer/unit_tests/bih_tests.cc"))
     json.dump(kats, open(os.path.join(HERE, "bih_kats.json"), "w"), indent=1)

@@ -110,3 +110,79 @@ def frame_tone_cases():
     import os
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_small.npz"))
     return [(k, t, tuple(aa)) for k, (t, aa) in enumerate(json.loads(g["ftone_cases"].tobytes().decode()))]
+
+
+EPSILON = 1e-3          # the reference's EPSILON: hits at t <= EPSILON are ignored
+DET_MIN = 1e-6          # |det| below which triangle::is_intersecting rejects
+
+
+class OcclusionJudge:
+    """FP64 brute-force classification of any-hit rays against every
+    triangle of a scene, for explaining occlusion differences ray by ray.
+
+    A triangle blocks a ray when the reference's test accepts it:
+    barycentrics inside, t in (EPSILON, tmax), |det| >= 1e-6, and the
+    triangle not flagged light or transparent (bvh_node.h:170-190).  In
+    FP64 a hit is *robust* when all three barycentrics exceed EDGE_EPS,
+    t lies more than 1e-5 relative inside (EPSILON, tmax) and |det| is more
+    than 0.1 % away from 1e-6; it is *fragile* when it fails one of those
+    margins but not by more than the margin.  classify() returns per ray
+    1 (a robust blocker exists: occluded), 0 (no blocker, robust or
+    fragile: free) or 2 (only fragile blockers: either answer is
+    legitimate in binary32)."""
+
+    def __init__(self, verts, tris, flags=None):
+        v = np.asarray(verts, np.float64)
+        t = np.asarray(tris, np.int64)
+        keep = np.ones(t.shape[0], bool) if flags is None else (np.asarray(flags) & 3) == 0
+        t = t[keep]
+        a, b, c = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+        self.a, self.e1, self.e2 = a, c - a, b - a
+        self.lo = np.minimum(np.minimum(a, b), c)
+        self.hi = np.maximum(np.maximum(a, b), c)
+
+    def _candidates(self, o, d, tmax):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            inv = 1.0 / d
+            t0 = (self.lo - o) * inv
+            t1 = (self.hi - o) * inv
+        # axis-parallel rays: inside the slab on that axis or not at all
+        par = d == 0.0
+        if par.any():
+            inside = (self.lo[:, par] <= o[par]) & (o[par] <= self.hi[:, par])
+            t0[:, par] = np.where(inside, -np.inf, np.inf)
+            t1[:, par] = np.where(inside, np.inf, -np.inf)
+        tn = np.minimum(t0, t1).max(1)
+        tf = np.maximum(t0, t1).min(1)
+        slack = 1e-6 * max(1.0, float(tmax))
+        return np.nonzero((tn <= tf + slack) & (tf >= -slack) & (tn <= tmax * (1 + 1e-5) + slack))[0]
+
+    def classify(self, ogn, dirs, tmax):
+        ogn = np.asarray(ogn, np.float64).reshape(-1, 3)
+        dirs = np.asarray(dirs, np.float64).reshape(-1, 3)
+        tmax = np.broadcast_to(np.asarray(tmax, np.float64), (ogn.shape[0],))
+        out = np.zeros(ogn.shape[0], np.int8)
+        for i in range(ogn.shape[0]):
+            o, d, tm = ogn[i], dirs[i], float(tmax[i])
+            k = self._candidates(o, d, tm)
+            if k.size == 0:
+                continue
+            e1, e2, a = self.e1[k], self.e2[k], self.a[k]
+            P = np.cross(d, e2)
+            det = (e1 * P).sum(1)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                T = o - a
+                u = (T * P).sum(1) / det
+                Q = np.cross(T, e1)
+                v = (Q @ d) / det
+                t = (e2 * Q).sum(1) / det
+            w = 1.0 - u - v
+            bary = np.minimum(np.minimum(u, v), w)
+            ad = np.abs(det)
+            ok = np.isfinite(t) & np.isfinite(bary)
+            robust = ok & (bary > EDGE_EPS) & (t > EPSILON * (1 + T_REL)) & (t < tm * (1 - T_REL)) & \
+                (ad > DET_MIN * 1.001)
+            maybe = ok & (bary > -EDGE_EPS) & (t > EPSILON * (1 - T_REL)) & (t < tm * (1 + T_REL)) & \
+                (ad > DET_MIN * 0.999)
+            out[i] = 1 if robust.any() else (2 if maybe.any() else 0)
+        return out

@@ -10,7 +10,7 @@ import pytest
 
 from conftest import ROOT
 
-REF = "/root/reference/RAPTor"
+REF = os.environ.get("RAPTOR_REF", "/root/reference/RAPTor")
 
 TU = r'''
 #include "raptor_gpu_bvh.h"

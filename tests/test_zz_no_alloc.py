@@ -30,9 +30,11 @@ def noalloc(rtlib, sc, rays, out):
 
 
 def same_hits(a, b):
+    """Both entry points run the same traversal kernel on the same rays, so
+    the hits agree bit for bit."""
     assert np.array_equal(a["tri"], b["tri"])
     for k in ("t", "u", "v"):
-        np.testing.assert_allclose(a[k], b[k], rtol=1e-5, atol=1e-6)
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
 
 
 def test_noalloc_matches_trace_closest(rtlib):
@@ -56,6 +58,23 @@ def test_noalloc_matches_trace_closest(rtlib):
     c.close()
 
 
+def test_noalloc_after_context_recreated(rtlib):
+    """The scratch address is looked up again after the last context on the
+    device is closed; a new context's calls still match rt_trace_closest."""
+    rng = np.random.default_rng(23)
+    scene, o, d = scene_and_rays(rng, 4096)
+    rays = rtlib.rays_array(o, d)
+    for _ in range(2):
+        c = rtlib.Context(0)
+        sc = rtlib.Scene(c, scene)
+        want = sc.closest(rays)
+        got = np.zeros(rays.shape[0], rtlib.HIT_DTYPE)
+        assert noalloc(rtlib, sc, rays, got) == 0
+        same_hits(got, want)
+        sc.close()
+        c.close()
+
+
 def test_noalloc_device_buffers_and_limit(rtlib):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(22)
@@ -73,15 +92,23 @@ def test_noalloc_device_buffers_and_limit(rtlib):
                                                     C.c_void_p(d_hits.data_ptr())) == 0
         got = d_hits.cpu().numpy().view(rtlib.HIT_DTYPE)
         same_hits(got, want)
-    # repeated calls at the maximum size take no device memory
+    # repeated calls at the maximum size take no device memory.  The free
+    # memory figure is device-wide, so another process allocating at the
+    # same moment could move it: one of three attempts must see it unchanged.
     big = rtlib.rays_array(np.repeat(o, 6, 0)[:MAX_RAYS], np.repeat(d, 6, 0)[:MAX_RAYS])
     out = np.zeros(MAX_RAYS, rtlib.HIT_DTYPE)
     assert noalloc(rtlib, sc, big, out) == 0
-    torch.cuda.synchronize()
-    free0 = torch.cuda.mem_get_info()[0]
+    unchanged = False
     for _ in range(3):
-        assert noalloc(rtlib, sc, big, out) == 0
-    assert torch.cuda.mem_get_info()[0] == free0
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for _ in range(3):
+            assert noalloc(rtlib, sc, big, out) == 0
+        torch.cuda.synchronize()
+        if torch.cuda.mem_get_info()[0] == free0:
+            unchanged = True
+            break
+    assert unchanged
     # one ray beyond the maximum is refused before any GPU work
     over = rtlib.rays_array(np.zeros((MAX_RAYS + 1, 3), np.float32), np.tile([0, -1, 0], (MAX_RAYS + 1, 1)).astype(np.float32))
     big_out = np.zeros(MAX_RAYS + 1, rtlib.HIT_DTYPE)
