@@ -87,6 +87,10 @@ typedef struct rt_camera {
 #define RT_LIGHT_POINT 0
 #define RT_LIGHT_DIRECTIONAL 1
 #define RT_LIGHT_SPOT 2
+/* OR-ed into kind: rgb is already divided by 255 -- the colour exactly as
+ * the reference's light stores it (light.h:17-34 keep rgb / 255.0f) --
+ * and is used as given. */
+#define RT_LIGHT_UNIT_RGB 0x100
 typedef struct rt_light {
     int32_t kind;
     float rgb[3];
@@ -305,6 +309,18 @@ rt_status rt_scene_set_normals(rt_scene *scene, const float *corner_normals, int
  * materials[0]; rt_render is the one-material case and ignores the
  * per-triangle indices.  Every index set on the scene must be below
  * nmaterials. */
+/* The camera's float image: what ray_tracer() (raytracer.cc:563-598)
+ * stores through camera::set_pixel (camera.h:281-285) before
+ * clip_image_to_rgb or tone_map read it -- the unclipped colour of every
+ * ray of the camera grid given (pass the supersampled grid, xres * x_a_res
+ * by yres * y_a_res, for an anti-aliased camera), 3 floats per sample,
+ * index x + y * xres.  Materials as rt_render_materials (one entry, or a
+ * table indexed per triangle; mirror and refracting materials trace their
+ * ray trees), the specular power evaluated exactly.  rgb_f32 is host or
+ * device memory. */
+rt_status rt_render_image(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                          const rt_material *materials, int32_t nmaterials, float *rgb_f32, rt_render_stats *stats);
+
 rt_status rt_render_materials(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
                               const rt_material *materials, int32_t nmaterials, uint8_t *rgb_out, int32_t *hit_ids,
                               rt_render_stats *stats);
@@ -476,15 +492,18 @@ typedef struct rt_job {
 
 /* Launch shape of the batched kernel, chosen by rt_batch_autotune:
  * threads per block (64/128/256), tiles claimed per queue access (1..16,
- * RT_KERNEL_PIXEL only), tile width (8 -> 8x4 tiles, 16 -> 16x2), kernel
- * (RT_KERNEL_WAVE / RT_KERNEL_PIXEL, see RT_OPT_RENDER_KERNEL) and the
- * measured ms per frame. */
+ * RT_KERNEL_PIXEL only: the queue depth a warp takes at once), tile width
+ * (8 -> 8x4 tiles, 16 -> 16x2), kernel (RT_KERNEL_WAVE / RT_KERNEL_PIXEL,
+ * see RT_OPT_RENDER_KERNEL), the measured ms per frame, and the traversal
+ * stack capacity in node groups (16, 24 or 48, RT_KERNEL_PIXEL only; at
+ * least the depth of the batch's deepest tree). */
 typedef struct rt_tune_config {
     int32_t block_threads;
     int32_t chunk_tiles;
     int32_t tile_w;
     int32_t kernel;
     float ms;
+    int32_t stack_entries;
 } rt_tune_config;
 
 rt_status rt_batch_create(rt_context *ctx, rt_batch **out);

@@ -107,7 +107,7 @@ class RtJob(C.Structure):
 
 class RtTuneConfig(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("chunk_tiles", C.c_int32), ("tile_w", C.c_int32),
-                ("kernel", C.c_int32), ("ms", C.c_float)]
+                ("kernel", C.c_int32), ("ms", C.c_float), ("stack_entries", C.c_int32)]
 
 
 # numpy views of the C structs
@@ -147,6 +147,8 @@ SIGNATURES = [
     ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_free", None, [C.POINTER(RtMesh)]),
+    ("rt_render_image", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
+                                    C.c_int32, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
                                         C.POINTER(RtMaterial), C.c_int32, _P, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_tone_mapped", C.c_int32, [_P, C.POINTER(RtCamera), C.c_int32, C.c_int32, C.POINTER(RtLight),
@@ -492,6 +494,21 @@ class Scene:
                                            C.byref(st)))
         return {"rgb": rgb, "stats": st}
 
+    def render_image(self, frame, aa=(1, 1), fimg=None):
+        """rt_render_image: the camera's float image on the aa-supersampled
+        grid (rows = y), frame["materials"] or frame["material"]; fimg: host
+        array or device tensor, allocated on the host when None."""
+        cam = make_camera(frame["camera"])
+        cam.xres, cam.yres = cam.xres * int(aa[0]), cam.yres * int(aa[1])
+        if fimg is None:
+            fimg = np.empty((cam.yres, cam.xres, 3), np.float32)
+        st = RtRenderStats()
+        ls = make_lights(frame["lights"])
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        _check(lib().rt_render_image(self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table), ptr(fimg),
+                                     C.byref(st)))
+        return {"fimg": fimg, "stats": st}
+
     def render_aa(self, frame, aa_x, aa_y, rgb=None):
         """Anti-aliased frame: aa_x * aa_y rays per output pixel, averaged."""
         cam = make_camera(frame["camera"])
@@ -603,10 +620,11 @@ class Batch:
         cfg = RtTuneConfig()
         _check(lib().rt_batch_autotune(self.h, reps, C.byref(cfg)))
         return {"block_threads": cfg.block_threads, "chunk_tiles": cfg.chunk_tiles, "tile_w": cfg.tile_w,
-                "kernel": "wave" if cfg.kernel == RT_KERNEL_WAVE else "pixel", "ms": cfg.ms}
+                "kernel": "wave" if cfg.kernel == RT_KERNEL_WAVE else "pixel", "ms": cfg.ms,
+                "stack_entries": cfg.stack_entries}
 
-    def set_config(self, block_threads=128, chunk_tiles=1, tile_w=8, kernel=0):
-        cfg = RtTuneConfig(block_threads, chunk_tiles, tile_w, kernel, 0.0)
+    def set_config(self, block_threads=128, chunk_tiles=1, tile_w=8, kernel=0, stack_entries=48):
+        cfg = RtTuneConfig(block_threads, chunk_tiles, tile_w, kernel, 0.0, stack_entries)
         _check(lib().rt_batch_set_config(self.h, C.byref(cfg)))
 
     def close(self):

@@ -265,7 +265,7 @@ rt_status check_frame(rt_scene *s, const rt_camera *cam, const rt_light *lights,
         return set_error(RT_ERR_INVALID_ARG,
                          "reflective or transparent materials (rf, tran > 0) are rendered by rt_render only");
     for (int32_t i = 0; i < nl; ++i)
-        if (lights[i].kind == RT_LIGHT_SPOT && lights[i].s_b != 0.0f)
+        if ((lights[i].kind & ~RT_LIGHT_UNIT_RGB) == RT_LIGHT_SPOT && lights[i].s_b != 0.0f)
             return set_error(RT_ERR_INVALID_ARG, "spot lights are not differentiated (rt_render renders them)");
     if (!s->built) return set_error(RT_ERR_NOT_BUILT, "hierarchy not built");
     return RT_OK;

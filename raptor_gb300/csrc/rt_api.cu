@@ -120,13 +120,16 @@ CameraView make_camera_view(const rt_camera &c)
 LightView make_light_view(const rt_light &l)
 {
     LightView v;
-    v.kind = l.kind;
-    v.rgb255 = make_float3(l.rgb[0] / 255.0f, l.rgb[1] / 255.0f, l.rgb[2] / 255.0f);   // light.h:17-34
+    v.kind = l.kind & ~RT_LIGHT_UNIT_RGB;
+    if (l.kind & RT_LIGHT_UNIT_RGB)
+        v.rgb255 = make_float3(l.rgb[0], l.rgb[1], l.rgb[2]);
+    else
+        v.rgb255 = make_float3(l.rgb[0] / 255.0f, l.rgb[1] / 255.0f, l.rgb[2] / 255.0f);   // light.h:17-34
     v.pos = make_float3(l.pos[0], l.pos[1], l.pos[2]);
     v.dir = make_float3(l.dir[0], l.dir[1], l.dir[2]);
     v.d = l.d;
-    v.s_a = (l.kind == RT_LIGHT_SPOT) ? l.s_a : 0.0f;
-    v.s_b = (l.kind == RT_LIGHT_SPOT) ? l.s_b : 0.0f;
+    v.s_a = (v.kind == RT_LIGHT_SPOT) ? l.s_a : 0.0f;
+    v.s_b = (v.kind == RT_LIGHT_SPOT) ? l.s_b : 0.0f;
     // light::find_major_direction (light.h:172-219)
     const float nx = l.dir[0], ny = l.dir[1], nz = l.dir[2];
     bool neg;
@@ -1009,6 +1012,50 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
     RT_CUDA(cudaGetLastError(), "tone-map launch");
     RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
     return finish_outputs(ctx, npix, rgb_out, nullptr, nullptr, o, stats);
+}
+
+rt_status rt_render_image(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                          const rt_material *materials, int32_t nmaterials, float *rgb_f32, rt_render_stats *stats)
+{
+    if (!s || !materials || !rgb_f32) return fail(RT_ERR_INVALID_ARG, "rt_render_image: NULL argument");
+    rt_status st = check_camera(camera);
+    if (st != RT_OK) return st;
+    st = check_table(s, lights, nlights, materials, nmaterials, "rt_render_image");
+    if (st != RT_OK) return st;
+    rt_context *ctx = s->ctx;
+    DeviceGuard g(ctx->device);
+    const size_t nsamples = (size_t)camera->xres * (size_t)camera->yres;
+    const bool host = !is_device_ptr(rgb_f32);
+    float *dst = rgb_f32;
+    if (host) {
+        RT_CUDA(ctx->fimg.reserve(nsamples * 3 * sizeof(float)), "float frame allocation");
+        dst = (float *)ctx->fimg.ptr;
+    }
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = 0;
+    for (int i = 0; i < nlights; ++i) ls.l[i] = make_light_view(lights[i]);
+    MaterialTable mt;
+    mt.n = nmaterials;
+    for (int i = 0; i < nmaterials; ++i) mt.m[i] = make_material_view(materials[i]);
+    bool secondary = false;
+    for (int i = 0; i < nmaterials; ++i) secondary = secondary || materials[i].rf > 0.0f || materials[i].tran > 0.0f;
+    RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
+    RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
+    if (secondary)
+        launch_render_tree(scene_view(s), make_camera_view(*camera), ls, mt, nullptr, dst, nullptr, ctx->d_counters,
+                           ctx->sm_count, ctx->stream, ctx->count_fetches);
+    else
+        launch_render_float(scene_view(s), make_camera_view(*camera), ls, mt, dst, ctx->d_counters, ctx->sm_count,
+                            ctx->stream, ctx->count_fetches);
+    RT_CUDA(cudaGetLastError(), "render launch");
+    RT_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "event record");
+    if (host)
+        RT_CUDA(cudaMemcpyAsync(rgb_f32, dst, nsamples * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+                "image copy");
+    RenderOut o;
+    o.rgb_host = false;
+    return finish_outputs(ctx, nsamples, nullptr, nullptr, nullptr, o, stats);
 }
 
 rt_status rt_render_materials(rt_scene *s, const rt_camera *camera, const rt_light *lights, int32_t nlights,

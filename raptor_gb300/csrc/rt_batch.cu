@@ -25,7 +25,9 @@ using BatchJob = FrameJob;
 
 namespace {
 
-template <int TW>
+// STACK: traversal stack capacity in node groups, chosen by the autotuner
+// among the capacities that hold the batch's deepest tree.
+template <int TW, int STACK>
 __global__ void __launch_bounds__(256, RT_RENDER_MIN_BLOCKS / 2) k_render_batched(const BatchJob *__restrict__ jobs, int32_t njobs,
                                                         int32_t total_items, int32_t chunk, Counters *ctr)
 {
@@ -51,11 +53,11 @@ __global__ void __launch_bounds__(256, RT_RENDER_MIN_BLOCKS / 2) k_render_batche
             po.secondary = 0;
             if (live) {
                 if (J.mode == RT_JOB_AO)
-                    po = shade_pixel_ao<false>(J.sc, J.cam, J.mat, J.ao_samples, J.ao_dist, J.ao_seed, x, y, status,
-                                               nullptr);
+                    po = shade_pixel_ao<false, STACK>(J.sc, J.cam, J.mat, J.ao_samples, J.ao_dist, J.ao_seed, x, y,
+                                                      status, nullptr);
                 else
-                    po = shade_pixel_lights<false>(J.sc, J.cam, J.lights, J.nlights, J.mat, x, y, status, nullptr,
-                                                   J.fast_pow != 0);
+                    po = shade_pixel_lights<false, false, STACK>(J.sc, J.cam, J.lights, J.nlights, J.mat, x, y,
+                                                                 status, nullptr, J.fast_pow != 0);
                 const size_t pix = (size_t)x + (size_t)y * (size_t)J.cam.xres;
                 store_rgb(J.rgb, pix, po.c);
                 if (J.ids) J.ids[pix] = po.id;
@@ -78,14 +80,19 @@ __global__ void __launch_bounds__(256, RT_WAVE_MIN_BLOCKS / 2) k_render_batched_
     wave_loop<TW, false>(nullptr, jobs, njobs, total_items, wave_state[threadIdx.x], ctr);
 }
 
-template <int TW>
+// Traversal stack capacities the pixel kernel is built for (the wave
+// kernel keeps kStackSize).
+constexpr int kBatchStacks[3] = {16, 24, kStackSize};
+
+template <int TW, int STACK>
 int grid_for(int kernel, int threads, int sm_count)
 {
     int per_sm = 0;
     cudaError_t e = (kernel == RT_KERNEL_WAVE)
                         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched_wave<TW>, threads,
                                                                         threads * sizeof(LaneShade))
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched<TW>, threads, 0);
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_render_batched<TW, STACK>, threads,
+                                                                        0);
     if (e != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
@@ -120,7 +127,7 @@ struct rt_batch {
     BatchJob *d_jobs = nullptr;
     int32_t total_items = 0;
     // launch configuration and its captured graph
-    rt_tune_config cfg{128, 1, 8, RT_KERNEL_PIXEL, 0.f};
+    rt_tune_config cfg{128, 1, 8, RT_KERNEL_PIXEL, 0.f, kStackSize};
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
 };
@@ -170,11 +177,36 @@ void launch_batch(rt_batch *b, cudaStream_t st, int grid)
             k_render_batched_wave<16><<<grid, threads, smem, st>>>(b->d_jobs, nj, b->total_items, b->ctx->d_counters);
         else
             k_render_batched_wave<8><<<grid, threads, smem, st>>>(b->d_jobs, nj, b->total_items, b->ctx->d_counters);
-    } else if (b->cfg.tile_w == 16) {
-        k_render_batched<16><<<grid, threads, 0, st>>>(b->d_jobs, nj, b->total_items, chunk, b->ctx->d_counters);
     } else {
-        k_render_batched<8><<<grid, threads, 0, st>>>(b->d_jobs, nj, b->total_items, chunk, b->ctx->d_counters);
+        Counters *ctr = b->ctx->d_counters;
+        const int stack = b->cfg.stack_entries;
+#define RT_BATCH_PIXEL(TW, S) k_render_batched<TW, S><<<grid, threads, 0, st>>>(b->d_jobs, nj, b->total_items, chunk, ctr)
+        if (b->cfg.tile_w == 16) {
+            if (stack == kBatchStacks[0]) RT_BATCH_PIXEL(16, kBatchStacks[0]);
+            else if (stack == kBatchStacks[1]) RT_BATCH_PIXEL(16, kBatchStacks[1]);
+            else RT_BATCH_PIXEL(16, kBatchStacks[2]);
+        } else {
+            if (stack == kBatchStacks[0]) RT_BATCH_PIXEL(8, kBatchStacks[0]);
+            else if (stack == kBatchStacks[1]) RT_BATCH_PIXEL(8, kBatchStacks[1]);
+            else RT_BATCH_PIXEL(8, kBatchStacks[2]);
+        }
+#undef RT_BATCH_PIXEL
     }
+}
+
+// Persistent grid of the configured shape: resident blocks per SM x SMs.
+int batch_grid(const rt_batch *b)
+{
+    const rt_tune_config &c = b->cfg;
+    const int sms = b->ctx->sm_count;
+    if (c.tile_w == 16) {
+        if (c.stack_entries == kBatchStacks[0]) return grid_for<16, kBatchStacks[0]>(c.kernel, c.block_threads, sms);
+        if (c.stack_entries == kBatchStacks[1]) return grid_for<16, kBatchStacks[1]>(c.kernel, c.block_threads, sms);
+        return grid_for<16, kBatchStacks[2]>(c.kernel, c.block_threads, sms);
+    }
+    if (c.stack_entries == kBatchStacks[0]) return grid_for<8, kBatchStacks[0]>(c.kernel, c.block_threads, sms);
+    if (c.stack_entries == kBatchStacks[1]) return grid_for<8, kBatchStacks[1]>(c.kernel, c.block_threads, sms);
+    return grid_for<8, kBatchStacks[2]>(c.kernel, c.block_threads, sms);
 }
 
 rt_status make_graph(rt_batch *b)
@@ -182,9 +214,7 @@ rt_status make_graph(rt_batch *b)
     drop_graph(b);
     cudaStream_t st = b->ctx->stream;
     cudaGraph_t g = nullptr;
-    // persistent grid: resident blocks per SM for this shape x SMs
-    const int grid = (b->cfg.tile_w == 16) ? grid_for<16>(b->cfg.kernel, b->cfg.block_threads, b->ctx->sm_count)
-                                           : grid_for<8>(b->cfg.kernel, b->cfg.block_threads, b->ctx->sm_count);
+    const int grid = batch_grid(b);
     RT_CUDA_B(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture begin");
     launch_batch(b, st, grid);
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -458,6 +488,11 @@ rt_status rt_batch_set_config(rt_batch *b, const rt_tune_config *cfg)
         (cfg->tile_w != 8 && cfg->tile_w != 16) || cfg->chunk_tiles < 1 || cfg->chunk_tiles > 16 ||
         (cfg->kernel != RT_KERNEL_WAVE && cfg->kernel != RT_KERNEL_PIXEL))
         return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_config: unsupported configuration");
+    if (std::find(std::begin(kBatchStacks), std::end(kBatchStacks), cfg->stack_entries) == std::end(kBatchStacks) ||
+        (cfg->kernel == RT_KERNEL_WAVE && cfg->stack_entries != kStackSize))
+        return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_config: unsupported traversal stack capacity");
+    if (b->built && cfg->stack_entries < b->depth)
+        return bfail(RT_ERR_INVALID_ARG, "rt_batch_set_config: traversal stack smaller than the deepest tree");
     Guard g(b->ctx->device);
     b->cfg = *cfg;
     if (b->built && !b->h_jobs.empty()) return layout_jobs(b);
@@ -484,13 +519,15 @@ rt_status rt_batch_autotune(rt_batch *b, int32_t reps, rt_tune_config *best_out)
     const int tiles[2] = {8, 16};
     const int chunks[3] = {1, 2, 4};
     const int kernels[2] = {RT_KERNEL_WAVE, RT_KERNEL_PIXEL};
-    rt_tune_config best{128, 1, 8, RT_KERNEL_WAVE, 1e30f};
+    rt_tune_config best{128, 1, 8, RT_KERNEL_WAVE, 1e30f, kStackSize};
     for (int kn : kernels)
     for (int tw : tiles)
         for (int th : threads)
-            for (int ch : chunks) {
-                if (kn == RT_KERNEL_WAVE && ch != 1) continue;   // the wave form refills per lane
-                rt_tune_config c{th, ch, tw, kn, 0.f};
+            for (int ch : chunks)
+            for (int sk : kBatchStacks) {
+                if (kn == RT_KERNEL_WAVE && (ch != 1 || sk != kStackSize)) continue;   // the wave form refills per lane
+                if (sk < b->depth) continue;   // the stack must hold the deepest tree
+                rt_tune_config c{th, ch, tw, kn, 0.f, sk};
                 rt_status s = rt_batch_set_config(b, &c);
                 if (s != RT_OK) return s;
                 RT_CUDA_B(cudaGraphLaunch(b->exec, ctx->stream), "graph launch");   // warm-up

@@ -59,7 +59,7 @@ struct PixelOut {
 // (ray_trace_engine::ray_trace, raytracer.cc:20-87).  TABLE: the hit
 // triangle's material from `table` (per-triangle indices in sc.mat), else
 // `mat0` for every triangle.
-template <bool COUNT, bool TABLE = false>
+template <bool COUNT, bool TABLE = false, int STACK = kStackSize>
 __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, const CameraView &cam, const LightView *lights,
                                                        int nl, const MaterialView &mat0, int x, int y,
                                                        uint32_t &status, FetchCount *fc, bool fast_pow,
@@ -71,7 +71,7 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
     const RayState r = camera_ray(cam, x, y);
     HitRecord h;
     bool occ;
-    status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
+    status |= traverse<false, COUNT, STACK>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
     out.hit = h.t < FLT_MAX;
     out.id = out.hit ? h.id - sc.tri_base : -1;
     out.c = cam.background;
@@ -94,7 +94,7 @@ __device__ __forceinline__ PixelOut shade_pixel_lights(const SceneView &sc, cons
             shadow_ray(L, start, ldir, len);
             HitRecord sh;
             bool blocked;
-            status |= traverse<true, COUNT>(sc, start, ldir, len, sh, blocked, fc);
+            status |= traverse<true, COUNT, STACK>(sc, start, ldir, len, sh, blocked, fc);
             ++out.secondary;
             if (blocked) blocked_bits |= 1u << l;
             if (fast_pow) phong_add<false>(L, mat, kd, sp.sn, r.d, ldir, len, blocked ? 0.0f : 1.0f, c);
@@ -256,7 +256,7 @@ __device__ __forceinline__ PixelOut shade_pixel_tree(const SceneView &sc, const 
 }
 
 // Primary ray, closest hit, `samples` cosine-weighted AO rays within ao_dist.
-template <bool COUNT>
+template <bool COUNT, int STACK = kStackSize>
 __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const CameraView &cam, const MaterialView &mat,
                                                    int samples, float ao_dist, uint32_t seed, int x, int y,
                                                    uint32_t &status, FetchCount *fc)
@@ -267,7 +267,7 @@ __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const Ca
     const RayState r = camera_ray(cam, x, y);
     HitRecord h;
     bool occ;
-    status |= traverse<false, COUNT>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
+    status |= traverse<false, COUNT, STACK>(sc, r.o, r.d, FLT_MAX, h, occ, fc);
     out.hit = h.t < FLT_MAX;
     out.id = out.hit ? h.id - sc.tri_base : -1;
     out.c = cam.background;
@@ -281,7 +281,7 @@ __device__ __forceinline__ PixelOut shade_pixel_ao(const SceneView &sc, const Ca
             const float3 d = ao_direction(ob, pix, (uint32_t)s, seed);
             HitRecord ah;
             bool blocked;
-            status |= traverse<true, COUNT>(sc, start, d, ao_dist, ah, blocked, fc);
+            status |= traverse<true, COUNT, STACK>(sc, start, d, ao_dist, ah, blocked, fc);
             if (!blocked) ++made;
         }
         const float3 kd = material_kd(mat, sp);

@@ -337,8 +337,10 @@ __device__ __forceinline__ void trav_begin(Trav &T, const SceneView &sc, const f
 
 // One traversal step; returns true when the ray is finished.  Closest hit
 // (any = false) or any hit inside (EPSILON, tmax) skipping light and
-// transparent triangles (any = true).  Status bits go to `status`.
-template <bool COUNT>
+// transparent triangles (any = true).  Status bits go to `status`.  STACK:
+// the stack's capacity in node groups (a ray holds at most one group per
+// tree level, so any capacity above the tree's depth suffices).
+template <bool COUNT, int STACK = kStackSize>
 __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView &sc, bool any, uint32_t &status,
                                           FetchCount *fc)
 {
@@ -351,7 +353,7 @@ __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView
         const uint32_t idx = T.ngroup.x + __popc(T.ngroup.y & ((1u << slot) - 1u) & 0xffu);
         if (idx >= (uint32_t)sc.nnodes) { status |= kStatusBadIndex; return true; }
         if (T.ngroup.y & 0xff000000u) {
-            if (T.sp >= kStackSize) { status |= kStatusStackOverflow; return true; }
+            if (T.sp >= STACK) { status |= kStatusStackOverflow; return true; }
             stack[T.sp++] = T.ngroup;
         }
         const NodeHits nh = intersect_node(sc.nodes, idx, T.o, T.inv, T.oct, T.box_tmax);
@@ -398,15 +400,15 @@ __device__ __forceinline__ bool trav_step(Trav &T, uint2 *stack, const SceneView
 }
 
 // Whole traversal of one ray.  Returns the device status bits.
-template <bool ANY, bool COUNT = false>
+template <bool ANY, bool COUNT = false, int STACK = kStackSize>
 __device__ __forceinline__ uint32_t traverse(const SceneView &sc, const float3 o, const float3 d, float tmax,
                                              HitRecord &hit, bool &occluded, FetchCount *fc = nullptr)
 {
-    uint2 stack[kStackSize];
+    uint2 stack[STACK];
     Trav T;
     trav_begin(T, sc, o, d, tmax, ANY);
     uint32_t status = 0u;
-    while (!trav_step<COUNT>(T, stack, sc, ANY, status, fc)) {
+    while (!trav_step<COUNT, STACK>(T, stack, sc, ANY, status, fc)) {
     }
     hit = T.hit;
     occluded = T.occluded;

@@ -1,38 +1,56 @@
 // raptor_gpu_bvh.h -- drop-in GPU acceleration structure and renderer for
 // RAPTor's raytracer, built on the C ABI in include/rtcore.h.
 //
-// Header-only; compiled INSIDE the RAPTor tree (it includes RAPTor's own
-// ssd.h, primitive_store.h, camera.h, light.h and links against
-// librtcore.so).  It adds no new interface: a `gpu_bvh` is an `ssd`
-// (raytracer/spatial_sub_division/ssd.h:26-44) usable wherever `bvh`, `bih`
-// or `kd_tree` is, and `ray_tracer_gpu` takes the arguments of ray_tracer()
-// (raytracer/raytracer.h:105).
+// Compiled INSIDE the RAPTor tree: this header includes RAPTor's own
+// camera.h, light.h, primitive_store.h, ssd.h and material headers; its one
+// source file, raptor_gpu_bvh.cc, joins the raytracer's sources and the
+// program links librtcore.so.  Nothing in RAPTor is edited.
 //
-//   gpu_bvh accel(primitive_store&)             <-> bvh accel(primitive_store&)
-//   accel.find_nearest_object(&ray, &hit)       <-> bvh::find_nearest_object (bvh.cc:649)
-//   accel.found_nearer_object(&ray, t)          <-> bvh::found_nearer_object (bvh.cc:711)
-//   ray_tracer_gpu(&accel, lights, cam_args,   <-> ray_tracer(&accel, lights, store, cam)
-//                  cam, ka, kd, ks, ns, colours)   (raytracer.cc:563)
+//   gpu_bvh accel(store)                        <-> bvh accel(store)                 (bvh.h:27-32)
+//   accel.find_nearest_object(&ray, &hit)       <-> bvh::find_nearest_object         (bvh.cc:649)
+//   accel.found_nearer_object(&ray, t)          <-> bvh::found_nearer_object         (bvh.cc:711)
+//   ray_tracer_gpu(&accel, lights, store, cam)  <-> ray_tracer(&accel, lights, store, cam)
+//                                                                                  (raytracer.h:105)
+//
+// ray_tracer_gpu has ray_tracer's signature and effect: every ray of the
+// camera's (supersampled) grid is traced and its colour stored with
+// camera::set_pixel, so clip_image_to_rgb, tone_map, gamma_correct and the
+// image writers then run on the camera unchanged.  It reads the scene from
+// the same objects ray_tracer reads: geometry, vertex attributes, vertex
+// normals and material pointers of the store's triangles, the lights of the
+// light_list and the camera's grid.  Where RAPTor keeps those fields
+// private and offers no accessor (light colour and fall-off, material
+// coefficients, a triangle's material and vertex data, the camera's grid
+// and background), raptor_gpu_bvh.cc reads them through pointers to
+// members formed in explicit template instantiations, which C++ exempts
+// from access checking ([temp.spec]: "the usual access checking rules do
+// not apply to names used to specify explicit instantiations").
 //
 // Differences a caller sees:
 //  - the store is uploaded once, in its current order; ids returned are the
 //    store's primitive indices (what primitive_store::indirection returns in
 //    the reference), and the store's indirection is left untouched;
-//  - single-ray queries each cross the PCIe/C2C link; batch rays with
+//  - single-ray queries each cross the host/device link; batch rays with
 //    find_nearest_objects / found_nearer_objects for throughput;
 //  - errors throw std::runtime_error carrying rt_last_error_string() (the
 //    reference asserts instead);
-//  - ray_tracer_gpu shades with the coloured Phong model of
-//    coloured_mapper_shader (ka, kd, ks, ns; kd modulated by a per-vertex
-//    colour), the only material on the GPU path.
+//  - the GPU path shades coloured_mapper_shader (no texture mappers, or a
+//    kd mapper that returns the triangle's per-vertex attribute x 255) and
+//    phong_shader without reflection or refraction, up to RT_MAX_MATERIALS
+//    distinct materials, point, directional and spot lights, a constant
+//    background and a pinhole camera; anything else (sky boxes, depth of
+//    field, other texture mappers, diffuse reflection or transmission)
+//    throws std::invalid_argument naming it.
 #pragma once
 
+#include <cstdint>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "camera.h"
 #include "light.h"
+#include "material.h"
 #include "primitive_store.h"
 #include "ssd.h"
 
@@ -48,68 +66,25 @@ inline void check(rt_status s)
 }
 
 // One process-wide context per device (created on first use).
-inline rt_context *context(int device = 0)
-{
-    static rt_context *ctx = nullptr;
-    if (!ctx) check(rt_ctx_create(device, &ctx));
-    return ctx;
-}
+rt_context *context(int device = 0);
 }  // namespace gpu_detail
 
 class gpu_bvh : public ssd
 {
     public :
-        // Uploads every triangle of the store (vertices a, b, c; light flag;
-        // transparency) and builds the GPU hierarchy.
-        explicit gpu_bvh(const primitive_store &prims, int device = 0) : _scene(nullptr)
-        {
-            gpu_detail::check(rt_scene_create(gpu_detail::context(device), &_scene));
-            const int n = prims.size();
-            std::vector<float> verts(9 * (size_t)n);
-            std::vector<int32_t> idx(3 * (size_t)n);
-            std::vector<uint32_t> flags((size_t)n);
-            for (int i = 0; i < n; ++i)
-            {
-                const triangle *t = prims.primitive(i);
-                const point_t<> v[3] = { t->get_vertex_a(), t->get_vertex_b(), t->get_vertex_c() };
-                for (int k = 0; k < 3; ++k)
-                {
-                    verts[9 * i + 3 * k + 0] = v[k].x;
-                    verts[9 * i + 3 * k + 1] = v[k].y;
-                    verts[9 * i + 3 * k + 2] = v[k].z;
-                    idx[3 * i + k] = 3 * i + k;
-                }
-                flags[i] = (t->get_light() ? RT_TRI_LIGHT : 0u) | (t->is_transparent() ? RT_TRI_TRANSPARENT : 0u);
-            }
-            gpu_detail::check(rt_scene_upload(_scene, verts.data(), 3 * n, idx.data(), n, nullptr, flags.data()));
-            gpu_detail::check(rt_bvh_build(_scene, nullptr));
-        }
+        // Uploads every triangle of the store (vertices a, b, c; per-vertex
+        // attributes and normals where the triangle carries them; light and
+        // transparency flags; material index) and builds the GPU hierarchy.
+        explicit gpu_bvh(const primitive_store &prims, int device = 0);
+        ~gpu_bvh() { rt_scene_destroy(_scene); }
+        gpu_bvh(const gpu_bvh &) = delete;
+        gpu_bvh &operator=(const gpu_bvh &) = delete;
 
         // Per-frame update of a simulation loop that keeps the same
         // primitives and moves their vertices (the rebuild at
         // physics_engine/simulation_environment.cc:56-58): refits the
         // existing hierarchy instead of building a new one.
-        void refit(const primitive_store &prims)
-        {
-            const int n = prims.size();
-            std::vector<float> verts(9 * (size_t)n);
-            for (int i = 0; i < n; ++i)
-            {
-                const triangle *t = prims.primitive(i);
-                const point_t<> v[3] = { t->get_vertex_a(), t->get_vertex_b(), t->get_vertex_c() };
-                for (int k = 0; k < 3; ++k)
-                {
-                    verts[9 * i + 3 * k + 0] = v[k].x;
-                    verts[9 * i + 3 * k + 1] = v[k].y;
-                    verts[9 * i + 3 * k + 2] = v[k].z;
-                }
-            }
-            gpu_detail::check(rt_scene_refit_vertices(_scene, verts.data(), 3 * n, nullptr));
-        }
-
-        ~gpu_bvh() { rt_scene_destroy(_scene); }
-        gpu_bvh(const gpu_bvh &) = delete;
-        gpu_bvh &operator=(const gpu_bvh &) = delete;
+        void refit(const primitive_store &prims);
 
         // ssd interface: one ray per call.
         int find_nearest_object(const ray *const r, hit_description *const h) const override
@@ -154,6 +129,10 @@ class gpu_bvh : public ssd
 
         rt_scene *scene() const { return _scene; }
 
+        // The store's distinct materials in order of first use: entry k is
+        // material index k of the uploaded triangles.
+        const std::vector<const material *> &materials() const { return _materials; }
+
     private :
         static rt_ray to_rt(const ray &r, const float tmax)
         {
@@ -165,83 +144,13 @@ class gpu_bvh : public ssd
         }
 
         rt_scene *_scene;
+        std::vector<const material *> _materials;
 };
 
-// Camera arguments of the reference camera constructor (camera.h:55-62):
-// the renderer needs them explicitly because camera keeps them private.
-struct gpu_camera_args
-{
-    point_t<> position, x_axis, y_axis, z_axis;
-    ext_colour_t background;
-    float w, h, t;
-    unsigned x_res, y_res;
-};
-
-struct gpu_light_args
-{
-    bool directional;
-    ext_colour_t rgb;      /* 0..255 */
-    point_t<> centre;      /* point and spot light */
-    point_t<> direction;   /* directional light; a spot light's n */
-    float d;
-    float s_a = 0.0f, s_b = 0.0f;   /* spot light cone (light.h:24-25); s_b = 0: not a spot light */
-};
-
-// ray_tracer() replacement: renders the frame on the GPU and writes every
-// pixel through camera::set_pixel (camera.h:281), so clip_image_to_rgb and
-// the image writers work unchanged.  vertex_colours: 3 floats per vertex of
-// the store in triangle order (a, b, c of triangle 0, then triangle 1, ...),
-// nullable.  rf, tran, ri: the material's reflectivity, transparency and
-// refractive index (coloured_mapper_shader's rf, tran, ri).
-inline void ray_tracer_gpu(const gpu_bvh *const accel, const std::vector<gpu_light_args> &lights,
-                           const gpu_camera_args &cam_args, camera &c, const ext_colour_t &ka, const ext_colour_t &kd,
-                           const ext_colour_t &ks, const float ns, const float *vertex_colours = nullptr,
-                           const float rf = 0.0f, const float tran = 0.0f, const float ri = 1.0f)
-{
-    rt_camera cam;
-    const point_t<> *ax[4] = { &cam_args.position, &cam_args.x_axis, &cam_args.y_axis, &cam_args.z_axis };
-    float *dst[4] = { cam.pos, cam.x_axis, cam.y_axis, cam.z_axis };
-    for (int i = 0; i < 4; ++i) { dst[i][0] = ax[i]->x; dst[i][1] = ax[i]->y; dst[i][2] = ax[i]->z; }
-    cam.background[0] = cam_args.background.r; cam.background[1] = cam_args.background.g; cam.background[2] = cam_args.background.b;
-    cam.w = cam_args.w; cam.h = cam_args.h; cam.t = cam_args.t;
-    cam.xres = (int32_t)cam_args.x_res; cam.yres = (int32_t)cam_args.y_res;
-    std::vector<rt_light> ls(lights.size());
-    for (size_t i = 0; i < lights.size(); ++i)
-    {
-        const gpu_light_args &l = lights[i];
-        ls[i].kind = l.directional ? RT_LIGHT_DIRECTIONAL : RT_LIGHT_POINT;
-        ls[i].rgb[0] = l.rgb.r; ls[i].rgb[1] = l.rgb.g; ls[i].rgb[2] = l.rgb.b;
-        ls[i].pos[0] = l.centre.x; ls[i].pos[1] = l.centre.y; ls[i].pos[2] = l.centre.z;
-        ls[i].dir[0] = l.direction.x; ls[i].dir[1] = l.direction.y; ls[i].dir[2] = l.direction.z;
-        ls[i].d = l.d;
-        if (!l.directional && l.s_b != 0.0f) ls[i].kind = RT_LIGHT_SPOT;
-        ls[i].s_a = l.s_a;
-        ls[i].s_b = l.s_b;
-    }
-    rt_material m;
-    m.ka[0] = ka.r; m.ka[1] = ka.g; m.ka[2] = ka.b;
-    m.kd[0] = kd.r; m.kd[1] = kd.g; m.kd[2] = kd.b;
-    m.ks[0] = ks.r; m.ks[1] = ks.g; m.ks[2] = ks.b;
-    m.ns = ns;
-    m.rf = rf;
-    m.tran = tran;
-    m.ri = ri;
-    m.flags = 0u;
-    rt_scene *s = accel->scene();
-    if (vertex_colours)
-    {
-        int32_t nodes, tris, depth;
-        gpu_detail::check(rt_bvh_info(s, &nodes, &tris, &depth));
-        gpu_detail::check(rt_scene_update_attributes(s, vertex_colours, 3 * tris));
-    }
-    const size_t npix = (size_t)cam.xres * (size_t)cam.yres;
-    std::vector<uint8_t> rgb(3 * npix);
-    gpu_detail::check(rt_render(s, &cam, ls.data(), (int32_t)ls.size(), &m, rgb.data(), nullptr, nullptr));
-    for (unsigned y = 0; y < cam_args.y_res; ++y)
-        for (unsigned x = 0; x < cam_args.x_res; ++x)
-        {
-            const size_t p = 3 * ((size_t)x + (size_t)y * cam_args.x_res);
-            c.set_pixel(ext_colour_t(rgb[p], rgb[p + 1], rgb[p + 2]), x, y);
-        }
-}
+// ray_tracer() (raytracer.cc:563-598) on the GPU: same arguments, same
+// effect on the camera.  sub_division is used when it is a gpu_bvh built
+// from `everything`; any other ssd (a bvh, kd_tree, ...) is replaced by a
+// gpu_bvh built from `everything` for this call.
+void ray_tracer_gpu(const ssd *const sub_division, const light_list &lights, const primitive_store &everything,
+                    camera &c);
 }  // namespace raptor_raytracer

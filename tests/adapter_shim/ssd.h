@@ -1,0 +1,3 @@
+// Stand-in for RAPTor's ssd.h (test infrastructure): see raptor_stand_in.h.
+#pragma once
+#include "raptor_stand_in.h"

@@ -1,8 +1,15 @@
-"""The hand-written adjoint (rt_render_adjoint) against FP64 central finite
-differences of the same frame evaluated on the host, and against torch
-autograd through a plain re-statement of the forward -- both with the hit
-triangle, shadow visibility and shading branches of every pixel held at
-the values of the CUDA forward pass (interior gradients)."""
+"""The hand-written adjoint (rt_render_adjoint) of the 50,000-triangle
+displaced icosphere at 256x256 (primary + shadow ray, Phong, L2 loss to a
+target rendered from perturbed vertices).
+
+The hit triangle, shadow visibility and shading branches of every pixel are
+held at the values of the CUDA forward pass (interior gradients).  Checks:
+the float forward equals an FP64 restatement of that model on every pixel
+outside a stated branch margin; the adjoint, a vector-Jacobian product,
+agrees with FP64 central finite differences to 1e-3 relative on every
+component of 200 random vertices; the end-to-end loss gradient agrees with
+the FP64 loss's finite differences; and torch autograd through the FP64
+model gives the same gradient over every vertex."""
 import numpy as np
 import pytest
 
@@ -96,60 +103,132 @@ def diff_setup(rtlib, ctx, oracle):
     return sc, scene, frame, target, V, C, img, ids.cpu().numpy().reshape(-1), occl.cpu().numpy().reshape(-1), o, d
 
 
-def host_state(scene, frame, ids, occl, o, d):
-    """Per-hit-pixel fixed quantities of the forward pass (sign of the
-    normal, lit side, specular branch) in FP64."""
-    hit = ids >= 0
-    V = scene["verts"].astype(np.float64)
-    t = scene["tris"][ids[hit]]
-    A, B, Cv = V[t[:, 0]], V[t[:, 1]], V[t[:, 2]]
-    m = np.cross(B - A, Cv - A)
-    dd = d[hit].astype(np.float64)
-    sgn = np.where((m * dd).sum(-1) > 0, -1.0, 1.0)
-    return hit, sgn
+# Branch margin of the fixed-visibility model: a pixel whose FP64 lit-side
+# term s = L.sn or grazing term d.n lies within this of zero may take the
+# other branch in binary32 (light skipped / normal flipped), so it is left
+# out of the comparisons below (weight 0 in the vector-Jacobian checks).
+BRANCH_MARGIN = 1e-4
 
 
-def test_forward_float_matches_model(diff_setup):
-    sc, scene, frame, target, V, C, img, ids, occl, o, d = diff_setup
-    hit, sgn = host_state(scene, frame, ids, occl, o, d)
-    lit = np.ones(hit.sum())
-    spec = np.ones(hit.sum(), bool)
-    # evaluate once to get the branch masks, then compare colours
-    c = pixel_model(scene["verts"].astype(np.float64), scene["vattr"].astype(np.float64), scene["tris"], ids[hit],
-                    occl[hit].astype(np.float64), o[hit].astype(np.float64), d[hit].astype(np.float64), sgn, lit,
-                    spec, frame, np)
-    gpu = img.cpu().numpy().reshape(-1, 3)[hit]
-    # pixels on the lit side with a specular term: the model's colour is the forward's
-    assert 0.3 < hit.mean() < 0.9
-    err = np.abs(c - gpu)
-    ok = err <= 1e-3 * np.maximum(np.abs(gpu), 1.0)
-    assert ok.mean() > 0.98
-
-
-def branch_masks(scene, frame, ids, occl, o, d, hit, sgn):
+def fp64_state(scene, frame, ids, o, d, hit):
+    """FP64 per-hit-pixel quantities of the forward: face-forwarding sign,
+    lit side (s >= 0), specular branch (R.V > 0) and the excluded pixels
+    (|s| or |d.n| within BRANCH_MARGIN of zero)."""
     V = scene["verts"].astype(np.float64)
     t = scene["tris"][ids[hit]]
     A, B, Cv = V[t[:, 0]], V[t[:, 1]], V[t[:, 2]]
     oo, dd = o[hit].astype(np.float64), d[hit].astype(np.float64)
     e1, e2 = Cv - A, B - A
+    m = np.cross(e2, e1)
+    n = m / np.linalg.norm(m, axis=1)[:, None]
+    dn = (n * dd).sum(-1)
+    sgn = np.where(dn > 0, -1.0, 1.0)
     P = np.cross(dd, e2)
     det = (e1 * P).sum(-1)
-    T = oo - A
-    Q = np.cross(T, e1)
+    Q = np.cross(oo - A, e1)
     tt = (e2 * Q).sum(-1) / det
     p = oo + tt[:, None] * dd
-    m = np.cross(e2, e1)
-    sn = m / np.linalg.norm(m, axis=1)[:, None] * sgn[:, None]
+    sn = n * sgn[:, None]
     ldir = np.asarray(frame["lights"][0]["pos"]) - p
     ldir /= np.linalg.norm(ldir, axis=1)[:, None]
     s = (ldir * sn).sum(-1)
     r = (dd * ldir).sum(-1) - 2 * s * (dd * sn).sum(-1)
-    return (s >= 0).astype(np.float64), r > 0
+    excluded = (np.abs(s) < BRANCH_MARGIN) | (np.abs(dn) < BRANCH_MARGIN)
+    return sgn, (s >= 0).astype(np.float64), r > 0, excluded
+
+
+def test_forward_float_matches_model(diff_setup):
+    """The CUDA float forward equals the FP64 fixed-visibility model on
+    every hit pixel outside the branch margin, to 1e-4 relative: the model
+    the finite differences below are taken on is the forward's."""
+    sc, scene, frame, target, V, C, img, ids, occl, o, d = diff_setup
+    hit = ids >= 0
+    sgn, lit, spec, excluded = fp64_state(scene, frame, ids, o, d, hit)
+    c = pixel_model(scene["verts"].astype(np.float64), scene["vattr"].astype(np.float64), scene["tris"], ids[hit],
+                    occl[hit].astype(np.float64), o[hit].astype(np.float64), d[hit].astype(np.float64), sgn, lit,
+                    spec, frame, np)
+    gpu = img.cpu().numpy().reshape(-1, 3)[hit]
+    assert 0.3 < hit.mean() < 0.9
+    assert excluded.mean() < 1e-3
+    err = np.abs(c - gpu) / np.maximum(np.abs(c), 1.0)
+    keep = ~excluded
+    assert err[keep].max() < 1e-4, (err[keep].max(), np.argmax(err[keep].max(-1)))
+
+
+def fd_vjp(scene, frame, ids, occl, o, d, w, picks, h=1e-4):
+    """FP64 central differences of F(V, C) = sum_pix w_pix . c_pix(V, C)
+    (c: the fixed-visibility model) with respect to the positions and
+    colours of the vertices in picks, using only the pixels that see a
+    triangle of each vertex."""
+    hit = ids >= 0
+    sgn, lit, spec, excluded = fp64_state(scene, frame, ids, o, d, hit)
+    hid = ids[hit]
+    oo, dd = o[hit].astype(np.float64), d[hit].astype(np.float64)
+    occ = occl[hit].astype(np.float64)
+    wh = w[hit]
+    V64 = scene["verts"].astype(np.float64)
+    C64 = scene["vattr"].astype(np.float64)
+    tris = scene["tris"]
+    fd_pos = np.zeros((len(picks), 3))
+    fd_col = np.zeros((len(picks), 3))
+    for k, vtx in enumerate(picks):
+        px = np.nonzero((tris[hid] == vtx).any(axis=1))[0]
+        args = (tris, hid[px], occ[px], oo[px], dd[px], sgn[px], lit[px], spec[px], frame, np)
+        for j in range(3):
+            for arr, fd in ((V64, fd_pos), (C64, fd_col)):
+                keep = arr[vtx, j]
+                arr[vtx, j] = keep + h
+                fp = (wh[px] * pixel_model(V64, C64, *args)).sum()
+                arr[vtx, j] = keep - h
+                fm = (wh[px] * pixel_model(V64, C64, *args)).sum()
+                arr[vtx, j] = keep
+                fd[k, j] = (fp - fm) / (2 * h)
+    return fd_pos, fd_col
 
 
 def test_adjoint_vs_fp64_finite_differences(diff_setup):
-    """dL/dvertex-position and dL/dvertex-colour against FP64 central
-    differences (h = 1e-4) on 200 random vertices seen by the camera."""
+    """rt_render_adjoint is the vector-Jacobian product of the frame: given
+    w = dL/dpixel it returns sum_pix w . dc_pix/dvertex.  With w = 2 (frame -
+    target), the gradient of the L2 loss to the target image, it is
+    checked against FP64 central differences (h = 1e-4) of
+    F = sum_pix w . c_pix on 200 random vertices seen by the camera: every
+    one of the 1,200 components (position and colour) agrees to 1e-3
+    relative, the denominator floored at 1e-2 of the RMS gradient for
+    near-zero components.  Pixels inside the branch margin get w = 0 on
+    both sides."""
+    sc, scene, frame, target, V, C, img, ids, occl, o, d = diff_setup
+    H, W = frame["camera"]["yres"], frame["camera"]["xres"]
+    hit = ids >= 0
+    _, _, _, excluded = fp64_state(scene, frame, ids, o, d, hit)
+    w = (2.0 * (img - target)).cpu().numpy().reshape(-1, 3)
+    mask = np.zeros(H * W, bool)
+    mask[np.nonzero(hit)[0][excluded]] = True
+    w[mask] = 0.0
+    w_dev = torch.from_numpy(w.reshape(H, W, 3)).cuda()
+    gpos = torch.empty_like(V)
+    gcol = torch.empty_like(C)
+    assert sc.render_adjoint(frame, w_dev, gpos, gcol).status == 0
+    gpos = gpos.cpu().numpy().astype(np.float64)
+    gcol = gcol.cpu().numpy().astype(np.float64)
+
+    seen = np.unique(scene["tris"][ids[hit]].reshape(-1))
+    picks = np.random.default_rng(4).choice(seen, 200, replace=False)
+    fd_pos, fd_col = fd_vjp(scene, frame, ids, occl, o, d, w.astype(np.float64), picks)
+    a_pos, a_col = gpos[picks], gcol[picks]
+    rel_p = np.abs(a_pos - fd_pos) / np.maximum(np.abs(fd_pos), 1e-2 * np.sqrt((fd_pos ** 2).mean()))
+    rel_c = np.abs(a_col - fd_col) / np.maximum(np.abs(fd_col), 1e-2 * np.sqrt((fd_col ** 2).mean()))
+    print(f"position grads: median rel {np.median(rel_p):.2e}, max {rel_p.max():.2e}; "
+          f"colour grads: median rel {np.median(rel_c):.2e}, max {rel_c.max():.2e}")
+    assert rel_p.max() <= 1e-3, (rel_p.max(), picks[np.argmax(rel_p.max(1))])
+    assert rel_c.max() <= 1e-3, (rel_c.max(), picks[np.argmax(rel_c.max(1))])
+
+
+def test_loss_gradient_vs_fp64_finite_differences(diff_setup):
+    """End to end through autograd: dL/dvertex of L = |frame - target|^2
+    against FP64 central differences of the FP64 model's loss.  Here the
+    residual itself differs (binary32 frame vs FP64 model, ~1e-5 of the
+    colour, where the residual may be 1e-2 of it), which bounds the
+    agreement; the vector-Jacobian test above isolates the adjoint."""
     sc, scene, frame, target, V, C, img, ids, occl, o, d = diff_setup
     Vt = V.clone().requires_grad_(True)
     Ct = C.clone().requires_grad_(True)
@@ -159,8 +238,8 @@ def test_adjoint_vs_fp64_finite_differences(diff_setup):
     gpos = Vt.grad.cpu().numpy().astype(np.float64)
     gcol = Ct.grad.cpu().numpy().astype(np.float64)
 
-    hit, sgn = host_state(scene, frame, ids, occl, o, d)
-    lit, spec = branch_masks(scene, frame, ids, occl, o, d, hit, sgn)
+    hit = ids >= 0
+    sgn, lit, spec, _ = fp64_state(scene, frame, ids, o, d, hit)
     hid = ids[hit]
     oo, dd = o[hit].astype(np.float64), d[hit].astype(np.float64)
     occ = occl[hit].astype(np.float64)
@@ -181,9 +260,9 @@ def test_adjoint_vs_fp64_finite_differences(diff_setup):
             for arr, fd in ((V64, fd_pos), (C64, fd_col)):
                 keep = arr[vtx, j]
                 arr[vtx, j] = keep + h
-                cp = pixel_model(V64, C64, *args) if arr is V64 else pixel_model(V64, arr, *args)
+                cp = pixel_model(V64, C64, *args)
                 arr[vtx, j] = keep - h
-                cm = pixel_model(V64, C64, *args) if arr is V64 else pixel_model(V64, arr, *args)
+                cm = pixel_model(V64, C64, *args)
                 arr[vtx, j] = keep
                 lp = ((cp - tgt[px]) ** 2).sum()
                 lm = ((cm - tgt[px]) ** 2).sum()
@@ -191,11 +270,10 @@ def test_adjoint_vs_fp64_finite_differences(diff_setup):
     a_pos, a_col = gpos[picks], gcol[picks]
     scale_p = np.sqrt((fd_pos ** 2).mean())
     scale_c = np.sqrt((fd_col ** 2).mean())
-    # relative error against each gradient, floored at 1% of the RMS gradient
     rel_p = np.abs(a_pos - fd_pos) / np.maximum(np.abs(fd_pos), 1e-2 * scale_p)
     rel_c = np.abs(a_col - fd_col) / np.maximum(np.abs(fd_col), 1e-2 * scale_c)
-    print(f"position grads: median rel {np.median(rel_p):.2e}, p99 {np.percentile(rel_p, 99):.2e}; "
-          f"colour grads: median rel {np.median(rel_c):.2e}, p99 {np.percentile(rel_c, 99):.2e}")
+    print(f"loss position grads: median rel {np.median(rel_p):.2e}, p95 {np.percentile(rel_p, 95):.2e}; "
+          f"colour grads: median rel {np.median(rel_c):.2e}, p95 {np.percentile(rel_c, 95):.2e}")
     assert np.median(rel_p) < 1e-3 and np.percentile(rel_p, 95) < 1e-2
     assert np.median(rel_c) < 1e-3 and np.percentile(rel_c, 95) < 1e-2
     rel_norm = np.linalg.norm(a_pos - fd_pos) / np.linalg.norm(fd_pos)
@@ -210,8 +288,8 @@ def test_adjoint_vs_autograd_reference(diff_setup):
     Ct = C.clone().requires_grad_(True)
     loss = ((RenderFn.apply(Vt, Ct, sc, frame) - target) ** 2).sum()
     loss.backward()
-    hit, sgn = host_state(scene, frame, ids, occl, o, d)
-    lit, spec = branch_masks(scene, frame, ids, occl, o, d, hit, sgn)
+    hit = ids >= 0
+    sgn, lit, spec, _ = fp64_state(scene, frame, ids, o, d, hit)
     dev = "cuda"
     V64 = torch.tensor(scene["verts"], dtype=torch.float64, device=dev, requires_grad=True)
     C64 = torch.tensor(scene["vattr"], dtype=torch.float64, device=dev, requires_grad=True)

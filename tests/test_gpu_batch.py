@@ -91,8 +91,10 @@ def test_autotune_keeps_results(rtlib, ctx, batch_setup):
     b.render()
     for (rgb, _), ref in zip(bufs, before):
         assert np.array_equal(rgb.cpu().numpy(), ref)
+    assert best["stack_entries"] in (16, 24, 48)
     # every shape gives the same frames
-    for shape in ((64, 4, 16, 1), (256, 2, 8, 1), (64, 1, 16, 0), (256, 1, 8, 0)):
+    for shape in ((64, 4, 16, 1, 48), (256, 2, 8, 1, 16), (128, 1, 8, 1, 24), (64, 1, 16, 0, 48),
+                  (256, 1, 8, 0, 48)):
         b.set_config(*shape)
         b.render()
         for (rgb, _), ref in zip(bufs, before):
