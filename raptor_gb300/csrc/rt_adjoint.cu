@@ -32,6 +32,10 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b)
 {
     return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
+__device__ __forceinline__ double3 cross3d(double3 a, double3 b)
+{
+    return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
 __device__ __forceinline__ void atomic_add3(float *p, float3 g)
 {
     atomicAdd(p, g.x);
@@ -194,13 +198,22 @@ __global__ void __launch_bounds__(kTraceThreads) k_diff(SceneView sc, const floa
                     atomic_add3(gcol + 3 * tv.y, gc * v);
                     atomic_add3(gcol + 3 * tv.x, gc * w);
                 }
-                // ray-triangle solve: rows d, -e1, -e2 of M^T; lambda = M^-T (g_t, g_u, g_v)
+                // ray-triangle solve: rows d, -e1, -e2 of M^T; lambda = M^-T (g_t, g_u, g_v).
+                // Its determinant d.(e1 x e2) shrinks with the grazing angle
+                // d.n, which scales the rounding error of a binary32 solve by
+                // 1/|d.n|; the solve is done in double (one per hit pixel).
                 const float g_t = dot3(g_p, d);
-                const float3 r0 = d, r1 = e1 * -1.0f, r2 = e2 * -1.0f;
-                const float3 c12 = cross3(r1, r2), c20 = cross3(r2, r0), c01 = cross3(r0, r1);
-                const float det = dot3(r0, c12);
-                if (fabsf(det) > 1e-30f) {
-                    const float3 lam = (c12 * g_t + c20 * g_u + c01 * g_v) * (1.0f / det);
+                const double3 r0 = make_double3(d.x, d.y, d.z);
+                const double3 r1 = make_double3(-(double)e1.x, -(double)e1.y, -(double)e1.z);
+                const double3 r2 = make_double3(-(double)e2.x, -(double)e2.y, -(double)e2.z);
+                const double3 c12 = cross3d(r1, r2), c20 = cross3d(r2, r0), c01 = cross3d(r0, r1);
+                const double det = r0.x * c12.x + r0.y * c12.y + r0.z * c12.z;
+                if (fabs(det) > 1e-300) {
+                    const double inv = 1.0 / det;
+                    const double gt = g_t, gu = g_u, gv = g_v;
+                    const float3 lam = f3((float)((c12.x * gt + c20.x * gu + c01.x * gv) * inv),
+                                          (float)((c12.y * gt + c20.y * gu + c01.y * gv) * inv),
+                                          (float)((c12.z * gt + c20.z * gu + c01.z * gv) * inv));
                     gA = gA + lam * w;
                     gB = gB + lam * v;
                     gC = gC + lam * u;
