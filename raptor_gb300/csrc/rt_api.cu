@@ -296,6 +296,12 @@ rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
         ctx->isect = (int)value;
         return RT_OK;
     }
+    if (option == RT_OPT_MORTON_BITS) {
+        if (value != 0 && (value < 10 || value > 21))
+            return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: Morton bits per axis must be 0 or 10..21");
+        ctx->morton_bits = (int)value;
+        return RT_OK;
+    }
     if (option == RT_OPT_BUILDER) {
         if (value != RT_BUILDER_LBVH && value != RT_BUILDER_PLOC)
             return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown builder");
@@ -443,6 +449,7 @@ rt_status rt_bvh_build(rt_scene *s, float *build_ms)
     in.sm_count = ctx->sm_count;
     in.host_scratch = ctx->h_scratch;
     in.builder = ctx->builder == RT_BUILDER_LBVH ? kBuilderLbvh : kBuilderPloc;
+    in.morton_bits = ctx->morton_bits;
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
     const BuildResult R = build_wide_bvh(in, s->temp.ptr, s->temp.cap, ctx->stream);
     if (R.status != 0) {

@@ -51,6 +51,7 @@ struct rt_context {
     int render_kernel = RT_KERNEL_PIXEL;
     int isect = RT_ISECT_REFERENCE;
     int builder = RT_BUILDER_PLOC;
+    int morton_bits = 0;                   // RT_OPT_MORTON_BITS
 };
 
 struct rt_scene {

@@ -1070,82 +1070,118 @@ __device__ __forceinline__ uint32_t quant_hi(float c, float p, float inv)
     return (uint32_t)fminf(fmaxf(q, 0.f), 255.f);
 }
 
+// Lane groups of 8 within a warp: ballots, reductions and shuffles confined
+// to the group (xor shuffles with offsets 4, 2, 1 never leave an aligned
+// group of 8).  Every lane of the warp executes each of them.
+__device__ __forceinline__ uint32_t gballot(bool p, int gbase)
+{
+    return (__ballot_sync(0xffffffffu, p) >> gbase) & 0xffu;
+}
+__device__ __forceinline__ int gmin(int v)
+{
+    v = min(v, __shfl_xor_sync(0xffffffffu, v, 4));
+    v = min(v, __shfl_xor_sync(0xffffffffu, v, 2));
+    return min(v, __shfl_xor_sync(0xffffffffu, v, 1));
+}
+__device__ __forceinline__ int gmax(int v)
+{
+    v = max(v, __shfl_xor_sync(0xffffffffu, v, 4));
+    v = max(v, __shfl_xor_sync(0xffffffffu, v, 2));
+    return max(v, __shfl_xor_sync(0xffffffffu, v, 1));
+}
+__device__ __forceinline__ uint32_t gor(uint32_t v)
+{
+    v |= __shfl_xor_sync(0xffffffffu, v, 4);
+    v |= __shfl_xor_sync(0xffffffffu, v, 2);
+    return v | __shfl_xor_sync(0xffffffffu, v, 1);
+}
+
 // Word h (0: slots 0-3, 1: slots 4-7) of a per-slot byte plane: every lane
-// that holds a child in that half contributes its byte; empty slots read
-// `empty`.
+// of the group that holds a child in that half contributes its byte; empty
+// slots read `empty`.
 __device__ __forceinline__ uint32_t plane_word(bool mine, int slot, uint32_t byte, int h, uint32_t empty)
 {
     const bool in = mine && (slot >> 2) == h;
     const uint32_t sh = 8u * (uint32_t)(slot & 3);
-    const uint32_t occ = __reduce_or_sync(0xffffffffu, in ? (0xffu << sh) : 0u);
-    const uint32_t val = __reduce_or_sync(0xffffffffu, in ? (byte << sh) : 0u);
+    const uint32_t occ = gor(in ? (0xffu << sh) : 0u);
+    const uint32_t val = gor(in ? (byte << sh) : 0u);
     return (empty & ~occ) | val;
 }
 
-// One wide node per warp (surface-area decisions): lane k holds child k.
-// The 8 slots are split between binary children in rounds (a lane that
-// splits keeps the left share and hands the right one to a new lane), then
-// lanes load their boxes, the node box is a warp reduction, slots go to
-// children by repeated warp arg-min of the octant cost, and the node's 20
-// words are assembled with warp OR reductions.  Same node as collapse_task
-// up to the order of equal-cost choices.
-__device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int2 task, int lane)
+// One wide node per group of 8 lanes (surface-area decisions), four per
+// warp: lane k of the group holds child k.  The 8 slots are split between
+// binary children in rounds (a lane that splits keeps the left share and
+// hands the right one to a new lane), then lanes load their boxes, the node
+// box is a group reduction, slots go to children by repeated group arg-min
+// of the octant cost, and the node's 20 words are assembled with group OR
+// reductions.  Same node as collapse_task up to the order of equal-cost
+// choices.  Several nodes per warp keep four times as many of a level's
+// dependent-load chains (decisions, children, boxes) in flight as one node
+// per warp, on the wide levels near the leaves where a level's tasks far
+// outnumber the resident warps.  Control flow stays warp-uniform (groups
+// without a task, or with a malformed one, only stop writing).
+__device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const int2 task, bool has_task, int gbase,
+                                                    int lane)
 {
     const uint32_t full = 0xffffffffu;
     int32_t ref = 0;
     int slots = 0;
-    bool active = false, done = false, lf = false;
-    if (task.x < 0) {
-        if (lane == 0) { ref = task.x; active = done = lf = true; }
-    } else {
-        const uint32_t d = A.dec[task.x];
-        const int k8 = (int)((d >> 21) & 7u);
-        if (lane == 0) { ref = A.left[task.x]; slots = k8; active = true; }
-        if (lane == 1) { ref = A.right[task.x]; slots = 8 - k8; active = true; }
-        for (int round = 0; round < 8; ++round) {
-            bool split = false;
-            int32_t rr = 0;
-            int rs = 0;
-            if (active && !done) {
-                if (ref < 0) {
-                    done = lf = true;
-                } else {
-                    const uint32_t dr = A.dec[ref];
-                    int i = slots;
-                    while (i >= 2 && ((dr >> (3 * (i - 2))) & 7u) == 0u) --i;
-                    if (i <= 1) {
-                        done = true;
-                        lf = (dr >> 31) != 0u;
-                    } else {
-                        const int kl = (int)((dr >> (3 * (i - 2))) & 7u);
-                        split = true;
-                        rr = A.right[ref];
-                        rs = i - kl;
-                        ref = A.left[ref];
-                        slots = kl;
-                    }
-                }
-            }
-            const uint32_t sb = __ballot_sync(full, split);
-            if (!sb) break;
-            const int nact = __popc(__ballot_sync(full, active));
-            if (nact + __popc(sb) > 8) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }   // slots sum to 8
-            // receiving lane nact + r takes the right share of the r-th splitter
-            const int r = lane - nact;
-            const int src = (r >= 0 && r < __popc(sb)) ? (int)__fns(sb, 0, r + 1) : lane;
-            const int32_t got_ref = __shfl_sync(full, rr, src);
-            const int got_slots = __shfl_sync(full, rs, src);
-            if (r >= 0 && r < __popc(sb)) {
-                ref = got_ref;
-                slots = got_slots;
-                active = true;
-                done = lf = false;
-            }
+    bool active = false, done = false, lf = false, err = false;
+    if (has_task) {
+        if (task.x < 0) {
+            if (lane == 0) { ref = task.x; active = done = lf = true; }
+        } else {
+            const uint32_t d = A.dec[task.x];
+            const int k8 = (int)((d >> 21) & 7u);
+            if (lane == 0) { ref = A.left[task.x]; slots = k8; active = true; }
+            if (lane == 1) { ref = A.right[task.x]; slots = 8 - k8; active = true; }
         }
     }
-    const uint32_t amask = __ballot_sync(full, active);
-    const int m = __popc(amask);
-    if (__ballot_sync(full, active && !done)) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }
+    for (int round = 0; round < 8; ++round) {
+        bool split = false;
+        int32_t rr = 0;
+        int rs = 0;
+        if (active && !done) {
+            if (ref < 0) {
+                done = lf = true;
+            } else {
+                const uint32_t dr = A.dec[ref];
+                int i = slots;
+                while (i >= 2 && ((dr >> (3 * (i - 2))) & 7u) == 0u) --i;
+                if (i <= 1) {
+                    done = true;
+                    lf = (dr >> 31) != 0u;
+                } else {
+                    const int kl = (int)((dr >> (3 * (i - 2))) & 7u);
+                    split = true;
+                    rr = A.right[ref];
+                    rs = i - kl;
+                    ref = A.left[ref];
+                    slots = kl;
+                }
+            }
+        }
+        const uint32_t sb = gballot(split, gbase);
+        if (!__any_sync(full, sb != 0u)) break;
+        const int nact = __popc(gballot(active, gbase));
+        const int nsb = __popc(sb);
+        if (nact + nsb > 8) err = true;   // the slot shares always sum to 8
+        // receiving lane nact + r takes the right share of the r-th splitter
+        const int r = lane - nact;
+        const bool recv = !err && r >= 0 && r < nsb;
+        const int src = recv ? (int)__fns(sb, 0, r + 1) : lane;
+        const int32_t got_ref = __shfl_sync(full, rr, gbase + src);
+        const int got_slots = __shfl_sync(full, rs, gbase + src);
+        if (recv) {
+            ref = got_ref;
+            slots = got_slots;
+            active = true;
+            done = lf = false;
+        }
+    }
+    const int m = __popc(gballot(active, gbase));
+    if (gballot(active && !done, gbase) != 0u) err = true;
+    if (err) active = false;
 
     float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.f), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f);
     int32_t cnt = 0;
@@ -1155,19 +1191,20 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
         if (lf && cnt > kMaxLeafTris) lf = false;   // cannot happen: the tables allow <= 3
     }
     // node box
-    const float nlox = of_ord(__reduce_min_sync(full, ord_of(lo.x)));
-    const float nloy = of_ord(__reduce_min_sync(full, ord_of(lo.y)));
-    const float nloz = of_ord(__reduce_min_sync(full, ord_of(lo.z)));
-    const float nhix = of_ord(__reduce_max_sync(full, ord_of(hi.x)));
-    const float nhiy = of_ord(__reduce_max_sync(full, ord_of(hi.y)));
-    const float nhiz = of_ord(__reduce_max_sync(full, ord_of(hi.z)));
+    const float nlox = of_ord(gmin(ord_of(lo.x)));
+    const float nloy = of_ord(gmin(ord_of(lo.y)));
+    const float nloz = of_ord(gmin(ord_of(lo.z)));
+    const float nhix = of_ord(gmax(ord_of(hi.x)));
+    const float nhiy = of_ord(gmax(ord_of(hi.y)));
+    const float nhiz = of_ord(gmax(ord_of(hi.z)));
     const float pcx = 0.5f * (nlox + nhix), pcy = 0.5f * (nloy + nhiy), pcz = 0.5f * (nloz + nhiz);
 
     // slots: slot s holds the child met first by rays of octant s
     const float ox = 0.5f * (lo.x + hi.x) - pcx, oy = 0.5f * (lo.y + hi.y) - pcy, oz = 0.5f * (lo.z + hi.z) - pcz;
     int myslot = -1;
     uint32_t taken = 0;
-    for (int it = 0; it < m; ++it) {
+    for (int it = 0; it < 8; ++it) {
+        if (!__any_sync(full, it < m)) break;
         const bool open = active && myslot < 0;
         float bc = FLT_MAX;
         int bs = 0;
@@ -1180,21 +1217,23 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
             }
         }
         const int o = open ? ord_of(bc) : 0x7fffffff;
-        const int mn = __reduce_min_sync(full, o);
-        const uint32_t cand = __ballot_sync(full, open && o == mn);
-        const int winner = __ffs(cand) - 1;
-        const int ws = __shfl_sync(full, bs, winner);
-        if (lane == winner) myslot = ws;
-        taken |= 1u << ws;
+        const int mn = gmin(o);
+        const uint32_t cand = gballot(open && o == mn, gbase);
+        const int winner = cand ? __ffs(cand) - 1 : 0;
+        const int ws = __shfl_sync(full, bs, gbase + winner);
+        if (cand) {
+            if (lane == winner) myslot = ws;
+            taken |= 1u << ws;
+        }
     }
 
     // allocation: internal children contiguous in slot order, leaf triangles
     // in slot order
     const bool internal = active && !lf;
-    const uint32_t imask = __reduce_or_sync(full, internal ? (1u << myslot) : 0u);
+    const uint32_t imask = gor(internal ? (1u << myslot) : 0u);
     const int n_int = __popc(imask);
-    const uint32_t cnt_lo = __reduce_or_sync(full, (active && lf && myslot < 4) ? ((uint32_t)cnt << (8 * myslot)) : 0u);
-    const uint32_t cnt_hi = __reduce_or_sync(full, (active && lf && myslot >= 4) ? ((uint32_t)cnt << (8 * (myslot - 4))) : 0u);
+    const uint32_t cnt_lo = gor((active && lf && myslot < 4) ? ((uint32_t)cnt << (8 * myslot)) : 0u);
+    const uint32_t cnt_hi = gor((active && lf && myslot >= 4) ? ((uint32_t)cnt << (8 * (myslot - 4))) : 0u);
     int n_tri = 0, tri_off = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
@@ -1202,16 +1241,19 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
         if (s < myslot) tri_off += c;
         n_tri += c;
     }
+    const bool writes = has_task && !err;
     int32_t child_base = 0, tri_base = 0, next = 0;
-    if (lane == 0) {
+    if (lane == 0 && writes) {
         if (n_int) child_base = atomicAdd(&A.counters[0], n_int);
         if (n_tri) tri_base = atomicAdd(&A.counters[1], n_tri);
         if (n_int) next = atomicAdd(A.next_count, n_int);
     }
-    child_base = __shfl_sync(full, child_base, 0);
-    tri_base = __shfl_sync(full, tri_base, 0);
-    next = __shfl_sync(full, next, 0);
-    if (child_base + n_int > A.max_nodes || tri_base + n_tri > A.n) { if (lane == 0) atomicExch(&A.counters[3], 1); return; }
+    child_base = __shfl_sync(full, child_base, gbase);
+    tri_base = __shfl_sync(full, tri_base, gbase);
+    next = __shfl_sync(full, next, gbase);
+    const bool fits = child_base + n_int <= A.max_nodes && tri_base + n_tri <= A.n;
+    if (has_task && lane == 0 && (err || !fits)) atomicExch(&A.counters[3], 1);
+    if (!writes || !fits) active = false;
 
     // quantisation frame
     const int ex = grid_exponent(nhix - nlox), ey = grid_exponent(nhiy - nloy), ez = grid_exponent(nhiz - nloz);
@@ -1243,6 +1285,8 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
         w[16 + h] = plane_word(active, myslot, qhy, h, 0u);
         w[18 + h] = plane_word(active, myslot, qhz, h, 0u);
     }
+    const uint32_t occ = gor(active ? (1u << myslot) : 0u);
+    if (!writes || !fits) return;   // after the last group operation
     if (lane < 5) {
         uint4 v;
         v.x = w[0]; v.y = w[1]; v.z = w[2]; v.w = w[3];
@@ -1251,11 +1295,8 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
             if (lane == q) { v.x = w[4 * q]; v.y = w[4 * q + 1]; v.z = w[4 * q + 2]; v.w = w[4 * q + 3]; }
         reinterpret_cast<uint4 *>(A.nodes + task.y)[lane] = v;
     }
-    {
-        const uint32_t occ = __reduce_or_sync(full, active ? (1u << myslot) : 0u);
-        if (active) A.slot_ref[8 * (size_t)task.y + myslot] = ref;
-        if (lane < 8 && !((occ >> lane) & 1u)) A.slot_ref[8 * (size_t)task.y + lane] = kEmptySlot;
-    }
+    if (active) A.slot_ref[8 * (size_t)task.y + myslot] = ref;
+    if (!((occ >> lane) & 1u)) A.slot_ref[8 * (size_t)task.y + lane] = kEmptySlot;
     if (internal) {
         const int rank = __popc(imask & ((1u << myslot) - 1u));
         A.tasks_out[next + rank] = make_int2(ref, child_base + rank);
@@ -1287,13 +1328,18 @@ __device__ __forceinline__ void collapse_task_warp(const BuildArgs &A, const int
     }
 }
 
-__global__ void __launch_bounds__(128) k_collapse_level_warp(BuildArgs A)
+__global__ void __launch_bounds__(128) k_collapse_level_group(BuildArgs A)
 {
     const int32_t ntasks = *A.cur_count;
-    const int lane = threadIdx.x & 31;
+    const int lane32 = threadIdx.x & 31;
+    const int g = lane32 >> 3;
     const int32_t wid = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int32_t nw = (int32_t)((gridDim.x * blockDim.x) >> 5);
-    for (int32_t ti = wid; ti < ntasks; ti += nw) collapse_task_warp(A, A.tasks_in[ti], lane);
+    for (int32_t t0 = 4 * wid; t0 < ntasks; t0 += 4 * nw) {
+        const int32_t ti = t0 + g;
+        const bool has = ti < ntasks;
+        collapse_task_group(A, has ? A.tasks_in[ti] : make_int2(0, 0), has, 8 * g, lane32 & 7);
+    }
 }
 
 // One tree level: every task of the level (count read on the device, so
@@ -1409,13 +1455,20 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     }
     int sb = 0;
     while ((1 << sb) < nseg) ++sb;
-    const int mbits = (63 - sb) / 3;
+    // Morton bits per axis: as asked, or about log2(n) / 3 + 3 (cells of a
+    // few triangles at most, so the order the builders start from keeps
+    // neighbours together), never more than the key holds
+    int lg = 0;
+    while (lg < 31 && (1 << lg) < n) ++lg;
+    int mbits = in.morton_bits > 0 ? in.morton_bits : (lg + 2) / 3 + 3;
+    mbits = max(10, min(mbits, (63 - sb) / 3));
+    const int key_bits = 3 * mbits + sb;
     const int threads = 256;
     if (n > 0) {
         const int grid_pts = min((n + threads - 1) / threads, in.sm_count * 8);
         k_prep<<<grid_pts, threads, 0, st>>>(in.verts, in.idx, n, in.seg_of_tri, nseg, in.shade, blo, bhi, cbounds);
         k_morton<<<grid_pts, threads, 0, st>>>(blo, bhi, n, in.seg_of_tri, nseg, mbits, cbounds, keys, vals);
-        cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, 64, st);
+        cub::DeviceRadixSort::SortPairs(cub_temp, cub_bytes, keys, keys2, vals, vals2, n, 0, key_bits, st);
         const int g = (n + threads - 1) / threads;
         k_leaf_boxes<<<g, threads, 0, st>>>(vals2, n, blo, bhi, llo, lhi);
         if (!ploc) {
@@ -1493,7 +1546,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             A.cur_count = level_count + level;
             A.next_count = level_count + level + 1;
             if (A.dec)
-                k_collapse_level_warp<<<wgrid, 128, 0, st>>>(A);
+                k_collapse_level_group<<<wgrid, 128, 0, st>>>(A);
             else
                 k_collapse_level<<<cgrid, 64, 0, st>>>(A);
         }

@@ -19,6 +19,7 @@ struct BuildInputs {
     int32_t sm_count;
     int32_t *host_scratch;    // pinned host, >= 5 + kMaxDepth ints
     int32_t builder = kBuilderPloc;   // binary tree: kBuilderLbvh or kBuilderPloc
+    int32_t morton_bits = 0;          // bits per axis of the sort key (0: from ntris)
     // several scenes in one build (a batch): segment of each triangle and
     // the triangle offset of each segment (nseg + 1 entries, host or device).
     // nseg <= 1: a single scene, both may be nullptr.  Segment s's root is

@@ -401,6 +401,45 @@ def test_builders_agree(rtlib, which):
     assert n1 <= n0 * 1.10
 
 
+@pytest.mark.parametrize("builder", ["lbvh", "ploc"])
+def test_morton_bits_do_not_change_results(rtlib, builder):
+    """The Morton code width the sort orders (RT_OPT_MORTON_BITS: 10, 21, or
+    sized from the triangle count) shapes the tree but not its answers:
+    hits, occlusion and frames identical, every triangle in one leaf slot."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.instances_scene(n_inst=120, xres=160, yres=90)
+    rng = np.random.default_rng(5)
+    v = scene["verts"].astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    o = rng.uniform(lo, hi, size=(20000, 3)).astype(np.float32)
+    d = rng.normal(size=(20000, 3))
+    d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
+    rays = rtlib.rays_array(o, d, tmax=np.float32(4.0))
+    out = []
+    for bits in (0, 10, 21):
+        c = rtlib.Context(0)
+        c.set_option(rtlib.RT_OPT_BUILDER, rtlib.RT_BUILDER_LBVH if builder == "lbvh" else rtlib.RT_BUILDER_PLOC)
+        c.set_option(rtlib.RT_OPT_MORTON_BITS, bits)
+        sc = rtlib.Scene(c, scene)
+        st = sc.stats()
+        assert sum(k * n for k, n in zip((1, 2, 3), st["leaf_tris"])) == scene["tris"].shape[0]
+        r = sc.render(frame, want_ids=True)
+        assert r["stats"].status == 0
+        out.append((sc.closest(rays), sc.any(rays), r["rgb"].copy(), r["ids"].copy()))
+        sc.close()
+        c.close()
+    for h, a, rgb, ids in out[1:]:
+        assert np.array_equal(h["tri"], out[0][0]["tri"]) and np.array_equal(h["t"], out[0][0]["t"])
+        assert np.array_equal(a, out[0][1])
+        assert np.array_equal(rgb, out[0][2]) and np.array_equal(ids, out[0][3])
+    with pytest.raises(rtlib.RtError):
+        c = rtlib.Context(0)
+        try:
+            c.set_option(rtlib.RT_OPT_MORTON_BITS, 9)
+        finally:
+            c.close()
+
+
 def test_builder_option_rejects_unknown(rtlib):
     c = rtlib.Context(0)
     with pytest.raises(rtlib.RtError):
