@@ -1441,7 +1441,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     if ((size_t)(p - (char *)temp) > temp_bytes) { R.status = -3; return R; }
 
     // segment offsets (sorted positions of each segment = its triangle range)
-    int32_t *h_cnt = in.host_scratch;   // pinned, >= 4 ints
+    int32_t *h_cnt = in.host_scratch;   // pinned, >= 6 + kMaxDepth ints
     std::vector<int> init_bounds(6 * (size_t)nseg);
     for (int s = 0; s < nseg; ++s)
         for (int k = 0; k < 3; ++k) { init_bounds[6 * s + k] = 0x7fffffff; init_bounds[6 * s + 3 + k] = (int)0x80000000; }
@@ -1510,6 +1510,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             }
             cudaMemcpyAsync(h_cnt, pstate, kStWords * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+            if (h_cnt[kStError]) { R.status = -6; return R; }
             finished = h_cnt[kStCount + (it & 1)] <= h_cnt[kStTarget];
             tail = !finished && h_cnt[kStCount + (it & 1)] <= kPlocTailMax;
             if (!finished && !tail && it >= kPlocMaxIterations) { R.status = -6; return R; }
@@ -1552,7 +1553,11 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         }
         cudaMemcpyAsync(h_cnt, counters, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(h_cnt + 4, level_count, (kMaxDepth + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        // the clustering's error word (the in-block tail's iteration cap),
+        // read with the first group of levels
+        if (ploc) cudaMemcpyAsync(h_cnt + 5 + kMaxDepth, pstate + kStError, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) { R.status = -2; return R; }
+        if (ploc && h_cnt[5 + kMaxDepth]) { R.status = -6; return R; }
         if (level >= kMaxDepth || h_cnt[4 + level] == 0 || h_cnt[3]) break;
     }
     if (h_cnt[3]) { R.status = -8; return R; }

@@ -17,7 +17,7 @@ struct BuildInputs {
     PackedTri *tris;          // device out, ntris
     int32_t max_nodes;
     int32_t sm_count;
-    int32_t *host_scratch;    // pinned host, >= 5 + kMaxDepth ints
+    int32_t *host_scratch;    // pinned host, >= 6 + kMaxDepth ints
     int32_t builder = kBuilderPloc;   // binary tree: kBuilderLbvh or kBuilderPloc
     int32_t morton_bits = 0;          // bits per axis of the sort key (0: from ntris)
     // several scenes in one build (a batch): segment of each triangle and
