@@ -238,21 +238,58 @@ def run_reference(args):
 NCU_SUMMARY = os.path.join(ROOT, "profiles", "k_render_terrain-2M-1080p_ncu.md")
 
 
-def ncu_traffic():
-    """DRAM bytes (read + write) of one k_render launch on this workload, from
-    the committed ncu summary (a capture cannot run inside the timed bench)."""
+def ncu_metric_sum(names):
+    """Sum of byte counters of one k_render launch on this workload, from the
+    committed ncu summary (a capture cannot run inside the timed bench), or
+    None when any is missing."""
     scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
     total, seen = 0.0, 0
     try:
         for line in open(NCU_SUMMARY):
-            for name in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            for name in names:
                 if line.startswith(f"| `{name}` |"):
                     value, unit = line.split("|")[2].split()
                     total += float(value) * scale[unit]
                     seen += 1
     except (OSError, ValueError, KeyError):
         return None
-    return total if seen == 2 else None
+    return total if seen == len(names) else None
+
+
+def ncu_traffic():
+    """DRAM bytes (read + write) of one k_render launch."""
+    return ncu_metric_sum(("dram__bytes_read.sum", "dram__bytes_write.sum"))
+
+
+def l2_copy_peak(stream):
+    """L2-resident copy bandwidth measured here (GB/s, bytes read + bytes
+    written): two 24 MB buffers, far inside the 129 MB L2, copied back and
+    forth 64 times in one CUDA graph (a single copy lasts only microseconds,
+    so separate launches would measure their own gaps), best of 10 replays
+    -- the L2 counterpart of the HBM copy figure the roofline uses."""
+    import torch
+    n = 24 * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    reps = 64
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            b.copy_(a)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for k in range(reps):
+                (b if k % 2 == 0 else a).copy_(a if k % 2 == 0 else b)
+        g.replay()
+        best = float("inf")
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / reps)
+    del g, a, b
+    return 2 * n * 4 / (best / 1e3) / 1e9
 
 
 # The extra workloads by name: (function, uses the L2 flush, steps from --steps).
@@ -384,6 +421,16 @@ def main():
     hits = st.primary_hits
     alg_bytes = nodes_per_frame * 80 + tris_per_frame * 48 + hits * (32 + 12 + 36) + W * H * 3
     achieved = alg_bytes / (mean_kernel_ms / 1e3) / 1e9
+    # L2-referenced view: coherent rays re-read the upper tree levels from
+    # L1/L2, so the same algorithmic bytes and the L2 traffic ncu counted
+    # are set against the measured L2 copy bandwidth too
+    l2_peak = l2_copy_peak(stream)
+    l2_traffic = ncu_metric_sum(("lts__t_bytes.sum",)) if args.size == 1024 else None
+    l2 = {"peak": l2_peak, "unit": "GB/s", "peak_source": "measured in this run (L2-resident copy)",
+          "achieved": achieved, "frac": achieved / l2_peak, "traffic": l2_traffic,
+          "traffic_gbs": l2_traffic / (mean_kernel_ms / 1e3) / 1e9 if l2_traffic else None,
+          "traffic_frac": l2_traffic / (mean_kernel_ms / 1e3) / 1e9 / l2_peak if l2_traffic else None,
+          "traffic_source": "lts__t_bytes.sum of the same launch in profiles/k_render_terrain-2M-1080p_ncu.md"}
 
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
@@ -401,7 +448,7 @@ def main():
                          "traffic_source": "profiles/k_render_terrain-2M-1080p_ncu.md (one launch, ncu --set full)",
                          "kernel": "k_render<false>", "peak_source": peak_src,
                          "bytes_per_frame": alg_bytes, "nodes_per_ray": nodes_per_frame / frame_rays,
-                         "tris_per_ray": tris_per_frame / frame_rays, "kernel_ms": mean_kernel_ms},
+                         "tris_per_ray": tris_per_frame / frame_rays, "kernel_ms": mean_kernel_ms, "l2": l2},
             "clocks": clk}
     if not args.no_workloads:
         sc.close()
