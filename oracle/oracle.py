@@ -18,6 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "librtoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libraptor_ref.so")
+# the reference built with soft shadows on (SOFT_SHADOW = REF_SOFT_SAMPLES)
+REF_SOFT_SAMPLES = 16
+REF_SOFT_SO = os.path.join(HERE, "_ref", f"libraptor_ref_soft{REF_SOFT_SAMPLES}.so")
 # RAPTor source tree (the directory holding common/ and raytracer/); the
 # RAPTOR_REF environment variable overrides the default checkout location.
 REF_SRC = os.environ.get("RAPTOR_REF", "/root/reference/RAPTor")
@@ -31,7 +34,7 @@ class Camera(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
-                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float)]
+                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float), ("r", C.c_float)]
 
 
 class Material(C.Structure):
@@ -80,6 +83,7 @@ def make_lights(ls):
         arr[i].d = d["d"]
         arr[i].s_a = d.get("s_a", 0.0)
         arr[i].s_b = d.get("s_b", 0.0)
+        arr[i].r = d.get("r", 0.0)
     return arr
 
 
@@ -111,6 +115,8 @@ def build(verbose: bool = False) -> None:
     if os.path.isdir(REF_SRC) and platform.machine() in ("x86_64", "AMD64"):
         subprocess.run(["make", "-s", "-C", os.path.join(HERE, "refbuild"), f"REF={REF_SRC}", "-j8"], check=True,
                        capture_output=not verbose)
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "refbuild"), f"REF={REF_SRC}",
+                        f"SOFT={REF_SOFT_SAMPLES}", "-j8"], check=True, capture_output=not verbose)
 
 
 def _p(a, t):
@@ -214,6 +220,16 @@ def oracle_lib():
                                         C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _U8, _I, _I]
         lib["ro_ao_rays"].argtypes = [_F, _F, C.c_uint32, C.c_int32, C.c_uint32, _F, _F]
         lib["ro_philox4x32"].argtypes = [_U32, C.c_uint32, C.c_uint32, _U32]
+        lib["ro_render_soft"].restype = C.c_int64
+        lib["ro_render_soft"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
+                                          C.POINTER(Material), C.c_int32, C.c_int32, C.c_int64, C.c_int32, _U8, _I,
+                                          _F, C.POINTER(C.c_int64)]
+        lib["ro_ref_random"].restype = None
+        lib["ro_ref_random"].argtypes = [C.c_int64, C.c_int32, _F]
+        lib["ro_lut_cos"].restype = C.c_float
+        lib["ro_lut_cos"].argtypes = [C.c_float]
+        lib["ro_lut_sin"].restype = C.c_float
+        lib["ro_lut_sin"].argtypes = [C.c_float]
         lib["ro_pixel_secondary_rays"].restype = C.c_int32
         lib["ro_pixel_secondary_rays"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
                                                    C.c_int32, C.c_float, C.c_uint32, C.c_int32, C.c_int32, _I, _F,
@@ -226,10 +242,37 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
+_ref_soft = None
+
+
+def ref_soft_lib():
+    """The reference built with SOFT_SHADOW = REF_SOFT_SAMPLES (x86 only).
+    Its random generator is process-wide: every soft frame it renders moves
+    it on."""
+    global _ref_soft
+    if _ref_soft is None:
+        lib = _load_ref(REF_SOFT_SO)
+        lib["rref_random"].restype = None
+        lib["rref_random"].argtypes = [C.c_int32, _F]
+        lib["rref_lut_cos"].restype = C.c_float
+        lib["rref_lut_cos"].argtypes = [C.c_float]
+        lib["rref_lut_sin"].restype = C.c_float
+        lib["rref_lut_sin"].argtypes = [C.c_float]
+        lib["rref_soft_shadow_samples"].restype = C.c_int32
+        _ref_soft = lib
+    return _ref_soft
+
+
 def ref_lib():
     global _ref
     if _ref is None:
-        lib = _Lib(REF_SO)
+        _ref = _load_ref(REF_SO)
+    return _ref
+
+
+def _load_ref(path):
+    if True:
+        lib = _Lib(path)
         _declare(lib, "rref_")
         lib["rref_scene_create"].restype = C.c_void_p
         lib["rref_scene_create"].argtypes = [_F, C.c_int32, _I, C.c_int32, _F, _U32, C.POINTER(Material)]
@@ -251,8 +294,7 @@ def ref_lib():
         lib["rref_render_tone_mapped"].restype = C.c_double
         lib["rref_render_tone_mapped"].argtypes = [C.c_void_p, C.POINTER(Camera), C.c_int32, C.c_int32,
                                                    C.POINTER(Light), C.c_int32, C.POINTER(ToneMap), _U8]
-        _ref = lib
-    return _ref
+    return lib
 
 
 def _scene_arrays(scene):
@@ -293,6 +335,25 @@ class OracleScene(_SceneBase):
 
     def node_count(self):
         return self.lib["ro_scene_node_count"](self.h)
+
+    def render_soft(self, frame, samples, stream_offset=0, threads=1, want_ids=False, want_float=False):
+        """ro_render_soft: the whole frame with `samples` soft-shadow rays per
+        spherical light, drawing the reference's random stream from position
+        stream_offset.  frame["materials"] or frame["material"]."""
+        cam = make_camera(frame["camera"])
+        W, H = cam.xres, cam.yres
+        rgb = np.zeros((H, W, 3), np.uint8)
+        ids = np.full((H, W), -2, np.int32) if want_ids else None
+        fimg = np.zeros((H, W, 3), np.float32) if want_float else None
+        ls = make_lights(frame["lights"])
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        end = C.c_int64(0)
+        n = self.lib["ro_render_soft"](self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table), int(samples),
+                                       int(stream_offset), threads, _p(rgb, C.c_uint8), _p(ids, C.c_int32),
+                                       _p(fimg, C.c_float), C.byref(end))
+        if n < 0:
+            raise ValueError("oracle soft-shadow render refused its arguments")
+        return {"rgb": rgb, "ids": ids, "fimg": fimg, "rays": n, "stream_end": end.value}
 
     def pixel_secondary_rays(self, frame, x, y):
         """(primary hit id, ogn, dir, tmax) of the secondary rays pixel
@@ -351,10 +412,11 @@ class RefScene(_SceneBase):
     """The reference's own bvh + ray_tracer behind the harness (x86 only)."""
     prefix = "rref_"
 
-    def __init__(self, scene, material):
+    def __init__(self, scene, material, soft=False):
         """material: one material dict, or a list of them indexed by
-        scene["mat_of_tri"] (one coloured_mapper_shader per entry)."""
-        self.lib = ref_lib()
+        scene["mat_of_tri"] (one coloured_mapper_shader per entry).  soft:
+        the reference built with soft shadows (ref_soft_lib)."""
+        self.lib = ref_soft_lib() if soft else ref_lib()
         v, t, a, f = _scene_arrays(scene)
         self._keep = (v, t, a, f)
         if isinstance(material, (list, tuple)):
@@ -505,6 +567,14 @@ def ao_rays(hit_point, geo_normal, pixel, nsamples, seed):
     lib["ro_ao_rays"](_p(hp, C.c_float), _p(gn, C.c_float), pixel, nsamples, seed, _p(ogn, C.c_float),
                       _p(dirs, C.c_float))
     return ogn, dirs
+
+
+def ref_random(start, n):
+    """n numbers of the reference's random stream from position start (the
+    restatement, ro_ref_random)."""
+    out = np.empty(n, np.float32)
+    oracle_lib()["ro_ref_random"](int(start), int(n), _p(out, C.c_float))
+    return out
 
 
 def philox(ctr, key0, key1):

@@ -227,9 +227,9 @@ double rref_render_tone_mapped(void *h, const ro_camera *c, int32_t aa_x, int32_
         if (ls[i].kind == 1)
             lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
         else if (ls[i].kind == 2)   // spot light (light.h:24-25)
-            lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, 0.0f);
+            lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, ls[i].r);
         else
-            lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
+            lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, ls[i].r);
     }
     null_buf nb;
     std::streambuf *old = std::cout.rdbuf(&nb);
@@ -339,9 +339,9 @@ int64_t rref_parse_and_render(const char *path, int32_t kind, const ro_camera *c
             if (ls[i].kind == 1)
                 lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
             else if (ls[i].kind == 2)
-                lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, 0.0f);
+                lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, ls[i].r);
             else
-                lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, 0.0f);
+                lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, ls[i].r);
         }
         null_buf nb;
         std::streambuf *old = std::cout.rdbuf(&nb);
@@ -352,5 +352,19 @@ int64_t rref_parse_and_render(const char *path, int32_t kind, const ro_camera *c
     for (material *m : mats) delete m;
     return n;
 }
+
+// The reference's own random stream (common/common.cc:35-105): the next n
+// numbers of the process-wide generator, which soft shadows draw from.
+void rref_random(int32_t n, float *out)
+{
+    for (int32_t i = 0; i < n; ++i) out[i] = gen_random_mersenne_twister();
+}
+
+// The reference's cosine table (common.h:171-209) as light::find_rays reads it.
+float rref_lut_cos(float a) { return cos_lut.get_cos(a); }
+float rref_lut_sin(float a) { return cos_lut.get_sin(a); }
+
+// Shadow rays per light of a primary hit in this build (SOFT_SHADOW, or 1).
+int32_t rref_soft_shadow_samples(void) { return SHADOW_ARRAY_SIZE; }
 
 }  // extern "C"

@@ -525,6 +525,13 @@ static inline v3 offset_start_in(v3 dst, v3 geo)
               offset_coord_d(dst.z, geo.z, -1.0f));
 }
 
+/* A light light::find_rays treats as directional (light.h:65): not the
+ * spherical / triangle constructors' n = (2, 2, 2), and no spot cone. */
+static inline int light_is_directional(const ro_light *L)
+{
+    return L->kind == 1 || (L->kind == 2 && L->s_b == 0.0f);
+}
+
 /* Light direction sign for directional lights (light.h:172-219): the light
  * sits at +/-1e15 along n by the sign of n's major component. */
 static float dir_light_dist(v3 n)
@@ -542,7 +549,7 @@ static float dir_light_dist(v3 n)
 static inline void shadow_ray(const ro_light *L, v3 start, ro_ray *r, float *len)
 {
     v3 target;
-    if (L->kind == 1) {
+    if (light_is_directional(L)) {
         const v3 n = ld3(L->dir);
         target = vadd(start, vmul(n, dir_light_dist(n)));
     } else {
@@ -573,9 +580,115 @@ typedef struct {
     float ao_dist;
     uint32_t ao_seed;
     int32_t *ao_count;
+    /* soft shadows (ro_render_soft): shadow rays per spherical light, the
+     * frame's slice of the reference's random stream and, per pixel, the
+     * index in it of the pixel's first number */
+    int32_t soft_n;
+    const float *stream;
+    const int64_t *px_draw;
     int32_t next_row;
     pthread_mutex_t *lock;
 } render_job;
+
+/* ------------------------------------------------------ Soft shadows */
+
+#define RO_PI 3.1415926535897932384626433f   /* common/common.cc:10 */
+#define RO_COS_LUT_SIZE 16384                  /* COS_LUT_SIZE, common/common.h:109-111 */
+
+/* static_cos (common/common.h:171-209): cos of size evenly spaced angles,
+ * the angle rounded to binary32 and its cosine taken in double. */
+static float g_cos_lut[RO_COS_LUT_SIZE];
+static pthread_once_t g_cos_lut_once = PTHREAD_ONCE_INIT;
+static void build_cos_lut(void)
+{
+    for (int32_t i = 0; i < RO_COS_LUT_SIZE; ++i)
+        g_cos_lut[i] = (float)cos((double)((((float)i * 2.0f) * RO_PI) / (float)RO_COS_LUT_SIZE));
+}
+
+/* static_cos::get_cos / get_sin: the index truncates toward zero and wraps
+ * modulo the table size (the unsigned conversion of a negative angle). */
+static inline float lut_cos(float a)
+{
+    const float v = ((1.0f / (2.0f * RO_PI)) * (float)RO_COS_LUT_SIZE) * a;
+    return g_cos_lut[(uint32_t)(int64_t)v & (RO_COS_LUT_SIZE - 1)];
+}
+static inline float lut_sin(float a) { return lut_cos(a - (RO_PI / 2.0f)); }
+
+float ro_lut_cos(float a) { pthread_once(&g_cos_lut_once, build_cos_lut); return lut_cos(a); }
+float ro_lut_sin(float a) { pthread_once(&g_cos_lut_once, build_cos_lut); return lut_sin(a); }
+
+/* The reference's random generator (common/common.cc:35-105): a Mersenne
+ * twister seeded with 5489 whose refill updates words 0..622 only, tempered
+ * and scaled to [0, 1] in binary32. */
+typedef struct { uint32_t mt[624]; int32_t idx; } ref_rng;
+
+static void ref_rng_init(ref_rng *g)
+{
+    g->mt[0] = 5489u;
+    for (int i = 1; i < 624; ++i) g->mt[i] = 1812433253u * (g->mt[i - 1] ^ (g->mt[i - 1] >> 30)) + (uint32_t)i;
+    g->idx = 624;
+}
+
+static void ref_rng_refill(ref_rng *g)
+{
+    uint32_t *mt = g->mt;
+    for (int i = 0; i < 227; ++i) {
+        const uint32_t y = (0x80000000u & mt[i]) + (0x7FFFFFFFu & mt[i + 1]);
+        mt[i] = mt[i + 397] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    for (int i = 227; i < 623; ++i) {
+        const uint32_t y = (0x80000000u & mt[i]) + (0x7FFFFFFFu & mt[i + 1]);
+        mt[i] = mt[i - 227] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    g->idx = 0;
+}
+
+static inline float ref_rng_next(ref_rng *g)
+{
+    if (g->idx >= 624) ref_rng_refill(g);
+    uint32_t y = g->mt[g->idx++];
+    y ^= (y >> 11);
+    y ^= ((y << 7) & 0x9d2c5680u);
+    y ^= ((y << 15) & 0xefc60000u);
+    y ^= (y >> 18);
+    return (float)y * (1.0f / 4294967296.0f);
+}
+
+void ro_ref_random(int64_t start, int32_t n, float *out)
+{
+    ref_rng g;
+    ref_rng_init(&g);
+    for (int64_t i = 0; i < start; ++i) (void)ref_rng_next(&g);
+    for (int32_t i = 0; i < n; ++i) out[i] = ref_rng_next(&g);
+}
+
+/* Numbers one primary hit draws for light L with n soft-shadow rays: three
+ * per ray of a spherical (point or spot) light, none otherwise. */
+static inline int32_t soft_draws(const ro_light *L, int32_t n)
+{
+    return (n > 1 && !light_is_directional(L)) ? 3 * n : 0;
+}
+
+/* Shadow ray i of n to spherical light L (light::find_rays, light.h:102-128):
+ * a random offset of the light's centre drawn from rnd[0..2] (angles a and b,
+ * radius), then ray::set_up(start, centre + offset) (ray.h:44-54). */
+static void soft_ray(const ro_light *L, v3 start, int32_t n, int32_t i, const float *rnd, ro_ray *r, float *len)
+{
+    const float a_scale = 1.0f / (float)((n >> 4) + ((n & 0xe) != 0) + 1);
+    const float b_scale = 1.0f / (float)((n >> 4) + ((n & 0xc) != 0) + 1);
+    const float r_scale = 1.0f / (float)((n >> 4) + ((n & 0x8) != 0) + 1);
+    const int32_t eighths = (i >> 2) & ~0x1;
+    const float a_off = (rnd[0] * (a_scale * (float)(eighths + (i & 0x1)))) * (2.0f * RO_PI);
+    const float b_off = (rnd[1] * (b_scale * (float)(eighths + (i & 0x2)))) * (2.0f * RO_PI);
+    const float r_off = (rnd[2] * (r_scale * (float)(eighths + (i & 0x4)))) * L->r;
+    const float sin_a = lut_sin(a_off), cos_a = lut_cos(a_off);
+    const float sin_b = lut_sin(b_off), cos_b = lut_cos(b_off);
+    const v3 off = mk((r_off * cos_a) * sin_b, (r_off * sin_a) * sin_b, r_off * cos_b);
+    const v3 d = vsub(vadd(ld3(L->pos), off), start);
+    *len = vmag(d);
+    r->o = start;
+    r->d = vdivs(d, *len);
+}
 
 /* Hit-point refinement + face-forwarding (raytracer.cc:30-31 and
  * triangle::normal_at_point, triangle.h:464-498), then the interpolated
@@ -675,15 +788,33 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
         *out = c;
         return id;
     }
+    int64_t draw = (first && J->soft_n > 1) ? J->px_draw[pix] : 0;
     for (int32_t l = 0; l < J->nlights; ++l) {
         const ro_light *L = &J->lights[l];
         ro_ray sr;
         float len;
-        shadow_ray(L, start, &sr, &len);
-        const int occ = nearer(s, &sr, len);
-        J->rays += 1;
-        if (first && J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
-        const float lmagn = occ ? 0.0f : 1.0f;   /* made_it / nr_pending_shadows */
+        int32_t nrays = 1, made = 0;
+        if (first && soft_draws(L, J->soft_n) > 0) {
+            /* soft shadows: n rays to random points of the light, shaded with
+             * the first one's direction and length (raytracer.cc:44-64) */
+            nrays = J->soft_n;
+            for (int32_t i = 0; i < nrays; ++i) {
+                ro_ray ri;
+                float li;
+                soft_ray(L, start, nrays, i, J->stream + draw + 3 * i, &ri, &li);
+                if (i == 0) { sr = ri; len = li; }
+                if (!nearer(s, &ri, li)) ++made;
+            }
+            draw += 3 * nrays;
+            J->rays += nrays;
+        } else {
+            shadow_ray(L, start, &sr, &len);
+            const int occ = nearer(s, &sr, len);
+            made = !occ;
+            J->rays += 1;
+            if (first && J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
+        }
+        const float lmagn = (float)made / (float)nrays;   /* made_it / nr_pending_shadows */
         const float shade = vdot(sr.d, sn);
         if (shade < 0.0f) continue;
         const v3 ref = vsub(sr.d, vmul(sn, 2.0f * shade));
@@ -823,6 +954,96 @@ int64_t ro_render_mt(const ro_scene *s, const ro_camera *cam, const ro_light *li
     J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mats; J.mats = mats; J.nmats = nmats;
     J.row0 = row0; J.row1 = row1; J.rgb = rgb; J.hit_id = hit_id; J.occl = occl; J.fimg = fimg;
     return run_render(&J, nthreads);
+}
+
+/* Pass 1 of a soft-shadow frame: 1 per pixel whose camera ray hits. */
+typedef struct {
+    const ro_scene *s;
+    const ro_camera *cam;
+    uint8_t *hit;
+    int32_t next_row;
+    pthread_mutex_t *lock;
+} hit_job;
+
+static void *hit_worker(void *arg)
+{
+    hit_job *H = (hit_job *)arg;
+    const cam_state cs = cam_setup(H->cam);
+    for (;;) {
+        pthread_mutex_lock(H->lock);
+        const int32_t y = H->next_row++;
+        pthread_mutex_unlock(H->lock);
+        if (y >= H->cam->yres) break;
+        for (int32_t x = 0; x < H->cam->xres; ++x) {
+            const ro_ray r = cam_ray(&cs, x, y);
+            ro_hit h;
+            (void)closest(H->s, &r, &h);
+            H->hit[(size_t)x + (size_t)y * (size_t)H->cam->xres] = (uint8_t)(h.d < RO_MAX_DIST);
+        }
+    }
+    return NULL;
+}
+
+int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                       const ro_material *mats, int32_t nmats, int32_t samples, int64_t stream_offset,
+                       int32_t nthreads, uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *stream_end)
+{
+    if (!s || !s->nodes || !cam || !mats || nmats < 1 || !rgb || samples < 1 || samples > 64 ||
+        stream_offset < 0 || nlights < 0 || (nlights > 0 && !lights))
+        return -1;
+    for (int32_t i = 0; i < nmats; ++i)
+        if (mats[i].rf > 0.0f || mats[i].tran > 0.0f) return -1;
+    if (s->mat)
+        for (int32_t i = 0; i < s->ntris; ++i)
+            if (s->mat[i] < 0 || s->mat[i] >= nmats) return -1;
+    pthread_once(&g_cos_lut_once, build_cos_lut);
+    const size_t npix = (size_t)cam->xres * (size_t)cam->yres;
+    uint8_t *hit = (uint8_t *)malloc(npix ? npix : 1);
+    int64_t *px_draw = (int64_t *)malloc((npix ? npix : 1) * sizeof(int64_t));
+    if (!hit || !px_draw) { free(hit); free(px_draw); return -1; }
+    /* pass 1: which pixels hit */
+    {
+        pthread_mutex_t lock;
+        pthread_mutex_init(&lock, NULL);
+        hit_job H = {s, cam, hit, 0, &lock};
+        if (nthreads < 1) nthreads = 1;
+        if (nthreads > 256) nthreads = 256;
+        pthread_t th[256];
+        int started = 0;
+        for (int i = 1; i < nthreads; ++i)
+            if (pthread_create(&th[started], NULL, hit_worker, &H) == 0) ++started;
+        hit_worker(&H);
+        for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+        pthread_mutex_destroy(&lock);
+    }
+    /* each hit pixel draws the same count, in pixel order (x + y * xres:
+     * ray_tracer's loops, y outer, raytracer.cc:586-592) */
+    int32_t per_hit = 0;
+    for (int32_t l = 0; l < nlights; ++l) per_hit += soft_draws(&lights[l], samples);
+    int64_t total = 0;
+    for (size_t p = 0; p < npix; ++p) {
+        px_draw[p] = total;
+        total += hit[p] ? per_hit : 0;
+    }
+    float *stream = (float *)malloc((size_t)(total > 0 ? total : 1) * sizeof(float));
+    if (!stream) { free(hit); free(px_draw); return -1; }
+    {
+        ref_rng g;
+        ref_rng_init(&g);
+        for (int64_t i = 0; i < stream_offset; ++i) (void)ref_rng_next(&g);
+        for (int64_t i = 0; i < total; ++i) stream[i] = ref_rng_next(&g);
+    }
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mats; J.mats = mats; J.nmats = nmats;
+    J.row0 = 0; J.row1 = cam->yres; J.rgb = rgb; J.hit_id = hit_id; J.fimg = fimg;
+    J.soft_n = samples; J.stream = stream; J.px_draw = px_draw;
+    const int64_t rays = run_render(&J, nthreads);
+    free(stream);
+    free(px_draw);
+    free(hit);
+    if (stream_end) *stream_end = stream_offset + total;
+    return rays;
 }
 
 int32_t ro_scene_set_normals(ro_scene *s, const float *corner_normals)

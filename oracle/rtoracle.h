@@ -49,6 +49,7 @@ typedef struct ro_light {
     float dir[3];
     float d;
     float s_a, s_b;   /* kind 2 (spot light at pos, axis dir): cone angles, light.h:24-25 */
+    float r;          /* kinds 0 and 2: radius of the spherical light (light.h:17-25); used by soft shadows */
 } ro_light;
 
 /* Coloured-mapper Phong material (materials/coloured_mapper_shader.h): ka,
@@ -151,6 +152,29 @@ int64_t ro_render_ao(const ro_scene *s, const ro_camera *cam, const ro_material 
 int32_t ro_pixel_secondary_rays(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
                                 int32_t ao_n, float ao_dist, uint32_t ao_seed, int32_t x, int32_t y,
                                 int32_t *hit_id, float *ogn, float *dir, float *tmax);
+
+/* Soft shadows as the reference renders them when built with
+ * SOFT_SHADOW = samples (ray.cc:91-104, light.h:62-128, raytracer.cc:44-64):
+ * every primary hit sends `samples` shadow rays to random points of each
+ * spherical light (kinds 0 and 2 with a cone; radius r) -- three numbers of
+ * the reference's random stream per ray, drawn in pixel order (x + y * xres)
+ * and light order -- and one ray to each directional light; a light's term
+ * is shaded with its first ray's direction and length and weighted by the
+ * unoccluded fraction.  stream_offset: how many numbers the reference's
+ * generator had produced before the frame; stream_end (nullable) receives
+ * the count after it.  Materials without reflection or refraction (-1
+ * otherwise).  Whole frame; returns rays traced. */
+int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                       const ro_material *mats, int32_t nmats, int32_t samples, int64_t stream_offset,
+                       int32_t nthreads, uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *stream_end);
+
+/* n numbers of the reference's random stream (common/common.cc:35-105)
+ * from position start of a freshly seeded generator. */
+void ro_ref_random(int64_t start, int32_t n, float *out);
+
+/* The reference's cosine table lookups (common/common.h:171-209). */
+float ro_lut_cos(float a);
+float ro_lut_sin(float a);
 
 /* The AO ray set for one hit (exposed so tests can trace single rays). */
 void ro_ao_rays(const float hit_point[3], const float geo_normal[3], uint32_t pixel, int32_t nsamples,

@@ -15,6 +15,11 @@ It writes
                     oracle/refbuild/Makefile) on small seeded scenes, also
                     with the camera's anti-aliasing factors (2x2, 3x2) and
                     with a reflective material
+  ref_soft.npz      the reference built with soft shadows (SOFT_SHADOW =
+                    16): the head of its random stream, its cosine table on
+                    angles that reach every entry, and its soft-shadow frames
+                    rendered one after another from a freshly started
+                    generator (written by a fresh process, `--soft`)
 The tests compare the C restatement (oracle/rtoracle.c) and the CUDA core
 against these files; nothing at test time reads the reference tree.
 """
@@ -278,10 +283,70 @@ def mesh_files():
     return out
 
 
+def soft_cases():
+    """(name, scene, frame) of the soft-shadow fixtures: spherical point
+    lights of several radii, one with a directional light beside it, a spot
+    light with a radius, and a terrain."""
+    from raptor_gb300 import scenes
+    s, f = scenes.icosphere_scene(freq=8, res=96)
+    pl = dict(f["lights"][0], r=0.8)
+    sun = scenes.directional_light((-0.4, -0.8, -0.3))
+    spot = dict(scenes.spot_light((2.0, 4.0, 2.0), (-0.4, -0.8, -0.4), 0.2, 0.5), r=0.6)
+    t, tf = scenes.terrain_scene(size_pow2=64, xres=120, yres=68)
+    return [("ico-point", s, dict(f, lights=[pl])),
+            ("ico-point-dir", s, dict(f, lights=[pl, sun])),
+            ("ico-spot-point", s, dict(f, lights=[spot, dict(pl, pos=(-3.0, 4.0, 1.0), r=1.5)])),
+            ("terrain-point-dir", t, dict(tf, lights=[dict(scenes.point_light((300.0, 260.0, 500.0)), r=40.0),
+                                                      tf["lights"][0]]))]
+
+
+def soft_main():
+    """ref_soft.npz, in a process whose reference generator is untouched."""
+    import ctypes as C
+    import oracle as O
+    lib = O.ref_soft_lib()
+    samples = lib["rref_soft_shadow_samples"]()
+    arrays = {"samples": np.array([samples], np.int32)}
+    head = np.empty(4096, np.float32)
+    lib["rref_random"](head.shape[0], head.ctypes.data_as(C.POINTER(C.c_float)))
+    arrays["stream_head"] = head
+    n = 16384
+    ang = np.concatenate([(np.arange(n, dtype=np.float64) + 0.5) * (2 * np.pi / n),
+                          np.random.default_rng(5).uniform(-20.0, 20.0, 20000)]).astype(np.float32)
+    arrays["lut_angles"] = ang
+    arrays["lut_cos"] = np.array([lib["rref_lut_cos"](float(a)) for a in ang], np.float32)
+    arrays["lut_sin"] = np.array([lib["rref_lut_sin"](float(a)) for a in ang], np.float32)
+    offset = head.shape[0]
+    cases = soft_cases()
+    for k, (name, s, f) in enumerate(cases):
+        arrays[f"soft{k}_rgb"] = O.RefScene(s, f["material"], soft=True).render(f)["rgb"]
+        arrays[f"soft{k}_frame"] = np.frombuffer(json.dumps(f).encode(), np.uint8)
+        arrays[f"soft{k}_scene"] = np.frombuffer(json.dumps(name).encode(), np.uint8)
+        arrays[f"soft{k}_offset"] = np.array([offset], np.int64)
+        for key in ("verts", "tris", "vattr"):
+            arrays[f"soft{k}_{key}"] = s[key]
+        # the stream position after the frame, as the restatement counts it
+        offset = O.OracleScene(s).render_soft(f, samples, offset, threads=os.cpu_count() or 1)["stream_end"]
+        print(f"soft frame {name}: stream {int(arrays[f'soft{k}_offset'][0])} -> {offset}")
+    # the reference's generator stands exactly where the restatement says
+    tail = np.empty(64, np.float32)
+    lib["rref_random"](64, tail.ctypes.data_as(C.POINTER(C.c_float)))
+    if not np.array_equal(tail, O.ref_random(offset, 64)):
+        raise SystemExit("soft-shadow stream accounting differs from the reference")
+    arrays["stream_end"] = np.array([offset], np.int64)
+    np.savez_compressed(os.path.join(HERE, "ref_soft.npz"), **arrays)
+    print("wrote ref_soft.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("RAPTOR_REF", "/root/reference/RAPTor"))
+    ap.add_argument("--soft", action="store_true", help="write only ref_soft.npz (needs a fresh process)")
     a = ap.parse_args()
+    if a.soft:
+        import oracle as O
+        O.build()
+        return soft_main()
     kats = parse_bih_tests(os.path.join(a.ref, "raytracer/unit_tests/bih_tests.cc"))
     json.dump(kats, open(os.path.join(HERE, "bih_kats.json"), "w"), indent=1)
     mort = parse_morton_tests(os.path.join(a.ref, "raytracer/unit_tests/vint_tests.cc"))
@@ -366,6 +431,9 @@ def main():
                    "soup_occ": occ})
     np.savez_compressed(os.path.join(HERE, "ref_small.npz"), **arrays)
     print("wrote ref_small.npz:", {k: v.shape for k, v in arrays.items()})
+    # the soft-shadow fixtures need the reference's generator untouched
+    import subprocess
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--soft", "--ref", a.ref], check=True)
 
 
 if __name__ == "__main__":
