@@ -82,8 +82,9 @@ typedef struct rt_camera {
  * dir; RT_LIGHT_SPOT: point light at pos whose intensity falls off with the
  * angle a = acos(shadow-ray direction . dir) as clamp(1 - (a - s_a) /
  * (s_b - s_a), 0, 1) (the spot-light constructor and get_light_intensity,
- * light.h:24-25, 44-59; s_b = 0 leaves it a point light).  rgb in 0..255, d
- * the distance drop-off. */
+ * light.h:24-25, 44-59; with s_b = 0 it is a directional light along dir,
+ * as light::find_rays treats it, light.h:65).  rgb in 0..255, d the distance
+ * drop-off. */
 #define RT_LIGHT_POINT 0
 #define RT_LIGHT_DIRECTIONAL 1
 #define RT_LIGHT_SPOT 2
@@ -445,6 +446,35 @@ rt_status rt_render_aa(rt_scene *scene, const rt_camera *camera, int32_t aa_x, i
 rt_status rt_render_ao(rt_scene *scene, const rt_camera *camera, const rt_material *material, int32_t samples,
                        float ao_dist, uint32_t seed, uint8_t *rgb_out, int32_t *hit_ids, int32_t *ao_count,
                        rt_render_stats *stats);
+
+/* ------------------------------------------------------ soft shadows */
+
+#define RT_MAX_SOFT_SAMPLES 64
+
+/* Soft shadows as RAPTor renders them when it is built with SOFT_SHADOW =
+ * samples (ray::find_rays ray.cc:91-104, light::find_rays light.h:62-128,
+ * ray_trace_engine::ray_trace raytracer.cc:44-64): every primary hit sends
+ * `samples` shadow rays to random points of each spherical light
+ * (RT_LIGHT_POINT and RT_LIGHT_SPOT; light_radius[l] is the radius r the
+ * reference's light constructors take, light.h:17-25; NULL: all 0) and one
+ * ray to each directional light; a light's term is shaded with its first
+ * ray's direction and length and weighted by the fraction of its rays that
+ * reach it.  The random points are the reference's own: its process-wide
+ * generator (common/common.cc:35-105) draws three numbers per ray, in pixel
+ * order (x + y * xres) and light order, and stream_offset says how many
+ * numbers it had produced before this frame (0: a freshly started
+ * program); stream_end (nullable) receives the count after the frame, the
+ * next frame's offset.  Frames without mirror or refracting materials
+ * (`materials` as rt_render_materials).  rgb_out (RGB8) and rgb_f32 (the
+ * camera's float image) are nullable, not both, host or device memory.
+ * Runs two passes with one host round trip between them: the camera rays,
+ * then the frame's slice of the random stream (generated on the host and
+ * copied over unless the previous frame's slice already covers it) and the
+ * shading. */
+rt_status rt_render_soft_shadows(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                                 const float *light_radius, const rt_material *materials, int32_t nmaterials,
+                                 int32_t samples, int64_t stream_offset, uint8_t *rgb_out, float *rgb_f32,
+                                 int64_t *stream_end, rt_render_stats *stats);
 
 /* ---------------------------------------------------- differentiation */
 

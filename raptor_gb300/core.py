@@ -148,6 +148,9 @@ SIGNATURES = [
     ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_free", None, [C.POINTER(RtMesh)]),
+    ("rt_render_soft_shadows", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, _P,
+                                           C.POINTER(RtMaterial), C.c_int32, C.c_int32, C.c_int64, _P, _P,
+                                           C.POINTER(C.c_int64), C.POINTER(RtRenderStats)]),
     ("rt_render_image", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
                                     C.c_int32, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
@@ -509,6 +512,27 @@ class Scene:
         _check(lib().rt_render_image(self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table), ptr(fimg),
                                      C.byref(st)))
         return {"fimg": fimg, "stats": st}
+
+    def render_soft(self, frame, samples, stream_offset=0, rgb=None, fimg=None, want_float=False):
+        """rt_render_soft_shadows: `samples` soft-shadow rays per spherical
+        light (radius: each light dict's "r", default 0), drawing the
+        reference's random stream from stream_offset.  rgb / fimg: host
+        arrays or device tensors (allocated on the host when None; fimg
+        only with want_float).  Returns rgb, fimg, stats and stream_end."""
+        cam = make_camera(frame["camera"])
+        if rgb is None:
+            rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
+        if fimg is None and want_float:
+            fimg = np.empty((cam.yres, cam.xres, 3), np.float32)
+        ls = make_lights(frame["lights"])
+        radius = np.array([float(l.get("r", 0.0)) for l in frame["lights"]] or [0.0], np.float32)
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        st = RtRenderStats()
+        end = C.c_int64(0)
+        _check(lib().rt_render_soft_shadows(self.h, C.byref(cam), ls, len(frame["lights"]), ptr(radius), table,
+                                            len(table), int(samples), int(stream_offset), ptr(rgb), ptr(fimg),
+                                            C.byref(end), C.byref(st)))
+        return {"rgb": rgb, "fimg": fimg, "stats": st, "stream_end": end.value}
 
     def render_aa(self, frame, aa_x, aa_y, rgb=None):
         """Anti-aliased frame: aa_x * aa_y rays per output pixel, averaged."""

@@ -130,6 +130,10 @@ LightView make_light_view(const rt_light &l)
     v.d = l.d;
     v.s_a = (v.kind == RT_LIGHT_SPOT) ? l.s_a : 0.0f;
     v.s_b = (v.kind == RT_LIGHT_SPOT) ? l.s_b : 0.0f;
+    // a spot light without a cone is directional to light::find_rays
+    // (light.h:65: n is not the spherical constructor's (2, 2, 2), s_b == 0)
+    if (v.kind == RT_LIGHT_SPOT && l.s_b == 0.0f) v.kind = RT_LIGHT_DIRECTIONAL;
+    v.radius = 0.0f;
     // light::find_major_direction (light.h:172-219)
     const float nx = l.dir[0], ny = l.dir[1], nz = l.dir[2];
     bool neg;
@@ -265,6 +269,7 @@ rt_status rt_ctx_destroy(rt_context *ctx)
     ctx->stage_b.release();
     ctx->stage_c.release();
     ctx->redo.release();
+    soft_release(ctx);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->h_scratch) cudaFreeHost(ctx->h_scratch);

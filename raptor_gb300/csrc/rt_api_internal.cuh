@@ -32,6 +32,10 @@ rt_status status_to_error(uint32_t st);
 void noalloc_context_opened(int device);
 void noalloc_context_closed(int device);
 
+// Per-context buffers of the soft-shadow path (rt_soft.cu), made on first use.
+struct SoftState;
+void soft_release(rt_context *ctx);
+
 }  // namespace rtc
 
 struct rt_context {
@@ -52,6 +56,7 @@ struct rt_context {
     int isect = RT_ISECT_REFERENCE;
     int builder = RT_BUILDER_PLOC;
     int morton_bits = 0;                   // RT_OPT_MORTON_BITS
+    rtc::SoftState *soft = nullptr;        // rt_render_soft_shadows state
 };
 
 struct rt_scene {

@@ -88,6 +88,7 @@ struct LightView {
     float dist_sign;   // +-1e15 for directional lights (light.h:69-86)
     float d;
     float s_a, s_b;    // spot cone (s_b = 0: none)
+    float radius;      // spherical light's radius (soft shadows only)
 };
 
 struct MaterialView {
