@@ -301,6 +301,7 @@ WORKLOADS = {
     "terrain-2M-ingest-ply": ("workload_ingest", False, lambda k: 3),
     "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
     "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
+    "terrain-2M-1080p-soft16": ("workload_terrain_soft", True, lambda k: max(3, k // 4)),
     "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
     "batched-64-scenes": ("workload_batched", False, lambda k: max(3, k // 4)),
     "adjoint-50k-256": ("workload_adjoint", False, lambda k: max(5, k // 2)),
@@ -633,6 +634,36 @@ def workload_terrain_1m(ctx, stream, flush, steps):
                     "secondary_rays": st.secondary_rays}
     sc.close()
     return out
+
+
+def workload_terrain_soft(ctx, stream, flush, steps):
+    """The headline terrain at 1920x1080 with soft shadows as the reference
+    renders them with SOFT_SHADOW = 16: a spherical light (radius 40) beside
+    the sun, 16 rays to the spherical light and one to the sun per hit, the
+    random points from the reference's stream.  Frame time with the frame's
+    slice of the stream already on the device (the same stream position
+    every step), and once the wall time of a frame whose slice is first
+    generated on the host and copied over (a new position)."""
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.terrain_scene()
+    frame = dict(frame, lights=[dict(scenes.point_light((300.0, 260.0, 500.0)), r=40.0), frame["lights"][0]])
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((1080, 1920, 3), dtype=torch.uint8, device="cuda")
+    first = sc.render_soft(frame, 16, 0, rgb=rgb)
+    for _ in range(2):
+        sc.render_soft(frame, 16, 0, rgb=rgb)
+    secs, st = time_frames(lambda: sc.render_soft(frame, 16, 0, rgb=rgb)["stats"], steps, stream, flush)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc.render_soft(frame, 16, first["stream_end"], rgb=rgb)
+    new_window_s = time.perf_counter() - t0
+    sc.close()
+    rays = st.primary_rays + st.secondary_rays
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080], "samples": 16,
+            "Mrays_s": rays * steps / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays,
+            "stream_numbers_per_frame": first["stream_end"],
+            "ms_per_frame_new_stream_slice": new_window_s * 1e3}
 
 
 def workload_adjoint(ctx, stream, steps):

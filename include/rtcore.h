@@ -187,9 +187,10 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
 #define RT_BUILDER_LBVH 0
 #define RT_BUILDER_PLOC 1
 /* RT_OPT_MORTON_BITS: bits per axis of the Morton codes the builders sort
- * (10..21), or 0 (default): sized from the triangle count, about 3 more
- * than log2(n) / 3, so that each Morton cell holds a few triangles at most.
- * The radix sort orders only the bits in use.  Hits do not depend on it. */
+ * (10..21), or 0 (default): 21 below a million triangles, else sized from
+ * the triangle count, about 3 more than log2(n) / 3, so that each Morton
+ * cell holds a few triangles at most.  The radix sort orders only the bits
+ * in use.  Hits do not depend on it. */
 #define RT_OPT_MORTON_BITS 5
 rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value);
 /* Message of the last error on the calling thread ("" if none). */

@@ -1455,12 +1455,15 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     }
     int sb = 0;
     while ((1 << sb) < nseg) ++sb;
-    // Morton bits per axis: as asked, or about log2(n) / 3 + 3 (cells of a
-    // few triangles at most, so the order the builders start from keeps
-    // neighbours together), never more than the key holds
+    // Morton bits per axis: as asked; else, from a million triangles up,
+    // about log2(n) / 3 + 3 (cells of a few triangles at most, so the order
+    // the builders start from keeps neighbours together, in fewer radix
+    // passes); below that the sort costs little and the full width keeps
+    // small meshes' finer order (20k-triangle icosphere: 0.116 ms per frame
+    // against 0.127 ms at 10 bits); never more than the key holds
     int lg = 0;
     while (lg < 31 && (1 << lg) < n) ++lg;
-    int mbits = in.morton_bits > 0 ? in.morton_bits : (lg + 2) / 3 + 3;
+    int mbits = in.morton_bits > 0 ? in.morton_bits : (n < (1 << 20) ? 21 : (lg + 2) / 3 + 3);
     mbits = max(10, min(mbits, (63 - sb) / 3));
     const int key_bits = 3 * mbits + sb;
     const int threads = 256;

@@ -17,9 +17,11 @@
 // to the device, then the shading pass, every pixel reading its own slice.
 // The cosine table the offsets go through (common/common.h:171-209) is
 // built on the host the same way and kept on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -93,6 +95,37 @@ struct RefRandom {
     }
 };
 
+// Numbers [offset, offset + total) of the stream into out.  The state only
+// changes at refills, so one pass walks the slice refill by refill
+// (without tempering) and keeps a copy of the generator at the start of
+// every chunk; host threads then temper their chunks in parallel.  The
+// generator is left at offset + total.
+void generate_slice(RefRandom &rng, int64_t offset, int64_t total, float *out)
+{
+    rng.seek(offset);
+    constexpr int64_t kChunk = 624 * 2048;
+    std::vector<RefRandom> starts;
+    std::vector<int64_t> begins;
+    for (int64_t b = 0; b < total; b += kChunk) {
+        starts.push_back(rng);
+        begins.push_back(b);
+        rng.seek(offset + std::min(total, b + kChunk));
+    }
+    const int tasks = (int)starts.size();
+    const int nthreads = std::max(1, std::min<int>(tasks, (int)std::thread::hardware_concurrency()));
+    auto work = [&](int first) {
+        for (int t = first; t < tasks; t += nthreads) {
+            RefRandom g = starts[(size_t)t];
+            const int64_t end = std::min(total, begins[(size_t)t] + kChunk);
+            for (int64_t i = begins[(size_t)t]; i < end; ++i) out[i] = g.next();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int k = 1; k < nthreads; ++k) pool.emplace_back(work, k);
+    work(0);
+    for (std::thread &th : pool) th.join();
+}
+
 }  // namespace
 
 // Per-context state of the soft-shadow path.
@@ -105,7 +138,8 @@ struct SoftState {
     DevBuf window;               // numbers [win_base, win_base + win_len) of the stream
     int64_t win_base = -1, win_len = 0;
     RefRandom rng;
-    std::vector<float> staging;
+    float *staging = nullptr;    // pinned host copy of the slice being uploaded
+    size_t staging_cap = 0;
 };
 
 void soft_release(rt_context *ctx)
@@ -117,6 +151,7 @@ void soft_release(rt_context *ctx)
     ctx->soft->prefix.release();
     ctx->soft->scan_temp.release();
     ctx->soft->window.release();
+    if (ctx->soft->staging) cudaFreeHost(ctx->soft->staging);
     delete ctx->soft;
     ctx->soft = nullptr;
 }
@@ -418,12 +453,17 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     // later frames fall inside it
     if (total > 0 && !(S.win_base >= 0 && stream_offset >= S.win_base &&
                        stream_offset + total <= S.win_base + S.win_len)) {
-        S.staging.resize((size_t)total);
-        S.rng.seek(stream_offset);
-        for (int64_t i = 0; i < total; ++i) S.staging[(size_t)i] = S.rng.next();
+        if (S.staging_cap < (size_t)total) {
+            if (S.staging) cudaFreeHost(S.staging);
+            S.staging = nullptr;
+            S.staging_cap = 0;
+            const size_t cap = (size_t)total + (size_t)total / 4;
+            RT_CUDA_S(cudaMallocHost(&S.staging, cap * sizeof(float)), "pinned stream staging");
+            S.staging_cap = cap;
+        }
+        generate_slice(S.rng, stream_offset, total, S.staging);
         RT_CUDA_S(S.window.reserve((size_t)total * sizeof(float)), "stream allocation");
-        RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging.data(), (size_t)total * sizeof(float),
-                                  cudaMemcpyHostToDevice, st),
+        RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging, (size_t)total * sizeof(float), cudaMemcpyHostToDevice, st),
                   "stream copy");
         S.win_base = stream_offset;
         S.win_len = total;
