@@ -241,12 +241,15 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
     if (inv.z < 0.f) { uint32_t t = nzl; nzl = fzl; fzl = t; t = nzh; nzh = fzh; fzh = t; }
     uint32_t hits_int = 0, hits_tri = 0;
     // slot s with its six plane distances: internal children set bit
-    // 24 + (s ^ oct), leaf slots their triangle bits
+    // 24 + (s ^ oct), leaf slots their triangle bits.  An empty slot needs
+    // no test of its meta byte: its box is inverted (low planes 255, high
+    // planes 0), and should rounding let it "hit", its clear internal bit
+    // and meta byte 0 add nothing.
     auto slot = [&](int s, float tnx, float tny, float tnz, float tfx, float tfy, float tfz) {
         const uint32_t meta = byte_of(meta_lo, meta_hi, s);
         const float tn = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
         const float tf = fmin3f(tfx, tfy, fminf(tfz, tmax));
-        if (tn <= tf && meta != 0u) {
+        if (tn <= tf) {
             if ((imask >> s) & 1u) hits_int |= 1u << (24 + (s ^ oct));
             else hits_tri |= (meta >> 5) << (meta & 31u);
         }
