@@ -452,28 +452,47 @@ rt_status rt_render_ao(rt_scene *scene, const rt_camera *camera, const rt_materi
 
 #define RT_MAX_SOFT_SAMPLES 64
 
+/* The extent of a light for rt_render_soft_shadows, one per light:
+ * radius is the radius r of a spherical light (the reference's spherical
+ * and spot-light constructors, light.h:17-18, 24-25); a light with
+ * ntris > 0 is instead defined by triangles of the scene (its triangle
+ * constructors, light.h:20-21, 27-29): tris lists ntris indices into the
+ * scene's triangles (the caller's order; host memory borrowed for the
+ * call), which should carry RT_TRI_LIGHT so shadow rays pass them, radius
+ * is then 0, and the light's pos is its centre. */
+typedef struct rt_light_shape {
+    float radius;
+    int32_t ntris;
+    const int32_t *tris;
+} rt_light_shape;
+
 /* Soft shadows as RAPTor renders them when it is built with SOFT_SHADOW =
- * samples (ray::find_rays ray.cc:91-104, light::find_rays light.h:62-128,
+ * samples (ray::find_rays ray.cc:91-104, light::find_rays light.h:62-164,
  * ray_trace_engine::ray_trace raytracer.cc:44-64): every primary hit sends
- * `samples` shadow rays to random points of each spherical light
- * (RT_LIGHT_POINT and RT_LIGHT_SPOT; light_radius[l] is the radius r the
- * reference's light constructors take, light.h:17-25; NULL: all 0) and one
- * ray to each directional light; a light's term is shaded with its first
- * ray's direction and length and weighted by the fraction of its rays that
- * reach it.  The random points are the reference's own: its process-wide
- * generator (common/common.cc:35-105) draws three numbers per ray, in pixel
- * order (x + y * xres) and light order, and stream_offset says how many
- * numbers it had produced before this frame (0: a freshly started
- * program); stream_end (nullable) receives the count after the frame, the
- * next frame's offset.  Frames without mirror or refracting materials
- * (`materials` as rt_render_materials).  rgb_out (RGB8) and rgb_f32 (the
- * camera's float image) are nullable, not both, host or device memory.
- * Runs two passes with one host round trip between them: the camera rays,
- * then the frame's slice of the random stream (generated on the host and
- * copied over unless the previous frame's slice already covers it) and the
- * shading. */
+ * `samples` shadow rays to random points of each spherical or
+ * triangle-defined light (RT_LIGHT_POINT and RT_LIGHT_SPOT; shapes[l] as
+ * above, NULL: all spherical with radius 0) and one ray to each directional
+ * light; a light's term is shaded with its first ray's direction and length
+ * and weighted by the fraction of its rays that reach it.  The random
+ * points are the reference's own: its process-wide generator
+ * (common/common.cc:35-105) draws, in pixel order (x + y * xres) and light
+ * order, three numbers per ray of a spherical light and two per ray a
+ * triangle-defined light makes (triangle::find_rays, triangle.h:504-525;
+ * samples / ntris rays per triangle plus one for the triangles its stride
+ * lands on, light.h:131-156, which is samples + 1 rays when ntris divides
+ * samples -- the reference's release build draws for all of them and
+ * traces the first `samples`; a light making fewer is refused).
+ * stream_offset says how many numbers the generator had produced before
+ * this frame (0: a freshly started program); stream_end (nullable)
+ * receives the count after the frame, the next frame's offset.  Frames
+ * without mirror or refracting materials (`materials` as
+ * rt_render_materials).  rgb_out (RGB8) and rgb_f32 (the camera's float
+ * image) are nullable, not both, host or device memory.  Runs two passes
+ * with one host round trip between them: the camera rays, then the frame's
+ * slice of the random stream (generated on the host and copied over unless
+ * the previous frame's slice already covers it) and the shading. */
 rt_status rt_render_soft_shadows(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
-                                 const float *light_radius, const rt_material *materials, int32_t nmaterials,
+                                 const rt_light_shape *shapes, const rt_material *materials, int32_t nmaterials,
                                  int32_t samples, int64_t stream_offset, uint8_t *rgb_out, float *rgb_f32,
                                  int64_t *stream_end, rt_render_stats *stats);
 

@@ -34,7 +34,8 @@ class Camera(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("kind", C.c_int32), ("rgb", C.c_float * 3), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
-                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float), ("r", C.c_float)]
+                ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float), ("r", C.c_float),
+                ("ntris", C.c_int32), ("tris", C.POINTER(C.c_int32))]
 
 
 class Material(C.Structure):
@@ -74,7 +75,10 @@ def make_camera(d):
 
 
 def make_lights(ls):
+    """Light array from light dicts; "tris" (triangle indices) makes a
+    triangle-defined light, its index arrays kept alive on the array."""
     arr = (Light * max(1, len(ls)))()
+    arr._tris = []
     for i, d in enumerate(ls):
         arr[i].kind = d["kind"]
         arr[i].rgb[:] = list(d["rgb"])
@@ -84,6 +88,11 @@ def make_lights(ls):
         arr[i].s_a = d.get("s_a", 0.0)
         arr[i].s_b = d.get("s_b", 0.0)
         arr[i].r = d.get("r", 0.0)
+        if d.get("tris") is not None:
+            t = np.ascontiguousarray(d["tris"], np.int32)
+            arr._tris.append(t)
+            arr[i].ntris = t.shape[0]
+            arr[i].tris = t.ctypes.data_as(C.POINTER(C.c_int32))
     return arr
 
 
@@ -226,6 +235,8 @@ def oracle_lib():
                                           _F, C.POINTER(C.c_int64)]
         lib["ro_ref_random"].restype = None
         lib["ro_ref_random"].argtypes = [C.c_int64, C.c_int32, _F]
+        lib["ro_area_light_rays"].restype = C.c_int32
+        lib["ro_area_light_rays"].argtypes = [C.c_int32, C.c_int32, _I]
         lib["ro_lut_cos"].restype = C.c_float
         lib["ro_lut_cos"].argtypes = [C.c_float]
         lib["ro_lut_sin"].restype = C.c_float
@@ -575,6 +586,14 @@ def ref_random(start, n):
     out = np.empty(n, np.float32)
     oracle_lib()["ro_ref_random"](int(start), int(n), _p(out, C.c_float))
     return out
+
+
+def area_light_rays(ntris, n):
+    """(rays made, rays per triangle) of a triangle-defined light of ntris
+    triangles asked for n rays (ro_area_light_rays)."""
+    cnt = np.zeros(max(1, int(ntris)), np.int32)
+    made = oracle_lib()["ro_area_light_rays"](int(ntris), int(n), _p(cnt, C.c_int32))
+    return made, cnt[:int(ntris)]
 
 
 def philox(ctr, key0, key1):

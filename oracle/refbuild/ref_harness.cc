@@ -207,6 +207,33 @@ void rref_camera_rays(const ro_camera *c, int32_t x0, int32_t y0, int32_t w, int
 double rref_render_aa(void *h, const ro_camera *c, int32_t aa_x, int32_t aa_y, const ro_light *ls, int32_t nl,
                       uint8_t *rgb);
 
+// The caller's lights as the reference's light objects: directional
+// (light.h:33-34), spot (light.h:24-25), spherical (light.h:17-18), or
+// defined by triangles of the store (light.h:20-21, spot form :27-29).
+// tri_lists keeps the lists those lights point to alive.
+static void make_lights(const ro_light *ls, int32_t nl, const primitive_store *store, light_list &lights,
+                        std::vector<std::vector<int>> &tri_lists)
+{
+    tri_lists.reserve((size_t)(nl > 0 ? nl : 0));
+    for (int32_t i = 0; i < nl; ++i) {
+        const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
+        if (ls[i].kind == 1) {
+            lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
+        } else if (ls[i].ntris > 0 && ls[i].tris) {
+            tri_lists.emplace_back(ls[i].tris, ls[i].tris + ls[i].ntris);
+            const std::vector<int> *t = &tri_lists.back();
+            if (ls[i].kind == 2)
+                lights.emplace_back(store, rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, t);
+            else
+                lights.emplace_back(store, rgbc, p3(ls[i].pos), ls[i].d, t);
+        } else if (ls[i].kind == 2) {
+            lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, ls[i].r);
+        } else {
+            lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, ls[i].r);
+        }
+    }
+}
+
 double rref_render(void *h, const ro_camera *c, const ro_light *ls, int32_t nl, uint8_t *rgb)
 {
     return rref_render_aa(h, c, 1, 1, ls, nl, rgb);
@@ -222,15 +249,8 @@ double rref_render_tone_mapped(void *h, const ro_camera *c, int32_t aa_x, int32_
     auto *s = static_cast<ref_scene *>(h);
     std::unique_ptr<camera> cam(make_camera(c, (unsigned)aa_x, (unsigned)aa_y));
     light_list lights;
-    for (int32_t i = 0; i < nl; ++i) {
-        const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
-        if (ls[i].kind == 1)
-            lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
-        else if (ls[i].kind == 2)   // spot light (light.h:24-25)
-            lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, ls[i].r);
-        else
-            lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, ls[i].r);
-    }
+    std::vector<std::vector<int>> tri_lists;
+    make_lights(ls, nl, &s->store, lights, tri_lists);
     null_buf nb;
     std::streambuf *old = std::cout.rdbuf(&nb);
     const auto t0 = std::chrono::steady_clock::now();
@@ -334,15 +354,8 @@ int64_t rref_parse_and_render(const char *path, int32_t kind, const ro_camera *c
         std::unique_ptr<bvh> accel(new bvh(store));
         std::unique_ptr<camera> cam(make_camera(c));
         light_list lights;
-        for (int32_t i = 0; i < nl; ++i) {
-            const ext_colour_t rgbc(ls[i].rgb[0], ls[i].rgb[1], ls[i].rgb[2]);
-            if (ls[i].kind == 1)
-                lights.emplace_back(rgbc, p3(ls[i].dir), ls[i].d);
-            else if (ls[i].kind == 2)
-                lights.emplace_back(rgbc, p3(ls[i].pos), p3(ls[i].dir), ls[i].d, ls[i].s_a, ls[i].s_b, ls[i].r);
-            else
-                lights.emplace_back(rgbc, p3(ls[i].pos), ls[i].d, ls[i].r);
-        }
+        std::vector<std::vector<int>> tri_lists;
+        make_lights(ls, nl, &store, lights, tri_lists);
         null_buf nb;
         std::streambuf *old = std::cout.rdbuf(&nb);
         ray_tracer(accel.get(), lights, store, *cam);

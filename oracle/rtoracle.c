@@ -582,10 +582,13 @@ typedef struct {
     int32_t *ao_count;
     /* soft shadows (ro_render_soft): shadow rays per spherical light, the
      * frame's slice of the reference's random stream and, per pixel, the
-     * index in it of the pixel's first number */
+     * index in it of the pixel's first number; per light the numbers a hit
+     * draws and, for a triangle-defined light, the rays it makes */
     int32_t soft_n;
     const float *stream;
     const int64_t *px_draw;
+    const int32_t *ldraw;
+    const struct area_ray *const *area;
     int32_t next_row;
     pthread_mutex_t *lock;
 } render_job;
@@ -662,11 +665,56 @@ void ro_ref_random(int64_t start, int32_t n, float *out)
     for (int32_t i = 0; i < n; ++i) out[i] = ref_rng_next(&g);
 }
 
-/* Numbers one primary hit draws for light L with n soft-shadow rays: three
- * per ray of a spherical (point or spot) light, none otherwise. */
-static inline int32_t soft_draws(const ro_light *L, int32_t n)
+int32_t ro_area_light_rays(int32_t ntris, int32_t n, int32_t *cnt)
 {
-    return (n > 1 && !light_is_directional(L)) ? 3 * n : 0;
+    if (ntris < 1 || n < 1) return -1;
+    const int32_t ppt = n / ntris;
+    const int32_t extra = n - ntris * ppt;
+    const float stride = (float)ntris / (float)(extra > 1 ? extra : 1);
+    float extra_point = 0.0f;
+    int32_t made = 0;
+    for (int32_t i = 0; i < ntris; ++i) {
+        int32_t k = ppt;
+        if (i == (int32_t)extra_point) {
+            k = ppt + 1;
+            extra_point += stride;
+        }
+        if (cnt) cnt[i] = k;
+        made += k;
+    }
+    return made;
+}
+
+/* One ray a triangle-defined light makes: triangle tri's ray i of the cnt
+ * it makes. */
+typedef struct area_ray { int32_t tri, cnt, i; } area_ray;
+
+/* Numbers one primary hit draws for light L with n soft-shadow rays: three
+ * per ray of a spherical (point or spot) light, two per ray a triangle-
+ * defined light makes (made), none for a directional light or n = 1. */
+static inline int32_t soft_draws(const ro_light *L, int32_t n, int32_t made)
+{
+    if (n <= 1 || light_is_directional(L)) return 0;
+    return L->ntris > 0 ? 2 * made : 3 * n;
+}
+
+/* A point of a triangle of a triangle-defined light (triangle::find_rays,
+ * triangle.h:504-525): barycentrics beta, gamma from rnd[0..1], then
+ * ray::set_up(start, point) (ray.h:44-54). */
+static void area_light_ray(const ro_scene *s, const area_ray *e, v3 start, const float *rnd, ro_ray *r, float *len)
+{
+    const int32_t n = e->cnt, i = e->i;
+    const float beta_scale = 1.0f / (float)((n >> 4) + ((n & 0xe) != 0) + 1);
+    const float gamma_scale = 1.0f / (float)((n >> 4) + ((n & 0xc) != 0) + 1);
+    const int32_t eighths = (i >> 2) & ~0x1;
+    const float beta = rnd[0] * (beta_scale * (float)(eighths + (i & 0x1)));
+    const float gamma = (rnd[1] * (gamma_scale * (float)(eighths + (i & 0x2)))) * (1.0f - beta);
+    const float alpha = 1.0f - (beta + gamma);
+    const v3 p = vadd(vadd(vmul(s->va[e->tri], alpha), vmul(s->vb[e->tri], beta)), vmul(s->vc[e->tri], gamma));
+    const v3 d = vsub(p, start);
+    *len = vmag(d);
+    r->o = start;
+    r->d = vdivs(d, *len);
 }
 
 /* Shadow ray i of n to spherical light L (light::find_rays, light.h:102-128):
@@ -794,18 +842,19 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
         ro_ray sr;
         float len;
         int32_t nrays = 1, made = 0;
-        if (first && soft_draws(L, J->soft_n) > 0) {
+        if (first && J->ldraw && J->ldraw[l] > 0) {
             /* soft shadows: n rays to random points of the light, shaded with
              * the first one's direction and length (raytracer.cc:44-64) */
             nrays = J->soft_n;
             for (int32_t i = 0; i < nrays; ++i) {
                 ro_ray ri;
                 float li;
-                soft_ray(L, start, nrays, i, J->stream + draw + 3 * i, &ri, &li);
+                if (J->area[l]) area_light_ray(s, &J->area[l][i], start, J->stream + draw + 2 * i, &ri, &li);
+                else soft_ray(L, start, nrays, i, J->stream + draw + 3 * i, &ri, &li);
                 if (i == 0) { sr = ri; len = li; }
                 if (!nearer(s, &ri, li)) ++made;
             }
-            draw += 3 * nrays;
+            draw += J->ldraw[l];
             J->rays += nrays;
         } else {
             shadow_ray(L, start, &sr, &len);
@@ -989,18 +1038,64 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
                        int32_t nthreads, uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *stream_end)
 {
     if (!s || !s->nodes || !cam || !mats || nmats < 1 || !rgb || samples < 1 || samples > 64 ||
-        stream_offset < 0 || nlights < 0 || (nlights > 0 && !lights))
+        stream_offset < 0 || nlights < 0 || nlights > 64 || (nlights > 0 && !lights))
         return -1;
+    /* per light: numbers a hit draws and, for a triangle-defined light, the
+     * first `samples` rays it makes */
+    int32_t ldraw[64];
+    area_ray *area[64];
+    memset(area, 0, sizeof(area));
+    int bad = 0;
+    for (int32_t l = 0; l < nlights && !bad; ++l) {
+        const ro_light *L = &lights[l];
+        int32_t made = 0;
+        if (L->ntris > 0) {
+            if (!L->tris || L->kind == 1 || L->r != 0.0f) { bad = 1; break; }
+            for (int32_t j = 0; j < L->ntris; ++j)
+                if (L->tris[j] < 0 || L->tris[j] >= s->ntris) bad = 1;
+            if (bad) break;
+            made = ro_area_light_rays(L->ntris, samples, NULL);
+            if (samples > 1 && !light_is_directional(L)) {
+                if (made < samples) { bad = 1; break; }
+                int32_t *cnt = (int32_t *)malloc((size_t)L->ntris * sizeof(int32_t));
+                area[l] = (area_ray *)malloc((size_t)made * sizeof(area_ray));
+                if (!cnt || !area[l]) { free(cnt); bad = 1; break; }
+                (void)ro_area_light_rays(L->ntris, samples, cnt);
+                int32_t k = 0;
+                for (int32_t j = 0; j < L->ntris; ++j)
+                    for (int32_t i = 0; i < cnt[j]; ++i) {
+                        area[l][k].tri = L->tris[j];
+                        area[l][k].cnt = cnt[j];
+                        area[l][k].i = i;
+                        ++k;
+                    }
+                free(cnt);
+            }
+        } else if (L->ntris < 0) {
+            bad = 1;
+            break;
+        }
+        ldraw[l] = soft_draws(L, samples, made);
+    }
+    if (bad) {
+        for (int32_t l = 0; l < nlights; ++l) free(area[l]);
+        return -1;
+    }
     for (int32_t i = 0; i < nmats; ++i)
-        if (mats[i].rf > 0.0f || mats[i].tran > 0.0f) return -1;
+        if (mats[i].rf > 0.0f || mats[i].tran > 0.0f) bad = 1;
     if (s->mat)
         for (int32_t i = 0; i < s->ntris; ++i)
-            if (s->mat[i] < 0 || s->mat[i] >= nmats) return -1;
+            if (s->mat[i] < 0 || s->mat[i] >= nmats) bad = 1;
     pthread_once(&g_cos_lut_once, build_cos_lut);
     const size_t npix = (size_t)cam->xres * (size_t)cam->yres;
-    uint8_t *hit = (uint8_t *)malloc(npix ? npix : 1);
-    int64_t *px_draw = (int64_t *)malloc((npix ? npix : 1) * sizeof(int64_t));
-    if (!hit || !px_draw) { free(hit); free(px_draw); return -1; }
+    uint8_t *hit = bad ? NULL : (uint8_t *)malloc(npix ? npix : 1);
+    int64_t *px_draw = bad ? NULL : (int64_t *)malloc((npix ? npix : 1) * sizeof(int64_t));
+    if (!hit || !px_draw) {
+        free(hit);
+        free(px_draw);
+        for (int32_t l = 0; l < nlights; ++l) free(area[l]);
+        return -1;
+    }
     /* pass 1: which pixels hit */
     {
         pthread_mutex_t lock;
@@ -1019,14 +1114,19 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
     /* each hit pixel draws the same count, in pixel order (x + y * xres:
      * ray_tracer's loops, y outer, raytracer.cc:586-592) */
     int32_t per_hit = 0;
-    for (int32_t l = 0; l < nlights; ++l) per_hit += soft_draws(&lights[l], samples);
+    for (int32_t l = 0; l < nlights; ++l) per_hit += ldraw[l];
     int64_t total = 0;
     for (size_t p = 0; p < npix; ++p) {
         px_draw[p] = total;
         total += hit[p] ? per_hit : 0;
     }
     float *stream = (float *)malloc((size_t)(total > 0 ? total : 1) * sizeof(float));
-    if (!stream) { free(hit); free(px_draw); return -1; }
+    if (!stream) {
+        free(hit);
+        free(px_draw);
+        for (int32_t l = 0; l < nlights; ++l) free(area[l]);
+        return -1;
+    }
     {
         ref_rng g;
         ref_rng_init(&g);
@@ -1037,8 +1137,10 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
     memset(&J, 0, sizeof(J));
     J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mat = mats; J.mats = mats; J.nmats = nmats;
     J.row0 = 0; J.row1 = cam->yres; J.rgb = rgb; J.hit_id = hit_id; J.fimg = fimg;
-    J.soft_n = samples; J.stream = stream; J.px_draw = px_draw;
+    J.soft_n = samples; J.stream = stream; J.px_draw = px_draw; J.ldraw = ldraw;
+    J.area = (const area_ray *const *)area;
     const int64_t rays = run_render(&J, nthreads);
+    for (int32_t l = 0; l < nlights; ++l) free(area[l]);
     free(stream);
     free(px_draw);
     free(hit);

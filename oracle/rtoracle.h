@@ -50,6 +50,8 @@ typedef struct ro_light {
     float d;
     float s_a, s_b;   /* kind 2 (spot light at pos, axis dir): cone angles, light.h:24-25 */
     float r;          /* kinds 0 and 2: radius of the spherical light (light.h:17-25); used by soft shadows */
+    int32_t ntris;    /* kinds 0 and 2: a triangle-defined light (light.h:20-21, 27-29) -- its ntris */
+    const int32_t *tris;  /* triangles (scene indices, flagged RO_TRI_LIGHT); pos is its centre.  NULL / 0: none */
 } ro_light;
 
 /* Coloured-mapper Phong material (materials/coloured_mapper_shader.h): ka,
@@ -154,19 +156,31 @@ int32_t ro_pixel_secondary_rays(const ro_scene *s, const ro_camera *cam, const r
                                 int32_t *hit_id, float *ogn, float *dir, float *tmax);
 
 /* Soft shadows as the reference renders them when built with
- * SOFT_SHADOW = samples (ray.cc:91-104, light.h:62-128, raytracer.cc:44-64):
+ * SOFT_SHADOW = samples (ray.cc:91-104, light.h:62-164, raytracer.cc:44-64):
  * every primary hit sends `samples` shadow rays to random points of each
  * spherical light (kinds 0 and 2 with a cone; radius r) -- three numbers of
  * the reference's random stream per ray, drawn in pixel order (x + y * xres)
- * and light order -- and one ray to each directional light; a light's term
- * is shaded with its first ray's direction and length and weighted by the
- * unoccluded fraction.  stream_offset: how many numbers the reference's
- * generator had produced before the frame; stream_end (nullable) receives
- * the count after it.  Materials without reflection or refraction (-1
- * otherwise).  Whole frame; returns rays traced. */
+ * and light order -- or of each triangle-defined light (ntris > 0, r = 0:
+ * two numbers per ray the light makes, triangle.h:504-525), and one ray to
+ * each directional light; a light's term is shaded with its first ray's
+ * direction and length and weighted by the unoccluded fraction.
+ * stream_offset: how many numbers the reference's generator had produced
+ * before the frame; stream_end (nullable) receives the count after it.
+ * Materials without reflection or refraction, light triangles in range and
+ * making at least `samples` rays (-1 otherwise).  Whole frame; returns rays
+ * traced. */
 int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
                        const ro_material *mats, int32_t nmats, int32_t samples, int64_t stream_offset,
                        int32_t nthreads, uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *stream_end);
+
+/* The rays light::find_rays makes for a triangle-defined light of ntris
+ * triangles asked for n (light.h:129-164): n / ntris per triangle and one
+ * more for every triangle the binary32 stride lands on.  cnt (nullable,
+ * ntris entries) receives each triangle's count; returns their sum, which
+ * is n + 1 when ntris divides n (the reference's assert on the sum is
+ * compiled out of its release build, which draws for every ray made and
+ * traces the first n), or -1 for ntris < 1 or n < 1. */
+int32_t ro_area_light_rays(int32_t ntris, int32_t n, int32_t *cnt);
 
 /* n numbers of the reference's random stream (common/common.cc:35-105)
  * from position start of a freshly seeded generator. */

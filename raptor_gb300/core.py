@@ -65,6 +65,10 @@ class RtLight(C.Structure):
                 ("d", C.c_float), ("s_a", C.c_float), ("s_b", C.c_float)]
 
 
+class RtLightShape(C.Structure):
+    _fields_ = [("radius", C.c_float), ("ntris", C.c_int32), ("tris", C.POINTER(C.c_int32))]
+
+
 class RtMaterial(C.Structure):
     _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
                 ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
@@ -148,7 +152,8 @@ SIGNATURES = [
     ("rt_mesh_load", C.c_int32, [C.c_char_p, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_parse", C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(RtMesh)]),
     ("rt_mesh_free", None, [C.POINTER(RtMesh)]),
-    ("rt_render_soft_shadows", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, _P,
+    ("rt_render_soft_shadows", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
+                                           C.POINTER(RtLightShape),
                                            C.POINTER(RtMaterial), C.c_int32, C.c_int32, C.c_int64, _P, _P,
                                            C.POINTER(C.c_int64), C.POINTER(RtRenderStats)]),
     ("rt_render_image", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
@@ -515,21 +520,31 @@ class Scene:
 
     def render_soft(self, frame, samples, stream_offset=0, rgb=None, fimg=None, want_float=False):
         """rt_render_soft_shadows: `samples` soft-shadow rays per spherical
-        light (radius: each light dict's "r", default 0), drawing the
-        reference's random stream from stream_offset.  rgb / fimg: host
-        arrays or device tensors (allocated on the host when None; fimg
-        only with want_float).  Returns rgb, fimg, stats and stream_end."""
+        light (radius: each light dict's "r", default 0) or triangle-defined
+        light (a light dict's "tris": indices of the scene's triangles),
+        drawing the reference's random stream from stream_offset.  rgb /
+        fimg: host arrays or device tensors (allocated on the host when
+        None; fimg only with want_float).  Returns rgb, fimg, stats and
+        stream_end."""
         cam = make_camera(frame["camera"])
         if rgb is None:
             rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
         if fimg is None and want_float:
             fimg = np.empty((cam.yres, cam.xres, 3), np.float32)
         ls = make_lights(frame["lights"])
-        radius = np.array([float(l.get("r", 0.0)) for l in frame["lights"]] or [0.0], np.float32)
+        shapes = (RtLightShape * max(1, len(frame["lights"])))()
+        keep = []
+        for i, l in enumerate(frame["lights"]):
+            shapes[i].radius = float(l.get("r", 0.0))
+            if l.get("tris") is not None:
+                t = np.ascontiguousarray(l["tris"], np.int32)
+                keep.append(t)
+                shapes[i].ntris = t.shape[0]
+                shapes[i].tris = t.ctypes.data_as(C.POINTER(C.c_int32))
         table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
         st = RtRenderStats()
         end = C.c_int64(0)
-        _check(lib().rt_render_soft_shadows(self.h, C.byref(cam), ls, len(frame["lights"]), ptr(radius), table,
+        _check(lib().rt_render_soft_shadows(self.h, C.byref(cam), ls, len(frame["lights"]), shapes, table,
                                             len(table), int(samples), int(stream_offset), ptr(rgb), ptr(fimg),
                                             C.byref(end), C.byref(st)))
         return {"rgb": rgb, "fimg": fimg, "stats": st, "stream_end": end.value}

@@ -1,15 +1,17 @@
 // rt_soft.cu -- soft shadows as RAPTor renders them when it is built with
 // SOFT_SHADOW = samples: every primary hit sends `samples` shadow rays to
-// random points of each spherical (point or spot) light and one to each
-// directional light; a light's term is shaded with its first ray's direction
-// and length and weighted by the fraction of rays that reach the light
-// (ray::find_rays ray.cc:91-104, light::find_rays light.h:62-128,
+// random points of each spherical (point or spot) or triangle-defined light
+// and one to each directional light; a light's term is shaded with its
+// first ray's direction and length and weighted by the fraction of rays that
+// reach the light (ray::find_rays ray.cc:91-104, light::find_rays
+// light.h:62-164, triangle::find_rays triangle.h:504-525,
 // ray_trace_engine::ray_trace raytracer.cc:44-64).
 //
 // The random points come from the reference's own generator, one process-
 // wide stream (common/common.cc:35-105) that the reference draws from in
 // pixel order (x + y * xres) and, within a pixel, in light order: three
-// numbers per ray of a spherical light.  A pixel's position in that stream
+// numbers per ray of a spherical light, two per ray a triangle-defined
+// light makes.  A pixel's position in that stream
 // is therefore fixed by how many pixels before it hit something, so a frame
 // is rendered in two passes: the camera rays first (hit records kept, one
 // flag per pixel), an exclusive scan of the flags (each hit draws the same
@@ -126,6 +128,29 @@ void generate_slice(RefRandom &rng, int64_t offset, int64_t total, float *out)
     for (std::thread &th : pool) th.join();
 }
 
+// The rays light::find_rays makes for a triangle-defined light of ntris
+// triangles asked for n (light.h:129-164): n / ntris per triangle, one more
+// for every triangle the binary32 stride lands on.  cnt (ntris entries,
+// nullable) receives the counts; returns their sum.
+int32_t area_light_rays(int32_t ntris, int32_t n, int32_t *cnt)
+{
+    const int32_t ppt = n / ntris;
+    const int32_t extra = n - ntris * ppt;
+    const float stride = (float)ntris / (float)std::max(extra, 1);
+    float at = 0.0f;
+    int32_t made = 0;
+    for (int32_t j = 0; j < ntris; ++j) {
+        int32_t k = ppt;
+        if (j == (int32_t)at) {
+            ++k;
+            at += stride;
+        }
+        if (cnt) cnt[j] = k;
+        made += k;
+    }
+    return made;
+}
+
 }  // namespace
 
 // Per-context state of the soft-shadow path.
@@ -136,6 +161,7 @@ struct SoftState {
     DevBuf flags, prefix;        // int per pixel: hit flag, exclusive scan of the flags
     DevBuf scan_temp;
     DevBuf window;               // numbers [win_base, win_base + win_len) of the stream
+    DevBuf area;                 // int4 per ray of a triangle-defined light: triangle, its rays, index
     int64_t win_base = -1, win_len = 0;
     RefRandom rng;
     float *staging = nullptr;    // pinned host copy of the slice being uploaded
@@ -151,6 +177,7 @@ void soft_release(rt_context *ctx)
     ctx->soft->prefix.release();
     ctx->soft->scan_temp.release();
     ctx->soft->window.release();
+    ctx->soft->area.release();
     if (ctx->soft->staging) cudaFreeHost(ctx->soft->staging);
     delete ctx->soft;
     ctx->soft = nullptr;
@@ -196,10 +223,41 @@ __device__ __forceinline__ void soft_ray(const LightView &L, const float *__rest
     dir = xdiv3(dv, len);
 }
 
+// Shadow ray to triangle-defined light point e = (triangle, rays it makes,
+// index of this one): barycentrics from rnd[0..1] (triangle.h:504-525),
+// then ray::set_up(start, point).
+__device__ __forceinline__ void area_ray(const float *__restrict__ verts, const int3 *__restrict__ idx, int4 e,
+                                         float3 start, const float *__restrict__ rnd, float3 &dir, float &len)
+{
+    const int n = e.y, i = e.z;
+    const float beta_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xe) != 0) + 1));
+    const float gamma_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xc) != 0) + 1));
+    const int eighths = (i >> 2) & ~0x1;
+    const float beta = xmul(__ldg(rnd), xmul(beta_scale, (float)(eighths + (i & 0x1))));
+    const float gamma = xmul(xmul(__ldg(rnd + 1), xmul(gamma_scale, (float)(eighths + (i & 0x2)))), xsub(1.0f, beta));
+    const float alpha = xsub(1.0f, xadd(beta, gamma));
+    const int3 t = idx[e.x];
+    const float3 a = make_float3(__ldg(verts + 3 * t.x), __ldg(verts + 3 * t.x + 1), __ldg(verts + 3 * t.x + 2));
+    const float3 b = make_float3(__ldg(verts + 3 * t.y), __ldg(verts + 3 * t.y + 1), __ldg(verts + 3 * t.y + 2));
+    const float3 c = make_float3(__ldg(verts + 3 * t.z), __ldg(verts + 3 * t.z + 1), __ldg(verts + 3 * t.z + 2));
+    const float3 p = xadd3(xadd3(xmul3(a, alpha), xmul3(b, beta)), xmul3(c, gamma));
+    const float3 dv = xsub3(p, start);
+    len = xmag(dv);
+    dir = xdiv3(dv, len);
+}
+
 __device__ __forceinline__ bool soft_light(const LightView &L, int samples)
 {
     return samples > 1 && L.kind != RT_LIGHT_DIRECTIONAL;
 }
+
+// Per light: first entry of its rays in the ray table and the rays it
+// makes (0: not triangle-defined); numbers a hit draws for it.
+struct AreaSet {
+    int32_t first[RT_MAX_LIGHTS];
+    int32_t made[RT_MAX_LIGHTS];
+    int32_t draws[RT_MAX_LIGHTS];
+};
 
 // Pass 1: the camera ray of every pixel; hit record and hit flag.
 __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_primary(SceneView sc, CameraView cam,
@@ -236,9 +294,10 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_pr
 // Pass 2: shading.  rnd holds the frame's numbers (rnd[0] = the frame's
 // first), nrnd of them; a hit pixel's first is prefix[pix] * per_hit.
 __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_shade(
-    SceneView sc, CameraView cam, LightSet lights, MaterialTable table, int32_t samples, int32_t per_hit,
-    const float *__restrict__ rnd, int64_t nrnd, const float *__restrict__ lut, const int4 *__restrict__ hits,
-    const int32_t *__restrict__ prefix, uint8_t *__restrict__ rgb, float *__restrict__ fimg, Counters *ctr)
+    SceneView sc, CameraView cam, LightSet lights, MaterialTable table, AreaSet areas, const int4 *__restrict__ area,
+    const float *__restrict__ verts, int32_t samples, int32_t per_hit, const float *__restrict__ rnd, int64_t nrnd,
+    const float *__restrict__ lut, const int4 *__restrict__ hits, const int32_t *__restrict__ prefix,
+    uint8_t *__restrict__ rgb, float *__restrict__ fimg, Counters *ctr)
 {
     int tiles_x;
     const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
@@ -279,21 +338,26 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_sh
                     int n = 1, made = 0;
                     if (soft_light(L, samples)) {
                         n = samples;
-                        if (draw + 3 * (int64_t)n > nrnd) {   // never expected: the host sized the slice
+                        if (draw + (int64_t)areas.draws[l] > nrnd) {   // never expected: the host sized the slice
                             status |= kStatusBadIndex;
                             break;
                         }
+                        const bool tri_light = areas.made[l] > 0;
                         for (int i = 0; i < n; ++i) {
                             float3 di;
                             float li;
-                            soft_ray(L, lut, start, n, i, rnd + draw + 3 * i, di, li);
+                            if (tri_light)
+                                area_ray(verts, sc.idx, __ldg(area + areas.first[l] + i), start, rnd + draw + 2 * i,
+                                         di, li);
+                            else
+                                soft_ray(L, lut, start, n, i, rnd + draw + 3 * i, di, li);
                             if (i == 0) { ldir = di; len = li; }
                             HitRecord sh;
                             bool blocked;
                             status |= traverse<true>(sc, start, di, li, sh, blocked);
                             if (!blocked) ++made;
                         }
-                        draw += 3 * n;
+                        draw += areas.draws[l];
                     } else {
                         shadow_ray(L, start, ldir, len);
                         HitRecord sh;
@@ -364,7 +428,7 @@ int soft_blocks_per_sm()
 }  // namespace
 
 extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera, const rt_light *lights,
-                                            int32_t nlights, const float *light_radius,
+                                            int32_t nlights, const rt_light_shape *shapes,
                                             const rt_material *materials, int32_t nmaterials, int32_t samples,
                                             int64_t stream_offset, uint8_t *rgb_out, float *rgb_f32,
                                             int64_t *stream_end, rt_render_stats *stats)
@@ -383,9 +447,19 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     for (int32_t i = 0; i < nmaterials; ++i)
         if (materials[i].rf != 0.0f || materials[i].tran != 0.0f)
             return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: mirror and refracting materials are not offered");
-    for (int32_t i = 0; i < nlights; ++i)
-        if (light_radius && !(light_radius[i] >= 0.0f && light_radius[i] < 3.0e38f))
+    for (int32_t i = 0; i < nlights && shapes; ++i) {
+        const rt_light_shape &sh = shapes[i];
+        if (!(sh.radius >= 0.0f && sh.radius < 3.0e38f))
             return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: light radius must be finite and >= 0");
+        if (sh.ntris < 0 || (sh.ntris > 0 && !sh.tris))
+            return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: bad triangle list of a light");
+        if (sh.ntris > 0 && (sh.radius != 0.0f || lights[i].kind == RT_LIGHT_DIRECTIONAL))
+            return sfail(RT_ERR_INVALID_ARG,
+                         "rt_render_soft_shadows: a triangle-defined light is a point or spot light of radius 0");
+        for (int32_t j = 0; j < sh.ntris; ++j)
+            if (sh.tris[j] < 0 || sh.tris[j] >= s->ntris)
+                return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: light triangle index out of range");
+    }
     if (!s->built) return sfail(RT_ERR_NOT_BUILT, "rt_render_soft_shadows: hierarchy not built");
     if (s->mat_max >= nmaterials)
         return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: the scene's material indices exceed the table");
@@ -419,11 +493,37 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     LightSet ls;
     ls.n = nlights;
     ls.fast_pow = 0;
+    AreaSet as = {};
+    std::vector<int4> area_rays;
     int32_t per_hit = 0;
     for (int i = 0; i < nlights; ++i) {
         ls.l[i] = make_light_view(lights[i]);
-        ls.l[i].radius = light_radius ? light_radius[i] : 0.0f;
-        if (samples > 1 && ls.l[i].kind != RT_LIGHT_DIRECTIONAL) per_hit += 3 * samples;
+        ls.l[i].radius = shapes ? shapes[i].radius : 0.0f;
+        if (!(samples > 1 && ls.l[i].kind != RT_LIGHT_DIRECTIONAL)) continue;
+        if (shapes && shapes[i].ntris > 0) {
+            // the light's rays in the order find_rays makes them; the first
+            // `samples` are traced, every one made draws two numbers
+            const int32_t nt = shapes[i].ntris;
+            std::vector<int32_t> cnt((size_t)nt);
+            const int32_t made = area_light_rays(nt, samples, cnt.data());
+            if (made < samples)
+                return sfail(RT_ERR_INVALID_ARG,
+                             "rt_render_soft_shadows: a triangle-defined light makes fewer rays than samples");
+            as.first[i] = (int32_t)area_rays.size();
+            as.made[i] = made;
+            as.draws[i] = 2 * made;
+            for (int32_t j = 0; j < nt; ++j)
+                for (int32_t k = 0; k < cnt[(size_t)j]; ++k) area_rays.push_back(make_int4(shapes[i].tris[j], cnt[(size_t)j], k, 0));
+        } else {
+            as.draws[i] = 3 * samples;
+        }
+        per_hit += as.draws[i];
+    }
+    if (!area_rays.empty()) {
+        RT_CUDA_S(S.area.reserve(area_rays.size() * sizeof(int4)), "light ray table allocation");
+        RT_CUDA_S(cudaMemcpyAsync(S.area.ptr, area_rays.data(), area_rays.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                  st),
+                  "light ray table copy");
     }
     MaterialTable mt;
     mt.n = nmaterials;
@@ -484,7 +584,8 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
         d_f = (float *)ctx->fimg.ptr;
     }
     RT_CUDA_S(cudaMemsetAsync(&ctx->d_counters->work, 0, sizeof(int), st), "work counter clear");
-    k_soft_shade<<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, samples, per_hit, rnd, total, (const float *)S.lut.ptr,
+    k_soft_shade<<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, as, (const int4 *)S.area.ptr, s->d_verts, samples,
+                                                 per_hit, rnd, total, (const float *)S.lut.ptr,
                                                  (const int4 *)S.hits.ptr, (const int32_t *)S.prefix.ptr, d_rgb, d_f,
                                                  ctx->d_counters);
     RT_CUDA_S(cudaGetLastError(), "shade launch");

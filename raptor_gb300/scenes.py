@@ -206,6 +206,47 @@ def directional_light(direction, rgb=(255.0, 255.0, 255.0), d=0.0):
             "dir": tuple(float(np.float32(x)) for x in n), "d": float(d)}
 
 
+def regular_polygon(centre, radius, k, tilt=0.0):
+    """k corners of a regular polygon of the given radius around centre, in
+    a plane tilted `tilt` radians from horizontal (about x)."""
+    a = np.arange(k) * (2.0 * np.pi / k)
+    x, z = radius * np.cos(a), radius * np.sin(a)
+    y, z = z * np.sin(tilt), z * np.cos(tilt)
+    return np.stack([x, y, z], 1) + np.asarray(centre)
+
+
+def add_area_light(scene, polygon, rgb=(255.0, 255.0, 255.0), d=0.0, spot=None, colour=(1.0, 1.0, 1.0)):
+    """The scene with a triangle-defined light appended: the convex polygon
+    (k >= 3 corners, in order) fanned into k - 2 triangles flagged as light
+    (skipped by shadow rays) with per-vertex attribute `colour`, and the light
+    dict (kind 0, or 2 with spot = (direction, s_a, s_b)) whose "tris" lists
+    them and whose pos is the corners' mean -- the arguments of the
+    reference's triangle-light constructors (light.h:20-21, 27-29)."""
+    p = np.asarray(polygon, np.float32)
+    k = p.shape[0]
+    v0 = scene["verts"].shape[0]
+    t0 = scene["tris"].shape[0]
+    fan = np.array([[v0, v0 + i, v0 + i + 1] for i in range(1, k - 1)], np.int32)
+    flags = scene.get("flags")
+    flags = np.zeros(t0, np.uint32) if flags is None else flags
+    out = dict(scene)
+    out["verts"] = np.ascontiguousarray(np.concatenate([scene["verts"], p]), np.float32)
+    out["tris"] = np.ascontiguousarray(np.concatenate([scene["tris"], fan]), np.int32)
+    if scene.get("vattr") is not None:
+        out["vattr"] = np.ascontiguousarray(
+            np.concatenate([scene["vattr"], np.tile(np.asarray(colour, np.float32), (k, 1))]), np.float32)
+    out["flags"] = np.concatenate([flags, np.ones(k - 2, np.uint32)])
+    if scene.get("mat_of_tri") is not None:
+        out["mat_of_tri"] = np.concatenate([scene["mat_of_tri"], np.zeros(k - 2, np.int32)])
+    centre = tuple(float(x) for x in p.astype(np.float64).mean(axis=0).astype(np.float32))
+    if spot is None:
+        light = point_light(centre, rgb, d)
+    else:
+        light = spot_light(centre, spot[0], spot[1], spot[2], rgb, d)
+    light["tris"] = list(range(t0, t0 + k - 2))
+    return out, light
+
+
 def _pack(verts, tris, vattr, flags=None):
     nt = tris.shape[0]
     return {"verts": np.ascontiguousarray(verts, dtype=np.float32),

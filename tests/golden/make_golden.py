@@ -286,18 +286,30 @@ def mesh_files():
 def soft_cases():
     """(name, scene, frame) of the soft-shadow fixtures: spherical point
     lights of several radii, one with a directional light beside it, a spot
-    light with a radius, and a terrain."""
+    light with a radius, a terrain, and triangle-defined lights: a quad (two
+    triangles, so 17 rays made for 16), a spot-light disk of 12 triangles
+    beside a spherical light, and a 9-triangle disk over the terrain (the
+    binary32 stride decides which triangles get a second ray)."""
     from raptor_gb300 import scenes
     s, f = scenes.icosphere_scene(freq=8, res=96)
     pl = dict(f["lights"][0], r=0.8)
     sun = scenes.directional_light((-0.4, -0.8, -0.3))
     spot = dict(scenes.spot_light((2.0, 4.0, 2.0), (-0.4, -0.8, -0.4), 0.2, 0.5), r=0.6)
     t, tf = scenes.terrain_scene(size_pow2=64, xres=120, yres=68)
+    sq, quad = scenes.add_area_light(s, [(-0.9, 2.6, -0.9), (0.9, 2.6, -0.9), (0.9, 2.6, 0.9), (-0.9, 2.6, 0.9)],
+                                     rgb=(255.0, 230.0, 200.0))
+    sd, disk = scenes.add_area_light(s, scenes.regular_polygon((1.5, 3.0, 1.5), 0.8, 14, 0.4),
+                                     spot=((-0.45, -0.8, -0.4), 0.25, 0.6))
+    td, tdisk = scenes.add_area_light(t, scenes.regular_polygon((520.0, 330.0, 480.0), 60.0, 11, 0.3),
+                                      rgb=(255.0, 240.0, 220.0))
     return [("ico-point", s, dict(f, lights=[pl])),
             ("ico-point-dir", s, dict(f, lights=[pl, sun])),
             ("ico-spot-point", s, dict(f, lights=[spot, dict(pl, pos=(-3.0, 4.0, 1.0), r=1.5)])),
             ("terrain-point-dir", t, dict(tf, lights=[dict(scenes.point_light((300.0, 260.0, 500.0)), r=40.0),
-                                                      tf["lights"][0]]))]
+                                                      tf["lights"][0]])),
+            ("ico-quad-light", sq, dict(f, lights=[quad])),
+            ("ico-disk-spot-point", sd, dict(f, lights=[disk, dict(pl, pos=(-3.0, 4.0, 1.0), r=1.0)])),
+            ("terrain-disk-dir", td, dict(tf, lights=[tdisk, tf["lights"][0]]))]
 
 
 def soft_main():
@@ -323,8 +335,9 @@ def soft_main():
         arrays[f"soft{k}_frame"] = np.frombuffer(json.dumps(f).encode(), np.uint8)
         arrays[f"soft{k}_scene"] = np.frombuffer(json.dumps(name).encode(), np.uint8)
         arrays[f"soft{k}_offset"] = np.array([offset], np.int64)
-        for key in ("verts", "tris", "vattr"):
-            arrays[f"soft{k}_{key}"] = s[key]
+        for key in ("verts", "tris", "vattr", "flags"):
+            if s.get(key) is not None:
+                arrays[f"soft{k}_{key}"] = s[key]
         # the stream position after the frame, as the restatement counts it
         offset = O.OracleScene(s).render_soft(f, samples, offset, threads=os.cpu_count() or 1)["stream_end"]
         print(f"soft frame {name}: stream {int(arrays[f'soft{k}_offset'][0])} -> {offset}")

