@@ -21,6 +21,10 @@ REF_SO = os.path.join(HERE, "_ref", "libraptor_ref.so")
 # the reference built with soft shadows on (SOFT_SHADOW = REF_SOFT_SAMPLES)
 REF_SOFT_SAMPLES = 16
 REF_SOFT_SO = os.path.join(HERE, "_ref", f"libraptor_ref_soft{REF_SOFT_SAMPLES}.so")
+# ... and with diffuse reflections too (DIFFUSE_REFLECTIONS = REF_DIFFUSE_SAMPLES)
+REF_DIFFUSE_SAMPLES = 16
+REF_DIFFUSE_SO = os.path.join(HERE, "_ref",
+                              f"libraptor_ref_soft{REF_SOFT_SAMPLES}_diffuse{REF_DIFFUSE_SAMPLES}.so")
 # RAPTor source tree (the directory holding common/ and raytracer/); the
 # RAPTOR_REF environment variable overrides the default checkout location.
 REF_SRC = os.environ.get("RAPTOR_REF", "/root/reference/RAPTor")
@@ -40,7 +44,17 @@ class Light(C.Structure):
 
 class Material(C.Structure):
     _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
-                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
+                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32),
+                ("rfd", C.c_float), ("td", C.c_float)]
+
+
+class Sampling(C.Structure):
+    _fields_ = [("soft", C.c_int32), ("diffuse", C.c_int32), ("stream", C.c_int32), ("reserved", C.c_int32),
+                ("offset", C.c_int64), ("seed", C.c_uint64)]
+
+
+STREAM_REFERENCE = 0
+STREAM_PIXEL = 1
 
 
 class ToneMap(C.Structure):
@@ -104,6 +118,8 @@ def make_material(d):
     m.tran = d.get("tran", 0.0)
     m.ri = d.get("ri", 1.0)
     m.flags = d.get("flags", 0)
+    m.rfd = d.get("rfd", 0.0)
+    m.td = d.get("td", 0.0)
     return m
 
 
@@ -126,6 +142,9 @@ def build(verbose: bool = False) -> None:
                        capture_output=not verbose)
         subprocess.run(["make", "-s", "-C", os.path.join(HERE, "refbuild"), f"REF={REF_SRC}",
                         f"SOFT={REF_SOFT_SAMPLES}", "-j8"], check=True, capture_output=not verbose)
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "refbuild"), f"REF={REF_SRC}",
+                        f"SOFT={REF_SOFT_SAMPLES}", f"DIFFUSE={REF_DIFFUSE_SAMPLES}", "-j8"], check=True,
+                       capture_output=not verbose)
 
 
 def _p(a, t):
@@ -235,6 +254,12 @@ def oracle_lib():
                                           _F, C.POINTER(C.c_int64)]
         lib["ro_ref_random"].restype = None
         lib["ro_ref_random"].argtypes = [C.c_int64, C.c_int32, _F]
+        lib["ro_render_distributed"].restype = C.c_int64
+        lib["ro_render_distributed"].argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(Light), C.c_int32,
+                                                 C.POINTER(Material), C.c_int32, C.POINTER(Sampling), C.c_int32,
+                                                 _U8, _I, _F, C.POINTER(C.c_int64)]
+        lib["ro_pixel_stream"].restype = C.c_float
+        lib["ro_pixel_stream"].argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         lib["ro_area_light_rays"].restype = C.c_int32
         lib["ro_area_light_rays"].argtypes = [C.c_int32, C.c_int32, _I]
         lib["ro_lut_cos"].restype = C.c_float
@@ -253,16 +278,12 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
-_ref_soft = None
+_ref_variants = {}
 
 
-def ref_soft_lib():
-    """The reference built with SOFT_SHADOW = REF_SOFT_SAMPLES (x86 only).
-    Its random generator is process-wide: every soft frame it renders moves
-    it on."""
-    global _ref_soft
-    if _ref_soft is None:
-        lib = _load_ref(REF_SOFT_SO)
+def _ref_variant(path):
+    if path not in _ref_variants:
+        lib = _load_ref(path)
         lib["rref_random"].restype = None
         lib["rref_random"].argtypes = [C.c_int32, _F]
         lib["rref_lut_cos"].restype = C.c_float
@@ -270,8 +291,23 @@ def ref_soft_lib():
         lib["rref_lut_sin"].restype = C.c_float
         lib["rref_lut_sin"].argtypes = [C.c_float]
         lib["rref_soft_shadow_samples"].restype = C.c_int32
-        _ref_soft = lib
-    return _ref_soft
+        lib["rref_diffuse_samples"].restype = C.c_int32
+        _ref_variants[path] = lib
+    return _ref_variants[path]
+
+
+def ref_soft_lib():
+    """The reference built with SOFT_SHADOW = REF_SOFT_SAMPLES (x86 only).
+    Its random generator is process-wide: every soft frame it renders moves
+    it on."""
+    return _ref_variant(REF_SOFT_SO)
+
+
+def ref_diffuse_lib():
+    """The reference built with SOFT_SHADOW = REF_SOFT_SAMPLES and
+    DIFFUSE_REFLECTIONS = REF_DIFFUSE_SAMPLES (x86 only); its own generator,
+    separate from ref_soft_lib's."""
+    return _ref_variant(REF_DIFFUSE_SO)
 
 
 def ref_lib():
@@ -366,6 +402,29 @@ class OracleScene(_SceneBase):
             raise ValueError("oracle soft-shadow render refused its arguments")
         return {"rgb": rgb, "ids": ids, "fimg": fimg, "rays": n, "stream_end": end.value}
 
+    def render_distributed(self, frame, soft=1, diffuse=0, stream=STREAM_REFERENCE, offset=0, seed=0, threads=1,
+                           want_ids=False, want_float=False):
+        """ro_render_distributed: the reference's ray tree with SOFT_SHADOW =
+        soft and DIFFUSE_REFLECTIONS = diffuse, numbers from the reference's
+        generator at position `offset` (serial) or from per-pixel streams
+        keyed by `seed`.  Returns rgb, ids, fimg, rays and drawn (numbers
+        the frame drew)."""
+        cam = make_camera(frame["camera"])
+        W, H = cam.xres, cam.yres
+        rgb = np.zeros((H, W, 3), np.uint8)
+        ids = np.full((H, W), -2, np.int32) if want_ids else None
+        fimg = np.zeros((H, W, 3), np.float32) if want_float else None
+        ls = make_lights(frame["lights"])
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        smp = Sampling(int(soft), int(diffuse), int(stream), 0, int(offset), int(seed))
+        drawn = C.c_int64(0)
+        n = self.lib["ro_render_distributed"](self.h, C.byref(cam), ls, len(frame["lights"]), table, len(table),
+                                              C.byref(smp), int(threads), _p(rgb, C.c_uint8), _p(ids, C.c_int32),
+                                              _p(fimg, C.c_float), C.byref(drawn))
+        if n < 0:
+            raise ValueError("oracle distributed render refused its arguments")
+        return {"rgb": rgb, "ids": ids, "fimg": fimg, "rays": n, "drawn": drawn.value}
+
     def pixel_secondary_rays(self, frame, x, y):
         """(primary hit id, ogn, dir, tmax) of the secondary rays pixel
         (x, y) of the frame spawns: its AO rays for an AO frame, else one
@@ -423,11 +482,12 @@ class RefScene(_SceneBase):
     """The reference's own bvh + ray_tracer behind the harness (x86 only)."""
     prefix = "rref_"
 
-    def __init__(self, scene, material, soft=False):
+    def __init__(self, scene, material, soft=False, diffuse=False):
         """material: one material dict, or a list of them indexed by
         scene["mat_of_tri"] (one coloured_mapper_shader per entry).  soft:
-        the reference built with soft shadows (ref_soft_lib)."""
-        self.lib = ref_soft_lib() if soft else ref_lib()
+        the reference built with soft shadows (ref_soft_lib); diffuse: with
+        soft shadows and diffuse reflections (ref_diffuse_lib)."""
+        self.lib = ref_diffuse_lib() if diffuse else ref_soft_lib() if soft else ref_lib()
         v, t, a, f = _scene_arrays(scene)
         self._keep = (v, t, a, f)
         if isinstance(material, (list, tuple)):
@@ -586,6 +646,11 @@ def ref_random(start, n):
     out = np.empty(n, np.float32)
     oracle_lib()["ro_ref_random"](int(start), int(n), _p(out, C.c_float))
     return out
+
+
+def pixel_stream(seed, pixel, k):
+    """Number k of pixel `pixel`'s stream (ro_pixel_stream)."""
+    return oracle_lib()["ro_pixel_stream"](int(seed), int(pixel), int(k))
 
 
 def area_light_rays(ntris, n):

@@ -81,7 +81,7 @@ void *rref_scene_create(const float *verts, int32_t nverts, const int32_t *tris,
     s->opaque.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
                                                ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
                                                ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.0f, 1.0f, m->rf,
-                                               0.0f, 0.0f, nullptr, kd_map));
+                                               0.0f, m->rfd, nullptr, kd_map));
     s->transparent.reset(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
                                                     ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
                                                     ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, 0.5f, 1.0f));
@@ -105,8 +105,8 @@ void *rref_scene_create(const float *verts, int32_t nverts, const int32_t *tris,
 
 // A scene whose triangles carry per-triangle materials from a table (the
 // reference's material pointer per triangle, triangle.h:99-106): one
-// coloured_mapper_shader per entry with its tran, ri and rf; kd follows the
-// vertex colour unless the entry says otherwise.
+// coloured_mapper_shader per entry with its tran, ri, rf, td and rfd; kd
+// follows the vertex colour unless the entry says otherwise.
 void *rref_scene_create_mt(const float *verts, int32_t nverts, const int32_t *tris, int32_t ntris, const float *vattr,
                            const uint32_t *flags, const ro_material *mats, int32_t nmats, const int32_t *mat_of_tri)
 {
@@ -120,7 +120,7 @@ void *rref_scene_create_mt(const float *verts, int32_t nverts, const int32_t *tr
         s->table.emplace_back(new coloured_mapper_shader(ext_colour_t(m->ka[0], m->ka[1], m->ka[2]),
                                                          ext_colour_t(m->kd[0], m->kd[1], m->kd[2]),
                                                          ext_colour_t(m->ks[0], m->ks[1], m->ks[2]), m->ns, m->tran,
-                                                         m->ri, m->rf, 0.0f, 0.0f, nullptr, map));
+                                                         m->ri, m->rf, m->td, m->rfd, nullptr, map));
     }
     s->store.reserve(ntris);
     for (int32_t i = 0; i < ntris; ++i) {
@@ -379,5 +379,16 @@ float rref_lut_sin(float a) { return cos_lut.get_sin(a); }
 
 // Shadow rays per light of a primary hit in this build (SOFT_SHADOW, or 1).
 int32_t rref_soft_shadow_samples(void) { return SHADOW_ARRAY_SIZE; }
+
+// Rays of a diffuse reflection of a primary hit in this build
+// (DIFFUSE_REFLECTIONS, or 0 when it is off).
+int32_t rref_diffuse_samples(void)
+{
+#ifdef DIFFUSE_REFLECTIONS
+    return MAX_SECONDARY_RAYS;
+#else
+    return 0;
+#endif
+}
 
 }  // extern "C"

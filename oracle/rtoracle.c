@@ -789,6 +789,39 @@ static inline uint8_t clip8(float v) { return (uint8_t)smin(255.0f, smax(0.0f, v
  * ray power is compared after promotion to double. */
 #define RO_MIN_REFLECTIVE_POWER 0.1
 
+/* One light's term of the coloured Phong (coloured_mapper_shader::shade,
+ * coloured_mapper_shader.cc:76-112) added to c: ldir / len the light's
+ * first shadow ray, lmagn the fraction of its rays that reached it, vd the
+ * incoming ray's direction.  Nothing when the surface faces away. */
+static void phong_term(const ro_light *L, v3 ldir, float len, float lmagn, v3 sn, v3 vd, v3 kd, v3 ks, float ns,
+                       v3 *c)
+{
+    const float shade = vdot(ldir, sn);
+    if (shade < 0.0f) return;
+    const v3 ref = vsub(ldir, vmul(sn, 2.0f * shade));
+    const float rdr = vdot(vd, ref);
+    v3 sc = mk(shade * kd.x, shade * kd.y, shade * kd.z);
+    if (rdr > 0.0f) {
+        const float p = (float)pow((double)rdr, (double)ns);
+        sc = mk(sc.x + p * ks.x, sc.y + p * ks.y, sc.z + p * ks.z);
+    }
+    /* light::get_light_intensity (light.h:44-59) */
+    const float dist = len * L->d;
+    const float d_scale = (dist * dist) + 1.0f;
+    v3 I;
+    if (L->kind == 2 && L->s_b != 0.0f) {
+        /* spot light: falls off with the angle off its axis */
+        const float a = acosf(vdot(ldir, ld3(L->dir)));
+        const float p = (a - L->s_a) / (L->s_b - L->s_a);
+        const float f = smax(0.0f, smin(1.0f, 1.0f - p));
+        const float fs = f / d_scale;
+        I = mk((L->rgb[0] / 255.0f) * fs, (L->rgb[1] / 255.0f) * fs, (L->rgb[2] / 255.0f) * fs);
+    } else {
+        I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale, (L->rgb[2] / 255.0f) / d_scale);
+    }
+    *c = mk(c->x + I.x * (sc.x * lmagn), c->y + I.y * (sc.y * lmagn), c->z + I.z * (sc.z * lmagn));
+}
+
 /* The colour of one ray (ray_trace_engine::ray_trace, raytracer.cc:20-87):
  * closest hit; hit refinement; one shadow ray per light; coloured Phong
  * (coloured_mapper_shader::shade, coloured_mapper_shader.cc:76-112); then,
@@ -864,30 +897,7 @@ static int32_t trace_colour(render_job *J, const ro_ray *r, float magn, int firs
             if (first && J->occl && l == 0) J->occl[pix] = (uint8_t)occ;
         }
         const float lmagn = (float)made / (float)nrays;   /* made_it / nr_pending_shadows */
-        const float shade = vdot(sr.d, sn);
-        if (shade < 0.0f) continue;
-        const v3 ref = vsub(sr.d, vmul(sn, 2.0f * shade));
-        const float rdr = vdot(r->d, ref);
-        v3 sc = mk(shade * kd.x, shade * kd.y, shade * kd.z);
-        if (rdr > 0.0f) {
-            const float p = (float)pow((double)rdr, (double)m->ns);
-            sc = mk(sc.x + p * ks.x, sc.y + p * ks.y, sc.z + p * ks.z);
-        }
-        /* light::get_light_intensity (light.h:44-59) */
-        const float dist = len * L->d;
-        const float d_scale = (dist * dist) + 1.0f;
-        v3 I;
-        if (L->kind == 2 && L->s_b != 0.0f) {
-            /* spot light: falls off with the angle off its axis */
-            const float a = acosf(vdot(sr.d, ld3(L->dir)));
-            const float p = (a - L->s_a) / (L->s_b - L->s_a);
-            const float f = smax(0.0f, smin(1.0f, 1.0f - p));
-            const float fs = f / d_scale;
-            I = mk((L->rgb[0] / 255.0f) * fs, (L->rgb[1] / 255.0f) * fs, (L->rgb[2] / 255.0f) * fs);
-        } else {
-            I = mk((L->rgb[0] / 255.0f) / d_scale, (L->rgb[1] / 255.0f) / d_scale, (L->rgb[2] / 255.0f) / d_scale);
-        }
-        c = mk(c.x + I.x * (sc.x * lmagn), c.y + I.y * (sc.y * lmagn), c.z + I.z * (sc.z * lmagn));
+        phong_term(L, sr.d, len, lmagn, sn, r->d, kd, ks, m->ns, &c);
     }
     c = vadd(c, ld3(m->ka));
     /* ray::reflect (ray.cc:118-135) */
@@ -1146,6 +1156,299 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
     free(hit);
     if (stream_end) *stream_end = stream_offset + total;
     return rays;
+}
+
+/* ------------------------------------------- Distributed ray tracing */
+
+float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint32_t k)
+{
+    const uint32_t ctr[4] = {pixel, k >> 2, 0u, 0x53545245u};
+    uint32_t w[4];
+    ro_philox4x32(ctr, (uint32_t)seed, (uint32_t)(seed >> 32), w);
+    return (float)w[k & 3u] * (1.0f / 4294967296.0f);
+}
+
+/* Where a pixel's numbers come from: the reference's generator (g), or
+ * the pixel's own stream. */
+typedef struct {
+    ref_rng *g;
+    uint64_t seed;
+    uint32_t pixel;
+    uint32_t k;       /* numbers this pixel has drawn */
+} draw_src;
+
+static inline float draw_next(draw_src *S)
+{
+    const uint32_t k = S->k++;
+    return S->g ? ref_rng_next(S->g) : ro_pixel_stream(S->seed, S->pixel, k);
+}
+
+typedef struct {
+    const ro_scene *s;
+    const ro_camera *cam;
+    const ro_light *lights;
+    int32_t nlights;
+    const ro_material *mats;
+    int32_t nmats;
+    ro_sampling smp;
+    uint8_t *rgb;
+    int32_t *hit_id;
+    float *fimg;
+    ref_rng *g;            /* RO_STREAM_REFERENCE */
+    int64_t rays, drawn;
+    int bad;               /* a case the reference cannot render (stale rays, componant overflow) */
+    int32_t next_row;
+    pthread_mutex_t *lock;
+} dist_job;
+
+/* A light's shadow rays at a hit (ray::find_rays, ray.cc:91-104 ->
+ * light::find_rays, light.h:62-164): one to the centre for a directional
+ * light or n = 1, else n rays to random points -- three numbers per ray of
+ * a spherical light, two per ray a triangle-defined light makes (the first
+ * n traced).  first / first_len: the first ray; returns the fraction that
+ * reached the light. */
+static float light_rays(dist_job *J, draw_src *S, const ro_light *L, v3 start, int32_t n, ro_ray *first,
+                        float *first_len)
+{
+    const ro_scene *s = J->s;
+    if (light_is_directional(L) || n == 1) {
+        shadow_ray(L, start, first, first_len);
+        J->rays += 1;
+        return nearer(s, first, *first_len) ? 0.0f : 1.0f;
+    }
+    int32_t made = 0;
+    if (L->ntris > 0) {
+        const int32_t T = L->ntris, ppt = n / T, extra = n - T * ppt;
+        const float stride = (float)T / (float)(extra > 1 ? extra : 1);
+        float at = 0.0f;
+        int32_t k = 0;
+        for (int32_t j = 0; j < T; ++j) {
+            int32_t cnt = ppt;
+            if (j == (int32_t)at) {
+                ++cnt;
+                at += stride;
+            }
+            for (int32_t i = 0; i < cnt; ++i, ++k) {
+                float rnd[2];
+                rnd[0] = draw_next(S);
+                rnd[1] = draw_next(S);
+                if (k >= n) continue;   /* made, not traced */
+                const area_ray e = {L->tris[j], cnt, i};
+                ro_ray ri;
+                float li;
+                area_light_ray(s, &e, start, rnd, &ri, &li);
+                if (k == 0) { *first = ri; *first_len = li; }
+                if (!nearer(s, &ri, li)) ++made;
+            }
+        }
+        if (k < n) J->bad = 1;   /* the reference would trace stale rays */
+    } else {
+        for (int32_t i = 0; i < n; ++i) {
+            float rnd[3];
+            rnd[0] = draw_next(S);
+            rnd[1] = draw_next(S);
+            rnd[2] = draw_next(S);
+            ro_ray ri;
+            float li;
+            soft_ray(L, start, n, i, rnd, &ri, &li);
+            if (i == 0) { *first = ri; *first_len = li; }
+            if (!nearer(s, &ri, li)) ++made;
+        }
+    }
+    J->rays += n;
+    return (float)made / (float)n;
+}
+
+/* The rays of a reflection or refraction set about direction ref from
+ * start (ray::reflect ray.cc:137-182, ray::refract ray.cc:236-280): one
+ * ray along ref when the frame has no diffuse reflections or spread is 0;
+ * else max(diffuse / comp, 1) rays ref + perpen * x + cross * y, with
+ * perpen = (ref.z, ref.y, -ref.x), cross = ref x perpen, x, y = r cos a,
+ * r sin a for r = spread * u1, a = 2 pi * u2 (through the cosine table);
+ * directions are not normalised.  Returns the count; *child_comp the
+ * rays' componant. */
+static int32_t spread_rays(dist_job *J, draw_src *S, v3 start, v3 ref, float spread, int32_t comp, ro_ray *out,
+                           int32_t *child_comp)
+{
+    if (J->smp.diffuse == 0 || spread == 0.0f) {
+        out[0].o = start;
+        out[0].d = ref;
+        *child_comp = comp;
+        return 1;
+    }
+    if (comp > (1 << 28)) {   /* comp << 2 would overflow the reference's int */
+        J->bad = 1;
+        *child_comp = comp;
+        return 0;
+    }
+    *child_comp = comp << 2;
+    const v3 perpen = mk(ref.z, ref.y, -ref.x);
+    const v3 cross = mk((ref.y * perpen.z) - (ref.z * perpen.y), (ref.z * perpen.x) - (ref.x * perpen.z),
+                        (ref.x * perpen.y) - (ref.y * perpen.x));
+    int32_t nr = J->smp.diffuse / comp;
+    if (nr < 1) nr = 1;
+    for (int32_t i = 0; i < nr; ++i) {
+        const float r_off = draw_next(S) * spread;
+        const float a_off = draw_next(S) * (2.0f * RO_PI);
+        const float x_off = r_off * lut_cos(a_off);
+        const float y_off = r_off * lut_sin(a_off);
+        out[i].o = start;
+        out[i].d = vadd(vadd(ref, vmul(perpen, x_off)), vmul(cross, y_off));
+    }
+    return nr;
+}
+
+/* The colour of one ray of a distributed frame (see ro_render_distributed). */
+static int32_t dist_colour(dist_job *J, draw_src *S, const ro_ray *r, float magn, int32_t comp, v3 *out)
+{
+    const ro_scene *s = J->s;
+    ro_hit h;
+    const int32_t id = closest(s, r, &h);
+    J->rays += 1;
+    if (!(h.d < RO_MAX_DIST)) {
+        *out = ld3(J->cam->background);
+        return id;
+    }
+    const ro_material *m = &J->mats[s->mat ? s->mat[id] : 0];
+    v3 dst, sn, geo, vt;
+    int out_in;
+    hit_setup(s, r, id, &h, &dst, &sn, &geo, &vt, &out_in);
+    const v3 start = offset_start(dst, geo);
+    const v3 kd = cur_kd(s, m, vt);
+    const v3 ks = ld3(m->ks);
+    /* generate_rays: every light's rays, then the reflection and the
+     * refraction sets (coloured_mapper_shader.cc:9-38) */
+    int32_t n = J->smp.soft / comp;
+    if (n < 1) n = 1;
+    ro_ray lray[64];
+    float llen[64], lmagn[64];
+    for (int32_t l = 0; l < J->nlights; ++l) lmagn[l] = light_rays(J, S, &J->lights[l], start, n, &lray[l], &llen[l]);
+    ro_ray refl[64], refr[64];
+    int32_t nrefl = 0, nrefr = 0, comp_refl = comp, comp_refr = comp;
+    const float refl_power = magn * m->rf;
+    if ((double)refl_power > RO_MIN_REFLECTIVE_POWER) {
+        const float rdn = 2.0f * vdot(r->d, sn);
+        nrefl = spread_rays(J, S, start, vsub(r->d, vmul(sn, rdn)), m->rfd, comp, refl, &comp_refl);
+    }
+    const float refr_power = magn * m->tran;
+    if ((double)refr_power > RO_MIN_REFLECTIVE_POWER) {
+        float ri = m->ri;
+        const float rdn = -vdot(r->d, sn);
+        if (out_in) ri = 1.0f / ri;
+        const float cos_t2 = 1.0f - (ri * ri) * (1.0f - rdn * rdn);
+        if (!(cos_t2 < 0.0f)) {
+            const float off = ri * rdn - sqrtf(cos_t2);
+            nrefr = spread_rays(J, S, offset_start_in(dst, geo), vadd(vmul(r->d, ri), vmul(sn, off)), m->td, comp,
+                                refr, &comp_refr);
+        }
+    }
+    /* shade with each light's first ray and unoccluded fraction */
+    v3 c = mk(0.0f, 0.0f, 0.0f);
+    for (int32_t l = 0; l < J->nlights; ++l) phong_term(&J->lights[l], lray[l].d, llen[l], lmagn[l], sn, r->d, kd, ks,
+                                                       m->ns, &c);
+    c = vadd(c, ld3(m->ka));
+    /* the secondary rays, in order, then their mean colours */
+    v3 sum_refl = mk(0.0f, 0.0f, 0.0f), sum_refr = mk(0.0f, 0.0f, 0.0f);
+    for (int32_t i = 0; i < nrefl && !J->bad; ++i) {
+        v3 ci;
+        (void)dist_colour(J, S, &refl[i], refl_power, comp_refl, &ci);
+        sum_refl = vadd(sum_refl, ci);
+    }
+    for (int32_t i = 0; i < nrefr && !J->bad; ++i) {
+        v3 ci;
+        (void)dist_colour(J, S, &refr[i], refr_power, comp_refr, &ci);
+        sum_refr = vadd(sum_refr, ci);
+    }
+    if (m->rf > 0.0f && nrefl > 0) c = vadd(c, vmul(vdivs(sum_refl, (float)nrefl), m->rf));
+    if (m->tran > 0.0f && nrefr > 0) c = vadd(c, vmul(vdivs(sum_refr, (float)nrefr), m->tran));
+    *out = c;
+    return id;
+}
+
+static void dist_pixel(dist_job *J, const cam_state *cs, ref_rng *g, int32_t x, int32_t y)
+{
+    const size_t pix = (size_t)x + (size_t)y * (size_t)J->cam->xres;
+    draw_src S = {g, J->smp.seed, (uint32_t)pix, 0u};
+    const ro_ray r = cam_ray(cs, x, y);
+    v3 c;
+    const int32_t id = dist_colour(J, &S, &r, 1.0f, 1, &c);
+    J->drawn += S.k;
+    if (J->hit_id) J->hit_id[pix] = id;
+    if (J->fimg) { J->fimg[3 * pix] = c.x; J->fimg[3 * pix + 1] = c.y; J->fimg[3 * pix + 2] = c.z; }
+    J->rgb[3 * pix] = clip8(c.x);
+    J->rgb[3 * pix + 1] = clip8(c.y);
+    J->rgb[3 * pix + 2] = clip8(c.z);
+}
+
+static void *dist_worker(void *arg)
+{
+    dist_job *J0 = (dist_job *)arg;
+    dist_job J = *J0;   /* private counters */
+    J.rays = 0;
+    J.drawn = 0;
+    J.bad = 0;
+    const cam_state cs = cam_setup(J.cam);
+    for (;;) {
+        pthread_mutex_lock(J0->lock);
+        const int32_t y = J0->next_row++;
+        pthread_mutex_unlock(J0->lock);
+        if (y >= J.cam->yres) break;
+        for (int32_t x = 0; x < J.cam->xres; ++x) dist_pixel(&J, &cs, J.g, x, y);
+    }
+    pthread_mutex_lock(J0->lock);
+    J0->rays += J.rays;
+    J0->drawn += J.drawn;
+    J0->bad |= J.bad;
+    pthread_mutex_unlock(J0->lock);
+    return NULL;
+}
+
+int64_t ro_render_distributed(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                              const ro_material *mats, int32_t nmats, const ro_sampling *smp, int32_t nthreads,
+                              uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *drawn)
+{
+    if (!s || !s->nodes || !cam || !mats || nmats < 1 || !rgb || !smp || smp->soft < 1 || smp->soft > 64 ||
+        smp->diffuse < 0 || smp->diffuse > 64 || nlights < 0 || nlights > 64 || (nlights > 0 && !lights) ||
+        (smp->stream != RO_STREAM_REFERENCE && smp->stream != RO_STREAM_PIXEL) || smp->offset < 0)
+        return -1;
+    for (int32_t l = 0; l < nlights; ++l) {
+        const ro_light *L = &lights[l];
+        if (L->ntris < 0 || (L->ntris > 0 && (!L->tris || L->kind == 1 || L->r != 0.0f))) return -1;
+        for (int32_t j = 0; j < L->ntris; ++j)
+            if (L->tris[j] < 0 || L->tris[j] >= s->ntris) return -1;
+    }
+    for (int32_t i = 0; i < nmats; ++i)
+        if (!(mats[i].rf >= 0.0f && mats[i].rf < 1.0f) || !(mats[i].tran >= 0.0f && mats[i].tran < 1.0f)) return -1;
+    if (s->mat)
+        for (int32_t i = 0; i < s->ntris; ++i)
+            if (s->mat[i] < 0 || s->mat[i] >= nmats) return -1;
+    pthread_once(&g_cos_lut_once, build_cos_lut);
+    dist_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.cam = cam; J.lights = lights; J.nlights = nlights; J.mats = mats; J.nmats = nmats; J.smp = *smp;
+    J.rgb = rgb; J.hit_id = hit_id; J.fimg = fimg;
+    ref_rng g;
+    if (smp->stream == RO_STREAM_REFERENCE) {
+        ref_rng_init(&g);
+        for (int64_t i = 0; i < smp->offset; ++i) (void)ref_rng_next(&g);
+        J.g = &g;
+        nthreads = 1;   /* one stream drawn in pixel order */
+    }
+    pthread_mutex_t lock;
+    pthread_mutex_init(&lock, NULL);
+    J.lock = &lock;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    int started = 0;
+    for (int i = 1; i < nthreads; ++i)
+        if (pthread_create(&th[started], NULL, dist_worker, &J) == 0) ++started;
+    dist_worker(&J);
+    for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+    pthread_mutex_destroy(&lock);
+    if (J.bad) return -1;
+    if (drawn) *drawn = J.drawn;
+    return J.rays;
 }
 
 int32_t ro_scene_set_normals(ro_scene *s, const float *corner_normals)

@@ -65,6 +65,8 @@ typedef struct ro_material {
     float tran;   /* transparency: refracted colour weight, the shader's tran (0: none) */
     float ri;     /* refractive index, the shader's ri */
     uint32_t flags;   /* RO_MAT_NO_VERTEX_COLOUR: kd not modulated by the vertex attribute */
+    float rfd;    /* spread of a diffuse reflection, the shader's rfd (0: sharp); DIFFUSE_REFLECTIONS builds only */
+    float td;     /* spread of a diffuse refraction, the shader's td (0: sharp); DIFFUSE_REFLECTIONS builds only */
 } ro_material;
 #define RO_MAT_NO_VERTEX_COLOUR 1u
 
@@ -181,6 +183,43 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
  * compiled out of its release build, which draws for every ray made and
  * traces the first n), or -1 for ntris < 1 or n < 1. */
 int32_t ro_area_light_rays(int32_t ntris, int32_t n, int32_t *cnt);
+
+/* Distributed ray tracing as the reference renders it when built with
+ * SOFT_SHADOW = soft and DIFFUSE_REFLECTIONS = diffuse
+ * (ray_trace_engine::ray_trace raytracer.cc:20-87 with ray::find_rays
+ * ray.cc:91-104, ray::reflect ray.cc:118-182, ray::refract ray.cc:198-281,
+ * light::find_rays light.h:62-164 and combind_secondary_rays
+ * coloured_mapper_shader.cc:117-130): at every hit of a ray of componant c
+ * (1 for camera rays), max(soft / c, 1) shadow rays per spherical or
+ * triangle-defined light; a reflection (power magn * rf above 0.1) is one
+ * mirror ray, or with diffuse > 0 and the material's rfd != 0,
+ * max(diffuse / c, 1) rays spread by rfd about it, each of componant 4c;
+ * refractions the same with tran and td; each set's mean colour is added
+ * times rf, then tran.  The random numbers come, in the reference's order
+ * within a pixel, from stream: RO_STREAM_REFERENCE, the reference's own
+ * process-wide generator from position offset, pixels in the reference's
+ * order (x + y * xres) -- serial, nthreads ignored; RO_STREAM_PIXEL, one
+ * stream per pixel (ro_pixel_stream with seed).  drawn (nullable) receives
+ * the count of numbers the frame drew.  Returns rays traced, or -1 on bad
+ * arguments. */
+typedef struct ro_sampling {
+    int32_t soft;       /* SOFT_SHADOW: 1..64 (1: the default build) */
+    int32_t diffuse;    /* DIFFUSE_REFLECTIONS: 0..64 (0: the default build) */
+    int32_t stream;     /* RO_STREAM_REFERENCE or RO_STREAM_PIXEL */
+    int32_t reserved;
+    int64_t offset;     /* RO_STREAM_REFERENCE: numbers drawn before the frame */
+    uint64_t seed;      /* RO_STREAM_PIXEL: the streams' key */
+} ro_sampling;
+#define RO_STREAM_REFERENCE 0
+#define RO_STREAM_PIXEL 1
+int64_t ro_render_distributed(const ro_scene *s, const ro_camera *cam, const ro_light *lights, int32_t nlights,
+                              const ro_material *mats, int32_t nmats, const ro_sampling *smp, int32_t nthreads,
+                              uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *drawn);
+
+/* Number k of pixel `pixel`'s stream: word k % 4 of Philox4x32-10 with
+ * counter (pixel, k / 4, 0, 0x53545245) and key (seed low, seed high), as
+ * (float)word * 2^-32 -- the reference generator's conversion. */
+float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint32_t k);
 
 /* n numbers of the reference's random stream (common/common.cc:35-105)
  * from position start of a freshly seeded generator. */

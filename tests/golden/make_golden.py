@@ -351,15 +351,79 @@ def soft_main():
     print("wrote ref_soft.npz")
 
 
+def dist_cases():
+    """(name, scene, frame, diffuse) of the distributed-ray-tracing
+    fixtures: ray trees (mirror and glass) with soft shadows from the
+    SOFT_SHADOW = 16 build (diffuse False), and diffuse reflections and
+    refractions from the SOFT_SHADOW = 16, DIFFUSE_REFLECTIONS = 16 build
+    (diffuse True)."""
+    from raptor_gb300 import scenes
+    g, gf = scenes.glass_scene(freq=8, res=64)
+    glights = [dict(gf["lights"][0], r=0.7), gf["lights"][1]]
+    gq, quad = scenes.add_area_light(g, [(1.5, 3.0, 1.5), (3.0, 3.0, 1.5), (3.0, 3.4, 3.0), (1.5, 3.4, 3.0)])
+    ico, fi = scenes.icosphere_scene(freq=8, res=72)
+    # off the sphere's symmetry plane x = 0, where mirror rays would run
+    # along edges (ties in secondary hits)
+    fi = dict(fi, camera=scenes.look_at_camera((0.013, 0.5, 4.0), (0.0, 0.0, 0.0), 60.0, 72, 72))
+    mirror = [dict(fi["material"], rf=0.5)]
+    ico = dict(ico, mat_of_tri=np.zeros(ico["tris"].shape[0], np.int32))
+    dm = [dict(gf["materials"][0], rfd=0.2), dict(gf["materials"][1], rfd=0.1, td=0.05)]
+    ishiny = [dict(fi["material"], rf=0.6, rfd=0.3)]
+    spot = dict(scenes.spot_light((2.0, 4.0, 2.0), (-0.4, -0.8, -0.4), 0.2, 0.5), r=0.6)
+    iq, iquad = scenes.add_area_light(ico, [(-0.9, 2.6, -0.9), (0.9, 2.6, -0.9), (0.9, 2.6, 0.9), (-0.9, 2.6, 0.9)])
+    return [("glass-soft", g, dict(gf, lights=glights), False),
+            ("glass-quad-light", gq, dict(gf, lights=[quad, gf["lights"][1]]), False),
+            ("ico-mirror-spot", ico, dict(fi, lights=[spot, dict(fi["lights"][0], r=0.8)], materials=mirror,
+                                          material=mirror[0]), False),
+            ("glass-diffuse", g, dict(gf, lights=glights, materials=dm, material=dm[0]), True),
+            ("ico-diffuse-quad", iq, dict(fi, lights=[iquad, spot], materials=ishiny, material=ishiny[0]), True)]
+
+
+def dist_main():
+    """ref_distributed.npz, in a process whose reference generators are
+    untouched: each build's frames rendered one after another."""
+    import ctypes as C
+    import oracle as O
+    arrays = {"soft": np.array([O.REF_SOFT_SAMPLES], np.int32), "diffuse": np.array([O.REF_DIFFUSE_SAMPLES], np.int32)}
+    offset = {False: 0, True: 0}
+    for k, (name, s, f, diffuse) in enumerate(dist_cases()):
+        arrays[f"dist{k}_rgb"] = O.RefScene(s, f["materials"], soft=not diffuse, diffuse=diffuse).render(f)["rgb"]
+        arrays[f"dist{k}_frame"] = np.frombuffer(json.dumps(f).encode(), np.uint8)
+        arrays[f"dist{k}_name"] = np.frombuffer(json.dumps(name).encode(), np.uint8)
+        arrays[f"dist{k}_diffuse"] = np.array([O.REF_DIFFUSE_SAMPLES if diffuse else 0], np.int32)
+        arrays[f"dist{k}_offset"] = np.array([offset[diffuse]], np.int64)
+        for key in ("verts", "tris", "vattr", "flags", "mat_of_tri"):
+            if s.get(key) is not None:
+                arrays[f"dist{k}_{key}"] = s[key]
+        out = O.OracleScene(s).render_distributed(f, soft=O.REF_SOFT_SAMPLES,
+                                                  diffuse=O.REF_DIFFUSE_SAMPLES if diffuse else 0,
+                                                  offset=offset[diffuse])
+        print(f"distributed frame {name}: stream {offset[diffuse]} -> {offset[diffuse] + out['drawn']}")
+        offset[diffuse] += out["drawn"]
+    for diffuse, lib in ((False, O.ref_soft_lib()), (True, O.ref_diffuse_lib())):
+        tail = np.empty(64, np.float32)
+        lib["rref_random"](64, tail.ctypes.data_as(C.POINTER(C.c_float)))
+        if not np.array_equal(tail, O.ref_random(offset[diffuse], 64)):
+            raise SystemExit("distributed stream accounting differs from the reference")
+    arrays["stream_end"] = np.array([offset[False], offset[True]], np.int64)
+    np.savez_compressed(os.path.join(HERE, "ref_distributed.npz"), **arrays)
+    print("wrote ref_distributed.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("RAPTOR_REF", "/root/reference/RAPTor"))
     ap.add_argument("--soft", action="store_true", help="write only ref_soft.npz (needs a fresh process)")
+    ap.add_argument("--dist", action="store_true", help="write only ref_distributed.npz (needs a fresh process)")
     a = ap.parse_args()
     if a.soft:
         import oracle as O
         O.build()
         return soft_main()
+    if a.dist:
+        import oracle as O
+        O.build()
+        return dist_main()
     kats = parse_bih_tests(os.path.join(a.ref, "raytracer/unit_tests/bih_tests.cc"))
     json.dump(kats, open(os.path.join(HERE, "bih_kats.json"), "w"), indent=1)
     mort = parse_morton_tests(os.path.join(a.ref, "raytracer/unit_tests/vint_tests.cc"))

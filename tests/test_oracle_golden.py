@@ -369,3 +369,63 @@ def test_oracle_soft_shadows_match_reference(oracle, soft_golden):
         hard = osc.render(frame)["rgb"]
         assert (np.abs(hard.astype(int) - ref.astype(int)).max(-1) > 1).mean() > 0.005
     assert end == int(soft_golden["stream_end"][0])
+
+
+@pytest.fixture(scope="module")
+def dist_golden():
+    return np.load(os.path.join(GOLDEN, "ref_distributed.npz"))
+
+
+def dist_cases(g):
+    k = 0
+    while f"dist{k}_rgb" in g.files:
+        frame = json.loads(g[f"dist{k}_frame"].tobytes().decode())
+        scene = {key: g[f"dist{k}_{key}"] for key in ("verts", "tris", "vattr", "flags", "mat_of_tri")
+                 if f"dist{k}_{key}" in g.files}
+        yield k, scene, frame, int(g[f"dist{k}_diffuse"][0]), int(g[f"dist{k}_offset"][0]), g[f"dist{k}_rgb"]
+        k += 1
+
+
+def test_oracle_distributed_match_reference(oracle, dist_golden):
+    """The reference built with SOFT_SHADOW = 16 (mirror and glass ray trees
+    with soft shadows, spherical, spot and triangle-defined lights) and with
+    SOFT_SHADOW = 16 and DIFFUSE_REFLECTIONS = 16 (diffuse reflections and
+    refractions), each build's frames rendered one after another from its
+    fresh generator: the restatement, drawing the reference's stream in the
+    reference's order from each frame's position, reproduces every pixel
+    except edge ties and counts the numbers each frame draws exactly."""
+    from parity import edge_distance
+    soft = int(dist_golden["soft"][0])
+    end = {0: 0}
+    for k, scene, frame, diffuse, offset, ref in dist_cases(dist_golden):
+        assert offset == end.get(diffuse, 0)
+        osc = oracle.OracleScene(scene)
+        out = osc.render_distributed(frame, soft=soft, diffuse=diffuse, offset=offset, want_ids=True)
+        end[diffuse] = offset + out["drawn"]
+        diff = np.abs(out["rgb"].astype(int) - ref.astype(int)).max(-1) > 0
+        o, d = oracle.camera_rays(frame["camera"])
+        near = (edge_distance(scene["verts"], scene["tris"], out["ids"].reshape(-1), o, d) < 1e-5).reshape(diff.shape)
+        assert not (diff & ~near).any(), (k, np.argwhere(diff & ~near)[:5])
+        # the frame is not the plain one: soft shadows or diffuse rays did shade
+        plain = osc.render(frame)["rgb"]
+        assert (np.abs(plain.astype(int) - ref.astype(int)).max(-1) > 1).mean() > 0.005, k
+    ends = dist_golden["stream_end"]
+    assert end[0] == int(ends[0]) and end[int(dist_golden["diffuse"][0])] == int(ends[1])
+
+
+def test_oracle_distributed_pixel_streams(oracle, dist_golden):
+    """Per-pixel streams: the same frame rendered serially and on 8 threads
+    is identical (each pixel draws only from its own stream), differs from
+    another seed, and a pixel's numbers are ro_pixel_stream's."""
+    k, scene, frame, diffuse, _, _ = list(dist_cases(dist_golden))[-1]
+    osc = oracle.OracleScene(scene)
+    a = osc.render_distributed(frame, soft=16, diffuse=diffuse, stream=oracle.STREAM_PIXEL, seed=7, threads=1,
+                               want_float=True)
+    b = osc.render_distributed(frame, soft=16, diffuse=diffuse, stream=oracle.STREAM_PIXEL, seed=7, threads=8,
+                               want_float=True)
+    c = osc.render_distributed(frame, soft=16, diffuse=diffuse, stream=oracle.STREAM_PIXEL, seed=8, threads=8)
+    assert np.array_equal(a["fimg"].view(np.uint32), b["fimg"].view(np.uint32)) and a["drawn"] == b["drawn"]
+    assert not np.array_equal(a["rgb"], c["rgb"])
+    # Philox4x32-10 word k % 4 of counter (pixel, k / 4, 0, 'STRE'), scaled by 2^-32
+    w = oracle.philox(np.array([123, 2, 0, 0x53545245], np.uint32), 7, 0)
+    assert oracle.pixel_stream(7, 123, 9) == np.float32(np.float32(w[1]) * np.float32(2.0 ** -32))
