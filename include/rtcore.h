@@ -127,6 +127,13 @@ typedef struct rt_material {
      * that shadow rays pass them. */
     float tran, ri;
     uint32_t flags;   /* RT_MAT_NO_VERTEX_COLOUR: kd ignores the vertex attribute */
+    /* rfd, td: spread of a diffuse reflection and refraction (the shader's
+     * rfd and td, coloured_mapper_shader.h:21-22; 0 = sharp).  Only a
+     * reference built with DIFFUSE_REFLECTIONS uses them (ray::reflect
+     * ray.cc:137-182, ray::refract ray.cc:236-280), here
+     * rt_render_distributed with diffuse_samples > 0; every other render
+     * ignores them, as the default build does. */
+    float rfd, td;
 } rt_material;
 #define RT_MAT_NO_VERTEX_COLOUR 1u
 #define RT_MAX_MATERIALS 16
@@ -495,6 +502,59 @@ rt_status rt_render_soft_shadows(rt_scene *scene, const rt_camera *camera, const
                                  const rt_light_shape *shapes, const rt_material *materials, int32_t nmaterials,
                                  int32_t samples, int64_t stream_offset, uint8_t *rgb_out, float *rgb_f32,
                                  int64_t *stream_end, rt_render_stats *stats);
+
+/* -------------------------------------------- distributed ray tracing */
+
+#define RT_STREAM_REFERENCE 0
+#define RT_STREAM_PIXEL 1
+
+/* What a distributed frame samples and where its random numbers come from.
+ * soft_samples: SOFT_SHADOW, 1..RT_MAX_SOFT_SAMPLES (1: the default build);
+ * diffuse_samples: DIFFUSE_REFLECTIONS, 0..RT_MAX_SOFT_SAMPLES (0: the
+ * default build).  stream: RT_STREAM_REFERENCE draws the reference's own
+ * process-wide generator (common/common.cc:35-105) in the reference's
+ * order, pixel after pixel from position stream_offset; RT_STREAM_PIXEL
+ * gives every pixel its own stream -- number k of pixel p is word k % 4 of
+ * Philox4x32-10 (Salmon et al., SC'11) with counter (p, k / 4, 0,
+ * 0x53545245) and key (seed low, seed high), as (float)word * 2^-32, the
+ * reference generator's conversion -- drawn in the reference's order within
+ * the pixel. */
+typedef struct rt_sampling {
+    int32_t soft_samples;
+    int32_t diffuse_samples;
+    int32_t stream;
+    int32_t reserved;          /* 0 */
+    int64_t stream_offset;     /* RT_STREAM_REFERENCE */
+    uint64_t seed;             /* RT_STREAM_PIXEL */
+} rt_sampling;
+
+/* Distributed ray tracing as RAPTor renders a frame when it is built with
+ * SOFT_SHADOW = soft_samples and DIFFUSE_REFLECTIONS = diffuse_samples
+ * (ray_trace_engine::ray_trace raytracer.cc:20-87, ray::find_rays
+ * ray.cc:91-104, ray::reflect ray.cc:118-182, ray::refract ray.cc:198-281,
+ * light::find_rays light.h:62-164, combind_secondary_rays
+ * coloured_mapper_shader.cc:117-130).  Every ray carries a componant c
+ * (1 for camera rays); at each hit, max(soft_samples / c, 1) shadow rays go
+ * to each spherical or triangle-defined light (shapes as for
+ * rt_render_soft_shadows) and one to each directional light; a reflection
+ * of power magn * rf above 0.1 is one mirror ray, or -- with
+ * diffuse_samples > 0 and the material's rfd != 0 -- max(diffuse_samples /
+ * c, 1) rays spread about the mirror direction by rfd, each of componant
+ * 4c; refractions likewise with tran, ri and td; each set's mean colour is
+ * added times rf, then tran.  Limits of rt_render_materials on the tree.
+ * RT_STREAM_REFERENCE renders the reference's frame exactly (one counting
+ * pass over the ray trees fixes every pixel's position in the stream; the
+ * frame's slice is generated on the host), but not with diffuse rays,
+ * whose count depends on where earlier random rays of the frame landed:
+ * replaying one stream through them is serial, so such frames need
+ * RT_STREAM_PIXEL.  stream_end (nullable) receives, for
+ * RT_STREAM_REFERENCE, the generator's position after the frame; for
+ * RT_STREAM_PIXEL, the numbers the frame drew.  rgb_out / rgb_f32 as for
+ * rt_render_soft_shadows. */
+rt_status rt_render_distributed(rt_scene *scene, const rt_camera *camera, const rt_light *lights, int32_t nlights,
+                                const rt_light_shape *shapes, const rt_material *materials, int32_t nmaterials,
+                                const rt_sampling *sampling, uint8_t *rgb_out, float *rgb_f32, int64_t *stream_end,
+                                rt_render_stats *stats);
 
 /* ---------------------------------------------------- differentiation */
 

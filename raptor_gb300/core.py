@@ -71,7 +71,17 @@ class RtLightShape(C.Structure):
 
 class RtMaterial(C.Structure):
     _fields_ = [("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3), ("ns", C.c_float),
-                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32)]
+                ("rf", C.c_float), ("tran", C.c_float), ("ri", C.c_float), ("flags", C.c_uint32),
+                ("rfd", C.c_float), ("td", C.c_float)]
+
+
+class RtSampling(C.Structure):
+    _fields_ = [("soft_samples", C.c_int32), ("diffuse_samples", C.c_int32), ("stream", C.c_int32),
+                ("reserved", C.c_int32), ("stream_offset", C.c_int64), ("seed", C.c_uint64)]
+
+
+RT_STREAM_REFERENCE = 0
+RT_STREAM_PIXEL = 1
 
 
 class RtToneMap(C.Structure):
@@ -156,6 +166,10 @@ SIGNATURES = [
                                            C.POINTER(RtLightShape),
                                            C.POINTER(RtMaterial), C.c_int32, C.c_int32, C.c_int64, _P, _P,
                                            C.POINTER(C.c_int64), C.POINTER(RtRenderStats)]),
+    ("rt_render_distributed", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
+                                          C.POINTER(RtLightShape), C.POINTER(RtMaterial), C.c_int32,
+                                          C.POINTER(RtSampling), _P, _P, C.POINTER(C.c_int64),
+                                          C.POINTER(RtRenderStats)]),
     ("rt_render_image", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32, C.POINTER(RtMaterial),
                                     C.c_int32, _P, C.POINTER(RtRenderStats)]),
     ("rt_render_materials", C.c_int32, [_P, C.POINTER(RtCamera), C.POINTER(RtLight), C.c_int32,
@@ -246,7 +260,24 @@ def make_material(d) -> RtMaterial:
     m.tran = d.get("tran", 0.0)
     m.ri = d.get("ri", 1.0)
     m.flags = d.get("flags", 0)
+    m.rfd = d.get("rfd", 0.0)
+    m.td = d.get("td", 0.0)
     return m
+
+
+def make_light_shapes(lights):
+    """(RtLightShape array, arrays to keep alive) from light dicts: "r" the
+    radius, "tris" the triangles of a triangle-defined light."""
+    shapes = (RtLightShape * max(1, len(lights)))()
+    keep = []
+    for i, l in enumerate(lights):
+        shapes[i].radius = float(l.get("r", 0.0))
+        if l.get("tris") is not None:
+            t = np.ascontiguousarray(l["tris"], np.int32)
+            keep.append(t)
+            shapes[i].ntris = t.shape[0]
+            shapes[i].tris = t.ctypes.data_as(C.POINTER(C.c_int32))
+    return shapes, keep
 
 
 def make_tone_map(d) -> RtToneMap:
@@ -532,21 +563,35 @@ class Scene:
         if fimg is None and want_float:
             fimg = np.empty((cam.yres, cam.xres, 3), np.float32)
         ls = make_lights(frame["lights"])
-        shapes = (RtLightShape * max(1, len(frame["lights"])))()
-        keep = []
-        for i, l in enumerate(frame["lights"]):
-            shapes[i].radius = float(l.get("r", 0.0))
-            if l.get("tris") is not None:
-                t = np.ascontiguousarray(l["tris"], np.int32)
-                keep.append(t)
-                shapes[i].ntris = t.shape[0]
-                shapes[i].tris = t.ctypes.data_as(C.POINTER(C.c_int32))
+        shapes, keep = make_light_shapes(frame["lights"])
         table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
         st = RtRenderStats()
         end = C.c_int64(0)
         _check(lib().rt_render_soft_shadows(self.h, C.byref(cam), ls, len(frame["lights"]), shapes, table,
                                             len(table), int(samples), int(stream_offset), ptr(rgb), ptr(fimg),
                                             C.byref(end), C.byref(st)))
+        return {"rgb": rgb, "fimg": fimg, "stats": st, "stream_end": end.value}
+
+    def render_distributed(self, frame, soft=1, diffuse=0, stream=RT_STREAM_REFERENCE, offset=0, seed=0, rgb=None,
+                           fimg=None, want_float=False):
+        """rt_render_distributed: the reference's ray tree with SOFT_SHADOW =
+        soft and DIFFUSE_REFLECTIONS = diffuse (materials' "rfd" / "td"),
+        numbers from the reference's stream at `offset` or from per-pixel
+        streams keyed by `seed`.  Returns rgb, fimg, stats and stream_end
+        (the generator's position after the frame, or the numbers drawn)."""
+        cam = make_camera(frame["camera"])
+        if rgb is None:
+            rgb = np.empty((cam.yres, cam.xres, 3), np.uint8)
+        if fimg is None and want_float:
+            fimg = np.empty((cam.yres, cam.xres, 3), np.float32)
+        ls = make_lights(frame["lights"])
+        shapes, keep = make_light_shapes(frame["lights"])
+        table = make_materials(frame["materials"] if frame.get("materials") else [frame["material"]])
+        smp = RtSampling(int(soft), int(diffuse), int(stream), 0, int(offset), int(seed))
+        st = RtRenderStats()
+        end = C.c_int64(0)
+        _check(lib().rt_render_distributed(self.h, C.byref(cam), ls, len(frame["lights"]), shapes, table, len(table),
+                                           C.byref(smp), ptr(rgb), ptr(fimg), C.byref(end), C.byref(st)))
         return {"rgb": rgb, "fimg": fimg, "stats": st, "stream_end": end.value}
 
     def render_aa(self, frame, aa_x, aa_y, rgb=None):

@@ -28,6 +28,7 @@ struct Counters {
     unsigned long long nodes;        // wide nodes fetched (counting kernels only)
     unsigned long long tris;         // triangles tested (counting kernels only)
     int redo;                        // pixels queued for an exact second pass
+    unsigned long long drawn;        // random numbers drawn (distributed frames)
 };
 
 // Tone-mapping parameters (rt_tone_map) and the per-frame accumulators of

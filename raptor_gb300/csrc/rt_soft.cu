@@ -162,6 +162,8 @@ struct SoftState {
     DevBuf scan_temp;
     DevBuf window;               // numbers [win_base, win_base + win_len) of the stream
     DevBuf area;                 // int4 per ray of a triangle-defined light: triangle, its rays, index
+    DevBuf counts, prefix64;     // int64 per pixel: numbers a distributed pixel draws, their exclusive scan
+    DevBuf scan64_temp;
     int64_t win_base = -1, win_len = 0;
     RefRandom rng;
     float *staging = nullptr;    // pinned host copy of the slice being uploaded
@@ -178,6 +180,9 @@ void soft_release(rt_context *ctx)
     ctx->soft->scan_temp.release();
     ctx->soft->window.release();
     ctx->soft->area.release();
+    ctx->soft->counts.release();
+    ctx->soft->prefix64.release();
+    ctx->soft->scan64_temp.release();
     if (ctx->soft->staging) cudaFreeHost(ctx->soft->staging);
     delete ctx->soft;
     ctx->soft = nullptr;
@@ -202,19 +207,19 @@ __device__ __forceinline__ float lut_sin(const float *__restrict__ lut, float a)
 }
 
 // Shadow ray i of n to spherical light L: a random offset of the light's
-// centre from rnd[0..2] (light.h:102-128), then ray::set_up(start,
-// centre + offset) (ray.h:44-54).
+// centre from the numbers u0, u1, u2 (light.h:102-128), then
+// ray::set_up(start, centre + offset) (ray.h:44-54).
 __device__ __forceinline__ void soft_ray(const LightView &L, const float *__restrict__ lut, float3 start, int n,
-                                         int i, const float *__restrict__ rnd, float3 &dir, float &len)
+                                         int i, float u0, float u1, float u2, float3 &dir, float &len)
 {
     const float a_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xe) != 0) + 1));
     const float b_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xc) != 0) + 1));
     const float r_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0x8) != 0) + 1));
     const int eighths = (i >> 2) & ~0x1;
     const float two_pi = xmul(2.0f, kRefPi);
-    const float a_off = xmul(xmul(__ldg(rnd), xmul(a_scale, (float)(eighths + (i & 0x1)))), two_pi);
-    const float b_off = xmul(xmul(__ldg(rnd + 1), xmul(b_scale, (float)(eighths + (i & 0x2)))), two_pi);
-    const float r_off = xmul(xmul(__ldg(rnd + 2), xmul(r_scale, (float)(eighths + (i & 0x4)))), L.radius);
+    const float a_off = xmul(xmul(u0, xmul(a_scale, (float)(eighths + (i & 0x1)))), two_pi);
+    const float b_off = xmul(xmul(u1, xmul(b_scale, (float)(eighths + (i & 0x2)))), two_pi);
+    const float r_off = xmul(xmul(u2, xmul(r_scale, (float)(eighths + (i & 0x4)))), L.radius);
     const float sin_a = lut_sin(lut, a_off), cos_a = lut_cos(lut, a_off);
     const float sin_b = lut_sin(lut, b_off), cos_b = lut_cos(lut, b_off);
     const float3 off = make_float3(xmul(xmul(r_off, cos_a), sin_b), xmul(xmul(r_off, sin_a), sin_b), xmul(r_off, cos_b));
@@ -224,17 +229,17 @@ __device__ __forceinline__ void soft_ray(const LightView &L, const float *__rest
 }
 
 // Shadow ray to triangle-defined light point e = (triangle, rays it makes,
-// index of this one): barycentrics from rnd[0..1] (triangle.h:504-525),
-// then ray::set_up(start, point).
+// index of this one): barycentrics from the numbers u0, u1
+// (triangle.h:504-525), then ray::set_up(start, point).
 __device__ __forceinline__ void area_ray(const float *__restrict__ verts, const int3 *__restrict__ idx, int4 e,
-                                         float3 start, const float *__restrict__ rnd, float3 &dir, float &len)
+                                         float3 start, float u0, float u1, float3 &dir, float &len)
 {
     const int n = e.y, i = e.z;
     const float beta_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xe) != 0) + 1));
     const float gamma_scale = xdiv(1.0f, (float)((n >> 4) + ((n & 0xc) != 0) + 1));
     const int eighths = (i >> 2) & ~0x1;
-    const float beta = xmul(__ldg(rnd), xmul(beta_scale, (float)(eighths + (i & 0x1))));
-    const float gamma = xmul(xmul(__ldg(rnd + 1), xmul(gamma_scale, (float)(eighths + (i & 0x2)))), xsub(1.0f, beta));
+    const float beta = xmul(u0, xmul(beta_scale, (float)(eighths + (i & 0x1))));
+    const float gamma = xmul(xmul(u1, xmul(gamma_scale, (float)(eighths + (i & 0x2)))), xsub(1.0f, beta));
     const float alpha = xsub(1.0f, xadd(beta, gamma));
     const int3 t = idx[e.x];
     const float3 a = make_float3(__ldg(verts + 3 * t.x), __ldg(verts + 3 * t.x + 1), __ldg(verts + 3 * t.x + 2));
@@ -346,11 +351,14 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_sh
                         for (int i = 0; i < n; ++i) {
                             float3 di;
                             float li;
-                            if (tri_light)
-                                area_ray(verts, sc.idx, __ldg(area + areas.first[l] + i), start, rnd + draw + 2 * i,
-                                         di, li);
-                            else
-                                soft_ray(L, lut, start, n, i, rnd + draw + 3 * i, di, li);
+                            if (tri_light) {
+                                const float *u = rnd + draw + 2 * i;
+                                area_ray(verts, sc.idx, __ldg(area + areas.first[l] + i), start, __ldg(u),
+                                         __ldg(u + 1), di, li);
+                            } else {
+                                const float *u = rnd + draw + 3 * i;
+                                soft_ray(L, lut, start, n, i, __ldg(u), __ldg(u + 1), __ldg(u + 2), di, li);
+                            }
                             if (i == 0) { ldir = di; len = li; }
                             HitRecord sh;
                             bool blocked;
@@ -383,6 +391,364 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_soft_sh
     if (status) atomicOr(&ctr->status, status);
 }
 
+// ------------------------------------------------ distributed ray tracing
+
+// Frames of a pixel's ray tree: one per level below the camera ray.
+constexpr int kDistDepth = RT_MAX_BOUNCES + 1;
+// Componant levels with their own counts: componant 4^k for k < 4; with
+// at most 64 samples every count max(samples / 4^k, 1) is 1 from k = 3 on.
+constexpr int kDistLevels = 4;
+
+// Per light and componant level: the first entry of the light's rays in
+// the ray table and the rays it makes (0: not triangle-defined), and the
+// numbers one hit draws for it.
+struct DistLights {
+    int32_t first[RT_MAX_LIGHTS][kDistLevels];
+    int32_t made[RT_MAX_LIGHTS][kDistLevels];
+    int32_t draws[RT_MAX_LIGHTS][kDistLevels];
+};
+
+struct DistParams {
+    int32_t soft, diffuse;
+    int32_t pixel_stream;        // 1: per-pixel Philox streams; 0: the frame's slice of the reference's
+    uint32_t key0, key1;
+    int32_t max_steps;           // frame visits per pixel (bounded by the tree's worst case)
+    float rfd[RT_MAX_MATERIALS];
+    float td[RT_MAX_MATERIALS];
+};
+
+// A pixel's random numbers: number k of its own Philox stream, or number
+// base + k of the frame's slice of the reference's stream.
+struct DistStream {
+    const float *win;
+    int64_t base, nwin;
+    uint32_t pixel, key0, key1;
+    bool pixel_mode;
+    uint32_t blk;                // last Philox block computed
+    uint4 w;
+
+    __device__ __forceinline__ float at(uint32_t k, uint32_t &status)
+    {
+        if (pixel_mode) {
+            if ((k >> 2) != blk) {
+                blk = k >> 2;
+                w = philox4x32(make_uint4(pixel, blk, 0u, 0x53545245u), key0, key1);
+            }
+            const uint32_t u = (k & 3u) == 0u ? w.x : (k & 3u) == 1u ? w.y : (k & 3u) == 2u ? w.z : w.w;
+            return xmul(__uint2float_rn(u), 2.3283064365386963e-10f);
+        }
+        const int64_t i = base + (int64_t)k;
+        if (i < 0 || i >= nwin) {   // never expected: the host sized the slice
+            status |= kStatusBadIndex;
+            return 0.0f;
+        }
+        return __ldg(win + i);
+    }
+};
+
+// One ray of a diffuse set about direction ref (ray::reflect
+// ray.cc:137-182, ray::refract ray.cc:236-280): ref + perpen * r cos a +
+// cross * r sin a, with perpen = (ref.z, ref.y, -ref.x), cross = ref x
+// perpen, r = spread * u0, a = 2 pi * u1 through the cosine table; the
+// direction is not normalised.
+__device__ __forceinline__ float3 spread_dir(float3 ref, float spread, float u0, float u1, const float *__restrict__ lut)
+{
+    const float3 perpen = make_float3(ref.z, ref.y, -ref.x);
+    const float3 cr = xcross(ref, perpen);
+    const float r_off = xmul(u0, spread);
+    const float a_off = xmul(u1, xmul(2.0f, kRefPi));
+    const float x_off = xmul(r_off, lut_cos(lut, a_off));
+    const float y_off = xmul(r_off, lut_sin(lut, a_off));
+    return xadd3(xadd3(ref, xmul3(perpen, x_off)), xmul3(cr, y_off));
+}
+
+struct DistFrame {
+    float3 o;            // the ray's origin; after its hit, the refined hit point
+    float3 d;            // its direction
+    float3 sn, geo;      // shading and geometric normal at the hit
+    float3 c;            // its colour: the lights and ka, then the sets' means
+    float3 sum;          // colours of the current set's rays so far
+    float magn;          // power
+    int32_t level;       // componant 4^level
+    int32_t mat;
+    int32_t stage;
+    int32_t out_in;
+    int32_t nrefl, nrefr, child;
+    uint32_t refl_at, refr_at;   // the pixel's number index of each set's first number
+};
+
+enum : int32_t { kDistTrace = 0, kDistRefl = 1, kDistRefr = 2, kDistDone = 3 };
+
+__device__ __forceinline__ int dist_count(int32_t samples, int32_t level)
+{
+    return max(samples >> (2 * min(level, kDistLevels - 1)), 1);
+}
+
+// A pixel of a distributed frame: the ray tree of ray_trace_engine::ray_trace
+// (raytracer.cc:20-87) as a post-order walk with an explicit stack, drawing
+// the pixel's numbers in the reference's order (at each hit: the lights'
+// rays, then the reflection set, then the refraction set; then the
+// children's subtrees in order).  SHADE false: the counting pass of a
+// reference-stream frame without diffuse rays -- the tree without shadow
+// rays, returning the count of numbers the pixel draws.
+template <bool SHADE>
+__device__ __forceinline__ uint32_t dist_pixel(const SceneView &sc, const CameraView &cam, const LightSet &lights,
+                                               const MaterialTable &table, const DistLights &dl, const DistParams &dp,
+                                               const int4 *__restrict__ area, const float *__restrict__ verts,
+                                               const float *__restrict__ lut, DistStream &S, int x, int y,
+                                               DistFrame *F, float3 &out, bool &hit, uint32_t &nsec,
+                                               uint32_t &status)
+{
+    uint32_t k = 0;
+    const RayState cr = camera_ray(cam, x, y);
+    F[0].o = cr.o;
+    F[0].d = cr.d;
+    F[0].magn = 1.0f;
+    F[0].level = 0;
+    F[0].stage = kDistTrace;
+    int sp = 1;
+    out = cam.background;
+    hit = false;
+    for (int step = 0; sp > 0 && step < dp.max_steps; ++step) {
+        DistFrame &f = F[sp - 1];
+        if (f.stage == kDistTrace) {
+            HitRecord h;
+            bool occ;
+            status |= traverse<false>(sc, f.o, f.d, FLT_MAX, h, occ);
+            if (sp > 1) ++nsec;
+            if (!(h.t < FLT_MAX)) {
+                f.c = cam.background;
+                f.stage = kDistDone;
+            } else {
+                const int32_t id = h.id - sc.tri_base;
+                if (sp == 1) hit = true;
+                int32_t mi = sc.mat ? __ldg(&sc.mat[id]) : 0;
+                if (mi < 0 || mi >= table.n) { status |= kStatusBadIndex; mi = 0; }
+                const MaterialView &m = table.m[mi];
+                RayState r;
+                r.o = f.o;
+                r.d = f.d;
+                const SurfacePoint spt = surface_at(sc, r, h);
+                const int lvl = min(f.level, kDistLevels - 1);
+                if (SHADE) {
+                    const float3 start = offset_start(spt.dst, spt.geo);
+                    const float3 kd = material_kd(m, spt);
+                    const int n = dist_count(dp.soft, f.level);
+                    float3 c = make_float3(0.f, 0.f, 0.f);
+                    for (int l = 0; l < lights.n; ++l) {
+                        const LightView &L = lights.l[l];
+                        float3 ldir;
+                        float len;
+                        int made = 0, nl = 1;
+                        if (L.kind == RT_LIGHT_DIRECTIONAL || n == 1) {
+                            shadow_ray(L, start, ldir, len);
+                            HitRecord sh;
+                            bool blocked;
+                            status |= traverse<true>(sc, start, ldir, len, sh, blocked);
+                            made = blocked ? 0 : 1;
+                        } else {
+                            nl = n;
+                            const bool tri_light = dl.made[l][lvl] > 0;
+                            for (int i = 0; i < n; ++i) {
+                                float3 di;
+                                float li;
+                                if (tri_light) {
+                                    const float u0 = S.at(k + 2 * i, status), u1 = S.at(k + 2 * i + 1, status);
+                                    area_ray(verts, sc.idx, __ldg(area + dl.first[l][lvl] + i), start, u0, u1, di, li);
+                                } else {
+                                    const float u0 = S.at(k + 3 * i, status), u1 = S.at(k + 3 * i + 1, status),
+                                                u2 = S.at(k + 3 * i + 2, status);
+                                    soft_ray(L, lut, start, n, i, u0, u1, u2, di, li);
+                                }
+                                if (i == 0) { ldir = di; len = li; }
+                                HitRecord sh;
+                                bool blocked;
+                                status |= traverse<true>(sc, start, di, li, sh, blocked);
+                                if (!blocked) ++made;
+                            }
+                        }
+                        k += (uint32_t)dl.draws[l][lvl];
+                        nsec += (uint32_t)nl;
+                        phong_add<true>(L, m, kd, spt.sn, f.d, ldir, len, xdiv((float)made, (float)nl), c);
+                    }
+                    f.c = xadd3(c, m.ka);
+                } else {
+                    for (int l = 0; l < lights.n; ++l) k += (uint32_t)dl.draws[l][lvl];
+                }
+                f.o = spt.dst;
+                f.sn = spt.sn;
+                f.geo = spt.geo;
+                f.mat = mi;
+                f.out_in = spt.out_in ? 1 : 0;
+                f.nrefl = 0;
+                f.nrefr = 0;
+                // the reflection set (ray::reflect): power magn * rf above 0.1
+                if ((double)xmul(f.magn, m.rf) > 0.1) {
+                    if (dp.diffuse > 0 && dp.rfd[mi] != 0.0f) {
+                        f.nrefl = dist_count(dp.diffuse, f.level);
+                        f.refl_at = k;
+                        k += 2u * (uint32_t)f.nrefl;
+                    } else {
+                        f.nrefl = 1;
+                    }
+                }
+                // the refraction set (ray::refract): none beyond the critical angle
+                if ((double)xmul(f.magn, m.tran) > 0.1) {
+                    float ri = m.ri;
+                    const float rdn = -xdot(f.d, f.sn);
+                    if (f.out_in) ri = xdiv(1.0f, ri);
+                    const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
+                    if (!(cos_t2 < 0.0f)) {
+                        if (dp.diffuse > 0 && dp.td[mi] != 0.0f) {
+                            f.nrefr = dist_count(dp.diffuse, f.level);
+                            f.refr_at = k;
+                            k += 2u * (uint32_t)f.nrefr;
+                        } else {
+                            f.nrefr = 1;
+                        }
+                    }
+                }
+                f.child = 0;
+                f.sum = make_float3(0.f, 0.f, 0.f);
+                f.stage = kDistRefl;
+            }
+        }
+        if (f.stage == kDistRefl) {
+            const MaterialView &m = table.m[f.mat];
+            if (f.child < f.nrefl) {
+                if (sp >= kDistDepth) {
+                    status |= kStatusStepLimit;
+                    f.child = f.nrefl;
+                    continue;
+                }
+                const bool spread = dp.diffuse > 0 && dp.rfd[f.mat] != 0.0f;
+                const float rdn = xmul(2.0f, xdot(f.d, f.sn));
+                const float3 ref = xsub3(f.d, xmul3(f.sn, rdn));
+                DistFrame &C = F[sp];
+                if (spread) {
+                    const uint32_t at = f.refl_at + 2u * (uint32_t)f.child;
+                    C.d = spread_dir(ref, dp.rfd[f.mat], S.at(at, status), S.at(at + 1, status), lut);
+                } else {
+                    C.d = ref;
+                }
+                C.o = offset_start(f.o, f.geo);
+                C.magn = xmul(f.magn, m.rf);
+                C.level = f.level + (spread ? 1 : 0);
+                C.stage = kDistTrace;
+                ++f.child;
+                ++sp;
+                continue;
+            }
+            if (SHADE && m.rf > 0.0f && f.nrefl > 0) f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefl), m.rf));
+            f.child = 0;
+            f.sum = make_float3(0.f, 0.f, 0.f);
+            f.stage = kDistRefr;
+        }
+        if (f.stage == kDistRefr) {
+            const MaterialView &m = table.m[f.mat];
+            if (f.child < f.nrefr) {
+                if (sp >= kDistDepth) {
+                    status |= kStatusStepLimit;
+                    f.child = f.nrefr;
+                    continue;
+                }
+                const bool spread = dp.diffuse > 0 && dp.td[f.mat] != 0.0f;
+                float ri = m.ri;
+                const float rdn = -xdot(f.d, f.sn);
+                if (f.out_in) ri = xdiv(1.0f, ri);
+                const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
+                const float off = xsub(xmul(ri, rdn), __fsqrt_rn(cos_t2));
+                const float3 ref = xadd3(xmul3(f.d, ri), xmul3(f.sn, off));
+                DistFrame &C = F[sp];
+                if (spread) {
+                    const uint32_t at = f.refr_at + 2u * (uint32_t)f.child;
+                    C.d = spread_dir(ref, dp.td[f.mat], S.at(at, status), S.at(at + 1, status), lut);
+                } else {
+                    C.d = ref;
+                }
+                C.o = offset_start_in(f.o, f.geo);
+                C.magn = xmul(f.magn, m.tran);
+                C.level = f.level + (spread ? 1 : 0);
+                C.stage = kDistTrace;
+                ++f.child;
+                ++sp;
+                continue;
+            }
+            if (SHADE && m.tran > 0.0f && f.nrefr > 0)
+                f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefr), m.tran));
+            f.stage = kDistDone;
+        }
+        // done: the frame's colour goes to its parent's current set
+        const float3 col = f.c;
+        --sp;
+        if (sp == 0) out = col;
+        else F[sp - 1].sum = xadd3(F[sp - 1].sum, col);
+    }
+    if (sp > 0) status |= kStatusStepLimit;
+    return k;
+}
+
+// One launch of the distributed walk: the counting pass (SHADE false:
+// counts[pix] = numbers the pixel draws) or the shading pass (numbers from
+// the pixels' own streams, or from rnd at prefix[pix]).
+template <bool SHADE>
+__global__ void __launch_bounds__(kTraceThreads) k_dist(SceneView sc, CameraView cam, LightSet lights,
+                                                        MaterialTable table, DistLights dl, DistParams dp,
+                                                        const int4 *__restrict__ area, const float *__restrict__ verts,
+                                                        const float *__restrict__ lut, const float *__restrict__ rnd,
+                                                        int64_t nrnd, const int64_t *__restrict__ prefix,
+                                                        int64_t *__restrict__ counts, uint8_t *__restrict__ rgb,
+                                                        float *__restrict__ fimg, Counters *ctr)
+{
+    DistFrame F[kDistDepth];
+    int tiles_x;
+    const int items = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
+    uint32_t status = 0;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items) break;
+        int x, y;
+        tile_pixel<8>(base + (threadIdx.x & 31), tiles_x, x, y);
+        const bool live = (x < cam.xres) && (y < cam.yres);
+        uint32_t nsec = 0, drawn = 0;
+        bool hit = false;
+        if (live) {
+            const size_t pix = (size_t)x + (size_t)y * (size_t)cam.xres;
+            DistStream S;
+            S.win = rnd;
+            S.nwin = nrnd;
+            S.base = (SHADE && !dp.pixel_stream) ? prefix[pix] : 0;
+            S.pixel = (uint32_t)pix;
+            S.key0 = dp.key0;
+            S.key1 = dp.key1;
+            S.pixel_mode = dp.pixel_stream != 0;
+            S.blk = 0xffffffffu;
+            float3 c;
+            drawn = dist_pixel<SHADE>(sc, cam, lights, table, dl, dp, area, verts, lut, S, x, y, F, c, hit, nsec,
+                                      status);
+            if (SHADE) {
+                if (rgb) store_rgb(rgb, pix, c);
+                if (fimg) {
+                    fimg[3 * pix] = c.x;
+                    fimg[3 * pix + 1] = c.y;
+                    fimg[3 * pix + 2] = c.z;
+                }
+            } else {
+                counts[pix] = (int64_t)drawn;
+            }
+        }
+        if (SHADE) {
+            warp_count(&ctr->primary, live);
+            warp_count(&ctr->hits, hit);
+            warp_add(&ctr->secondary, nsec);
+            unsigned long long d = drawn;
+            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            if ((threadIdx.x & 31) == 0 && d) atomicAdd(&ctr->drawn, d);
+        }
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
 }  // namespace
 }  // namespace rtc
 
@@ -411,6 +777,10 @@ struct SGuard {
         if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
     }
 };
+
+rt_status check_shapes(const rt_scene *s, const rt_light *lights, int32_t nlights, const rt_light_shape *shapes,
+                       const char *who);
+rt_status stream_window(SoftState &S, int64_t offset, int64_t total, cudaStream_t st, const float **rnd);
 
 int soft_blocks_per_sm()
 {
@@ -447,18 +817,9 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     for (int32_t i = 0; i < nmaterials; ++i)
         if (materials[i].rf != 0.0f || materials[i].tran != 0.0f)
             return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: mirror and refracting materials are not offered");
-    for (int32_t i = 0; i < nlights && shapes; ++i) {
-        const rt_light_shape &sh = shapes[i];
-        if (!(sh.radius >= 0.0f && sh.radius < 3.0e38f))
-            return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: light radius must be finite and >= 0");
-        if (sh.ntris < 0 || (sh.ntris > 0 && !sh.tris))
-            return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: bad triangle list of a light");
-        if (sh.ntris > 0 && (sh.radius != 0.0f || lights[i].kind == RT_LIGHT_DIRECTIONAL))
-            return sfail(RT_ERR_INVALID_ARG,
-                         "rt_render_soft_shadows: a triangle-defined light is a point or spot light of radius 0");
-        for (int32_t j = 0; j < sh.ntris; ++j)
-            if (sh.tris[j] < 0 || sh.tris[j] >= s->ntris)
-                return sfail(RT_ERR_INVALID_ARG, "rt_render_soft_shadows: light triangle index out of range");
+    {
+        const rt_status st = check_shapes(s, lights, nlights, shapes, "rt_render_soft_shadows");
+        if (st != RT_OK) return st;
     }
     if (!s->built) return sfail(RT_ERR_NOT_BUILT, "rt_render_soft_shadows: hierarchy not built");
     if (s->mat_max >= nmaterials)
@@ -549,26 +910,12 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
     const int64_t nhits = (int64_t)h[0] + h[1];
     const int64_t total = nhits * per_hit;
-    // the frame's slice of the reference's stream, kept on the device while
-    // later frames fall inside it
-    if (total > 0 && !(S.win_base >= 0 && stream_offset >= S.win_base &&
-                       stream_offset + total <= S.win_base + S.win_len)) {
-        if (S.staging_cap < (size_t)total) {
-            if (S.staging) cudaFreeHost(S.staging);
-            S.staging = nullptr;
-            S.staging_cap = 0;
-            const size_t cap = (size_t)total + (size_t)total / 4;
-            RT_CUDA_S(cudaMallocHost(&S.staging, cap * sizeof(float)), "pinned stream staging");
-            S.staging_cap = cap;
-        }
-        generate_slice(S.rng, stream_offset, total, S.staging);
-        RT_CUDA_S(S.window.reserve((size_t)total * sizeof(float)), "stream allocation");
-        RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging, (size_t)total * sizeof(float), cudaMemcpyHostToDevice, st),
-                  "stream copy");
-        S.win_base = stream_offset;
-        S.win_len = total;
+    // the frame's slice of the reference's stream
+    const float *rnd = nullptr;
+    {
+        const rt_status wst = stream_window(S, stream_offset, total, st, &rnd);
+        if (wst != RT_OK) return wst;
     }
-    const float *rnd = total > 0 ? (const float *)S.window.ptr + (stream_offset - S.win_base) : nullptr;
 
     // outputs: device pointers as given, host ones staged
     const bool rgb_host = rgb_out && !is_device_ptr(rgb_out);
@@ -608,5 +955,360 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
         stats->device_ms = ms;
     }
     if (stream_end) *stream_end = stream_offset + total;
+    return status_to_error(c.status);
+}
+
+namespace {
+
+int dist_blocks_per_sm()
+{
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_dist<true>, kTraceThreads, 0) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 2;
+        }
+        return b;
+    }();
+    return per_sm;
+}
+
+// Worst-case ray tree of a distributed frame: a ray of power a^i * b^j
+// (a, b the largest rf and tran of the table) at componant level k spawns,
+// while the child's power exceeds 0.1, a reflection set -- one mirror ray,
+// or max(diffuse / 4^k, 1) rays at level k + 1 where some reflective
+// material spreads -- and likewise a refraction set.  rays: the largest
+// tree; depth: its levels below the camera ray; levels: the deepest
+// componant level.
+struct TreeBound {
+    double rays = 0.0;
+    int depth = 0, levels = 0;
+};
+
+struct TreeBounder {
+    double a, b;
+    bool mirror_r, spread_r, mirror_t, spread_t;
+    int diffuse;
+    static constexpr int kI = 4 * RT_MAX_BOUNCES + 2, kK = 18;
+    std::vector<double> memo;
+    std::vector<int> deep, lev;
+
+    TreeBounder() : memo((size_t)kI * kI * kK, -1.0), deep((size_t)kI * kI * kK, 0), lev((size_t)kI * kI * kK, 0) {}
+
+    // rays of the worst tree below a ray of power a^i b^j at level k
+    double f(int i, int j, int k)
+    {
+        const size_t at = ((size_t)i * kI + (size_t)j) * kK + (size_t)k;
+        if (memo[at] >= 0.0) return memo[at];
+        const double thr = 0.1 * (1.0 - 1.0e-5);
+        double r = 1.0;
+        int d = 0, l = k;
+        for (int side = 0; side < 2; ++side) {
+            const int ni = i + (side == 0), nj = j + (side == 1);
+            if (ni + nj >= kI - 1 || !(std::pow(a, ni) * std::pow(b, nj) > thr)) continue;
+            const bool mirror = side == 0 ? mirror_r : mirror_t, spread = side == 0 ? spread_r : spread_t;
+            double best = 0.0;
+            if (mirror) {
+                best = f(ni, nj, k);
+                const size_t c = ((size_t)ni * kI + (size_t)nj) * kK + (size_t)k;
+                d = std::max(d, 1 + deep[c]);
+                l = std::max(l, lev[c]);
+            }
+            if (spread) {
+                const int kk = std::min(k + 1, kK - 1);
+                const double nr = (double)std::max(diffuse >> (2 * std::min(k, kDistLevels - 1)), 1);
+                best = std::max(best, nr * f(ni, nj, kk));
+                const size_t c = ((size_t)ni * kI + (size_t)nj) * kK + (size_t)kk;
+                d = std::max(d, 1 + deep[c]);
+                l = std::max(l, lev[c]);
+            }
+            r += best;
+        }
+        memo[at] = r;
+        deep[at] = d;
+        lev[at] = l;
+        return r;
+    }
+};
+
+TreeBound dist_tree_bound(const rt_material *m, int32_t n, int32_t diffuse)
+{
+    TreeBounder tb;
+    tb.a = tb.b = 0.0;
+    tb.mirror_r = tb.spread_r = tb.mirror_t = tb.spread_t = false;
+    tb.diffuse = diffuse;
+    for (int32_t i = 0; i < n; ++i) {
+        tb.a = std::max(tb.a, (double)m[i].rf);
+        tb.b = std::max(tb.b, (double)m[i].tran);
+        if (m[i].rf > 0.0f) {
+            if (diffuse > 0 && m[i].rfd != 0.0f) tb.spread_r = true;
+            else tb.mirror_r = true;
+        }
+        if (m[i].tran > 0.0f) {
+            if (diffuse > 0 && m[i].td != 0.0f) tb.spread_t = true;
+            else tb.mirror_t = true;
+        }
+    }
+    TreeBound out;
+    out.rays = tb.f(0, 0, 0);
+    out.depth = tb.deep[0];
+    out.levels = tb.lev[0];
+    return out;
+}
+
+// Shapes of the lights (rt_light_shape): radii finite and >= 0; triangle
+// lists in range on point or spot lights of radius 0.
+rt_status check_shapes(const rt_scene *s, const rt_light *lights, int32_t nlights, const rt_light_shape *shapes,
+                       const char *who)
+{
+    for (int32_t i = 0; i < nlights && shapes; ++i) {
+        const rt_light_shape &sh = shapes[i];
+        const std::string w(who);
+        if (!(sh.radius >= 0.0f && sh.radius < 3.0e38f))
+            return sfail(RT_ERR_INVALID_ARG, (w + ": light radius must be finite and >= 0").c_str());
+        if (sh.ntris < 0 || (sh.ntris > 0 && !sh.tris))
+            return sfail(RT_ERR_INVALID_ARG, (w + ": bad triangle list of a light").c_str());
+        if (sh.ntris > 0 && (sh.radius != 0.0f || lights[i].kind == RT_LIGHT_DIRECTIONAL))
+            return sfail(RT_ERR_INVALID_ARG,
+                         (w + ": a triangle-defined light is a point or spot light of radius 0").c_str());
+        for (int32_t j = 0; j < sh.ntris; ++j)
+            if (sh.tris[j] < 0 || sh.tris[j] >= s->ntris)
+                return sfail(RT_ERR_INVALID_ARG, (w + ": light triangle index out of range").c_str());
+    }
+    return RT_OK;
+}
+
+// The frame's numbers [offset, offset + total) of the reference's stream on
+// the device (generated on the host into pinned memory, copied over), kept
+// while later frames fall inside them; *rnd points at number offset.
+rt_status stream_window(SoftState &S, int64_t offset, int64_t total, cudaStream_t st, const float **rnd)
+{
+    *rnd = nullptr;
+    if (total <= 0) return RT_OK;
+    if (!(S.win_base >= 0 && offset >= S.win_base && offset + total <= S.win_base + S.win_len)) {
+        if (S.staging_cap < (size_t)total) {
+            if (S.staging) cudaFreeHost(S.staging);
+            S.staging = nullptr;
+            S.staging_cap = 0;
+            const size_t cap = (size_t)total + (size_t)total / 4;
+            RT_CUDA_S(cudaMallocHost(&S.staging, cap * sizeof(float)), "pinned stream staging");
+            S.staging_cap = cap;
+        }
+        // the copy below reads the staging buffer: an earlier frame's copy
+        // from it must be done before it is overwritten
+        RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
+        generate_slice(S.rng, offset, total, S.staging);
+        RT_CUDA_S(S.window.reserve((size_t)total * sizeof(float)), "stream allocation");
+        RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging, (size_t)total * sizeof(float), cudaMemcpyHostToDevice, st),
+                  "stream copy");
+        S.win_base = offset;
+        S.win_len = total;
+    }
+    *rnd = (const float *)S.window.ptr + (offset - S.win_base);
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" rt_status rt_render_distributed(rt_scene *s, const rt_camera *camera, const rt_light *lights,
+                                           int32_t nlights, const rt_light_shape *shapes,
+                                           const rt_material *materials, int32_t nmaterials,
+                                           const rt_sampling *sampling, uint8_t *rgb_out, float *rgb_f32,
+                                           int64_t *stream_end, rt_render_stats *stats)
+{
+    if (!s || !camera || !materials || !sampling || (!rgb_out && !rgb_f32))
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: NULL argument");
+    if (camera->xres <= 0 || camera->yres <= 0 || (int64_t)camera->xres * camera->yres > (int64_t)1 << 28)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: camera resolution out of range");
+    if (nlights < 0 || nlights > RT_MAX_LIGHTS || (nlights > 0 && !lights))
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: light count out of range");
+    if (nmaterials < 1 || nmaterials > RT_MAX_MATERIALS)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: material count must be 1..RT_MAX_MATERIALS");
+    const rt_sampling smp = *sampling;
+    if (smp.soft_samples < 1 || smp.soft_samples > RT_MAX_SOFT_SAMPLES || smp.diffuse_samples < 0 ||
+        smp.diffuse_samples > RT_MAX_SOFT_SAMPLES)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: sample counts out of range");
+    if (smp.stream != RT_STREAM_REFERENCE && smp.stream != RT_STREAM_PIXEL)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: unknown stream");
+    if (smp.stream == RT_STREAM_REFERENCE && smp.stream_offset < 0)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: negative stream offset");
+    bool tree = false, spread = false;
+    for (int32_t i = 0; i < nmaterials; ++i) {
+        const rt_material &m = materials[i];
+        if (!(m.rf >= 0.0f && m.rf < 1.0f) || !(m.tran >= 0.0f && m.tran < 1.0f))
+            return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: reflectivity and transparency must be in [0, 1)");
+        if (m.tran > 0.0f && !(m.ri > 0.0f && m.ri < 3.0e38f))
+            return sfail(RT_ERR_INVALID_ARG,
+                         "rt_render_distributed: a transparent material needs a finite positive refractive index");
+        if (!(std::fabs(m.rfd) < 3.0e38f) || !(std::fabs(m.td) < 3.0e38f))
+            return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: diffuse spreads must be finite");
+        tree = tree || m.rf > 0.0f || m.tran > 0.0f;
+        spread = spread || (smp.diffuse_samples > 0 && ((m.rf > 0.0f && m.rfd != 0.0f) || (m.tran > 0.0f && m.td != 0.0f)));
+    }
+    if (spread && smp.stream == RT_STREAM_REFERENCE)
+        return sfail(RT_ERR_INVALID_ARG,
+                     "rt_render_distributed: diffuse rays draw the reference's stream in an order one pass cannot "
+                     "replay in parallel (a pixel's count depends on where earlier random rays landed); use "
+                     "RT_STREAM_PIXEL");
+    {
+        const rt_status st = check_shapes(s, lights, nlights, shapes, "rt_render_distributed");
+        if (st != RT_OK) return st;
+    }
+    if (!s->built) return sfail(RT_ERR_NOT_BUILT, "rt_render_distributed: hierarchy not built");
+    if (s->mat_max >= nmaterials)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: the scene's material indices exceed the table");
+    // without ray trees or diffuse rays, the reference-stream frame is the
+    // soft-shadow frame
+    if (!tree && smp.stream == RT_STREAM_REFERENCE)
+        return rt_render_soft_shadows(s, camera, lights, nlights, shapes, materials, nmaterials, smp.soft_samples,
+                                      smp.stream_offset, rgb_out, rgb_f32, stream_end, stats);
+    const TreeBound tb = dist_tree_bound(materials, nmaterials, smp.diffuse_samples);
+    if (tb.depth > RT_MAX_BOUNCES || tb.rays > (double)RT_MAX_TREE_RAYS || tb.levels > 15)
+        return sfail(RT_ERR_INVALID_ARG, "rt_render_distributed: the materials allow more than RT_MAX_BOUNCES levels "
+                                         "or RT_MAX_TREE_RAYS rays per pixel");
+
+    rt_context *ctx = s->ctx;
+    SGuard g(ctx->device);
+    if (!ctx->soft) {
+        ctx->soft = new (std::nothrow) SoftState();
+        if (!ctx->soft) return sfail(RT_ERR_OUT_OF_MEMORY, "rt_render_distributed: state allocation");
+    }
+    SoftState &S = *ctx->soft;
+    cudaStream_t st = ctx->stream;
+    if (!S.lut_ready) {
+        std::vector<float> lut(kCosLutSize);
+        for (int i = 0; i < kCosLutSize; ++i)
+            lut[i] = (float)std::cos((double)((((float)i * 2.0f) * kRefPi) / (float)kCosLutSize));
+        RT_CUDA_S(S.lut.reserve(kCosLutSize * sizeof(float)), "cosine table allocation");
+        RT_CUDA_S(cudaMemcpy(S.lut.ptr, lut.data(), kCosLutSize * sizeof(float), cudaMemcpyHostToDevice),
+                  "cosine table copy");
+        S.lut_ready = true;
+    }
+    // lights: per componant level, the rays of every triangle-defined
+    // light and the numbers a hit draws
+    LightSet ls;
+    ls.n = nlights;
+    ls.fast_pow = 0;
+    DistLights dl = {};
+    std::vector<int4> area_rays;
+    for (int i = 0; i < nlights; ++i) {
+        ls.l[i] = make_light_view(lights[i]);
+        ls.l[i].radius = shapes ? shapes[i].radius : 0.0f;
+        if (ls.l[i].kind == RT_LIGHT_DIRECTIONAL) continue;
+        for (int k = 0; k < kDistLevels; ++k) {
+            const int32_t n = std::max(smp.soft_samples >> (2 * k), 1);
+            if (n == 1) continue;
+            if (shapes && shapes[i].ntris > 0) {
+                const int32_t nt = shapes[i].ntris;
+                std::vector<int32_t> cnt((size_t)nt);
+                const int32_t made = area_light_rays(nt, n, cnt.data());
+                if (made < n)
+                    return sfail(RT_ERR_INVALID_ARG,
+                                 "rt_render_distributed: a triangle-defined light makes fewer rays than asked");
+                dl.first[i][k] = (int32_t)area_rays.size();
+                dl.made[i][k] = made;
+                dl.draws[i][k] = 2 * made;
+                for (int32_t j = 0; j < nt; ++j)
+                    for (int32_t q = 0; q < cnt[(size_t)j]; ++q)
+                        area_rays.push_back(make_int4(shapes[i].tris[j], cnt[(size_t)j], q, 0));
+            } else {
+                dl.draws[i][k] = 3 * n;
+            }
+        }
+    }
+    if (!area_rays.empty()) {
+        RT_CUDA_S(S.area.reserve(area_rays.size() * sizeof(int4)), "light ray table allocation");
+        RT_CUDA_S(cudaMemcpyAsync(S.area.ptr, area_rays.data(), area_rays.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                  st),
+                  "light ray table copy");
+    }
+    MaterialTable mt;
+    mt.n = nmaterials;
+    DistParams dp = {};
+    dp.soft = smp.soft_samples;
+    dp.diffuse = smp.diffuse_samples;
+    dp.pixel_stream = smp.stream == RT_STREAM_PIXEL ? 1 : 0;
+    dp.key0 = (uint32_t)smp.seed;
+    dp.key1 = (uint32_t)(smp.seed >> 32);
+    dp.max_steps = (int32_t)std::min(8.0 * tb.rays + 64.0, 1.0e9);
+    for (int i = 0; i < nmaterials; ++i) {
+        mt.m[i] = make_material_view(materials[i]);
+        dp.rfd[i] = materials[i].rfd;
+        dp.td[i] = materials[i].td;
+    }
+    const SceneView sv = scene_view(s);
+    const CameraView cv = make_camera_view(*camera);
+    const size_t npix = (size_t)camera->xres * (size_t)camera->yres;
+    const int grid = dist_blocks_per_sm() * ctx->sm_count;
+
+    RT_CUDA_S(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), st), "counter clear");
+    RT_CUDA_S(cudaEventRecord(ctx->ev0, st), "event record");
+    const float *rnd = nullptr;
+    int64_t total = 0;
+    if (smp.stream == RT_STREAM_REFERENCE) {
+        // counting pass, scan, the frame's slice of the stream
+        RT_CUDA_S(S.counts.reserve(npix * sizeof(int64_t)), "count allocation");
+        RT_CUDA_S(S.prefix64.reserve(npix * sizeof(int64_t)), "prefix allocation");
+        size_t scan_bytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const int64_t *)S.counts.ptr, (int64_t *)S.prefix64.ptr,
+                                      (int)npix, st);
+        RT_CUDA_S(S.scan64_temp.reserve(scan_bytes), "scan scratch allocation");
+        k_dist<false><<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
+                                                      (const float *)S.lut.ptr, nullptr, 0, nullptr,
+                                                      (int64_t *)S.counts.ptr, nullptr, nullptr, ctx->d_counters);
+        RT_CUDA_S(cudaGetLastError(), "counting launch");
+        cub::DeviceScan::ExclusiveSum(S.scan64_temp.ptr, scan_bytes, (const int64_t *)S.counts.ptr,
+                                      (int64_t *)S.prefix64.ptr, (int)npix, st);
+        RT_CUDA_S(cudaGetLastError(), "scan launch");
+        int64_t last[2];
+        RT_CUDA_S(cudaMemcpyAsync(&last[0], (const int64_t *)S.prefix64.ptr + (npix - 1), sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, st),
+                  "prefix read");
+        RT_CUDA_S(cudaMemcpyAsync(&last[1], (const int64_t *)S.counts.ptr + (npix - 1), sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, st),
+                  "count read");
+        RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
+        total = last[0] + last[1];
+        const rt_status wst = stream_window(S, smp.stream_offset, total, st, &rnd);
+        if (wst != RT_OK) return wst;
+        RT_CUDA_S(cudaMemsetAsync(&ctx->d_counters->work, 0, sizeof(int), st), "work counter clear");
+    }
+    const bool rgb_host = rgb_out && !is_device_ptr(rgb_out);
+    const bool f_host = rgb_f32 && !is_device_ptr(rgb_f32);
+    uint8_t *d_rgb = rgb_out;
+    float *d_f = rgb_f32;
+    if (rgb_host) {
+        RT_CUDA_S(ctx->stage_a.reserve(npix * 3), "staging allocation");
+        d_rgb = (uint8_t *)ctx->stage_a.ptr;
+    }
+    if (f_host) {
+        RT_CUDA_S(ctx->fimg.reserve(npix * 3 * sizeof(float)), "float frame allocation");
+        d_f = (float *)ctx->fimg.ptr;
+    }
+    k_dist<true><<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
+                                                 (const float *)S.lut.ptr, rnd, total,
+                                                 (const int64_t *)S.prefix64.ptr, nullptr, d_rgb, d_f,
+                                                 ctx->d_counters);
+    RT_CUDA_S(cudaGetLastError(), "shade launch");
+    RT_CUDA_S(cudaEventRecord(ctx->ev1, st), "event record");
+    if (rgb_host) RT_CUDA_S(cudaMemcpyAsync(rgb_out, d_rgb, npix * 3, cudaMemcpyDeviceToHost, st), "rgb copy");
+    if (f_host)
+        RT_CUDA_S(cudaMemcpyAsync(rgb_f32, d_f, npix * 3 * sizeof(float), cudaMemcpyDeviceToHost, st), "image copy");
+    Counters c;
+    RT_CUDA_S(cudaMemcpyAsync(&c, ctx->d_counters, sizeof(Counters), cudaMemcpyDeviceToHost, st), "counter read");
+    RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
+    if (stats) {
+        stats->primary_rays = (int64_t)c.primary;
+        stats->secondary_rays = (int64_t)c.secondary;
+        stats->primary_hits = (int64_t)c.hits;
+        stats->status = (int32_t)c.status;
+        stats->nodes_fetched = 0;
+        stats->tris_tested = 0;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->device_ms = ms;
+    }
+    if (stream_end)
+        *stream_end = smp.stream == RT_STREAM_REFERENCE ? smp.stream_offset + total : (int64_t)c.drawn;
     return status_to_error(c.status);
 }

@@ -135,8 +135,6 @@ rt_material describe(const material *m)
         if (field(*c, cms_t_ka{}) || field(*c, cms_t_ks{}) || field(*c, cms_t_ns{}) || field(*c, cms_t_refl{}) ||
             field(*c, cms_t_d{}))
             unsupported("a coloured_mapper_shader texture mapper other than kd's");
-        if (field(*c, cms_td{}) != 0.0f || field(*c, cms_rfd{}) != 0.0f)
-            unsupported("diffuse transmission or reflection (td, rfd)");
         put3(out.ka, field(*c, cms_ka{}));
         put3(out.kd, field(*c, cms_kd{}));
         put3(out.ks, field(*c, cms_ks{}));
@@ -144,6 +142,11 @@ rt_material describe(const material *m)
         out.rf = field(*c, cms_rf{});
         out.tran = field(*c, cms_tran{});
         out.ri = field(*c, cms_ri{});
+        // spreads of diffuse reflection and refraction: a build without
+        // DIFFUSE_REFLECTIONS ignores them (ray.cc:118-135, 198-235), as the
+        // renders ray_tracer_gpu uses do
+        out.rfd = field(*c, cms_rfd{});
+        out.td = field(*c, cms_td{});
         // a kd texture mapper samples the triangle's per-vertex attribute
         out.flags = field(*c, cms_t_kd{}) ? 0u : RT_MAT_NO_VERTEX_COLOUR;
         return out;
@@ -161,6 +164,8 @@ rt_material describe(const material *m)
         out.tran = 0.0f;
         out.ri = 1.0f;
         out.flags = RT_MAT_NO_VERTEX_COLOUR;
+        out.rfd = 0.0f;
+        out.td = 0.0f;
         return out;
     }
     unsupported("a material other than coloured_mapper_shader and phong_shader");

@@ -34,7 +34,9 @@ def test_struct_sizes(rtlib):
     assert C.sizeof(rtlib.RtHit) == 16
     assert C.sizeof(rtlib.RtCamera) == 4 * (15 + 3) + 8
     assert C.sizeof(rtlib.RtLight) == 4 * 13
-    assert C.sizeof(rtlib.RtMaterial) == 56
+    assert C.sizeof(rtlib.RtMaterial) == 64
+    assert C.sizeof(rtlib.RtLightShape) == 16
+    assert C.sizeof(rtlib.RtSampling) == 32
     assert rtlib.RAY_DTYPE.itemsize == 32 and rtlib.HIT_DTYPE.itemsize == 16
 
 
