@@ -302,6 +302,8 @@ WORKLOADS = {
     "terrain-1M-1080p": ("workload_terrain_1m", True, lambda k: max(5, k // 2)),
     "terrain-2M-1080p-aa2x2": ("workload_terrain_aa", True, lambda k: max(3, k // 4)),
     "terrain-2M-1080p-soft16": ("workload_terrain_soft", True, lambda k: max(3, k // 4)),
+    "glass-41k-512-soft16": ("workload_glass_soft", True, lambda k: max(3, k // 4)),
+    "glass-41k-512-diffuse16": ("workload_glass_diffuse", True, lambda k: max(3, k // 4)),
     "instances-4M-720p-ao16": ("workload_instances_ao", True, lambda k: max(3, k // 4)),
     "batched-64-scenes": ("workload_batched", False, lambda k: max(3, k // 4)),
     "adjoint-50k-256": ("workload_adjoint", False, lambda k: max(5, k // 2)),
@@ -557,6 +559,47 @@ def workload_glass(ctx, stream, flush, steps):
     sc.close()
     return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512],
             "Mrays_s": rays / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays / steps}
+
+
+def _glass_distributed(ctx, stream, flush, steps, diffuse):
+    import torch
+    from raptor_gb300 import core, scenes
+    scene, frame = scenes.glass_scene(freq=32, res=512)
+    frame = dict(frame, lights=[dict(frame["lights"][0], r=0.7), frame["lights"][1]])
+    if diffuse:
+        mats = [dict(frame["materials"][0], rfd=0.2), dict(frame["materials"][1], rfd=0.1, td=0.05)]
+        frame = dict(frame, materials=mats, material=mats[0])
+        kw = {"soft": 16, "diffuse": 16, "stream": core.RT_STREAM_PIXEL, "seed": 1}
+    else:
+        kw = {"soft": 16, "stream": core.RT_STREAM_REFERENCE, "offset": 0}
+    sc = core.Scene(ctx, scene)
+    rgb = torch.empty((512, 512, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        first = sc.render_distributed(frame, rgb=rgb, **kw)
+    secs, st = time_frames(lambda: sc.render_distributed(frame, rgb=rgb, **kw)["stats"], steps, stream, flush)
+    rays = st.primary_rays + st.secondary_rays
+    sc.close()
+    return {"triangles": int(scene["tris"].shape[0]), "resolution": [512, 512], "soft_samples": 16,
+            "diffuse_samples": 16 if diffuse else 0, "stream": "pixel" if diffuse else "reference",
+            "Mrays_s": rays * steps / secs / 1e6, "ms_per_frame": secs / steps * 1e3, "rays_per_frame": rays,
+            "numbers_per_frame": first["stream_end"]}
+
+
+def workload_glass_soft(ctx, stream, flush, steps):
+    """The glass scene (refraction and mirror ray trees, 41k triangles,
+    512x512) with soft shadows as the SOFT_SHADOW = 16 build renders them:
+    16 rays to the spherical light (radius 0.7) at every hit of every tree
+    ray, numbers from the reference's stream (counting pass, scan, shading
+    pass; the slice already on the device)."""
+    return _glass_distributed(ctx, stream, flush, steps, False)
+
+
+def workload_glass_diffuse(ctx, stream, flush, steps):
+    """The glass scene with diffuse reflections and refractions
+    (DIFFUSE_REFLECTIONS = 16: 16 spread rays per reflection of a camera
+    ray's hit, 4 at the next level, then 1; ground rfd 0.2, glass rfd 0.1
+    and td 0.05) and 16 soft-shadow samples, per-pixel streams."""
+    return _glass_distributed(ctx, stream, flush, steps, True)
 
 
 def workload_ingest(ctx, stream, steps):
