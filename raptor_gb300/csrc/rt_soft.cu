@@ -690,9 +690,15 @@ __device__ __forceinline__ uint32_t dist_pixel(const SceneView &sc, const Camera
 
 // One launch of the distributed walk: the counting pass (SHADE false:
 // counts[pix] = numbers the pixel draws) or the shading pass (numbers from
-// the pixels' own streams, or from rnd at prefix[pix]).
+// the pixels' own streams, or from rnd at prefix[pix]).  A warp walks the 32
+// pixels of an 8x4 tile, each lane one stage of its pixel's tree per loop
+// iteration.  RT_DIST_MIN_BLOCKS: resident blocks per SM the register
+// allocation must allow (4: 128 registers, no spills, measured fastest).
+#ifndef RT_DIST_MIN_BLOCKS
+#define RT_DIST_MIN_BLOCKS 4
+#endif
 template <bool SHADE>
-__global__ void __launch_bounds__(kTraceThreads) k_dist(SceneView sc, CameraView cam, LightSet lights,
+__global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist(SceneView sc, CameraView cam, LightSet lights,
                                                         MaterialTable table, DistLights dl, DistParams dp,
                                                         const int4 *__restrict__ area, const float *__restrict__ verts,
                                                         const float *__restrict__ lut, const float *__restrict__ rnd,
