@@ -189,10 +189,13 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
  * locally-ordered clustering of mutual nearest neighbours over the Morton
  * order (Meister and Bittner 2018): lower surface area, fewer nodes per
  * ray; RT_BUILDER_LBVH -- the Morton radix tree (Karras 2012): faster to
- * build.  Hits do not depend on the tree. */
+ * build; RT_BUILDER_HPLOC -- the same clustering run inside the radix tree
+ * bottom-up in one launch (H-PLOC, Benthin et al. 2024); batched builds
+ * use RT_BUILDER_PLOC for it.  Hits do not depend on the tree. */
 #define RT_OPT_BUILDER 4
 #define RT_BUILDER_LBVH 0
 #define RT_BUILDER_PLOC 1
+#define RT_BUILDER_HPLOC 2
 /* RT_OPT_MORTON_BITS: bits per axis of the Morton codes the builders sort
  * (10..21), or 0 (default): 21 below a million triangles, else sized from
  * the triangle count, about 3 more than log2(n) / 3, so that each Morton

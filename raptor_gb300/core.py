@@ -36,6 +36,7 @@ RT_ISECT_WATERTIGHT = 1
 RT_OPT_BUILDER = 4
 RT_BUILDER_LBVH = 0
 RT_BUILDER_PLOC = 1
+RT_BUILDER_HPLOC = 2
 RT_OPT_MORTON_BITS = 5
 
 

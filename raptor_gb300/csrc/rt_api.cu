@@ -308,7 +308,7 @@ rt_status rt_ctx_set_option(rt_context *ctx, int32_t option, int64_t value)
         return RT_OK;
     }
     if (option == RT_OPT_BUILDER) {
-        if (value != RT_BUILDER_LBVH && value != RT_BUILDER_PLOC)
+        if (value != RT_BUILDER_LBVH && value != RT_BUILDER_PLOC && value != RT_BUILDER_HPLOC)
             return fail(RT_ERR_INVALID_ARG, "rt_ctx_set_option: unknown builder");
         ctx->builder = (int)value;
         return RT_OK;
@@ -424,6 +424,11 @@ rt_status rt_scene_update_vertices(rt_scene *s, const float *verts, int32_t nver
     return rt_bvh_build(s, nullptr);
 }
 
+static int32_t builder_of(int b)
+{
+    return b == RT_BUILDER_LBVH ? kBuilderLbvh : b == RT_BUILDER_HPLOC ? kBuilderHploc : kBuilderPloc;
+}
+
 rt_status rt_bvh_build(rt_scene *s, float *build_ms)
 {
     if (!s) return fail(RT_ERR_INVALID_ARG, "rt_bvh_build: NULL scene");
@@ -453,7 +458,7 @@ rt_status rt_bvh_build(rt_scene *s, float *build_ms)
     in.max_nodes = s->ntris + 1;
     in.sm_count = ctx->sm_count;
     in.host_scratch = ctx->h_scratch;
-    in.builder = ctx->builder == RT_BUILDER_LBVH ? kBuilderLbvh : kBuilderPloc;
+    in.builder = builder_of(ctx->builder);
     in.morton_bits = ctx->morton_bits;
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
     const BuildResult R = build_wide_bvh(in, s->temp.ptr, s->temp.cap, ctx->stream);

@@ -371,7 +371,7 @@ rt_status rt_bvh_build_batched(rt_batch *b, float *build_ms)
     in.max_nodes = ntris + ns + 1;
     in.sm_count = ctx->sm_count;
     in.host_scratch = ctx->h_scratch;
-    in.builder = ctx->builder == RT_BUILDER_LBVH ? kBuilderLbvh : kBuilderPloc;
+    in.builder = ctx->builder == RT_BUILDER_LBVH ? kBuilderLbvh : ctx->builder == RT_BUILDER_HPLOC ? kBuilderHploc : kBuilderPloc;
     in.morton_bits = ctx->morton_bits;
     in.nseg = ns;
     in.seg_of_tri = b->d_seg;

@@ -237,7 +237,7 @@ __device__ __forceinline__ void sah_child(const float *sah, int32_t ref, float4 
 
 // Table and decision word of internal node id from its children's tables.
 __device__ __forceinline__ void sah_node(float *sah, uint32_t *dec, int32_t id, float area, int32_t count,
-                                         const float *cl, const float *cr)
+                                         const float *cl, const float *cr, float *row = nullptr)
 {
     float dist[9];
     uint32_t split[9];
@@ -272,6 +272,20 @@ __device__ __forceinline__ void sah_node(float *sah, uint32_t *dec, int32_t id, 
     __stcg(p, make_float4(c[0], c[1], c[2], c[3]));
     __stcg(p + 1, make_float4(c[4], c[5], c[6], c[7]));
     __stcg(dec + id, d);
+    if (row) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) row[i] = c[i];
+    }
+}
+
+// atomicAdd with acquire-release order at device scope: the caller's
+// earlier stores are visible to whoever later reads the counter, and the
+// caller sees everything released before the value it reads.
+__device__ __forceinline__ int atomic_add_acq_rel(int32_t *p, int32_t v)
+{
+    int32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
 }
 
 constexpr int kRefitMaxDepth = 1 << 16;   // binary levels a refit walk may climb
@@ -286,28 +300,39 @@ __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32
 {
     const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    // the child this thread climbs from: its ref, box and surface-area row
+    // stay in registers; only the sibling's are loaded
+    int32_t cur = ~k;
+    float4 mlo = llo[k], mhi = lhi[k];
+    float mrow[8];
+    if (sah) sah_child(sah, cur, mlo, mhi, mrow);
     int32_t p = leaf_parent[k];
     int guard = 0;
     while (p >= 0) {
         if (++guard > kRefitMaxDepth) { atomicExch(err, 1); return; }
-        __threadfence();
-        if (atomicAdd(&flags[p], 1) == 0) return;   // first arrival: sibling not ready
-        __threadfence();
+        // releases this thread's stores for the sibling's thread; the second
+        // to arrive acquires the first's
+        if (atomic_add_acq_rel(&flags[p], 1) == 0) return;   // first arrival: sibling not ready
         const int32_t l = left[p], r = right[p];
-        const float4 a0 = (l < 0) ? llo[~l] : __ldcg(&ilo[l]);
-        const float4 a1 = (l < 0) ? lhi[~l] : __ldcg(&ihi[l]);
-        const float4 b0 = (r < 0) ? llo[~r] : __ldcg(&ilo[r]);
-        const float4 b1 = (r < 0) ? lhi[~r] : __ldcg(&ihi[r]);
-        const float4 plo = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.f);
-        const float4 phi = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.f);
+        const bool from_left = l == cur;
+        const int32_t sib = from_left ? r : l;
+        const float4 s0 = (sib < 0) ? llo[~sib] : __ldcg(&ilo[sib]);
+        const float4 s1 = (sib < 0) ? lhi[~sib] : __ldcg(&ihi[sib]);
+        const float4 plo = make_float4(fminf(mlo.x, s0.x), fminf(mlo.y, s0.y), fminf(mlo.z, s0.z), 0.f);
+        const float4 phi = make_float4(fmaxf(mhi.x, s1.x), fmaxf(mhi.y, s1.y), fmaxf(mhi.z, s1.z), 0.f);
         __stcg(&ilo[p], plo);
         __stcg(&ihi[p], phi);
         if (sah) {
-            float cl[8], cr[8];
-            sah_child(sah, l, a0, a1, cl);
-            sah_child(sah, r, b0, b1, cr);
-            sah_node(sah, dec, p, half_area(plo, phi), count[p], cl, cr);
+            float srow[8], prow[8];
+            sah_child(sah, sib, s0, s1, srow);
+            if (from_left) sah_node(sah, dec, p, half_area(plo, phi), count[p], mrow, srow, prow);
+            else sah_node(sah, dec, p, half_area(plo, phi), count[p], srow, mrow, prow);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) mrow[i] = prow[i];
         }
+        cur = p;
+        mlo = plo;
+        mhi = phi;
         p = parent[p];
     }
 }
@@ -794,6 +819,218 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
     }
 }
 
+// ---------------------------------------------------------------- H-PLOC
+//
+// Hierarchical PLOC (Benthin, Meister, Barczak, Mohan, Oldfield, HPG 2024):
+// the clustering of PLOC without global iterations.  Every leaf climbs the
+// Morton radix tree bottom-up (Apetrei 2014: the parent of the node covering
+// sorted positions [L, R] sits at whichever boundary split, L - 1 or R, has
+// the longer common key prefix; the second of the two children to arrive
+// goes on, the first stops), carrying its subtree's clusters as binary refs
+// (>= 0 internal node, < 0 leaf ~k) at the start of its range in `cref`.  At
+// a parent the warp loads the two children's refs one per lane (at most
+// kHplocKeep each) and, when there are more than kHplocKeep of them (or the
+// parent is the root), their boxes, and merges mutual nearest neighbours
+// (smallest merged surface area, lowest index on ties -- the smallest such
+// pair is always mutual) until kHplocKeep remain (one at the root); then it
+// stores the refs at the start of the parent's range.  Warps handle their
+// lanes' parents one after another with all 32 lanes.  Stores a subtree
+// leaves for its parent are fenced at the end of every level, before the
+// next 64-bit exchange that tells a parent which child came first; data
+// written in the launch is read through L2.  Single-scene builds; nodes,
+// counts and surface-area tables as the PLOC kernels write them.
+constexpr int kHplocKeep = 16;
+constexpr int kHplocBlock = 256;
+constexpr unsigned long long kHplocEmpty = ~0ull;
+
+// Is the pair (a, a + 1) of sorted keys closer (longer common prefix) than
+// (b, b + 1)?  Equal keys fall back to the positions' xor (balanced trees
+// over runs of equal codes), then to the positions themselves: a strict
+// total order, so every split has exactly two children.
+__device__ __forceinline__ bool hploc_closer(const uint64_t *__restrict__ keys, int32_t a, int32_t b)
+{
+    const uint64_t ka = __ldg(keys + a) ^ __ldg(keys + a + 1), kb = __ldg(keys + b) ^ __ldg(keys + b + 1);
+    if (ka != kb) return ka < kb;
+    const uint32_t ia = (uint32_t)a ^ (uint32_t)(a + 1), ib = (uint32_t)b ^ (uint32_t)(b + 1);
+    if (ia != ib) return ia < ib;
+    return a < b;
+}
+
+__global__ void k_hploc_init(int32_t n, int32_t *__restrict__ cref, unsigned long long *__restrict__ meet)
+{
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        cref[k] = ~k;
+        meet[k] = kHplocEmpty;
+    }
+}
+
+__global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t *__restrict__ keys,
+                                                       int32_t *__restrict__ cref,
+                                                       unsigned long long *__restrict__ meet, int32_t *state,
+                                                       const float4 *__restrict__ llo, const float4 *__restrict__ lhi,
+                                                       float4 *__restrict__ cl, float4 *__restrict__ ch,
+                                                       int32_t *__restrict__ left, int32_t *__restrict__ right,
+                                                       int32_t *__restrict__ ncount, float4 *__restrict__ ilo,
+                                                       float4 *__restrict__ ihi, float *sah, uint32_t *dec,
+                                                       int32_t *__restrict__ parent,
+                                                       int32_t *__restrict__ leaf_parent)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t below = (1u << lane) - 1u;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t ninternal = n - 1;
+    int32_t L = i, R = i, nc = 1;          // the lane's subtree: range, refs at cref[L .. L + nc)
+    bool active = i < n && n > 1;
+    bool bad = false;
+    int guard = 0;
+    while (__any_sync(0xffffffffu, active)) {
+        // climb one level: the parent split and who arrived first
+        bool go_on = false, root = false;
+        int32_t lpos = 0, nl = 0, rpos = 0, nr = 0;
+        if (active) {
+            const bool go_right = (L == 0) || (R != n - 1 && hploc_closer(keys, R, L - 1));
+            const int32_t split = go_right ? R : L - 1;
+            const unsigned long long mine =
+                ((unsigned long long)(uint32_t)(go_right ? L : R) << 32) | (uint32_t)nc;
+            const unsigned long long other = atomicExch(&meet[split], mine);
+            if (other == kHplocEmpty) {
+                active = false;                  // the sibling's lane goes on
+            } else {
+                __threadfence();
+                const int32_t far = (int32_t)(other >> 32), sn = (int32_t)(uint32_t)other;
+                if (go_right) {                  // this lane holds the left child [L, split]
+                    lpos = L; nl = nc; rpos = split + 1; nr = sn;
+                    R = far;
+                } else {                         // the left child is [far, split]
+                    lpos = far; nl = sn; rpos = L; nr = nc;
+                    L = far;
+                }
+                if (L < 0 || R >= n || L > R || nl < 1 || nr < 1 || nl > kHplocKeep || nr > kHplocKeep) {
+                    bad = true;                  // never expected; keeps every access in bounds
+                    active = false;
+                } else {
+                    go_on = true;
+                    root = (L == 0 && R == n - 1);
+                }
+            }
+        }
+        // the warp serves each of its lanes' parents in turn
+        uint32_t todo = __ballot_sync(0xffffffffu, go_on);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int32_t p_l = __shfl_sync(0xffffffffu, lpos, src), p_nl = __shfl_sync(0xffffffffu, nl, src);
+            const int32_t p_r = __shfl_sync(0xffffffffu, rpos, src), p_nr = __shfl_sync(0xffffffffu, nr, src);
+            const bool p_root = __shfl_sync(0xffffffffu, root, src);
+            int cnt = p_nl + p_nr;
+            bool valid = (int)lane < cnt;
+            int32_t ref = 0;
+            if (valid) {
+                const int32_t g = (int)lane < p_nl ? p_l + (int32_t)lane : p_r + ((int32_t)lane - p_nl);
+                if (g >= 0 && g < n) ref = __ldcg(cref + g);
+                else { bad = true; ref = ~0; }
+            }
+            if (valid && (ref >= ninternal || ref < -n)) { bad = true; ref = ~0; }
+            const int target = p_root ? 1 : kHplocKeep;
+            if (cnt > target) {
+                float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+                if (valid) {
+                    c0 = ref < 0 ? __ldg(llo + ~ref) : __ldcg(ilo + ref);
+                    c1 = ref < 0 ? __ldg(lhi + ~ref) : __ldcg(ihi + ref);
+                }
+                while (cnt > target) {
+                    if (++guard > 65536) {       // never expected: a mutual pair always merges
+                        bad = true;
+                        break;
+                    }
+                    // nearest neighbour among the cnt clusters
+                    float best = __int_as_float(0x7f800000);
+                    int bk = (int)lane;
+                    for (int k = 0; k < cnt; ++k) {
+                        const float ox = __shfl_sync(0xffffffffu, c0.x, k), oy = __shfl_sync(0xffffffffu, c0.y, k);
+                        const float oz = __shfl_sync(0xffffffffu, c0.z, k);
+                        const float px = __shfl_sync(0xffffffffu, c1.x, k), py = __shfl_sync(0xffffffffu, c1.y, k);
+                        const float pz = __shfl_sync(0xffffffffu, c1.z, k);
+                        if (valid && k != (int)lane) {
+                            const float dx = fmaxf(c1.x, px) - fminf(c0.x, ox);
+                            const float dy = fmaxf(c1.y, py) - fminf(c0.y, oy);
+                            const float dz = fmaxf(c1.z, pz) - fminf(c0.z, oz);
+                            const float a = dx * dy + dx * dz + dy * dz;
+                            if (a < best) { best = a; bk = k; }
+                        }
+                    }
+                    const int back = __shfl_sync(0xffffffffu, bk, bk);
+                    const bool mutual = valid && bk != (int)lane && back == (int)lane;
+                    const bool make = mutual && (int)lane < bk;
+                    const bool drop = mutual && (int)lane > bk;
+                    const uint32_t mm = __ballot_sync(0xffffffffu, make);
+                    int idb = 0;
+                    if (lane == 0 && mm) idb = atomicAdd(&state[kStBase], __popc(mm));
+                    idb = __shfl_sync(0xffffffffu, idb, 0);
+                    const float4 b0 = make_float4(__shfl_sync(0xffffffffu, c0.x, bk),
+                                                  __shfl_sync(0xffffffffu, c0.y, bk),
+                                                  __shfl_sync(0xffffffffu, c0.z, bk), 0.f);
+                    const float4 b1 = make_float4(__shfl_sync(0xffffffffu, c1.x, bk),
+                                                  __shfl_sync(0xffffffffu, c1.y, bk),
+                                                  __shfl_sync(0xffffffffu, c1.z, bk), 0.f);
+                    const int32_t rb = __shfl_sync(0xffffffffu, ref, bk);
+                    if (make) {
+                        const int32_t id = idb + __popc(mm & below);
+                        if (id >= ninternal) {
+                            bad = true;
+                        } else {
+                            const int32_t l = ref, r = rb;
+                            left[id] = l;
+                            right[id] = r;
+                            if (l < 0) leaf_parent[~l] = id; else parent[l] = id;
+                            if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
+                            const int32_t cntl = l < 0 ? 1 : __ldcg(ncount + l);
+                            const int32_t cntr = r < 0 ? 1 : __ldcg(ncount + r);
+                            __stcg(ncount + id, cntl + cntr);
+                            float sl[8], sr[8];
+                            if (sah) {
+                                sah_child(sah, l, c0, c1, sl);
+                                sah_child(sah, r, b0, b1, sr);
+                            }
+                            c0 = box_min(c0, b0);
+                            c1 = box_max(c1, b1);
+                            if (sah) sah_node(sah, dec, id, half_area(c0, c1), cntl + cntr, sl, sr);
+                            __stcg(ilo + id, make_float4(c0.x, c0.y, c0.z, 0.f));
+                            __stcg(ihi + id, make_float4(c1.x, c1.y, c1.z, 0.f));
+                            ref = id;
+                        }
+                    }
+                    // stable compaction of the kept clusters
+                    const uint32_t km = __ballot_sync(0xffffffffu, valid && !drop);
+                    const int kc = __popc(km);
+                    const int from = (int)lane < kc ? (int)__fns(km, 0, (int)lane + 1) : (int)lane;
+                    c0 = make_float4(__shfl_sync(0xffffffffu, c0.x, from), __shfl_sync(0xffffffffu, c0.y, from),
+                                     __shfl_sync(0xffffffffu, c0.z, from), 0.f);
+                    c1 = make_float4(__shfl_sync(0xffffffffu, c1.x, from), __shfl_sync(0xffffffffu, c1.y, from),
+                                     __shfl_sync(0xffffffffu, c1.z, from), 0.f);
+                    ref = __shfl_sync(0xffffffffu, ref, from);
+                    cnt = kc;
+                    valid = (int)lane < cnt;
+                }
+                if (p_root && lane == 0) {
+                    // the root cluster, where the roots pass looks for it
+                    cl[0] = make_float4(c0.x, c0.y, c0.z, __int_as_float(0));
+                    ch[0] = make_float4(c1.x, c1.y, c1.z, __int_as_float(ref));
+                }
+            }
+            if (valid && p_l + (int32_t)lane < n) __stcg(cref + p_l + (int32_t)lane, ref);
+            if ((int)lane == src) {
+                nc = cnt;
+                if (p_root) active = false;
+            }
+        }
+        // this level's stores reach the device before any lane's next exchange
+        __threadfence();
+    }
+    if (bad) atomicExch(&state[kStError], 1);
+    if (i == 0) state[kStCount] = 1;
+}
+
 // The remaining clusters (one per non-empty segment, in segment order) are
 // the roots: level-0 collapse tasks (binary ref, wide node = segment).
 __global__ void k_ploc_roots(const float4 *__restrict__ cl, const float4 *__restrict__ ch,
@@ -1242,15 +1479,29 @@ __device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const in
         n_tri += c;
     }
     const bool writes = has_task && !err;
+    // allocation for the warp's four tasks at once: one atomic per counter
+    // (every task of a level adds to the same three addresses)
     int32_t child_base = 0, tri_base = 0, next = 0;
-    if (lane == 0 && writes) {
-        if (n_int) child_base = atomicAdd(&A.counters[0], n_int);
-        if (n_tri) tri_base = atomicAdd(&A.counters[1], n_tri);
-        if (n_int) next = atomicAdd(A.next_count, n_int);
+    {
+        const int mi = writes ? n_int : 0, mt = writes ? n_tri : 0;
+        int pi = 0, pt = 0, si = 0, st = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int vi = __shfl_sync(full, mi, 8 * q), vt = __shfl_sync(full, mt, 8 * q);
+            if (8 * q < gbase) { pi += vi; pt += vt; }
+            si += vi;
+            st += vt;
+        }
+        int32_t cb = 0, tb = 0, nb = 0;
+        if ((threadIdx.x & 31) == 0) {
+            if (si) cb = atomicAdd(&A.counters[0], si);
+            if (st) tb = atomicAdd(&A.counters[1], st);
+            if (si) nb = atomicAdd(A.next_count, si);
+        }
+        child_base = __shfl_sync(full, cb, 0) + pi;
+        tri_base = __shfl_sync(full, tb, 0) + pt;
+        next = __shfl_sync(full, nb, 0) + pi;
     }
-    child_base = __shfl_sync(full, child_base, gbase);
-    tri_base = __shfl_sync(full, tri_base, gbase);
-    next = __shfl_sync(full, next, gbase);
     const bool fits = child_base + n_int <= A.max_nodes && tri_base + n_tri <= A.n;
     if (has_task && lane == 0 && (err || !fits)) atomicExch(&A.counters[3], 1);
     if (!writes || !fits) active = false;
@@ -1416,9 +1667,12 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     int32_t *slot_ref = (int32_t *)carve(p, 8 * ((size_t)in.max_nodes + 1) * sizeof(int32_t));
     float *sah = RT_COLLAPSE_SAH ? (float *)carve(p, 8 * nn * sizeof(float)) : nullptr;
     uint32_t *dec = RT_COLLAPSE_SAH ? (uint32_t *)carve(p, nn * sizeof(uint32_t)) : nullptr;
-    const bool ploc = in.builder == kBuilderPloc;
+    const bool ploc = in.builder == kBuilderPloc || in.builder == kBuilderHploc;
+    const bool hploc = in.builder == kBuilderHploc && nseg == 1;   // batches cluster with PLOC
     float4 *cl[2] = {nullptr, nullptr}, *chh[2] = {nullptr, nullptr};
     int32_t *nnb = nullptr, *pstate = nullptr;
+    unsigned long long *meet = nullptr;
+    int32_t *cref = nullptr;
     int2 *bsum = nullptr;
     if (ploc) {
         cl[0] = (float4 *)carve(p, nn * sizeof(float4));
@@ -1426,6 +1680,10 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         cl[1] = (float4 *)carve(p, nn * sizeof(float4));
         chh[1] = (float4 *)carve(p, nn * sizeof(float4));
         nnb = (int32_t *)carve(p, nn * sizeof(int32_t));
+        if (hploc) {
+            meet = (unsigned long long *)carve(p, nn * sizeof(unsigned long long));
+            cref = (int32_t *)carve(p, nn * sizeof(int32_t));
+        }
         bsum = (int2 *)carve(p, (nn / kPlocBlock + 2) * sizeof(int2));
         pstate = (int32_t *)carve(p, kStWords * sizeof(int32_t));
     }
@@ -1500,7 +1758,14 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
         const size_t tail_smem = 2 * kPlocTailMax * sizeof(float4) + kPlocTailMax * sizeof(int32_t);
         if (cudaFuncSetAttribute(k_ploc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem) !=
             cudaSuccess) { R.status = -2; return R; }
-        bool tail = !finished && n <= kPlocTailMax;
+        bool tail = !finished && n <= kPlocTailMax && !hploc;
+        if (hploc && !finished) {
+            k_hploc_init<<<min((n + threads - 1) / threads, in.sm_count * 8), threads, 0, st>>>(n, cref, meet);
+            k_hploc<<<(n + kHplocBlock - 1) / kHplocBlock, kHplocBlock, 0, st>>>(
+                n, keys2, cref, meet, pstate, llo, lhi, cl[0], chh[0], left, right, ncount, ilo, ihi, sah, dec,
+                parent, leaf_parent);
+            finished = true;
+        }
         while (!finished && !tail) {
             for (int k = 0; k < kPlocGroup; ++k, ++it) {
                 const int a = it & 1;

@@ -5,7 +5,7 @@
 
 namespace rtc {
 
-enum : int32_t { kBuilderLbvh = 0, kBuilderPloc = 1 };
+enum : int32_t { kBuilderLbvh = 0, kBuilderPloc = 1, kBuilderHploc = 2 };
 
 struct BuildInputs {
     int32_t ntris;
@@ -18,7 +18,7 @@ struct BuildInputs {
     int32_t max_nodes;
     int32_t sm_count;
     int32_t *host_scratch;    // pinned host, >= 6 + kMaxDepth ints
-    int32_t builder = kBuilderPloc;   // binary tree: kBuilderLbvh or kBuilderPloc
+    int32_t builder = kBuilderPloc;   // binary tree: kBuilderLbvh, kBuilderPloc or kBuilderHploc
     int32_t morton_bits = 0;          // bits per axis of the sort key (0: from ntris)
     // several scenes in one build (a batch): segment of each triangle and
     // the triangle offset of each segment (nseg + 1 entries, host or device).

@@ -361,10 +361,10 @@ def test_watertight_intersector(rtlib, oracle):
 
 @pytest.mark.parametrize("which", ["terrain", "instances", "sphere"])
 def test_builders_agree(rtlib, which):
-    """The clustered (PLOC) and Morton radix (LBVH) trees are different trees
-    over the same triangles: closest hits, occlusion and frames must be
-    identical, every triangle must sit in exactly one leaf slot, and the
-    clustered tree must not need more node visits."""
+    """The clustered (PLOC, H-PLOC) and Morton radix (LBVH) trees are
+    different trees over the same triangles: closest hits, occlusion and
+    frames must be identical, every triangle must sit in exactly one leaf
+    slot, and the clustered trees must not need more node visits."""
     from raptor_gb300 import scenes
     if which == "terrain":
         scene, frame = scenes.terrain_scene(size_pow2=128, xres=160, yres=90)
@@ -381,7 +381,7 @@ def test_builders_agree(rtlib, which):
     d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
     rays = rtlib.rays_array(o, d, tmax=np.float32(0.5) * np.linalg.norm(tgt - o, axis=1).astype(np.float32))
     out = {}
-    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC, rtlib.RT_BUILDER_HPLOC):
         c = rtlib.Context(0)
         c.set_option(rtlib.RT_OPT_BUILDER, b)
         c.set_option(rtlib.RT_OPT_COUNT_FETCHES, 1)
@@ -393,15 +393,20 @@ def test_builders_agree(rtlib, which):
         out[b] = (sc.closest(rays), sc.any(rays), r["rgb"], r["ids"], r["stats"].nodes_fetched)
         sc.close()
         c.close()
-    (h0, a0, rgb0, id0, n0), (h1, a1, rgb1, id1, n1) = out[0], out[1]
-    assert np.array_equal(h0["tri"], h1["tri"])
-    assert np.array_equal(h0["t"], h1["t"])
-    assert np.array_equal(a0, a1)
-    assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
-    assert n1 <= n0 * 1.10
+    h0, a0, rgb0, id0, n0 = out[rtlib.RT_BUILDER_LBVH]
+    for b in (rtlib.RT_BUILDER_PLOC, rtlib.RT_BUILDER_HPLOC):
+        h1, a1, rgb1, id1, n1 = out[b]
+        assert np.array_equal(h0["tri"], h1["tri"])
+        assert np.array_equal(h0["t"], h1["t"])
+        assert np.array_equal(a0, a1)
+        assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
+        assert n1 <= n0 * 1.10, (b, n1, n0)
 
 
-@pytest.mark.parametrize("builder", ["lbvh", "ploc"])
+BUILDERS = {"lbvh": 0, "ploc": 1, "hploc": 2}
+
+
+@pytest.mark.parametrize("builder", ["lbvh", "ploc", "hploc"])
 def test_morton_bits_do_not_change_results(rtlib, builder):
     """The Morton code width the sort orders (RT_OPT_MORTON_BITS: 10, 21, or
     sized from the triangle count) shapes the tree but not its answers:
@@ -418,7 +423,7 @@ def test_morton_bits_do_not_change_results(rtlib, builder):
     out = []
     for bits in (0, 10, 21):
         c = rtlib.Context(0)
-        c.set_option(rtlib.RT_OPT_BUILDER, rtlib.RT_BUILDER_LBVH if builder == "lbvh" else rtlib.RT_BUILDER_PLOC)
+        c.set_option(rtlib.RT_OPT_BUILDER, BUILDERS[builder])
         c.set_option(rtlib.RT_OPT_MORTON_BITS, bits)
         sc = rtlib.Scene(c, scene)
         st = sc.stats()
@@ -449,7 +454,7 @@ def test_builder_option_rejects_unknown(rtlib):
 
 def test_builders_on_degenerate_input(rtlib):
     """Thousands of identical triangles (every merge distance ties) and a
-    scene in two far-apart clusters: both builders must finish and agree,
+    scene in two far-apart clusters: every builder must finish and agree,
     with ties broken towards the lowest triangle id."""
     from raptor_gb300 import scenes
     v, t = scenes.geodesic_sphere(6)
@@ -467,7 +472,7 @@ def test_builders_on_degenerate_input(rtlib):
     d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
     rays = rtlib.rays_array(o, d)
     res = []
-    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC, rtlib.RT_BUILDER_HPLOC):
         c = rtlib.Context(0)
         c.set_option(rtlib.RT_OPT_BUILDER, b)
         sc = rtlib.Scene(c, scene)
@@ -476,7 +481,8 @@ def test_builders_on_degenerate_input(rtlib):
         res.append(sc.closest(rays))
         sc.close()
         c.close()
-    assert np.array_equal(res[0]["tri"], res[1]["tri"]) and np.array_equal(res[0]["t"], res[1]["t"])
+    for r in res[1:]:
+        assert np.array_equal(res[0]["tri"], r["tri"]) and np.array_equal(res[0]["t"], r["t"])
     hit_copy = (res[1]["tri"] >= 0) & (res[1]["tri"] < copies)
     assert hit_copy.sum() > 100
     assert (res[1]["tri"][hit_copy] == 0).all()     # equal t: the lowest id wins
@@ -581,7 +587,7 @@ def test_batch_at_the_scene_limit(rtlib, ctx):
     b.close()
 
 
-@pytest.mark.parametrize("builder", ["lbvh", "ploc"])
+@pytest.mark.parametrize("builder", ["lbvh", "ploc", "hploc"])
 def test_refit_equals_fresh_upload(rtlib, builder):
     """rt_scene_refit_vertices keeps the tree's topology and refits boxes and
     quantisation: after small and large motions the closest hits, any hits
@@ -589,7 +595,7 @@ def test_refit_equals_fresh_upload(rtlib, builder):
     node count does not change.  Refit needs a built scene."""
     from raptor_gb300 import scenes
     c = rtlib.Context(0)
-    c.set_option(rtlib.RT_OPT_BUILDER, rtlib.RT_BUILDER_LBVH if builder == "lbvh" else rtlib.RT_BUILDER_PLOC)
+    c.set_option(rtlib.RT_OPT_BUILDER, BUILDERS[builder])
     scene, frame = scenes.terrain_scene(size_pow2=128, xres=160, yres=90)
     sc = rtlib.Scene(c, scene)
     nodes0 = sc.info()["nodes"]
@@ -790,9 +796,9 @@ def test_materials_per_triangle(rtlib, ctx, oracle):
 
 def test_large_scene_33m_triangles(rtlib):
     """A 4096^2 heightfield (33,554,432 triangles, 16x the headline scene):
-    both builders finish, place every triangle in one leaf slot, and give
-    the same closest hits, occlusion and frame; a refit keeps the hits of a
-    rebuild."""
+    every builder finishes, places every triangle in one leaf slot, and
+    gives the same closest hits, occlusion and frame; a refit keeps the hits
+    of a rebuild."""
     from raptor_gb300 import scenes
     scene, frame = scenes.terrain_scene(size_pow2=4096, xres=320, yres=180)
     n = scene["tris"].shape[0]
@@ -806,7 +812,7 @@ def test_large_scene_33m_triangles(rtlib):
     d = (d / np.linalg.norm(d, axis=1)[:, None]).astype(np.float32)
     rays = rtlib.rays_array(o.astype(np.float32), d, tmax=np.float32(150.0))
     res = []
-    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC):
+    for b in (rtlib.RT_BUILDER_LBVH, rtlib.RT_BUILDER_PLOC, rtlib.RT_BUILDER_HPLOC):
         c = rtlib.Context(0)
         c.set_option(rtlib.RT_OPT_BUILDER, b)
         sc = rtlib.Scene(c, scene)
@@ -828,11 +834,12 @@ def test_large_scene_33m_triangles(rtlib):
             assert np.array_equal(after_refit["t"], after_build["t"])
         sc.close()
         c.close()
-    (h0, a0, rgb0, id0), (h1, a1, rgb1, id1) = res
-    assert np.array_equal(h0["tri"], h1["tri"]) and np.array_equal(h0["t"], h1["t"])
-    assert np.array_equal(a0, a1)
-    assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
-    assert (h1["tri"] >= 0).mean() > 0.5
+    h0, a0, rgb0, id0 = res[0]
+    for h1, a1, rgb1, id1 in res[1:]:
+        assert np.array_equal(h0["tri"], h1["tri"]) and np.array_equal(h0["t"], h1["t"])
+        assert np.array_equal(a0, a1)
+        assert np.array_equal(rgb0, rgb1) and np.array_equal(id0, id1)
+    assert (h0["tri"] >= 0).mean() > 0.5
 
 
 @pytest.mark.parametrize("case", tone_cases(), ids=lambda c: f"tone{c[0]}")
