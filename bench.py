@@ -639,7 +639,9 @@ def workload_ingest(ctx, stream, steps):
 def workload_terrain_tonemap(ctx, stream, flush, steps):
     """The headline terrain frame (2,097,152 triangles, 1920x1080) through the
     framebuffer epilogue: float frame, exposure tone mapping (key 0.18) and
-    sRGB gamma, then RGB8; the plain frame beside it."""
+    sRGB gamma, then RGB8; the plain frame beside it; and the bilateral
+    tone mapper with sRGB gamma (its grid, exact Gaussian blur by Fourier
+    transforms in double, slice and compression)."""
     import torch
     from raptor_gb300 import core, scenes
     scene, frame = scenes.terrain_scene()
@@ -647,8 +649,10 @@ def workload_terrain_tonemap(ctx, stream, flush, steps):
     rgb = torch.empty((1080, 1920, 3), dtype=torch.uint8, device="cuda")
     tone = {"mode": 5, "gamma": 2.2}
     out = {"triangles": int(scene["tris"].shape[0]), "resolution": [1920, 1080], "tone": tone}
+    bil = {"mode": 8, "gamma": 2.2}
     for key, fn in (("plain", lambda: sc.render(frame, rgb=rgb)["stats"]),
-                    ("tone_mapped", lambda: sc.render_tone_mapped(frame, tone, rgb=rgb)["stats"])):
+                    ("tone_mapped", lambda: sc.render_tone_mapped(frame, tone, rgb=rgb)["stats"]),
+                    ("bilateral", lambda: sc.render_tone_mapped(frame, bil, rgb=rgb)["stats"])):
         for _ in range(3):
             fn()
         secs, st = time_frames(fn, steps, stream, flush)

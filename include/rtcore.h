@@ -386,7 +386,16 @@ void rt_mesh_free(rt_mesh *mesh);
  * none.  The histogram modes (camera::histogram_tone_map, camera.cc:
  * 1843-2062) resample the frame to one block per degree of the camera's
  * view and need a view of 2 to 4096 degrees each way (measured as the
- * reference measures it: 2w/t and 2h/t radians). */
+ * reference measures it: 2w/t and 2h/t radians).  The bilateral mode
+ * (camera::bilateral_filter_tone_map(0.4, s, 0.4, s), s = 0.02 * min(w,
+ * h), camera.cc:1354-1358, 1632-1812) runs the reference's bilateral grid
+ * with its Gaussian blur computed exactly (the reference's FFTW rounding
+ * is not reproduced, so a pixel may differ by a level); like the reference
+ * it compresses the base to a contrast of 300 without removing its
+ * maximum, so frames of ordinary brightness saturate.  A sample at or below
+ * the 3.18e-7 luminance floor, which the reference leaves unset, counts as
+ * log-luminance 0.  Frames whose grid would exceed 2^26 cells (extreme
+ * aspect ratios) are refused. */
 #define RT_TONE_NONE 0
 #define RT_TONE_GLOBAL_CONTRAST 1
 #define RT_TONE_LOCAL_HISTOGRAM 2          /* camera::histogram_tone_map(false) */
@@ -395,6 +404,7 @@ void rt_mesh_free(rt_mesh *mesh);
 #define RT_TONE_GLOBAL_EXPOSURE 5
 #define RT_TONE_GLOBAL_AVG_LUMINANCE 6
 #define RT_TONE_GLOBAL_MAX_LUMINANCE 7
+#define RT_TONE_GLOBAL_BILATERAL 8
 #define RT_TONE_GLOBAL_FERWERDA 9
 typedef struct rt_tone_map {
     int32_t mode;

@@ -1,6 +1,6 @@
-// Declaration-only stand-in for FFTW (single precision).  The reference's
-// camera.cc uses it for its glare filter, which the harness never enables;
-// io_stubs.cc defines the names so the library loads.
+// Stand-in for FFTW's single-precision interface (declarations).  The
+// reference's camera.cc uses it for its glare filter and its bilateral tone
+// mapper; io_stubs.cc defines the functions with direct transforms.
 #pragma once
 #include <cstddef>
 typedef float fftwf_complex[2];

@@ -1732,10 +1732,187 @@ static void tm_histogram(float *img, int32_t w, int32_t h, const ro_tone_map *tm
     free(sl);
 }
 
+/* One discrete Fourier transform, sign -1 (forward) or +1, along axis ax of
+ * a complex array (re, im) of dims n[0..2], row-major (the last fastest). */
+static void dft_axis(double *re, double *im, const int32_t n[3], int ax, int sign)
+{
+    const int32_t m = n[ax];
+    size_t inner = 1;
+    for (int k = ax + 1; k < 3; ++k) inner *= (size_t)n[k];
+    const size_t outer = ((size_t)n[0] * (size_t)n[1] * (size_t)n[2]) / ((size_t)m * inner);
+    double *cs = (double *)malloc(2 * (size_t)m * sizeof(double));
+    double *lr = (double *)malloc(4 * (size_t)m * sizeof(double));
+    double *li = lr + m, *orr = lr + 2 * m, *oi = lr + 3 * m;
+    for (int32_t k = 0; k < m; ++k) {
+        const double a = 6.283185307179586476925286766559 * (double)k / (double)m;
+        cs[2 * k] = cos(a);
+        cs[2 * k + 1] = (double)sign * sin(a);
+    }
+    for (size_t o = 0; o < outer; ++o)
+        for (size_t q = 0; q < inner; ++q) {
+            const size_t base = o * (size_t)m * inner + q;
+            for (int32_t j = 0; j < m; ++j) { lr[j] = re[base + (size_t)j * inner]; li[j] = im[base + (size_t)j * inner]; }
+            for (int32_t k = 0; k < m; ++k) {
+                double sr = 0.0, si = 0.0;
+                for (int32_t j = 0; j < m; ++j) {
+                    const int32_t t = (int32_t)(((int64_t)j * k) % m);
+                    sr += lr[j] * cs[2 * t] - li[j] * cs[2 * t + 1];
+                    si += lr[j] * cs[2 * t + 1] + li[j] * cs[2 * t];
+                }
+                orr[k] = sr;
+                oi[k] = si;
+            }
+            for (int32_t k = 0; k < m; ++k) { re[base + (size_t)k * inner] = orr[k]; im[base + (size_t)k * inner] = oi[k]; }
+        }
+    free(lr);
+    free(cs);
+}
+
+/* Circular convolution over dims n[0..2] (row-major) of nch real channels
+ * (channel c at data + c * N) with kern, evaluated through the Fourier
+ * transform in double: what the reference's single-precision FFTW plans
+ * compute, without their rounding.  out: nch * N floats. */
+static void circ_conv3(const float *data, int nch, const float *kern, const int32_t n[3], float *out)
+{
+    const size_t N = (size_t)n[0] * (size_t)n[1] * (size_t)n[2];
+    double *kr = (double *)calloc(2 * N, sizeof(double)), *ki = kr + N;
+    double *dr = (double *)calloc(2 * N, sizeof(double)), *di = dr + N;
+    for (size_t i = 0; i < N; ++i) kr[i] = kern[i];
+    for (int ax = 0; ax < 3; ++ax) dft_axis(kr, ki, n, ax, -1);
+    for (int c = 0; c < nch; ++c) {
+        for (size_t i = 0; i < N; ++i) { dr[i] = data[(size_t)c * N + i]; di[i] = 0.0; }
+        for (int ax = 0; ax < 3; ++ax) dft_axis(dr, di, n, ax, -1);
+        for (size_t i = 0; i < N; ++i) {
+            const double a = dr[i] * kr[i] - di[i] * ki[i], b = dr[i] * ki[i] + di[i] * kr[i];
+            dr[i] = a;
+            di[i] = b;
+        }
+        for (int ax = 0; ax < 3; ++ax) dft_axis(dr, di, n, ax, +1);
+        for (size_t i = 0; i < N; ++i) out[(size_t)c * N + i] = (float)(dr[i] / (double)N);
+    }
+    free(dr);
+    free(kr);
+}
+
+/* camera::bilateral_filter_tone_map(0.4, s, 0.4, s), s = 0.02 * min(w, h)
+ * (camera.cc:1354-1358, 1632-1812): the bilateral grid of log10 luminance
+ * (one cell per s pixels and per 0.4 decades, 3 cells of padding), blurred
+ * by a Gaussian of one cell through a Fourier-domain product, sliced
+ * trilinearly at every pixel, then the detail (log luminance less the
+ * blurred base) kept and the base compressed to a contrast of 300:
+ * Y = 10^(base * gamma + detail) / 255.  The reference hands its
+ * x-fastest grid (index x + W (y + H z)) to FFTW as dims (W, H, D), whose
+ * last dimension varies fastest, so its "Gaussian" is convolved over those
+ * axes of the flat array; restated as such.  A pixel at or below 3.18e-7
+ * has no log value in the reference (its array is left unset there): here
+ * it is 0, what a glibc host's fresh pages hold for frames over 32,768
+ * pixels, and its grid cell is clamped into the grid. */
+static void tm_bilateral(float *img, int32_t w, int32_t h)
+{
+    const int32_t n = w * h;
+    const float r_s = 0.4f, s_s = 0.02f * (float)(w < h ? w : h), r_sa = 0.4f, s_sa = s_s;
+    float *logi = (float *)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
+    float in_max = -RO_MAX_DIST, in_min = RO_MAX_DIST;
+    for (int32_t i = 0; i < n; ++i) {
+        const float g = img[3 * (size_t)i + 1];
+        if (g > 3.18e-7f) {
+            logi[i] = log10f(g);
+            in_max = smax(in_max, logi[i]);
+            in_min = smin(in_min, logi[i]);
+        } else {
+            logi[i] = 0.0f;
+        }
+    }
+    const float delta = in_max - in_min;
+    const float sigma_r = r_s / r_sa, sigma_s = s_s / s_sa;
+    const int32_t pxy = (int32_t)(2.0f * sigma_s) + 1, pz = (int32_t)(2.0f * sigma_r) + 1;
+    const int32_t W = (int32_t)((float)(w - 1) / s_sa) + 1 + (pxy << 1);
+    const int32_t H = (int32_t)((float)(h - 1) / s_sa) + 1 + (pxy << 1);
+    const int32_t D = (int32_t)(delta / r_sa) + 1 + (pz << 1);
+    const size_t N = (size_t)W * (size_t)H * (size_t)D;
+    float *wiw = (float *)calloc(2 * N, sizeof(float));
+    for (int32_t x = 0; x < w; ++x)
+        for (int32_t y = 0; y < h; ++y) {
+            const int32_t sx = (int32_t)((float)x / s_sa + 0.5f) + pxy;
+            const int32_t sy = (int32_t)((float)y / s_sa + 0.5f) + pxy;
+            int32_t sz = (int32_t)((logi[x + w * y] - in_min) / r_sa + 0.5f) + pz;
+            sz = sz < 0 ? 0 : (sz > D - 1 ? D - 1 : sz);
+            const size_t c = (size_t)sx + (size_t)W * ((size_t)sy + (size_t)H * (size_t)sz);
+            wiw[c] += 1.0f;
+            wiw[c + N] += logi[x + w * y];
+        }
+    float *kern = (float *)malloc(N * sizeof(float));
+    const int32_t hw = W >> 1, hh = H >> 1, hd = D >> 1;
+    for (int32_t x = 0; x < W; ++x) {
+        const float X = (float)x - ((x > hw) ? (float)W : 0.0f);
+        for (int32_t y = 0; y < H; ++y) {
+            const float Y = (float)y - ((y > hh) ? (float)H : 0.0f);
+            for (int32_t z = 0; z < D; ++z) {
+                const float Z = (float)z - ((z > hd) ? (float)D : 0.0f);
+                const float rr = ((X * X) + (Y * Y)) / (sigma_s * sigma_s) + (Z * Z) / (sigma_r * sigma_r);
+                kern[(size_t)x + (size_t)W * ((size_t)y + (size_t)H * (size_t)z)] = expf(-rr * 0.5f);
+            }
+        }
+    }
+    float *blur = (float *)malloc(2 * N * sizeof(float));
+    const int32_t dims[3] = {W, H, D};
+    circ_conv3(wiw, 2, kern, dims, blur);
+    const float *bw = blur, *biw = blur + N;
+    float *res = (float *)malloc((size_t)(n > 0 ? n : 1) * sizeof(float));
+    float max_v = -RO_MAX_DIST, min_v = RO_MAX_DIST;
+    for (int32_t x = 0; x < w; ++x)
+        for (int32_t y = 0; y < h; ++y) {
+            const float z = logi[x + w * y] - in_min;
+            const float xa_ = (float)x / s_sa + (float)pxy;
+            const int32_t xi = (int32_t)xa_ < W - 1 ? (int32_t)xa_ : W - 1, xi0 = xi < 0 ? 0 : xi;
+            const int32_t xx = xi0 + 1 < W - 1 ? xi0 + 1 : W - 1;
+            const float ya_ = (float)y / s_sa + (float)pxy;
+            const int32_t yi = (int32_t)ya_ < H - 1 ? (int32_t)ya_ : H - 1, yi0 = yi < 0 ? 0 : yi;
+            const int32_t yy = yi0 + 1 < H - 1 ? yi0 + 1 : H - 1;
+            const float za_ = z / r_sa + (float)pz;
+            const int32_t zi = (int32_t)za_ < D - 1 ? (int32_t)za_ : D - 1, zi0 = zi < 0 ? 0 : zi;
+            const int32_t zz = zi0 + 1 < D - 1 ? zi0 + 1 : D - 1;
+            const float ax = xa_ - (float)xi0, ay = ya_ - (float)yi0, az = za_ - (float)zi0;
+#define RO_AT(A, X_, Y_, Z_) (A)[(size_t)(X_) + (size_t)W * ((size_t)(Y_) + (size_t)H * (size_t)(Z_))]
+            const float IW = (1.0f - ax) * (1.0f - ay) * (1.0f - az) * RO_AT(biw, xi0, yi0, zi0) +
+                             ax * (1.0f - ay) * (1.0f - az) * RO_AT(biw, xx, yi0, zi0) +
+                             (1.0f - ax) * ay * (1.0f - az) * RO_AT(biw, xi0, yy, zi0) +
+                             ax * ay * (1.0f - az) * RO_AT(biw, xx, yy, zi0) +
+                             (1.0f - ax) * (1.0f - ay) * az * RO_AT(biw, xi0, yi0, zz) +
+                             ax * (1.0f - ay) * az * RO_AT(biw, xx, yi0, zz) +
+                             (1.0f - ax) * ay * az * RO_AT(biw, xi0, yy, zz) +
+                             ax * ay * az * RO_AT(biw, xx, yy, zz);
+            const float Wt = (1.0f - ax) * (1.0f - ay) * (1.0f - az) * RO_AT(bw, xi0, yi0, zi0) +
+                             ax * (1.0f - ay) * (1.0f - az) * RO_AT(bw, xx, yi0, zi0) +
+                             (1.0f - ax) * ay * (1.0f - az) * RO_AT(bw, xi0, yy, zi0) +
+                             ax * ay * (1.0f - az) * RO_AT(bw, xx, yy, zi0) +
+                             (1.0f - ax) * (1.0f - ay) * az * RO_AT(bw, xi0, yi0, zz) +
+                             ax * (1.0f - ay) * az * RO_AT(bw, xx, yi0, zz) +
+                             (1.0f - ax) * ay * az * RO_AT(bw, xi0, yy, zz) +
+                             ax * ay * az * RO_AT(bw, xx, yy, zz);
+#undef RO_AT
+            const float r = IW / Wt;
+            res[x + w * y] = r;
+            max_v = smax(max_v, r);
+            min_v = smin(min_v, r);
+        }
+    const float contrast = 300.0f;
+    const float gamma = log10f(contrast) / (max_v - min_v);
+    for (int32_t i = 0; i < n; ++i) {
+        const float scaled = powf(10.0f, (res[i] * gamma + (logi[i] - res[i])));
+        img[3 * (size_t)i + 1] = scaled * (1.0f / 255.0f);
+    }
+    free(res);
+    free(blur);
+    free(kern);
+    free(wiw);
+    free(logi);
+}
+
 int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *tm)
 {
     const int32_t mode = tm->mode;
-    if (!(mode >= 0 && mode <= 9 && mode != 8)) return -1;
+    if (!(mode >= 0 && mode <= 9)) return -1;
     const int32_t n = w * h;
     /* first pass: to CIE Yxy, log-average and maximum luminance */
     float Yi = 0.0f, maxY = 0.0f, rgbAvg = 0.0f;
@@ -1816,6 +1993,8 @@ int32_t ro_tone_map_frame(float *img, int32_t w, int32_t h, const ro_tone_map *t
         for (int32_t i = 0; i < n; ++i) img[3 * (size_t)i + 1] *= sf;
     } else if (mode == 2 || mode == 3) {
         tm_histogram(img, w, h, tm, mode == 3, Yi);
+    } else if (mode == 8) {
+        tm_bilateral(img, w, h);
     } else if (mode == 9) {
         const float lda = 800.0f;
         const float log_lda = logf(lda * 0.5f);

@@ -860,8 +860,11 @@ static rt_status tone_view(const rt_tone_map *tone, const rt_camera &cam, int32_
     const int m = tone->mode;
     if (!(m == RT_TONE_NONE || m == RT_TONE_GLOBAL_CONTRAST || m == RT_TONE_LOCAL_HISTOGRAM ||
           m == RT_TONE_LOCAL_HUMAN_HISTOGRAM || m == RT_TONE_GLOBAL_NON_LINEAR || m == RT_TONE_GLOBAL_EXPOSURE ||
-          m == RT_TONE_GLOBAL_AVG_LUMINANCE || m == RT_TONE_GLOBAL_MAX_LUMINANCE || m == RT_TONE_GLOBAL_FERWERDA))
+          m == RT_TONE_GLOBAL_AVG_LUMINANCE || m == RT_TONE_GLOBAL_MAX_LUMINANCE || m == RT_TONE_GLOBAL_FERWERDA ||
+          m == RT_TONE_GLOBAL_BILATERAL))
         return fail(RT_ERR_INVALID_ARG, w + ": unsupported tone-mapping mode");
+    if (m == RT_TONE_GLOBAL_BILATERAL && !bilateral_grid_fits(fw, fh))
+        return fail(RT_ERR_INVALID_ARG, w + ": the bilateral grid of this frame would exceed 2^26 cells");
     const float lim = 3.0e38f;
     if (!(std::fabs(tone->key) < lim && std::fabs(tone->xw) < lim && std::fabs(tone->yw) < lim && tone->gamma >= 0.0f &&
           tone->gamma < lim))
@@ -892,6 +895,10 @@ static rt_status tone_view(const rt_tone_map *tone, const rt_camera &cam, int32_
 }
 
 static int64_t tone_blocks(const ToneView &tv) { return (int64_t)tv.hist_sx * tv.hist_sy; }
+static size_t tone_extra(const ToneView &tv, const rt_camera &fine)
+{
+    return tv.enabled && tv.mode == RT_TONE_GLOBAL_BILATERAL ? bilateral_scratch_bytes(fine.xres, fine.yres) : 0;
+}
 
 rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa_x, int32_t aa_y, const float *fimg,
                             const rt_tone_map *tone, uint8_t *rgb_out)
@@ -918,7 +925,7 @@ rt_status rt_tone_map_image(rt_context *ctx, const rt_camera *camera, int32_t aa
     RenderOut o;
     st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
     if (st != RT_OK) return st;
-    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv))), "scratch allocation");
+    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv)) + tone_extra(tv, fine)), "scratch allocation");
     RT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), ctx->stream), "counter clear");
     RT_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "event record");
     launch_tone_map((const float *)dimg, fine.xres, fine.yres, aa_x, aa_y, tv, o.rgb, (ToneAcc *)ctx->tone.ptr,
@@ -1004,7 +1011,7 @@ rt_status rt_render_tone_mapped(rt_scene *s, const rt_camera *camera, int32_t aa
     st = prepare_outputs(ctx, npix, rgb_out, nullptr, nullptr, o);
     if (st != RT_OK) return st;
     RT_CUDA(ctx->fimg.reserve(nfine * 3 * sizeof(float)), "float frame allocation");
-    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv))),
+    RT_CUDA(ctx->tone.reserve(kToneScratch + tone_scratch_bytes((int64_t)nfine, tone_blocks(tv)) + tone_extra(tv, fine)),
             "tone accumulator allocation");
     LightSet ls;
     ls.n = nlights;

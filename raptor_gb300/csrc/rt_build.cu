@@ -358,7 +358,9 @@ __global__ void k_roots(int32_t nseg, int32_t n, const int32_t *__restrict__ seg
         return;
     }
     int32_t root = ~f;
-    if (l > f) {
+    if (nseg == 1 && l > f) {
+        root = 0;   // the radix tree of one scene: node 0 spans every leaf
+    } else if (l > f) {
         int32_t p = leaf_parent[f];
         int guard = 0;
         while (p >= 0 && !(first[p] <= f && last[p] >= l) && guard++ < 128) p = parent[p];

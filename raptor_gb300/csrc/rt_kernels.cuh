@@ -43,6 +43,8 @@ struct ToneView {
     // hist_inc_x x hist_inc_y samples (one per degree of view)
     int32_t hist_sx, hist_sy;
     float hist_inc_x, hist_inc_y;
+    // bilateral mode: each sample's mapped luminance (set by launch_tone_map)
+    const float *bil;
 };
 // The luminance map of the histogram modes (camera::histogram_tone_map).
 struct ToneHist {
@@ -104,6 +106,10 @@ void launch_sequential_sum(const float *v, int64_t n, float max_abs, ToneAcc *ac
 // scratch: tone_scratch_bytes(fw * fh, blocks) of device memory (blocks:
 // hist_sx * hist_sy of a histogram mode, else 0).
 size_t tone_scratch_bytes(int64_t n, int64_t blocks = 0);
+// The bilateral mode's extra scratch (after tone_scratch_bytes(n, 0)), and
+// whether its grid fits (at most 2^26 cells, 4096 per axis).
+size_t bilateral_scratch_bytes(int32_t fw, int32_t fh);
+bool bilateral_grid_fits(int32_t fw, int32_t fh);
 void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
                      uint8_t *rgb, ToneAcc *acc, void *scratch, int sm_count, cudaStream_t st);
 void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet &lights, const MaterialView &mat,

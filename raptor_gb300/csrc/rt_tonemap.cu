@@ -882,7 +882,8 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_range(const float *__rest
     uint32_t lo = 0xffffffffu, hi = 0u;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const Yxy p = to_yxy<true>(make_float3(fimg[3 * i], fimg[3 * i + 1], fimg[3 * i + 2]), t);
-        const uint32_t key = order_key(map_lum<true>(p.Y, t, k, acc->h));
+        const uint32_t key =
+            order_key((t.mode == RT_TONE_GLOBAL_BILATERAL) ? t.bil[i] : map_lum<true>(p.Y, t, k, acc->h));
         lo = min(lo, key);
         hi = max(hi, key);
     }
@@ -911,7 +912,7 @@ __device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int
             float3 c = make_float3(fimg[3 * s], fimg[3 * s + 1], fimg[3 * s + 2]);
             if (t.enabled) {
                 const Yxy p = to_yxy<EXACT>(c, t);
-                float g = map_lum<EXACT>(p.Y, t, k, hh);
+                float g = (t.mode == RT_TONE_GLOBAL_BILATERAL) ? t.bil[s] : map_lum<EXACT>(p.Y, t, k, hh);
                 if (stretch) g = xmul(xadd(g, offset), scale);
                 c = to_rgb<EXACT>(p.x, g, p.y, t.gamma);
             }
@@ -1010,6 +1011,268 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_fix(const float *__restri
     }
 }
 
+// ---- camera::bilateral_filter_tone_map(0.4, s, 0.4, s), s = 0.02 min(w, h)
+// (camera.cc:1354-1358, 1632-1812)
+//
+// The bilateral grid of log10 luminance: one cell per s samples each way and
+// per 0.4 decades, 3 cells of padding (sigma = 1 cell: 2 * 1 + 1).  The
+// reference blurs it with a Gaussian through single-precision FFTW plans of
+// dims (W, H, D) over its x-fastest array (index x + W (y + H z)), FFTW's
+// last dimension varying fastest: the circular convolution runs over those
+// axes of the flat array.  Here the same convolution is computed exactly, as
+// discrete Fourier transforms along the three axes in double.  Grid depth D
+// depends on the frame's log-luminance range, so the kernels read the grid's
+// size from BilState; the host sizes the scratch for the deepest grid a
+// float's range allows.
+constexpr int32_t kBilMaxDepth = 119;     // (log10 FLT_MAX - log10 3.18e-7) / 0.4 + 1 + 6
+constexpr int32_t kBilMaxAxis = 4096;
+
+struct BilState {
+    uint32_t kmin, kmax;    // range of the log-luminance above the floor (order keys)
+    uint32_t rmin, rmax;    // range of the sliced base (order keys)
+    int32_t W, H, D;
+    float in_min;
+    int32_t err;
+};
+
+struct BilGeom {            // what the frame size fixes
+    int32_t fw, fh;
+    float s_sa;             // cells per sample: 0.02 * min(fw, fh)
+    int32_t W, H;           // grid width and height (padding included)
+};
+
+__host__ __device__ inline BilGeom bil_geom(int32_t fw, int32_t fh)
+{
+    BilGeom g;
+    g.fw = fw;
+    g.fh = fh;
+    g.s_sa = 0.02f * (float)(fw < fh ? fw : fh);
+    g.W = (int32_t)((float)(fw - 1) / g.s_sa) + 1 + 6;
+    g.H = (int32_t)((float)(fh - 1) / g.s_sa) + 1 + 6;
+    return g;
+}
+
+// Log10 luminance of every sample (0 at or below the floor) and the range
+// of those above it.
+__global__ void __launch_bounds__(kToneThreads) k_bil_log(const float *__restrict__ fimg, int64_t n, ToneView t,
+                                                          float *__restrict__ logi, BilState *bs)
+{
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const Yxy p = to_yxy<true>(make_float3(fimg[3 * i], fimg[3 * i + 1], fimg[3 * i + 2]), t);
+        float l = 0.0f;
+        if (p.Y > 3.18e-7f) {
+            l = log10_f(p.Y);
+            const uint32_t k = order_key(l);
+            lo = min(lo, k);
+            hi = max(hi, k);
+        }
+        logi[i] = l;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&bs->kmin, lo);
+        atomicMax(&bs->kmax, hi);
+    }
+}
+
+// The grid's depth from the range, and the twiddle factors of each axis
+// (dims in FFTW's order: W slowest, D fastest).
+__global__ void k_bil_dims(BilGeom g, BilState *bs, double *__restrict__ tw)
+{
+    __shared__ int32_t dims[3];
+    if (threadIdx.x == 0) {
+        bs->W = g.W;
+        bs->H = g.H;
+        int32_t D = 7;
+        float in_min = 0.0f;
+        if (bs->kmin <= bs->kmax) {
+            in_min = key_float(bs->kmin);
+            const float delta = xsub(key_float(bs->kmax), in_min);
+            D = (int32_t)xdiv(delta, 0.4f) + 1 + 6;
+        } else {
+            bs->err = 1;   // no sample above the floor: the reference's range is undefined
+        }
+        if (D > kBilMaxDepth) { D = kBilMaxDepth; bs->err = 1; }
+        bs->D = D;
+        bs->in_min = in_min;
+        dims[0] = g.W;
+        dims[1] = g.H;
+        dims[2] = D;
+    }
+    __syncthreads();
+    for (int a = 0; a < 3; ++a) {
+        const int32_t m = dims[a];
+        for (int32_t k = threadIdx.x; k < m; k += blockDim.x) {
+            double s, c;
+            sincospi(2.0 * (double)k / (double)m, &s, &c);
+            tw[2 * ((size_t)a * kBilMaxAxis + (size_t)k)] = c;
+            tw[2 * ((size_t)a * kBilMaxAxis + (size_t)k) + 1] = s;
+        }
+    }
+}
+
+// The splat: count and log-luminance sum per cell (sample order as the
+// reference's loops, sums in double).  The cell of a sample outside the
+// grid's depth (a floor sample's 0 beyond the range) is clamped into it.
+__global__ void __launch_bounds__(kToneThreads) k_bil_splat(const float *__restrict__ logi, BilGeom g,
+                                                            const BilState *bs, double *__restrict__ cnt,
+                                                            double *__restrict__ sum)
+{
+    const int32_t W = bs->W, H = bs->H, D = bs->D;
+    const float in_min = bs->in_min;
+    const int64_t n = (int64_t)g.fw * g.fh;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t y = (int32_t)(i / g.fw), x = (int32_t)(i - (int64_t)y * g.fw);
+        const int32_t sx = (int32_t)xadd(xdiv((float)x, g.s_sa), 0.5f) + 3;
+        const int32_t sy = (int32_t)xadd(xdiv((float)y, g.s_sa), 0.5f) + 3;
+        int32_t sz = (int32_t)xadd(xdiv(xsub(logi[i], in_min), 0.4f), 0.5f) + 3;
+        sz = sz < 0 ? 0 : (sz > D - 1 ? D - 1 : sz);
+        if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;   // never: the grid spans the frame
+        const size_t c = (size_t)sx + (size_t)W * ((size_t)sy + (size_t)H * (size_t)sz);
+        atomicAdd(cnt + c, 1.0);
+        atomicAdd(sum + c, (double)logi[i]);
+    }
+}
+
+// The Gaussian of one cell with the reference's wrap-around coordinates,
+// in binary32 (camera.cc:1678-1697).
+__global__ void __launch_bounds__(kToneThreads) k_bil_kernel(const BilState *bs, double *__restrict__ kre,
+                                                             double *__restrict__ kim)
+{
+    const int32_t W = bs->W, H = bs->H, D = bs->D;
+    const int64_t N = (int64_t)W * H * D;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t x = (int32_t)(i % W), y = (int32_t)((i / W) % H), z = (int32_t)(i / ((int64_t)W * H));
+        const float X = xsub((float)x, (x > (W >> 1)) ? (float)W : 0.0f);
+        const float Y = xsub((float)y, (y > (H >> 1)) ? (float)H : 0.0f);
+        const float Z = xsub((float)z, (z > (D >> 1)) ? (float)D : 0.0f);
+        const float rr = xadd(xdiv(xadd(xmul(X, X), xmul(Y, Y)), 1.0f), xdiv(xmul(Z, Z), 1.0f));
+        kre[i] = (double)exp_f(xmul(-rr, 0.5f));
+        kim[i] = 0.0;
+    }
+}
+
+// One discrete Fourier transform (sign -1 forward, +1 backward, not
+// normalised) along axis a of nch complex channels (channel c at offset
+// c * cstride) of dims (W, H, D), row-major with D fastest.
+__global__ void __launch_bounds__(kToneThreads) k_bil_dft(const double *__restrict__ ire, const double *__restrict__ iim,
+                                                          double *__restrict__ ore, double *__restrict__ oim,
+                                                          const BilState *bs, const double *__restrict__ tw, int a,
+                                                          double sign, int nch, int64_t cstride)
+{
+    const int32_t W = bs->W, H = bs->H, D = bs->D;
+    const int64_t N = (int64_t)W * H * D;
+    const int32_t m = a == 0 ? W : (a == 1 ? H : D);
+    const int64_t stride = a == 0 ? (int64_t)H * D : (a == 1 ? (int64_t)D : 1);
+    const double *twa = tw + 2 * (size_t)a * kBilMaxAxis;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < (int64_t)nch * N;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = g / N, i = g - c * N;
+        const int32_t k = (int32_t)((i / stride) % m);
+        const int64_t base = c * cstride + i - (int64_t)k * stride;
+        double sr = 0.0, si = 0.0;
+        int32_t t = 0;   // j * k mod m
+        for (int32_t j = 0; j < m; ++j) {
+            const double vr = ire[base + (int64_t)j * stride], vi = iim[base + (int64_t)j * stride];
+            const double cr = twa[2 * t], ci = sign * twa[2 * t + 1];
+            sr = fma(vr, cr, fma(-vi, ci, sr));
+            si = fma(vr, ci, fma(vi, cr, si));
+            t += k;
+            if (t >= m) t -= m;
+        }
+        ore[c * cstride + i] = sr;
+        oim[c * cstride + i] = si;
+    }
+}
+
+// The product of the channels' spectra with the kernel's, over N (the
+// inverse transform is not normalised).
+__global__ void __launch_bounds__(kToneThreads) k_bil_mul(const double *__restrict__ are, const double *__restrict__ aim,
+                                                          const double *__restrict__ kre,
+                                                          const double *__restrict__ kim, double *__restrict__ ore,
+                                                          double *__restrict__ oim, const BilState *bs, int64_t cstride)
+{
+    const int64_t N = (int64_t)bs->W * bs->H * bs->D;
+    const double inv = 1.0 / (double)N;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < 2 * N; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = g / N, i = g - c * N;
+        const double ar = are[c * cstride + i], ai = aim[c * cstride + i];
+        ore[c * cstride + i] = (ar * kre[i] - ai * kim[i]) * inv;
+        oim[c * cstride + i] = (ar * kim[i] + ai * kre[i]) * inv;
+    }
+}
+
+// The trilinear slice of the blurred grid at every sample (camera.cc:
+// 1740-1789, binary32 in the reference's order on the grid rounded to
+// binary32) and the range of the result.
+__global__ void __launch_bounds__(kToneThreads) k_bil_slice(const float *__restrict__ logi, BilGeom g,
+                                                            BilState *bs, const double *__restrict__ blur,
+                                                            int64_t cstride, float *__restrict__ res)
+{
+    const int32_t W = bs->W, H = bs->H, D = bs->D;
+    const float in_min = bs->in_min;
+    const int64_t n = (int64_t)g.fw * g.fh;
+    const double *bw = blur, *biw = blur + cstride;
+    uint32_t lo = 0xffffffffu, hi = 0u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t y = (int32_t)(i / g.fw), x = (int32_t)(i - (int64_t)y * g.fw);
+        const float z = xsub(logi[i], in_min);
+        const float xa_ = xadd(xdiv((float)x, g.s_sa), 3.0f);
+        const float ya_ = xadd(xdiv((float)y, g.s_sa), 3.0f);
+        const float za_ = xadd(xdiv(z, 0.4f), 3.0f);
+        const int32_t xi = max(0, min((int32_t)xa_, W - 1)), xx = max(0, min(xi + 1, W - 1));
+        const int32_t yi = max(0, min((int32_t)ya_, H - 1)), yy = max(0, min(yi + 1, H - 1));
+        const int32_t zi = max(0, min((int32_t)za_, D - 1)), zz = max(0, min(zi + 1, D - 1));
+        const float ax = xsub(xa_, (float)xi), ay = xsub(ya_, (float)yi), az = xsub(za_, (float)zi);
+        const float bx = xsub(1.0f, ax), by = xsub(1.0f, ay), bz = xsub(1.0f, az);
+        auto at = [&](const double *a, int32_t X, int32_t Y, int32_t Z) {
+            return (float)a[(size_t)X + (size_t)W * ((size_t)Y + (size_t)H * (size_t)Z)];
+        };
+        auto tri = [&](const double *a) {
+            float s = xmul(xmul(xmul(bx, by), bz), at(a, xi, yi, zi));
+            s = xadd(s, xmul(xmul(xmul(ax, by), bz), at(a, xx, yi, zi)));
+            s = xadd(s, xmul(xmul(xmul(bx, ay), bz), at(a, xi, yy, zi)));
+            s = xadd(s, xmul(xmul(xmul(ax, ay), bz), at(a, xx, yy, zi)));
+            s = xadd(s, xmul(xmul(xmul(bx, by), az), at(a, xi, yi, zz)));
+            s = xadd(s, xmul(xmul(xmul(ax, by), az), at(a, xx, yi, zz)));
+            s = xadd(s, xmul(xmul(xmul(bx, ay), az), at(a, xi, yy, zz)));
+            s = xadd(s, xmul(xmul(xmul(ax, ay), az), at(a, xx, yy, zz)));
+            return s;
+        };
+        const float r = xdiv(tri(biw), tri(bw));
+        res[i] = r;
+        const uint32_t k = order_key(r);
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&bs->rmin, lo);
+        atomicMax(&bs->rmax, hi);
+    }
+}
+
+// The contrast compression (camera.cc:1793-1800): Y = 10^(base * gamma +
+// detail) / 255, gamma = log10(300) / (base range).
+__global__ void __launch_bounds__(kToneThreads) k_bil_scale(const float *__restrict__ logi,
+                                                            const float *__restrict__ res, int64_t n,
+                                                            const BilState *bs, float *__restrict__ bil)
+{
+    const float gamma = xdiv(log10_f(300.0f), xsub(key_float(bs->rmax), key_float(bs->rmin)));
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float r = res[i];
+        const float scaled = pow_f(10.0f, xadd(xmul(r, gamma), xsub(logi[i], r)));
+        bil[i] = xmul(scaled, 1.0f / 255.0f);
+    }
+}
+
 int blocks_for(int64_t n, int sm_count)
 {
     const int64_t b = (n + kToneThreads - 1) / kToneThreads;
@@ -1029,9 +1292,72 @@ size_t tone_scratch_bytes(int64_t n, int64_t blocks)
            (size_t)2 * 2 * 4096 * sizeof(float);   // and their bounds (at most 4096 per axis)
 }
 
-void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t,
+bool bilateral_grid_fits(int32_t fw, int32_t fh)
+{
+    const BilGeom g = bil_geom(fw, fh);
+    return g.W <= kBilMaxAxis && g.H <= kBilMaxAxis && (int64_t)g.W * g.H * kBilMaxDepth <= ((int64_t)1 << 26);
+}
+
+size_t bilateral_scratch_bytes(int32_t fw, int32_t fh)
+{
+    const BilGeom g = bil_geom(fw, fh);
+    const size_t nmax = (size_t)g.W * (size_t)g.H * (size_t)kBilMaxDepth;
+    const size_t n = (size_t)fw * (size_t)fh;
+    // 256-byte alignment of the start and of the doubles
+    return 3 * 256 + 3 * n * sizeof(float) + 12 * nmax * sizeof(double) + 6 * (size_t)kBilMaxAxis * sizeof(double);
+}
+
+static char *align256(char *p) { return (char *)(((uintptr_t)p + 255u) & ~(uintptr_t)255u); }
+
+// The bilateral mode's per-sample luminance into scratch (layout: state |
+// log | base | mapped | kernel re, im | temp re, im | A re, im (2 channels)
+// | B re, im (2 channels) | twiddles); returns the mapped array.
+static const float *launch_bilateral(const float *fimg, int32_t fw, int32_t fh, const ToneView &t, void *scratch,
+                                     int sm_count, cudaStream_t st)
+{
+    const BilGeom g = bil_geom(fw, fh);
+    const int64_t n = (int64_t)fw * fh;
+    const int64_t nmax = (int64_t)g.W * g.H * kBilMaxDepth;
+    char *p = align256((char *)scratch);
+    BilState *bs = (BilState *)p;
+    p += 256;
+    float *logi = (float *)p;
+    float *res = logi + n;
+    float *bil = res + n;
+    double *kre = (double *)align256((char *)(bil + n));
+    double *kim = kre + nmax, *tre = kim + nmax, *tim = tre + nmax;
+    double *are = tim + nmax, *aim = are + 2 * nmax, *bre = aim + 2 * nmax, *bim = bre + 2 * nmax;
+    double *tw = bim + 2 * nmax;
+    const BilState init = {0xffffffffu, 0u, 0xffffffffu, 0u, 0, 0, 0, 0.0f, 0};
+    cudaMemcpyAsync(bs, &init, sizeof(init), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(are, 0, 4 * (size_t)nmax * sizeof(double), st);   // A re and im, both channels
+    const int bn = blocks_for(n, sm_count), bg = blocks_for(2 * nmax, sm_count);
+    k_bil_log<<<bn, kToneThreads, 0, st>>>(fimg, n, t, logi, bs);
+    k_bil_dims<<<1, 256, 0, st>>>(g, bs, tw);
+    k_bil_splat<<<bn, kToneThreads, 0, st>>>(logi, g, bs, are, are + nmax);
+    k_bil_kernel<<<bg, kToneThreads, 0, st>>>(bs, kre, kim);
+    // kernel spectrum: K -> T -> K -> T
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(kre, kim, tre, tim, bs, tw, 0, -1.0, 1, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(tre, tim, kre, kim, bs, tw, 1, -1.0, 1, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(kre, kim, tre, tim, bs, tw, 2, -1.0, 1, nmax);
+    // the two channels' spectra: A -> B -> A -> B
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(are, aim, bre, bim, bs, tw, 0, -1.0, 2, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(bre, bim, are, aim, bs, tw, 1, -1.0, 2, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(are, aim, bre, bim, bs, tw, 2, -1.0, 2, nmax);
+    k_bil_mul<<<bg, kToneThreads, 0, st>>>(bre, bim, tre, tim, are, aim, bs, nmax);
+    // back: A -> B -> A -> B
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(are, aim, bre, bim, bs, tw, 0, +1.0, 2, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(bre, bim, are, aim, bs, tw, 1, +1.0, 2, nmax);
+    k_bil_dft<<<bg, kToneThreads, 0, st>>>(are, aim, bre, bim, bs, tw, 2, +1.0, 2, nmax);
+    k_bil_slice<<<bn, kToneThreads, 0, st>>>(logi, g, bs, bre, nmax, res);
+    k_bil_scale<<<bn, kToneThreads, 0, st>>>(logi, res, n, bs, bil);
+    return bil;
+}
+
+void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, int32_t aa_y, const ToneView &t_in,
                      uint8_t *rgb, ToneAcc *acc, void *scratch, int sm_count, cudaStream_t st)
 {
+    ToneView t = t_in;
     const int64_t n = (int64_t)fw * fh;
     const int32_t ow = fw / aa_x, oh = fh / aa_y;
     // scratch: terms | chunk records | coarse records | redo queue
@@ -1043,6 +1369,8 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
     int32_t *redo = (int32_t *)(crec + ncoarse * 32);
     float *hblocks = (float *)(redo + n);
     cudaMemsetAsync(acc, 0, sizeof(ToneAcc), st);
+    if (t.enabled && t.mode == RT_TONE_GLOBAL_BILATERAL)
+        t.bil = launch_bilateral(fimg, fw, fh, t, (char *)scratch + tone_scratch_bytes(n, 0), sm_count, st);
     if (t.enabled) {
         // candidate binades: |S| <= 39 n (|log10 Y| < 39 for any float Y)
         const int32_t e_hi = (int32_t)std::floor(std::log2(39.0 * (double)n)) + 1;

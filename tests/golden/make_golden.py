@@ -410,12 +410,60 @@ def dist_main():
     print("wrote ref_distributed.npz")
 
 
+def bilateral_cases():
+    """(name, float frame, camera, tone, aa) of the bilateral tone-map
+    fixtures: rendered float frames dimmed so the reference's bilateral
+    mode, which does not subtract the base's maximum, keeps contrast; no
+    pixel at or below the reference's 3.18e-7 luminance floor (the
+    reference reads an unset value there)."""
+    import oracle as O
+    from raptor_gb300 import scenes
+    out = []
+    t, tf = scenes.terrain_scene(size_pow2=128, xres=320, yres=180)
+    tf = dict(tf, camera=dict(tf["camera"], background=(40.0, 60.0, 90.0)))
+    tfimg = O.OracleScene(t).render(tf, want_float=True)["fimg"]
+    out.append(("terrain320", (tfimg * np.float32(0.01)).astype(np.float32), tf["camera"], {"mode": 8}, (1, 1)))
+    out.append(("terrain320-gamma", (tfimg * np.float32(0.01)).astype(np.float32), tf["camera"],
+                {"mode": 8, "gamma": 2.2}, (1, 1)))
+    g, gf = scenes.glass_scene(freq=8, res=96)
+    gfimg = O.OracleScene(g).render(gf, want_float=True)["fimg"]
+    out.append(("glass96-gamma", (gfimg * np.float32(1.0 / 300.0)).astype(np.float32), gf["camera"],
+                {"mode": 8, "gamma": 2.2}, (1, 1)))
+    a, af = scenes.glass_scene(freq=8, res=64)
+    ss = O.supersampled(af, 2, 2)
+    afimg = O.OracleScene(a).render(ss, want_float=True)["fimg"]
+    out.append(("glass64-aa2x2", (afimg * np.float32(1.0 / 300.0)).astype(np.float32), af["camera"],
+                {"mode": 8, "gamma": 2.2, "stretch": True}, (2, 2)))
+    return out
+
+
+def bilateral_main():
+    """ref_bilateral.npz: the reference's bilateral tone mapper
+    (camera::bilateral_filter_tone_map) on fixed float frames, its FFTW
+    calls served by the harness's transforms."""
+    import oracle as O
+    arrays = {}
+    for k, (name, fimg, cam, tone, aa) in enumerate(bilateral_cases()):
+        arrays[f"bil{k}_fimg"] = fimg
+        arrays[f"bil{k}_rgb"] = O.ref_tone_map_image(fimg, cam, tone, aa)
+        arrays[f"bil{k}_args"] = np.frombuffer(json.dumps({"name": name, "camera": cam, "tone": tone,
+                                                           "aa": list(aa)}).encode(), np.uint8)
+        print(f"bilateral {name}: std {arrays[f'bil{k}_rgb'].std():.1f}")
+    np.savez_compressed(os.path.join(HERE, "ref_bilateral.npz"), **arrays)
+    print("wrote ref_bilateral.npz")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("RAPTOR_REF", "/root/reference/RAPTor"))
     ap.add_argument("--soft", action="store_true", help="write only ref_soft.npz (needs a fresh process)")
     ap.add_argument("--dist", action="store_true", help="write only ref_distributed.npz (needs a fresh process)")
+    ap.add_argument("--bilateral", action="store_true", help="write only ref_bilateral.npz")
     a = ap.parse_args()
+    if a.bilateral:
+        import oracle as O
+        O.build()
+        return bilateral_main()
     if a.soft:
         import oracle as O
         O.build()

@@ -879,7 +879,7 @@ def test_tone_map_off_equals_plain_frames(rtlib, ctx):
     for ax, ay in ((2, 2), (3, 2)):
         assert np.array_equal(sc.render_tone_mapped(frame, None, (ax, ay))["rgb"], sc.render_aa(frame, ax, ay)["rgb"])
     with pytest.raises(rtlib.RtError):
-        sc.render_tone_mapped(frame, {"mode": 8})       # the bilateral-filter mapper is not offered
+        sc.render_tone_mapped(frame, {"mode": 10})      # no such tone_mapping_mode_t
     with pytest.raises(rtlib.RtError):
         sc.render_tone_mapped(frame, {"mode": 0, "gamma": -1.0})
     sc.close()
