@@ -250,8 +250,11 @@ __device__ __forceinline__ float map_lum(float g, const ToneView &t, const ToneS
 }
 
 // Yxy -> RGB in 0..255 (camera.cc:2085-2096), then gamma (camera.cc:1470-1497).
+// powed (nullable) is set when a gamma power is evaluated on a value
+// strictly between the clamp bounds (a clamped 0 or 1 gives the same
+// channel in single and double precision).
 template <bool EXACT>
-__device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma)
+__device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma, bool *powed = nullptr)
 {
     const float X = xdiv(xmul(x, Y), y);
     const float Z = xdiv(xmul(xsub(xsub(1.0f, x), y), Y), y);
@@ -269,6 +272,7 @@ __device__ __forceinline__ float3 to_rgb(float x, float Y, float y, float gamma)
             float a = v[i];
             a = (a < 0.0f) ? 0.0f : a;   // std::max(a, 0), then std::min(., 1)
             a = (1.0f < a) ? 1.0f : a;
+            if (powed && ((plain && a > 0.0f && a < 1.0f) || (srgb && a > 0.0031308f && a < 1.0f))) *powed = true;
             if (plain) a = tl_pow<EXACT>(a, inv);
             else if (srgb)
                 a = (a <= 0.0031308f) ? xmul(12.92f, a) : xsub(xmul(1.055f, tl_pow<EXACT>(a, 1.0f / 2.4f)), 0.055f);
@@ -898,13 +902,17 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_range(const float *__rest
 }
 
 // One output pixel: each of its aa_x * aa_y samples through the chain, then
-// clip_image_to_rgb's sum (a_x outer, a_y inner) and division.
+// clip_image_to_rgb's sum (a_x outer, a_y inner) and division.  inexact
+// (nullable) is set when a single-precision library call took part: every
+// mode's luminance map but the bilateral one (precomputed exactly), or a
+// gamma power inside (0, 1).
 template <bool EXACT>
 __device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int32_t fw, int32_t aa_x, int32_t aa_y,
                                              int32_t ox, int32_t oy, const ToneView &t, const ToneScalars &k,
                                              const ToneHist &hh, bool stretch, float offset, float scale,
-                                             float samples)
+                                             float samples, bool *inexact = nullptr)
 {
+    if (inexact) *inexact = t.enabled && t.mode != RT_TONE_GLOBAL_BILATERAL;
     float3 a = make_float3(0.0f, 0.0f, 0.0f);
     for (int32_t ax = 0; ax < aa_x; ++ax)
         for (int32_t ay = 0; ay < aa_y; ++ay) {
@@ -914,7 +922,7 @@ __device__ __forceinline__ float3 tone_pixel(const float *__restrict__ fimg, int
                 const Yxy p = to_yxy<EXACT>(c, t);
                 float g = (t.mode == RT_TONE_GLOBAL_BILATERAL) ? t.bil[s] : map_lum<EXACT>(p.Y, t, k, hh);
                 if (stretch) g = xmul(xadd(g, offset), scale);
-                c = to_rgb<EXACT>(p.x, g, p.y, t.gamma);
+                c = to_rgb<EXACT>(p.x, g, p.y, t.gamma, inexact);
             }
             a = xadd3(a, c);
         }
@@ -978,9 +986,10 @@ __global__ void __launch_bounds__(kToneThreads) k_tone_final(const float *__rest
         bool queue = false;
         if (o < npix) {
             const int32_t oy = (int32_t)(o / ow), ox = (int32_t)(o - (int64_t)oy * ow);
-            const float3 v =
-                tone_pixel<false>(fimg, fw, aa_x, aa_y, ox, oy, t, k, acc->h, sr.on, sr.offset, sr.scale, samples);
-            queue = t.enabled && (near_integer(v.x) || near_integer(v.y) || near_integer(v.z));
+            bool inexact = false;
+            const float3 v = tone_pixel<false>(fimg, fw, aa_x, aa_y, ox, oy, t, k, acc->h, sr.on, sr.offset, sr.scale,
+                                               samples, &inexact);
+            queue = inexact && (near_integer(v.x) || near_integer(v.y) || near_integer(v.z));
             if (!queue) store_pixel(rgb, o, v);
         }
         const uint32_t b = __ballot_sync(0xffffffffu, queue);
@@ -1062,7 +1071,7 @@ __global__ void __launch_bounds__(kToneThreads) k_bil_log(const float *__restric
         const Yxy p = to_yxy<true>(make_float3(fimg[3 * i], fimg[3 * i + 1], fimg[3 * i + 2]), t);
         float l = 0.0f;
         if (p.Y > 3.18e-7f) {
-            l = log10_f(p.Y);
+            if (!log10_ff(p.Y, l)) l = log10_f(p.Y);   // correctly rounded either way
             const uint32_t k = order_key(l);
             lo = min(lo, k);
             hi = max(hi, k);
@@ -1115,9 +1124,12 @@ __global__ void k_bil_dims(BilGeom g, BilState *bs, double *__restrict__ tw)
     }
 }
 
-// The splat: count and log-luminance sum per cell (sample order as the
-// reference's loops, sums in double).  The cell of a sample outside the
-// grid's depth (a floor sample's 0 beyond the range) is clamped into it.
+// The splat: count and log-luminance sum per cell (sums in double).  A
+// cell spans about (0.02 min(w, h))^2 samples, so neighbouring lanes mostly
+// share one: each run of lanes with the same cell sums first (one atomic
+// per run).
+// The cell of a sample outside the grid's depth (a floor sample's 0 beyond
+// the range) is clamped into it.
 __global__ void __launch_bounds__(kToneThreads) k_bil_splat(const float *__restrict__ logi, BilGeom g,
                                                             const BilState *bs, double *__restrict__ cnt,
                                                             double *__restrict__ sum)
@@ -1125,16 +1137,41 @@ __global__ void __launch_bounds__(kToneThreads) k_bil_splat(const float *__restr
     const int32_t W = bs->W, H = bs->H, D = bs->D;
     const float in_min = bs->in_min;
     const int64_t n = (int64_t)g.fw * g.fh;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t y = (int32_t)(i / g.fw), x = (int32_t)(i - (int64_t)y * g.fw);
-        const int32_t sx = (int32_t)xadd(xdiv((float)x, g.s_sa), 0.5f) + 3;
-        const int32_t sy = (int32_t)xadd(xdiv((float)y, g.s_sa), 0.5f) + 3;
-        int32_t sz = (int32_t)xadd(xdiv(xsub(logi[i], in_min), 0.4f), 0.5f) + 3;
-        sz = sz < 0 ? 0 : (sz > D - 1 ? D - 1 : sz);
-        if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;   // never: the grid spans the frame
-        const size_t c = (size_t)sx + (size_t)W * ((size_t)sy + (size_t)H * (size_t)sz);
-        atomicAdd(cnt + c, 1.0);
-        atomicAdd(sum + c, (double)logi[i]);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t steps = (n + stride - 1) / stride;   // uniform trip count: whole warps match
+    const int lane = threadIdx.x & 31;
+    for (int64_t it = 0; it < steps; ++it) {
+        const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+        int64_t c = -1;
+        double l = 0.0;
+        if (i < n) {
+            const int32_t y = (int32_t)(i / g.fw), x = (int32_t)(i - (int64_t)y * g.fw);
+            const int32_t sx = (int32_t)xadd(xdiv((float)x, g.s_sa), 0.5f) + 3;
+            const int32_t sy = (int32_t)xadd(xdiv((float)y, g.s_sa), 0.5f) + 3;
+            int32_t sz = (int32_t)xadd(xdiv(xsub(logi[i], in_min), 0.4f), 0.5f) + 3;
+            sz = sz < 0 ? 0 : (sz > D - 1 ? D - 1 : sz);
+            if (sx >= 0 && sx < W && sy >= 0 && sy < H)   // always: the grid spans the frame
+                c = (int64_t)sx + (int64_t)W * ((int64_t)sy + (int64_t)H * (int64_t)sz);
+            l = (double)logi[i];
+        }
+        // runs of equal cells over consecutive lanes: each run's first lane
+        // sums it (segmented tree reduction) and adds it to the cell
+        const int64_t prev = __shfl_up_sync(0xffffffffu, c, 1);
+        const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0 || prev != c);
+        const int run = __popc(heads & ((2u << lane) - 1u));
+        double gc = (c >= 0) ? 1.0 : 0.0, gs = l;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double vc = __shfl_down_sync(0xffffffffu, gc, o), vs = __shfl_down_sync(0xffffffffu, gs, o);
+            const int r = __shfl_down_sync(0xffffffffu, run, o);
+            if (lane + o < 32 && r == run) {
+                gc += vc;
+                gs += vs;
+            }
+        }
+        if (((heads >> lane) & 1u) && c >= 0) {
+            atomicAdd(cnt + c, gc);
+            atomicAdd(sum + c, gs);
+        }
     }
 }
 
@@ -1268,7 +1305,10 @@ __global__ void __launch_bounds__(kToneThreads) k_bil_scale(const float *__restr
     const float gamma = xdiv(log10_f(300.0f), xsub(key_float(bs->rmax), key_float(bs->rmin)));
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float r = res[i];
-        const float scaled = pow_f(10.0f, xadd(xmul(r, gamma), xsub(logi[i], r)));
+        // powf(10, e) as 2^(e log2 10) in double, rounded once: the
+        // product's relative error (2^-53) is far below a float's ulp
+        const float e = xadd(xmul(r, gamma), xsub(logi[i], r));
+        const float scaled = (float)exp2((double)e * 3.321928094887362347870319429489);
         bil[i] = xmul(scaled, 1.0f / 255.0f);
     }
 }
@@ -1369,9 +1409,11 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
     int32_t *redo = (int32_t *)(crec + ncoarse * 32);
     float *hblocks = (float *)(redo + n);
     cudaMemsetAsync(acc, 0, sizeof(ToneAcc), st);
+    // the stretch range starts empty (k_tone_sum sets it too, for the other modes)
+    cudaMemsetAsync(&acc->gmin, 0xff, sizeof(uint32_t), st);
     if (t.enabled && t.mode == RT_TONE_GLOBAL_BILATERAL)
         t.bil = launch_bilateral(fimg, fw, fh, t, (char *)scratch + tone_scratch_bytes(n, 0), sm_count, st);
-    if (t.enabled) {
+    if (t.enabled && t.mode != RT_TONE_GLOBAL_BILATERAL) {
         // candidate binades: |S| <= 39 n (|log10 Y| < 39 for any float Y)
         const int32_t e_hi = (int32_t)std::floor(std::log2(39.0 * (double)n)) + 1;
         const int32_t e_lo = e_hi - 31;
@@ -1385,8 +1427,8 @@ void launch_tone_map(const float *fimg, int32_t fw, int32_t fh, int32_t aa_x, in
             k_hist_blocks<<<blocks_for(nb, sm_count), kToneThreads, 0, st>>>(fimg, fw, fh, t, bx, by, hblocks);
             k_hist_main<<<1, 128, 0, st>>>(hblocks, t, acc);
         }
-        if (t.stretch) k_tone_range<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(fimg, n, t, acc);
     }
+    if (t.enabled && t.stretch) k_tone_range<<<blocks_for(n, sm_count), kToneThreads, 0, st>>>(fimg, n, t, acc);
     k_tone_final<<<blocks_for((int64_t)ow * oh, sm_count), kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, oh, t, acc,
                                                                                   redo, rgb);
     if (t.enabled) k_tone_fix<<<sm_count, kToneThreads, 0, st>>>(fimg, fw, aa_x, aa_y, ow, t, acc, redo, rgb);
