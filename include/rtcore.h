@@ -185,13 +185,14 @@ rt_status rt_ctx_synchronize(rt_context *ctx);
 #define RT_ISECT_REFERENCE 0
 #define RT_ISECT_WATERTIGHT 1
 /* RT_OPT_BUILDER: the binary tree that rt_bvh_build / rt_bvh_build_batched
- * collapse into 8-wide nodes.  RT_BUILDER_PLOC (default) -- bottom-up
- * locally-ordered clustering of mutual nearest neighbours over the Morton
- * order (Meister and Bittner 2018): lower surface area, fewer nodes per
- * ray; RT_BUILDER_LBVH -- the Morton radix tree (Karras 2012): faster to
- * build; RT_BUILDER_HPLOC -- the same clustering run inside the radix tree
- * bottom-up in one launch (H-PLOC, Benthin et al. 2024); batched builds
- * use RT_BUILDER_PLOC for it.  Hits do not depend on the tree. */
+ * collapse into 8-wide nodes.  RT_BUILDER_HPLOC (default) -- clustering of
+ * mutual nearest neighbours (surface area of the merged box) run bottom-up
+ * inside the Morton radix tree in one launch (H-PLOC, Benthin et al. 2024;
+ * batched builds use RT_BUILDER_PLOC for it); RT_BUILDER_PLOC -- the same
+ * clustering by global iterations over the Morton order (Meister and
+ * Bittner 2018); RT_BUILDER_LBVH -- the Morton radix tree itself (Karras
+ * 2012): fastest to build, ~10 % more nodes per ray.  Hits do not depend on
+ * the tree. */
 #define RT_OPT_BUILDER 4
 #define RT_BUILDER_LBVH 0
 #define RT_BUILDER_PLOC 1

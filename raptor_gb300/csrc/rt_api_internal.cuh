@@ -54,7 +54,7 @@ struct rt_context {
     bool count_fetches = false;
     int render_kernel = RT_KERNEL_PIXEL;
     int isect = RT_ISECT_REFERENCE;
-    int builder = RT_BUILDER_PLOC;
+    int builder = RT_BUILDER_HPLOC;
     int morton_bits = 0;                   // RT_OPT_MORTON_BITS
     rtc::SoftState *soft = nullptr;        // rt_render_soft_shadows state
 };

@@ -833,6 +833,7 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
 // a parent the warp loads the two children's refs one per lane (at most
 // kHplocKeep each) and, when there are more than kHplocKeep of them (or the
 // parent is the root), their boxes, and merges mutual nearest neighbours
+// among the RT_HPLOC_RADIUS clusters on either side in Morton order
 // (smallest merged surface area, lowest index on ties -- the smallest such
 // pair is always mutual) until kHplocKeep remain (one at the root); then it
 // stores the refs at the start of the parent's range.  Warps handle their
@@ -843,6 +844,12 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
 // counts and surface-area tables as the PLOC kernels write them.
 constexpr int kHplocKeep = 16;
 constexpr int kHplocBlock = 256;
+// neighbours searched on either side in Morton order (>= 31: all of them);
+// 3 measured best: terrain 2M builds in 1.72 ms (all: 2.24) with the same
+// frame time, the 4M instances in 2.97 ms (all: 4.10) and render faster
+#ifndef RT_HPLOC_RADIUS
+#define RT_HPLOC_RADIUS 3
+#endif
 constexpr unsigned long long kHplocEmpty = ~0ull;
 
 // Is the pair (a, a + 1) of sorted keys closer (longer common prefix) than
@@ -948,11 +955,23 @@ __global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t
                     // nearest neighbour among the cnt clusters
                     float best = __int_as_float(0x7f800000);
                     int bk = (int)lane;
+#if RT_HPLOC_RADIUS >= 31
                     for (int k = 0; k < cnt; ++k) {
                         const float ox = __shfl_sync(0xffffffffu, c0.x, k), oy = __shfl_sync(0xffffffffu, c0.y, k);
                         const float oz = __shfl_sync(0xffffffffu, c0.z, k);
                         const float px = __shfl_sync(0xffffffffu, c1.x, k), py = __shfl_sync(0xffffffffu, c1.y, k);
                         const float pz = __shfl_sync(0xffffffffu, c1.z, k);
+#else
+                    // candidates lane - R .. lane + R, visited in increasing index order
+                    for (int d = -RT_HPLOC_RADIUS; d <= RT_HPLOC_RADIUS; ++d) {
+                        const int src = ((int)lane + d) & 31;
+                        const int k = (int)lane + d;
+                        const float ox = __shfl_sync(0xffffffffu, c0.x, src), oy = __shfl_sync(0xffffffffu, c0.y, src);
+                        const float oz = __shfl_sync(0xffffffffu, c0.z, src);
+                        const float px = __shfl_sync(0xffffffffu, c1.x, src), py = __shfl_sync(0xffffffffu, c1.y, src);
+                        const float pz = __shfl_sync(0xffffffffu, c1.z, src);
+                        if (k < 0 || k >= cnt) continue;
+#endif
                         if (valid && k != (int)lane) {
                             const float dx = fmaxf(c1.x, px) - fminf(c0.x, ox);
                             const float dy = fmaxf(c1.y, py) - fminf(c0.y, oy);
