@@ -1074,7 +1074,7 @@ rt_status check_shapes(const rt_scene *s, const rt_light *lights, int32_t nlight
             return sfail(RT_ERR_INVALID_ARG, (w + ": light radius must be finite and >= 0").c_str());
         if (sh.ntris < 0 || (sh.ntris > 0 && !sh.tris))
             return sfail(RT_ERR_INVALID_ARG, (w + ": bad triangle list of a light").c_str());
-        if (sh.ntris > 0 && (sh.radius != 0.0f || lights[i].kind == RT_LIGHT_DIRECTIONAL))
+        if (sh.ntris > 0 && (sh.radius != 0.0f || (lights[i].kind & 0xff) == RT_LIGHT_DIRECTIONAL))
             return sfail(RT_ERR_INVALID_ARG,
                          (w + ": a triangle-defined light is a point or spot light of radius 0").c_str());
         for (int32_t j = 0; j < sh.ntris; ++j)

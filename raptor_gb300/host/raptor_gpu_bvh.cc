@@ -62,6 +62,8 @@ RAPTOR_GPU_MEMBER(light_n, light, const point_t<>, n)
 RAPTOR_GPU_MEMBER(light_d, light, const float, d)
 RAPTOR_GPU_MEMBER(light_s_a, light, const float, s_a)
 RAPTOR_GPU_MEMBER(light_s_b, light, const float, s_b)
+RAPTOR_GPU_MEMBER(light_r, light, const float, r)
+RAPTOR_GPU_MEMBER(light_t, light, const std::vector<int> *const, t)
 // triangle (triangle.h:100-112)
 RAPTOR_GPU_MEMBER(tri_m, triangle, std::int64_t, m)
 RAPTOR_GPU_MEMBER(tri_vnt, triangle, point_t<> *, vnt)
@@ -300,6 +302,18 @@ void gpu_bvh::refit(const primitive_store &prims)
     check(rt_scene_refit_vertices(_scene, verts.data(), 3 * prims.size(), nullptr));
 }
 
+int64_t &ray_tracer_gpu_stream_position()
+{
+    static int64_t pos = 0;
+    return pos;
+}
+
+uint64_t &ray_tracer_gpu_pixel_seed()
+{
+    static uint64_t seed = 0;
+    return seed;
+}
+
 void ray_tracer_gpu(const ssd *const sub_division, const light_list &lights, const primitive_store &everything,
                     camera &c)
 {
@@ -318,8 +332,61 @@ void ray_tracer_gpu(const ssd *const sub_division, const light_list &lights, con
     for (const material *m : accel->materials()) mats.push_back(describe(m));
     const size_t nsamples = (size_t)cam.xres * (size_t)cam.yres;
     std::vector<float> image(3 * nsamples);
-    check(rt_render_image(accel->scene(), &cam, ls.data(), (int32_t)ls.size(), mats.data(), (int32_t)mats.size(),
-                          image.data(), nullptr));
+    // the compile-time sampling of the build this is compiled into
+    // (common.h:34-44): SOFT_SHADOW shadow rays per light, DIFFUSE_REFLECTIONS
+    // rays per diffuse reflection
+#ifdef SOFT_SHADOW
+    const int32_t soft = (int32_t)(SOFT_SHADOW);
+#else
+    const int32_t soft = 1;
+#endif
+#ifdef DIFFUSE_REFLECTIONS
+    const int32_t diffuse = (int32_t)(DIFFUSE_REFLECTIONS);
+#else
+    const int32_t diffuse = 0;
+#endif
+    if (soft > 1 || diffuse > 0)
+    {
+        // lights' extents: the radius of a spherical light, the triangles of
+        // a triangle-defined one (light.h:17-29); a directional light has none
+        std::vector<rt_light_shape> shapes(ls.size());
+        std::vector<std::vector<int32_t>> tris(ls.size());
+        size_t i = 0;
+        for (const light &l : lights)
+        {
+            shapes[i].radius = field(l, light_r{});
+            shapes[i].ntris = 0;
+            shapes[i].tris = nullptr;
+            const std::vector<int> *t = field(l, light_t{});
+            if (t && !t->empty() && (ls[i].kind & 0xff) != RT_LIGHT_DIRECTIONAL)
+            {
+                tris[i].assign(t->begin(), t->end());
+                shapes[i].ntris = (int32_t)tris[i].size();
+                shapes[i].tris = tris[i].data();
+            }
+            ++i;
+        }
+        bool spread = false;
+        for (const rt_material &m : mats)
+            spread = spread || (diffuse > 0 && ((m.rf > 0.0f && m.rfd != 0.0f) || (m.tran > 0.0f && m.td != 0.0f)));
+        rt_sampling smp;
+        smp.soft_samples = soft;
+        smp.diffuse_samples = diffuse;
+        smp.stream = spread ? RT_STREAM_PIXEL : RT_STREAM_REFERENCE;
+        smp.reserved = 0;
+        smp.stream_offset = ray_tracer_gpu_stream_position();
+        smp.seed = ray_tracer_gpu_pixel_seed();
+        int64_t end = 0;
+        check(rt_render_distributed(accel->scene(), &cam, ls.data(), (int32_t)ls.size(), shapes.data(), mats.data(),
+                                    (int32_t)mats.size(), &smp, nullptr, image.data(), &end, nullptr));
+        if (spread) ++ray_tracer_gpu_pixel_seed();
+        else ray_tracer_gpu_stream_position() = end;
+    }
+    else
+    {
+        check(rt_render_image(accel->scene(), &cam, ls.data(), (int32_t)ls.size(), mats.data(), (int32_t)mats.size(),
+                              image.data(), nullptr));
+    }
     // camera::set_pixel for every ray of the grid, as ray_trace_one_pixel does
     for (int32_t y = 0; y < cam.yres; ++y)
         for (int32_t x = 0; x < cam.xres; ++x)

@@ -37,10 +37,20 @@
 //  - the GPU path shades coloured_mapper_shader (no texture mappers, or a
 //    kd mapper that returns the triangle's per-vertex attribute x 255) and
 //    phong_shader without reflection or refraction, up to RT_MAX_MATERIALS
-//    distinct materials, point, directional and spot lights, a constant
-//    background and a pinhole camera; anything else (sky boxes, depth of
-//    field, other texture mappers, diffuse reflection or transmission)
-//    throws std::invalid_argument naming it.
+//    distinct materials, point, directional, spot, spherical and
+//    triangle-defined lights, a constant background and a pinhole camera;
+//    anything else (sky boxes, depth of field, other texture mappers)
+//    throws std::invalid_argument naming it;
+//  - in a build with SOFT_SHADOW (and DIFFUSE_REFLECTIONS) defined, as the
+//    reference's build defines them, frames are rendered as that build
+//    renders them (rt_render_distributed): soft shadows draw the
+//    reference's random stream from ray_tracer_gpu_stream_position(),
+//    which starts at 0 (a fresh program) and moves on by each frame's
+//    draws -- a caller that also draws from gen_random_mersenne_twister
+//    itself moves it as well; frames with diffuse spreads draw per-pixel
+//    streams keyed by ray_tracer_gpu_pixel_seed(), which goes up by one
+//    per frame (the reference's single stream cannot be replayed in
+//    parallel through diffuse rays).
 #pragma once
 
 #include <cstdint>
@@ -153,4 +163,10 @@ class gpu_bvh : public ssd
 // gpu_bvh built from `everything` for this call.
 void ray_tracer_gpu(const ssd *const sub_division, const light_list &lights, const primitive_store &everything,
                     camera &c);
+
+// SOFT_SHADOW builds: numbers of the reference's random stream drawn so far
+// (the position the next frame's soft shadows start from).
+int64_t &ray_tracer_gpu_stream_position();
+// DIFFUSE_REFLECTIONS builds: the key of the next frame's per-pixel streams.
+uint64_t &ray_tracer_gpu_pixel_seed();
 }  // namespace raptor_raytracer

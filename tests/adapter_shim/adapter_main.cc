@@ -62,6 +62,8 @@ int main(int argc, char **argv)
     const std::vector<float> mdesc = rd.take<float>(16 * (size_t)nmats);
     const std::vector<float> ldesc = rd.take<float>(16 * (size_t)nlights);
     const std::vector<float> rays = rd.take<float>(7 * (size_t)nrays);
+    const int nlt = rd.take<int32_t>(1)[0];
+    const std::vector<int32_t> light_tris = rd.take<int32_t>((size_t)nlt);
     fclose(in);
 
     vertex_colour_mapper mapper;
@@ -71,7 +73,7 @@ int main(int argc, char **argv)
         const float *m = &mdesc[16 * (size_t)i];
         const ext_colour_t ka(m[1], m[2], m[3]), kd(m[4], m[5], m[6]), ks(m[7], m[8], m[9]);
         if (m[0] == 0.0f)
-            mats.emplace_back(new coloured_mapper_shader(ka, kd, ks, m[10], m[11], m[12], m[13], 0.0f, 0.0f, nullptr,
+            mats.emplace_back(new coloured_mapper_shader(ka, kd, ks, m[10], m[11], m[12], m[13], 0.0f, m[15], nullptr,
                                                          m[14] != 0.0f ? &mapper : nullptr));
         else
             mats.emplace_back(new phong_shader(ka, kd, ks, m[10]));
@@ -90,15 +92,28 @@ int main(int argc, char **argv)
                            point_t<>(t[6], t[7], t[8]), tri_light[i] != 0, has_normals ? vn : nullptr,
                            has_attr ? vt : nullptr);
     }
+    // kind 0 spherical (radius l[13]), 1 directional, 2 spot (radius l[13]),
+    // 3 defined by l[14] triangles of the store (the next ones of light_tris)
     light_list lights;
+    std::vector<std::vector<int>> tri_lists;
+    tri_lists.reserve((size_t)nlights);
+    size_t lt = 0;
     for (int i = 0; i < nlights; ++i)
     {
         const float *l = &ldesc[16 * (size_t)i];
         const ext_colour_t rgb(l[1], l[2], l[3]);
         const point_t<> pos(l[4], l[5], l[6]), dir(l[7], l[8], l[9]);
-        if (l[0] == 0.0f) lights.emplace_back(rgb, pos, l[10], 0.0f);
+        if (l[0] == 0.0f) lights.emplace_back(rgb, pos, l[10], l[13]);
         else if (l[0] == 1.0f) lights.emplace_back(rgb, dir, l[10]);
-        else lights.emplace_back(rgb, pos, dir, l[10], l[11], l[12], 0.0f);
+        else if (l[0] == 2.0f) lights.emplace_back(rgb, pos, dir, l[10], l[11], l[12], l[13]);
+        else
+        {
+            const size_t k = (size_t)l[14];
+            if (lt + k > light_tris.size()) return 6;
+            tri_lists.emplace_back(light_tris.begin() + (long)lt, light_tris.begin() + (long)(lt + k));
+            lt += k;
+            lights.emplace_back(&store, rgb, pos, l[10], &tri_lists.back());
+        }
     }
     camera c(point_t<>(cam[0], cam[1], cam[2]), point_t<>(cam[3], cam[4], cam[5]), point_t<>(cam[6], cam[7], cam[8]),
              point_t<>(cam[9], cam[10], cam[11]), ext_colour_t(cam[12], cam[13], cam[14]), cam[15], cam[16], cam[17],

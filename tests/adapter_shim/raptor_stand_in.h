@@ -220,6 +220,10 @@ class light
         light(const ext_colour_t &rgb, const point_t<> &n, const float d)
             : e(nullptr), t(nullptr), rgb(rgb.r / 255.0f, rgb.g / 255.0f, rgb.b / 255.0f), c(), n(n), r(0.0f), d(d),
               s_a(0.0f), s_b(0.0f) {}
+        light(const primitive_store *const e, const ext_colour_t &rgb, const point_t<> &c, const float d,
+              const std::vector<int> *const t)
+            : e(e), t(t), rgb(rgb.r / 255.0f, rgb.g / 255.0f, rgb.b / 255.0f), c(c), n(2.0f, 2.0f, 2.0f), r(0.0f),
+              d(d), s_a(0.0f), s_b(0.0f) {}
         const point_t<> &get_centre() const { return c; }
     private :
         const primitive_store *const e;

@@ -23,18 +23,24 @@ pytestmark = pytest.mark.gpu
 NO_VERTEX_COLOUR = 1
 
 
-@pytest.fixture(scope="module")
-def adapter_exe(rtlib, tmp_path_factory):
+def compile_adapter(tmp_path_factory, defines=()):
+    """adapter_main + raptor_gpu_bvh.cc against the stand-in headers, with
+    the build's defines (e.g. SOFT_SHADOW=16, as a RAPTor build sets it)."""
     from raptor_gb300 import build
     exe = tmp_path_factory.mktemp("adapter") / "adapter_main"
     shim = os.path.join(ROOT, "tests", "adapter_shim")
-    cmd = ["g++", "-std=c++17", "-O2", "-I", shim, "-I", os.path.join(ROOT, "include"), "-I",
-           os.path.join(ROOT, "raptor_gb300", "host"), os.path.join(shim, "adapter_main.cc"),
-           os.path.join(ROOT, "raptor_gb300", "host", "raptor_gpu_bvh.cc"), "-L", build.OUT_DIR, "-lrtcore",
-           f"-Wl,-rpath,{build.OUT_DIR}", "-o", str(exe)]
+    cmd = ["g++", "-std=c++17", "-O2", *[f"-D{d}" for d in defines], "-I", shim, "-I",
+           os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "raptor_gb300", "host"),
+           os.path.join(shim, "adapter_main.cc"), os.path.join(ROOT, "raptor_gb300", "host", "raptor_gpu_bvh.cc"),
+           "-L", build.OUT_DIR, "-lrtcore", f"-Wl,-rpath,{build.OUT_DIR}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     return exe
+
+
+@pytest.fixture(scope="module")
+def adapter_exe(rtlib, tmp_path_factory):
+    return compile_adapter(tmp_path_factory)
 
 
 def run_adapter(exe, tmp_path, scene, frame, materials, mat_of_tri, aa, rays, tmax, kinds):
@@ -58,11 +64,16 @@ def run_adapter(exe, tmp_path, scene, frame, materials, mat_of_tri, aa, rays, tm
         mats[i, 1:4], mats[i, 4:7], mats[i, 7:10] = m["ka"], m["kd"], m["ks"]
         mats[i, 10:14] = [m["ns"], m.get("tran", 0.0), m.get("ri", 1.0), m.get("rf", 0.0)]
         mats[i, 14] = 0.0 if m.get("flags", 0) & NO_VERTEX_COLOUR else 1.0
+        mats[i, 15] = m.get("rfd", 0.0)
     ls = np.zeros((len(lights), 16), np.float32)
+    light_tris = []
     for i, l in enumerate(lights):
-        ls[i, 0] = l["kind"]
+        ls[i, 0] = 3 if l.get("tris") is not None else l["kind"]
         ls[i, 1:4], ls[i, 4:7], ls[i, 7:10] = l["rgb"], l["pos"], l["dir"]
-        ls[i, 10:13] = [l["d"], l.get("s_a", 0.0), l.get("s_b", 0.0)]
+        ls[i, 10:14] = [l["d"], l.get("s_a", 0.0), l.get("s_b", 0.0), l.get("r", 0.0)]
+        if l.get("tris") is not None:
+            ls[i, 14] = len(l["tris"])
+            light_tris.extend(l["tris"])
     flags = scene.get("flags")
     light_tri = np.zeros(nt, np.int32) if flags is None else (np.asarray(flags) & 1).astype(np.int32)
     path = tmp_path / "scene.bin"
@@ -78,6 +89,8 @@ def run_adapter(exe, tmp_path, scene, frame, materials, mat_of_tri, aa, rays, tm
         for a in (np.asarray(mat_of_tri, np.int32), light_tri, mats, ls):
             f.write(a.tobytes())
         f.write(np.concatenate([rays["o"], rays["d"], tmax[:, None]], 1).astype(np.float32).tobytes())
+        f.write(np.int32(len(light_tris)).tobytes())
+        f.write(np.asarray(light_tris, np.int32).tobytes())
     out = tmp_path / "out.bin"
     r = subprocess.run([str(exe), str(path), str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -211,4 +224,64 @@ def test_render_image_is_the_reference_float_frame(rtlib, ctx, oracle, mirror):
     same = rgb["ids"] == ref["ids"]
     exact = (img.view(np.uint32) == ref["fimg"].view(np.uint32)).all(-1)
     assert exact[same].mean() >= 0.999, exact[same].mean()
+    sc.close()
+
+
+def soft_case(name):
+    """The icosphere with a spherical light (radius 0.8), a quad light of two
+    scene triangles and the sun; "mirror": the sphere reflects (rf 0.5);
+    "diffuse": and spreads its reflection (rfd 0.2)."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=8, res=80)
+    scene, quad = scenes.add_area_light(scene, [(-0.9, 2.6, -0.9), (0.9, 2.6, -0.9), (0.9, 2.6, 0.9), (-0.9, 2.6, 0.9)],
+                                        rgb=(255.0, 230.0, 200.0))
+    nt = scene["tris"].shape[0]
+    lights = [dict(frame["lights"][0], r=0.8), quad, scenes.directional_light((-0.4, -0.8, -0.3), rgb=(60.0, 60.0, 70.0))]
+    mat = dict(frame["material"])
+    materials, mat_of_tri = [mat], np.zeros(nt, np.int32)
+    if name in ("mirror", "diffuse"):
+        m1 = dict(mat, rf=0.5, rfd=0.2 if name == "diffuse" else 0.0)
+        materials = [mat, m1]
+        mat_of_tri = (scene["verts"][scene["tris"]][:, :, 1].max(1) > -0.999).astype(np.int32)
+        mat_of_tri[-2:] = 0        # the light's triangles
+    return scene, dict(frame, lights=lights), materials, mat_of_tri
+
+
+@pytest.mark.parametrize("name", ["plain", "mirror"])
+def test_adapter_soft_shadow_build(rtlib, ctx, tmp_path_factory, tmp_path, name):
+    """The adapter compiled as part of a SOFT_SHADOW = 16 build: its frames
+    are rt_render_distributed's with soft = 16 on the reference's stream --
+    the first from position 0 (a fresh program), the second (another ssd)
+    from where the first left it -- bit for bit; spherical, triangle-defined
+    and directional lights, with and without mirror ray trees."""
+    exe = compile_adapter(tmp_path_factory, ["SOFT_SHADOW=16"])
+    scene, frame, materials, mat_of_tri = soft_case(name)
+    rays, tmax = scene_rays(rtlib, scene, 100, seed=5)
+    rgb, rgb2, *_ = run_adapter(exe, tmp_path, scene, frame, materials, mat_of_tri, (1, 1), rays, tmax,
+                                [0] * len(materials))
+    sd = dict(scene, mat_of_tri=mat_of_tri) if len(materials) > 1 else scene
+    sc = rtlib.Scene(ctx, sd)
+    f = dict(frame, materials=materials)
+    a = sc.render_distributed(f, soft=16, offset=0)
+    b = sc.render_distributed(f, soft=16, offset=a["stream_end"])
+    assert np.array_equal(rgb, a["rgb"])
+    assert np.array_equal(rgb2, b["rgb"])
+    assert not np.array_equal(rgb, rgb2)      # the second frame drew new numbers
+    sc.close()
+
+
+def test_adapter_diffuse_build(rtlib, ctx, tmp_path_factory, tmp_path):
+    """The adapter compiled as part of a SOFT_SHADOW = 16,
+    DIFFUSE_REFLECTIONS = 16 build, with a diffuse mirror: per-pixel streams
+    keyed 0 for the first frame and 1 for the second, as
+    rt_render_distributed renders them."""
+    exe = compile_adapter(tmp_path_factory, ["SOFT_SHADOW=16", "DIFFUSE_REFLECTIONS=16"])
+    scene, frame, materials, mat_of_tri = soft_case("diffuse")
+    rays, tmax = scene_rays(rtlib, scene, 100, seed=6)
+    rgb, rgb2, *_ = run_adapter(exe, tmp_path, scene, frame, materials, mat_of_tri, (1, 1), rays, tmax, [0, 0])
+    sc = rtlib.Scene(ctx, dict(scene, mat_of_tri=mat_of_tri))
+    f = dict(frame, materials=materials)
+    for got, seed in ((rgb, 0), (rgb2, 1)):
+        want = sc.render_distributed(f, soft=16, diffuse=16, stream=rtlib.RT_STREAM_PIXEL, seed=seed)["rgb"]
+        assert np.array_equal(got, want), seed
     sc.close()

@@ -62,3 +62,16 @@ def test_adapter_compiles_against_reference_headers(tmp_path):
     src = os.path.join(ROOT, "raptor_gb300", "host", "raptor_gpu_bvh.cc")
     r = subprocess.run(compile_cmd("-c", src, tmp_path), capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF) or shutil.which("g++") is None, reason="reference tree not present")
+def test_adapter_compiles_into_soft_shadow_builds(tmp_path):
+    """raptor_gpu_bvh.cc compiled as a SOFT_SHADOW / DIFFUSE_REFLECTIONS
+    build of the reference compiles it, reading the lights' radius and
+    triangle list (light.h:228-233) for rt_render_distributed."""
+    src = os.path.join(ROOT, "raptor_gb300", "host", "raptor_gpu_bvh.cc")
+    for defines in (["-DSOFT_SHADOW=16"], ["-DSOFT_SHADOW=16", "-DDIFFUSE_REFLECTIONS=16"]):
+        cmd = compile_cmd("-c", src, tmp_path)
+        cmd[2:2] = defines
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, (defines, r.stderr[-3000:])
