@@ -828,25 +828,37 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
 // Morton radix tree bottom-up (Apetrei 2014: the parent of the node covering
 // sorted positions [L, R] sits at whichever boundary split, L - 1 or R, has
 // the longer common key prefix; the second of the two children to arrive
-// goes on, the first stops), carrying its subtree's clusters as binary refs
-// (>= 0 internal node, < 0 leaf ~k) at the start of its range in `cref`.  At
-// a parent the warp loads the two children's refs one per lane (at most
-// kHplocKeep each) and, when there are more than kHplocKeep of them (or the
-// parent is the root), their boxes, and merges mutual nearest neighbours
-// among the RT_HPLOC_RADIUS clusters on either side in Morton order
-// (smallest merged surface area, lowest index on ties -- the smallest such
-// pair is always mutual) until kHplocKeep remain (one at the root); then it
-// stores the refs at the start of the parent's range.  Warps handle their
-// lanes' parents one after another with all 32 lanes.  Stores a subtree
-// leaves for its parent are fenced at the end of every level, before the
-// next 64-bit exchange that tells a parent which child came first; data
-// written in the launch is read through L2.  Single-scene builds; nodes,
-// counts and surface-area tables as the PLOC kernels write them.
+// goes on, the first stops).  A subtree of at most kHplocKeep leaves is its
+// leaves (nothing merged, nothing stored); a larger one is at most
+// kHplocKeep clusters, stored as binary refs (>= 0 internal node, < 0 leaf
+// ~k) at the start of its range in `cref`.  At a parent of more than
+// kHplocKeep leaves (or the root) the warp loads the two children's refs and
+// boxes one per lane and, while more than kHplocKeep remain (one at the
+// root), merges every mutual nearest-neighbour pair among the RT_HPLOC_RADIUS
+// clusters on either side in Morton order (smallest merged surface area,
+// lowest index on ties -- the smallest such pair is always mutual); then it
+// stores the refs at the start of the parent's range.  Warps serve their
+// lanes' parents one after another with all 32 lanes; the node ids of a
+// parent's merges are reserved with one atomic (one more when the last
+// round merges past kHplocKeep).  The stores a level leaves for the parents above are fenced before
+// the next 64-bit exchange that tells a parent which child came first, and
+// read after a fence that follows it (through L2).  Single-scene builds;
+// nodes, counts and surface-area tables as the PLOC kernels write them
+// (an internal node's box also carries its triangle count in .w).
 constexpr int kHplocKeep = 16;
-constexpr int kHplocBlock = 256;
+// One warp per block, 64 registers: a block's resources free as soon as its
+// warp's lanes have all stopped climbing (measured: 4 % faster than 64- and
+// 128-thread blocks, 30 % faster than 256 threads at 75 registers).
+#ifndef RT_HPLOC_BLOCK
+#define RT_HPLOC_BLOCK 32
+#endif
+#ifndef RT_HPLOC_MIN_BLOCKS
+#define RT_HPLOC_MIN_BLOCKS 32
+#endif
+constexpr int kHplocBlock = RT_HPLOC_BLOCK;
 // neighbours searched on either side in Morton order (>= 31: all of them);
-// 3 measured best: terrain 2M builds in 1.72 ms (all: 2.24) with the same
-// frame time, the 4M instances in 2.97 ms (all: 4.10) and render faster
+// 3 measured best: 2 builds 2 % faster but renders the terrain 5 % slower,
+// 4..6 build 3..10 % slower and render no faster (all: 1.3x the build time)
 #ifndef RT_HPLOC_RADIUS
 #define RT_HPLOC_RADIUS 3
 #endif
@@ -865,15 +877,13 @@ __device__ __forceinline__ bool hploc_closer(const uint64_t *__restrict__ keys, 
     return a < b;
 }
 
-__global__ void k_hploc_init(int32_t n, int32_t *__restrict__ cref, unsigned long long *__restrict__ meet)
+__global__ void k_hploc_init(int32_t n, unsigned long long *__restrict__ meet)
 {
-    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        cref[k] = ~k;
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         meet[k] = kHplocEmpty;
-    }
 }
 
-__global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t *__restrict__ keys,
+__global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int32_t n, const uint64_t *__restrict__ keys,
                                                        int32_t *__restrict__ cref,
                                                        unsigned long long *__restrict__ meet, int32_t *state,
                                                        const float4 *__restrict__ llo, const float4 *__restrict__ lhi,
@@ -888,7 +898,7 @@ __global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t
     const uint32_t below = (1u << lane) - 1u;
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int32_t ninternal = n - 1;
-    int32_t L = i, R = i, nc = 1;          // the lane's subtree: range, refs at cref[L .. L + nc)
+    int32_t L = i, R = i, nc = 1;          // the lane's subtree: range and cluster count
     bool active = i < n && n > 1;
     bool bad = false;
     int guard = 0;
@@ -905,7 +915,6 @@ __global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t
             if (other == kHplocEmpty) {
                 active = false;                  // the sibling's lane goes on
             } else {
-                __threadfence();
                 const int32_t far = (int32_t)(other >> 32), sn = (int32_t)(uint32_t)other;
                 if (go_right) {                  // this lane holds the left child [L, split]
                     lpos = L; nl = nc; rpos = split + 1; nr = sn;
@@ -914,139 +923,184 @@ __global__ void __launch_bounds__(kHplocBlock) k_hploc(int32_t n, const uint64_t
                     lpos = far; nl = sn; rpos = L; nr = nc;
                     L = far;
                 }
-                if (L < 0 || R >= n || L > R || nl < 1 || nr < 1 || nl > kHplocKeep || nr > kHplocKeep) {
+                if (L < 0 || R >= n || L > R || nl < 1 || nr < 1 || nl > kHplocKeep || nr > kHplocKeep ||
+                    nl > rpos - lpos || nr > R - rpos + 1) {
                     bad = true;                  // never expected; keeps every access in bounds
                     active = false;
                 } else {
-                    go_on = true;
                     root = (L == 0 && R == n - 1);
+                    if (root || R - L + 1 > kHplocKeep) {
+                        __threadfence();         // the children's stored refs and nodes
+                        go_on = true;
+                    } else {
+                        nc = nl + nr;            // still its leaves
+                    }
                 }
             }
         }
+        __syncwarp();
         // the warp serves each of its lanes' parents in turn
         uint32_t todo = __ballot_sync(0xffffffffu, go_on);
+        const bool stored = todo != 0u;
         while (todo) {
             const int src = __ffs(todo) - 1;
             todo &= todo - 1;
             const int32_t p_l = __shfl_sync(0xffffffffu, lpos, src), p_nl = __shfl_sync(0xffffffffu, nl, src);
             const int32_t p_r = __shfl_sync(0xffffffffu, rpos, src), p_nr = __shfl_sync(0xffffffffu, nr, src);
+            const int32_t p_end = __shfl_sync(0xffffffffu, R, src);
             const bool p_root = __shfl_sync(0xffffffffu, root, src);
             int cnt = p_nl + p_nr;
             bool valid = (int)lane < cnt;
             int32_t ref = 0;
+            float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
             if (valid) {
-                const int32_t g = (int)lane < p_nl ? p_l + (int32_t)lane : p_r + ((int32_t)lane - p_nl);
-                if (g >= 0 && g < n) ref = __ldcg(cref + g);
-                else { bad = true; ref = ~0; }
+                // a child of as many leaves as clusters is its leaves; else its refs are stored
+                const bool in_left = (int)lane < p_nl;
+                const int32_t g = in_left ? p_l + (int32_t)lane : p_r + ((int32_t)lane - p_nl);
+                const bool leaves = in_left ? p_nl == p_r - p_l : p_nr == p_end - p_r + 1;
+                ref = leaves ? ~g : __ldcg(cref + g);
+                if (ref >= ninternal || ref < -n) { bad = true; ref = ~0; }
+                if (ref < 0) {
+                    c0 = __ldg(llo + ~ref);
+                    c1 = __ldg(lhi + ~ref);
+                    c0.w = __int_as_float(1);
+                } else {
+                    c0 = __ldcg(ilo + ref);      // .w: the node's triangle count
+                    c1 = __ldcg(ihi + ref);
+                }
             }
-            if (valid && (ref >= ninternal || ref < -n)) { bad = true; ref = ~0; }
             const int target = p_root ? 1 : kHplocKeep;
-            if (cnt > target) {
-                float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
-                if (valid) {
-                    c0 = ref < 0 ? __ldg(llo + ~ref) : __ldcg(ilo + ref);
-                    c1 = ref < 0 ? __ldg(lhi + ~ref) : __ldcg(ihi + ref);
-                }
-                while (cnt > target) {
-                    if (++guard > 65536) {       // never expected: a mutual pair always merges
-                        bad = true;
-                        break;
-                    }
-                    // nearest neighbour among the cnt clusters
-                    float best = __int_as_float(0x7f800000);
-                    int bk = (int)lane;
-#if RT_HPLOC_RADIUS >= 31
-                    for (int k = 0; k < cnt; ++k) {
-                        const float ox = __shfl_sync(0xffffffffu, c0.x, k), oy = __shfl_sync(0xffffffffu, c0.y, k);
-                        const float oz = __shfl_sync(0xffffffffu, c0.z, k);
-                        const float px = __shfl_sync(0xffffffffu, c1.x, k), py = __shfl_sync(0xffffffffu, c1.y, k);
-                        const float pz = __shfl_sync(0xffffffffu, c1.z, k);
-#else
-                    // candidates lane - R .. lane + R, visited in increasing index order
-                    for (int d = -RT_HPLOC_RADIUS; d <= RT_HPLOC_RADIUS; ++d) {
-                        const int src = ((int)lane + d) & 31;
-                        const int k = (int)lane + d;
-                        const float ox = __shfl_sync(0xffffffffu, c0.x, src), oy = __shfl_sync(0xffffffffu, c0.y, src);
-                        const float oz = __shfl_sync(0xffffffffu, c0.z, src);
-                        const float px = __shfl_sync(0xffffffffu, c1.x, src), py = __shfl_sync(0xffffffffu, c1.y, src);
-                        const float pz = __shfl_sync(0xffffffffu, c1.z, src);
-                        if (k < 0 || k >= cnt) continue;
-#endif
-                        if (valid && k != (int)lane) {
-                            const float dx = fmaxf(c1.x, px) - fminf(c0.x, ox);
-                            const float dy = fmaxf(c1.y, py) - fminf(c0.y, oy);
-                            const float dz = fmaxf(c1.z, pz) - fminf(c0.z, oz);
-                            const float a = dx * dy + dx * dz + dy * dz;
-                            if (a < best) { best = a; bk = k; }
-                        }
-                    }
-                    const int back = __shfl_sync(0xffffffffu, bk, bk);
-                    const bool mutual = valid && bk != (int)lane && back == (int)lane;
-                    const bool make = mutual && (int)lane < bk;
-                    const bool drop = mutual && (int)lane > bk;
-                    const uint32_t mm = __ballot_sync(0xffffffffu, make);
-                    int idb = 0;
-                    if (lane == 0 && mm) idb = atomicAdd(&state[kStBase], __popc(mm));
-                    idb = __shfl_sync(0xffffffffu, idb, 0);
-                    const float4 b0 = make_float4(__shfl_sync(0xffffffffu, c0.x, bk),
-                                                  __shfl_sync(0xffffffffu, c0.y, bk),
-                                                  __shfl_sync(0xffffffffu, c0.z, bk), 0.f);
-                    const float4 b1 = make_float4(__shfl_sync(0xffffffffu, c1.x, bk),
-                                                  __shfl_sync(0xffffffffu, c1.y, bk),
-                                                  __shfl_sync(0xffffffffu, c1.z, bk), 0.f);
-                    const int32_t rb = __shfl_sync(0xffffffffu, ref, bk);
-                    if (make) {
-                        const int32_t id = idb + __popc(mm & below);
-                        if (id >= ninternal) {
-                            bad = true;
-                        } else {
-                            const int32_t l = ref, r = rb;
-                            left[id] = l;
-                            right[id] = r;
-                            if (l < 0) leaf_parent[~l] = id; else parent[l] = id;
-                            if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
-                            const int32_t cntl = l < 0 ? 1 : __ldcg(ncount + l);
-                            const int32_t cntr = r < 0 ? 1 : __ldcg(ncount + r);
-                            __stcg(ncount + id, cntl + cntr);
-                            float sl[8], sr[8];
-                            if (sah) {
-                                sah_child(sah, l, c0, c1, sl);
-                                sah_child(sah, r, b0, b1, sr);
-                            }
-                            c0 = box_min(c0, b0);
-                            c1 = box_max(c1, b1);
-                            if (sah) sah_node(sah, dec, id, half_area(c0, c1), cntl + cntr, sl, sr);
-                            __stcg(ilo + id, make_float4(c0.x, c0.y, c0.z, 0.f));
-                            __stcg(ihi + id, make_float4(c1.x, c1.y, c1.z, 0.f));
-                            ref = id;
-                        }
-                    }
-                    // stable compaction of the kept clusters
-                    const uint32_t km = __ballot_sync(0xffffffffu, valid && !drop);
-                    const int kc = __popc(km);
-                    const int from = (int)lane < kc ? (int)__fns(km, 0, (int)lane + 1) : (int)lane;
-                    c0 = make_float4(__shfl_sync(0xffffffffu, c0.x, from), __shfl_sync(0xffffffffu, c0.y, from),
-                                     __shfl_sync(0xffffffffu, c0.z, from), 0.f);
-                    c1 = make_float4(__shfl_sync(0xffffffffu, c1.x, from), __shfl_sync(0xffffffffu, c1.y, from),
-                                     __shfl_sync(0xffffffffu, c1.z, from), 0.f);
-                    ref = __shfl_sync(0xffffffffu, ref, from);
-                    cnt = kc;
-                    valid = (int)lane < cnt;
-                }
-                if (p_root && lane == 0) {
-                    // the root cluster, where the roots pass looks for it
-                    cl[0] = make_float4(c0.x, c0.y, c0.z, __int_as_float(0));
-                    ch[0] = make_float4(c1.x, c1.y, c1.z, __int_as_float(ref));
-                }
+            int32_t base = 0, extra = 0, made = 0;
+            const int32_t reserved = cnt > target ? cnt - target : 0;
+            if (reserved > 0) {
+                if (lane == 0) base = atomicAdd(&state[kStBase], reserved);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base < 0 || base > ninternal - reserved) { bad = true; cnt = 0; valid = false; }
             }
-            if (valid && p_l + (int32_t)lane < n) __stcg(cref + p_l + (int32_t)lane, ref);
+            while (cnt > target) {
+                if (++guard > 65536) {           // never expected: a mutual pair always merges
+                    bad = true;
+                    break;
+                }
+                // nearest neighbour among the cnt clusters
+                float best = __int_as_float(0x7f800000);
+                int bk = (int)lane;
+#if RT_HPLOC_RADIUS >= 31
+                for (int k = 0; k < cnt; ++k) {
+                    const float ox = __shfl_sync(0xffffffffu, c0.x, k), oy = __shfl_sync(0xffffffffu, c0.y, k);
+                    const float oz = __shfl_sync(0xffffffffu, c0.z, k);
+                    const float px = __shfl_sync(0xffffffffu, c1.x, k), py = __shfl_sync(0xffffffffu, c1.y, k);
+                    const float pz = __shfl_sync(0xffffffffu, c1.z, k);
+                    if (valid && k != (int)lane) {
+                        const float dx = fmaxf(c1.x, px) - fminf(c0.x, ox);
+                        const float dy = fmaxf(c1.y, py) - fminf(c0.y, oy);
+                        const float dz = fmaxf(c1.z, pz) - fminf(c0.z, oz);
+                        const float a = dx * dy + dx * dz + dy * dz;
+                        if (a < best) { best = a; bk = k; }
+                    }
+                }
+#else
+                // the merged area is symmetric: each lane forms it with the
+                // RT_HPLOC_RADIUS lanes above it and takes the ones below it
+                // from them; candidates visited in increasing index order
+                float up[RT_HPLOC_RADIUS];
+#pragma unroll
+                for (int d = 1; d <= RT_HPLOC_RADIUS; ++d) {
+                    const int from = ((int)lane + d) & 31;
+                    const float ox = __shfl_sync(0xffffffffu, c0.x, from), oy = __shfl_sync(0xffffffffu, c0.y, from);
+                    const float oz = __shfl_sync(0xffffffffu, c0.z, from);
+                    const float px = __shfl_sync(0xffffffffu, c1.x, from), py = __shfl_sync(0xffffffffu, c1.y, from);
+                    const float pz = __shfl_sync(0xffffffffu, c1.z, from);
+                    const float dx = fmaxf(c1.x, px) - fminf(c0.x, ox);
+                    const float dy = fmaxf(c1.y, py) - fminf(c0.y, oy);
+                    const float dz = fmaxf(c1.z, pz) - fminf(c0.z, oz);
+                    up[d - 1] = dx * dy + dx * dz + dy * dz;
+                }
+#pragma unroll
+                for (int d = RT_HPLOC_RADIUS; d >= 1; --d) {
+                    const float a = __shfl_sync(0xffffffffu, up[d - 1], ((int)lane - d) & 31);
+                    if (valid && (int)lane - d >= 0 && a < best) { best = a; bk = (int)lane - d; }
+                }
+#pragma unroll
+                for (int d = 1; d <= RT_HPLOC_RADIUS; ++d)
+                    if (valid && (int)lane + d < cnt && up[d - 1] < best) { best = up[d - 1]; bk = (int)lane + d; }
+#endif
+                const int back = __shfl_sync(0xffffffffu, bk, bk);
+                const bool mutual = valid && bk != (int)lane && back == (int)lane;
+                // the lower lane of a pair makes the node
+                const bool make = mutual && (int)lane < bk;
+                const bool drop = mutual && (int)lane > bk;
+                const uint32_t mm = __ballot_sync(0xffffffffu, make);
+                const int over = made + __popc(mm) - reserved;
+                if (over > 0) {                  // merged past kHplocKeep: ids for the rest
+                    int32_t more = 0;
+                    if (lane == 0) more = atomicAdd(&state[kStBase], over);
+                    more = __shfl_sync(0xffffffffu, more, 0);
+                    if (more < 0 || more > ninternal - over) { bad = true; break; }
+                    extra = more - reserved;     // id of merge m >= reserved: extra + m
+                }
+                const float4 b0 = make_float4(__shfl_sync(0xffffffffu, c0.x, bk),
+                                              __shfl_sync(0xffffffffu, c0.y, bk),
+                                              __shfl_sync(0xffffffffu, c0.z, bk),
+                                              __shfl_sync(0xffffffffu, c0.w, bk));
+                const float4 b1 = make_float4(__shfl_sync(0xffffffffu, c1.x, bk),
+                                              __shfl_sync(0xffffffffu, c1.y, bk),
+                                              __shfl_sync(0xffffffffu, c1.z, bk), 0.f);
+                const int32_t rb = __shfl_sync(0xffffffffu, ref, bk);
+                if (make) {
+                    const int32_t m = made + __popc(mm & below);
+                    const int32_t id = m < reserved ? base + m : extra + m;
+                    const int32_t l = ref, r = rb;
+                    left[id] = l;
+                    right[id] = r;
+                    if (l < 0) leaf_parent[~l] = id; else parent[l] = id;
+                    if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
+                    const int32_t count = __float_as_int(c0.w) + __float_as_int(b0.w);
+                    __stcg(ncount + id, count);
+                    float sl[8], sr[8];
+                    if (sah) {
+                        sah_child(sah, l, c0, c1, sl);
+                        sah_child(sah, r, b0, b1, sr);
+                    }
+                    c0 = box_min(c0, b0);
+                    c1 = box_max(c1, b1);
+                    c0.w = __int_as_float(count);
+                    if (sah) sah_node(sah, dec, id, half_area(c0, c1), count, sl, sr);
+                    __stcg(ilo + id, c0);
+                    __stcg(ihi + id, make_float4(c1.x, c1.y, c1.z, 0.f));
+                    ref = id;
+                }
+                made += __popc(mm);
+                // stable compaction of the kept clusters
+                const uint32_t km = __ballot_sync(0xffffffffu, valid && !drop);
+                const int kc = __popc(km);
+                const int from = (int)lane < kc ? (int)__fns(km, 0, (int)lane + 1) : (int)lane;
+                c0 = make_float4(__shfl_sync(0xffffffffu, c0.x, from), __shfl_sync(0xffffffffu, c0.y, from),
+                                 __shfl_sync(0xffffffffu, c0.z, from), __shfl_sync(0xffffffffu, c0.w, from));
+                c1 = make_float4(__shfl_sync(0xffffffffu, c1.x, from), __shfl_sync(0xffffffffu, c1.y, from),
+                                 __shfl_sync(0xffffffffu, c1.z, from), 0.f);
+                ref = __shfl_sync(0xffffffffu, ref, from);
+                if (kc == cnt) {                 // never expected: no mutual pair
+                    bad = true;
+                    break;
+                }
+                cnt = kc;
+                valid = (int)lane < cnt;
+            }
+            if (p_root && lane == 0) {
+                // the root cluster, where the roots pass looks for it
+                cl[0] = make_float4(c0.x, c0.y, c0.z, __int_as_float(0));
+                ch[0] = make_float4(c1.x, c1.y, c1.z, __int_as_float(ref));
+            }
+            if (valid && !p_root) __stcg(cref + p_l + (int32_t)lane, ref);
             if ((int)lane == src) {
                 nc = cnt;
-                if (p_root) active = false;
+                if (p_root || cnt > target) active = false;
             }
         }
         // this level's stores reach the device before any lane's next exchange
-        __threadfence();
+        if (stored) __threadfence();
+        __syncwarp();
     }
     if (bad) atomicExch(&state[kStError], 1);
     if (i == 0) state[kStCount] = 1;
@@ -1113,6 +1167,58 @@ __device__ __forceinline__ void ref_box(const BuildArgs &A, int32_t ref, float4 
 __device__ __forceinline__ int32_t ref_count(const BuildArgs &A, int32_t ref)
 {
     return (ref < 0) ? 1 : A.count[ref];
+}
+
+// The (at most kMaxLeafTris) leaves under a leaf slot's binary ref, left
+// first, in at most one round trip per tree level (such a subtree is at most
+// two levels deep).  False when the subtree holds more leaves than that.
+__device__ __forceinline__ bool leaf_refs(const BuildArgs &A, int32_t ref, int32_t *lv, int &nlv)
+{
+    static_assert(kMaxLeafTris == 3, "leaf_refs walks at most two levels");
+    if (ref < 0) {
+        lv[0] = ref;
+        nlv = 1;
+        return true;
+    }
+    const int32_t a = A.left[ref], b = A.right[ref];
+    int32_t a0 = a, a1 = 0, b0 = b, b1 = 0;
+    if (a >= 0) { a0 = A.left[a]; a1 = A.right[a]; }
+    if (b >= 0) { b0 = A.left[b]; b1 = A.right[b]; }
+    if ((a >= 0 && b >= 0) || a0 >= 0 || b0 >= 0 || (a >= 0 && a1 >= 0) || (b >= 0 && b1 >= 0)) return false;
+    lv[0] = a0;
+    lv[1] = a >= 0 ? a1 : b0;
+    lv[2] = a >= 0 ? b0 : b1;
+    nlv = (a >= 0 || b >= 0) ? 3 : 2;
+    return true;
+}
+
+// The packed triangles of leaves lv[0 .. nlv) at tris[at ..]: the caller's
+// ids, then their indices and flags, then the vertices, each step's loads
+// issued together.
+__device__ __forceinline__ void emit_leaf_tris(const BuildArgs &A, const int32_t *lv, int nlv, int32_t at)
+{
+    int32_t id[kMaxLeafTris];
+    int3 t[kMaxLeafTris];
+    uint32_t fl[kMaxLeafTris];
+#pragma unroll
+    for (int j = 0; j < kMaxLeafTris; ++j)
+        if (j < nlv) id[j] = A.vals[~lv[j]];
+#pragma unroll
+    for (int j = 0; j < kMaxLeafTris; ++j)
+        if (j < nlv) {
+            t[j] = A.idx[id[j]];
+            fl[j] = A.flags ? A.flags[id[j]] : 0u;
+        }
+#pragma unroll
+    for (int j = 0; j < kMaxLeafTris; ++j)
+        if (j < nlv) {
+            const float *v = A.verts;
+            PackedTri P;
+            P.w0 = make_float4(v[3 * t[j].x], v[3 * t[j].x + 1], v[3 * t[j].x + 2], v[3 * t[j].y]);
+            P.w1 = make_float4(v[3 * t[j].y + 1], v[3 * t[j].y + 2], v[3 * t[j].z], v[3 * t[j].z + 1]);
+            P.w2 = make_float4(v[3 * t[j].z + 2], __int_as_float(id[j]), __uint_as_float(fl[j]), 0.f);
+            A.tris[at + j] = P;
+        }
 }
 
 // The children of wide node `node` by the surface-area decisions: its 8
@@ -1286,30 +1392,10 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
         } else {
             const int c = cnt[k];
             W.meta[s] = (uint8_t)((((1u << c) - 1u) << 5) | (uint32_t)tri_off);
-            // the (at most kMaxLeafTris) leaves under this child, left first
-            int32_t todo[kMaxLeafTris];
-            int sp = 0, j = 0;
-            todo[sp++] = ch[k];
-            while (sp > 0 && j < c) {
-                const int32_t r = todo[--sp];
-                if (r >= 0) {
-                    if (sp + 2 > kMaxLeafTris) { atomicExch(&A.counters[3], 1); break; }
-                    todo[sp++] = A.right[r];
-                    todo[sp++] = A.left[r];
-                    continue;
-                }
-                const int32_t id = A.vals[~r];
-                const int3 t = A.idx[id];
-                const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
-                const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
-                const float3 cc = make_float3(A.verts[3 * t.z], A.verts[3 * t.z + 1], A.verts[3 * t.z + 2]);
-                PackedTri P;
-                P.w0 = make_float4(a.x, a.y, a.z, b.x);
-                P.w1 = make_float4(b.y, b.z, cc.x, cc.y);
-                P.w2 = make_float4(cc.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
-                A.tris[tri_base + tri_off + j] = P;
-                ++j;
-            }
+            int32_t lv[kMaxLeafTris];
+            int nlv = 0;
+            if (!leaf_refs(A, ch[k], lv, nlv) || nlv != c) { atomicExch(&A.counters[3], 1); return; }
+            emit_leaf_tris(A, lv, nlv, tri_base + tri_off);
             tri_off += c;
         }
     }
@@ -1403,7 +1489,9 @@ __device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const in
             if (ref < 0) {
                 done = lf = true;
             } else {
+                // the children are loaded with the decision (one round trip)
                 const uint32_t dr = A.dec[ref];
+                const int32_t lref = A.left[ref], rref = A.right[ref];
                 int i = slots;
                 while (i >= 2 && ((dr >> (3 * (i - 2))) & 7u) == 0u) --i;
                 if (i <= 1) {
@@ -1412,9 +1500,9 @@ __device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const in
                 } else {
                     const int kl = (int)((dr >> (3 * (i - 2))) & 7u);
                     split = true;
-                    rr = A.right[ref];
+                    rr = rref;
                     rs = i - kl;
-                    ref = A.left[ref];
+                    ref = lref;
                     slots = kl;
                 }
             }
@@ -1573,34 +1661,23 @@ __device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const in
         const int rank = __popc(imask & ((1u << myslot) - 1u));
         A.tasks_out[next + rank] = make_int2(ref, child_base + rank);
     } else if (active) {
-        // the (at most kMaxLeafTris) leaves under this child, left first
-        int32_t todo[kMaxLeafTris];
-        int sp = 0, j = 0;
-        todo[sp++] = ref;
-        while (sp > 0 && j < cnt) {
-            const int32_t r = todo[--sp];
-            if (r >= 0) {
-                if (sp + 2 > kMaxLeafTris) { atomicExch(&A.counters[3], 1); break; }
-                todo[sp++] = A.right[r];
-                todo[sp++] = A.left[r];
-                continue;
-            }
-            const int32_t id = A.vals[~r];
-            const int3 t = A.idx[id];
-            const float3 a = make_float3(A.verts[3 * t.x], A.verts[3 * t.x + 1], A.verts[3 * t.x + 2]);
-            const float3 b = make_float3(A.verts[3 * t.y], A.verts[3 * t.y + 1], A.verts[3 * t.y + 2]);
-            const float3 cc = make_float3(A.verts[3 * t.z], A.verts[3 * t.z + 1], A.verts[3 * t.z + 2]);
-            PackedTri P;
-            P.w0 = make_float4(a.x, a.y, a.z, b.x);
-            P.w1 = make_float4(b.y, b.z, cc.x, cc.y);
-            P.w2 = make_float4(cc.z, __int_as_float(id), __uint_as_float(A.flags ? A.flags[id] : 0u), 0.f);
-            A.tris[tri_base + tri_off + j] = P;
-            ++j;
+        int32_t lv[kMaxLeafTris];
+        int nlv = 0;
+        if (!leaf_refs(A, ref, lv, nlv) || nlv != cnt) {
+            atomicExch(&A.counters[3], 1);
+            return;
         }
+        emit_leaf_tris(A, lv, nlv, tri_base + tri_off);
     }
 }
 
-__global__ void __launch_bounds__(128) k_collapse_level_group(BuildArgs A)
+// 10 resident blocks (48 registers): the level launches are bound by the
+// latency of each task's chain of dependent loads, so resident warps count
+// for more than the registers that keep the leaf loads in flight together
+#ifndef RT_COLLAPSE_MIN_BLOCKS
+#define RT_COLLAPSE_MIN_BLOCKS 10
+#endif
+__global__ void __launch_bounds__(128, RT_COLLAPSE_MIN_BLOCKS) k_collapse_level_group(BuildArgs A)
 {
     const int32_t ntasks = *A.cur_count;
     const int lane32 = threadIdx.x & 31;
@@ -1768,7 +1845,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     if (ploc) {
         cudaMemsetAsync(pstate, 0, kStWords * sizeof(int32_t), st);
         k_ploc_segments<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, n, seg_first, pstate, in.nodes);
-        if (n > 0)
+        if (n > 0 && (!hploc || n == 1))
             k_ploc_init<<<min((n + threads - 1) / threads, in.sm_count * 8), threads, 0, st>>>(
                 n, keys2, 3 * mbits, nseg, llo, lhi, cl[0], chh[0]);
         // iterations in groups of kPlocGroup, then one read-back of the count
@@ -1781,7 +1858,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
             cudaSuccess) { R.status = -2; return R; }
         bool tail = !finished && n <= kPlocTailMax && !hploc;
         if (hploc && !finished) {
-            k_hploc_init<<<min((n + threads - 1) / threads, in.sm_count * 8), threads, 0, st>>>(n, cref, meet);
+            k_hploc_init<<<min((n + threads - 1) / threads, in.sm_count * 8), threads, 0, st>>>(n, meet);
             k_hploc<<<(n + kHplocBlock - 1) / kHplocBlock, kHplocBlock, 0, st>>>(
                 n, keys2, cref, meet, pstate, llo, lhi, cl[0], chh[0], left, right, ncount, ilo, ihi, sah, dec,
                 parent, leaf_parent);
@@ -1822,6 +1899,7 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     A.verts = in.verts; A.idx = in.idx; A.flags = in.flags;
     A.nodes = in.nodes; A.tris = in.tris; A.counters = counters;
     A.max_nodes = in.max_nodes;
+    int depth = 0;
     // levels back to back in groups of kCollapseGroup (a level past the last
     // one finds no tasks), one read-back per group: most trees end within
     // the first group
@@ -1851,7 +1929,6 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     }
     if (h_cnt[3]) { R.status = -8; return R; }
     if (h_cnt[4 + kMaxDepth] != 0) { R.status = -5; return R; }   // deeper than kMaxDepth levels
-    int depth = 0;
     while (depth < kMaxDepth && h_cnt[4 + depth] > 0) ++depth;
     R.status = 0;
     R.nodes = h_cnt[0];
