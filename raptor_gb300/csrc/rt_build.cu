@@ -863,6 +863,12 @@ constexpr int kHplocBlock = RT_HPLOC_BLOCK;
 #define RT_HPLOC_RADIUS 3
 #endif
 constexpr unsigned long long kHplocEmpty = ~0ull;
+// Carry each cluster's surface-area cost row in registers through the merges
+// (shuffled with its box) instead of loading the children's rows from the
+// table at every merge.
+#ifndef RT_HPLOC_ROWS
+#define RT_HPLOC_ROWS 1
+#endif
 
 // Is the pair (a, a + 1) of sorted keys closer (longer common prefix) than
 // (b, b + 1)?  Equal keys fall back to the positions' xor (balanced trees
@@ -953,6 +959,11 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
             bool valid = (int)lane < cnt;
             int32_t ref = 0;
             float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+#if RT_HPLOC_ROWS
+            float row[8];                        // the cluster's surface-area cost row
+#pragma unroll
+            for (int q = 0; q < 8; ++q) row[q] = 0.f;
+#endif
             if (valid) {
                 // a child of as many leaves as clusters is its leaves; else its refs are stored
                 const bool in_left = (int)lane < p_nl;
@@ -968,6 +979,9 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
                     c0 = __ldcg(ilo + ref);      // .w: the node's triangle count
                     c1 = __ldcg(ihi + ref);
                 }
+#if RT_HPLOC_ROWS
+                if (sah) sah_child(sah, ref, c0, c1, row);
+#endif
             }
             const int target = p_root ? 1 : kHplocKeep;
             int32_t base = 0, extra = 0, made = 0;
@@ -1047,6 +1061,11 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
                                               __shfl_sync(0xffffffffu, c1.y, bk),
                                               __shfl_sync(0xffffffffu, c1.z, bk), 0.f);
                 const int32_t rb = __shfl_sync(0xffffffffu, ref, bk);
+#if RT_HPLOC_ROWS
+                float rowb[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) rowb[q] = __shfl_sync(0xffffffffu, row[q], bk);
+#endif
                 if (make) {
                     const int32_t m = made + __popc(mm & below);
                     const int32_t id = m < reserved ? base + m : extra + m;
@@ -1057,6 +1076,17 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
                     if (r < 0) leaf_parent[~r] = id; else parent[r] = id;
                     const int32_t count = __float_as_int(c0.w) + __float_as_int(b0.w);
                     __stcg(ncount + id, count);
+#if RT_HPLOC_ROWS
+                    c0 = box_min(c0, b0);
+                    c1 = box_max(c1, b1);
+                    c0.w = __int_as_float(count);
+                    if (sah) {
+                        float prow[8];
+                        sah_node(sah, dec, id, half_area(c0, c1), count, row, rowb, prow);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) row[q] = prow[q];
+                    }
+#else
                     float sl[8], sr[8];
                     if (sah) {
                         sah_child(sah, l, c0, c1, sl);
@@ -1066,6 +1096,7 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
                     c1 = box_max(c1, b1);
                     c0.w = __int_as_float(count);
                     if (sah) sah_node(sah, dec, id, half_area(c0, c1), count, sl, sr);
+#endif
                     __stcg(ilo + id, c0);
                     __stcg(ihi + id, make_float4(c1.x, c1.y, c1.z, 0.f));
                     ref = id;
@@ -1080,6 +1111,10 @@ __global__ void __launch_bounds__(kHplocBlock, RT_HPLOC_MIN_BLOCKS) k_hploc(int3
                 c1 = make_float4(__shfl_sync(0xffffffffu, c1.x, from), __shfl_sync(0xffffffffu, c1.y, from),
                                  __shfl_sync(0xffffffffu, c1.z, from), 0.f);
                 ref = __shfl_sync(0xffffffffu, ref, from);
+#if RT_HPLOC_ROWS
+#pragma unroll
+                for (int q = 0; q < 8; ++q) row[q] = __shfl_sync(0xffffffffu, row[q], from);
+#endif
                 if (kc == cnt) {                 // never expected: no mutual pair
                     bad = true;
                     break;
@@ -1158,6 +1193,15 @@ struct BuildArgs {
     int2 *tasks_out;
     int32_t max_nodes;
 };
+
+// Wide nodes and triangle slots allocated together: counters[0] and
+// counters[1] form one 64-bit word (nodes low, slots high; both stay below
+// 2^31), so a task makes one atomic instead of two on the same line.
+__device__ __forceinline__ unsigned long long alloc_nodes_tris(int32_t *counters, int32_t nodes, int32_t tris)
+{
+    return atomicAdd(reinterpret_cast<unsigned long long *>(counters),
+                     ((unsigned long long)(uint32_t)tris << 32) | (uint32_t)nodes);
+}
 
 __device__ __forceinline__ void ref_box(const BuildArgs &A, int32_t ref, float4 &lo, float4 &hi)
 {
@@ -1345,8 +1389,9 @@ __device__ __forceinline__ void collapse_task(const BuildArgs &A, const int2 tas
     for (int k = 0; k < m; ++k) {
         if (!leaf[k]) ++n_int; else n_tri += cnt[k];
     }
-    const int32_t child_base = n_int ? atomicAdd(&A.counters[0], n_int) : 0;
-    const int32_t tri_base = n_tri ? atomicAdd(&A.counters[1], n_tri) : 0;
+    const unsigned long long old = (n_int || n_tri) ? alloc_nodes_tris(A.counters, n_int, n_tri) : 0ull;
+    const int32_t child_base = (int32_t)(uint32_t)old;
+    const int32_t tri_base = (int32_t)(old >> 32);
     if (child_base + n_int > A.max_nodes || tri_base + n_tri > A.n) { atomicExch(&A.counters[3], 1); return; }
 
     // quantisation frame
@@ -1603,8 +1648,11 @@ __device__ __forceinline__ void collapse_task_group(const BuildArgs &A, const in
         }
         int32_t cb = 0, tb = 0, nb = 0;
         if ((threadIdx.x & 31) == 0) {
-            if (si) cb = atomicAdd(&A.counters[0], si);
-            if (st) tb = atomicAdd(&A.counters[1], st);
+            if (si || st) {
+                const unsigned long long old = alloc_nodes_tris(A.counters, si, st);
+                cb = (int32_t)(uint32_t)old;
+                tb = (int32_t)(old >> 32);
+            }
             if (si) nb = atomicAdd(A.next_count, si);
         }
         child_base = __shfl_sync(full, cb, 0) + pi;
@@ -1688,6 +1736,33 @@ __global__ void __launch_bounds__(128, RT_COLLAPSE_MIN_BLOCKS) k_collapse_level_
         const int32_t ti = t0 + g;
         const bool has = ti < ntasks;
         collapse_task_group(A, has ? A.tasks_in[ti] : make_int2(0, 0), has, 8 * g, lane32 & 7);
+    }
+}
+
+// The first kCollapseTopLevels levels of a single-root tree (at most 1, 8
+// and 64 tasks) in one block, between block barriers: the levels near the
+// root are a chain of dependent loads per task, and one launch for all
+// three saves two launches' fixed cost.
+constexpr int kCollapseTopLevels = 3;
+__global__ void __launch_bounds__(1024) k_collapse_top(BuildArgs A, int2 *tq0, int2 *tq1, int32_t *level_count)
+{
+    const int lane32 = threadIdx.x & 31;
+    const int g = lane32 >> 3;
+    const int32_t wid = (int32_t)(threadIdx.x >> 5);
+    const int32_t nw = (int32_t)(blockDim.x >> 5);
+    for (int level = 0; level < kCollapseTopLevels; ++level) {
+        BuildArgs B = A;
+        B.tasks_in = (level & 1) ? tq1 : tq0;
+        B.tasks_out = (level & 1) ? tq0 : tq1;
+        B.cur_count = level_count + level;
+        B.next_count = level_count + level + 1;
+        const int32_t ntasks = __ldcg(B.cur_count);   // counted by this block's previous level
+        for (int32_t t0 = 4 * wid; t0 < ntasks; t0 += 4 * nw) {
+            const int32_t ti = t0 + g;
+            const bool has = ti < ntasks;
+            collapse_task_group(B, has ? __ldcg(B.tasks_in + ti) : make_int2(0, 0), has, 8 * g, lane32 & 7);
+        }
+        __syncthreads();
     }
 }
 
@@ -1902,12 +1977,17 @@ BuildResult build_wide_bvh(const BuildInputs &in, void *temp, size_t temp_bytes,
     int depth = 0;
     // levels back to back in groups of kCollapseGroup (a level past the last
     // one finds no tasks), one read-back per group: most trees end within
-    // the first group
+    // the first group; a single root's first levels in one block
     const int cgrid = max(1, min((n + nseg + 63) / 64, in.sm_count * 16));
     const int wgrid = max(1, min((n + nseg + 3) / 4, in.sm_count * 32));
     int level = 0;
-    for (;;) {
-        const int stop = min(level + kCollapseGroup, kMaxDepth);
+    if (A.dec && nseg == 1) {
+        k_collapse_top<<<1, 1024, 0, st>>>(A, tq0, tq1, level_count);
+        level = kCollapseTopLevels;
+    }
+    for (bool first = true;; first = false) {
+        // the first group ends at level kCollapseGroup whichever level it starts at
+        const int stop = min(first ? max(level + 1, kCollapseGroup) : level + kCollapseGroup, kMaxDepth);
         for (; level < stop; ++level) {
             A.tasks_in = (level & 1) ? tq1 : tq0;
             A.tasks_out = (level & 1) ? tq0 : tq1;
