@@ -165,14 +165,31 @@ struct SoftState {
     DevBuf counts, prefix64;     // int64 per pixel: numbers a distributed pixel draws, their exclusive scan
     DevBuf scan64_temp;
     int64_t win_base = -1, win_len = 0;
+    // Host side of the stream: staging holds numbers [stage_base, stage_base
+    // + stage_len) and rng stands at their end.  After each upload a thread
+    // reads ahead: it generates the numbers that follow the frame's slice
+    // (where the next frame starts, drawing about as many) while the GPU
+    // renders; the next window joins it first.
     RefRandom rng;
-    float *staging = nullptr;    // pinned host copy of the slice being uploaded
+    float *staging = nullptr;    // pinned
     size_t staging_cap = 0;
+    int64_t stage_base = -1, stage_len = 0;
+    std::thread ahead;
+    cudaEvent_t copied = nullptr;   // the last upload out of staging
+    int device = 0;
 };
+
+// Waits for a read-ahead in flight.
+void join_ahead(SoftState &S)
+{
+    if (S.ahead.joinable()) S.ahead.join();
+}
 
 void soft_release(rt_context *ctx)
 {
     if (!ctx->soft) return;
+    join_ahead(*ctx->soft);
+    if (ctx->soft->copied) cudaEventDestroy(ctx->soft->copied);
     ctx->soft->lut.release();
     ctx->soft->hits.release();
     ctx->soft->flags.release();
@@ -835,6 +852,7 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
     if (!ctx->soft) {
         ctx->soft = new (std::nothrow) SoftState();
         if (!ctx->soft) return sfail(RT_ERR_OUT_OF_MEMORY, "rt_render_soft_shadows: state allocation");
+        ctx->soft->device = ctx->device;
     }
     SoftState &S = *ctx->soft;
     cudaStream_t st = ctx->stream;
@@ -1086,31 +1104,67 @@ rt_status check_shapes(const rt_scene *s, const rt_light *lights, int32_t nlight
 
 // The frame's numbers [offset, offset + total) of the reference's stream on
 // the device (generated on the host into pinned memory, copied over), kept
-// while later frames fall inside them; *rnd points at number offset.
+// while later frames fall inside them; *rnd points at number offset.  A
+// frame that starts where the last one ended finds its numbers already
+// generated by the read-ahead (or the read-ahead still running: it is
+// joined).
 rt_status stream_window(SoftState &S, int64_t offset, int64_t total, cudaStream_t st, const float **rnd)
 {
     *rnd = nullptr;
     if (total <= 0) return RT_OK;
-    if (!(S.win_base >= 0 && offset >= S.win_base && offset + total <= S.win_base + S.win_len)) {
-        if (S.staging_cap < (size_t)total) {
+    if (S.win_base >= 0 && offset >= S.win_base && offset + total <= S.win_base + S.win_len) {
+        *rnd = (const float *)S.window.ptr + (offset - S.win_base);
+        return RT_OK;
+    }
+    join_ahead(S);
+    const int64_t want = total + total / 4;   // read-ahead length: the next frame draws about as many
+    if (!(S.stage_base >= 0 && offset >= S.stage_base && offset + total <= S.stage_base + S.stage_len)) {
+        // not read ahead: generate the slice here
+        // the last upload reads the staging buffer: it must be done first
+        RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
+        if (S.staging_cap < (size_t)want) {
             if (S.staging) cudaFreeHost(S.staging);
             S.staging = nullptr;
             S.staging_cap = 0;
-            const size_t cap = (size_t)total + (size_t)total / 4;
-            RT_CUDA_S(cudaMallocHost(&S.staging, cap * sizeof(float)), "pinned stream staging");
-            S.staging_cap = cap;
+            S.stage_base = -1;
+            S.stage_len = 0;
+            RT_CUDA_S(cudaMallocHost(&S.staging, (size_t)want * sizeof(float)), "pinned stream staging");
+            S.staging_cap = (size_t)want;
         }
-        // the copy below reads the staging buffer: an earlier frame's copy
-        // from it must be done before it is overwritten
-        RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
         generate_slice(S.rng, offset, total, S.staging);
-        RT_CUDA_S(S.window.reserve((size_t)total * sizeof(float)), "stream allocation");
-        RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging, (size_t)total * sizeof(float), cudaMemcpyHostToDevice, st),
-                  "stream copy");
-        S.win_base = offset;
-        S.win_len = total;
+        S.stage_base = offset;
+        S.stage_len = total;
     }
-    *rnd = (const float *)S.window.ptr + (offset - S.win_base);
+    RT_CUDA_S(S.window.reserve((size_t)total * sizeof(float)), "stream allocation");
+    RT_CUDA_S(cudaMemcpyAsync(S.window.ptr, S.staging + (offset - S.stage_base), (size_t)total * sizeof(float),
+                              cudaMemcpyHostToDevice, st),
+              "stream copy");
+    if (!S.copied) RT_CUDA_S(cudaEventCreateWithFlags(&S.copied, cudaEventDisableTiming), "event creation");
+    RT_CUDA_S(cudaEventRecord(S.copied, st), "event record");
+    S.win_base = offset;
+    S.win_len = total;
+    *rnd = (const float *)S.window.ptr;
+    // read ahead [offset + total, offset + total + want): the numbers already
+    // generated past the frame move to the front of staging (once the
+    // upload is done), the rest continue from rng, which stands at their end
+    if ((size_t)want <= S.staging_cap) {
+        const int64_t next = offset + total;
+        SoftState *P = &S;
+        S.ahead = std::thread([P, next, want] {
+            cudaSetDevice(P->device);
+            if (cudaEventSynchronize(P->copied) != cudaSuccess) {
+                P->stage_base = -1;   // nothing kept: the next window generates its own
+                P->stage_len = 0;
+                return;
+            }
+            const int64_t keep = P->stage_base + P->stage_len - next;
+            if (keep > 0) std::memmove(P->staging, P->staging + (next - P->stage_base), (size_t)keep * sizeof(float));
+            if (want > keep) generate_slice(P->rng, next + std::max<int64_t>(keep, 0), want - std::max<int64_t>(keep, 0),
+                                            P->staging + std::max<int64_t>(keep, 0));
+            P->stage_base = next;
+            P->stage_len = std::max(keep, want);
+        });
+    }
     return RT_OK;
 }
 
@@ -1178,6 +1232,7 @@ extern "C" rt_status rt_render_distributed(rt_scene *s, const rt_camera *camera,
     if (!ctx->soft) {
         ctx->soft = new (std::nothrow) SoftState();
         if (!ctx->soft) return sfail(RT_ERR_OUT_OF_MEMORY, "rt_render_distributed: state allocation");
+        ctx->soft->device = ctx->device;
     }
     SoftState &S = *ctx->soft;
     cudaStream_t st = ctx->stream;

@@ -130,6 +130,37 @@ def test_soft_shadows_stream_window_and_outputs(rtlib, ctx):
     sc.close()
 
 
+def test_soft_shadows_read_ahead_frames(rtlib):
+    """Consecutive frames, each starting at the last one's stream_end (whose
+    numbers a host thread generated while the last frame rendered), a jump
+    past the numbers read ahead and a jump back to an earlier position all
+    equal the frames a fresh context renders at the same positions."""
+    from raptor_gb300 import scenes
+    scene, frame = scenes.icosphere_scene(freq=16, res=96)
+    frame = dict(frame, lights=[dict(frame["lights"][0], r=0.7)])
+    c1 = rtlib.Context(0)
+    sc = rtlib.Scene(c1, scene)
+    seen = []
+    pos = 0
+    for _ in range(4):
+        out = sc.render_soft(frame, 8, pos, want_float=True)
+        seen.append((pos, out))
+        pos = out["stream_end"]
+    per_frame = seen[0][1]["stream_end"]
+    for p in (pos + 3 * per_frame, seen[1][0], seen[2][0]):
+        seen.append((p, sc.render_soft(frame, 8, p, want_float=True)))
+    sc.close()
+    c1.close()
+    c2 = rtlib.Context(0)
+    fresh = rtlib.Scene(c2, scene)
+    for p, out in seen:
+        ref = fresh.render_soft(frame, 8, p, want_float=True)
+        assert out["stream_end"] == ref["stream_end"] == p + per_frame
+        assert np.array_equal(out["fimg"].view(np.uint32), ref["fimg"].view(np.uint32)), p
+    fresh.close()
+    c2.close()
+
+
 def test_triangle_lights_match_oracle_float_frames(rtlib, ctx, oracle):
     """480x270 terrain with two triangle-defined lights beside the sun: a
     quad (two triangles) and a 7-triangle spot-light disk.  With 16 samples
