@@ -291,22 +291,16 @@ __device__ __forceinline__ int atomic_add_acq_rel(int32_t *p, int32_t v)
 constexpr int kRefitMaxDepth = 1 << 16;   // binary levels a refit walk may climb
 constexpr int32_t kEmptySlot = INT32_MIN;
 
-// Bottom-up box refit: the second child to arrive at a node unions both.
-__global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
-                        const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
-                        const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
-                        int32_t *flags, const int32_t *__restrict__ count, float *sah, uint32_t *dec,
-                        int32_t *err)
+// Bottom-up box refit from one child up: the second child to arrive at a
+// node unions both and goes on.  The climbing child's ref, box and
+// surface-area row stay in registers; only the sibling's are loaded.
+__device__ __forceinline__ void refit_climb(int32_t cur, float4 mlo, float4 mhi, float *mrow, int32_t p,
+                                            const int32_t *__restrict__ left, const int32_t *__restrict__ right,
+                                            const int32_t *__restrict__ parent, const float4 *__restrict__ llo,
+                                            const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
+                                            int32_t *flags, const int32_t *__restrict__ count, float *sah,
+                                            uint32_t *dec, int32_t *err)
 {
-    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    // the child this thread climbs from: its ref, box and surface-area row
-    // stay in registers; only the sibling's are loaded
-    int32_t cur = ~k;
-    float4 mlo = llo[k], mhi = lhi[k];
-    float mrow[8];
-    if (sah) sah_child(sah, cur, mlo, mhi, mrow);
-    int32_t p = leaf_parent[k];
     int guard = 0;
     while (p >= 0) {
         if (++guard > kRefitMaxDepth) { atomicExch(err, 1); return; }
@@ -335,6 +329,21 @@ __global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32
         mhi = phi;
         p = parent[p];
     }
+}
+
+__global__ void k_refit(int32_t n, const int32_t *__restrict__ left, const int32_t *__restrict__ right,
+                        const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent,
+                        const float4 *__restrict__ llo, const float4 *__restrict__ lhi, float4 *ilo, float4 *ihi,
+                        int32_t *flags, const int32_t *__restrict__ count, float *sah, uint32_t *dec,
+                        int32_t *err)
+{
+    const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 mlo = llo[k], mhi = lhi[k];
+    float mrow[8];
+    if (sah) sah_child(sah, ~k, mlo, mhi, mrow);
+    refit_climb(~k, mlo, mhi, mrow, leaf_parent[k], left, right, parent, llo, lhi, ilo, ihi, flags, count, sah, dec,
+                err);
 }
 
 // Root of each segment: the binary node whose range is exactly the
