@@ -528,11 +528,16 @@ rt_status rt_render_soft_shadows(rt_scene *scene, const rt_camera *camera, const
  * default build).  stream: RT_STREAM_REFERENCE draws the reference's own
  * process-wide generator (common/common.cc:35-105) in the reference's
  * order, pixel after pixel from position stream_offset; RT_STREAM_PIXEL
- * gives every pixel its own stream -- number k of pixel p is word k % 4 of
- * Philox4x32-10 (Salmon et al., SC'11) with counter (p, k / 4, 0,
- * 0x53545245) and key (seed low, seed high), as (float)word * 2^-32, the
- * reference generator's conversion -- drawn in the reference's order within
- * the pixel. */
+ * gives every node of every pixel's ray tree its own stream -- number k
+ * that node q of pixel p draws is word k % 4 of Philox4x32-10 (Salmon et
+ * al., SC'11) with counter (p, q low, q high, k / 4) and key (seed low,
+ * seed high), as (float)word * 2^-32, the reference generator's conversion;
+ * the camera ray is node 0x6A09E667F3BCC909 and ray i of a node's
+ * reflection (s = 0) or refraction (s = 1) set is node SplitMix64(q + (64 s
+ * + i + 1) * 0x9E3779B97F4A7C15) -- drawn in the reference's order within
+ * the node (the lights' rays, then the reflection set, then the refraction
+ * set).  Keyed by node, a subtree's numbers do not depend on how many its
+ * elder siblings drew, so the subtrees of a pixel are traced in parallel. */
 typedef struct rt_sampling {
     int32_t soft_samples;
     int32_t diffuse_samples;

@@ -259,7 +259,9 @@ def oracle_lib():
                                                  C.POINTER(Material), C.c_int32, C.POINTER(Sampling), C.c_int32,
                                                  _U8, _I, _F, C.POINTER(C.c_int64)]
         lib["ro_pixel_stream"].restype = C.c_float
-        lib["ro_pixel_stream"].argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        lib["ro_pixel_stream"].argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32]
+        lib["ro_tree_child"].restype = C.c_uint64
+        lib["ro_tree_child"].argtypes = [C.c_uint64, C.c_int32, C.c_int32]
         lib["ro_area_light_rays"].restype = C.c_int32
         lib["ro_area_light_rays"].argtypes = [C.c_int32, C.c_int32, _I]
         lib["ro_lut_cos"].restype = C.c_float
@@ -648,9 +650,18 @@ def ref_random(start, n):
     return out
 
 
-def pixel_stream(seed, pixel, k):
-    """Number k of pixel `pixel`'s stream (ro_pixel_stream)."""
-    return oracle_lib()["ro_pixel_stream"](int(seed), int(pixel), int(k))
+TREE_ROOT = 0x6A09E667F3BCC909
+
+
+def pixel_stream(seed, pixel, node, k):
+    """Number k that tree node `node` of pixel `pixel` draws (ro_pixel_stream)."""
+    return oracle_lib()["ro_pixel_stream"](int(seed), int(pixel), int(node), int(k))
+
+
+def tree_child(parent, set_, index):
+    """The tree node of ray `index` of a node's reflection (0) or refraction
+    (1) set (ro_tree_child)."""
+    return oracle_lib()["ro_tree_child"](int(parent), int(set_), int(index))
 
 
 def area_light_rays(ntris, n):

@@ -1160,27 +1160,46 @@ int64_t ro_render_soft(const ro_scene *s, const ro_camera *cam, const ro_light *
 
 /* ------------------------------------------- Distributed ray tracing */
 
-float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint32_t k)
+float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint64_t node, uint32_t k)
 {
-    const uint32_t ctr[4] = {pixel, k >> 2, 0u, 0x53545245u};
+    const uint32_t ctr[4] = {pixel, (uint32_t)node, (uint32_t)(node >> 32), k >> 2};
     uint32_t w[4];
     ro_philox4x32(ctr, (uint32_t)seed, (uint32_t)(seed >> 32), w);
     return (float)w[k & 3u] * (1.0f / 4294967296.0f);
 }
 
-/* Where a pixel's numbers come from: the reference's generator (g), or
- * the pixel's own stream. */
+/* SplitMix64's output function (Steele, Lea and Flood 2014; Vigna's
+ * constants). */
+static inline uint64_t splitmix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+uint64_t ro_tree_child(uint64_t parent, int32_t set, int32_t index)
+{
+    return splitmix64(parent + (uint64_t)(set * 64 + index + 1) * 0x9E3779B97F4A7C15ull);
+}
+
+/* Where a node's numbers come from: the reference's generator (g), whose
+ * order is the pixel's drawing order, or the pixel's stream of this tree
+ * node. */
 typedef struct {
     ref_rng *g;
     uint64_t seed;
     uint32_t pixel;
-    uint32_t k;       /* numbers this pixel has drawn */
+    uint64_t node;    /* RO_STREAM_PIXEL: the node drawing */
+    uint32_t k;       /* numbers the node has drawn */
+    int64_t *drawn;   /* numbers the pixel has drawn */
 } draw_src;
 
 static inline float draw_next(draw_src *S)
 {
     const uint32_t k = S->k++;
-    return S->g ? ref_rng_next(S->g) : ro_pixel_stream(S->seed, S->pixel, k);
+    ++*S->drawn;
+    return S->g ? ref_rng_next(S->g) : ro_pixel_stream(S->seed, S->pixel, S->node, k);
 }
 
 typedef struct {
@@ -1298,10 +1317,17 @@ static int32_t spread_rays(dist_job *J, draw_src *S, v3 start, v3 ref, float spr
     return nr;
 }
 
-/* The colour of one ray of a distributed frame (see ro_render_distributed). */
-static int32_t dist_colour(dist_job *J, draw_src *S, const ro_ray *r, float magn, int32_t comp, v3 *out)
+/* The colour of one ray of a distributed frame (see ro_render_distributed);
+ * node: its tree node (RO_TREE_ROOT for the camera ray, ro_tree_child of
+ * its parent's for the others). */
+static int32_t dist_colour(dist_job *J, const draw_src *P, const ro_ray *r, float magn, int32_t comp, uint64_t node,
+                           v3 *out)
 {
     const ro_scene *s = J->s;
+    draw_src N = *P;
+    N.node = node;
+    N.k = 0;
+    draw_src *S = &N;
     ro_hit h;
     const int32_t id = closest(s, r, &h);
     J->rays += 1;
@@ -1351,12 +1377,12 @@ static int32_t dist_colour(dist_job *J, draw_src *S, const ro_ray *r, float magn
     v3 sum_refl = mk(0.0f, 0.0f, 0.0f), sum_refr = mk(0.0f, 0.0f, 0.0f);
     for (int32_t i = 0; i < nrefl && !J->bad; ++i) {
         v3 ci;
-        (void)dist_colour(J, S, &refl[i], refl_power, comp_refl, &ci);
+        (void)dist_colour(J, S, &refl[i], refl_power, comp_refl, ro_tree_child(node, 0, i), &ci);
         sum_refl = vadd(sum_refl, ci);
     }
     for (int32_t i = 0; i < nrefr && !J->bad; ++i) {
         v3 ci;
-        (void)dist_colour(J, S, &refr[i], refr_power, comp_refr, &ci);
+        (void)dist_colour(J, S, &refr[i], refr_power, comp_refr, ro_tree_child(node, 1, i), &ci);
         sum_refr = vadd(sum_refr, ci);
     }
     if (m->rf > 0.0f && nrefl > 0) c = vadd(c, vmul(vdivs(sum_refl, (float)nrefl), m->rf));
@@ -1368,11 +1394,12 @@ static int32_t dist_colour(dist_job *J, draw_src *S, const ro_ray *r, float magn
 static void dist_pixel(dist_job *J, const cam_state *cs, ref_rng *g, int32_t x, int32_t y)
 {
     const size_t pix = (size_t)x + (size_t)y * (size_t)J->cam->xres;
-    draw_src S = {g, J->smp.seed, (uint32_t)pix, 0u};
+    int64_t drawn = 0;
+    const draw_src S = {g, J->smp.seed, (uint32_t)pix, RO_TREE_ROOT, 0u, &drawn};
     const ro_ray r = cam_ray(cs, x, y);
     v3 c;
-    const int32_t id = dist_colour(J, &S, &r, 1.0f, 1, &c);
-    J->drawn += S.k;
+    const int32_t id = dist_colour(J, &S, &r, 1.0f, 1, RO_TREE_ROOT, &c);
+    J->drawn += drawn;
     if (J->hit_id) J->hit_id[pix] = id;
     if (J->fimg) { J->fimg[3 * pix] = c.x; J->fimg[3 * pix + 1] = c.y; J->fimg[3 * pix + 2] = c.z; }
     J->rgb[3 * pix] = clip8(c.x);

@@ -199,7 +199,7 @@ int32_t ro_area_light_rays(int32_t ntris, int32_t n, int32_t *cnt);
  * within a pixel, from stream: RO_STREAM_REFERENCE, the reference's own
  * process-wide generator from position offset, pixels in the reference's
  * order (x + y * xres) -- serial, nthreads ignored; RO_STREAM_PIXEL, one
- * stream per pixel (ro_pixel_stream with seed).  drawn (nullable) receives
+ * stream per pixel and tree node (ro_pixel_stream with seed).  drawn (nullable) receives
  * the count of numbers the frame drew.  Returns rays traced, or -1 on bad
  * arguments. */
 typedef struct ro_sampling {
@@ -216,10 +216,19 @@ int64_t ro_render_distributed(const ro_scene *s, const ro_camera *cam, const ro_
                               const ro_material *mats, int32_t nmats, const ro_sampling *smp, int32_t nthreads,
                               uint8_t *rgb, int32_t *hit_id, float *fimg, int64_t *drawn);
 
-/* Number k of pixel `pixel`'s stream: word k % 4 of Philox4x32-10 with
- * counter (pixel, k / 4, 0, 0x53545245) and key (seed low, seed high), as
- * (float)word * 2^-32 -- the reference generator's conversion. */
-float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint32_t k);
+/* Number k that tree node `node` of pixel `pixel` draws (in the
+ * reference's order within the node: the lights' rays, then the reflection
+ * set, then the refraction set): word k % 4 of Philox4x32-10 with counter
+ * (pixel, node low, node high, k / 4) and key (seed low, seed high), as
+ * (float)word * 2^-32 -- the reference generator's conversion.  Keyed by
+ * node, a subtree's numbers do not depend on how many its elder siblings
+ * drew, so subtrees can be traced apart. */
+float ro_pixel_stream(uint64_t seed, uint32_t pixel, uint64_t node, uint32_t k);
+/* Tree nodes: the camera ray is RO_TREE_ROOT; ray `index` of its
+ * reflection (set 0) or refraction (set 1) set is ro_tree_child(node, set,
+ * index) = SplitMix64(node + (64 set + index + 1) * 0x9E3779B97F4A7C15). */
+#define RO_TREE_ROOT 0x6A09E667F3BCC909ull
+uint64_t ro_tree_child(uint64_t parent, int32_t set, int32_t index);
 
 /* n numbers of the reference's random stream (common/common.cc:35-105)
  * from position start of a freshly seeded generator. */

@@ -164,6 +164,11 @@ struct SoftState {
     DevBuf area;                 // int4 per ray of a triangle-defined light: triangle, its rays, index
     DevBuf counts, prefix64;     // int64 per pixel: numbers a distributed pixel draws, their exclusive scan
     DevBuf scan64_temp;
+    // distributed frames on per-pixel streams: each pixel's camera-ray node
+    // (colour, material; first item, set sizes), the items (its sets' rays),
+    // their subtrees' colours, the item count
+    DevBuf root_c, root_sets, items, item_c, nitems;
+    int64_t item_cap = 0;
     int64_t win_base = -1, win_len = 0;
     // Host side of the stream: staging holds numbers [stage_base, stage_base
     // + stage_len) and rng stands at their end.  After each upload a thread
@@ -200,6 +205,11 @@ void soft_release(rt_context *ctx)
     ctx->soft->counts.release();
     ctx->soft->prefix64.release();
     ctx->soft->scan64_temp.release();
+    ctx->soft->root_c.release();
+    ctx->soft->root_sets.release();
+    ctx->soft->items.release();
+    ctx->soft->item_c.release();
+    ctx->soft->nitems.release();
     if (ctx->soft->staging) cudaFreeHost(ctx->soft->staging);
     delete ctx->soft;
     ctx->soft = nullptr;
@@ -434,22 +444,39 @@ struct DistParams {
     float td[RT_MAX_MATERIALS];
 };
 
-// A pixel's random numbers: number k of its own Philox stream, or number
-// base + k of the frame's slice of the reference's stream.
+// Tree nodes of a pixel's per-pixel streams: the camera ray is kTreeRoot;
+// ray `index` of a node's reflection (set 0) or refraction (set 1) set is
+// SplitMix64 (Steele, Lea and Flood 2014) of node + (64 set + index + 1) *
+// 0x9E3779B97F4A7C15.
+constexpr uint64_t kTreeRoot = 0x6A09E667F3BCC909ull;
+__device__ __forceinline__ uint64_t tree_child(uint64_t parent, int set, int index)
+{
+    uint64_t z = parent + (uint64_t)(set * 64 + index + 1) * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// A pixel's random numbers: number k that tree node `node` draws from the
+// pixel's Philox streams (counter (pixel, node low, node high, k / 4)), or
+// number base + k of the frame's slice of the reference's stream (k the
+// pixel's running index; node unused).
 struct DistStream {
     const float *win;
     int64_t base, nwin;
     uint32_t pixel, key0, key1;
     bool pixel_mode;
-    uint32_t blk;                // last Philox block computed
+    uint32_t blk;                // last Philox block computed, and its node
+    uint64_t bnode;
     uint4 w;
 
-    __device__ __forceinline__ float at(uint32_t k, uint32_t &status)
+    __device__ __forceinline__ float at(uint64_t node, uint32_t k, uint32_t &status)
     {
         if (pixel_mode) {
-            if ((k >> 2) != blk) {
+            if ((k >> 2) != blk || node != bnode) {
                 blk = k >> 2;
-                w = philox4x32(make_uint4(pixel, blk, 0u, 0x53545245u), key0, key1);
+                bnode = node;
+                w = philox4x32(make_uint4(pixel, (uint32_t)node, (uint32_t)(node >> 32), blk), key0, key1);
             }
             const uint32_t u = (k & 3u) == 0u ? w.x : (k & 3u) == 1u ? w.y : (k & 3u) == 2u ? w.z : w.w;
             return xmul(__uint2float_rn(u), 2.3283064365386963e-10f);
@@ -487,6 +514,7 @@ struct DistFrame {
     float3 sum;          // colours of the current set's rays so far
     float magn;          // power
     int32_t level;       // componant 4^level
+    uint64_t node;       // its tree node (per-pixel streams)
     int32_t mat;
     int32_t stage;
     int32_t out_in;
@@ -494,27 +522,68 @@ struct DistFrame {
     uint32_t refl_at, refr_at;   // the pixel's number index of each set's first number
 };
 
-enum : int32_t { kDistTrace = 0, kDistRefl = 1, kDistRefr = 2, kDistDone = 3 };
+enum : int32_t { kDistTrace = 0, kDistRefl = 1, kDistRefr = 2, kDistDone = 3, kDistLights = 4 };
 
 __device__ __forceinline__ int dist_count(int32_t samples, int32_t level)
 {
     return max(samples >> (2 * min(level, kDistLevels - 1)), 1);
 }
 
-// A pixel of a distributed frame: the ray tree of ray_trace_engine::ray_trace
-// (raytracer.cc:20-87) as a post-order walk with an explicit stack, drawing
-// the pixel's numbers in the reference's order (at each hit: the lights'
-// rays, then the reflection set, then the refraction set; then the
-// children's subtrees in order).  SHADE false: the counting pass of a
-// reference-stream frame without diffuse rays -- the tree without shadow
-// rays, returning the count of numbers the pixel draws.
-template <bool SHADE>
-__device__ __forceinline__ uint32_t dist_pixel(const SceneView &sc, const CameraView &cam, const LightSet &lights,
-                                               const MaterialTable &table, const DistLights &dl, const DistParams &dp,
-                                               const int4 *__restrict__ area, const float *__restrict__ verts,
-                                               const float *__restrict__ lut, DistStream &S, int x, int y,
-                                               DistFrame *F, float3 &out, bool &hit, uint32_t &nsec,
-                                               uint32_t &status)
+// Child ray i of frame f's reflection (set 0: ray::reflect ray.cc:118-182,
+// power magn * rf) or refraction (set 1: ray::refract ray.cc:198-281, power
+// magn * tran, ri inverted for a ray entering the front face, start point
+// pushed into the surface) set, its direction spread by the set's numbers
+// when the material spreads it.
+__device__ __forceinline__ void spawn_child(const DistFrame &f, const MaterialView &m, const DistParams &dp, int set,
+                                            int i, const float *__restrict__ lut, DistStream &S, uint32_t &status,
+                                            DistFrame &C)
+{
+    if (set == 0) {
+        const bool spread = dp.diffuse > 0 && dp.rfd[f.mat] != 0.0f;
+        const float rdn = xmul(2.0f, xdot(f.d, f.sn));
+        const float3 ref = xsub3(f.d, xmul3(f.sn, rdn));
+        if (spread) {
+            const uint32_t at = f.refl_at + 2u * (uint32_t)i;
+            C.d = spread_dir(ref, dp.rfd[f.mat], S.at(f.node, at, status), S.at(f.node, at + 1, status), lut);
+        } else {
+            C.d = ref;
+        }
+        C.o = offset_start(f.o, f.geo);
+        C.magn = xmul(f.magn, m.rf);
+        C.level = f.level + (spread ? 1 : 0);
+    } else {
+        const bool spread = dp.diffuse > 0 && dp.td[f.mat] != 0.0f;
+        float ri = m.ri;
+        const float rdn = -xdot(f.d, f.sn);
+        if (f.out_in) ri = xdiv(1.0f, ri);
+        const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
+        const float off = xsub(xmul(ri, rdn), __fsqrt_rn(cos_t2));
+        const float3 ref = xadd3(xmul3(f.d, ri), xmul3(f.sn, off));
+        if (spread) {
+            const uint32_t at = f.refr_at + 2u * (uint32_t)i;
+            C.d = spread_dir(ref, dp.td[f.mat], S.at(f.node, at, status), S.at(f.node, at + 1, status), lut);
+        } else {
+            C.d = ref;
+        }
+        C.o = offset_start_in(f.o, f.geo);
+        C.magn = xmul(f.magn, m.tran);
+        C.level = f.level + (spread ? 1 : 0);
+    }
+    C.node = tree_child(f.node, set, i);
+    C.stage = kDistTrace;
+}
+
+// The counting pass of a reference-stream frame without diffuse rays: the
+// pixel's ray tree (ray_trace_engine::ray_trace, raytracer.cc:20-87) walked
+// post-order with an explicit stack, without shadow rays, counting the
+// numbers the pixel draws in the reference's order (at each hit: the
+// lights' rays, then the reflection set, then the refraction set; then the
+// children's subtrees in order).
+__device__ __forceinline__ uint32_t dist_count_pixel(const SceneView &sc, const CameraView &cam,
+                                                     const LightSet &lights, const MaterialTable &table,
+                                                     const DistLights &dl, const DistParams &dp,
+                                                     const float *__restrict__ lut, DistStream &S, int x, int y,
+                                                     DistFrame *F, uint32_t &status)
 {
     uint32_t k = 0;
     const RayState cr = camera_ray(cam, x, y);
@@ -522,23 +591,20 @@ __device__ __forceinline__ uint32_t dist_pixel(const SceneView &sc, const Camera
     F[0].d = cr.d;
     F[0].magn = 1.0f;
     F[0].level = 0;
+    F[0].node = kTreeRoot;
     F[0].stage = kDistTrace;
     int sp = 1;
-    out = cam.background;
-    hit = false;
     for (int step = 0; sp > 0 && step < dp.max_steps; ++step) {
         DistFrame &f = F[sp - 1];
         if (f.stage == kDistTrace) {
             HitRecord h;
             bool occ;
             status |= traverse<false>(sc, f.o, f.d, FLT_MAX, h, occ);
-            if (sp > 1) ++nsec;
-            if (!(h.t < FLT_MAX)) {
-                f.c = cam.background;
-                f.stage = kDistDone;
-            } else {
+            f.nrefl = 0;
+            f.nrefr = 0;
+            f.stage = kDistDone;
+            if (h.t < FLT_MAX) {
                 const int32_t id = h.id - sc.tri_base;
-                if (sp == 1) hit = true;
                 int32_t mi = sc.mat ? __ldg(&sc.mat[id]) : 0;
                 if (mi < 0 || mi >= table.n) { status |= kStatusBadIndex; mi = 0; }
                 const MaterialView &m = table.m[mi];
@@ -547,172 +613,357 @@ __device__ __forceinline__ uint32_t dist_pixel(const SceneView &sc, const Camera
                 r.d = f.d;
                 const SurfacePoint spt = surface_at(sc, r, h);
                 const int lvl = min(f.level, kDistLevels - 1);
-                if (SHADE) {
-                    const float3 start = offset_start(spt.dst, spt.geo);
-                    const float3 kd = material_kd(m, spt);
-                    const int n = dist_count(dp.soft, f.level);
-                    float3 c = make_float3(0.f, 0.f, 0.f);
-                    for (int l = 0; l < lights.n; ++l) {
-                        const LightView &L = lights.l[l];
-                        float3 ldir;
-                        float len;
-                        int made = 0, nl = 1;
-                        if (L.kind == RT_LIGHT_DIRECTIONAL || n == 1) {
-                            shadow_ray(L, start, ldir, len);
-                            HitRecord sh;
-                            bool blocked;
-                            status |= traverse<true>(sc, start, ldir, len, sh, blocked);
-                            made = blocked ? 0 : 1;
-                        } else {
-                            nl = n;
-                            const bool tri_light = dl.made[l][lvl] > 0;
-                            for (int i = 0; i < n; ++i) {
-                                float3 di;
-                                float li;
-                                if (tri_light) {
-                                    const float u0 = S.at(k + 2 * i, status), u1 = S.at(k + 2 * i + 1, status);
-                                    area_ray(verts, sc.idx, __ldg(area + dl.first[l][lvl] + i), start, u0, u1, di, li);
-                                } else {
-                                    const float u0 = S.at(k + 3 * i, status), u1 = S.at(k + 3 * i + 1, status),
-                                                u2 = S.at(k + 3 * i + 2, status);
-                                    soft_ray(L, lut, start, n, i, u0, u1, u2, di, li);
-                                }
-                                if (i == 0) { ldir = di; len = li; }
-                                HitRecord sh;
-                                bool blocked;
-                                status |= traverse<true>(sc, start, di, li, sh, blocked);
-                                if (!blocked) ++made;
-                            }
-                        }
-                        k += (uint32_t)dl.draws[l][lvl];
-                        nsec += (uint32_t)nl;
-                        phong_add<true>(L, m, kd, spt.sn, f.d, ldir, len, xdiv((float)made, (float)nl), c);
-                    }
-                    f.c = xadd3(c, m.ka);
-                } else {
-                    for (int l = 0; l < lights.n; ++l) k += (uint32_t)dl.draws[l][lvl];
-                }
+                for (int l = 0; l < lights.n; ++l) k += (uint32_t)dl.draws[l][lvl];
                 f.o = spt.dst;
                 f.sn = spt.sn;
                 f.geo = spt.geo;
                 f.mat = mi;
                 f.out_in = spt.out_in ? 1 : 0;
-                f.nrefl = 0;
-                f.nrefr = 0;
-                // the reflection set (ray::reflect): power magn * rf above 0.1
                 if ((double)xmul(f.magn, m.rf) > 0.1) {
-                    if (dp.diffuse > 0 && dp.rfd[mi] != 0.0f) {
-                        f.nrefl = dist_count(dp.diffuse, f.level);
-                        f.refl_at = k;
-                        k += 2u * (uint32_t)f.nrefl;
-                    } else {
-                        f.nrefl = 1;
-                    }
+                    f.nrefl = (dp.diffuse > 0 && dp.rfd[mi] != 0.0f) ? dist_count(dp.diffuse, f.level) : 1;
+                    if (dp.diffuse > 0 && dp.rfd[mi] != 0.0f) { f.refl_at = k; k += 2u * (uint32_t)f.nrefl; }
                 }
-                // the refraction set (ray::refract): none beyond the critical angle
                 if ((double)xmul(f.magn, m.tran) > 0.1) {
                     float ri = m.ri;
                     const float rdn = -xdot(f.d, f.sn);
                     if (f.out_in) ri = xdiv(1.0f, ri);
                     const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
                     if (!(cos_t2 < 0.0f)) {
-                        if (dp.diffuse > 0 && dp.td[mi] != 0.0f) {
-                            f.nrefr = dist_count(dp.diffuse, f.level);
-                            f.refr_at = k;
-                            k += 2u * (uint32_t)f.nrefr;
-                        } else {
-                            f.nrefr = 1;
-                        }
+                        f.nrefr = (dp.diffuse > 0 && dp.td[mi] != 0.0f) ? dist_count(dp.diffuse, f.level) : 1;
+                        if (dp.diffuse > 0 && dp.td[mi] != 0.0f) { f.refr_at = k; k += 2u * (uint32_t)f.nrefr; }
                     }
                 }
                 f.child = 0;
-                f.sum = make_float3(0.f, 0.f, 0.f);
                 f.stage = kDistRefl;
             }
         }
         if (f.stage == kDistRefl) {
-            const MaterialView &m = table.m[f.mat];
             if (f.child < f.nrefl) {
-                if (sp >= kDistDepth) {
-                    status |= kStatusStepLimit;
-                    f.child = f.nrefl;
-                    continue;
-                }
-                const bool spread = dp.diffuse > 0 && dp.rfd[f.mat] != 0.0f;
-                const float rdn = xmul(2.0f, xdot(f.d, f.sn));
-                const float3 ref = xsub3(f.d, xmul3(f.sn, rdn));
-                DistFrame &C = F[sp];
-                if (spread) {
-                    const uint32_t at = f.refl_at + 2u * (uint32_t)f.child;
-                    C.d = spread_dir(ref, dp.rfd[f.mat], S.at(at, status), S.at(at + 1, status), lut);
-                } else {
-                    C.d = ref;
-                }
-                C.o = offset_start(f.o, f.geo);
-                C.magn = xmul(f.magn, m.rf);
-                C.level = f.level + (spread ? 1 : 0);
-                C.stage = kDistTrace;
+                if (sp >= kDistDepth) { status |= kStatusStepLimit; f.child = f.nrefl; continue; }
+                spawn_child(f, table.m[f.mat], dp, 0, f.child, lut, S, status, F[sp]);
                 ++f.child;
                 ++sp;
                 continue;
             }
-            if (SHADE && m.rf > 0.0f && f.nrefl > 0) f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefl), m.rf));
             f.child = 0;
-            f.sum = make_float3(0.f, 0.f, 0.f);
             f.stage = kDistRefr;
         }
         if (f.stage == kDistRefr) {
-            const MaterialView &m = table.m[f.mat];
             if (f.child < f.nrefr) {
-                if (sp >= kDistDepth) {
-                    status |= kStatusStepLimit;
-                    f.child = f.nrefr;
-                    continue;
-                }
-                const bool spread = dp.diffuse > 0 && dp.td[f.mat] != 0.0f;
-                float ri = m.ri;
-                const float rdn = -xdot(f.d, f.sn);
-                if (f.out_in) ri = xdiv(1.0f, ri);
-                const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
-                const float off = xsub(xmul(ri, rdn), __fsqrt_rn(cos_t2));
-                const float3 ref = xadd3(xmul3(f.d, ri), xmul3(f.sn, off));
-                DistFrame &C = F[sp];
-                if (spread) {
-                    const uint32_t at = f.refr_at + 2u * (uint32_t)f.child;
-                    C.d = spread_dir(ref, dp.td[f.mat], S.at(at, status), S.at(at + 1, status), lut);
-                } else {
-                    C.d = ref;
-                }
-                C.o = offset_start_in(f.o, f.geo);
-                C.magn = xmul(f.magn, m.tran);
-                C.level = f.level + (spread ? 1 : 0);
-                C.stage = kDistTrace;
+                if (sp >= kDistDepth) { status |= kStatusStepLimit; f.child = f.nrefr; continue; }
+                spawn_child(f, table.m[f.mat], dp, 1, f.child, lut, S, status, F[sp]);
                 ++f.child;
                 ++sp;
                 continue;
             }
-            if (SHADE && m.tran > 0.0f && f.nrefr > 0)
-                f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefr), m.tran));
             f.stage = kDistDone;
         }
-        // done: the frame's colour goes to its parent's current set
-        const float3 col = f.c;
         --sp;
-        if (sp == 0) out = col;
-        else F[sp - 1].sum = xadd3(F[sp - 1].sum, col);
     }
     if (sp > 0) status |= kStatusStepLimit;
     return k;
 }
 
+// How dist_walk walks: the whole tree from the camera ray; the camera ray's
+// node alone (its colour from the lights and ka, its sets left in F[0] for
+// the caller to hand out); or the subtree of a ray given in F[0].
+enum : int { kDistWhole = 0, kDistRoot = 1, kDistSub = 2 };
+
+// A pixel's ray tree shaded (ray_trace_engine::ray_trace, raytracer.cc:
+// 20-87): the post-order walk of dist_count_pixel with every node shaded
+// -- the coloured Phong of each light with its first ray's direction and
+// length, weighted by the fraction of its rays that reach it (ray::find_rays
+// ray.cc:91-104, light::find_rays light.h:62-164), plus ka; then each set's
+// mean colour times rf, then tran -- drawing the numbers in the reference's
+// order.  The walk is resumable: walk_advance moves it to the lane's next
+// ray (a node's camera, mirror, refracted or diffuse ray: closest hit; a
+// light's ray: any hit), the caller traces it, walk_consume takes the
+// result -- so a warp's lanes trace together at one call site whatever
+// stage their trees are at.  Walk holds the state besides the frame stack;
+// the top frame's lights are shaded before any child is pushed, so one set
+// of light state serves every frame.
+struct Walk {
+    int sp, step;
+    float3 start, kd, ldir, c, out;
+    float len;
+    int light, sample, nl, made, lvl;
+    uint32_t k;            // reference stream: the pixel's next number
+    uint32_t kb, k0;       // the node's next number and its first
+    uint32_t drawn, nsec;
+    bool hit;
+};
+
+// A walk from the camera ray of (x, y), or (kDistSub) from the ray already
+// in F[0].
+template <int MODE>
+__device__ __forceinline__ void walk_start(Walk &w, const CameraView &cam, DistFrame *F, int x, int y)
+{
+    if (MODE != kDistSub) {
+        const RayState cr = camera_ray(cam, x, y);
+        F[0].o = cr.o;
+        F[0].d = cr.d;
+        F[0].magn = 1.0f;
+        F[0].level = 0;
+        F[0].node = kTreeRoot;
+        F[0].stage = kDistTrace;
+    }
+    w.sp = 1;
+    w.step = 0;
+    w.start = w.kd = w.ldir = w.c = make_float3(0.f, 0.f, 0.f);
+    w.out = cam.background;
+    w.len = 0.f;
+    w.light = w.sample = w.made = w.lvl = 0;
+    w.nl = 1;
+    w.k = w.kb = w.k0 = w.drawn = w.nsec = 0;
+    w.hit = false;
+}
+
+// Moves the walk to its next ray (true: ray in ro, rd, rt, any) or to its
+// end (false: colour in w.out; kDistRoot: also when the camera ray's node
+// is shaded, its sets left in F[0]).
+template <int MODE>
+__device__ __forceinline__ bool walk_advance(Walk &w, const SceneView &sc, const LightSet &lights,
+                                             const MaterialTable &table, const DistLights &dl, const DistParams &dp,
+                                             const int4 *__restrict__ area, const float *__restrict__ verts,
+                                             const float *__restrict__ lut, DistStream &S, DistFrame *F,
+                                             float3 &ro, float3 &rd, float &rt, bool &any, uint32_t &status)
+{
+    if (w.sp <= 0) return false;
+    if (++w.step > dp.max_steps) {
+        status |= kStatusStepLimit;
+        w.sp = 0;
+        return false;
+    }
+    for (int guard = 0; w.sp > 0 && guard < 4 * kDistDepth + 2 * RT_MAX_LIGHTS + 4; ++guard) {
+        DistFrame &f = F[w.sp - 1];
+        if (f.stage == kDistTrace) {
+            ro = f.o;
+            rd = f.d;
+            rt = FLT_MAX;
+            any = false;
+            return true;
+        }
+        if (f.stage == kDistLights) {
+            const MaterialView &m = table.m[f.mat];
+            if (w.light < lights.n) {
+                const LightView &L = lights.l[w.light];
+                if (w.sample < w.nl) {
+                    // ray `sample` of this light
+                    float3 di;
+                    float li;
+                    if (w.nl == 1) {
+                        shadow_ray(L, w.start, di, li);
+                    } else if (dl.made[w.light][w.lvl] > 0) {
+                        const float u0 = S.at(f.node, w.kb + 2 * w.sample, status);
+                        const float u1 = S.at(f.node, w.kb + 2 * w.sample + 1, status);
+                        area_ray(verts, sc.idx, __ldg(area + dl.first[w.light][w.lvl] + w.sample), w.start, u0, u1, di,
+                                 li);
+                    } else {
+                        const float u0 = S.at(f.node, w.kb + 3 * w.sample, status);
+                        const float u1 = S.at(f.node, w.kb + 3 * w.sample + 1, status);
+                        const float u2 = S.at(f.node, w.kb + 3 * w.sample + 2, status);
+                        soft_ray(L, lut, w.start, w.nl, w.sample, u0, u1, u2, di, li);
+                    }
+                    if (w.sample == 0) {
+                        w.ldir = di;
+                        w.len = li;
+                    }
+                    ro = w.start;
+                    rd = di;
+                    rt = li;
+                    any = true;
+                    return true;
+                }
+                w.kb += (uint32_t)dl.draws[w.light][w.lvl];
+                w.nsec += (uint32_t)w.nl;
+                phong_add<true>(L, m, w.kd, f.sn, f.d, w.ldir, w.len, xdiv((float)w.made, (float)w.nl), w.c);
+                ++w.light;
+                w.sample = 0;
+                w.made = 0;
+                if (w.light < lights.n)
+                    w.nl = (lights.l[w.light].kind == RT_LIGHT_DIRECTIONAL) ? 1 : dist_count(dp.soft, f.level);
+                continue;
+            }
+            // shaded: ka, then the sets (their numbers after the lights')
+            f.c = xadd3(w.c, m.ka);
+            if ((double)xmul(f.magn, m.rf) > 0.1) {
+                if (dp.diffuse > 0 && dp.rfd[f.mat] != 0.0f) {
+                    f.nrefl = dist_count(dp.diffuse, f.level);
+                    f.refl_at = w.kb;
+                    w.kb += 2u * (uint32_t)f.nrefl;
+                } else {
+                    f.nrefl = 1;
+                }
+            }
+            if ((double)xmul(f.magn, m.tran) > 0.1) {
+                float ri = m.ri;
+                const float rdn = -xdot(f.d, f.sn);
+                if (f.out_in) ri = xdiv(1.0f, ri);
+                const float cos_t2 = xsub(1.0f, xmul(xmul(ri, ri), xsub(1.0f, xmul(rdn, rdn))));
+                if (!(cos_t2 < 0.0f)) {
+                    if (dp.diffuse > 0 && dp.td[f.mat] != 0.0f) {
+                        f.nrefr = dist_count(dp.diffuse, f.level);
+                        f.refr_at = w.kb;
+                        w.kb += 2u * (uint32_t)f.nrefr;
+                    } else {
+                        f.nrefr = 1;
+                    }
+                }
+            }
+            w.drawn += w.kb - w.k0;
+            if (!dp.pixel_stream) w.k = w.kb;
+            f.child = 0;
+            f.sum = make_float3(0.f, 0.f, 0.f);
+            f.stage = kDistRefl;
+            if (MODE == kDistRoot) {   // the camera ray's node alone: its sets stay in F[0]
+                w.out = f.c;
+                w.sp = 0;
+                return false;
+            }
+            continue;
+        }
+        if (f.stage == kDistRefl) {
+            const MaterialView &m = table.m[f.mat];
+            if (f.child < f.nrefl) {
+                if (w.sp >= kDistDepth) {
+                    status |= kStatusStepLimit;
+                    f.child = f.nrefl;
+                } else {
+                    spawn_child(f, m, dp, 0, f.child, lut, S, status, F[w.sp]);
+                    ++f.child;
+                    ++w.sp;
+                }
+            } else {
+                if (m.rf > 0.0f && f.nrefl > 0) f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefl), m.rf));
+                f.child = 0;
+                f.sum = make_float3(0.f, 0.f, 0.f);
+                f.stage = kDistRefr;
+            }
+            continue;
+        }
+        if (f.stage == kDistRefr) {
+            const MaterialView &m = table.m[f.mat];
+            if (f.child < f.nrefr) {
+                if (w.sp >= kDistDepth) {
+                    status |= kStatusStepLimit;
+                    f.child = f.nrefr;
+                } else {
+                    spawn_child(f, m, dp, 1, f.child, lut, S, status, F[w.sp]);
+                    ++f.child;
+                    ++w.sp;
+                }
+            } else {
+                if (m.tran > 0.0f && f.nrefr > 0) f.c = xadd3(f.c, xmul3(xdiv3(f.sum, (float)f.nrefr), m.tran));
+                f.stage = kDistDone;
+            }
+            continue;
+        }
+        // done: the frame's colour goes to its parent's current set
+        const float3 col = f.c;
+        --w.sp;
+        if (w.sp == 0) w.out = col;
+        else F[w.sp - 1].sum = xadd3(F[w.sp - 1].sum, col);
+    }
+    if (w.sp > 0) {   // never expected: the guard bounds the moves between two rays
+        status |= kStatusStepLimit;
+        w.sp = 0;
+    }
+    return false;
+}
+
+// Takes the result of the ray walk_advance asked for.
+template <int MODE>
+__device__ __forceinline__ void walk_consume(Walk &w, const Trav &T, bool any, const SceneView &sc,
+                                             const CameraView &cam, const LightSet &lights, const MaterialTable &table,
+                                             const DistParams &dp, DistFrame *F, uint32_t &status)
+{
+    DistFrame &f = F[w.sp - 1];
+    if (any) {
+        if (!T.occluded) ++w.made;
+        ++w.sample;
+        return;
+    }
+    // the node's closest hit
+    if (w.sp > 1 || MODE == kDistSub) ++w.nsec;
+    f.nrefl = 0;
+    f.nrefr = 0;
+    if (!(T.hit.t < FLT_MAX)) {
+        f.c = cam.background;
+        f.stage = kDistDone;
+        if (MODE == kDistRoot) {
+            w.out = f.c;
+            w.sp = 0;
+        }
+        return;
+    }
+    const int32_t id = T.hit.id - sc.tri_base;
+    if (w.sp == 1 && MODE != kDistSub) w.hit = true;
+    int32_t mi = sc.mat ? __ldg(&sc.mat[id]) : 0;
+    if (mi < 0 || mi >= table.n) { status |= kStatusBadIndex; mi = 0; }
+    const MaterialView &m = table.m[mi];
+    RayState r;
+    r.o = f.o;
+    r.d = f.d;
+    const SurfacePoint spt = surface_at(sc, r, T.hit);
+    w.start = offset_start(spt.dst, spt.geo);
+    w.kd = material_kd(m, spt);
+    w.c = make_float3(0.f, 0.f, 0.f);
+    w.lvl = min(f.level, kDistLevels - 1);
+    // this node's first number: its own stream's first, or the pixel's next
+    // in the reference's stream
+    w.k0 = dp.pixel_stream ? 0u : w.k;
+    w.kb = w.k0;
+    w.light = 0;
+    w.sample = 0;
+    w.made = 0;
+    w.nl = (lights.n > 0 && lights.l[0].kind == RT_LIGHT_DIRECTIONAL) ? 1 : dist_count(dp.soft, f.level);
+    f.o = spt.dst;
+    f.sn = spt.sn;
+    f.geo = spt.geo;
+    f.mat = mi;
+    f.out_in = spt.out_in ? 1 : 0;
+    f.stage = kDistLights;
+}
+
+// The whole walk of one lane (its lanes' rays traced together while their
+// walks last).
+template <int MODE>
+__device__ __forceinline__ uint32_t dist_walk(const SceneView &sc, const CameraView &cam, const LightSet &lights,
+                                              const MaterialTable &table, const DistLights &dl, const DistParams &dp,
+                                              const int4 *__restrict__ area, const float *__restrict__ verts,
+                                              const float *__restrict__ lut, DistStream &S, int x, int y,
+                                              DistFrame *F, float3 &out, bool &hit, uint32_t &nsec,
+                                              uint32_t &status)
+{
+    Walk w;
+    walk_start<MODE>(w, cam, F, x, y);
+    uint2 stack[kStackSize];
+    for (;;) {
+        float3 ro, rd;
+        float rt;
+        bool any;
+        if (!walk_advance<MODE>(w, sc, lights, table, dl, dp, area, verts, lut, S, F, ro, rd, rt, any, status)) break;
+        Trav T;
+        trav_begin(T, sc, ro, rd, rt, any);
+        while (!trav_step<false>(T, stack, sc, any, status, nullptr)) {
+        }
+        walk_consume<MODE>(w, T, any, sc, cam, lights, table, dp, F, status);
+    }
+    out = w.out;
+    hit = w.hit;
+    nsec += w.nsec;
+    return w.drawn;
+}
+
 // One launch of the distributed walk: the counting pass (SHADE false:
 // counts[pix] = numbers the pixel draws) or the shading pass (numbers from
 // the pixels' own streams, or from rnd at prefix[pix]).  A warp walks the 32
-// pixels of an 8x4 tile, each lane one stage of its pixel's tree per loop
-// iteration.  RT_DIST_MIN_BLOCKS: resident blocks per SM the register
-// allocation must allow (4: 128 registers, no spills, measured fastest).
+// pixels of an 8x4 tile, its lanes' rays traced together.
+// RT_DIST_MIN_BLOCKS: resident blocks per SM the register allocation must
+// allow (5: 96 registers, measured fastest for the converged walk; 4 was
+// for the walk that traced at three call sites).
 #ifndef RT_DIST_MIN_BLOCKS
-#define RT_DIST_MIN_BLOCKS 4
+#define RT_DIST_MIN_BLOCKS 5
 #endif
 template <bool SHADE>
 __global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist(SceneView sc, CameraView cam, LightSet lights,
@@ -746,9 +997,13 @@ __global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist(Scen
             S.key1 = dp.key1;
             S.pixel_mode = dp.pixel_stream != 0;
             S.blk = 0xffffffffu;
+            S.bnode = 0;
             float3 c;
-            drawn = dist_pixel<SHADE>(sc, cam, lights, table, dl, dp, area, verts, lut, S, x, y, F, c, hit, nsec,
-                                      status);
+            if (SHADE)
+                drawn = dist_walk<kDistWhole>(sc, cam, lights, table, dl, dp, area, verts, lut, S, x, y, F, c, hit,
+                                              nsec, status);
+            else
+                drawn = dist_count_pixel(sc, cam, lights, table, dl, dp, lut, S, x, y, F, status);
             if (SHADE) {
                 if (rgb) store_rgb(rgb, pix, c);
                 if (fimg) {
@@ -767,6 +1022,189 @@ __global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist(Scen
             unsigned long long d = drawn;
             for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
             if ((threadIdx.x & 31) == 0 && d) atomicAdd(&ctr->drawn, d);
+        }
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// Frames of per-pixel streams with ray trees are traced in three launches:
+// the camera ray's node of every pixel (k_dist_root: its colour from the
+// lights and ka, its sets' rays handed out as separate items), every item's
+// subtree (k_dist_sub), then every pixel's colour from its node's and its
+// items' (k_dist_combine, in the walk's order of additions).  A node's
+// numbers are keyed by the node, so an item's subtree draws the same numbers
+// traced alone as in the pixel's walk, and neighbouring items -- the rays of
+// one set -- trace together.
+struct DistItem {
+    float4 o_magn;       // origin, power
+    float4 d_level;      // direction, componant level (int bits)
+    ulonglong2 node;     // tree node, pixel
+};
+
+__device__ __forceinline__ DistStream pixel_streams(const DistParams &dp, uint32_t pix)
+{
+    DistStream S;
+    S.win = nullptr;
+    S.nwin = 0;
+    S.base = 0;
+    S.pixel = pix;
+    S.key0 = dp.key0;
+    S.key1 = dp.key1;
+    S.pixel_mode = true;
+    S.blk = 0xffffffffu;
+    S.bnode = 0;
+    return S;
+}
+
+__global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist_root(
+    SceneView sc, CameraView cam, LightSet lights, MaterialTable table, DistLights dl, DistParams dp,
+    const int4 *__restrict__ area, const float *__restrict__ verts, const float *__restrict__ lut,
+    float4 *__restrict__ root_c, int4 *__restrict__ root_sets, DistItem *__restrict__ items, int32_t cap,
+    int32_t *__restrict__ nitems, Counters *ctr)
+{
+    DistFrame F[kDistDepth];   // the walk stops at F[0]
+    int tiles_x;
+    const int items_n = tiles_of<8>(cam.xres, cam.yres, tiles_x) * 32;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t status = 0;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= items_n) break;
+        int x, y;
+        tile_pixel<8>(base + (int)lane, tiles_x, x, y);
+        const bool live = (x < cam.xres) && (y < cam.yres);
+        uint32_t nsec = 0, drawn = 0;
+        bool hit = false;
+        float3 c = cam.background;
+        int cnt = 0;
+        const size_t pix = live ? (size_t)x + (size_t)y * (size_t)cam.xres : 0;
+        if (live) {
+            DistStream S = pixel_streams(dp, (uint32_t)pix);
+            drawn = dist_walk<kDistRoot>(sc, cam, lights, table, dl, dp, area, verts, lut, S, x, y, F, c, hit,
+                                                nsec, status);
+            if (F[0].stage == kDistRefl) cnt = F[0].nrefl + F[0].nrefr;
+        }
+        // the warp's items in lane order, one allocation per warp
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += v;
+        }
+        int wbase = 0;
+        if (lane == 31u && incl) wbase = atomicAdd(nitems, incl);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        const int first = wbase + incl - cnt;
+        if (live) {
+            const bool fits = first >= 0 && first + cnt <= cap;   // else the host grows the list and runs again
+            if (cnt > 0 && fits) {
+                DistStream S = pixel_streams(dp, (uint32_t)pix);
+                const MaterialView &m = table.m[F[0].mat];
+                for (int j = 0; j < cnt; ++j) {
+                    const int set = j < F[0].nrefl ? 0 : 1;
+                    DistFrame C;
+                    spawn_child(F[0], m, dp, set, set ? j - F[0].nrefl : j, lut, S, status, C);
+                    DistItem it;
+                    it.o_magn = make_float4(C.o.x, C.o.y, C.o.z, C.magn);
+                    it.d_level = make_float4(C.d.x, C.d.y, C.d.z, __int_as_float(C.level));
+                    it.node = make_ulonglong2(C.node, (unsigned long long)pix);
+                    items[first + j] = it;
+                }
+            }
+            root_c[pix] = make_float4(c.x, c.y, c.z, __int_as_float(cnt > 0 ? F[0].mat : 0));
+            root_sets[pix] = make_int4(first, cnt > 0 ? F[0].nrefl : 0, cnt > 0 ? F[0].nrefr : 0, 0);
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, hit);
+        warp_add(&ctr->secondary, nsec);
+        unsigned long long d = drawn;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0u && d) atomicAdd(&ctr->drawn, d);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// The items' subtrees, one per lane; a warp takes 32 consecutive items
+// (the rays of one or two sets) at a time.  (Lanes that take the next item
+// as soon as theirs is finished were measured slower: 61 against 41 ms on
+// the 512x512 glass frame with 16-ray diffuse sets, their rays no longer
+// neighbours.)
+// 6 resident blocks (80 registers): 34.1 ms against 41.3 at 4 and 37.1 at 5
+// on the 512x512 glass frame with 16-ray diffuse sets; 7 and 8 no faster
+#ifndef RT_DIST_SUB_MIN_BLOCKS
+#define RT_DIST_SUB_MIN_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(kTraceThreads, RT_DIST_SUB_MIN_BLOCKS) k_dist_sub(
+    SceneView sc, CameraView cam, LightSet lights, MaterialTable table, DistLights dl, DistParams dp,
+    const int4 *__restrict__ area, const float *__restrict__ verts, const float *__restrict__ lut,
+    const DistItem *__restrict__ items, int32_t n, float4 *__restrict__ item_c, Counters *ctr)
+{
+    DistFrame F[kDistDepth];
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t status = 0;
+    for (;;) {
+        const int base = warp_claim(&ctr->work, 32);
+        if (base >= n) break;
+        const int i = base + (int)lane;
+        uint32_t nsec = 0, drawn = 0;
+        if (i < n) {
+            const DistItem it = items[i];
+            F[0].o = make_float3(it.o_magn.x, it.o_magn.y, it.o_magn.z);
+            F[0].magn = it.o_magn.w;
+            F[0].d = make_float3(it.d_level.x, it.d_level.y, it.d_level.z);
+            F[0].level = __float_as_int(it.d_level.w);
+            F[0].node = it.node.x;
+            F[0].stage = kDistTrace;
+            DistStream S = pixel_streams(dp, (uint32_t)it.node.y);
+            float3 c;
+            bool hit;
+            drawn = dist_walk<kDistSub>(sc, cam, lights, table, dl, dp, area, verts, lut, S, 0, 0, F, c, hit, nsec,
+                                        status);
+            item_c[i] = make_float4(c.x, c.y, c.z, 0.f);
+        }
+        warp_add(&ctr->secondary, nsec);
+        unsigned long long d = drawn;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0u && d) atomicAdd(&ctr->drawn, d);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// A pixel's colour: its node's, then each set's mean added times rf, then
+// tran (the walk's additions, in its order).
+__global__ void k_dist_combine(CameraView cam, MaterialTable table, const float4 *__restrict__ root_c,
+                               const int4 *__restrict__ root_sets, const float4 *__restrict__ item_c, int32_t n,
+                               uint8_t *__restrict__ rgb, float *__restrict__ fimg, Counters *ctr)
+{
+    const int32_t npix = cam.xres * cam.yres;
+    uint32_t status = 0;
+    for (int32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const float4 r = root_c[p];
+        const int4 sets = root_sets[p];
+        float3 c = make_float3(r.x, r.y, r.z);
+        if (sets.y + sets.z > 0) {
+            if (sets.x < 0 || sets.x + sets.y + sets.z > n) {
+                status |= kStatusBadIndex;
+            } else {
+                const MaterialView &m = table.m[__float_as_int(r.w)];
+                float3 sum = make_float3(0.f, 0.f, 0.f);
+                for (int j = 0; j < sets.y; ++j) {
+                    const float4 q = item_c[sets.x + j];
+                    sum = xadd3(sum, make_float3(q.x, q.y, q.z));
+                }
+                if (m.rf > 0.0f && sets.y > 0) c = xadd3(c, xmul3(xdiv3(sum, (float)sets.y), m.rf));
+                sum = make_float3(0.f, 0.f, 0.f);
+                for (int j = 0; j < sets.z; ++j) {
+                    const float4 q = item_c[sets.x + sets.y + j];
+                    sum = xadd3(sum, make_float3(q.x, q.y, q.z));
+                }
+                if (m.tran > 0.0f && sets.z > 0) c = xadd3(c, xmul3(xdiv3(sum, (float)sets.z), m.tran));
+            }
+        }
+        if (rgb) store_rgb(rgb, (size_t)p, c);
+        if (fimg) {
+            fimg[3 * (size_t)p] = c.x;
+            fimg[3 * (size_t)p + 1] = c.y;
+            fimg[3 * (size_t)p + 2] = c.z;
         }
     }
     if (status) atomicOr(&ctr->status, status);
@@ -983,6 +1421,19 @@ extern "C" rt_status rt_render_soft_shadows(rt_scene *s, const rt_camera *camera
 }
 
 namespace {
+
+int sub_blocks_per_sm()
+{
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_dist_sub, kTraceThreads, 0) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 2;
+        }
+        return b;
+    }();
+    return per_sm;
+}
 
 int dist_blocks_per_sm()
 {
@@ -1291,7 +1742,8 @@ extern "C" rt_status rt_render_distributed(rt_scene *s, const rt_camera *camera,
     dp.pixel_stream = smp.stream == RT_STREAM_PIXEL ? 1 : 0;
     dp.key0 = (uint32_t)smp.seed;
     dp.key1 = (uint32_t)(smp.seed >> 32);
-    dp.max_steps = (int32_t)std::min(8.0 * tb.rays + 64.0, 1.0e9);
+    // walk steps per pixel: every ray of the tree and every light's rays at each of its hits
+    dp.max_steps = (int32_t)std::min(8.0 * tb.rays * (1.0 + (double)nlights * smp.soft_samples) + 64.0, 1.0e9);
     for (int i = 0; i < nmaterials; ++i) {
         mt.m[i] = make_material_view(materials[i]);
         dp.rfd[i] = materials[i].rfd;
@@ -1346,10 +1798,49 @@ extern "C" rt_status rt_render_distributed(rt_scene *s, const rt_camera *camera,
         RT_CUDA_S(ctx->fimg.reserve(npix * 3 * sizeof(float)), "float frame allocation");
         d_f = (float *)ctx->fimg.ptr;
     }
-    k_dist<true><<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
-                                                 (const float *)S.lut.ptr, rnd, total,
-                                                 (const int64_t *)S.prefix64.ptr, nullptr, d_rgb, d_f,
-                                                 ctx->d_counters);
+    // per-pixel streams with ray trees: the camera rays' nodes, then their
+    // sets' subtrees as separate items, then the pixels' colours
+    const int64_t per_pixel = 2 * (int64_t)std::max(smp.diffuse_samples, 1);   // items a pixel can hand out
+    const bool split = smp.stream == RT_STREAM_PIXEL && tree && (int64_t)npix * per_pixel < ((int64_t)1 << 31);
+    if (split) {
+        RT_CUDA_S(S.root_c.reserve(npix * sizeof(float4)), "node allocation");
+        RT_CUDA_S(S.root_sets.reserve(npix * sizeof(int4)), "node allocation");
+        RT_CUDA_S(S.nitems.reserve(sizeof(int32_t)), "item counter allocation");
+        int64_t cap = std::min((int64_t)npix * per_pixel, std::max(S.item_cap, (int64_t)npix * 4));
+        int32_t n = 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            RT_CUDA_S(S.items.reserve((size_t)cap * sizeof(DistItem)), "item allocation");
+            RT_CUDA_S(S.item_c.reserve((size_t)cap * sizeof(float4)), "item colour allocation");
+            RT_CUDA_S(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), st), "counter clear");
+            RT_CUDA_S(cudaMemsetAsync(S.nitems.ptr, 0, sizeof(int32_t), st), "item counter clear");
+            k_dist_root<<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
+                                                        (const float *)S.lut.ptr, (float4 *)S.root_c.ptr,
+                                                        (int4 *)S.root_sets.ptr, (DistItem *)S.items.ptr, (int32_t)cap,
+                                                        (int32_t *)S.nitems.ptr, ctx->d_counters);
+            RT_CUDA_S(cudaGetLastError(), "node launch");
+            RT_CUDA_S(cudaMemcpyAsync(&n, S.nitems.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st), "item count read");
+            RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
+            if (n >= 0 && n <= cap) break;
+            if (n < 0 || attempt == 1) return sfail(RT_ERR_INTERNAL, "rt_render_distributed: item count out of range");
+            cap = std::min((int64_t)npix * per_pixel, (int64_t)n + n / 8);   // grow to fit and run again
+        }
+        S.item_cap = cap;
+        RT_CUDA_S(cudaMemsetAsync(&ctx->d_counters->work, 0, sizeof(int), st), "work counter clear");
+        if (n > 0)
+            k_dist_sub<<<sub_blocks_per_sm() * ctx->sm_count, kTraceThreads, 0, st>>>(
+                sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
+                                                       (const float *)S.lut.ptr, (const DistItem *)S.items.ptr, n,
+                                                       (float4 *)S.item_c.ptr, ctx->d_counters);
+        RT_CUDA_S(cudaGetLastError(), "subtree launch");
+        k_dist_combine<<<ctx->sm_count * 8, 256, 0, st>>>(cv, mt, (const float4 *)S.root_c.ptr,
+                                                          (const int4 *)S.root_sets.ptr, (const float4 *)S.item_c.ptr,
+                                                          n, d_rgb, d_f, ctx->d_counters);
+    } else {
+        k_dist<true><<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
+                                                     (const float *)S.lut.ptr, rnd, total,
+                                                     (const int64_t *)S.prefix64.ptr, nullptr, d_rgb, d_f,
+                                                     ctx->d_counters);
+    }
     RT_CUDA_S(cudaGetLastError(), "shade launch");
     RT_CUDA_S(cudaEventRecord(ctx->ev1, st), "event record");
     if (rgb_host) RT_CUDA_S(cudaMemcpyAsync(rgb_out, d_rgb, npix * 3, cudaMemcpyDeviceToHost, st), "rgb copy");

@@ -415,8 +415,9 @@ def test_oracle_distributed_match_reference(oracle, dist_golden):
 
 def test_oracle_distributed_pixel_streams(oracle, dist_golden):
     """Per-pixel streams: the same frame rendered serially and on 8 threads
-    is identical (each pixel draws only from its own stream), differs from
-    another seed, and a pixel's numbers are ro_pixel_stream's."""
+    is identical (each pixel draws only from its own streams), differs from
+    another seed; a node's numbers are ro_pixel_stream's and its children's
+    nodes SplitMix64 of its own."""
     k, scene, frame, diffuse, _, _ = list(dist_cases(dist_golden))[-1]
     osc = oracle.OracleScene(scene)
     a = osc.render_distributed(frame, soft=16, diffuse=diffuse, stream=oracle.STREAM_PIXEL, seed=7, threads=1,
@@ -426,9 +427,20 @@ def test_oracle_distributed_pixel_streams(oracle, dist_golden):
     c = osc.render_distributed(frame, soft=16, diffuse=diffuse, stream=oracle.STREAM_PIXEL, seed=8, threads=8)
     assert np.array_equal(a["fimg"].view(np.uint32), b["fimg"].view(np.uint32)) and a["drawn"] == b["drawn"]
     assert not np.array_equal(a["rgb"], c["rgb"])
-    # Philox4x32-10 word k % 4 of counter (pixel, k / 4, 0, 'STRE'), scaled by 2^-32
-    w = oracle.philox(np.array([123, 2, 0, 0x53545245], np.uint32), 7, 0)
-    assert oracle.pixel_stream(7, 123, 9) == np.float32(np.float32(w[1]) * np.float32(2.0 ** -32))
+    # Philox4x32-10 word k % 4 of counter (pixel, node low, node high, k / 4), scaled by 2^-32
+    node = oracle.tree_child(oracle.TREE_ROOT, 1, 5)
+    w = oracle.philox(np.array([123, node & 0xffffffff, node >> 32, 2], np.uint32), 7, 0)
+    assert oracle.pixel_stream(7, 123, node, 9) == np.float32(np.float32(w[1]) * np.float32(2.0 ** -32))
+
+    def splitmix64(z):
+        m = (1 << 64) - 1
+        z = (z + 0x9E3779B97F4A7C15) & m
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        return z ^ (z >> 31)
+
+    assert node == splitmix64((oracle.TREE_ROOT + (64 + 5 + 1) * 0x9E3779B97F4A7C15) & ((1 << 64) - 1))
+    assert len({oracle.tree_child(oracle.TREE_ROOT, st, i) for st in (0, 1) for i in range(64)}) == 128
 
 
 def bilateral_cases():
