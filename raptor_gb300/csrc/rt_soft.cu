@@ -1084,34 +1084,41 @@ __global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist_root
                                                 nsec, status);
             if (F[0].stage == kDistRefl) cnt = F[0].nrefl + F[0].nrefr;
         }
-        // the warp's items in lane order, one allocation per warp
-        int incl = cnt;
+        // the warp's items in lane order, reflection and refraction sets in
+        // lists of their own (a warp of subtrees then holds one kind), one
+        // allocation per list per warp
+        const int nr = cnt > 0 ? F[0].nrefl : 0, nt = cnt > 0 ? F[0].nrefr : 0;
+        int ir = nr, it_ = nt;
         for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((int)lane >= o) incl += v;
+            const int vr = __shfl_up_sync(0xffffffffu, ir, o), vt = __shfl_up_sync(0xffffffffu, it_, o);
+            if ((int)lane >= o) { ir += vr; it_ += vt; }
         }
-        int wbase = 0;
-        if (lane == 31u && incl) wbase = atomicAdd(nitems, incl);
-        wbase = __shfl_sync(0xffffffffu, wbase, 31);
-        const int first = wbase + incl - cnt;
+        int rbase = 0, tbase = 0;
+        if (lane == 31u) {
+            if (ir) rbase = atomicAdd(&nitems[0], ir);
+            if (it_) tbase = atomicAdd(&nitems[1], it_);
+        }
+        rbase = __shfl_sync(0xffffffffu, rbase, 31) + ir - nr;
+        tbase = __shfl_sync(0xffffffffu, tbase, 31) + it_ - nt;
         if (live) {
-            const bool fits = first >= 0 && first + cnt <= cap;   // else the host grows the list and runs again
+            // else the host grows the lists and runs again
+            const bool fits = rbase >= 0 && rbase + nr <= cap && tbase >= 0 && tbase + nt <= cap;
             if (cnt > 0 && fits) {
                 DistStream S = pixel_streams(dp, (uint32_t)pix);
                 const MaterialView &m = table.m[F[0].mat];
                 for (int j = 0; j < cnt; ++j) {
-                    const int set = j < F[0].nrefl ? 0 : 1;
+                    const int set = j < nr ? 0 : 1;
                     DistFrame C;
-                    spawn_child(F[0], m, dp, set, set ? j - F[0].nrefl : j, lut, S, status, C);
+                    spawn_child(F[0], m, dp, set, set ? j - nr : j, lut, S, status, C);
                     DistItem it;
                     it.o_magn = make_float4(C.o.x, C.o.y, C.o.z, C.magn);
                     it.d_level = make_float4(C.d.x, C.d.y, C.d.z, __int_as_float(C.level));
                     it.node = make_ulonglong2(C.node, (unsigned long long)pix);
-                    items[first + j] = it;
+                    items[set ? (size_t)cap + tbase + (j - nr) : (size_t)rbase + j] = it;
                 }
             }
             root_c[pix] = make_float4(c.x, c.y, c.z, __int_as_float(cnt > 0 ? F[0].mat : 0));
-            root_sets[pix] = make_int4(first, cnt > 0 ? F[0].nrefl : 0, cnt > 0 ? F[0].nrefr : 0, 0);
+            root_sets[pix] = make_int4(rbase, nr, tbase, nt);
         }
         warp_count(&ctr->primary, live);
         warp_count(&ctr->hits, hit);
@@ -1136,17 +1143,23 @@ __global__ void __launch_bounds__(kTraceThreads, RT_DIST_MIN_BLOCKS) k_dist_root
 __global__ void __launch_bounds__(kTraceThreads, RT_DIST_SUB_MIN_BLOCKS) k_dist_sub(
     SceneView sc, CameraView cam, LightSet lights, MaterialTable table, DistLights dl, DistParams dp,
     const int4 *__restrict__ area, const float *__restrict__ verts, const float *__restrict__ lut,
-    const DistItem *__restrict__ items, int32_t n, float4 *__restrict__ item_c, Counters *ctr)
+    const DistItem *__restrict__ items, int32_t nr, int32_t nt, int32_t cap, float4 *__restrict__ item_c,
+    Counters *ctr)
 {
     DistFrame F[kDistDepth];
     const uint32_t lane = threadIdx.x & 31u;
+    // the reflection list's items, then (from a warp boundary on) the
+    // refraction list's
+    const int rw = (nr + 31) & ~31;
+    const int n = rw + nt;
     uint32_t status = 0;
     for (;;) {
         const int base = warp_claim(&ctr->work, 32);
         if (base >= n) break;
-        const int i = base + (int)lane;
+        const int v = base + (int)lane;
+        const int i = v < rw ? (v < nr ? v : -1) : (v - rw < nt ? cap + (v - rw) : -1);
         uint32_t nsec = 0, drawn = 0;
-        if (i < n) {
+        if (i >= 0) {
             const DistItem it = items[i];
             F[0].o = make_float3(it.o_magn.x, it.o_magn.y, it.o_magn.z);
             F[0].magn = it.o_magn.w;
@@ -1172,17 +1185,18 @@ __global__ void __launch_bounds__(kTraceThreads, RT_DIST_SUB_MIN_BLOCKS) k_dist_
 // A pixel's colour: its node's, then each set's mean added times rf, then
 // tran (the walk's additions, in its order).
 __global__ void k_dist_combine(CameraView cam, MaterialTable table, const float4 *__restrict__ root_c,
-                               const int4 *__restrict__ root_sets, const float4 *__restrict__ item_c, int32_t n,
-                               uint8_t *__restrict__ rgb, float *__restrict__ fimg, Counters *ctr)
+                               const int4 *__restrict__ root_sets, const float4 *__restrict__ item_c, int32_t nr,
+                               int32_t nt, int32_t cap, uint8_t *__restrict__ rgb, float *__restrict__ fimg,
+                               Counters *ctr)
 {
     const int32_t npix = cam.xres * cam.yres;
     uint32_t status = 0;
     for (int32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const float4 r = root_c[p];
-        const int4 sets = root_sets[p];
+        const int4 sets = root_sets[p];   // reflection list's first, count; refraction list's first, count
         float3 c = make_float3(r.x, r.y, r.z);
-        if (sets.y + sets.z > 0) {
-            if (sets.x < 0 || sets.x + sets.y + sets.z > n) {
+        if (sets.y + sets.w > 0) {
+            if (sets.x < 0 || sets.x + sets.y > nr || sets.z < 0 || sets.z + sets.w > nt) {
                 status |= kStatusBadIndex;
             } else {
                 const MaterialView &m = table.m[__float_as_int(r.w)];
@@ -1193,11 +1207,11 @@ __global__ void k_dist_combine(CameraView cam, MaterialTable table, const float4
                 }
                 if (m.rf > 0.0f && sets.y > 0) c = xadd3(c, xmul3(xdiv3(sum, (float)sets.y), m.rf));
                 sum = make_float3(0.f, 0.f, 0.f);
-                for (int j = 0; j < sets.z; ++j) {
-                    const float4 q = item_c[sets.x + sets.y + j];
+                for (int j = 0; j < sets.w; ++j) {
+                    const float4 q = item_c[(size_t)cap + sets.z + j];
                     sum = xadd3(sum, make_float3(q.x, q.y, q.z));
                 }
-                if (m.tran > 0.0f && sets.z > 0) c = xadd3(c, xmul3(xdiv3(sum, (float)sets.z), m.tran));
+                if (m.tran > 0.0f && sets.w > 0) c = xadd3(c, xmul3(xdiv3(sum, (float)sets.w), m.tran));
             }
         }
         if (rgb) store_rgb(rgb, (size_t)p, c);
@@ -1805,36 +1819,39 @@ extern "C" rt_status rt_render_distributed(rt_scene *s, const rt_camera *camera,
     if (split) {
         RT_CUDA_S(S.root_c.reserve(npix * sizeof(float4)), "node allocation");
         RT_CUDA_S(S.root_sets.reserve(npix * sizeof(int4)), "node allocation");
-        RT_CUDA_S(S.nitems.reserve(sizeof(int32_t)), "item counter allocation");
-        int64_t cap = std::min((int64_t)npix * per_pixel, std::max(S.item_cap, (int64_t)npix * 4));
-        int32_t n = 0;
+        RT_CUDA_S(S.nitems.reserve(2 * sizeof(int32_t)), "item counter allocation");
+        // items per list (reflection sets, refraction sets)
+        int64_t cap = std::min((int64_t)npix * per_pixel / 2, std::max(S.item_cap, (int64_t)npix * 2));
+        int32_t n[2] = {0, 0};
         for (int attempt = 0; attempt < 2; ++attempt) {
-            RT_CUDA_S(S.items.reserve((size_t)cap * sizeof(DistItem)), "item allocation");
-            RT_CUDA_S(S.item_c.reserve((size_t)cap * sizeof(float4)), "item colour allocation");
+            RT_CUDA_S(S.items.reserve(2 * (size_t)cap * sizeof(DistItem)), "item allocation");
+            RT_CUDA_S(S.item_c.reserve(2 * (size_t)cap * sizeof(float4)), "item colour allocation");
             RT_CUDA_S(cudaMemsetAsync(ctx->d_counters, 0, sizeof(Counters), st), "counter clear");
-            RT_CUDA_S(cudaMemsetAsync(S.nitems.ptr, 0, sizeof(int32_t), st), "item counter clear");
+            RT_CUDA_S(cudaMemsetAsync(S.nitems.ptr, 0, 2 * sizeof(int32_t), st), "item counter clear");
             k_dist_root<<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
                                                         (const float *)S.lut.ptr, (float4 *)S.root_c.ptr,
                                                         (int4 *)S.root_sets.ptr, (DistItem *)S.items.ptr, (int32_t)cap,
                                                         (int32_t *)S.nitems.ptr, ctx->d_counters);
             RT_CUDA_S(cudaGetLastError(), "node launch");
-            RT_CUDA_S(cudaMemcpyAsync(&n, S.nitems.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st), "item count read");
+            RT_CUDA_S(cudaMemcpyAsync(n, S.nitems.ptr, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
+                      "item count read");
             RT_CUDA_S(cudaStreamSynchronize(st), "synchronize");
-            if (n >= 0 && n <= cap) break;
-            if (n < 0 || attempt == 1) return sfail(RT_ERR_INTERNAL, "rt_render_distributed: item count out of range");
-            cap = std::min((int64_t)npix * per_pixel, (int64_t)n + n / 8);   // grow to fit and run again
+            if (n[0] >= 0 && n[1] >= 0 && n[0] <= cap && n[1] <= cap) break;
+            if (n[0] < 0 || n[1] < 0 || attempt == 1)
+                return sfail(RT_ERR_INTERNAL, "rt_render_distributed: item count out of range");
+            const int64_t need = std::max(n[0], n[1]);
+            cap = std::min((int64_t)npix * per_pixel / 2, need + need / 8);   // grow to fit and run again
         }
         S.item_cap = cap;
         RT_CUDA_S(cudaMemsetAsync(&ctx->d_counters->work, 0, sizeof(int), st), "work counter clear");
-        if (n > 0)
+        if (n[0] + n[1] > 0)
             k_dist_sub<<<sub_blocks_per_sm() * ctx->sm_count, kTraceThreads, 0, st>>>(
-                sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
-                                                       (const float *)S.lut.ptr, (const DistItem *)S.items.ptr, n,
-                                                       (float4 *)S.item_c.ptr, ctx->d_counters);
+                sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts, (const float *)S.lut.ptr,
+                (const DistItem *)S.items.ptr, n[0], n[1], (int32_t)cap, (float4 *)S.item_c.ptr, ctx->d_counters);
         RT_CUDA_S(cudaGetLastError(), "subtree launch");
         k_dist_combine<<<ctx->sm_count * 8, 256, 0, st>>>(cv, mt, (const float4 *)S.root_c.ptr,
                                                           (const int4 *)S.root_sets.ptr, (const float4 *)S.item_c.ptr,
-                                                          n, d_rgb, d_f, ctx->d_counters);
+                                                          n[0], n[1], (int32_t)cap, d_rgb, d_f, ctx->d_counters);
     } else {
         k_dist<true><<<grid, kTraceThreads, 0, st>>>(sv, cv, ls, mt, dl, dp, (const int4 *)S.area.ptr, s->d_verts,
                                                      (const float *)S.lut.ptr, rnd, total,
