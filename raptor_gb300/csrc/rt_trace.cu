@@ -303,11 +303,12 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
                                                              uint8_t *__restrict__ rgb, int32_t *__restrict__ redo,
                                                              Counters *ctr)
 {
-    int tiles_x;
-    const int items = tiles_of<8>(out_x, out_y, tiles_x) * 32;
-    const float nsamples = (float)(aa_x * aa_y);
+    const int S = aa_x * aa_y;
+    const float nsamples = (float)S;
     uint32_t status = 0;
     FetchCount fc;
+    int tiles_x;
+    const int items = tiles_of<8>(out_x, out_y, tiles_x) * 32;
     for (;;) {
         const int base = warp_claim(&ctr->work, 32);
         if (base >= items) break;
@@ -338,6 +339,74 @@ __global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_
         warp_add(&ctr->primary, primary);
         warp_add(&ctr->hits, hits);
         warp_add(&ctr->secondary, secondary);
+    }
+    if (COUNT) {
+        atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
+        atomicAdd(&ctr->tris, (unsigned long long)fc.tris);
+    }
+    if (status) atomicOr(&ctr->status, status);
+}
+
+// k_render_aa with one sample per lane (aa_x * aa_y <= 32): a warp covers
+// a tile of output pixels, lane g * S + s taking sample s (x outer, y
+// inner) of pixel g; the pixel's first lane sums the samples in that order
+// (shuffled from their lanes), so the frame is the per-pixel loop's bit for
+// bit, while the warp's lanes trace one sample each instead of looping
+// over a pixel's samples.
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads, RT_RENDER_MIN_BLOCKS) k_render_aa_lanes(SceneView sc, CameraView cam,
+                                                             LightSet lights, MaterialView mat, int32_t aa_x,
+                                                             int32_t aa_y, int32_t out_x, int32_t out_y,
+                                                             uint8_t *__restrict__ rgb, int32_t *__restrict__ redo,
+                                                             Counters *ctr)
+{
+    const int S = aa_x * aa_y;
+    const float nsamples = (float)S;
+    uint32_t status = 0;
+    FetchCount fc;
+    // one sample per lane: a warp covers a tile of tw x th output
+    // pixels, lane g * S + s taking sample s (x outer, y inner) of
+    // pixel g; the pixel's first lane sums the samples in that order
+    const int per = 32 / S;
+    const int tw = per >= 8 ? 4 : per, th = per >= 8 ? per / 4 : 1;
+    const int lane = threadIdx.x & 31;
+    const int g = lane / S, smp = lane % S;
+    const int ax = smp / aa_y, ay = smp % aa_y;
+    const int tiles_x = (out_x + tw - 1) / tw;
+    const int ntiles = tiles_x * ((out_y + th - 1) / th);
+    for (;;) {
+        const int tile = warp_claim(&ctr->work, 32) >> 5;
+        if (tile >= ntiles) break;
+        const int x = (tile % tiles_x) * tw + g % tw, y = (tile / tiles_x) * th + g / tw;
+        const bool live = g < tw * th && x < out_x && y < out_y;
+        PixelOut po;
+        po.c = make_float3(0.f, 0.f, 0.f);
+        po.hit = false;
+        po.secondary = 0;
+        if (live)
+            po = shade_pixel_lights<COUNT>(sc, cam, lights.l, lights.n, mat, x * aa_x + ax, y * aa_y + ay, status,
+                                           &fc, lights.fast_pow != 0);
+        const int first = g * S;
+        float3 sum = make_float3(0.f, 0.f, 0.f);
+        for (int k = 0; k < S; ++k) {
+            const int src = min(first + k, 31);
+            const float3 q = make_float3(__shfl_sync(0xffffffffu, po.c.x, src), __shfl_sync(0xffffffffu, po.c.y, src),
+                                         __shfl_sync(0xffffffffu, po.c.z, src));
+            sum = xadd3(sum, q);
+        }
+        if (live && smp == 0) {
+            const float3 avg = make_float3(xdiv(sum.x, nsamples), xdiv(sum.y, nsamples), xdiv(sum.z, nsamples));
+            const int32_t pix = x + y * out_x;
+            if (lights.fast_pow && near_truncation(avg)) {
+                const int slot = atomicAdd(&ctr->redo, 1);
+                if (slot < out_x * out_y) redo[slot] = pix;
+            } else {
+                store_rgb(rgb, (size_t)pix, avg);
+            }
+        }
+        warp_count(&ctr->primary, live);
+        warp_count(&ctr->hits, po.hit);
+        warp_add(&ctr->secondary, po.secondary);
     }
     if (COUNT) {
         atomicAdd(&ctr->nodes, (unsigned long long)fc.nodes);
@@ -538,7 +607,14 @@ void launch_render_aa(const SceneView &sc, const CameraView &cam, const LightSet
 {
     static const int per_sm = blocks_per_sm(k_render_aa<false>);
     const int grid = per_sm * sm_count;
-    if (count)
+    if (aa_x * aa_y <= 32) {
+        if (count)
+            k_render_aa_lanes<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y,
+                                                                     rgb, redo, ctr);
+        else
+            k_render_aa_lanes<false><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y,
+                                                                      rgb, redo, ctr);
+    } else if (count)
         k_render_aa<true><<<grid, kTraceThreads, 0, st>>>(sc, cam, lights, mat, aa_x, aa_y, out_x, out_y, rgb, redo,
                                                            ctr);
     else
