@@ -122,10 +122,20 @@ void generate_slice(RefRandom &rng, int64_t offset, int64_t total, float *out)
             for (int64_t i = begins[(size_t)t]; i < end; ++i) out[i] = g.next();
         }
     };
+    // chunk t goes to thread t % started; a thread that cannot be started
+    // leaves its chunks to the ones that did
     std::vector<std::thread> pool;
-    for (int k = 1; k < nthreads; ++k) pool.emplace_back(work, k);
+    int started = 1;
+    try {
+        for (int k = 1; k < nthreads; ++k) {
+            pool.emplace_back(work, k);
+            ++started;
+        }
+    } catch (...) {
+    }
     work(0);
     for (std::thread &th : pool) th.join();
+    for (int k = started; k < nthreads; ++k) work(k);
 }
 
 // The rays light::find_rays makes for a triangle-defined light of ntris
@@ -1596,7 +1606,13 @@ rt_status stream_window(SoftState &S, int64_t offset, int64_t total, cudaStream_
             RT_CUDA_S(cudaMallocHost(&S.staging, (size_t)want * sizeof(float)), "pinned stream staging");
             S.staging_cap = (size_t)want;
         }
-        generate_slice(S.rng, offset, total, S.staging);
+        S.stage_base = -1;
+        S.stage_len = 0;
+        try {
+            generate_slice(S.rng, offset, total, S.staging);
+        } catch (...) {
+            return sfail(RT_ERR_OUT_OF_MEMORY, "random stream: host memory for the slice's generator states");
+        }
         S.stage_base = offset;
         S.stage_len = total;
     }
@@ -1615,20 +1631,29 @@ rt_status stream_window(SoftState &S, int64_t offset, int64_t total, cudaStream_
     if ((size_t)want <= S.staging_cap) {
         const int64_t next = offset + total;
         SoftState *P = &S;
-        S.ahead = std::thread([P, next, want] {
-            cudaSetDevice(P->device);
-            if (cudaEventSynchronize(P->copied) != cudaSuccess) {
-                P->stage_base = -1;   // nothing kept: the next window generates its own
-                P->stage_len = 0;
-                return;
-            }
-            const int64_t keep = P->stage_base + P->stage_len - next;
-            if (keep > 0) std::memmove(P->staging, P->staging + (next - P->stage_base), (size_t)keep * sizeof(float));
-            if (want > keep) generate_slice(P->rng, next + std::max<int64_t>(keep, 0), want - std::max<int64_t>(keep, 0),
-                                            P->staging + std::max<int64_t>(keep, 0));
-            P->stage_base = next;
-            P->stage_len = std::max(keep, want);
-        });
+        try {
+            S.ahead = std::thread([P, next, want] {
+                cudaSetDevice(P->device);
+                if (cudaEventSynchronize(P->copied) != cudaSuccess) {
+                    P->stage_base = -1;   // nothing kept: the next window generates its own
+                    P->stage_len = 0;
+                    return;
+                }
+                const int64_t keep = P->stage_base + P->stage_len - next;
+                if (keep > 0)
+                    std::memmove(P->staging, P->staging + (next - P->stage_base), (size_t)keep * sizeof(float));
+                const int64_t kept = std::max<int64_t>(keep, 0);
+                try {
+                    if (want > kept) generate_slice(P->rng, next + kept, want - kept, P->staging + kept);
+                    P->stage_base = next;
+                    P->stage_len = std::max(kept, want);
+                } catch (...) {   // out of host memory: keep what is there
+                    P->stage_base = kept > 0 ? next : -1;
+                    P->stage_len = kept;
+                }
+            });
+        } catch (...) {   // no thread: the next window generates its own numbers
+        }
     }
     return RT_OK;
 }
