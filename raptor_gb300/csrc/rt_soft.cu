@@ -122,8 +122,8 @@ void generate_slice(RefRandom &rng, int64_t offset, int64_t total, float *out)
             for (int64_t i = begins[(size_t)t]; i < end; ++i) out[i] = g.next();
         }
     };
-    // chunk t goes to thread t % started; a thread that cannot be started
-    // leaves its chunks to the ones that did
+    // worker k tempers chunks k, k + nthreads, ...; the workers whose thread
+    // could not be started run here, one after another, once the rest are done
     std::vector<std::thread> pool;
     int started = 1;
     try {
