@@ -854,7 +854,11 @@ __global__ void __launch_bounds__(kPlocBlock) k_ploc_tail(float4 *__restrict__ c
 // read after a fence that follows it (through L2).  Single-scene builds;
 // nodes, counts and surface-area tables as the PLOC kernels write them
 // (an internal node's box also carries its triangle count in .w).
-constexpr int kHplocKeep = 16;
+#ifndef RT_HPLOC_KEEP
+#define RT_HPLOC_KEEP 16
+#endif
+constexpr int kHplocKeep = RT_HPLOC_KEEP;
+static_assert(2 * kHplocKeep <= 32, "the two children's clusters must fit one warp");
 // One warp per block, 64 registers: a block's resources free as soon as its
 // warp's lanes have all stopped climbing (measured: 4 % faster than 64- and
 // 128-thread blocks, 30 % faster than 256 threads at 75 registers).
